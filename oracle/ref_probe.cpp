@@ -1,0 +1,319 @@
+// Probe program linked against the reference GOMC objects (built by
+// oracle/ref.mk).  It loads a generated fixture through the reference's own
+// Simulation constructor and dumps, at full FP64 precision, the numbers that
+// pin the oracle and the GPU path:
+//   - per-term initial energies (CalculateEnergy::SystemTotal,
+//     src/CalculateEnergy.cpp:83-138) and the k-vector tables / structure
+//     factors (Ewald::RecipInitOrth + BoxReciprocalSetup, src/Ewald.cpp:193-274,
+//     847-903),
+//   - cell-list membership (CellList::GetCellListNeighbor,
+//     src/CellList.cpp:258-285),
+//   - MoleculeInter / MolReciprocal / SwapDestRecip / SwapSourceRecip deltas for
+//     a list of proposals read from a file (src/CalculateEnergy.cpp:581-686,
+//     src/Ewald.cpp:409-531,657-710),
+//   - BoxForce / BoxForceReciprocal / CalculateTorque outputs when the
+//     fixture enables the MultiParticle move,
+//   - a per-step trace of the reference Monte Carlo loop
+//     (src/Simulation.cpp:94-96 without output, src/System.cpp:262-302).
+// It is test infrastructure: it runs only in the build container.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include <cmath>
+#include <sstream>
+#include <memory>
+#include <functional>
+#include <iomanip>
+#include <set>
+#include <list>
+#include <unordered_map>
+#include <array>
+#include <limits>
+#include <cassert>
+#include <random>
+
+// Access the reference's non-public state from this probe only.
+#define private public
+#define protected public
+#include "Simulation.h"
+#include "System.h"
+#include "StaticVals.h"
+#include "CalculateEnergy.h"
+#include "Ewald.h"
+#include "CellList.h"
+#include "MoveBase.h"
+#include "Translate.h"
+#include "Rotation.h"
+#include "MultiParticle.h"
+#include "TrialMol.h"
+#undef private
+#undef protected
+
+static FILE *open_out(const std::string &dir, const char *name) {
+  std::string p = dir + "/" + name;
+  FILE *f = fopen(p.c_str(), "w");
+  if (!f) {
+    fprintf(stderr, "cannot write %s\n", p.c_str());
+    exit(2);
+  }
+  return f;
+}
+
+static void dump_energy(FILE *f, const char *tag, const Energy &e) {
+  fprintf(f, "%s inter %.17g\n", tag, e.inter);
+  fprintf(f, "%s real %.17g\n", tag, e.real);
+  fprintf(f, "%s recip %.17g\n", tag, e.recip);
+  fprintf(f, "%s self %.17g\n", tag, e.self);
+  fprintf(f, "%s correction %.17g\n", tag, e.correction);
+  fprintf(f, "%s tailCorrection %.17g\n", tag, e.tailCorrection);
+  fprintf(f, "%s intraBond %.17g\n", tag, e.intraBond);
+  fprintf(f, "%s intraNonbond %.17g\n", tag, e.intraNonbond);
+  fprintf(f, "%s total %.17g\n", tag, e.total);
+}
+
+static void dump_coords(const std::string &dir, const char *name,
+                        const XYZArray &c) {
+  FILE *f = open_out(dir, name);
+  for (uint i = 0; i < c.Count(); ++i)
+    fprintf(f, "%.17g %.17g %.17g\n", c.x[i], c.y[i], c.z[i]);
+  fclose(f);
+}
+
+// Known-answer vectors of the reference's random streams: MTRand(seed)
+// (src/MersenneTwister.h) and Random123Wrapper's Philox4x64-10
+// (src/Random123Wrapper.cpp:16-84).
+static int dump_kat(const std::string &dir) {
+  FILE *f = open_out(dir, "kat_mt.txt");
+  const unsigned seeds[3] = {1234u, 4321u, 4294967295u};
+  for (unsigned s : seeds) {
+    MTRand g(s);
+    for (int i = 0; i < 1500; ++i) fprintf(f, "%u %u\n", s, g.randInt());
+  }
+  fclose(f);
+  f = open_out(dir, "kat_philox.txt");
+  const unsigned long steps[3] = {0ul, 1ul, 123456ul};
+  const unsigned long pseeds[3] = {0ul, 4321ul, 4294967295ul};
+  const unsigned ctrs[4] = {0u, 1u, 255u, 8000u};
+  for (unsigned long st : steps)
+    for (unsigned long sd : pseeds)
+      for (unsigned c : ctrs) {
+        Random123Wrapper w;
+        w.SetStep(st);
+        w.SetRandomSeed(sd);
+        RNG::ctr_type r = w.getRNG(c);
+        XYZ rc = w.GetRandomCoords(c);
+        XYZ sc = w.GetSymRandomCoords(c, 1.0);
+        fprintf(f, "%lu %lu %u %llu %llu %llu %llu %.17g %.17g %.17g %.17g %.17g %.17g\n",
+                st, sd, c, (unsigned long long)r[0], (unsigned long long)r[1],
+                (unsigned long long)r[2], (unsigned long long)r[3], rc.x, rc.y,
+                rc.z, sc.x, sc.y, sc.z);
+      }
+  fclose(f);
+  return 0;
+}
+
+int main(int argc, char **argv) {
+  if (argc == 3 && std::string(argv[1]) == "--kat")
+    return dump_kat(argv[2]);
+  if (argc < 4) {
+    fprintf(stderr,
+            "usage: ref_probe in.conf outdir nsteps [proposals.txt]\n");
+    return 1;
+  }
+  std::string outdir = argv[2];
+  long nsteps = atol(argv[3]);
+  const char *propFile = argc > 4 ? argv[4] : nullptr;
+
+  Simulation sim(argv[1]);
+  System &sys = *sim.system;
+  StaticVals &stat = *sim.staticValues;
+  Ewald *ew = sys.calcEwald;
+  const uint box = 0;
+
+  // ---- initial state -------------------------------------------------------
+  {
+    FILE *f = open_out(outdir, "energies_init.txt");
+    sys.potential.Total();
+    dump_energy(f, "box0", sys.potential.boxEnergy[0]);
+#if ENSEMBLE == GEMC || ENSEMBLE == GCMC
+    dump_energy(f, "box1", sys.potential.boxEnergy[1]);
+#endif
+    fprintf(f, "alpha %.17g\n", stat.forcefield.alpha[0]);
+    fprintf(f, "recip_rcut %.17g\n", stat.forcefield.recip_rcut[0]);
+    fprintf(f, "beta %.17g\n", stat.forcefield.beta);
+    if (stat.forcefield.ewald) {
+      fprintf(f, "imageSize %u\n", ew->imageSizeRef[0]);
+      fprintf(f, "kmax %u\n", ew->kmax[0]);
+      fprintf(f, "imageTotal %u\n", ew->imageTotal);
+    }
+    fprintf(f, "edgeCells %d %d %d\n", sys.cellList.edgeCells[0][0],
+            sys.cellList.edgeCells[0][1], sys.cellList.edgeCells[0][2]);
+    fclose(f);
+  }
+  dump_coords(outdir, "coords_init.txt", sys.coordinates);
+  dump_coords(outdir, "com_init.txt", sys.com);
+
+  if (stat.forcefield.ewald) {
+    FILE *f = open_out(outdir, "kvec.txt");
+    for (uint i = 0; i < ew->imageSizeRef[box]; ++i)
+      fprintf(f, "%.17g %.17g %.17g %.17g %.17g %.17g %.17g\n", ew->kxRef[box][i],
+              ew->kyRef[box][i], ew->kzRef[box][i], ew->prefactRef[box][i],
+              ew->sumRref[box][i], ew->sumIref[box][i], ew->hsqrRef[box][i]);
+    fclose(f);
+  }
+
+  for (uint b = 0; b < BOX_TOTAL; ++b) {
+    std::vector<int> cellVector, cellStart, mapP;
+    sys.cellList.GetCellListNeighbor(b, sys.coordinates.Count(), cellVector,
+                                     cellStart, mapP);
+    char name[64];
+    snprintf(name, sizeof name, "cells_box%u.txt", b);
+    FILE *f = open_out(outdir, name);
+    fprintf(f, "%d %d %d\n", sys.cellList.edgeCells[b][0],
+            sys.cellList.edgeCells[b][1], sys.cellList.edgeCells[b][2]);
+    // membership of every particle that sits in box b
+    for (int c = 0; c + 1 < (int)cellStart.size(); ++c)
+      for (int i = cellStart[c]; i < cellStart[c + 1]; ++i)
+        fprintf(f, "%d %d\n", cellVector[i], c);
+    fclose(f);
+  }
+
+  // ---- forces (only when the MultiParticle move is enabled) ---------------
+  if (stat.multiParticleEnabled) {
+    uint nAtoms = sys.coordinates.Count();
+    uint nMol = sys.com.Count();
+    XYZArray aF(nAtoms), mF(nMol), aR(nAtoms), mR(nMol), tq(nMol);
+    SystemPotential p = sys.potential;
+    p = sys.calcEnergy.BoxForce(p, sys.coordinates, aF, mF, sys.boxDimRef, box);
+    ew->CopyRecip(box);
+    ew->BoxForceReciprocal(sys.coordinates, aR, mR, box);
+    std::vector<uint> molIdx(nMol);
+    for (uint m = 0; m < nMol; ++m) molIdx[m] = m;
+    sys.calcEnergy.CalculateTorque(molIdx, sys.coordinates, sys.com, aF, aR, tq,
+                                   box);
+    FILE *f = open_out(outdir, "forces_atom.txt");
+    for (uint i = 0; i < nAtoms; ++i)
+      fprintf(f, "%.17g %.17g %.17g %.17g %.17g %.17g\n", aF.x[i], aF.y[i],
+              aF.z[i], aR.x[i], aR.y[i], aR.z[i]);
+    fclose(f);
+    f = open_out(outdir, "forces_mol.txt");
+    for (uint m = 0; m < nMol; ++m)
+      fprintf(f, "%.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g\n",
+              mF.x[m], mF.y[m], mF.z[m], mR.x[m], mR.y[m], mR.z[m], tq.x[m],
+              tq.y[m], tq.z[m]);
+    fclose(f);
+    f = open_out(outdir, "force_energy.txt");
+    fprintf(f, "inter %.17g\nreal %.17g\n", p.boxEnergy[box].inter,
+            p.boxEnergy[box].real);
+    fclose(f);
+  }
+
+  // ---- per-proposal deltas on the initial state ---------------------------
+  if (propFile) {
+    std::ifstream in(propFile);
+    int nprop = 0;
+    in >> nprop;
+    FILE *f = open_out(outdir, "proposals_out.txt");
+    for (int i = 0; i < nprop; ++i) {
+      uint m, na;
+      in >> m >> na;
+      XYZArray pos(na);
+      for (uint a = 0; a < na; ++a) in >> pos.x[a] >> pos.y[a] >> pos.z[a];
+      Intermolecular lj, coul;
+      sys.cellList.RemoveMol(m, box, sys.coordinates);
+      bool overlap =
+          sys.calcEnergy.MoleculeInter(lj, coul, pos, m, box);
+      sys.cellList.AddMol(m, box, sys.coordinates);
+      double recip = 0.0, dest = 0.0, src = 0.0;
+      if (stat.forcefield.ewald) {
+        recip = ew->MolReciprocal(pos, m, box);
+        // insertion of the proposed copy and deletion of the current one
+        const MoleculeKind &kind = stat.mol.GetKind(m);
+        cbmc::TrialMol tNew(kind, sys.boxDimRef, box);
+        tNew.SetCoords(pos, 0);
+        dest = ew->SwapDestRecip(tNew, box, m);
+        cbmc::TrialMol tOld(kind, sys.boxDimRef, box);
+        XYZArray cur(na);
+        for (uint a = 0; a < na; ++a)
+          cur.Set(a, sys.coordinates[stat.mol.MolStart(m) + a]);
+        tOld.SetCoords(cur, 0);
+        src = ew->SwapSourceRecip(tOld, box, m);
+      }
+      fprintf(f, "%u %d %.17g %.17g %.17g %.17g %.17g\n", m, (int)overlap,
+              lj.energy, coul.energy, recip, dest, src);
+    }
+    fclose(f);
+  }
+
+  // ---- Monte Carlo trace ---------------------------------------------------
+  if (nsteps > 0) {
+    FILE *f = open_out(outdir, "trace.txt");
+    MoveSettings &ms = sys.moveSettings;
+    for (long step = 0; step < nsteps; ++step) {
+      ms.AdjustMoves(step);
+      sys.r123wrapper.SetStep(step);
+      double draw = 0;
+      uint kind = 0;
+      sys.PickMove(kind, draw);
+      uint acc0 = 0, acc1 = 0;
+      for (uint k = 0; k < mv::MOVE_KINDS_TOTAL; ++k)
+        acc0 += ms.GetAcceptTot(box, k);
+      sys.RunMove(kind, draw, step);
+      for (uint k = 0; k < mv::MOVE_KINDS_TOTAL; ++k)
+        acc1 += ms.GetAcceptTot(box, k);
+      int accepted = acc1 > acc0;
+      long m = -1;
+      int overlap = 0;
+      double dLJ = 0, dReal = 0, dRecip = 0;
+      if (kind == mv::DISPLACE) {
+        Translate *t = static_cast<Translate *>(sys.moves[kind]);
+        m = t->m;
+        overlap = t->overlap;
+        dLJ = t->inter_LJ.energy;
+        dReal = t->inter_Real.energy;
+        dRecip = t->recip.energy;
+      } else if (kind == mv::ROTATE) {
+        Rotate *r = static_cast<Rotate *>(sys.moves[kind]);
+        m = r->m;
+        overlap = r->overlap;
+        dLJ = r->inter_LJ.energy;
+        dReal = r->inter_Real.energy;
+        dRecip = r->recip.energy;
+      } else if (kind == mv::MULTIPARTICLE) {
+        MultiParticle *mp = static_cast<MultiParticle *>(sys.moves[kind]);
+        m = mp->moveType;
+        dLJ = mp->sysPotNew.boxEnergy[box].inter;
+        dReal = mp->sysPotNew.boxEnergy[box].real;
+        dRecip = mp->sysPotNew.boxEnergy[box].recip;
+      }
+      Energy &e = sys.potential.boxEnergy[box];
+      fprintf(f, "%ld %u %ld %d %d %.17g %.17g %.17g %.17g %.17g %.17g\n", step,
+              kind, m, accepted, overlap, dLJ, dReal, dRecip, e.inter, e.real,
+              e.recip);
+    }
+    fclose(f);
+    f = open_out(outdir, "energies_final.txt");
+    sys.potential.Total();
+    dump_energy(f, "running", sys.potential.boxEnergy[0]);
+    ew->UpdateVectorsAndRecipTerms(false);
+    SystemPotential pot = sys.calcEnergy.SystemTotal();
+    dump_energy(f, "recalc", pot.boxEnergy[0]);
+    for (uint k = 0; k < mv::MOVE_KINDS_TOTAL; ++k)
+      if (ms.GetTrialTot(box, k) > 0)
+        fprintf(f, "move %u tries %u accepted %u scale %.17g\n", k,
+                ms.GetTrialTot(box, k), ms.GetAcceptTot(box, k),
+                ms.GetScaleTot(box, k));
+    fprintf(f, "mp_t_max %.17g\nmp_r_max %.17g\n", ms.GetTMAX(box),
+            ms.GetRMAX(box));
+    fclose(f);
+    dump_coords(outdir, "coords_final.txt", sys.coordinates);
+    dump_coords(outdir, "com_final.txt", sys.com);
+  }
+  return 0;
+}

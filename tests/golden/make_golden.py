@@ -1,0 +1,210 @@
+"""Generate the golden vectors that pin the oracle and the GPU path.
+
+Run in a container that has the reference sources (read-only) at
+``/root/reference``::
+
+    python tests/golden/make_golden.py [--ref /root/reference]
+
+It builds the reference CPU path from its own sources with ``oracle/ref.mk``
+(outputs in ``oracle/_ref/``), writes seeded fixtures in the reference's input
+formats, runs ``oracle/_ref/ref_probe_ens1`` on each and stores the probe's
+full-precision outputs as compressed ``.npz`` files beside this script.  The
+GPU machine never needs the reference: tests read only the ``.npz`` files.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from gomc_gb300.config import SimConfig  # noqa: E402
+from gomc_gb300.systems import (lj_sphere_box, spce_water_box,  # noqa: E402
+                                water_box_length, write_reference_inputs)
+
+# name -> (system builder, config, MC steps, number of proposals)
+FIXTURES = {
+    # 256 SPC/E waters, 19.7 A box, Rcut 9, Ewald tolerance 1e-5, T = 298 K
+    "c0_water": (lambda: spce_water_box(256, 19.7, seed=7),
+                 SimConfig(temperature=298.0, rcut=9.0, tolerance=1e-5,
+                           run_steps=2000, eq_steps=1000, adj_steps=10,
+                           dis_freq=0.5, rot_freq=0.5, random_seed=1234),
+                 2000, 64),
+    # same geometry family with the MultiParticle move in the mix
+    "c0_water_mp": (lambda: spce_water_box(256, 19.7, seed=11),
+                    SimConfig(temperature=298.0, rcut=9.0, tolerance=1e-5,
+                              run_steps=600, eq_steps=300, adj_steps=10,
+                              dis_freq=0.45, rot_freq=0.45,
+                              multi_particle_freq=0.1, random_seed=4321),
+                    600, 16),
+    # 1728 waters (12^3 lattice) at 1 g/cm3: 4x4x4 cells, K ~ 8.6k
+    "w1728": (lambda: spce_water_box(1728, round(water_box_length(1728), 3),
+                                     seed=5),
+              SimConfig(temperature=298.0, rcut=9.0, tolerance=1e-5,
+                        run_steps=400, eq_steps=200, adj_steps=10,
+                        dis_freq=0.5, rot_freq=0.5, random_seed=99),
+              400, 32),
+    # single-site LJ spheres, no charges, no Ewald (GEMC-style particles)
+    "lj500": (lambda: lj_sphere_box(500, 30.0, seed=3, epsilon=148.0,
+                                    sigma=3.73, min_sep=3.0, name="LJ"),
+              SimConfig(temperature=150.0, rcut=12.0, ewald=False,
+                        electrostatic=False, run_steps=1500, eq_steps=1000,
+                        adj_steps=10, dis_freq=1.0, rot_freq=0.0,
+                        random_seed=777),
+              1500, 32),
+}
+
+
+def build_reference(ref: str) -> str:
+    subprocess.check_call(["make", "-s", "-f", os.path.join(ROOT, "oracle",
+                                                             "ref.mk"),
+                           "REF=" + ref, "OUT=" + os.path.join(ROOT, "oracle",
+                                                               "_ref"),
+                           "-j8"], cwd=ROOT)
+    return os.path.join(ROOT, "oracle", "_ref", "ref_probe_ens1")
+
+
+def _energies(path):
+    out = {}
+    for line in open(path):
+        t = line.split()
+        if len(t) == 3 and t[0] in ("box0", "running", "recalc"):
+            out[t[0] + "_" + t[1]] = float(t[2])
+        elif len(t) == 2:
+            try:
+                out[t[0]] = float(t[1])
+            except ValueError:
+                pass
+        elif len(t) == 4 and t[0] == "edgeCells":
+            out["edgeCells"] = [int(v) for v in t[1:]]
+        elif t and t[0] == "move":
+            out["move%s" % t[1]] = [float(t[3]), float(t[5]), float(t[7])]
+    return out
+
+
+def make_one(probe: str, name: str) -> None:
+    builder, cfg, nsteps, nprop = FIXTURES[name]
+    sysm = builder()
+    rng = np.random.default_rng(1000 + len(name))
+    with tempfile.TemporaryDirectory() as d:
+        write_reference_inputs(d, sysm, cfg)
+        # proposals: random rigid shifts of random molecules, wrapped
+        props_m = rng.integers(0, sysm.n_mol, size=nprop)
+        na = int(sysm.mol_start[1] - sysm.mol_start[0])
+        shifts = rng.uniform(-0.6, 0.6, size=(nprop, 3))
+        # proposal coordinates are taken relative to the coordinates the
+        # reference holds after its set-up wrap; the probe dumps those first,
+        # so run it once without proposals, then build them.
+        out0 = os.path.join(d, "out0")
+        os.makedirs(out0)
+        subprocess.check_call([probe, "in.conf", out0, "0"], cwd=d,
+                              stdout=subprocess.DEVNULL)
+        c0 = np.loadtxt(os.path.join(out0, "coords_init.txt")).reshape(-1, 3)
+        props = np.empty((nprop, na, 3))
+        for i, m in enumerate(props_m):
+            a0 = int(sysm.mol_start[m])
+            props[i] = np.mod(c0[a0:a0 + na] + shifts[i], sysm.box)
+        with open(os.path.join(d, "props.txt"), "w") as f:
+            f.write("%d\n" % nprop)
+            for m, p in zip(props_m, props):
+                f.write("%d %d %s\n" % (m, na, " ".join("%.17g" % v
+                                                        for v in p.ravel())))
+        # proposals and the Monte Carlo trace run in separate processes: the
+        # proposal calls relink the cell lists, which would change the
+        # summation order the trace starts from.
+        outp = os.path.join(d, "outp")
+        os.makedirs(outp)
+        subprocess.check_call([probe, "in.conf", outp, "0", "props.txt"],
+                              cwd=d, stdout=subprocess.DEVNULL)
+        out = os.path.join(d, "out")
+        os.makedirs(out)
+        subprocess.check_call([probe, "in.conf", out, str(nsteps)], cwd=d,
+                              stdout=subprocess.DEVNULL)
+
+        def load(fn, **kw):
+            p = os.path.join(out, fn)
+            if not os.path.exists(p):
+                p = os.path.join(outp, fn)
+            return np.loadtxt(p, **kw) if os.path.exists(p) else None
+
+        arrays = dict(
+            pos=sysm.pos, box=sysm.box, atom_kind=sysm.atom_kind,
+            atom_charge=sysm.atom_charge, mol_start=sysm.mol_start,
+            kind_eps=np.array([k.epsilon for k in sysm.kinds]),
+            kind_sigma=np.array([k.sigma for k in sysm.kinds]),
+            kind_n=np.array([k.n for k in sysm.kinds]),
+            coords_init=load("coords_init.txt"),
+            com_init=load("com_init.txt"),
+            cells=load("cells_box0.txt", skiprows=1, dtype=np.int64),
+            prop_mol=props_m, prop_pos=props,
+            prop_out=load("proposals_out.txt"),
+            trace=load("trace.txt"),
+            coords_final=load("coords_final.txt"),
+            com_final=load("com_final.txt"),
+        )
+        kv = load("kvec.txt")
+        if kv is not None:
+            arrays["kvec"] = kv
+        fa = load("forces_atom.txt")
+        if fa is not None:
+            arrays["forces_atom"] = fa
+            arrays["forces_mol"] = load("forces_mol.txt")
+        meta = dict(
+            name=name,
+            config=dict(temperature=cfg.temperature, rcut=cfg.rcut,
+                        rcut_low=cfg.rcut_low, tolerance=cfg.tolerance,
+                        ewald=cfg.ewald, electrostatic=cfg.electrostatic,
+                        adj_steps=cfg.adj_steps, dis_freq=cfg.dis_freq,
+                        rot_freq=cfg.rot_freq,
+                        multi_particle_freq=cfg.multi_particle_freq,
+                        random_seed=cfg.random_seed, nsteps=nsteps),
+            kinds=[k.name for k in sysm.kinds],
+            init=_energies(os.path.join(out, "energies_init.txt")),
+            final=_energies(os.path.join(out, "energies_final.txt")),
+        )
+        if os.path.exists(os.path.join(out, "force_energy.txt")):
+            meta["force_energy"] = _energies(os.path.join(out,
+                                                          "force_energy.txt"))
+        arrays["meta_json"] = np.frombuffer(json.dumps(meta).encode(),
+                                            dtype=np.uint8)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **{
+            k: v for k, v in arrays.items() if v is not None})
+        print("wrote", name)
+
+
+def make_kat(probe: str) -> None:
+    """Known-answer vectors of the reference's MT19937 and Philox4x64-10."""
+    with tempfile.TemporaryDirectory() as d:
+        subprocess.check_call([probe, "--kat", d], stdout=subprocess.DEVNULL)
+        mt = np.loadtxt(os.path.join(d, "kat_mt.txt"), dtype=np.uint64)
+        ph = np.loadtxt(os.path.join(d, "kat_philox.txt"), dtype=np.float64,
+                        usecols=range(7, 13))
+        phi = np.loadtxt(os.path.join(d, "kat_philox.txt"), dtype=np.uint64,
+                         usecols=range(0, 7))
+        np.savez_compressed(os.path.join(HERE, "kat_rng.npz"), mt=mt,
+                            philox_int=phi, philox_real=ph)
+        print("wrote kat_rng")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("names", nargs="*")
+    a = ap.parse_args()
+    probe = build_reference(a.ref)
+    if not a.names:
+        make_kat(probe)
+    for n in (a.names or list(FIXTURES)):
+        make_one(probe, n)
+
+
+if __name__ == "__main__":
+    main()

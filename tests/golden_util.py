@@ -1,0 +1,50 @@
+"""Loading the committed golden vectors (tests/golden/*.npz)."""
+import json
+import os
+
+import numpy as np
+
+from gomc_gb300.config import SimConfig
+from gomc_gb300.systems import AtomKind, MoleculeType, MolSystem
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+NAMES = ["c0_water", "c0_water_mp", "w1728", "lj500"]
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    meta = json.loads(bytes(z["meta_json"]).decode())
+    return z, meta
+
+
+def system_of(z, meta):
+    kinds = [AtomKind(n, float(e), float(s), float(x)) for n, e, s, x in
+             zip(meta["kinds"], z["kind_eps"], z["kind_sigma"], z["kind_n"])]
+    ms = z["mol_start"].astype(np.int32)
+    n_mol = len(ms) - 1
+    na = int(ms[1] - ms[0])
+    mt = MoleculeType("MOL", ["A%d" % i for i in range(na)],
+                      list(z["atom_kind"][:na]), list(z["atom_charge"][:na]))
+    atom_mol = np.repeat(np.arange(n_mol, dtype=np.int32), np.diff(ms))
+    return MolSystem(box=z["box"].astype(np.float64), kinds=kinds,
+                     mol_types=[mt], pos=z["pos"].astype(np.float64),
+                     atom_kind=z["atom_kind"].astype(np.int32),
+                     atom_charge=z["atom_charge"].astype(np.float64),
+                     atom_mol=atom_mol, mol_start=ms,
+                     mol_type=np.zeros(n_mol, np.int32))
+
+
+def config_of(meta):
+    c = meta["config"]
+    return SimConfig(temperature=c["temperature"], rcut=c["rcut"],
+                     rcut_low=c["rcut_low"], tolerance=c["tolerance"],
+                     ewald=c["ewald"], electrostatic=c["electrostatic"],
+                     adj_steps=c["adj_steps"], eq_steps=max(c["adj_steps"], 1),
+                     dis_freq=c["dis_freq"], rot_freq=c["rot_freq"],
+                     multi_particle_freq=c["multi_particle_freq"],
+                     random_seed=c["random_seed"])
+
+
+def move_fractions(meta):
+    c = meta["config"]
+    return [c["dis_freq"], c["rot_freq"], c["multi_particle_freq"]]

@@ -1,0 +1,134 @@
+"""The oracle against the reference's own outputs (golden vectors).
+
+The golden files were produced by running the reference GOMC CPU code on
+seeded fixtures (tests/golden/make_golden.py).  The oracle restates the same
+FP64 algorithms in C, so on one thread it must agree bit for bit on
+coordinates, k-vectors, structure factors, cell membership, accept decisions
+and, up to summation order, on energies (1e-12 relative here; the product
+contract is 1e-10).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.golden_util import NAMES, config_of, load, move_fractions, system_of
+
+REL = 1e-12
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _single_thread():
+    O.set_threads(1)
+
+
+def rel(a, b):
+    return abs(a - b) / max(abs(b), 1e-300)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_initial_state(name):
+    z, meta = load(name)
+    box = O.OracleBox(system_of(z, meta), config_of(meta))
+    st = box.system_total()
+    for term in ("inter", "real", "recip", "self", "correction", "total"):
+        ref = meta["init"]["box0_" + term]
+        assert rel(st[term], ref) <= REL or abs(st[term] - ref) < 1e-9, term
+    np.testing.assert_array_equal(box.coords(), z["coords_init"])
+    np.testing.assert_array_equal(box.com(), z["com_init"].reshape(-1, 3))
+    cells, edge = box.cells()
+    assert list(edge) == meta["init"]["edgeCells"]
+    ref_cells = np.full(box.n_atoms, -1)
+    ref_cells[z["cells"][:, 0]] = z["cells"][:, 1]
+    np.testing.assert_array_equal(cells, ref_cells)
+    if "kvec" in z:
+        kv = box.kvec()
+        assert box.num_k == int(meta["init"]["imageSize"])
+        for i, key in enumerate(["kx", "ky", "kz", "prefact", "sumRref",
+                                 "sumIref", "hsqr"]):
+            np.testing.assert_array_equal(kv[key], z["kvec"][:, i])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_proposal_deltas(name):
+    z, meta = load(name)
+    box = O.OracleBox(system_of(z, meta), config_of(meta))
+    cur = box.coords()
+    ms = z["mol_start"]
+    for i, m in enumerate(z["prop_mol"]):
+        ref = z["prop_out"][i]
+        ov, lj, re = box.molecule_inter(int(m), z["prop_pos"][i])
+        assert int(ref[0]) == m and int(ref[1]) == int(ov)
+        assert lj == ref[2] and re == ref[3]
+        if meta["config"]["ewald"]:
+            assert box.mol_reciprocal(int(m), z["prop_pos"][i]) == ref[4]
+            assert box.swap_dest_recip(int(m), z["prop_pos"][i]) == ref[5]
+            old = cur[ms[m]:ms[m + 1]]
+            assert box.swap_source_recip(int(m), old) == ref[6]
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_mc_trace(name):
+    z, meta = load(name)
+    box = O.OracleBox(system_of(z, meta), config_of(meta))
+    box.mc_init(meta["config"]["random_seed"], move_fractions(meta),
+                meta["config"]["adj_steps"])
+    tr = z["trace"]
+    n = tr.shape[0]
+    r = box.mc_run(0, n)
+    np.testing.assert_array_equal(r["kind"], tr[:, 1].astype(int))
+    np.testing.assert_array_equal(r["mol"], tr[:, 2].astype(int))
+    np.testing.assert_array_equal(r["accepted"], tr[:, 3].astype(int))
+    # per-move deltas: bit-exact for single-molecule moves; MultiParticle rows
+    # hold new box energies
+    single = tr[:, 1] < 2
+    np.testing.assert_array_equal(r["de"][single], tr[single, 5:8])
+    mp = ~single
+    if mp.any():
+        np.testing.assert_allclose(r["de"][mp], tr[mp, 5:8], rtol=1e-12,
+                                   atol=1e-9)
+    e = box.energy()
+    np.testing.assert_allclose(e[:3], tr[-1, 8:11], rtol=REL, atol=1e-9)
+    np.testing.assert_array_equal(box.coords(), z["coords_final"])
+    sc, cnt = box.mc_state()
+    for k in range(3):
+        key = "move%d" % k
+        if key in meta["final"]:
+            tries, acc, scale = meta["final"][key]
+            assert cnt[2 * k] == tries and cnt[2 * k + 1] == acc
+            if k < 2:
+                assert sc[k] == scale
+
+
+def test_forces_against_reference():
+    z, meta = load("c0_water_mp")
+    box = O.OracleBox(system_of(z, meta), config_of(meta))
+    aF, mF, lj, re = box.box_force()
+    box.copy_recip()
+    aR, mR = box.box_force_recip()
+    tq = box.torque(box.coords(), box.com(), aF, aR)
+    fa, fm = z["forces_atom"], z["forces_mol"]
+    np.testing.assert_array_equal(aF, fa[:, 0:3])
+    np.testing.assert_array_equal(aR, fa[:, 3:6])
+    np.testing.assert_array_equal(mF, fm[:, 0:3])
+    np.testing.assert_array_equal(mR, fm[:, 3:6])
+    np.testing.assert_array_equal(tq, fm[:, 6:9])
+    assert lj == meta["force_energy"]["inter"]
+    assert re == meta["force_energy"]["real"]
+
+
+def test_rng_known_answers():
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "kat_rng.npz"))
+    mt = z["mt"]
+    for seed in np.unique(mt[:, 0]):
+        g = O.MT19937(int(seed))
+        ref = mt[mt[:, 0] == seed, 1]
+        got = np.array([g.u32() for _ in range(len(ref))], dtype=np.uint64)
+        np.testing.assert_array_equal(got, ref)
+    for row_i, row_r in zip(z["philox_int"], z["philox_real"]):
+        step, seed, ctr = (int(v) for v in row_i[:3])
+        r = O.philox4x64((ctr, 0, 0, 0), (step, seed))
+        assert r == [int(v) for v in row_i[3:7]]
+        for d in range(3):
+            assert O.u01_64(r[d]) == row_r[d]
+            assert 1.0 * O.uneg11_64(r[d]) == row_r[3 + d]
