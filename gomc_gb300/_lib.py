@@ -1,0 +1,130 @@
+"""ctypes binding of the C ABI in include/gomc_gb300.h.
+
+The library is the in-tree ``gomc_gb300/_build/libgomc_gb300.so`` built by
+``gomc_gb300.build``.  There is no fallback: if the library is missing or
+cannot load, :func:`lib` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+_LIB = None
+
+STATUS = {0: "GB_OK", 1: "GB_ERR_ARG", 2: "GB_ERR_CUDA", 3: "GB_ERR_NOMEM",
+          4: "GB_ERR_CAPACITY", 5: "GB_ERR_TIMEOUT", 6: "GB_ERR_STATE",
+          7: "GB_ERR_UNSUPPORTED"}
+
+GB_FP64 = 0
+GB_MIXED = 1
+
+
+class GbError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s: %s" % (STATUS.get(code, code), msg))
+        self.code = code
+
+
+class SystemDesc(C.Structure):
+    _fields_ = [("n_atoms", C.c_int32), ("n_mol", C.c_int32),
+                ("n_kinds", C.c_int32),
+                ("pos", C.POINTER(C.c_double)),
+                ("atom_kind", C.POINTER(C.c_int32)),
+                ("atom_charge", C.POINTER(C.c_double)),
+                ("mol_start", C.POINTER(C.c_int32)),
+                ("kind_epsilon", C.POINTER(C.c_double)),
+                ("kind_sigma", C.POINTER(C.c_double)),
+                ("kind_n", C.POINTER(C.c_double)),
+                ("box", C.c_double * 3)]
+
+
+class Config(C.Structure):
+    _fields_ = [("temperature", C.c_double), ("rcut", C.c_double),
+                ("rcut_low", C.c_double), ("rcut_coulomb", C.c_double),
+                ("tolerance", C.c_double), ("ewald", C.c_int32),
+                ("electrostatic", C.c_int32), ("precision", C.c_int32),
+                ("device", C.c_int32)]
+
+
+class McParams(C.Structure):
+    _fields_ = [("seed", C.c_uint32), ("frac", C.c_double * 3),
+                ("adj_steps", C.c_int32), ("use_scales", C.c_int32),
+                ("scales", C.c_double * 4), ("recompute_freq", C.c_int32)]
+
+
+# every function the header declares: name -> (restype, argtypes)
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int32)
+_L = C.POINTER(C.c_int64)
+SIGNATURES = {
+    "gb_version": (C.c_char_p, []),
+    "gb_last_error": (C.c_char_p, [_P]),
+    "gb_box_create": (C.c_int, [C.POINTER(SystemDesc), C.POINTER(Config),
+                                C.POINTER(_P)]),
+    "gb_box_destroy": (None, [_P]),
+    "gb_system_total": (C.c_int, [_P, _D]),
+    "gb_box_inter": (C.c_int, [_P, _D, _D]),
+    "gb_molecule_inter": (C.c_int, [_P, C.c_int32, _D, _D, _D, _I]),
+    "gb_particle_inter": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_double, _D,
+                                    C.c_int32, _D, _D, _I]),
+    "gb_box_force": (C.c_int, [_P, _D, _D, _D, _D]),
+    "gb_calculate_torque": (C.c_int, [_P, _D]),
+    "gb_num_kvectors": (C.c_int, [_P, _I, _I]),
+    "gb_get_kvectors": (C.c_int, [_P, _D]),
+    "gb_get_sums_new": (C.c_int, [_P, _D, _D]),
+    "gb_box_reciprocal_setup": (C.c_int, [_P]),
+    "gb_box_reciprocal_sums": (C.c_int, [_P]),
+    "gb_box_reciprocal": (C.c_int, [_P, C.c_int32, _D]),
+    "gb_mol_reciprocal": (C.c_int, [_P, C.c_int32, _D, _D]),
+    "gb_swap_dest_recip": (C.c_int, [_P, C.c_int32, _D, _D]),
+    "gb_swap_source_recip": (C.c_int, [_P, C.c_int32, _D, _D]),
+    "gb_update_recip": (C.c_int, [_P]),
+    "gb_copy_recip": (C.c_int, [_P]),
+    "gb_box_self": (C.c_int, [_P, _D]),
+    "gb_mol_correction": (C.c_int, [_P, C.c_int32, _D]),
+    "gb_box_force_reciprocal": (C.c_int, [_P, _D, _D]),
+    "gb_grid_all": (C.c_int, [_P]),
+    "gb_cell_membership": (C.c_int, [_P, _I, _I]),
+    "gb_get_coords": (C.c_int, [_P, _D, _D]),
+    "gb_set_coords": (C.c_int, [_P, _D, _D]),
+    "gb_get_energy": (C.c_int, [_P, _D]),
+    "gb_set_energy": (C.c_int, [_P, _D]),
+    "gb_mc_init": (C.c_int, [_P, C.POINTER(McParams)]),
+    "gb_mc_run": (C.c_int, [_P, C.c_int64, C.c_int64, _I, _I, _I, _D]),
+    "gb_mc_state": (C.c_int, [_P, _D, _L]),
+    "gb_mc_run_batch": (C.c_int, [C.POINTER(_P), C.c_int32, C.c_int64,
+                                  C.c_int64]),
+}
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def lib(build_if_missing: bool = False):
+    """Load the library (optionally building it first); raise if absent."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError("libgomc_gb300.so is not built (%s); run "
+                               "python -m gomc_gb300.build" % path)
+        _build.build()
+    L = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _LIB = L
+    return L
+
+
+def check(rc: int, box=None) -> None:
+    if rc != 0:
+        msg = lib().gb_last_error(box)
+        raise GbError(rc, msg.decode() if msg else "")

@@ -1,0 +1,906 @@
+// Box set-up, resident state and the host side of the energy-path calls.
+#include "gb_box.h"
+
+#include <cmath>
+#include <cstring>
+#include <algorithm>
+
+namespace gb {
+
+// ---------------------------------------------------------------------------
+// Force field: FFSetup::Particle::Read zeroing (src/FFSetup.cpp:246-255),
+// FFParticle::Blend (src/FFParticle.cpp:200-242) and
+// Forcefield::InitBasicVals (src/Forcefield.cpp:37-83).
+// ---------------------------------------------------------------------------
+void build_ff(const HostSystem &s, const BoxConfig &c, FF *ff) {
+  std::memset(ff, 0, sizeof(FF));
+  int nk = s.n_kinds;
+  ff->n_kinds = nk;
+  for (int i = 0; i < nk; ++i)
+    for (int j = 0; j < nk; ++j) {
+      int idx = i + j * nk;
+      double ei = std::fabs(s.eps[i]) < 1.0e-20 ? 0.0 : s.eps[i];
+      double ej = std::fabs(s.eps[j]) < 1.0e-20 ? 0.0 : s.eps[j];
+      double ni = std::fabs(s.eps[i]) < 1.0e-20 ? 12.0 : s.nexp[i];
+      double nj = std::fabs(s.eps[j]) < 1.0e-20 ? 12.0 : s.nexp[j];
+      double n = (ni + nj) * 0.5;
+      double cn = n / (n - 6.0) * std::pow(n / 6.0, (6.0 / (n - 6.0)));
+      double sg = (s.sigma[i] + s.sigma[j]) * 0.5;
+      ff->nexp[idx] = n;
+      ff->sigmaSq[idx] = sg * sg;
+      double e = std::sqrt(ei * ej);
+      ff->eps_cn[idx] = cn * e;
+      ff->eps_cn_6[idx] = ff->eps_cn[idx] * 6;
+      ff->nOver6[idx] = n / 6;
+      ff->sigmaSq_f[idx] = (float)ff->sigmaSq[idx];
+      ff->eps_cn_f[idx] = (float)ff->eps_cn[idx];
+    }
+  ff->rcut = c.rcut;
+  ff->rcutSq = c.rcut * c.rcut;
+  ff->rcutLowSq = c.rcut_low * c.rcut_low;
+  ff->rcutCoulSq = c.rcut_coulomb * c.rcut_coulomb;
+  ff->ewald = c.ewald;
+  ff->electrostatic = c.electrostatic;
+  if (c.ewald) {
+    ff->alpha = std::sqrt(-std::log(c.tolerance)) / c.rcut_coulomb;
+    ff->alphaSq = ff->alpha * ff->alpha;
+    ff->recip_rcut = -2.0 * std::log(c.tolerance) / c.rcut_coulomb;
+    ff->recip_rcutSq = ff->recip_rcut * ff->recip_rcut;
+  }
+  ff->beta = 1 / c.temperature;
+}
+
+// ---------------------------------------------------------------------------
+// k-vectors of an orthogonal box, in the reference's order: x outer (x >= 0),
+// y, z inner, |k|^2 < k_c^2 (Ewald::RecipInitOrth, src/Ewald.cpp:847-903).
+// ---------------------------------------------------------------------------
+void recip_vectors(const double L[3], double volume, double alphaSq,
+                   double recip_rcutSq, double recip_rcut,
+                   std::vector<double> &kx, std::vector<double> &ky,
+                   std::vector<double> &kz, std::vector<double> &hsqr,
+                   std::vector<double> &prefact, std::vector<char4> &kn,
+                   int *kmax) {
+  double alpsqr4 = 1.0 / (4.0 * alphaSq);
+  double cv[3];
+  for (int d = 0; d < 3; ++d) {
+    cv[d] = 1.0 / L[d];
+    cv[d] *= 2.0 * M_PI;
+  }
+  double vol = volume / (4.0 * M_PI);
+  int nkx = (int)(recip_rcut * L[0] / (2.0 * M_PI)) + 1;
+  int nky = (int)(recip_rcut * L[1] / (2.0 * M_PI)) + 1;
+  int nkz = (int)(recip_rcut * L[2] / (2.0 * M_PI)) + 1;
+  *kmax = std::max(std::max(nkx, nky), std::max(nky, nkz));
+  kx.clear(); ky.clear(); kz.clear(); hsqr.clear(); prefact.clear(); kn.clear();
+  for (int x = 0; x <= nkx; x++) {
+    int nky_min = (x == 0) ? 0 : -nky;
+    for (int y = nky_min; y <= nky; y++) {
+      int nkz_min = (x == 0 && y == 0) ? 1 : -nkz;
+      for (int z = nkz_min; z <= nkz; z++) {
+        double kX = cv[0] * x;
+        double kY = cv[1] * y;
+        double kZ = cv[2] * z;
+        double ksqr = kX * kX + kY * kY + kZ * kZ;
+        if (ksqr < recip_rcutSq) {
+          kx.push_back(kX);
+          ky.push_back(kY);
+          kz.push_back(kZ);
+          hsqr.push_back(ksqr);
+          prefact.push_back(QQ_FACT * std::exp(-ksqr * alpsqr4) /
+                            (ksqr * vol));
+          kn.push_back(make_char4((signed char)x, (signed char)y,
+                                  (signed char)z, 0));
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+Box::~Box() { FreeAll(); }
+
+int Box::Fail(int code, const std::string &msg) {
+  last_error = msg;
+  return code;
+}
+
+int Box::CudaCheck(cudaError_t e, const char *what) {
+  if (e == cudaSuccess)
+    return OK;
+  last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? ERR_NOMEM : ERR_CUDA;
+}
+
+template <class T>
+int Box::Alloc(T **p, size_t n) {
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+  if (e != cudaSuccess)
+    return CudaCheck(e, "cudaMalloc");
+  allocs_.push_back(q);
+  *p = (T *)q;
+  return OK;
+}
+
+void Box::FreeAll() {
+  if (stream)
+    cudaStreamSynchronize(stream);
+  for (void *p : allocs_)
+    cudaFree(p);
+  allocs_.clear();
+  if (h_pinned)
+    cudaFreeHost(h_pinned);
+  h_pinned = nullptr;
+  if (own_stream && stream)
+    cudaStreamDestroy(stream);
+  stream = nullptr;
+}
+
+int Box::EnsureScratch(size_t n) {
+  if (n <= scratch_len)
+    return OK;
+  int rc = Alloc(&d_scratch, n);
+  if (rc)
+    return rc;
+  scratch_len = n;
+  return OK;
+}
+
+int Box::Sync() {
+  return CudaCheck(cudaStreamSynchronize(stream), "stream synchronize");
+}
+
+int Box::Create(const HostSystem &sys, const BoxConfig &cfg, Box **out,
+                std::string *err) {
+  Box *b = new Box();
+  int rc = b->Init(sys, cfg);
+  if (rc) {
+    if (err)
+      *err = b->last_error;
+    delete b;
+    return rc;
+  }
+  *out = b;
+  return OK;
+}
+
+int Box::Init(const HostSystem &s0, const BoxConfig &c) {
+  cfg = c;
+  if (s0.n_atoms <= 0 || s0.n_mol <= 0 || s0.n_kinds <= 0 ||
+      s0.n_kinds > MAX_KINDS)
+    return Fail(ERR_ARG, "atom, molecule or kind count out of range");
+  for (int d = 0; d < 3; ++d)
+    if (!(s0.L[d] > 0))
+      return Fail(ERR_ARG, "box edge must be positive");
+  if (!(c.rcut > 0) || !(c.temperature > 0))
+    return Fail(ERR_ARG, "Rcut and Temperature must be positive");
+  if (c.ewald && !(c.tolerance > 0 && c.tolerance < 1))
+    return Fail(ERR_ARG, "Ewald tolerance must be in (0, 1)");
+  if ((int)s0.mstart.size() != s0.n_mol + 1 || s0.mstart[0] != 0 ||
+      s0.mstart[s0.n_mol] != s0.n_atoms)
+    return Fail(ERR_ARG, "molecule start offsets are inconsistent");
+  for (int m = 0; m < s0.n_mol; ++m)
+    if (s0.mstart[m + 1] <= s0.mstart[m])
+      return Fail(ERR_ARG, "empty molecule");
+  for (int i = 0; i < s0.n_atoms; ++i)
+    if (s0.kind[i] < 0 || s0.kind[i] >= s0.n_kinds)
+      return Fail(ERR_ARG, "atom kind out of range");
+
+  int rc = CudaCheck(cudaSetDevice(c.device), "cudaSetDevice");
+  if (rc)
+    return rc;
+  cudaDeviceProp prop;
+  rc = CudaCheck(cudaGetDeviceProperties(&prop, c.device), "device props");
+  if (rc)
+    return rc;
+  sm_count = prop.multiProcessorCount;
+  rc = CudaCheck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking),
+                 "stream");
+  if (rc)
+    return rc;
+  own_stream = true;
+
+  host = s0;
+  HostSystem &s = host;
+  int N = s.n_atoms, M = s.n_mol;
+  s.mol.assign(N, 0);
+  for (int m = 0; m < M; ++m)
+    for (int a = s.mstart[m]; a < s.mstart[m + 1]; ++a)
+      s.mol[a] = m;
+  // Coordinates::WrapCoordinate (src/Coordinates.cpp:24-73)
+  for (int i = 0; i < N; ++i) {
+    s.x[i] = wrap1(s.x[i], s.L[0]);
+    s.y[i] = wrap1(s.y[i], s.L[1]);
+    s.z[i] = wrap1(s.z[i], s.L[2]);
+    if (!(s.x[i] >= 0 && s.x[i] <= s.L[0] && s.y[i] >= 0 && s.y[i] <= s.L[1] &&
+          s.z[i] >= 0 && s.z[i] <= s.L[2]))
+      return Fail(ERR_ARG, "an atom lies outside the box after wrapping");
+  }
+  // COM::CalcCOM (src/COM.h:47-68), including its unwrap / re-wrap of the
+  // atom coordinates.
+  double half[3] = {s.L[0] * 0.5, s.L[1] * 0.5, s.L[2] * 0.5};
+  s.cx.assign(M, 0);
+  s.cy.assign(M, 0);
+  s.cz.assign(M, 0);
+  for (int m = 0; m < M; ++m) {
+    int a0 = s.mstart[m], a1 = s.mstart[m + 1];
+    double rx = s.x[a0], ry = s.y[a0], rz = s.z[a0];
+    for (int p = a0; p < a1; ++p) {
+      s.x[p] = unwrap1(s.x[p], rx, s.L[0], half[0]);
+      s.y[p] = unwrap1(s.y[p], ry, s.L[1], half[1]);
+      s.z[p] = unwrap1(s.z[p], rz, s.L[2], half[2]);
+    }
+    double cx = 0, cy = 0, cz = 0;
+    for (int p = a0; p < a1; ++p) {
+      cx += s.x[p];
+      cy += s.y[p];
+      cz += s.z[p];
+    }
+    for (int p = a0; p < a1; ++p) {
+      s.x[p] = wrap1(s.x[p], s.L[0]);
+      s.y[p] = wrap1(s.y[p], s.L[1]);
+      s.z[p] = wrap1(s.z[p], s.L[2]);
+    }
+    double inv = 1.0 / (double)(a1 - a0);
+    cx *= inv;
+    cy *= inv;
+    cz *= inv;
+    s.cx[m] = wrap1(cx, s.L[0]);
+    s.cy[m] = wrap1(cy, s.L[1]);
+    s.cz[m] = wrap1(cz, s.L[2]);
+  }
+
+  build_ff(s, c, &ff);
+  DevBox &d = dev;
+  for (int k = 0; k < 3; ++k) {
+    d.L[k] = s.L[k];
+    d.half[k] = half[k];
+  }
+  d.volume = s.L[0] * s.L[1] * s.L[2];
+  d.n_atoms = N;
+  d.n_mol = M;
+
+  // cell grid (CellList::ResizeGrid / RebuildNeighbors,
+  // src/CellList.cpp:138-218)
+  for (int k = 0; k < 3; ++k) {
+    d.edge[k] = std::max((int)std::floor(s.L[k] / c.rcut), 3);
+    d.cellSize[k] = s.L[k] / d.edge[k];
+  }
+  d.ncell = d.edge[0] * d.edge[1] * d.edge[2];
+  std::vector<int> nbr((size_t)d.ncell * NB27);
+  {
+    int *e = d.edge;
+    for (int x = 0; x < e[0]; ++x)
+      for (int y = 0; y < e[1]; ++y)
+        for (int z = 0; z < e[2]; ++z) {
+          int cell = x * e[2] * e[1] + y * e[2] + z;
+          int n = 0;
+          for (int dx = -1; dx <= 1; ++dx)
+            for (int dy = -1; dy <= 1; ++dy)
+              for (int dz = -1; dz <= 1; ++dz)
+                nbr[(size_t)cell * NB27 + n++] =
+                    ((x + dx + e[0]) % e[0]) * e[2] * e[1] +
+                    ((y + dy + e[1]) % e[1]) * e[2] + ((z + dz + e[2]) % e[2]);
+        }
+  }
+  // capacity: three times the fullest cell at set-up, at least 32 slots
+  {
+    std::vector<int> cnt(d.ncell, 0);
+    int mx = 0;
+    for (int i = 0; i < N; ++i) {
+      int cc = position_to_cell(d, s.x[i], s.y[i], s.z[i]);
+      mx = std::max(mx, ++cnt[cc]);
+    }
+    int cap = std::max(3 * mx, 32);
+    d.cap = (cap + 31) / 32 * 32;
+  }
+
+  // device allocations
+  size_t NC = (size_t)d.ncell * d.cap;
+  if ((rc = Alloc(&d.x, N)) || (rc = Alloc(&d.y, N)) || (rc = Alloc(&d.z, N)) ||
+      (rc = Alloc(&d.cx, M)) || (rc = Alloc(&d.cy, M)) ||
+      (rc = Alloc(&d.cz, M)) || (rc = Alloc(&d.q, N)) ||
+      (rc = Alloc(&d.kind, N)) || (rc = Alloc(&d.mol, N)) ||
+      (rc = Alloc(&d.mstart, M + 1)) || (rc = Alloc(&d.nbr, nbr.size())) ||
+      (rc = Alloc(&d.cell_count, d.ncell)) || (rc = Alloc(&d.cell_atom, NC)) ||
+      (rc = Alloc(&d.cell_pos, NC)) || (rc = Alloc(&d.cell_meta, NC)) ||
+      (rc = Alloc(&d.cell_fix, NC)) || (rc = Alloc(&d.atom_cell, N)) ||
+      (rc = Alloc(&d.atom_slot, N)) || (rc = Alloc(&d.energy, 8)) ||
+      (rc = Alloc(&d.err, 4)) || (rc = Alloc(&d_ff, 1)) ||
+      (rc = Alloc(&d_small, 4096)) || (rc = Alloc(&d_aF, 3 * (size_t)N)) ||
+      (rc = Alloc(&d_mF, 3 * (size_t)M)) || (rc = Alloc(&d_aR, 3 * (size_t)N)) ||
+      (rc = Alloc(&d_mR, 3 * (size_t)M)) || (rc = Alloc(&d_tq, 3 * (size_t)M)))
+    return rc;
+  rc = CudaCheck(cudaMallocHost(&h_pinned, 4096 * sizeof(double)), "pinned");
+  if (rc)
+    return rc;
+
+  auto up = [&](void *dst, const void *src, size_t bytes) {
+    return CudaCheck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice,
+                                     stream),
+                     "upload");
+  };
+  if ((rc = up(d.x, s.x.data(), N * 8)) || (rc = up(d.y, s.y.data(), N * 8)) ||
+      (rc = up(d.z, s.z.data(), N * 8)) ||
+      (rc = up(d.cx, s.cx.data(), M * 8)) ||
+      (rc = up(d.cy, s.cy.data(), M * 8)) ||
+      (rc = up(d.cz, s.cz.data(), M * 8)) ||
+      (rc = up(d.q, s.q.data(), N * 8)) ||
+      (rc = up(d.kind, s.kind.data(), N * 4)) ||
+      (rc = up(d.mol, s.mol.data(), N * 4)) ||
+      (rc = up(d.mstart, s.mstart.data(), (M + 1) * 4)) ||
+      (rc = up(d.nbr, nbr.data(), nbr.size() * 4)) ||
+      (rc = up(d_ff, &ff, sizeof(FF))))
+    return rc;
+  if ((rc = CudaCheck(cudaMemsetAsync(d.err, 0, 16, stream), "memset")) ||
+      (rc = CudaCheck(cudaMemsetAsync(d.energy, 0, 64, stream), "memset")))
+    return rc;
+
+  // Ewald tables
+  if (c.ewald) {
+    std::vector<double> kx, ky, kz, hs, pf;
+    std::vector<char4> kn;
+    recip_vectors(s.L, d.volume, ff.alphaSq, ff.recip_rcutSq, ff.recip_rcut,
+                  kx, ky, kz, hs, pf, kn, &d.kmax);
+    d.K = (int)kx.size();
+    if (d.kmax > 127)
+      return Fail(ERR_UNSUPPORTED, "k-vector index above 127");
+    std::vector<float> pff(pf.begin(), pf.end());
+    size_t K = d.K;
+    if ((rc = Alloc(&d.kx, K)) || (rc = Alloc(&d.ky, K)) ||
+        (rc = Alloc(&d.kz, K)) || (rc = Alloc(&d.prefact, K)) ||
+        (rc = Alloc(&d.hsqr, K)) || (rc = Alloc(&d.kn, K)) ||
+        (rc = Alloc(&d.prefact_f, K)) || (rc = Alloc(&d.sumRref, K)) ||
+        (rc = Alloc(&d.sumIref, K)) || (rc = Alloc(&d.sumRnew, K)) ||
+        (rc = Alloc(&d.sumInew, K)))
+      return rc;
+    if ((rc = up(d.kx, kx.data(), K * 8)) || (rc = up(d.ky, ky.data(), K * 8)) ||
+        (rc = up(d.kz, kz.data(), K * 8)) ||
+        (rc = up(d.prefact, pf.data(), K * 8)) ||
+        (rc = up(d.hsqr, hs.data(), K * 8)) ||
+        (rc = up(d.kn, kn.data(), K * 4)) ||
+        (rc = up(d.prefact_f, pff.data(), K * 4)))
+      return rc;
+  }
+  if ((rc = GridAll()))
+    return rc;
+  // initial energies (System::Init -> SystemTotal)
+  double tot[9];
+  if ((rc = SystemTotal(tot)))
+    return rc;
+  return OK;
+}
+
+int Box::CheckError() {
+  int herr[4] = {0, 0, 0, 0};
+  int rc = CudaCheck(cudaMemcpyAsync(herr, dev.err, 16, cudaMemcpyDeviceToHost,
+                                     stream),
+                     "error read");
+  if (rc)
+    return rc;
+  if ((rc = Sync()))
+    return rc;
+  if (herr[0] & DERR_CELL_OVERFLOW)
+    return Fail(ERR_CAPACITY, "a cell exceeded its slot capacity");
+  if (herr[0] & DERR_BARRIER_TIMEOUT)
+    return Fail(ERR_TIMEOUT, "a device-side wait ran out of iterations");
+  if (herr[0] & DERR_BAD_INPUT)
+    return Fail(ERR_ARG, "invalid input detected on the device");
+  return OK;
+}
+
+int Box::GridAll() {
+  int rc = launch_grid_all(*this, dev);
+  if (rc)
+    return rc;
+  return OK;
+}
+
+int Box::BoxInter(double *inter, double *real) {
+  int rc = launch_box_inter(*this, d_small);
+  if (rc)
+    return rc;
+  rc = CudaCheck(cudaMemcpyAsync(h_pinned, d_small, 16, cudaMemcpyDeviceToHost,
+                                 stream),
+                 "download");
+  if (rc || (rc = Sync()))
+    return rc;
+  *inter = h_pinned[0];
+  *real = h_pinned[1];
+  return CheckError();
+}
+
+int Box::RecipSums(const double *x, const double *y, const double *z) {
+  if (!cfg.ewald)
+    return OK;
+  return launch_recip_sums(*this, x, y, z, dev.sumRnew, dev.sumInew);
+}
+
+int Box::RecipSetup() {
+  if (!cfg.ewald)
+    return OK;
+  int rc = RecipSums(dev.x, dev.y, dev.z);
+  if (rc)
+    return rc;
+  // SetRecipRef: Ref <- New
+  size_t bytes = (size_t)dev.K * 8;
+  if ((rc = CudaCheck(cudaMemcpyAsync(dev.sumRref, dev.sumRnew, bytes,
+                                      cudaMemcpyDeviceToDevice, stream),
+                      "copy")) ||
+      (rc = CudaCheck(cudaMemcpyAsync(dev.sumIref, dev.sumInew, bytes,
+                                      cudaMemcpyDeviceToDevice, stream),
+                      "copy")))
+    return rc;
+  return OK;
+}
+
+int Box::RecipEnergy(double *e, bool ref_sums) {
+  if (!cfg.ewald) {
+    *e = 0;
+    return OK;
+  }
+  int rc = launch_recip_energy(*this, ref_sums ? dev.sumRref : dev.sumRnew,
+                               ref_sums ? dev.sumIref : dev.sumInew, d_small);
+  if (rc)
+    return rc;
+  if ((rc = CudaCheck(cudaMemcpyAsync(h_pinned, d_small, 8,
+                                      cudaMemcpyDeviceToHost, stream),
+                      "download")) ||
+      (rc = Sync()))
+    return rc;
+  *e = h_pinned[0];
+  return OK;
+}
+
+int Box::BoxSelf(double *e) {
+  // Ewald::BoxSelf (src/Ewald.cpp:1125-1163): per molecule kind, the sum of
+  // squared charges of one molecule times the molecule count.  Molecules are
+  // grouped by identical (kind, charge) lists in first-seen order.
+  if (!cfg.ewald) {
+    *e = 0;
+    return OK;
+  }
+  const HostSystem &s = host;
+  std::vector<int> seen(s.n_mol, 0);
+  double self = 0.0;
+  for (int m = 0; m < s.n_mol; ++m) {
+    if (seen[m])
+      continue;
+    int len = s.mstart[m + 1] - s.mstart[m];
+    long count = 0;
+    for (int m2 = m; m2 < s.n_mol; ++m2) {
+      if (seen[m2] || s.mstart[m2 + 1] - s.mstart[m2] != len)
+        continue;
+      bool same = true;
+      for (int a = 0; a < len && same; ++a)
+        same = s.q[s.mstart[m2] + a] == s.q[s.mstart[m] + a] &&
+               s.kind[s.mstart[m2] + a] == s.kind[s.mstart[m] + a];
+      if (same) {
+        seen[m2] = 1;
+        count++;
+      }
+    }
+    double molSelf = 0.0;
+    for (int a = 0; a < len; ++a)
+      molSelf += (s.q[s.mstart[m] + a] * s.q[s.mstart[m] + a]);
+    self += (molSelf * count);
+  }
+  self *= -1.0 * ff.alpha * QQ_FACT * M_2_SQRTPI * 0.5;
+  *e = self;
+  return OK;
+}
+
+int Box::BoxCorrection(double *e) {
+  if (!cfg.ewald) {
+    *e = 0;
+    return OK;
+  }
+  int rc = launch_correction(*this, d_small);
+  if (rc)
+    return rc;
+  if ((rc = CudaCheck(cudaMemcpyAsync(h_pinned, d_small, 8,
+                                      cudaMemcpyDeviceToHost, stream),
+                      "download")) ||
+      (rc = Sync()))
+    return rc;
+  *e = h_pinned[0];
+  return OK;
+}
+
+int Box::MolCorrection(int m, double *e) {
+  // Ewald::MolCorrection (src/Ewald.cpp:1056-1085), on the host copy of the
+  // molecule's current coordinates.
+  if (m < 0 || m >= dev.n_mol)
+    return Fail(ERR_ARG, "molecule index out of range");
+  if (!cfg.ewald) {
+    *e = 0;
+    return OK;
+  }
+  int a0 = host.mstart[m], n = host.mstart[m + 1] - a0;
+  std::vector<double> xyz(3 * n);
+  for (int d = 0; d < 3; ++d) {
+    double *src = d == 0 ? dev.x : d == 1 ? dev.y : dev.z;
+    int rc = CudaCheck(cudaMemcpyAsync(h_pinned + d * n, src + a0, n * 8,
+                                       cudaMemcpyDeviceToHost, stream),
+                       "download");
+    if (rc)
+      return rc;
+  }
+  int rc = Sync();
+  if (rc)
+    return rc;
+  double corr = 0.0;
+  for (int i = 0; i < n; ++i) {
+    if (std::fabs(host.q[a0 + i]) < 0.000000001)
+      continue;
+    for (int j = i + 1; j < n; ++j) {
+      double dx = min_image(h_pinned[i] - h_pinned[j], dev.L[0], dev.half[0]);
+      double dy = min_image(h_pinned[n + i] - h_pinned[n + j], dev.L[1],
+                            dev.half[1]);
+      double dz = min_image(h_pinned[2 * n + i] - h_pinned[2 * n + j],
+                            dev.L[2], dev.half[2]);
+      double distSq = dx * dx + dy * dy + dz * dz;
+      double dist = std::sqrt(distSq);
+      corr += (host.q[a0 + i] * host.q[a0 + j] * std::erf(ff.alpha * dist) /
+               dist);
+    }
+  }
+  *e = -1.0 * QQ_FACT * corr * 1.0 * 1.0;
+  return OK;
+}
+
+int Box::SystemTotal(double out[9]) {
+  // CalculateEnergy::SystemTotal (src/CalculateEnergy.cpp:83-138) after
+  // Ewald::UpdateVectorsAndRecipTerms: real space, reciprocal sums of the
+  // current coordinates (Ref <- New), self and correction terms.
+  double inter, real;
+  int rc = BoxInter(&inter, &real);
+  if (rc)
+    return rc;
+  double recip = 0.0, self = 0.0, corr = 0.0;
+  if (cfg.ewald) {
+    if ((rc = RecipSetup()) || (rc = RecipEnergy(&recip, true)) ||
+        (rc = BoxCorrection(&corr)) || (rc = BoxSelf(&self)))
+      return rc;
+  }
+  out[0] = inter;
+  out[1] = real;
+  out[2] = recip;
+  out[3] = self;
+  out[4] = corr;
+  out[5] = 0.0;
+  out[6] = 0.0;
+  out[7] = 0.0;
+  out[8] = 0.0 + 0.0 + inter + 0.0 + real + recip + self + corr;
+  double e5[5] = {inter, real, recip, self, corr};
+  return SetEnergy(e5);
+}
+
+int Box::GetEnergy(double e5[5]) {
+  int rc = CudaCheck(cudaMemcpyAsync(h_pinned, dev.energy, 40,
+                                     cudaMemcpyDeviceToHost, stream),
+                     "download");
+  if (rc || (rc = Sync()))
+    return rc;
+  for (int i = 0; i < 5; ++i)
+    e5[i] = h_pinned[i];
+  return OK;
+}
+
+int Box::SetEnergy(const double e5[5]) {
+  for (int i = 0; i < 5; ++i)
+    h_pinned[i] = e5[i];
+  int rc = CudaCheck(cudaMemcpyAsync(dev.energy, h_pinned, 40,
+                                     cudaMemcpyHostToDevice, stream),
+                     "upload");
+  if (rc)
+    return rc;
+  return Sync();
+}
+
+static int check_newpos(const Box &b, int m, const double *p, int n) {
+  for (int a = 0; a < n; ++a)
+    for (int d = 0; d < 3; ++d) {
+      double v = p[3 * a + d];
+      if (!(v >= 0.0 && v <= b.dev.L[d]))
+        return ERR_ARG;
+    }
+  return OK;
+}
+
+int Box::MoleculeInter(int m, const double *new_pos, double *lj, double *real,
+                       int *overlap) {
+  if (m < 0 || m >= dev.n_mol)
+    return Fail(ERR_ARG, "molecule index out of range");
+  int n = host.mstart[m + 1] - host.mstart[m];
+  if (n > 64)
+    return Fail(ERR_UNSUPPORTED, "molecule larger than 64 atoms");
+  if (check_newpos(*this, m, new_pos, n))
+    return Fail(ERR_ARG, "trial coordinates must lie inside the box");
+  std::memcpy(h_pinned, new_pos, 3 * n * sizeof(double));
+  int rc = CudaCheck(cudaMemcpyAsync(d_small + 1024, h_pinned, 3 * n * 8,
+                                     cudaMemcpyHostToDevice, stream),
+                     "upload");
+  if (rc || (rc = launch_mol_inter(*this, m, d_small + 1024, d_small)))
+    return rc;
+  if ((rc = CudaCheck(cudaMemcpyAsync(h_pinned, d_small, 24,
+                                      cudaMemcpyDeviceToHost, stream),
+                      "download")) ||
+      (rc = Sync()))
+    return rc;
+  *lj = h_pinned[0];
+  *real = h_pinned[1];
+  *overlap = h_pinned[2] != 0.0;
+  return CheckError();
+}
+
+int Box::ParticleInter(int m, int kind, double charge, const double *trials,
+                       int ntrials, double *en, double *real, int *overlap) {
+  if (m < 0 || m >= dev.n_mol || kind < 0 || kind >= ff.n_kinds ||
+      ntrials <= 0 || ntrials > 256)
+    return Fail(ERR_ARG, "ParticleInter arguments out of range");
+  if (check_newpos(*this, m, trials, ntrials))
+    return Fail(ERR_ARG, "trial coordinates must lie inside the box");
+  std::memcpy(h_pinned, trials, 3 * ntrials * sizeof(double));
+  int rc = CudaCheck(cudaMemcpyAsync(d_small + 1024, h_pinned, 3 * ntrials * 8,
+                                     cudaMemcpyHostToDevice, stream),
+                     "upload");
+  if (rc || (rc = launch_particle_inter(*this, m, kind, charge, d_small + 1024,
+                                        ntrials, d_small)))
+    return rc;
+  if ((rc = CudaCheck(cudaMemcpyAsync(h_pinned, d_small, 3 * ntrials * 8,
+                                      cudaMemcpyDeviceToHost, stream),
+                      "download")) ||
+      (rc = Sync()))
+    return rc;
+  for (int t = 0; t < ntrials; ++t) {
+    en[t] = h_pinned[3 * t];
+    real[t] = h_pinned[3 * t + 1];
+    overlap[t] = h_pinned[3 * t + 2] != 0.0;
+  }
+  return CheckError();
+}
+
+int Box::MolReciprocal(int m, const double *new_pos, double *de) {
+  if (m < 0 || m >= dev.n_mol)
+    return Fail(ERR_ARG, "molecule index out of range");
+  if (!cfg.ewald) {
+    *de = 0;
+    return OK;
+  }
+  int n = host.mstart[m + 1] - host.mstart[m];
+  if (n > 64)
+    return Fail(ERR_UNSUPPORTED, "molecule larger than 64 atoms");
+  std::memcpy(h_pinned, new_pos, 3 * n * sizeof(double));
+  int rc = CudaCheck(cudaMemcpyAsync(d_small + 1024, h_pinned, 3 * n * 8,
+                                     cudaMemcpyHostToDevice, stream),
+                     "upload");
+  if (rc || (rc = launch_mol_recip(*this, m, d_small + 1024, 0, d_small)))
+    return rc;
+  if ((rc = CudaCheck(cudaMemcpyAsync(h_pinned, d_small, 8,
+                                      cudaMemcpyDeviceToHost, stream),
+                      "download")) ||
+      (rc = Sync()))
+    return rc;
+  *de = h_pinned[0];
+  return OK;
+}
+
+int Box::SwapRecip(int m, const double *pos, bool insert, double *de) {
+  if (m < 0 || m >= dev.n_mol)
+    return Fail(ERR_ARG, "molecule index out of range");
+  if (!cfg.ewald) {
+    *de = 0;
+    return OK;
+  }
+  int n = host.mstart[m + 1] - host.mstart[m];
+  if (n > 64)
+    return Fail(ERR_UNSUPPORTED, "molecule larger than 64 atoms");
+  std::memcpy(h_pinned, pos, 3 * n * sizeof(double));
+  int rc = CudaCheck(cudaMemcpyAsync(d_small + 1024, h_pinned, 3 * n * 8,
+                                     cudaMemcpyHostToDevice, stream),
+                     "upload");
+  if (rc || (rc = launch_mol_recip(*this, m, d_small + 1024, insert ? 1 : 2,
+                                   d_small)))
+    return rc;
+  if ((rc = CudaCheck(cudaMemcpyAsync(h_pinned, d_small, 8,
+                                      cudaMemcpyDeviceToHost, stream),
+                      "download")) ||
+      (rc = Sync()))
+    return rc;
+  *de = h_pinned[0];
+  return OK;
+}
+
+int Box::UpdateRecip() {
+  // Ewald::UpdateRecip (src/Ewald.cpp:1420-1434): swap New and Ref
+  std::swap(dev.sumRnew, dev.sumRref);
+  std::swap(dev.sumInew, dev.sumIref);
+  return OK;
+}
+
+int Box::CopyRecip() {
+  if (!cfg.ewald)
+    return OK;
+  size_t bytes = (size_t)dev.K * 8;
+  int rc;
+  if ((rc = CudaCheck(cudaMemcpyAsync(dev.sumRnew, dev.sumRref, bytes,
+                                      cudaMemcpyDeviceToDevice, stream),
+                      "copy")) ||
+      (rc = CudaCheck(cudaMemcpyAsync(dev.sumInew, dev.sumIref, bytes,
+                                      cudaMemcpyDeviceToDevice, stream),
+                      "copy")))
+    return rc;
+  return OK;
+}
+
+int Box::BoxForce(double *inter, double *real, double *h_aF, double *h_mF) {
+  int rc = launch_box_force(*this, dev, d_aF, d_mF, d_small);
+  if (rc)
+    return rc;
+  if ((rc = CudaCheck(cudaMemcpyAsync(h_pinned, d_small, 16,
+                                      cudaMemcpyDeviceToHost, stream),
+                      "download")))
+    return rc;
+  if (h_aF && (rc = CudaCheck(cudaMemcpyAsync(h_aF, d_aF,
+                                              (size_t)dev.n_atoms * 24,
+                                              cudaMemcpyDeviceToHost, stream),
+                              "download")))
+    return rc;
+  if (h_mF && (rc = CudaCheck(cudaMemcpyAsync(h_mF, d_mF,
+                                              (size_t)dev.n_mol * 24,
+                                              cudaMemcpyDeviceToHost, stream),
+                              "download")))
+    return rc;
+  if ((rc = Sync()))
+    return rc;
+  *inter = h_pinned[0];
+  *real = h_pinned[1];
+  return CheckError();
+}
+
+int Box::BoxForceRecip(double *h_aR, double *h_mR) {
+  int rc = launch_force_recip(*this, dev, dev.sumRnew, dev.sumInew, d_aR, d_mR);
+  if (rc)
+    return rc;
+  if (h_aR && (rc = CudaCheck(cudaMemcpyAsync(h_aR, d_aR,
+                                              (size_t)dev.n_atoms * 24,
+                                              cudaMemcpyDeviceToHost, stream),
+                              "download")))
+    return rc;
+  if (h_mR && (rc = CudaCheck(cudaMemcpyAsync(h_mR, d_mR,
+                                              (size_t)dev.n_mol * 24,
+                                              cudaMemcpyDeviceToHost, stream),
+                              "download")))
+    return rc;
+  return Sync();
+}
+
+int Box::Torque(double *h_tq) {
+  int rc = launch_torque(*this, dev, d_aF, d_aR, d_tq);
+  if (rc)
+    return rc;
+  if (h_tq && (rc = CudaCheck(cudaMemcpyAsync(h_tq, d_tq,
+                                              (size_t)dev.n_mol * 24,
+                                              cudaMemcpyDeviceToHost, stream),
+                              "download")))
+    return rc;
+  return Sync();
+}
+
+int Box::GetCoords(double *xyz, double *com) {
+  int N = dev.n_atoms, M = dev.n_mol;
+  std::vector<double> t(3 * (size_t)std::max(N, M));
+  double *src[3] = {dev.x, dev.y, dev.z};
+  double *csrc[3] = {dev.cx, dev.cy, dev.cz};
+  int rc;
+  if (xyz) {
+    for (int d = 0; d < 3; ++d)
+      if ((rc = CudaCheck(cudaMemcpyAsync(t.data() + (size_t)d * N, src[d],
+                                          (size_t)N * 8, cudaMemcpyDeviceToHost,
+                                          stream),
+                          "download")))
+        return rc;
+    if ((rc = Sync()))
+      return rc;
+    for (int i = 0; i < N; ++i)
+      for (int d = 0; d < 3; ++d)
+        xyz[3 * i + d] = t[(size_t)d * N + i];
+  }
+  if (com) {
+    for (int d = 0; d < 3; ++d)
+      if ((rc = CudaCheck(cudaMemcpyAsync(t.data() + (size_t)d * M, csrc[d],
+                                          (size_t)M * 8, cudaMemcpyDeviceToHost,
+                                          stream),
+                          "download")))
+        return rc;
+    if ((rc = Sync()))
+      return rc;
+    for (int i = 0; i < M; ++i)
+      for (int d = 0; d < 3; ++d)
+        com[3 * i + d] = t[(size_t)d * M + i];
+  }
+  return OK;
+}
+
+int Box::SetCoords(const double *xyz, const double *com) {
+  int N = dev.n_atoms, M = dev.n_mol;
+  std::vector<double> t(3 * (size_t)std::max(N, M));
+  double *dst[3] = {dev.x, dev.y, dev.z};
+  double *cdst[3] = {dev.cx, dev.cy, dev.cz};
+  int rc;
+  for (int i = 0; i < N; ++i)
+    for (int d = 0; d < 3; ++d) {
+      double v = xyz[3 * i + d];
+      if (!(v >= 0.0 && v <= dev.L[d]))
+        return Fail(ERR_ARG, "coordinates must lie inside the box");
+      t[(size_t)d * N + i] = v;
+    }
+  for (int d = 0; d < 3; ++d)
+    if ((rc = CudaCheck(cudaMemcpyAsync(dst[d], t.data() + (size_t)d * N,
+                                        (size_t)N * 8, cudaMemcpyHostToDevice,
+                                        stream),
+                        "upload")))
+      return rc;
+  if ((rc = Sync()))
+    return rc;
+  if (com) {
+    for (int i = 0; i < M; ++i)
+      for (int d = 0; d < 3; ++d)
+        t[(size_t)d * M + i] = com[3 * i + d];
+    for (int d = 0; d < 3; ++d)
+      if ((rc = CudaCheck(cudaMemcpyAsync(cdst[d], t.data() + (size_t)d * M,
+                                          (size_t)M * 8, cudaMemcpyHostToDevice,
+                                          stream),
+                          "upload")))
+        return rc;
+    if ((rc = Sync()))
+      return rc;
+  }
+  return GridAll();
+}
+
+int Box::GetCells(int *cell_of_atom, int edge[3]) {
+  int rc = CudaCheck(cudaMemcpyAsync(cell_of_atom, dev.atom_cell,
+                                     (size_t)dev.n_atoms * 4,
+                                     cudaMemcpyDeviceToHost, stream),
+                     "download");
+  if (rc || (rc = Sync()))
+    return rc;
+  for (int k = 0; k < 3; ++k)
+    edge[k] = dev.edge[k];
+  return OK;
+}
+
+int Box::GetKVectors(double *o) {
+  if (!cfg.ewald)
+    return OK;
+  size_t K = dev.K;
+  double *src[7] = {dev.kx, dev.ky, dev.kz, dev.prefact, dev.hsqr,
+                    dev.sumRref, dev.sumIref};
+  for (int i = 0; i < 7; ++i) {
+    int rc = CudaCheck(cudaMemcpyAsync(o + i * K, src[i], K * 8,
+                                       cudaMemcpyDeviceToHost, stream),
+                       "download");
+    if (rc)
+      return rc;
+  }
+  return Sync();
+}
+
+int Box::GetSumNew(double *sr, double *si) {
+  if (!cfg.ewald)
+    return OK;
+  size_t K = dev.K;
+  int rc;
+  if ((rc = CudaCheck(cudaMemcpyAsync(sr, dev.sumRnew, K * 8,
+                                      cudaMemcpyDeviceToHost, stream),
+                      "download")) ||
+      (rc = CudaCheck(cudaMemcpyAsync(si, dev.sumInew, K * 8,
+                                      cudaMemcpyDeviceToHost, stream),
+                      "download")))
+    return rc;
+  return Sync();
+}
+
+}  // namespace gb

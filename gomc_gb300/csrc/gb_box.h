@@ -1,0 +1,127 @@
+// gb_box: one simulation box resident on one GPU, and the host-side set-up
+// that mirrors System::Init (src/System.cpp:67-100).
+#pragma once
+
+#include "gb_internal.h"
+
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace gb {
+
+struct McState;  // Monte Carlo loop state (gb_mc.cu)
+
+struct BoxConfig {
+  double temperature = 298.0;
+  double rcut = 9.0, rcut_low = 0.0, rcut_coulomb = 9.0, tolerance = 1e-5;
+  int ewald = 1, electrostatic = 1;
+  int precision = 0;  // 0 = FP64 plain form, 1 = mixed
+  int device = 0;
+};
+
+class Box {
+ public:
+  ~Box();
+  static int Create(const HostSystem &sys, const BoxConfig &cfg, Box **out,
+                    std::string *err);
+
+  // ---- energy path (all run on `stream`) ----
+  int GridAll();                                 // CellList::GridAll
+  int BoxInter(double *inter, double *real);     // CalculateEnergy::BoxInter
+  int RecipSetup();                              // Ewald::BoxReciprocalSetup
+  int RecipSums(const double *d_x, const double *d_y, const double *d_z);
+  int RecipEnergy(double *e, bool ref_sums);     // Ewald::BoxReciprocal
+  int SystemTotal(double out9[9]);               // CalculateEnergy::SystemTotal
+  int MoleculeInter(int m, const double *new_pos, double *lj, double *real,
+                    int *overlap);
+  int ParticleInter(int m, int kind, double charge, const double *trials,
+                    int ntrials, double *en, double *real, int *overlap);
+  int MolReciprocal(int m, const double *new_pos, double *de);
+  int SwapRecip(int m, const double *pos, bool insert, double *de);
+  int UpdateRecip();
+  int CopyRecip();
+  int BoxSelf(double *e);
+  int MolCorrection(int m, double *e);
+  int BoxCorrection(double *e);
+  int BoxForce(double *inter, double *real, double *h_aF, double *h_mF);
+  int BoxForceRecip(double *h_aR, double *h_mR);
+  int Torque(double *h_tq);
+
+  // ---- state transfer ----
+  int GetCoords(double *xyz, double *com);
+  int SetCoords(const double *xyz, const double *com);
+  int GetEnergy(double e5[5]);
+  int SetEnergy(const double e5[5]);
+  int GetCells(int *cell_of_atom, int edge[3]);
+  int GetKVectors(double *out7);
+  int GetSumNew(double *sr, double *si);
+  int CheckError();
+
+  // ---- internals shared with the Monte Carlo loop ----
+  DevBox dev{};
+  FF ff{};
+  FF *d_ff = nullptr;
+  BoxConfig cfg;
+  HostSystem host;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int sm_count = 0;
+  std::string last_error;
+  McState *mc = nullptr;
+
+  // scratch buffers
+  double *d_scratch = nullptr;   // reduction partials
+  size_t scratch_len = 0;
+  double *h_pinned = nullptr;    // small pinned staging
+  double *d_small = nullptr;     // small device staging (positions, results)
+  // force buffers: atom/molecule forces, reciprocal forces, torque
+  double *d_aF = nullptr, *d_mF = nullptr, *d_aR = nullptr, *d_mR = nullptr,
+         *d_tq = nullptr;
+
+  int Fail(int code, const std::string &msg);
+  int CudaCheck(cudaError_t e, const char *what);
+  int EnsureScratch(size_t n);
+  int Sync();
+
+ private:
+  Box() = default;
+  int Init(const HostSystem &sys, const BoxConfig &cfg);
+  void FreeAll();
+  std::vector<void *> allocs_;
+  template <class T>
+  int Alloc(T **p, size_t n);
+};
+
+// host helpers (gb_box.cu)
+void build_ff(const HostSystem &s, const BoxConfig &c, FF *ff);
+void recip_vectors(const double L[3], double volume, double alphaSq,
+                   double recip_rcutSq, double recip_rcut,
+                   std::vector<double> &kx, std::vector<double> &ky,
+                   std::vector<double> &kz, std::vector<double> &hsqr,
+                   std::vector<double> &prefact, std::vector<char4> &kn,
+                   int *kmax);
+
+// kernel launchers (gb_cells.cu / gb_real.cu / gb_recip.cu).  Launchers
+// that take a DevBox run on that view (coordinates and cell grid), which lets
+// the MultiParticle move evaluate its trial state in separate buffers.
+int launch_grid_all(Box &b, const DevBox &d);
+int launch_box_inter(Box &b, double *d_out2);
+int launch_recip_sums(Box &b, const double *x, const double *y,
+                      const double *z, double *sumR, double *sumI);
+int launch_recip_energy(Box &b, const double *sumR, const double *sumI,
+                        double *d_out);
+int launch_mol_recip(Box &b, int m, const double *d_newpos, int sign_mode,
+                     double *d_out);
+int launch_mol_inter(Box &b, int m, const double *d_newpos, double *d_out3);
+int launch_particle_inter(Box &b, int m, int kind, double charge,
+                          const double *d_trials, int ntrials, double *d_out);
+int launch_correction(Box &b, double *d_out);
+int launch_box_force(Box &b, const DevBox &d, double *aF, double *mF,
+                     double *d_out2);
+int launch_force_recip(Box &b, const DevBox &d, const double *sumR,
+                       const double *sumI, double *aR, double *mR);
+int launch_torque(Box &b, const DevBox &d, const double *aF, const double *aR,
+                  double *tq);
+
+}  // namespace gb

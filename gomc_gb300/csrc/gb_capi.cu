@@ -1,0 +1,274 @@
+// extern "C" entry points (include/gomc_gb300.h) over gb::Box.
+#include "gomc_gb300.h"
+#include "gb_box.h"
+#include "gb_mc.h"
+
+#include <cstring>
+#include <string>
+
+struct gb_box {
+  gb::Box *b;
+};
+
+namespace {
+thread_local std::string g_create_error;
+
+int guard(gb_box *box) {
+  if (!box || !box->b)
+    return gb::ERR_ARG;
+  return gb::OK;
+}
+}  // namespace
+
+extern "C" {
+
+const char *gb_version(void) { return "gomc_gb300 0.1 (sm_103a)"; }
+
+const char *gb_last_error(const gb_box *box) {
+  if (!box || !box->b)
+    return g_create_error.c_str();
+  return box->b->last_error.c_str();
+}
+
+int gb_box_create(const gb_system_desc *sys, const gb_config *cfg,
+                  gb_box **out) {
+  if (!sys || !cfg || !out || !sys->pos || !sys->atom_kind ||
+      !sys->atom_charge || !sys->mol_start || !sys->kind_epsilon ||
+      !sys->kind_sigma || !sys->kind_n) {
+    g_create_error = "null argument";
+    return gb::ERR_ARG;
+  }
+  if (sys->n_atoms <= 0 || sys->n_mol <= 0 || sys->n_kinds <= 0) {
+    g_create_error = "empty system";
+    return gb::ERR_ARG;
+  }
+  gb::HostSystem h;
+  h.n_atoms = sys->n_atoms;
+  h.n_mol = sys->n_mol;
+  h.n_kinds = sys->n_kinds;
+  h.x.resize(h.n_atoms);
+  h.y.resize(h.n_atoms);
+  h.z.resize(h.n_atoms);
+  h.q.assign(sys->atom_charge, sys->atom_charge + h.n_atoms);
+  h.kind.assign(sys->atom_kind, sys->atom_kind + h.n_atoms);
+  h.mstart.assign(sys->mol_start, sys->mol_start + h.n_mol + 1);
+  h.eps.assign(sys->kind_epsilon, sys->kind_epsilon + h.n_kinds);
+  h.sigma.assign(sys->kind_sigma, sys->kind_sigma + h.n_kinds);
+  h.nexp.assign(sys->kind_n, sys->kind_n + h.n_kinds);
+  for (int i = 0; i < h.n_atoms; ++i) {
+    h.x[i] = sys->pos[3 * i];
+    h.y[i] = sys->pos[3 * i + 1];
+    h.z[i] = sys->pos[3 * i + 2];
+  }
+  for (int d = 0; d < 3; ++d)
+    h.L[d] = sys->box[d];
+  gb::BoxConfig c;
+  c.temperature = cfg->temperature;
+  c.rcut = cfg->rcut;
+  c.rcut_low = cfg->rcut_low;
+  c.rcut_coulomb = cfg->rcut_coulomb > 0 ? cfg->rcut_coulomb : cfg->rcut;
+  c.tolerance = cfg->tolerance;
+  c.ewald = cfg->ewald ? 1 : 0;
+  c.electrostatic = cfg->electrostatic ? 1 : 0;
+  c.precision = cfg->precision;
+  c.device = cfg->device;
+  if (c.precision != GB_FP64 && c.precision != GB_MIXED) {
+    g_create_error = "precision must be GB_FP64 or GB_MIXED";
+    return gb::ERR_ARG;
+  }
+  gb::Box *b = nullptr;
+  std::string err;
+  int rc = gb::Box::Create(h, c, &b, &err);
+  if (rc) {
+    g_create_error = err;
+    return rc;
+  }
+  *out = new gb_box{b};
+  return gb::OK;
+}
+
+void gb_box_destroy(gb_box *box) {
+  if (!box)
+    return;
+  gb::mc_destroy(*box->b);
+  delete box->b;
+  delete box;
+}
+
+#define BOX_CALL(expr)          \
+  do {                          \
+    int rc_ = guard(box);       \
+    if (rc_)                    \
+      return rc_;               \
+    return box->b->expr;        \
+  } while (0)
+
+int gb_system_total(gb_box *box, double *out9) {
+  if (!out9)
+    return gb::ERR_ARG;
+  BOX_CALL(SystemTotal(out9));
+}
+int gb_box_inter(gb_box *box, double *inter, double *real) {
+  if (!inter || !real)
+    return gb::ERR_ARG;
+  BOX_CALL(BoxInter(inter, real));
+}
+int gb_molecule_inter(gb_box *box, int32_t mol, const double *new_pos,
+                      double *lj, double *real, int32_t *overlap) {
+  if (!new_pos || !lj || !real || !overlap)
+    return gb::ERR_ARG;
+  int ov = 0;
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  rc = box->b->MoleculeInter(mol, new_pos, lj, real, &ov);
+  *overlap = ov;
+  return rc;
+}
+int gb_particle_inter(gb_box *box, int32_t mol, int32_t kind, double charge,
+                      const double *trials, int32_t ntrials, double *en,
+                      double *real, int32_t *overlap) {
+  if (!trials || !en || !real || !overlap)
+    return gb::ERR_ARG;
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  std::vector<int> ov(ntrials > 0 ? ntrials : 1, 0);
+  rc = box->b->ParticleInter(mol, kind, charge, trials, ntrials, en, real,
+                             ov.data());
+  for (int t = 0; t < ntrials && !rc; ++t)
+    overlap[t] = ov[t];
+  return rc;
+}
+int gb_box_force(gb_box *box, double *inter, double *real, double *atom_force,
+                 double *mol_force) {
+  if (!inter || !real)
+    return gb::ERR_ARG;
+  BOX_CALL(BoxForce(inter, real, atom_force, mol_force));
+}
+int gb_calculate_torque(gb_box *box, double *mol_torque) {
+  BOX_CALL(Torque(mol_torque));
+}
+int gb_num_kvectors(gb_box *box, int32_t *k_count, int32_t *kmax) {
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  if (k_count)
+    *k_count = box->b->cfg.ewald ? box->b->dev.K : 0;
+  if (kmax)
+    *kmax = box->b->cfg.ewald ? box->b->dev.kmax : 0;
+  return gb::OK;
+}
+int gb_get_kvectors(gb_box *box, double *out7) {
+  if (!out7)
+    return gb::ERR_ARG;
+  BOX_CALL(GetKVectors(out7));
+}
+int gb_get_sums_new(gb_box *box, double *sum_r, double *sum_i) {
+  if (!sum_r || !sum_i)
+    return gb::ERR_ARG;
+  BOX_CALL(GetSumNew(sum_r, sum_i));
+}
+int gb_box_reciprocal_setup(gb_box *box) { BOX_CALL(RecipSetup()); }
+int gb_box_reciprocal_sums(gb_box *box) {
+  BOX_CALL(RecipSums(box->b->dev.x, box->b->dev.y, box->b->dev.z));
+}
+int gb_box_reciprocal(gb_box *box, int32_t use_ref, double *energy) {
+  if (!energy)
+    return gb::ERR_ARG;
+  BOX_CALL(RecipEnergy(energy, use_ref != 0));
+}
+int gb_mol_reciprocal(gb_box *box, int32_t mol, const double *new_pos,
+                      double *delta) {
+  if (!new_pos || !delta)
+    return gb::ERR_ARG;
+  BOX_CALL(MolReciprocal(mol, new_pos, delta));
+}
+int gb_swap_dest_recip(gb_box *box, int32_t mol, const double *pos,
+                       double *delta) {
+  if (!pos || !delta)
+    return gb::ERR_ARG;
+  BOX_CALL(SwapRecip(mol, pos, true, delta));
+}
+int gb_swap_source_recip(gb_box *box, int32_t mol, const double *pos,
+                         double *delta) {
+  if (!pos || !delta)
+    return gb::ERR_ARG;
+  BOX_CALL(SwapRecip(mol, pos, false, delta));
+}
+int gb_update_recip(gb_box *box) { BOX_CALL(UpdateRecip()); }
+int gb_copy_recip(gb_box *box) { BOX_CALL(CopyRecip()); }
+int gb_box_self(gb_box *box, double *self) {
+  if (!self)
+    return gb::ERR_ARG;
+  BOX_CALL(BoxSelf(self));
+}
+int gb_mol_correction(gb_box *box, int32_t mol, double *corr) {
+  if (!corr)
+    return gb::ERR_ARG;
+  BOX_CALL(MolCorrection(mol, corr));
+}
+int gb_box_force_reciprocal(gb_box *box, double *atom_force_rec,
+                            double *mol_force_rec) {
+  BOX_CALL(BoxForceRecip(atom_force_rec, mol_force_rec));
+}
+int gb_grid_all(gb_box *box) { BOX_CALL(GridAll()); }
+int gb_cell_membership(gb_box *box, int32_t *cell_of_atom, int32_t *edge3) {
+  if (!cell_of_atom || !edge3)
+    return gb::ERR_ARG;
+  BOX_CALL(GetCells(cell_of_atom, edge3));
+}
+int gb_get_coords(gb_box *box, double *xyz, double *com) {
+  BOX_CALL(GetCoords(xyz, com));
+}
+int gb_set_coords(gb_box *box, const double *xyz, const double *com) {
+  if (!xyz)
+    return gb::ERR_ARG;
+  BOX_CALL(SetCoords(xyz, com));
+}
+int gb_get_energy(gb_box *box, double *e5) {
+  if (!e5)
+    return gb::ERR_ARG;
+  BOX_CALL(GetEnergy(e5));
+}
+int gb_set_energy(gb_box *box, const double *e5) {
+  if (!e5)
+    return gb::ERR_ARG;
+  BOX_CALL(SetEnergy(e5));
+}
+
+int gb_mc_init(gb_box *box, const gb_mc_params *p) {
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  if (!p)
+    return gb::ERR_ARG;
+  return gb::mc_init(*box->b, *p);
+}
+int gb_mc_run(gb_box *box, int64_t first_step, int64_t nsteps, int32_t *kind,
+              int32_t *mol, int32_t *accepted, double *de) {
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  return gb::mc_run(*box->b, first_step, nsteps, kind, mol, accepted, de);
+}
+int gb_mc_state(gb_box *box, double *scales4, int64_t *counts6) {
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  return gb::mc_state(*box->b, scales4, counts6);
+}
+int gb_mc_run_batch(gb_box **boxes, int32_t nboxes, int64_t first_step,
+                    int64_t nsteps) {
+  if (!boxes || nboxes <= 0)
+    return gb::ERR_ARG;
+  std::vector<gb::Box *> v;
+  for (int i = 0; i < nboxes; ++i) {
+    if (!boxes[i] || !boxes[i]->b)
+      return gb::ERR_ARG;
+    v.push_back(boxes[i]->b);
+  }
+  return gb::mc_run_batch(v, first_step, nsteps);
+}
+
+}  // extern "C"

@@ -1,0 +1,172 @@
+// Internal definitions of the GB300 Monte Carlo energy engine.
+//
+// One gb_box holds one orthogonal periodic box resident in HBM: FP64 master
+// coordinates, per-atom charge / kind / molecule, a padded cell grid in
+// cell-ordered SoA form, the Ewald k-vector tables and structure factors, and
+// the running box energies.  All kernels of the engine see it through the
+// plain-pointer view DevBox.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+namespace gb {
+
+constexpr double QQ_FACT = 167103.208067979;  // lib/NumLib.h:22
+constexpr int NB27 = 27;
+constexpr int MAX_KINDS = 8;
+constexpr int MAX_MOL_ATOMS = 8;   // rigid molecules handled by the move loop
+constexpr int END_CELL = -1;
+
+// Status codes of the C ABI (include/gomc_gb300.h).
+enum Status : int {
+  OK = 0,
+  ERR_ARG = 1,
+  ERR_CUDA = 2,
+  ERR_NOMEM = 3,
+  ERR_CAPACITY = 4,
+  ERR_TIMEOUT = 5,
+  ERR_STATE = 6,
+  ERR_UNSUPPORTED = 7,
+};
+
+// Device error word bits (DevBox::err).
+enum DevErr : int {
+  DERR_CELL_OVERFLOW = 1,
+  DERR_BARRIER_TIMEOUT = 2,
+  DERR_BAD_INPUT = 4,
+};
+
+// Force-field constants, FlatIndex(i, j) = i + j * n_kinds
+// (src/FFParticle.h:116) and Forcefield::InitBasicVals
+// (src/Forcefield.cpp:37-83).
+struct FF {
+  int n_kinds;
+  int ewald, electrostatic;
+  double rcut, rcutSq, rcutLowSq, rcutCoulSq;
+  double alpha, alphaSq, recip_rcut, recip_rcutSq, beta;
+  double sigmaSq[MAX_KINDS * MAX_KINDS];
+  double eps_cn[MAX_KINDS * MAX_KINDS];
+  double nexp[MAX_KINDS * MAX_KINDS];
+  double eps_cn_6[MAX_KINDS * MAX_KINDS];
+  double nOver6[MAX_KINDS * MAX_KINDS];
+  // FP32 copies for the mixed form
+  float sigmaSq_f[MAX_KINDS * MAX_KINDS];
+  float eps_cn_f[MAX_KINDS * MAX_KINDS];
+};
+
+// Plain-pointer view of one box, passed by value to kernels.
+struct DevBox {
+  double L[3], half[3];
+  double volume;
+  int n_atoms, n_mol;
+  // atoms, indexed by atom id
+  double *x, *y, *z;
+  double *cx, *cy, *cz;  // molecule centres (COM::CalcCOM)
+  double *q;
+  int *kind, *mol, *mstart;
+  // cell grid: `cap` padded slots per cell, SoA by slot
+  int edge[3];
+  double cellSize[3];
+  int ncell, cap;
+  int *nbr;          // [ncell * 27], src/CellList.cpp:191-218 order
+  int *cell_count;   // [ncell]
+  int *cell_atom;    // [ncell * cap]
+  double4_32a *cell_pos; // [ncell * cap] x, y, z, q
+  int *cell_meta;    // [ncell * cap] (mol << 4) | kind
+  uint4 *cell_fix;   // [ncell * cap] fixed-point turns x, y, z; q as float bits
+  int *atom_cell, *atom_slot;  // [n_atoms]
+  // Ewald
+  int K, kmax;
+  double *kx, *ky, *kz, *prefact, *hsqr;  // [K]
+  char4 *kn;                              // [K] integer k indices
+  float *prefact_f;                       // [K]
+  double *sumRref, *sumIref, *sumRnew, *sumInew;  // [K]
+  // running energies: inter, real, recip, self, correction
+  double *energy;
+  int *err;
+};
+
+// ---------------------------------------------------------------------------
+// Host-side description of a box (owned by gb_box).
+// ---------------------------------------------------------------------------
+struct HostSystem {
+  int n_atoms = 0, n_mol = 0, n_kinds = 0;
+  std::vector<double> x, y, z, cx, cy, cz, q;
+  std::vector<int> kind, mol, mstart;
+  std::vector<double> eps, sigma, nexp;
+  double L[3] = {0, 0, 0};
+};
+
+// ---------------------------------------------------------------------------
+// Device math shared by the kernels
+// ---------------------------------------------------------------------------
+#ifdef __CUDACC__
+#define GB_HD __host__ __device__ __forceinline__
+#else
+#define GB_HD inline
+#endif
+
+// BoxDimensions::MinImageSigned, src/BoxDimensions.h:169-175
+GB_HD double min_image(double raw, double ax, double half) {
+  if (raw > half)
+    raw -= ax;
+  else if (raw < -half)
+    raw += ax;
+  return raw;
+}
+// BoxDimensions::WrapPBC(double&, double), src/BoxDimensions.cpp:283-313
+GB_HD double wrap1(double v, double ax) {
+  if (v >= ax)
+    v -= ax;
+  else if (v < 0)
+    v += ax;
+  return v;
+}
+// BoxDimensions::UnwrapPBC(double&, ...), src/BoxDimensions.cpp:315-339
+GB_HD double unwrap1(double v, double ref, double ax, double half) {
+  if (fabs(ref - v) > half) {
+    if (ref < half)
+      v -= ax;
+    else
+      v += ax;
+  }
+  return v;
+}
+
+#ifdef __CUDACC__
+// Products and sums without contraction so that FP64 distances round the way
+// the reference's host build rounds them.
+__device__ __forceinline__ double dsq3(double dx, double dy, double dz) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                   __dmul_rn(dz, dz));
+}
+#endif
+
+// CellList::PositionToCell, src/CellList.h:88-101
+GB_HD int position_to_cell(const DevBox &b, double px, double py, double pz) {
+  int x = (int)(px / b.cellSize[0]);
+  int y = (int)(py / b.cellSize[1]);
+  int z = (int)(pz / b.cellSize[2]);
+  x -= (x == b.edge[0] ? 1 : 0);
+  y -= (y == b.edge[1] ? 1 : 0);
+  z -= (z == b.edge[2] ? 1 : 0);
+  return x * b.edge[1] * b.edge[2] + y * b.edge[2] + z;
+}
+
+// Fixed-point fraction of the box edge: round(v / L * 2^32) mod 2^32.
+GB_HD uint32_t to_turns(double v, double L) {
+  double t = v / L;
+  t -= floor(t);
+  double s = t * 4294967296.0;
+  unsigned long long u = (unsigned long long)(s + 0.5);
+  return (uint32_t)(u & 0xffffffffULL);
+}
+
+}  // namespace gb
+
+// The opaque handle of the C ABI.
+struct gb_box;

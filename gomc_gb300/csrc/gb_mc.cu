@@ -1,0 +1,1351 @@
+// Device-resident Monte Carlo loop (FP64 plain form).
+//
+// Host: an MT19937 stream (the reference's PRNG, src/PRNG.h,
+// src/MersenneTwister.h) pre-draws every number that does not depend on the
+// accept history -- move kind, molecule, displacement and angle draws, the
+// rotation axis and the Metropolis uniform -- into MoveRec records.
+//
+// Device: a persistent cooperative "chain" kernel runs a segment of
+// displacement / rotation moves.  Every CTA owns a fixed chunk of k-vectors
+// whose Ref and New structure factors live in its shared memory for the whole
+// segment, plus a share of the (atom, old/new, neighbour cell) real-space
+// units.  Per move:
+//   phase A  all CTAs: real-space and reciprocal partials -> global slots
+//   barrier
+//   phase B  all CTAs: add the partials in one fixed order (identical in every
+//            CTA), take the same Metropolis decision, commit their own k-chunk;
+//            CTA 0 commits coordinates and the cell grid; designated CTAs
+//            build the next move's phase tables
+//   barrier
+// Move-size adjustment (MoveSettings::AdjustMoves) is replayed identically in
+// every CTA.  Barriers spin a bounded number of times and then raise an error
+// flag that the host turns into GB_ERR_TIMEOUT.
+//
+// MultiParticle moves run as a kernel sequence between chain segments
+// (src/moves/MultiParticle.h:164-544), with Philox4x64-10 keyed
+// (step, seed) as in Random123Wrapper (src/Random123Wrapper.cpp:16-84).
+#include "gb_mc.h"
+#include "gb_cells.cuh"
+#include "gb_pair.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace gb {
+
+// ===========================================================================
+// Host: MT19937 and the move stream
+// ===========================================================================
+MT19937::MT19937(uint32_t seed) {
+  st_[0] = seed;
+  for (int i = 1; i < 624; ++i)
+    st_[i] = 1812433253u * (st_[i - 1] ^ (st_[i - 1] >> 30)) + (uint32_t)i;
+  reload();
+}
+
+void MT19937::reload() {
+  for (int i = 0; i < 624; ++i) {
+    uint32_t nx = st_[(i + 1) % 624];
+    uint32_t y = (st_[i] & 0x80000000u) | (nx & 0x7fffffffu);
+    st_[i] = st_[(i + 397) % 624] ^ (y >> 1) ^ ((nx & 1u) ? 0x9908b0dfu : 0u);
+  }
+  left_ = 624;
+  next_ = 0;
+}
+
+uint32_t MT19937::u32() {
+  if (left_ == 0)
+    reload();
+  --left_;
+  uint32_t y = st_[next_++];
+  y ^= (y >> 11);
+  y ^= (y << 7) & 0x9d2c5680u;
+  y ^= (y << 15) & 0xefc60000u;
+  return y ^ (y >> 18);
+}
+
+uint32_t MT19937::randInt(uint32_t n) {
+  uint32_t used = n;
+  used |= used >> 1;
+  used |= used >> 2;
+  used |= used >> 4;
+  used |= used >> 8;
+  used |= used >> 16;
+  uint32_t i;
+  do
+    i = u32() & used;
+  while (i > n);
+  return i;
+}
+
+MoveStream::MoveStream(uint32_t seed, const double frac[3], int n_mol,
+                       const std::vector<int> &mol_len)
+    : mt_(seed), n_mol_(n_mol), mol_len_(mol_len) {
+  // StaticVals normalises movePerc over the nine NVT move kinds
+  // (src/StaticVals.cpp:37-96, src/MoveConst.h:22-33).
+  double tot = 0.0;
+  double raw[9] = {frac[0], frac[1], frac[2], 0, 0, 0, 0, 0, 0};
+  for (int i = 0; i < 9; ++i)
+    tot += raw[i];
+  for (int i = 0; i < 9; ++i)
+    perc_[i] = raw[i] / tot;
+  all_single_ = true;
+  for (int l : mol_len)
+    if (l != 1)
+      all_single_ = false;
+}
+
+void MoveStream::Next(MoveRec *r) {
+  std::memset(r, 0, sizeof(MoveRec));
+  // PRNG::PickArbDist (src/PRNG.h:153-163) with Wt = 1
+  double sum = 0.0, draw = mt_.rand01() * 1.0;
+  int pick;
+  for (pick = 0; pick < 9 && sum < draw; ++pick)
+    sum += perc_[pick];
+  if (pick != 0)
+    --pick;
+  if (pick > 2 || perc_[pick] == 0.0) {
+    // only reachable by rounding at draw ~ 1: the last kind with weight
+    pick = perc_[2] > 0 ? 2 : (perc_[1] > 0 ? 1 : 0);
+  }
+  if (pick == 2) {
+    // MultiParticle::Prep: randIntExc(MPTOTALTYPES) unless all molecules
+    // are single sites (src/moves/MultiParticle.h:178-183)
+    r->kind = 2;
+    r->mol = all_single_ ? 0 : (int)mt_.randInt(1);
+    return;
+  }
+  // PRNG::PickMolAndBox, one box and one movable kind: randIntExc(count)
+  uint32_t m = mt_.randInt((uint32_t)(n_mol_ - 1));
+  r->mol = (int)m;
+  if (pick == 1 && mol_len_[m] <= 1)
+    pick = 0;  // ROTATE_ON_SINGLE_ATOM -> displacement (src/System.cpp:291-297)
+  r->kind = pick;
+  if (pick == 0) {
+    // Coordinates::TranslateRand -> PRNG::SymXYZ (src/PRNG.h:69-75)
+    r->u[0] = mt_.rand01();
+    r->u[1] = mt_.rand01();
+    r->u[2] = mt_.rand01();
+  } else {
+    // Coordinates::RotateRand: Sym(max), then PickOnUnitSphere
+    r->u[0] = mt_.rand01();
+    double u = mt_.rand01() * 2.0 - 1.0;
+    double theta = mt_.randExc01() * (2.0 * M_PI);
+    double rootTerm = std::sqrt(1.0 - u * u);
+    r->ax[0] = rootTerm * std::cos(theta);
+    r->ax[1] = rootTerm * std::sin(theta);
+    r->ax[2] = u;
+  }
+  r->pacc = mt_.rand01();  // Translate/Rotate::Accept prng()
+}
+
+// ===========================================================================
+// Move settings, identical on host and device
+// ===========================================================================
+GB_HD double bound_d(double v, double lo, double hi) {
+  return v < lo ? lo : (v > hi ? hi : v);
+}
+
+// MoveSettings::AdjustMoves / Adjust / AdjustMultiParticle
+// (src/MoveSettings.cpp:157-265), called at the start of every step.
+GB_HD void settings_adjust(Settings &s, long long step) {
+  if ((step + 1) % s.adj != 0)
+    return;
+  for (int mv = 0; mv < 3; ++mv) {
+    if (mv < 2) {
+      if (s.tempTries[mv] > 0) {
+        double currentAccept =
+            (double)s.tempAccepted[mv] / (double)s.tempTries[mv];
+        double fract = currentAccept / 0.5;
+        if (fract > 0.0)
+          s.scale[mv] *= fract;
+        else
+          s.scale[mv] *= 0.5;
+      }
+      if (mv == 0)
+        s.scale[0] = bound_d(s.scale[0], 1.0e-10, (s.amin * 0.5) - 1.0e-7);
+      else
+        s.scale[1] = bound_d(s.scale[1], 1.0e-6, M_PI - 1.0e-7);
+    }
+    s.tempTries[mv] = 0;
+    s.tempAccepted[mv] = 0;
+  }
+  for (int t = 0; t < 2; ++t) {
+    if (s.mp_itries[t] > 0) {
+      s.mp_tries[t] += s.mp_itries[t];
+      s.mp_acc[t] += s.mp_iacc[t];
+      double fTot = ((double)s.mp_acc[t] / (double)s.mp_tries[t]) / 0.3;
+      double fInt = ((double)s.mp_iacc[t] / (double)s.mp_itries[t]) / 0.3;
+      double &mx = (t == 0) ? s.mp_t_max : s.mp_r_max;
+      if (fInt == 0.0)
+        mx *= 0.5;
+      else if (fabs(fInt - 0.3) > 0.1)
+        mx *= ((1.0 - 0.2) * fTot + 0.2 * fInt);
+      if (t == 0)
+        mx = bound_d(mx, 0.001, (s.amin * 0.5) - 0.001);
+      else
+        mx = bound_d(mx, 0.001, M_PI - 0.001);
+      s.mp_iacc[t] = 0;
+      s.mp_itries[t] = 0;
+    }
+  }
+}
+
+// MoveSettings::Update (src/MoveSettings.cpp:100-155), one molecule kind
+GB_HD void settings_update(Settings &s, int mv, int accepted) {
+  s.tries[mv]++;
+  s.tempTries[mv]++;
+  if (accepted) {
+    s.tempAccepted[mv]++;
+    s.accepted[mv]++;
+    s.singleMoveAccepted = 1;
+  }
+  if (mv == 2)
+    s.singleMoveAccepted = 0;
+}
+
+// ===========================================================================
+// Device helpers
+// ===========================================================================
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+constexpr unsigned SPIN_LIMIT = 1u << 22;
+
+// Grid-wide barrier with a bounded wait.  bar[0] counts arrivals, bar[1] is
+// the generation.  Returns false (and sets DERR_BARRIER_TIMEOUT) when the
+// wait gives up or another CTA reported an error.
+__device__ bool grid_sync(unsigned *bar, unsigned nblocks, unsigned &gen,
+                          int *err, int *s_flag) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    unsigned g = gen;
+    __threadfence();
+    unsigned prev = atomicAdd(&bar[0], 1u);
+    if (prev == nblocks - 1) {
+      bar[0] = 0;
+      __threadfence();
+      atomicExch(&bar[1], g + 1);
+    } else {
+      unsigned it = 0;
+      while (ld_acquire(&bar[1]) == g) {
+        if (++it > SPIN_LIMIT) {
+          atomicOr(err, DERR_BARRIER_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        if ((it & 255u) == 0 && *(volatile int *)err) {
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    gen = g + 1;
+    *s_flag = ok && (*(volatile int *)err == 0);
+  }
+  __syncthreads();
+  return *s_flag != 0;
+}
+
+// Rotation matrix from an angle and a unit axis
+// (RotationMatrix::FromAxisAngle, src/TransformMatrix.h:165-214).
+__device__ __forceinline__ void axis_angle_matrix(double theta, const double *u,
+                                                  double *r) {
+  double c = cos(theta);
+  double s = sin(theta);
+  double cross[9] = {0.0, -(u[2]), u[1], u[2], 0.0, -(u[0]), -(u[1]), u[0], 0.0};
+  double omc = 1 - c;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double t = __dmul_rn(u[i], u[j]);
+      double add = __dadd_rn(__dmul_rn(s, cross[3 * i + j]), __dmul_rn(omc, t));
+      r[3 * i + j] = __dadd_rn(i == j ? c : 0.0, add);
+    }
+}
+
+// Apply a stored proposal to the atoms of molecule m.
+// kind 0: shift (Coordinates::TranslateRand, src/Coordinates.cpp:83-100)
+// kind 1: rotation about the molecule centre (RotateRand, :103-128)
+__device__ __forceinline__ void apply_proposal(const DevBox &b, int kind,
+                                               const double *prop, int na,
+                                               const double (*oldp)[3],
+                                               const double *com,
+                                               double (*newp)[3],
+                                               double *newcom) {
+  if (kind == 0) {
+    for (int a = 0; a < na; ++a)
+      for (int d = 0; d < 3; ++d)
+        newp[a][d] = wrap1(__dadd_rn(oldp[a][d], prop[d]), b.L[d]);
+    for (int d = 0; d < 3; ++d)
+      newcom[d] = wrap1(__dadd_rn(com[d], prop[d]), b.L[d]);
+  } else {
+    for (int a = 0; a < na; ++a) {
+      double v[3];
+      for (int d = 0; d < 3; ++d) {
+        v[d] = unwrap1(oldp[a][d], com[d], b.L[d], b.half[d]);
+        v[d] = __dadd_rn(v[d], -com[d]);
+      }
+      for (int i = 0; i < 3; ++i) {
+        double w = __dadd_rn(__dadd_rn(__dmul_rn(prop[3 * i], v[0]),
+                                       __dmul_rn(prop[3 * i + 1], v[1])),
+                             __dmul_rn(prop[3 * i + 2], v[2]));
+        newp[a][i] = wrap1(__dadd_rn(w, com[i]), b.L[i]);
+      }
+    }
+    for (int d = 0; d < 3; ++d)
+      newcom[d] = com[d];
+  }
+}
+
+// Proposal of one move for the current scales: shift (3) or matrix (9).
+__device__ __forceinline__ void make_proposal(const MoveRec &r,
+                                              const Settings &s, double *prop) {
+  if (r.kind == 0) {
+    double bnd = s.scale[0];
+    double b2 = 2.0 * bnd;
+    for (int d = 0; d < 3; ++d)
+      prop[d] = __dadd_rn(__dmul_rn(r.u[d], b2), -bnd);
+  } else if (r.kind == 1) {
+    double mx = s.scale[1];
+    double theta = __dadd_rn(__dmul_rn(r.u[0], 2.0 * mx), -mx);
+    axis_angle_matrix(theta, r.ax, prop);
+  }
+}
+
+__device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 tab_at(const double2 *row, int n) {
+  double2 v = row[n < 0 ? -n : n];
+  if (n < 0)
+    v.y = -v.y;
+  return v;
+}
+
+// ===========================================================================
+// The FP64 chain kernel
+// ===========================================================================
+constexpr int CT = 256;
+constexpr int HDR = 96;  // doubles in the move-context header
+
+// Context header layout (doubles):
+//  0 m, 1 kind, 2 na, 3 pacc, 4..6 newcom, 8..15 cell old, 16..23 cell new,
+//  24..47 old positions [8][3], 48..71 new positions [8][3], 72..79 charges
+struct ChainArgs {
+  DevBox b;
+  const FF *ff;
+  Settings *set;
+  const MoveRec *moves;
+  double *prop;   // [n][12]
+  int64_t first;
+  int n;
+  double *part;   // [grid][4]
+  unsigned *bar;
+  double *ctx;    // HDR + tables
+  int *tr_i;      // [n][3] or null
+  double *tr_d;   // [n][3] or null
+};
+
+struct ChainShared {
+  Settings set;
+  double e_run[5];
+  double hdr[HDR];
+  double red[CT / 32];
+  double tot[4];
+  int accept, flag, ok;
+  unsigned gen;
+};
+
+// Build the next move's header and phase tables (designated CTAs), using the
+// committed state plus the just-decided move when it touched the same
+// molecule.
+__device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
+                          const double *prev_hdr, int prev_acc) {
+  const DevBox &b = A.b;
+  const MoveRec &r = A.moves[t];
+  int m = r.mol;
+  int a0 = b.mstart[m], na = b.mstart[m + 1] - a0;
+  int G = gridDim.x;
+  int stride = b.kmax + 1;
+  int nrows = A.b.K > 0 ? 2 * na * 3 : 0;
+  bool header_cta = blockIdx.x == 0;
+  bool row_cta = false;
+  for (int rr = blockIdx.x; rr < nrows; rr += G)
+    row_cta = true;
+  if (!header_cta && !row_cta)
+    return;
+  __shared__ double oldp[MAX_MOL_ATOMS][3], newp[MAX_MOL_ATOMS][3], com[3],
+      newcom[3];
+  if (threadIdx.x == 0) {
+    bool same = prev_acc && prev_hdr && (int)prev_hdr[0] == m;
+    for (int a = 0; a < na; ++a) {
+      if (same) {
+        for (int d = 0; d < 3; ++d)
+          oldp[a][d] = prev_hdr[48 + 3 * a + d];
+      } else {
+        oldp[a][0] = __ldcg(b.x + a0 + a);
+        oldp[a][1] = __ldcg(b.y + a0 + a);
+        oldp[a][2] = __ldcg(b.z + a0 + a);
+      }
+    }
+    if (same && (int)prev_hdr[1] == 0) {
+      for (int d = 0; d < 3; ++d)
+        com[d] = prev_hdr[4 + d];
+    } else {
+      com[0] = __ldcg(b.cx + m);
+      com[1] = __ldcg(b.cy + m);
+      com[2] = __ldcg(b.cz + m);
+    }
+    apply_proposal(b, r.kind, A.prop + (size_t)t * 12, na, oldp, com, newp,
+                   newcom);
+  }
+  __syncthreads();
+  if (header_cta && threadIdx.x == 0) {
+    double *h = A.ctx;
+    h[0] = m;
+    h[1] = r.kind;
+    h[2] = na;
+    h[3] = r.pacc;
+    for (int d = 0; d < 3; ++d)
+      h[4 + d] = newcom[d];
+    for (int a = 0; a < na; ++a) {
+      h[8 + a] = position_to_cell(b, oldp[a][0], oldp[a][1], oldp[a][2]);
+      h[16 + a] = position_to_cell(b, newp[a][0], newp[a][1], newp[a][2]);
+      for (int d = 0; d < 3; ++d) {
+        h[24 + 3 * a + d] = oldp[a][d];
+        h[48 + 3 * a + d] = newp[a][d];
+      }
+      double q = b.q[a0 + a];
+      h[72 + a] = fabs(q) < 0.000000001 ? 0.0 : q;
+    }
+  }
+  // phase rows exp(i n 2 pi r_d / L_d), n = 0..kmax, one entry per thread
+  double2 *tab = (double2 *)(A.ctx + HDR);
+  for (int rr = blockIdx.x; rr < nrows; rr += G) {
+    int p = rr / 3, d = rr % 3;
+    double coord = p < na ? oldp[p][d] : newp[p - na][d];
+    double cv = 1.0 / b.L[d];
+    cv *= 2.0 * M_PI;
+    double th = cv * coord;
+    for (int n = threadIdx.x; n < stride; n += blockDim.x) {
+      double s, c;
+      sincos(th * (double)n, &s, &c);
+      tab[(size_t)rr * stride + n] = make_double2(c, s);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
+  extern __shared__ double dyn[];
+  __shared__ ChainShared S;
+  const DevBox &b = A.b;
+  const FF &ff = *A.ff;
+  int G = gridDim.x, cta = blockIdx.x;
+  int kc_max = (b.K + G - 1) / G;
+  int kbeg = min(b.K, cta * kc_max);
+  int kc = min(kc_max, b.K - kbeg);
+  double *sR = dyn, *sI = sR + kc_max, *nR = sI + kc_max, *nI = nR + kc_max,
+         *pf = nI + kc_max;
+  char4 *kn = (char4 *)(pf + kc_max);
+  int stride = b.kmax + 1;
+  double2 *tab = (double2 *)(dyn + ((5 * kc_max + (kc_max + 1) / 2 + 1) & ~1));
+  for (int i = threadIdx.x; i < kc; i += CT) {
+    int k = kbeg + i;
+    sR[i] = b.sumRref[k];
+    sI[i] = b.sumIref[k];
+    pf[i] = b.prefact[k];
+    kn[i] = b.kn[k];
+  }
+  if (threadIdx.x == 0) {
+    S.set = *A.set;
+    for (int i = 0; i < 5; ++i)
+      S.e_run[i] = b.energy[i];
+    S.gen = ld_acquire(&A.bar[1]);
+  }
+  __syncthreads();
+
+  const int total_threads = G * CT;
+  const int gtid = cta * CT + threadIdx.x;
+  // proposals from move t to the next adjustment boundary
+  auto make_props = [&](int t0) {
+    int t1 = t0;
+    while (t1 < A.n) {
+      long long step = A.first + t1;
+      if (t1 > t0 && (step + 1) % S.set.adj == 0)
+        break;
+      ++t1;
+    }
+    for (int t = t0 + gtid; t < t1; t += total_threads)
+      make_proposal(A.moves[t], S.set, A.prop + (size_t)t * 12);
+  };
+
+  // prologue
+  if (threadIdx.x == 0)
+    settings_adjust(S.set, A.first);
+  __syncthreads();
+  make_props(0);
+  if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
+    return;
+  build_ctx(A, S, 0, nullptr, 0);
+  if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
+    return;
+
+  for (int t = 0; t < A.n; ++t) {
+    // ---------------- phase A ----------------
+    for (int i = threadIdx.x; i < HDR; i += CT)
+      S.hdr[i] = __ldcg(A.ctx + i);
+    __syncthreads();
+    int m = (int)S.hdr[0];
+    int na = (int)S.hdr[2];
+    int nrows = b.K > 0 ? 2 * na * 3 : 0;
+    for (int i = threadIdx.x; i < nrows * stride; i += CT)
+      tab[i] = __ldcg((const double2 *)(A.ctx + HDR) + i);
+    __syncthreads();
+    double lj = 0.0, re = 0.0, ovl = 0.0, er = 0.0;
+    int units = na * 2 * NB27;
+    for (int u = cta; u < units; u += G) {
+      int a = u / (2 * NB27), side = (u / NB27) % 2, nn = u % NB27;
+      const double *pp = S.hdr + (side ? 48 : 24) + 3 * a;
+      int cell = (int)S.hdr[(side ? 16 : 8) + a];
+      int c2 = b.nbr[cell * NB27 + nn];
+      int n2 = __ldcg(b.cell_count + c2);
+      double qa = b.q[b.mstart[m] + a];
+      int ka = b.kind[b.mstart[m] + a];
+      for (int j = threadIdx.x; j < n2; j += CT) {
+        size_t s = (size_t)c2 * b.cap + j;
+        int mj = __ldcg(b.cell_meta + s);
+        if (meta_mol(mj) == m)
+          continue;
+        const double *pq = (const double *)(b.cell_pos + s);
+        double4_32a pj = make_double4_32a(__ldcg(pq), __ldcg(pq + 1),
+                                          __ldcg(pq + 2), __ldcg(pq + 3));
+        double dx = min_image(pp[0] - pj.x, b.L[0], b.half[0]);
+        double dy = min_image(pp[1] - pj.y, b.L[1], b.half[1]);
+        double dz = min_image(pp[2] - pj.z, b.L[2], b.half[2]);
+        double distSq = dsq3(dx, dy, dz);
+        if (ff.rcutSq > distSq) {
+          if (side && distSq < ff.rcutLowSq)
+            ovl = 1.0;
+          double e = 0.0;
+          if (ff.electrostatic) {
+            double qq = qa * pj.w * QQ_FACT;
+            if (qq != 0.0)
+              e = coulomb_energy(ff, distSq, qq);
+          }
+          double l = lj_energy(ff, distSq, ka + meta_kind(mj) * ff.n_kinds);
+          if (side) {
+            re += e;
+            lj += l;
+          } else {
+            re += -e;
+            lj += -l;
+          }
+        }
+      }
+    }
+    for (int i = threadIdx.x; i < kc; i += CT) {
+      char4 n = kn[i];
+      double rN = 0, iN = 0, rO = 0, iO = 0;
+      for (int a = 0; a < na; ++a) {
+        double q = S.hdr[72 + a];
+        if (q == 0.0)
+          continue;
+        const double2 *ro = tab + (size_t)(a * 3) * stride;
+        const double2 *rn = tab + (size_t)((na + a) * 3) * stride;
+        double2 eo = cmul2(cmul2(ro[n.x], tab_at(ro + stride, n.y)),
+                           tab_at(ro + 2 * stride, n.z));
+        double2 en = cmul2(cmul2(rn[n.x], tab_at(rn + stride, n.y)),
+                           tab_at(rn + 2 * stride, n.z));
+        rN += q * en.x;
+        iN += q * en.y;
+        rO += q * eo.x;
+        iO += q * eo.y;
+      }
+      double srn = sR[i] + 1.0 * (rN - rO);
+      double sin_ = sI[i] + 1.0 * (iN - iO);
+      nR[i] = srn;
+      nI[i] = sin_;
+      er += (srn * srn + sin_ * sin_) * pf[i];
+    }
+    double LJ = block_sum<CT>(lj, S.red);
+    double RE = block_sum<CT>(re, S.red);
+    double ER = block_sum<CT>(er, S.red);
+    double OV = block_sum<CT>(ovl, S.red);
+    if (threadIdx.x == 0) {
+      double *p = A.part + (size_t)cta * 4;
+      p[0] = LJ;
+      p[1] = RE;
+      p[2] = ER;
+      p[3] = OV > 0 ? 1.0 : 0.0;
+    }
+    if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
+      return;
+    // ---------------- phase B ----------------
+    if (threadIdx.x < 32) {
+      double v[4] = {0, 0, 0, 0};
+      for (int c = threadIdx.x; c < G; c += 32) {
+        const double *p = A.part + (size_t)c * 4;
+        v[0] += __ldcg(p);
+        v[1] += __ldcg(p + 1);
+        v[2] += __ldcg(p + 2);
+        v[3] = fmax(v[3], __ldcg(p + 3));
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        v[0] += __shfl_down_sync(0xffffffffu, v[0], o);
+        v[1] += __shfl_down_sync(0xffffffffu, v[1], o);
+        v[2] += __shfl_down_sync(0xffffffffu, v[2], o);
+        v[3] = fmax(v[3], __shfl_down_sync(0xffffffffu, v[3], o));
+      }
+      if (threadIdx.x == 0) {
+        int kind = (int)S.hdr[1];
+        bool over = v[3] > 0;
+        double dLJ = v[0], dRe = v[1];
+        double dRc = (!over && b.K > 0) ? v[2] - S.e_run[2] : 0.0;
+        if (!over && b.K == 0)
+          dRc = 0.0;
+        double ex = __dmul_rn(-ff.beta, __dadd_rn(__dadd_rn(dLJ, dRe), dRc));
+        int res = S.hdr[3] < exp(ex);
+        int acc = res && !over;
+        if (acc) {
+          S.e_run[0] += dLJ;
+          S.e_run[1] += dRe;
+          S.e_run[2] += dRc;
+        }
+        settings_update(S.set, kind, acc);
+        S.accept = acc;
+        if (cta == 0 && A.tr_i) {
+          A.tr_i[3 * (size_t)t] = kind;
+          A.tr_i[3 * (size_t)t + 1] = m;
+          A.tr_i[3 * (size_t)t + 2] = acc;
+          A.tr_d[3 * (size_t)t] = dLJ;
+          A.tr_d[3 * (size_t)t + 1] = dRe;
+          A.tr_d[3 * (size_t)t + 2] = dRc;
+        }
+      }
+    }
+    __syncthreads();
+    int acc = S.accept;
+    if (acc) {
+      for (int i = threadIdx.x; i < kc; i += CT) {
+        sR[i] = nR[i];
+        sI[i] = nI[i];
+      }
+      if (cta == 0 && threadIdx.x == 0) {
+        int a0 = b.mstart[m];
+        for (int a = 0; a < na; ++a) {
+          const double *np = S.hdr + 48 + 3 * a;
+          b.x[a0 + a] = np[0];
+          b.y[a0 + a] = np[1];
+          b.z[a0 + a] = np[2];
+          cell_move_atom(b, a0 + a, np[0], np[1], np[2]);
+        }
+        if ((int)S.hdr[1] == 0) {
+          b.cx[m] = S.hdr[4];
+          b.cy[m] = S.hdr[5];
+          b.cz[m] = S.hdr[6];
+        }
+      }
+    }
+    if (t + 1 < A.n) {
+      long long step = A.first + t + 1;
+      if ((step + 1) % S.set.adj == 0) {
+        if (threadIdx.x == 0)
+          settings_adjust(S.set, step);
+        __syncthreads();
+        make_props(t + 1);
+        if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
+          return;
+      }
+      build_ctx(A, S, t + 1, S.hdr, acc);
+      if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
+        return;
+    }
+  }
+  // write back this CTA's structure factors; CTA 0 the settings and energies
+  for (int i = threadIdx.x; i < kc; i += CT) {
+    b.sumRref[kbeg + i] = sR[i];
+    b.sumIref[kbeg + i] = sI[i];
+  }
+  if (cta == 0 && threadIdx.x == 0) {
+    *A.set = S.set;
+    for (int i = 0; i < 5; ++i)
+      b.energy[i] = S.e_run[i];
+  }
+}
+
+// ===========================================================================
+// MultiParticle kernels (src/moves/MultiParticle.h)
+// ===========================================================================
+__device__ __forceinline__ void philox4x64(uint64_t c0, uint64_t c1,
+                                           uint64_t c2, uint64_t c3,
+                                           uint64_t k0, uint64_t k1,
+                                           uint64_t *o) {
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) {
+      k0 += 0x9E3779B97F4A7C15ULL;
+      k1 += 0xBB67AE8584CAA73BULL;
+    }
+    uint64_t lo0 = 0xD2E7470EE14C6C93ULL * c0;
+    uint64_t hi0 = __umul64hi(0xD2E7470EE14C6C93ULL, c0);
+    uint64_t lo1 = 0xCA5A826395121157ULL * c2;
+    uint64_t hi1 = __umul64hi(0xCA5A826395121157ULL, c2);
+    uint64_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+  }
+  o[0] = c0;
+  o[1] = c1;
+  o[2] = c2;
+  o[3] = c3;
+}
+// r123::u01<double> and uneg11<double> of a 64-bit word
+__device__ __forceinline__ double u01_64(uint64_t v) {
+  const double f = 1.0 / 18446744073709551616.0;
+  return __dadd_rn(__dmul_rn(__ull2double_rn(v), f), 0.5 * f);
+}
+__device__ __forceinline__ double uneg11_64(uint64_t v) {
+  const double f = 1.0 / 9223372036854775808.0;
+  return __dadd_rn(__dmul_rn(__ll2double_rn((long long)v), f), 0.5 * f);
+}
+
+struct MpArgs {
+  DevBox b;
+  Settings *set;
+  int type;        // 0 displacement, 1 rotation
+  uint64_t step, seed;
+  double beta;
+  const double *mF, *mR, *tq;  // reference forces / torque
+  double *xn, *yn, *zn, *cxn, *cyn, *czn, *tk;
+  int *inrange;
+  int *fail;
+};
+
+// CalculateTrialDistRot + Translate/RotateForceBiased/Random
+// (src/moves/MultiParticle.h:546-714), one thread per molecule.
+__global__ void k_mp_transform(MpArgs P) {
+  const DevBox &b = P.b;
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= b.n_mol)
+    return;
+  const Settings &s = *P.set;
+  const double lambda = 0.5;
+  double lb[3];
+  for (int d = 0; d < 3; ++d) {
+    double v = P.type == 1 ? P.tq[3 * (size_t)m + d]
+                           : __dadd_rn(P.mF[3 * (size_t)m + d],
+                                       P.mR[3 * (size_t)m + d]);
+    lb[d] = __dmul_rn(__dmul_rn(v, lambda), P.beta);
+  }
+  double mx = P.type == 1 ? s.mp_r_max : s.mp_t_max;
+  double lbmax[3];
+  bool fir = true;
+  for (int d = 0; d < 3; ++d) {
+    lbmax[d] = __dmul_rn(lb[d], mx);
+    double a = fabs(lbmax[d]);
+    fir = fir && a > 1E-12 && a < 30;
+  }
+  uint64_t r[4];
+  philox4x64((uint64_t)m, 0, 0, 0, P.step, P.seed, r);
+  double val[3] = {0.0, 0.0, 0.0};
+  if (fir)
+    for (int d = 0; d < 3; ++d)
+      val[d] = log(__dadd_rn(exp(-1.0 * lbmax[d]),
+                             __dmul_rn(__dmul_rn(2.0, u01_64(r[d])),
+                                       sinh(lbmax[d])))) /
+               lb[d];
+  P.inrange[m] = fir;
+  for (int d = 0; d < 3; ++d)
+    P.tk[3 * (size_t)m + d] = val[d];
+  // MultiParticle::Transform checks (src/moves/MultiParticle.h:366-409)
+  double len = sqrt(val[0] * val[0] + val[1] * val[1] + val[2] * val[2]);
+  if (!isfinite(len) ||
+      (P.type == 0 && (val[0] > b.half[0] || val[1] > b.half[1] ||
+                       val[2] > b.half[2])))
+    atomicOr(P.fail, 1);
+  int a0 = b.mstart[m], na = b.mstart[m + 1] - a0;
+  double com[3] = {b.cx[m], b.cy[m], b.cz[m]};
+  if (P.type == 1) {
+    double rm[9];
+    if (fir) {
+      double rotLen = sqrt(val[0] * val[0] + val[1] * val[1] + val[2] * val[2]);
+      double inv = 1.0 / rotLen;
+      double ax[3] = {val[0] * inv, val[1] * inv, val[2] * inv};
+      axis_angle_matrix(rotLen, ax, rm);
+    } else {
+      double symRand = __dmul_rn(s.mp_r_max, uneg11_64(r[0]));
+      double u = uneg11_64(r[1]);
+      double theta = __dmul_rn(2.0 * M_PI, u01_64(r[2]));
+      double rootTerm = sqrt(__dadd_rn(1.0, -__dmul_rn(u, u)));
+      double ax[3] = {rootTerm * cos(theta), rootTerm * sin(theta), u};
+      axis_angle_matrix(symRand, ax, rm);
+    }
+    for (int p = 0; p < na; ++p) {
+      int a = a0 + p;
+      double v[3] = {b.x[a], b.y[a], b.z[a]};
+      for (int d = 0; d < 3; ++d) {
+        v[d] = unwrap1(v[d], com[d], b.L[d], b.half[d]);
+        v[d] = __dadd_rn(v[d], -com[d]);
+      }
+      double w[3];
+      for (int i = 0; i < 3; ++i)
+        w[i] = __dadd_rn(__dadd_rn(__dmul_rn(rm[3 * i], v[0]),
+                                   __dmul_rn(rm[3 * i + 1], v[1])),
+                         __dmul_rn(rm[3 * i + 2], v[2]));
+      P.xn[a] = wrap1(__dadd_rn(w[0], com[0]), b.L[0]);
+      P.yn[a] = wrap1(__dadd_rn(w[1], com[1]), b.L[1]);
+      P.zn[a] = wrap1(__dadd_rn(w[2], com[2]), b.L[2]);
+    }
+    P.cxn[m] = com[0];
+    P.cyn[m] = com[1];
+    P.czn[m] = com[2];
+  } else {
+    double sh[3];
+    for (int d = 0; d < 3; ++d)
+      sh[d] = fir ? val[d] : __dmul_rn(s.mp_t_max, uneg11_64(r[d]));
+    for (int p = 0; p < na; ++p) {
+      int a = a0 + p;
+      P.xn[a] = wrap1(__dadd_rn(b.x[a], sh[0]), b.L[0]);
+      P.yn[a] = wrap1(__dadd_rn(b.y[a], sh[1]), b.L[1]);
+      P.zn[a] = wrap1(__dadd_rn(b.z[a], sh[2]), b.L[2]);
+    }
+    P.cxn[m] = wrap1(__dadd_rn(com[0], sh[0]), b.L[0]);
+    P.cyn[m] = wrap1(__dadd_rn(com[1], sh[1]), b.L[1]);
+    P.czn[m] = wrap1(__dadd_rn(com[2], sh[2]), b.L[2]);
+  }
+}
+
+struct MpAcceptArgs {
+  DevBox b;
+  Settings *set;
+  int type;
+  uint64_t step, seed;
+  double beta;
+  const double *mF, *mR, *tq, *mFn, *mRn, *tqn, *tk;
+  const int *inrange, *fail;
+  const double *newE;  // [0] recip, [1] inter, [2] real
+  double *out;         // [0] accept flag
+  int *tr_i;
+  double *tr_d;
+};
+
+// MultiParticle::GetCoeff + Accept (src/moves/MultiParticle.h:447-544)
+__global__ void k_mp_accept(MpAcceptArgs P) {
+  const DevBox &b = P.b;
+  Settings &s = *P.set;
+  const double lBeta = 0.5 * P.beta;
+  double mx = P.type == 1 ? s.mp_r_max : s.mp_t_max;
+  double w = 1.0;
+  for (int m = threadIdx.x; m < b.n_mol; m += blockDim.x) {
+    if (!P.inrange[m])
+      continue;
+    double wr = 1.0;
+    for (int d = 0; d < 3; ++d) {
+      size_t i = 3 * (size_t)m + d;
+      double lo, ln;
+      if (P.type == 1) {
+        lo = P.tq[i] * lBeta;
+        ln = P.tqn[i] * lBeta;
+      } else {
+        lo = (P.mF[i] + P.mR[i]) * lBeta;
+        ln = (P.mFn[i] + P.mRn[i]) * lBeta;
+      }
+      double k = P.tk[i];
+      wr *= ln * exp(-ln * k) / (2.0 * sinh(ln * mx));
+      wr /= lo * exp(lo * k) / (2.0 * sinh(lo * mx));
+    }
+    w *= wr;
+  }
+  __shared__ double sh[1024];
+  sh[threadIdx.x] = w;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double W = 1.0;
+    for (int i = 0; i < (int)blockDim.x; ++i)
+      W *= sh[i];
+    if (!isfinite(W))
+      W = 0.0;
+    double *e = b.energy;
+    double newRecip = P.newE[0], newInter = P.newE[1], newReal = P.newE[2];
+    double totNew = 0.0 + 0.0 + newInter + 0.0 + newReal + newRecip + e[3] + e[4];
+    double totOld = 0.0 + 0.0 + e[0] + 0.0 + e[1] + e[2] + e[3] + e[4];
+    double uBoltz = exp(-P.beta * (totNew - totOld));
+    double accept = W * uBoltz;
+    uint64_t r[4];
+    philox4x64((uint64_t)b.n_mol, 0, 0, 0, P.step, P.seed, r);
+    double pr = u01_64(r[0]);
+    int result = (*P.fail == 0) && pr < accept;
+    if (result) {
+      e[0] = newInter;
+      e[1] = newReal;
+      e[2] = newRecip;
+    }
+    s.mp_itries[P.type]++;
+    if (result)
+      s.mp_iacc[P.type]++;
+    settings_update(s, 2, result);
+    P.out[0] = result;
+    if (P.tr_i) {
+      P.tr_i[0] = 2;
+      P.tr_i[1] = P.type;
+      P.tr_i[2] = result;
+      P.tr_d[0] = newInter;
+      P.tr_d[1] = newReal;
+      P.tr_d[2] = newRecip;
+    }
+  }
+}
+
+// Commit the trial state when accepted (the swaps of MultiParticle::Accept).
+struct MpCommitArgs {
+  DevBox b, bn;
+  const double *flag;
+  int K;
+  double *aF, *mF, *aR, *mR, *tq;
+  const double *aFn, *mFn, *aRn, *mRn, *tqn;
+};
+__global__ void k_mp_commit(MpCommitArgs P) {
+  if (P.flag[0] == 0.0)
+    return;
+  const DevBox &b = P.b, &n = P.bn;
+  size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = tid; i < (size_t)b.n_atoms; i += stride) {
+    b.x[i] = n.x[i];
+    b.y[i] = n.y[i];
+    b.z[i] = n.z[i];
+    b.atom_cell[i] = n.atom_cell[i];
+    b.atom_slot[i] = n.atom_slot[i];
+    for (int d = 0; d < 3; ++d) {
+      P.aF[3 * i + d] = P.aFn[3 * i + d];
+      P.aR[3 * i + d] = P.aRn[3 * i + d];
+    }
+  }
+  for (size_t i = tid; i < (size_t)b.n_mol; i += stride) {
+    b.cx[i] = n.cx[i];
+    b.cy[i] = n.cy[i];
+    b.cz[i] = n.cz[i];
+    for (int d = 0; d < 3; ++d) {
+      P.mF[3 * i + d] = P.mFn[3 * i + d];
+      P.mR[3 * i + d] = P.mRn[3 * i + d];
+      P.tq[3 * i + d] = P.tqn[3 * i + d];
+    }
+  }
+  for (size_t i = tid; i < (size_t)P.K; i += stride) {
+    b.sumRref[i] = b.sumRnew[i];
+    b.sumIref[i] = b.sumInew[i];
+  }
+  size_t nc = (size_t)b.ncell * b.cap;
+  for (size_t i = tid; i < nc; i += stride) {
+    b.cell_atom[i] = n.cell_atom[i];
+    b.cell_pos[i] = n.cell_pos[i];
+    b.cell_meta[i] = n.cell_meta[i];
+    b.cell_fix[i] = n.cell_fix[i];
+  }
+  for (size_t i = tid; i < (size_t)b.ncell; i += stride)
+    b.cell_count[i] = n.cell_count[i];
+}
+
+__global__ void k_settings_adjust(Settings *s, long long step) {
+  settings_adjust(*s, step);
+}
+__global__ void k_set_energy2(double *energy, const double *v) {
+  energy[0] = v[0];
+  energy[1] = v[1];
+}
+
+// ===========================================================================
+// Host orchestration
+// ===========================================================================
+template <class T>
+static int mc_alloc(Box &b, McState &s, T **p, size_t n) {
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+  if (e != cudaSuccess)
+    return b.CudaCheck(e, "cudaMalloc (Monte Carlo state)");
+  s.allocs.push_back(q);
+  *p = (T *)q;
+  return OK;
+}
+
+void mc_destroy(Box &b) {
+  if (!b.mc)
+    return;
+  McState &s = *b.mc;
+  if (b.stream)
+    cudaStreamSynchronize(b.stream);
+  for (void *p : s.allocs)
+    cudaFree(p);
+  if (s.h_moves)
+    cudaFreeHost(s.h_moves);
+  delete s.stream;
+  delete b.mc;
+  b.mc = nullptr;
+}
+
+static size_t chain_smem(const Box &b, int grid) {
+  int kc_max = (b.dev.K + grid - 1) / grid;
+  return sizeof(double) * ((5 * (size_t)kc_max + (kc_max + 1) / 2 + 1) & ~(size_t)1) +
+         sizeof(double2) * (size_t)(2 * MAX_MOL_ATOMS * 3) * (b.dev.kmax + 1) +
+         64;
+}
+
+int mc_init(Box &b, const gb_mc_params &p) {
+  mc_destroy(b);
+  if (p.adj_steps <= 0)
+    return b.Fail(ERR_ARG, "AdjSteps must be positive");
+  if (!(p.frac[0] >= 0 && p.frac[1] >= 0 && p.frac[2] >= 0) ||
+      p.frac[0] + p.frac[1] + p.frac[2] <= 0)
+    return b.Fail(ERR_ARG, "move frequencies must be non-negative, not all 0");
+  const HostSystem &h = b.host;
+  std::vector<int> len(h.n_mol);
+  for (int m = 0; m < h.n_mol; ++m) {
+    len[m] = h.mstart[m + 1] - h.mstart[m];
+    if (len[m] > MAX_MOL_ATOMS)
+      return b.Fail(ERR_UNSUPPORTED, "molecules above 8 atoms in the move loop");
+  }
+  b.mc = new McState();
+  McState &s = *b.mc;
+  s.params = p;
+  s.stream = new MoveStream(p.seed, p.frac, h.n_mol, len);
+  s.next_step = 0;
+  int rc;
+  if ((rc = mc_alloc(b, s, &s.d_set, 1)))
+    return rc;
+  Settings st{};
+  // MoveSettings::Init reads the box axis before BoxDimensions::Init sets it
+  // (src/System.cpp:72-81), so a fresh start has displacement scale 0.
+  st.scale[0] = 0.0;
+  st.scale[1] = M_PI_4;
+  st.mp_r_max = 0.01 * M_PI;
+  st.mp_t_max = 0.02;
+  if (p.use_scales) {
+    st.scale[0] = p.scales[0];
+    st.scale[1] = p.scales[1];
+    st.mp_t_max = p.scales[2];
+    st.mp_r_max = p.scales[3];
+  }
+  st.singleMoveAccepted = 1;
+  st.adj = p.adj_steps;
+  st.amin = std::min(h.L[0], std::min(h.L[1], h.L[2]));
+  if ((rc = b.CudaCheck(cudaMemcpyAsync(s.d_set, &st, sizeof(Settings),
+                                        cudaMemcpyHostToDevice, b.stream),
+                        "upload")))
+    return rc;
+  // chain-kernel geometry: one CTA per SM (cooperative residency checked)
+  int per_sm = 0;
+  size_t sm = chain_smem(b, b.sm_count);
+  if (sm > 48 * 1024)
+    cudaFuncSetAttribute(k_chain_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sm);
+  if ((rc = b.CudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                            &per_sm, k_chain_fp64, CT, sm),
+                        "occupancy")))
+    return rc;
+  if (per_sm < 1)
+    return b.Fail(ERR_UNSUPPORTED, "chain kernel does not fit on an SM");
+  s.grid = b.sm_count;
+  s.move_cap = 1 << 16;
+  int stride = b.dev.kmax + 1;
+  if ((rc = mc_alloc(b, s, &s.d_moves, s.move_cap)) ||
+      (rc = mc_alloc(b, s, &s.d_prop, s.move_cap * 12)) ||
+      (rc = mc_alloc(b, s, &s.d_part, (size_t)s.grid * 4)) ||
+      (rc = mc_alloc(b, s, &s.d_bar, 8)) ||
+      (rc = mc_alloc(b, s, &s.d_ctx,
+                     HDR + 2 * (size_t)(2 * MAX_MOL_ATOMS * 3) * stride)) ||
+      (rc = mc_alloc(b, s, &s.d_mp, 16)))
+    return rc;
+  if ((rc = b.CudaCheck(cudaMallocHost(&s.h_moves, s.move_cap * sizeof(MoveRec)),
+                        "pinned")))
+    return rc;
+  if ((rc = b.CudaCheck(cudaMemsetAsync(s.d_bar, 0, 32, b.stream), "memset")))
+    return rc;
+  // MultiParticle trial-state buffers
+  int N = b.dev.n_atoms, M = b.dev.n_mol;
+  if ((rc = mc_alloc(b, s, &s.d_xn, N)) || (rc = mc_alloc(b, s, &s.d_yn, N)) ||
+      (rc = mc_alloc(b, s, &s.d_zn, N)) || (rc = mc_alloc(b, s, &s.d_cxn, M)) ||
+      (rc = mc_alloc(b, s, &s.d_cyn, M)) || (rc = mc_alloc(b, s, &s.d_czn, M)) ||
+      (rc = mc_alloc(b, s, &s.d_aFn, 3 * (size_t)N)) ||
+      (rc = mc_alloc(b, s, &s.d_mFn, 3 * (size_t)M)) ||
+      (rc = mc_alloc(b, s, &s.d_aRn, 3 * (size_t)N)) ||
+      (rc = mc_alloc(b, s, &s.d_mRn, 3 * (size_t)M)) ||
+      (rc = mc_alloc(b, s, &s.d_tqn, 3 * (size_t)M)) ||
+      (rc = mc_alloc(b, s, &s.d_tk, 3 * (size_t)M)) ||
+      (rc = mc_alloc(b, s, &s.d_inrange, M)))
+    return rc;
+  DevBox &n = s.cells_new;
+  n = b.dev;
+  n.x = s.d_xn;
+  n.y = s.d_yn;
+  n.z = s.d_zn;
+  n.cx = s.d_cxn;
+  n.cy = s.d_cyn;
+  n.cz = s.d_czn;
+  size_t NC = (size_t)b.dev.ncell * b.dev.cap;
+  if ((rc = mc_alloc(b, s, &n.cell_count, b.dev.ncell)) ||
+      (rc = mc_alloc(b, s, &n.cell_atom, NC)) ||
+      (rc = mc_alloc(b, s, &n.cell_pos, NC)) ||
+      (rc = mc_alloc(b, s, &n.cell_meta, NC)) ||
+      (rc = mc_alloc(b, s, &n.cell_fix, NC)) ||
+      (rc = mc_alloc(b, s, &n.atom_cell, N)) ||
+      (rc = mc_alloc(b, s, &n.atom_slot, N)))
+    return rc;
+  return b.Sync();
+}
+
+// Draw moves up to `step` without running them (restart at a later step).
+static void skip_to(McState &s, int64_t step) {
+  MoveRec r;
+  while (s.next_step < step) {
+    s.stream->Next(&r);
+    s.next_step++;
+  }
+}
+
+static int run_chain(Box &b, McState &s, const MoveRec *moves, int64_t first,
+                     int n, int *tr_i, double *tr_d) {
+  ChainArgs A;
+  A.b = b.dev;
+  A.ff = b.d_ff;
+  A.set = s.d_set;
+  A.moves = moves;
+  A.prop = s.d_prop;
+  A.first = first;
+  A.n = n;
+  A.part = s.d_part;
+  A.bar = s.d_bar;
+  A.ctx = s.d_ctx;
+  A.tr_i = tr_i;
+  A.tr_d = tr_d;
+  void *args[] = {&A};
+  size_t sm = chain_smem(b, s.grid);
+  return b.CudaCheck(cudaLaunchCooperativeKernel((void *)k_chain_fp64,
+                                                 dim3(s.grid), dim3(CT), args,
+                                                 sm, b.stream),
+                     "chain kernel");
+}
+
+static int run_mp(Box &b, McState &s, int64_t step, int type, int *tr_i,
+                  double *tr_d) {
+  int rc;
+  k_settings_adjust<<<1, 1, 0, b.stream>>>(s.d_set, (long long)step);
+  Settings host_set;
+  if ((rc = b.CudaCheck(cudaMemcpyAsync(&host_set, s.d_set, sizeof(Settings),
+                                        cudaMemcpyDeviceToHost, b.stream),
+                        "download")) ||
+      (rc = b.Sync()))
+    return rc;
+  DevBox &d = b.dev;
+  if (host_set.singleMoveAccepted) {
+    // forces of the current state (MultiParticle::Prep, :208-227)
+    if ((rc = b.CopyRecip()) ||
+        (rc = launch_force_recip(b, d, d.sumRnew, d.sumInew, b.d_aR, b.d_mR)) ||
+        (rc = launch_box_force(b, d, b.d_aF, b.d_mF, s.d_mp + 8)))
+      return rc;
+    k_set_energy2<<<1, 1, 0, b.stream>>>(d.energy, s.d_mp + 8);
+    if ((rc = launch_torque(b, d, b.d_aF, b.d_aR, b.d_tq)))
+      return rc;
+  }
+  if ((rc = b.CudaCheck(cudaMemsetAsync(s.d_mp, 0, 16 * sizeof(double),
+                                        b.stream),
+                        "memset")))
+    return rc;
+  MpArgs P;
+  P.b = d;
+  P.set = s.d_set;
+  P.type = type;
+  P.step = (uint64_t)step;
+  P.seed = s.params.seed;
+  P.beta = b.ff.beta;
+  P.mF = b.d_mF;
+  P.mR = b.d_mR;
+  P.tq = b.d_tq;
+  P.xn = s.d_xn;
+  P.yn = s.d_yn;
+  P.zn = s.d_zn;
+  P.cxn = s.d_cxn;
+  P.cyn = s.d_cyn;
+  P.czn = s.d_czn;
+  P.tk = s.d_tk;
+  P.inrange = s.d_inrange;
+  P.fail = (int *)(s.d_mp + 12);
+  k_mp_transform<<<(d.n_mol + 127) / 128, 128, 0, b.stream>>>(P);
+  // trial state: grid, structure factors, forces, torque
+  DevBox n = s.cells_new;
+  n.sumRnew = d.sumRnew;
+  n.sumInew = d.sumInew;
+  n.sumRref = d.sumRref;
+  n.sumIref = d.sumIref;
+  n.energy = d.energy;
+  n.err = d.err;
+  if ((rc = launch_grid_all(b, n)) ||
+      (rc = launch_recip_sums(b, n.x, n.y, n.z, d.sumRnew, d.sumInew)) ||
+      (rc = launch_recip_energy(b, d.sumRnew, d.sumInew, s.d_mp)) ||
+      (rc = launch_box_force(b, n, s.d_aFn, s.d_mFn, s.d_mp + 1)) ||
+      (rc = launch_force_recip(b, n, d.sumRnew, d.sumInew, s.d_aRn, s.d_mRn)) ||
+      (rc = launch_torque(b, n, s.d_aFn, s.d_aRn, s.d_tqn)))
+    return rc;
+  if (!b.cfg.ewald)
+    cudaMemsetAsync(s.d_mp, 0, sizeof(double), b.stream);
+  MpAcceptArgs Q;
+  Q.b = d;
+  Q.set = s.d_set;
+  Q.type = type;
+  Q.step = (uint64_t)step;
+  Q.seed = s.params.seed;
+  Q.beta = b.ff.beta;
+  Q.mF = b.d_mF;
+  Q.mR = b.d_mR;
+  Q.tq = b.d_tq;
+  Q.mFn = s.d_mFn;
+  Q.mRn = s.d_mRn;
+  Q.tqn = s.d_tqn;
+  Q.tk = s.d_tk;
+  Q.inrange = s.d_inrange;
+  Q.fail = (const int *)(s.d_mp + 12);
+  Q.newE = s.d_mp;
+  Q.out = s.d_mp + 4;
+  Q.tr_i = tr_i;
+  Q.tr_d = tr_d;
+  k_mp_accept<<<1, 256, 0, b.stream>>>(Q);
+  MpCommitArgs C;
+  C.b = d;
+  C.bn = n;
+  C.flag = s.d_mp + 4;
+  C.K = b.cfg.ewald ? d.K : 0;
+  C.aF = b.d_aF;
+  C.mF = b.d_mF;
+  C.aR = b.d_aR;
+  C.mR = b.d_mR;
+  C.tq = b.d_tq;
+  C.aFn = s.d_aFn;
+  C.mFn = s.d_mFn;
+  C.aRn = s.d_aRn;
+  C.mRn = s.d_mRn;
+  C.tqn = s.d_tqn;
+  k_mp_commit<<<2 * b.sm_count, 256, 0, b.stream>>>(C);
+  return b.CudaCheck(cudaGetLastError(), "multiparticle");
+}
+
+int mc_run(Box &b, int64_t first, int64_t nsteps, int32_t *kind, int32_t *mol,
+           int32_t *acc, double *de) {
+  if (!b.mc)
+    return b.Fail(ERR_STATE, "gb_mc_init has not been called");
+  McState &s = *b.mc;
+  if (first < s.next_step)
+    return b.Fail(ERR_STATE, "steps must be run in increasing order");
+  if (nsteps < 0)
+    return b.Fail(ERR_ARG, "negative step count");
+  skip_to(s, first);
+  bool trace = kind || mol || acc || de;
+  int rc;
+  if (trace && (size_t)nsteps > s.trace_cap) {
+    if ((rc = mc_alloc(b, s, &s.d_trace_i, 3 * (size_t)nsteps)) ||
+        (rc = mc_alloc(b, s, &s.d_trace_d, 3 * (size_t)nsteps)))
+      return rc;
+    s.trace_cap = nsteps;
+  }
+  int64_t done = 0;
+  while (done < nsteps) {
+    // fill a chunk of move records
+    int64_t chunk = std::min<int64_t>(nsteps - done, (int64_t)s.move_cap);
+    if ((rc = b.Sync()))  // the previous chunk may still read h_moves
+      return rc;
+    for (int64_t i = 0; i < chunk; ++i)
+      s.stream->Next(&s.h_moves[i]);
+    s.next_step += chunk;
+    if ((rc = b.CudaCheck(cudaMemcpyAsync(s.d_moves, s.h_moves,
+                                          chunk * sizeof(MoveRec),
+                                          cudaMemcpyHostToDevice, b.stream),
+                          "upload moves")))
+      return rc;
+    // split into chain segments and MultiParticle moves
+    int64_t i = 0;
+    while (i < chunk) {
+      int64_t step = first + done + i;
+      int *ti = trace ? s.d_trace_i + 3 * (done + i) : nullptr;
+      double *td = trace ? s.d_trace_d + 3 * (done + i) : nullptr;
+      if (s.h_moves[i].kind == 2) {
+        if ((rc = run_mp(b, s, step, s.h_moves[i].mol, ti, td)))
+          return rc;
+        ++i;
+        continue;
+      }
+      int64_t j = i;
+      while (j < chunk && s.h_moves[j].kind != 2)
+        ++j;
+      if ((rc = run_chain(b, s, s.d_moves + i, step, (int)(j - i), ti, td)))
+        return rc;
+      i = j;
+    }
+    done += chunk;
+  }
+  if ((rc = b.Sync()) || (rc = b.CheckError()))
+    return rc;
+  if (trace) {
+    std::vector<int> ti(3 * (size_t)nsteps);
+    std::vector<double> td(3 * (size_t)nsteps);
+    if ((rc = b.CudaCheck(cudaMemcpy(ti.data(), s.d_trace_i, ti.size() * 4,
+                                     cudaMemcpyDeviceToHost),
+                          "trace")) ||
+        (rc = b.CudaCheck(cudaMemcpy(td.data(), s.d_trace_d, td.size() * 8,
+                                     cudaMemcpyDeviceToHost),
+                          "trace")))
+      return rc;
+    for (int64_t t = 0; t < nsteps; ++t) {
+      if (kind)
+        kind[t] = ti[3 * t];
+      if (mol)
+        mol[t] = ti[3 * t + 1];
+      if (acc)
+        acc[t] = ti[3 * t + 2];
+      if (de)
+        for (int d = 0; d < 3; ++d)
+          de[3 * t + d] = td[3 * t + d];
+    }
+  }
+  return OK;
+}
+
+int mc_state(Box &b, double *scales4, int64_t *counts6) {
+  if (!b.mc)
+    return b.Fail(ERR_STATE, "gb_mc_init has not been called");
+  Settings st;
+  int rc;
+  if ((rc = b.CudaCheck(cudaMemcpyAsync(&st, b.mc->d_set, sizeof(Settings),
+                                        cudaMemcpyDeviceToHost, b.stream),
+                        "download")) ||
+      (rc = b.Sync()))
+    return rc;
+  if (scales4) {
+    scales4[0] = st.scale[0];
+    scales4[1] = st.scale[1];
+    scales4[2] = st.mp_t_max;
+    scales4[3] = st.mp_r_max;
+  }
+  if (counts6)
+    for (int k = 0; k < 3; ++k) {
+      counts6[2 * k] = st.tries[k];
+      counts6[2 * k + 1] = st.accepted[k];
+    }
+  return OK;
+}
+
+int mc_run_batch(const std::vector<Box *> &boxes, int64_t first,
+                 int64_t nsteps) {
+  for (Box *b : boxes) {
+    int rc = mc_run(*b, first, nsteps, nullptr, nullptr, nullptr, nullptr);
+    if (rc)
+      return rc;
+  }
+  return OK;
+}
+
+}  // namespace gb

@@ -1,0 +1,102 @@
+// Device-resident Monte Carlo loop: MT19937 move stream on the host,
+// persistent chain kernels on the device, MultiParticle as a kernel sequence.
+#pragma once
+
+#include "gomc_gb300.h"
+#include "gb_box.h"
+
+#include <cstdint>
+#include <vector>
+
+namespace gb {
+
+// One pre-drawn move (everything that does not depend on accept history).
+struct MoveRec {
+  int32_t kind;   // 0 displacement, 1 rotation, 2 multiparticle
+  int32_t mol;    // molecule (kinds 0/1) or MultiParticle type (kind 2)
+  double u[3];    // displacement: three rand() draws; rotation: u[0] = angle draw
+  double ax[3];   // rotation axis (PRNG::PickOnUnitSphere, src/PRNG.h:143-151)
+  double pacc;    // Metropolis uniform (Translate::Accept, src/moves/Translate.h:101)
+};
+
+// MoveSettings state (src/MoveSettings.h:28-160) for one box, one kind.
+struct Settings {
+  double scale[2];          // DISPLACE, ROTATE
+  double mp_t_max, mp_r_max;
+  long long tries[3], accepted[3], tempTries[3], tempAccepted[3];
+  long long mp_tries[2], mp_acc[2], mp_itries[2], mp_iacc[2];
+  int singleMoveAccepted;
+  int adj;
+  double amin;              // smallest box edge
+};
+
+// MT19937 (Matsumoto & Nishimura 1998) seeded as MTRand(uint32)
+// (src/MersenneTwister.h:194-230) and the PRNG wrappers the moves draw from
+// (src/PRNG.h:48-170).
+class MT19937 {
+ public:
+  explicit MT19937(uint32_t seed);
+  uint32_t u32();
+  double rand01() { return (double)u32() * (1.0 / 4294967295.0); }
+  double randExc01() { return (double)u32() * (1.0 / 4294967296.0); }
+  uint32_t randInt(uint32_t n);
+
+ private:
+  void reload();
+  uint32_t st_[624];
+  int left_ = 0, next_ = 0;
+};
+
+// Host generator of the move stream of one box (System::PickMove,
+// MolTransformBase::GetBoxAndMol, Coordinates::TranslateRand / RotateRand,
+// MultiParticle::Prep, the Accept draw).
+class MoveStream {
+ public:
+  MoveStream(uint32_t seed, const double frac[3], int n_mol,
+             const std::vector<int> &mol_len);
+  void Next(MoveRec *r);
+
+ private:
+  MT19937 mt_;
+  double perc_[9];
+  int n_mol_;
+  std::vector<int> mol_len_;
+  bool all_single_;
+};
+
+struct McState {
+  gb_mc_params params{};
+  MoveStream *stream = nullptr;
+  int64_t next_step = 0;     // step the stream is positioned at
+  Settings *d_set = nullptr; // device copy of Settings
+  MoveRec *d_moves = nullptr;
+  MoveRec *h_moves = nullptr;  // pinned
+  size_t move_cap = 0;
+  double *d_prop = nullptr;  // per-move proposal (matrix or shift)
+  int *d_trace_i = nullptr;  // kind, mol, acc per step
+  double *d_trace_d = nullptr;
+  size_t trace_cap = 0;
+  double *d_part = nullptr;  // per-CTA partials
+  unsigned *d_bar = nullptr; // grid barrier words
+  double *d_ctx = nullptr;   // per-move context (positions, tables)
+  int grid = 0, kchunk = 0;
+  // MultiParticle buffers (new state)
+  double *d_xn = nullptr, *d_yn = nullptr, *d_zn = nullptr;
+  double *d_cxn = nullptr, *d_cyn = nullptr, *d_czn = nullptr;
+  double *d_aFn = nullptr, *d_mFn = nullptr, *d_aRn = nullptr,
+         *d_mRn = nullptr, *d_tqn = nullptr, *d_tk = nullptr;
+  int *d_inrange = nullptr;
+  double *d_mp = nullptr;    // MultiParticle scalars
+  DevBox cells_new{};        // cell grid of the trial state
+  std::vector<void *> allocs;
+};
+
+int mc_init(Box &b, const gb_mc_params &p);
+int mc_run(Box &b, int64_t first_step, int64_t nsteps, int32_t *kind,
+           int32_t *mol, int32_t *acc, double *de);
+int mc_state(Box &b, double *scales4, int64_t *counts6);
+int mc_run_batch(const std::vector<Box *> &boxes, int64_t first_step,
+                 int64_t nsteps);
+void mc_destroy(Box &b);
+
+}  // namespace gb

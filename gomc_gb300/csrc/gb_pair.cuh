@@ -1,0 +1,80 @@
+// Pair terms and reductions shared by the real-space kernels.
+#pragma once
+
+#include "gb_internal.h"
+
+namespace gb {
+
+// FFParticle::CalcEn for lambda = 1 (src/FFParticle.cpp:295-325); the caller
+// has checked r^2 < Rcut^2.  For n = 12 the (sigma^2/r^2)^6 term is the square
+// of the attractive term instead of pow(), one rounding apart.
+__device__ __forceinline__ double lj_energy(const FF &ff, double distSq,
+                                            int idx) {
+  double rRat2 = ff.sigmaSq[idx] / distSq;
+  double rRat4 = rRat2 * rRat2;
+  double attract = rRat4 * rRat2;
+  double n = ff.nexp[idx];
+  double repulse = (n == 12.0) ? attract * attract : pow(rRat2, n * 0.5);
+  return ff.eps_cn[idx] * (repulse - attract);
+}
+
+// FFParticle::CalcVir for lambda = 1 (src/FFParticle.cpp:344-359)
+__device__ __forceinline__ double lj_virial(const FF &ff, double distSq,
+                                            int idx) {
+  double rNeg2 = 1.0 / distSq;
+  double rRat2 = rNeg2 * ff.sigmaSq[idx];
+  double rRat4 = rRat2 * rRat2;
+  double attract = rRat4 * rRat2;
+  double n = ff.nexp[idx];
+  double repulse = (n == 12.0) ? attract * attract : pow(rRat2, n * 0.5);
+  return ff.eps_cn_6[idx] * (ff.nOver6[idx] * repulse - attract) * rNeg2;
+}
+
+// FFParticle::CalcCoulomb, Ewald real-space term (src/FFParticle.cpp:361-399)
+__device__ __forceinline__ double coulomb_energy(const FF &ff, double distSq,
+                                                 double qq) {
+  if (ff.rcutCoulSq < distSq)
+    return 0.0;
+  double dist = sqrt(distSq);
+  if (ff.ewald) {
+    double val = ff.alpha * dist;
+    return qq * erfc(val) / dist;
+  }
+  return qq / dist;
+}
+
+// FFParticle::CalcCoulombVir (src/FFParticle.cpp:401-446)
+__device__ __forceinline__ double coulomb_virial(const FF &ff, double distSq,
+                                                 double qq) {
+  if (ff.rcutCoulSq < distSq)
+    return 0.0;
+  double dist = sqrt(distSq);
+  if (ff.ewald) {
+    double constValue = ff.alpha * M_2_SQRTPI;
+    double expConstValue = exp(-1.0 * ff.alphaSq * distSq);
+    double temp = 1.0 - erf(ff.alpha * dist);
+    return qq * (temp / dist + constValue * expConstValue) / distSq;
+  }
+  return qq / (distSq * dist);
+}
+
+// Block-wide sum of one double, deterministic order; result valid in thread 0.
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+  for (int o = 16; o > 0; o >>= 1)
+    v += __shfl_down_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0)
+    sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < NT / 32; ++i)
+      r += sh[i];
+  }
+  __syncthreads();
+  return r;
+}
+
+}  // namespace gb

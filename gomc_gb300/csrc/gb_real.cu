@@ -1,0 +1,484 @@
+// Real-space kernels (FP64 plain form):
+//   BoxInter        one CTA per (cell, neighbour) tile, i < j pairs
+//                   (src/CalculateEnergy.cpp:157-266)
+//   MoleculeInter   one CTA per (atom, old/new, neighbour cell)
+//                   (src/CalculateEnergy.cpp:581-686)
+//   ParticleInter   one CTA per (trial, neighbour cell)
+//                   (src/CalculateEnergy.cpp:727-785)
+//   BoxForce        one CTA per (cell, third of the neighbour shell); each
+//                   thread gathers the force on one atom, so no atomics
+//                   (src/CalculateEnergy.cpp:268-406)
+//   MolCorrection   per molecule (src/Ewald.cpp:1056-1085)
+//   CalculateTorque per molecule (src/CalculateEnergy.cpp:1365-1406)
+// Partial sums land in per-CTA slots and a final single-CTA kernel adds them
+// in a fixed order, so every result is reproducible run to run.
+#include "gb_box.h"
+#include "gb_cells.cuh"
+#include "gb_pair.cuh"
+
+namespace gb {
+
+constexpr int RT = 128;  // threads per real-space CTA
+
+// Sum `n` partials of width `w` (stride w) into out[0..w), fixed order.
+__global__ void k_reduce_partials(const double *__restrict__ part, int n, int w,
+                                  double *out, int max_mode) {
+  __shared__ double sh[RT / 32];
+  for (int c = 0; c < w; ++c) {
+    double v = 0.0;
+    if (max_mode && c == w - 1) {
+      for (int i = threadIdx.x; i < n; i += RT)
+        v = fmax(v, part[(size_t)i * w + c]);
+      for (int o = 16; o > 0; o >>= 1)
+        v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+      if ((threadIdx.x & 31) == 0)
+        sh[threadIdx.x >> 5] = v;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double r = 0;
+        for (int i = 0; i < RT / 32; ++i)
+          r = fmax(r, sh[i]);
+        out[c] = r;
+      }
+      __syncthreads();
+      continue;
+    }
+    for (int i = threadIdx.x; i < n; i += RT)
+      v += part[(size_t)i * w + c];
+    double r = block_sum<RT>(v, sh);
+    if (threadIdx.x == 0)
+      out[c] = r;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// BoxInter
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(RT) k_box_inter(DevBox b, const FF *__restrict__ pff,
+                                                  double *part) {
+  extern __shared__ __align__(32) unsigned char smem[];
+  const FF &ff = *pff;
+  int tile = blockIdx.x;
+  int c = tile / NB27, n = tile % NB27;
+  int c2 = b.nbr[c * NB27 + n];
+  int n1 = b.cell_count[c], n2 = b.cell_count[c2];
+  double4_32a *sp = (double4_32a *)smem;
+  int *sm = (int *)(sp + b.cap);
+  int *sa = sm + b.cap;
+  for (int j = threadIdx.x; j < n2; j += RT) {
+    size_t s = (size_t)c2 * b.cap + j;
+    sp[j] = b.cell_pos[s];
+    sm[j] = b.cell_meta[s];
+    sa[j] = b.cell_atom[s];
+  }
+  __syncthreads();
+  double lj = 0.0, re = 0.0;
+  for (int i = threadIdx.x; i < n1; i += RT) {
+    size_t si = (size_t)c * b.cap + i;
+    double4_32a pi = b.cell_pos[si];
+    int mi = b.cell_meta[si], ai = b.cell_atom[si];
+    int moli = meta_mol(mi), ki = meta_kind(mi);
+    for (int j = 0; j < n2; ++j) {
+      int aj = sa[j];
+      int mj = sm[j];
+      if (ai < aj && moli != meta_mol(mj)) {
+        double4_32a pj = sp[j];
+        double dx = min_image(pi.x - pj.x, b.L[0], b.half[0]);
+        double dy = min_image(pi.y - pj.y, b.L[1], b.half[1]);
+        double dz = min_image(pi.z - pj.z, b.L[2], b.half[2]);
+        double distSq = dsq3(dx, dy, dz);
+        if (ff.rcutSq > distSq) {
+          int kj = meta_kind(mj);
+          if (ff.electrostatic) {
+            double qq = pi.w * pj.w * QQ_FACT;
+            if (qq != 0.0)
+              re += coulomb_energy(ff, distSq, qq);
+          }
+          lj += lj_energy(ff, distSq, ki + kj * ff.n_kinds);
+        }
+      }
+    }
+  }
+  __shared__ double red[RT / 32];
+  double a = block_sum<RT>(lj, red);
+  double r = block_sum<RT>(re, red);
+  if (threadIdx.x == 0) {
+    part[2 * tile] = a;
+    part[2 * tile + 1] = r;
+  }
+}
+
+int launch_box_inter(Box &bx, double *d_out2) {
+  DevBox &b = bx.dev;
+  int tiles = b.ncell * NB27;
+  int rc = bx.EnsureScratch((size_t)tiles * 2);
+  if (rc)
+    return rc;
+  size_t sh = (size_t)b.cap * (sizeof(double4_32a) + 2 * sizeof(int));
+  if (sh > 48 * 1024)
+    cudaFuncSetAttribute(k_box_inter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sh);
+  k_box_inter<<<tiles, RT, sh, bx.stream>>>(b, bx.d_ff, bx.d_scratch);
+  k_reduce_partials<<<1, RT, 0, bx.stream>>>(bx.d_scratch, tiles, 2, d_out2, 0);
+  return bx.CudaCheck(cudaGetLastError(), "box inter");
+}
+
+// ---------------------------------------------------------------------------
+// MoleculeInter: unit u = ((atom * 2 + side) * 27 + neighbour)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(RT) k_mol_inter(DevBox b, const FF *__restrict__ pff,
+                                                  int m, const double *__restrict__ newpos,
+                                                  double *part) {
+  const FF &ff = *pff;
+  int u = blockIdx.x;
+  int a = u / (2 * NB27), side = (u / NB27) % 2, n = u % NB27;
+  int atom = b.mstart[m] + a;
+  double px, py, pz;
+  if (side == 0) {
+    px = b.x[atom];
+    py = b.y[atom];
+    pz = b.z[atom];
+  } else {
+    px = newpos[3 * a];
+    py = newpos[3 * a + 1];
+    pz = newpos[3 * a + 2];
+  }
+  int cell = position_to_cell(b, px, py, pz);
+  int c2 = b.nbr[cell * NB27 + n];
+  int n2 = b.cell_count[c2];
+  double qa = b.q[atom];
+  int ka = b.kind[atom];
+  double lj = 0.0, re = 0.0, ovl = 0.0;
+  for (int j = threadIdx.x; j < n2; j += RT) {
+    size_t s = (size_t)c2 * b.cap + j;
+    int mj = b.cell_meta[s];
+    if (meta_mol(mj) == m)
+      continue;  // the moving molecule is out of the cell list
+    double4_32a pj = b.cell_pos[s];
+    double dx = min_image(px - pj.x, b.L[0], b.half[0]);
+    double dy = min_image(py - pj.y, b.L[1], b.half[1]);
+    double dz = min_image(pz - pj.z, b.L[2], b.half[2]);
+    double distSq = dsq3(dx, dy, dz);
+    if (ff.rcutSq > distSq) {
+      if (side == 1 && distSq < ff.rcutLowSq)
+        ovl = 1.0;
+      double e = 0.0;
+      if (ff.electrostatic) {
+        double qq = qa * pj.w * QQ_FACT;
+        if (qq != 0.0)
+          e = coulomb_energy(ff, distSq, qq);
+      }
+      double l = lj_energy(ff, distSq, ka + meta_kind(mj) * ff.n_kinds);
+      if (side == 0) {
+        re += -e;
+        lj += -l;
+      } else {
+        re += e;
+        lj += l;
+      }
+    }
+  }
+  __shared__ double red[RT / 32];
+  double A = block_sum<RT>(lj, red);
+  double R = block_sum<RT>(re, red);
+  double O = block_sum<RT>(ovl, red);
+  if (threadIdx.x == 0) {
+    part[3 * u] = A;
+    part[3 * u + 1] = R;
+    part[3 * u + 2] = O > 0 ? 1.0 : 0.0;
+  }
+}
+
+int launch_mol_inter(Box &bx, int m, const double *d_newpos, double *d_out3) {
+  int na = bx.host.mstart[m + 1] - bx.host.mstart[m];
+  int units = na * 2 * NB27;
+  int rc = bx.EnsureScratch((size_t)units * 3);
+  if (rc)
+    return rc;
+  k_mol_inter<<<units, RT, 0, bx.stream>>>(bx.dev, bx.d_ff, m, d_newpos,
+                                           bx.d_scratch);
+  k_reduce_partials<<<1, RT, 0, bx.stream>>>(bx.d_scratch, units, 3, d_out3, 1);
+  return bx.CudaCheck(cudaGetLastError(), "molecule inter");
+}
+
+// ---------------------------------------------------------------------------
+// ParticleInter: unit u = trial * 27 + neighbour; atoms of molecule m are
+// treated as absent from the cell list (the molecule being grown).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(RT) k_particle_inter(DevBox b, const FF *__restrict__ pff,
+                                                       int m, int ka, double qa,
+                                                       const double *__restrict__ trials,
+                                                       double *part) {
+  const FF &ff = *pff;
+  int u = blockIdx.x;
+  int t = u / NB27, n = u % NB27;
+  double px = trials[3 * t], py = trials[3 * t + 1], pz = trials[3 * t + 2];
+  int cell = position_to_cell(b, px, py, pz);
+  int c2 = b.nbr[cell * NB27 + n];
+  int n2 = b.cell_count[c2];
+  double lj = 0.0, re = 0.0, ovl = 0.0;
+  for (int j = threadIdx.x; j < n2; j += RT) {
+    size_t s = (size_t)c2 * b.cap + j;
+    int mj = b.cell_meta[s];
+    if (meta_mol(mj) == m)
+      continue;
+    double4_32a pj = b.cell_pos[s];
+    double dx = min_image(px - pj.x, b.L[0], b.half[0]);
+    double dy = min_image(py - pj.y, b.L[1], b.half[1]);
+    double dz = min_image(pz - pj.z, b.L[2], b.half[2]);
+    double distSq = dsq3(dx, dy, dz);
+    if (ff.rcutSq > distSq) {
+      if (distSq < ff.rcutLowSq)
+        ovl = 1.0;
+      lj += lj_energy(ff, distSq, ka + meta_kind(mj) * ff.n_kinds);
+      if (ff.electrostatic) {
+        double qq = pj.w * qa * QQ_FACT;
+        if (qq != 0.0)
+          re += coulomb_energy(ff, distSq, qq);
+      }
+    }
+  }
+  __shared__ double red[RT / 32];
+  double A = block_sum<RT>(lj, red);
+  double R = block_sum<RT>(re, red);
+  double O = block_sum<RT>(ovl, red);
+  if (threadIdx.x == 0) {
+    part[3 * u] = A;
+    part[3 * u + 1] = R;
+    part[3 * u + 2] = O > 0 ? 1.0 : 0.0;
+  }
+}
+
+__global__ void k_reduce_trials(const double *__restrict__ part, int ntrials,
+                                double *out) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntrials)
+    return;
+  double a = 0, r = 0, o = 0;
+  for (int n = 0; n < NB27; ++n) {
+    const double *p = part + 3 * ((size_t)t * NB27 + n);
+    a += p[0];
+    r += p[1];
+    o = fmax(o, p[2]);
+  }
+  out[3 * t] = a;
+  out[3 * t + 1] = r;
+  out[3 * t + 2] = o;
+}
+
+int launch_particle_inter(Box &bx, int m, int kind, double charge,
+                          const double *d_trials, int ntrials, double *d_out) {
+  int units = ntrials * NB27;
+  int rc = bx.EnsureScratch((size_t)units * 3);
+  if (rc)
+    return rc;
+  k_particle_inter<<<units, RT, 0, bx.stream>>>(bx.dev, bx.d_ff, m, kind, charge,
+                                                d_trials, bx.d_scratch);
+  k_reduce_trials<<<(ntrials + 127) / 128, 128, 0, bx.stream>>>(bx.d_scratch,
+                                                               ntrials, d_out);
+  return bx.CudaCheck(cudaGetLastError(), "particle inter");
+}
+
+// ---------------------------------------------------------------------------
+// Ewald intramolecular correction, one thread per molecule
+// ---------------------------------------------------------------------------
+__global__ void k_correction(DevBox b, const FF *__restrict__ pff, double *part) {
+  const FF &ff = *pff;
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  double corr = 0.0;
+  if (m < b.n_mol) {
+    int a0 = b.mstart[m], n = b.mstart[m + 1] - a0;
+    for (int i = 0; i < n; i++) {
+      if (fabs(b.q[a0 + i]) < 0.000000001)
+        continue;
+      for (int j = i + 1; j < n; j++) {
+        int p = a0 + i, q = a0 + j;
+        double dx = min_image(b.x[p] - b.x[q], b.L[0], b.half[0]);
+        double dy = min_image(b.y[p] - b.y[q], b.L[1], b.half[1]);
+        double dz = min_image(b.z[p] - b.z[q], b.L[2], b.half[2]);
+        double distSq = dsq3(dx, dy, dz);
+        double dist = sqrt(distSq);
+        corr += (b.q[p] * b.q[q] * erf(ff.alpha * dist) / dist);
+      }
+    }
+    corr = -1.0 * QQ_FACT * corr;
+  }
+  __shared__ double red[RT / 32];
+  double s = block_sum<RT>(corr, red);
+  if (threadIdx.x == 0)
+    part[blockIdx.x] = s;
+}
+
+int launch_correction(Box &bx, double *d_out) {
+  int nb = (bx.dev.n_mol + RT - 1) / RT;
+  int rc = bx.EnsureScratch(nb);
+  if (rc)
+    return rc;
+  k_correction<<<nb, RT, 0, bx.stream>>>(bx.dev, bx.d_ff, bx.d_scratch);
+  k_reduce_partials<<<1, RT, 0, bx.stream>>>(bx.d_scratch, nb, 1, d_out, 0);
+  return bx.CudaCheck(cudaGetLastError(), "correction");
+}
+
+// ---------------------------------------------------------------------------
+// BoxForce: CTA (cell c, group g of 9 neighbour cells); thread = atom of c.
+// Energies count each pair once (i < j); forces gather every pair.
+// ---------------------------------------------------------------------------
+constexpr int FG = 3;  // neighbour-shell groups
+__global__ void __launch_bounds__(RT) k_box_force(DevBox b, const FF *__restrict__ pff,
+                                                  double *fpart, double *epart) {
+  extern __shared__ __align__(32) unsigned char smem[];
+  const FF &ff = *pff;
+  int c = blockIdx.x, g = blockIdx.y;
+  int n1 = b.cell_count[c];
+  double4_32a *sp = (double4_32a *)smem;
+  int *sm = (int *)(sp + b.cap);
+  int *sa = sm + b.cap;
+  double lj = 0.0, re = 0.0;
+  // each thread owns up to ceil(n1 / RT) atoms; loop per owned atom
+  for (int base = 0; base < n1; base += RT) {
+    int i = base + threadIdx.x;
+    bool own = i < n1;
+    double4_32a pi = make_double4_32a(0, 0, 0, 0);
+    int mi = 0, ai = -1;
+    if (own) {
+      size_t si = (size_t)c * b.cap + i;
+      pi = b.cell_pos[si];
+      mi = b.cell_meta[si];
+      ai = b.cell_atom[si];
+    }
+    double fx = 0, fy = 0, fz = 0;
+    for (int nn = g * (NB27 / FG); nn < (g + 1) * (NB27 / FG); ++nn) {
+      int c2 = b.nbr[c * NB27 + nn];
+      int n2 = b.cell_count[c2];
+      __syncthreads();
+      for (int j = threadIdx.x; j < n2; j += RT) {
+        size_t s = (size_t)c2 * b.cap + j;
+        sp[j] = b.cell_pos[s];
+        sm[j] = b.cell_meta[s];
+        sa[j] = b.cell_atom[s];
+      }
+      __syncthreads();
+      if (!own)
+        continue;
+      int moli = meta_mol(mi), ki = meta_kind(mi);
+      for (int j = 0; j < n2; ++j) {
+        int mj = sm[j];
+        if (moli == meta_mol(mj))
+          continue;
+        double4_32a pj = sp[j];
+        double dx = min_image(pi.x - pj.x, b.L[0], b.half[0]);
+        double dy = min_image(pi.y - pj.y, b.L[1], b.half[1]);
+        double dz = min_image(pi.z - pj.z, b.L[2], b.half[2]);
+        double distSq = dsq3(dx, dy, dz);
+        if (ff.rcutSq > distSq) {
+          int idx = ki + meta_kind(mj) * ff.n_kinds;
+          double fR = 0.0;
+          bool hasR = false;
+          if (ff.electrostatic) {
+            double qq = pi.w * pj.w * QQ_FACT;
+            if (qq != 0.0) {
+              if (ai < sa[j])
+                re += coulomb_energy(ff, distSq, qq);
+              fR = coulomb_virial(ff, distSq, qq);
+              hasR = true;
+            }
+          }
+          if (ai < sa[j])
+            lj += lj_energy(ff, distSq, idx);
+          double fL = lj_virial(ff, distSq, idx);
+          fx += dx * fL + (hasR ? dx * fR : 0.0);
+          fy += dy * fL + (hasR ? dy * fR : 0.0);
+          fz += dz * fL + (hasR ? dz * fR : 0.0);
+        }
+      }
+    }
+    if (own) {
+      double *f = fpart + ((size_t)g * b.n_atoms + ai) * 3;
+      f[0] = fx;
+      f[1] = fy;
+      f[2] = fz;
+    }
+  }
+  __shared__ double red[RT / 32];
+  double A = block_sum<RT>(lj, red);
+  double R = block_sum<RT>(re, red);
+  if (threadIdx.x == 0) {
+    size_t t = (size_t)c * FG + g;
+    epart[2 * t] = A;
+    epart[2 * t + 1] = R;
+  }
+}
+
+__global__ void k_force_gather(DevBox b, const double *__restrict__ fpart,
+                               double *aF, double *mF) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= b.n_mol)
+    return;
+  double mx = 0, my = 0, mz = 0;
+  for (int a = b.mstart[m]; a < b.mstart[m + 1]; ++a) {
+    double f[3] = {0, 0, 0};
+    for (int g = 0; g < FG; ++g)
+      for (int d = 0; d < 3; ++d)
+        f[d] += fpart[((size_t)g * b.n_atoms + a) * 3 + d];
+    for (int d = 0; d < 3; ++d)
+      aF[3 * (size_t)a + d] = f[d];
+    mx += f[0];
+    my += f[1];
+    mz += f[2];
+  }
+  mF[3 * (size_t)m] = mx;
+  mF[3 * (size_t)m + 1] = my;
+  mF[3 * (size_t)m + 2] = mz;
+}
+
+int launch_box_force(Box &bx, const DevBox &b, double *aF, double *mF,
+                     double *d_out2) {
+  size_t need = (size_t)FG * b.n_atoms * 3 + (size_t)b.ncell * FG * 2;
+  int rc = bx.EnsureScratch(need);
+  if (rc)
+    return rc;
+  double *fpart = bx.d_scratch;
+  double *epart = fpart + (size_t)FG * b.n_atoms * 3;
+  size_t sh = (size_t)b.cap * (sizeof(double4_32a) + 2 * sizeof(int));
+  if (sh > 48 * 1024)
+    cudaFuncSetAttribute(k_box_force, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sh);
+  k_box_force<<<dim3(b.ncell, FG), RT, sh, bx.stream>>>(b, bx.d_ff, fpart, epart);
+  k_force_gather<<<(b.n_mol + 127) / 128, 128, 0, bx.stream>>>(b, fpart, aF,
+                                                              mF);
+  k_reduce_partials<<<1, RT, 0, bx.stream>>>(epart, b.ncell * FG, 2, d_out2, 0);
+  return bx.CudaCheck(cudaGetLastError(), "box force");
+}
+
+// ---------------------------------------------------------------------------
+// CalculateTorque: molecule torque from atom forces (real + reciprocal)
+// ---------------------------------------------------------------------------
+__global__ void k_torque(DevBox b, const double *__restrict__ aF,
+                         const double *__restrict__ aR, double *tq) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= b.n_mol)
+    return;
+  double tx = 0, ty = 0, tz = 0;
+  for (int p = b.mstart[m]; p < b.mstart[m + 1]; ++p) {
+    double d0 = min_image(b.x[p] - b.cx[m], b.L[0], b.half[0]);
+    double d1 = min_image(b.y[p] - b.cy[m], b.L[1], b.half[1]);
+    double d2 = min_image(b.z[p] - b.cz[m], b.L[2], b.half[2]);
+    double f0 = aF[3 * (size_t)p] + aR[3 * (size_t)p];
+    double f1 = aF[3 * (size_t)p + 1] + aR[3 * (size_t)p + 1];
+    double f2 = aF[3 * (size_t)p + 2] + aR[3 * (size_t)p + 2];
+    tx += d1 * f2 - d2 * f1;
+    ty += d2 * f0 - d0 * f2;
+    tz += d0 * f1 - d1 * f0;
+  }
+  tq[3 * (size_t)m] = tx;
+  tq[3 * (size_t)m + 1] = ty;
+  tq[3 * (size_t)m + 2] = tz;
+}
+
+int launch_torque(Box &bx, const DevBox &d, const double *aF,
+                  const double *aR, double *tq) {
+  k_torque<<<(d.n_mol + 127) / 128, 128, 0, bx.stream>>>(d, aF, aR, tq);
+  return bx.CudaCheck(cudaGetLastError(), "torque");
+}
+
+}  // namespace gb

@@ -1,0 +1,402 @@
+// Ewald reciprocal-space kernels (FP64 plain form).
+//
+//   structure factor  sumR/I[k] = sum_j q_j {cos, sin}(k . r_j)
+//                     (Ewald::BoxReciprocalSetup/Sums, src/Ewald.cpp:193-361)
+//   energy            sum_k prefact_k (sumR^2 + sumI^2)
+//                     (Ewald::BoxReciprocal, src/Ewald.cpp:375-406)
+//   molecule delta    sumNew = sumRef + new - old, energy difference
+//                     (Ewald::MolReciprocal, src/Ewald.cpp:409-473) and the
+//                     insert / delete deltas (SwapDestRecip / SwapSourceRecip,
+//                     src/Ewald.cpp:478-531, 657-710)
+//   reciprocal force  (Ewald::BoxForceReciprocal, src/Ewald.cpp:1496-1596)
+//
+// The full-box kernels evaluate exp(i k.r) as a product of per-axis phase
+// factors exp(i n_x t_x) exp(i n_y t_y) exp(i n_z t_z), t = 2 pi r / L, held
+// per atom in shared memory; each CTA owns a chunk of k-vectors and one
+// chunk of atoms, and chunk partials are added in a fixed order.
+#include "gb_box.h"
+#include "gb_pair.cuh"
+
+namespace gb {
+
+constexpr int KT = 256;     // threads per reciprocal CTA
+constexpr int KPT = 2;      // k-vectors per thread
+constexpr int TA = 16;      // atoms per shared-memory tile
+constexpr int NCH_MAX = 32; // atom chunks
+
+struct Phase {
+  double2 *e;  // [atoms][3][kmax + 1]
+  int stride;  // kmax + 1
+};
+
+// exp(i n t) for n = 0..kmax by recurrence from exp(i t).
+__device__ __forceinline__ void phase_row(double2 *row, double t, int kmax) {
+  double s, c;
+  sincos(t, &s, &c);
+  double2 e = make_double2(1.0, 0.0);
+  row[0] = e;
+  for (int n = 1; n <= kmax; ++n) {
+    double re = e.x * c - e.y * s;
+    double im = e.x * s + e.y * c;
+    e = make_double2(re, im);
+    row[n] = e;
+  }
+}
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 pick(const double2 *row, int n) {
+  double2 v = row[n < 0 ? -n : n];
+  if (n < 0)
+    v.y = -v.y;
+  return v;
+}
+
+__global__ void __launch_bounds__(KT) k_recip_sums(DevBox b, const double *__restrict__ X,
+                                                   const double *__restrict__ Y,
+                                                   const double *__restrict__ Z,
+                                                   int nch, double *part) {
+  extern __shared__ double2 tab[];
+  __shared__ double qs[TA];
+  int stride = b.kmax + 1;
+  int k0 = blockIdx.x * KT * KPT;
+  int ch = blockIdx.y;
+  int a_begin = (int)((long long)b.n_atoms * ch / nch);
+  int a_end = (int)((long long)b.n_atoms * (ch + 1) / nch);
+  char4 kn[KPT];
+  double sR[KPT], sI[KPT];
+  for (int t = 0; t < KPT; ++t) {
+    int k = k0 + t * KT + threadIdx.x;
+    kn[t] = k < b.K ? b.kn[k] : make_char4(0, 0, 0, 0);
+    sR[t] = 0.0;
+    sI[t] = 0.0;
+  }
+  double cv[3];
+  for (int d = 0; d < 3; ++d) {
+    cv[d] = 1.0 / b.L[d];
+    cv[d] *= 2.0 * M_PI;
+  }
+  for (int a0 = a_begin; a0 < a_end; a0 += TA) {
+    int na = min(TA, a_end - a0);
+    __syncthreads();
+    if (threadIdx.x < na * 3) {
+      int a = threadIdx.x / 3, d = threadIdx.x % 3;
+      int atom = a0 + a;
+      double coord = d == 0 ? X[atom] : d == 1 ? Y[atom] : Z[atom];
+      phase_row(tab + (a * 3 + d) * stride, cv[d] * coord, b.kmax);
+    }
+    if (threadIdx.x < na) {
+      double q = b.q[a0 + threadIdx.x];
+      qs[threadIdx.x] = fabs(q) < 0.000000001 ? 0.0 : q;
+    }
+    __syncthreads();
+    for (int a = 0; a < na; ++a) {
+      double q = qs[a];
+      if (q == 0.0)
+        continue;
+      const double2 *ex = tab + (a * 3 + 0) * stride;
+      const double2 *ey = tab + (a * 3 + 1) * stride;
+      const double2 *ez = tab + (a * 3 + 2) * stride;
+#pragma unroll
+      for (int t = 0; t < KPT; ++t) {
+        double2 e = cmul(cmul(ex[kn[t].x], pick(ey, kn[t].y)), pick(ez, kn[t].z));
+        sR[t] += q * e.x;
+        sI[t] += q * e.y;
+      }
+    }
+  }
+  for (int t = 0; t < KPT; ++t) {
+    int k = k0 + t * KT + threadIdx.x;
+    if (k < b.K) {
+      part[((size_t)ch * b.K + k) * 2] = sR[t];
+      part[((size_t)ch * b.K + k) * 2 + 1] = sI[t];
+    }
+  }
+}
+
+__global__ void k_recip_chunk_sum(int K, int nch, const double *__restrict__ part,
+                                  double *sumR, double *sumI) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K)
+    return;
+  double r = 0.0, i = 0.0;
+  for (int c = 0; c < nch; ++c) {
+    r += part[((size_t)c * K + k) * 2];
+    i += part[((size_t)c * K + k) * 2 + 1];
+  }
+  sumR[k] = r;
+  sumI[k] = i;
+}
+
+static int recip_chunks(const Box &bx) {
+  int kb = (bx.dev.K + KT * KPT - 1) / (KT * KPT);
+  int want = (4 * bx.sm_count + kb - 1) / kb;
+  int nch = std::max(1, std::min(NCH_MAX, want));
+  int maxch = std::max(1, bx.dev.n_atoms / TA);
+  return std::min(nch, maxch);
+}
+
+int launch_recip_sums(Box &bx, const double *x, const double *y,
+                      const double *z, double *sumR, double *sumI) {
+  DevBox &b = bx.dev;
+  int nch = recip_chunks(bx);
+  int rc = bx.EnsureScratch((size_t)nch * b.K * 2);
+  if (rc)
+    return rc;
+  int kb = (b.K + KT * KPT - 1) / (KT * KPT);
+  size_t sh = (size_t)TA * 3 * (b.kmax + 1) * sizeof(double2) + 16;
+  if (sh > 48 * 1024)
+    cudaFuncSetAttribute(k_recip_sums, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sh);
+  k_recip_sums<<<dim3(kb, nch), KT, sh, bx.stream>>>(b, x, y, z, nch,
+                                                     bx.d_scratch);
+  k_recip_chunk_sum<<<(b.K + 255) / 256, 256, 0, bx.stream>>>(
+      b.K, nch, bx.d_scratch, sumR, sumI);
+  return bx.CudaCheck(cudaGetLastError(), "recip sums");
+}
+
+// ---------------------------------------------------------------------------
+// Energy of a set of structure factors
+// ---------------------------------------------------------------------------
+constexpr int ET = 256;
+__global__ void k_recip_energy(DevBox b, const double *__restrict__ sR,
+                               const double *__restrict__ sI, double *part) {
+  int k = blockIdx.x * ET + threadIdx.x;
+  double e = 0.0;
+  if (k < b.K)
+    e = ((sR[k] * sR[k] + sI[k] * sI[k]) * b.prefact[k]);
+  __shared__ double red[ET / 32];
+  double s = block_sum<ET>(e, red);
+  if (threadIdx.x == 0)
+    part[blockIdx.x] = s;
+}
+
+__global__ void k_sum_in_order(const double *__restrict__ part, int n,
+                               const double *sub, double *out) {
+  __shared__ double red[ET / 32];
+  double v = 0.0;
+  for (int i = threadIdx.x; i < n; i += ET)
+    v += part[i];
+  double s = block_sum<ET>(v, red);
+  if (threadIdx.x == 0)
+    out[0] = sub ? s - sub[0] : s;
+}
+
+int launch_recip_energy(Box &bx, const double *sumR, const double *sumI,
+                        double *d_out) {
+  DevBox &b = bx.dev;
+  int nb = (b.K + ET - 1) / ET;
+  int rc = bx.EnsureScratch(nb);
+  if (rc)
+    return rc;
+  k_recip_energy<<<nb, ET, 0, bx.stream>>>(b, sumR, sumI, bx.d_scratch);
+  k_sum_in_order<<<1, ET, 0, bx.stream>>>(bx.d_scratch, nb, nullptr, d_out);
+  return bx.CudaCheck(cudaGetLastError(), "recip energy");
+}
+
+// ---------------------------------------------------------------------------
+// One-molecule delta.  mode 0: displacement/rotation (new - old),
+// 1: insertion (+ new), 2: deletion (- given positions).  One thread per k,
+// with the reference's dot-product phases.
+// ---------------------------------------------------------------------------
+__global__ void k_mol_recip(DevBox b, int m, const double *__restrict__ newpos,
+                            int mode, double *part) {
+  int k = blockIdx.x * ET + threadIdx.x;
+  double e = 0.0;
+  if (k < b.K) {
+    int a0 = b.mstart[m], n = b.mstart[m + 1] - a0;
+    double kx = b.kx[k], ky = b.ky[k], kz = b.kz[k];
+    double rN = 0, iN = 0, rO = 0, iO = 0;
+    for (int p = 0; p < n; ++p) {
+      int a = a0 + p;
+      double q = b.q[a];
+      if (fabs(q) < 0.000000001)
+        continue;
+      double dn = (newpos[3 * p] * kx + newpos[3 * p + 1] * ky +
+                   newpos[3 * p + 2] * kz);
+      double s, c;
+      sincos(dn, &s, &c);
+      rN += q * c;
+      iN += q * s;
+      if (mode == 0) {
+        double dold = (b.x[a] * kx + b.y[a] * ky + b.z[a] * kz);
+        sincos(dold, &s, &c);
+        rO += q * c;
+        iO += q * s;
+      }
+    }
+    double sr, si;
+    if (mode == 0) {
+      sr = b.sumRref[k] + 1.0 * (rN - rO);
+      si = b.sumIref[k] + 1.0 * (iN - iO);
+    } else if (mode == 1) {
+      sr = b.sumRref[k] + rN;
+      si = b.sumIref[k] + iN;
+    } else {
+      sr = b.sumRref[k] - rN;
+      si = b.sumIref[k] - iN;
+    }
+    b.sumRnew[k] = sr;
+    b.sumInew[k] = si;
+    e = (sr * sr + si * si) * b.prefact[k];
+  }
+  __shared__ double red[ET / 32];
+  double s = block_sum<ET>(e, red);
+  if (threadIdx.x == 0)
+    part[blockIdx.x] = s;
+}
+
+int launch_mol_recip(Box &bx, int m, const double *d_newpos, int mode,
+                     double *d_out) {
+  DevBox &b = bx.dev;
+  int nb = (b.K + ET - 1) / ET;
+  int rc = bx.EnsureScratch(nb);
+  if (rc)
+    return rc;
+  k_mol_recip<<<nb, ET, 0, bx.stream>>>(b, m, d_newpos, mode, bx.d_scratch);
+  // energyRecipNew - sysPotRef.boxEnergy[box].recip
+  k_sum_in_order<<<1, ET, 0, bx.stream>>>(bx.d_scratch, nb, b.energy + 2, d_out);
+  return bx.CudaCheck(cudaGetLastError(), "mol recip");
+}
+
+// ---------------------------------------------------------------------------
+// Reciprocal force on every atom, with the intramolecular erf correction.
+// CTA = 64 atoms x one quarter of the k-vectors; thread = atom.
+// ---------------------------------------------------------------------------
+constexpr int FA = 64;      // atoms per CTA
+constexpr int FK = 128;     // k-vectors staged per step
+constexpr int FKS = 4;      // k splits
+__global__ void __launch_bounds__(FA) k_force_recip(DevBox b, const FF *__restrict__ pff,
+                                                    const double *__restrict__ sR,
+                                                    const double *__restrict__ sI,
+                                                    double *fpart) {
+  extern __shared__ double2 tab[];
+  const FF &ff = *pff;
+  int stride = b.kmax + 1;
+  int pad = 3 * stride + 1;  // per-atom table stride (odd) against conflicts
+  double2 *ktab = tab + (size_t)FA * pad;
+  double *kxs = (double *)ktab;
+  double *kys = kxs + FK, *kzs = kys + FK, *pfs = kzs + FK, *srs = pfs + FK,
+         *sis = srs + FK;
+  char4 *kns = (char4 *)(sis + FK);
+  int a = blockIdx.x * FA + threadIdx.x;
+  bool own = a < b.n_atoms;
+  double cv[3];
+  for (int d = 0; d < 3; ++d) {
+    cv[d] = 1.0 / b.L[d];
+    cv[d] *= 2.0 * M_PI;
+  }
+  double q = 0.0, FX = 0.0, FY = 0.0, FZ = 0.0;
+  double2 *my = tab + (size_t)threadIdx.x * pad;
+  if (own) {
+    q = b.q[a];
+    phase_row(my, cv[0] * b.x[a], b.kmax);
+    phase_row(my + stride, cv[1] * b.y[a], b.kmax);
+    phase_row(my + 2 * stride, cv[2] * b.z[a], b.kmax);
+    if (blockIdx.y == 0 && fabs(q) >= 0.000000001 && ff.ewald) {
+      // intramolecular correction (src/Ewald.cpp:1556-1575)
+      double constValue = ff.alpha * M_2_SQRTPI;
+      int m = b.mol[a];
+      for (int j = b.mstart[m]; j < b.mstart[m + 1]; j++) {
+        if (j == a)
+          continue;
+        double dx = min_image(b.x[a] - b.x[j], b.L[0], b.half[0]);
+        double dy = min_image(b.y[a] - b.y[j], b.L[1], b.half[1]);
+        double dz = min_image(b.z[a] - b.z[j], b.L[2], b.half[2]);
+        double distSq = dsq3(dx, dy, dz);
+        double dist = sqrt(distSq);
+        double expConstValue = exp(-1.0 * ff.alphaSq * distSq);
+        double qiqj = q * b.q[j] * QQ_FACT;
+        double intraForce = qiqj * 1.0 * 1.0 / distSq;
+        intraForce *= ((erf(ff.alpha * dist) / dist) - constValue * expConstValue);
+        FX -= intraForce * dx;
+        FY -= intraForce * dy;
+        FZ -= intraForce * dz;
+      }
+    }
+  }
+  bool charged = own && fabs(q) >= 0.000000001 && ff.ewald;
+  int kper = (b.K + FKS - 1) / FKS;
+  int kbeg = blockIdx.y * kper, kend = min(b.K, kbeg + kper);
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  for (int k0 = kbeg; k0 < kend; k0 += FK) {
+    int nk = min(FK, kend - k0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nk; i += FA) {
+      int k = k0 + i;
+      kxs[i] = b.kx[k];
+      kys[i] = b.ky[k];
+      kzs[i] = b.kz[k];
+      pfs[i] = b.prefact[k];
+      srs[i] = sR[k];
+      sis[i] = sI[k];
+      kns[i] = b.kn[k];
+    }
+    __syncthreads();
+    if (!charged)
+      continue;
+    for (int i = 0; i < nk; ++i) {
+      char4 n = kns[i];
+      double2 e = cmul(cmul(my[n.x], pick(my + stride, n.y)),
+                       pick(my + 2 * stride, n.z));
+      double factor = 2.0 * q * pfs[i] * 1.0 * (e.y * srs[i] - e.x * sis[i]);
+      fx += factor * kxs[i];
+      fy += factor * kys[i];
+      fz += factor * kzs[i];
+    }
+  }
+  if (own) {
+    double *f = fpart + ((size_t)blockIdx.y * b.n_atoms + a) * 3;
+    f[0] = fx + (blockIdx.y == 0 ? FX : 0.0);
+    f[1] = fy + (blockIdx.y == 0 ? FY : 0.0);
+    f[2] = fz + (blockIdx.y == 0 ? FZ : 0.0);
+  }
+}
+
+__global__ void k_force_recip_gather(DevBox b, const double *__restrict__ fpart,
+                                     double *aR, double *mR) {
+  int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= b.n_mol)
+    return;
+  double mx = 0, my = 0, mz = 0;
+  for (int a = b.mstart[m]; a < b.mstart[m + 1]; ++a) {
+    double f[3] = {0, 0, 0};
+    for (int s = 0; s < FKS; ++s)
+      for (int d = 0; d < 3; ++d)
+        f[d] += fpart[((size_t)s * b.n_atoms + a) * 3 + d];
+    for (int d = 0; d < 3; ++d)
+      aR[3 * (size_t)a + d] = f[d];
+    mx += f[0];
+    my += f[1];
+    mz += f[2];
+  }
+  mR[3 * (size_t)m] = mx;
+  mR[3 * (size_t)m + 1] = my;
+  mR[3 * (size_t)m + 2] = mz;
+}
+
+int launch_force_recip(Box &bx, const DevBox &b, const double *sumR,
+                       const double *sumI, double *aR, double *mR) {
+  if (!bx.cfg.ewald) {
+    cudaMemsetAsync(aR, 0, (size_t)b.n_atoms * 24, bx.stream);
+    cudaMemsetAsync(mR, 0, (size_t)b.n_mol * 24, bx.stream);
+    return bx.CudaCheck(cudaGetLastError(), "force recip");
+  }
+  int rc = bx.EnsureScratch((size_t)FKS * b.n_atoms * 3);
+  if (rc)
+    return rc;
+  int pad = 3 * (b.kmax + 1) + 1;
+  size_t sh = (size_t)FA * pad * sizeof(double2) + (size_t)FK * (6 * 8 + 4);
+  if (sh > 48 * 1024)
+    cudaFuncSetAttribute(k_force_recip, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sh);
+  dim3 grid((b.n_atoms + FA - 1) / FA, FKS);
+  k_force_recip<<<grid, FA, sh, bx.stream>>>(b, bx.d_ff, sumR, sumI,
+                                             bx.d_scratch);
+  k_force_recip_gather<<<(b.n_mol + 127) / 128, 128, 0, bx.stream>>>(
+      b, bx.d_scratch, aR, mR);
+  return bx.CudaCheck(cudaGetLastError(), "force recip");
+}
+
+}  // namespace gb

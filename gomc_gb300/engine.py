@@ -1,0 +1,376 @@
+"""Python host layer over the C ABI.
+
+:class:`Box` owns one resident GB300 machine.  :class:`CalculateEnergy`,
+:class:`Ewald` and :class:`CellList` expose the same method names and
+argument meaning as the reference classes (src/CalculateEnergy.h:48-293,
+src/Ewald.h:46-228, src/CellList.h:22-86) on top of a Box, so code written
+against the reference's interfaces reads the same here.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import GB_FP64, GB_MIXED, check, lib
+
+ENERGY_TERMS = ["inter", "real", "recip", "self", "correction",
+                "tailCorrection", "intraBond", "intraNonbond", "total"]
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class Box:
+    """One orthogonal periodic box resident on one GPU."""
+
+    def __init__(self, sysm, cfg, device: int = 0,
+                 precision: Optional[int] = None):
+        L = lib()
+        self.sysm = sysm
+        self.cfg = cfg
+        self.n_atoms = sysm.n_atoms
+        self.n_mol = sysm.n_mol
+        self.mol_start = np.ascontiguousarray(sysm.mol_start, dtype=np.int32)
+        self._keep = [np.ascontiguousarray(sysm.pos, dtype=np.float64),
+                      np.ascontiguousarray(sysm.atom_kind, dtype=np.int32),
+                      np.ascontiguousarray(sysm.atom_charge, dtype=np.float64),
+                      self.mol_start,
+                      np.array([k.epsilon for k in sysm.kinds], np.float64),
+                      np.array([k.sigma for k in sysm.kinds], np.float64),
+                      np.array([k.n for k in sysm.kinds], np.float64)]
+        pos, kind, q, ms, eps, sig, nex = self._keep
+        d = _lib.SystemDesc()
+        d.n_atoms, d.n_mol, d.n_kinds = self.n_atoms, self.n_mol, len(sysm.kinds)
+        d.pos, d.atom_kind, d.atom_charge, d.mol_start = _dp(pos), _ip(kind), \
+            _dp(q), _ip(ms)
+        d.kind_epsilon, d.kind_sigma, d.kind_n = _dp(eps), _dp(sig), _dp(nex)
+        for i in range(3):
+            d.box[i] = float(sysm.box[i])
+        c = _lib.Config()
+        c.temperature = cfg.temperature
+        c.rcut = cfg.rcut
+        c.rcut_low = cfg.rcut_low
+        c.rcut_coulomb = cfg.rcut_coulomb_value
+        c.tolerance = cfg.tolerance
+        c.ewald = int(cfg.ewald)
+        c.electrostatic = int(cfg.electrostatic)
+        if precision is None:
+            precision = GB_MIXED if getattr(cfg, "precision", "fp64") == "mixed" \
+                else GB_FP64
+        c.precision = precision
+        c.device = device
+        h = C.c_void_p()
+        rc = L.gb_box_create(C.byref(d), C.byref(c), C.byref(h))
+        if rc != 0:
+            raise _lib.GbError(rc, (L.gb_last_error(None) or b"").decode())
+        self.h = h
+        self.precision = precision
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            lib().gb_box_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _chk(self, rc: int) -> None:
+        check(rc, self.h)
+
+    def mol_atoms(self, m: int) -> int:
+        return int(self.mol_start[m + 1] - self.mol_start[m])
+
+    # ---- energies ---------------------------------------------------------
+    def system_total(self) -> dict:
+        o = np.empty(9)
+        self._chk(lib().gb_system_total(self.h, _dp(o)))
+        return dict(zip(ENERGY_TERMS, o.tolist()))
+
+    def box_inter(self):
+        a, b = C.c_double(), C.c_double()
+        self._chk(lib().gb_box_inter(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def molecule_inter(self, m: int, new_pos):
+        p = np.ascontiguousarray(new_pos, dtype=np.float64).reshape(-1, 3)
+        if p.shape[0] != self.mol_atoms(m):
+            raise ValueError("new_pos must hold every atom of the molecule")
+        a, b, o = C.c_double(), C.c_double(), C.c_int32()
+        self._chk(lib().gb_molecule_inter(self.h, int(m), _dp(p), C.byref(a),
+                                          C.byref(b), C.byref(o)))
+        return bool(o.value), a.value, b.value
+
+    def particle_inter(self, m: int, kind: int, charge: float, trials):
+        t = np.ascontiguousarray(trials, dtype=np.float64).reshape(-1, 3)
+        n = t.shape[0]
+        en, re = np.empty(n), np.empty(n)
+        ov = np.empty(n, dtype=np.int32)
+        self._chk(lib().gb_particle_inter(self.h, int(m), int(kind),
+                                          float(charge), _dp(t), n, _dp(en),
+                                          _dp(re), _ip(ov)))
+        return ov.astype(bool), en, re
+
+    def box_force(self):
+        a, b = C.c_double(), C.c_double()
+        aF = np.empty((self.n_atoms, 3))
+        mF = np.empty((self.n_mol, 3))
+        self._chk(lib().gb_box_force(self.h, C.byref(a), C.byref(b), _dp(aF),
+                                     _dp(mF)))
+        return aF, mF, a.value, b.value
+
+    def calculate_torque(self):
+        tq = np.empty((self.n_mol, 3))
+        self._chk(lib().gb_calculate_torque(self.h, _dp(tq)))
+        return tq
+
+    # ---- Ewald --------------------------------------------------------------
+    def num_kvectors(self):
+        k, m = C.c_int32(), C.c_int32()
+        self._chk(lib().gb_num_kvectors(self.h, C.byref(k), C.byref(m)))
+        return k.value, m.value
+
+    def kvectors(self) -> dict:
+        K, _ = self.num_kvectors()
+        o = np.empty(7 * max(K, 1))
+        self._chk(lib().gb_get_kvectors(self.h, _dp(o)))
+        o = o[:7 * K].reshape(7, K)
+        return dict(kx=o[0], ky=o[1], kz=o[2], prefact=o[3], hsqr=o[4],
+                    sumRref=o[5], sumIref=o[6])
+
+    def sums_new(self):
+        K, _ = self.num_kvectors()
+        a, b = np.empty(max(K, 1)), np.empty(max(K, 1))
+        self._chk(lib().gb_get_sums_new(self.h, _dp(a), _dp(b)))
+        return a[:K], b[:K]
+
+    def box_reciprocal_setup(self) -> None:
+        self._chk(lib().gb_box_reciprocal_setup(self.h))
+
+    def box_reciprocal_sums(self) -> None:
+        self._chk(lib().gb_box_reciprocal_sums(self.h))
+
+    def box_reciprocal(self, use_ref: bool = False) -> float:
+        e = C.c_double()
+        self._chk(lib().gb_box_reciprocal(self.h, int(use_ref), C.byref(e)))
+        return e.value
+
+    def mol_reciprocal(self, m: int, new_pos) -> float:
+        p = np.ascontiguousarray(new_pos, dtype=np.float64).reshape(-1, 3)
+        e = C.c_double()
+        self._chk(lib().gb_mol_reciprocal(self.h, int(m), _dp(p), C.byref(e)))
+        return e.value
+
+    def swap_dest_recip(self, m: int, pos) -> float:
+        p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        e = C.c_double()
+        self._chk(lib().gb_swap_dest_recip(self.h, int(m), _dp(p), C.byref(e)))
+        return e.value
+
+    def swap_source_recip(self, m: int, pos) -> float:
+        p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        e = C.c_double()
+        self._chk(lib().gb_swap_source_recip(self.h, int(m), _dp(p),
+                                             C.byref(e)))
+        return e.value
+
+    def update_recip(self) -> None:
+        self._chk(lib().gb_update_recip(self.h))
+
+    def copy_recip(self) -> None:
+        self._chk(lib().gb_copy_recip(self.h))
+
+    def box_self(self) -> float:
+        e = C.c_double()
+        self._chk(lib().gb_box_self(self.h, C.byref(e)))
+        return e.value
+
+    def mol_correction(self, m: int) -> float:
+        e = C.c_double()
+        self._chk(lib().gb_mol_correction(self.h, int(m), C.byref(e)))
+        return e.value
+
+    def box_force_reciprocal(self):
+        aR = np.empty((self.n_atoms, 3))
+        mR = np.empty((self.n_mol, 3))
+        self._chk(lib().gb_box_force_reciprocal(self.h, _dp(aR), _dp(mR)))
+        return aR, mR
+
+    # ---- cell list ----------------------------------------------------------
+    def grid_all(self) -> None:
+        self._chk(lib().gb_grid_all(self.h))
+
+    def cell_membership(self):
+        c = np.empty(self.n_atoms, dtype=np.int32)
+        e = np.empty(3, dtype=np.int32)
+        self._chk(lib().gb_cell_membership(self.h, _ip(c), _ip(e)))
+        return c, tuple(int(v) for v in e)
+
+    # ---- state --------------------------------------------------------------
+    def coords(self):
+        xyz = np.empty((self.n_atoms, 3))
+        self._chk(lib().gb_get_coords(self.h, _dp(xyz), None))
+        return xyz
+
+    def com(self):
+        c = np.empty((self.n_mol, 3))
+        self._chk(lib().gb_get_coords(self.h, None, _dp(c)))
+        return c
+
+    def set_coords(self, xyz, com=None) -> None:
+        x = np.ascontiguousarray(xyz, dtype=np.float64)
+        c = None if com is None else np.ascontiguousarray(com, np.float64)
+        self._chk(lib().gb_set_coords(self.h, _dp(x),
+                                      None if c is None else _dp(c)))
+
+    def energy(self) -> np.ndarray:
+        e = np.empty(5)
+        self._chk(lib().gb_get_energy(self.h, _dp(e)))
+        return e
+
+    def set_energy(self, e5) -> None:
+        e = np.ascontiguousarray(e5, dtype=np.float64)
+        self._chk(lib().gb_set_energy(self.h, _dp(e)))
+
+    # ---- Monte Carlo ----------------------------------------------------------
+    def mc_init(self, seed: int, move_frac: Sequence[float], adj_steps: int,
+                scales: Optional[Sequence[float]] = None,
+                recompute_freq: int = 0) -> None:
+        p = _lib.McParams()
+        p.seed = int(seed) & 0xFFFFFFFF
+        for i in range(3):
+            p.frac[i] = float(move_frac[i])
+        p.adj_steps = int(adj_steps)
+        p.use_scales = 0 if scales is None else 1
+        if scales is not None:
+            for i in range(4):
+                p.scales[i] = float(scales[i])
+        p.recompute_freq = int(recompute_freq)
+        self._chk(lib().gb_mc_init(self.h, C.byref(p)))
+
+    def mc_run(self, first_step: int, nsteps: int, trace: bool = False):
+        if not trace:
+            self._chk(lib().gb_mc_run(self.h, int(first_step), int(nsteps),
+                                      None, None, None, None))
+            return None
+        k = np.empty(nsteps, np.int32)
+        m = np.empty(nsteps, np.int32)
+        a = np.empty(nsteps, np.int32)
+        de = np.empty((nsteps, 3))
+        self._chk(lib().gb_mc_run(self.h, int(first_step), int(nsteps), _ip(k),
+                                  _ip(m), _ip(a), _dp(de)))
+        return dict(kind=k, mol=m, accepted=a, de=de)
+
+    def mc_state(self):
+        sc = np.empty(4)
+        cnt = np.empty(6, dtype=np.int64)
+        self._chk(lib().gb_mc_state(self.h, _dp(sc),
+                                    cnt.ctypes.data_as(C.POINTER(C.c_int64))))
+        return sc, cnt
+
+
+def mc_run_batch(boxes: Sequence[Box], first_step: int, nsteps: int) -> None:
+    arr = (C.c_void_p * len(boxes))(*[b.h for b in boxes])
+    rc = lib().gb_mc_run_batch(arr, len(boxes), int(first_step), int(nsteps))
+    if rc:
+        check(rc, boxes[0].h)
+
+
+# ---------------------------------------------------------------------------
+# Reference-shaped facades
+# ---------------------------------------------------------------------------
+class CalculateEnergy:
+    """src/CalculateEnergy.h:48-293 on a resident Box."""
+
+    def __init__(self, box: Box):
+        self.box = box
+
+    def SystemTotal(self) -> dict:
+        return self.box.system_total()
+
+    def BoxInter(self):
+        return self.box.box_inter()
+
+    def MoleculeInter(self, molCoords, molIndex: int):
+        """Returns (overlap, inter_LJ, inter_coulomb)."""
+        return self.box.molecule_inter(molIndex, molCoords)
+
+    def ParticleInter(self, trialPos, partIndex_kind: int, charge: float,
+                      molIndex: int):
+        return self.box.particle_inter(molIndex, partIndex_kind, charge,
+                                       trialPos)
+
+    def BoxForce(self):
+        return self.box.box_force()
+
+    def CalculateTorque(self):
+        return self.box.calculate_torque()
+
+
+class Ewald:
+    """src/Ewald.h:46-228 on a resident Box."""
+
+    def __init__(self, box: Box):
+        self.box = box
+
+    def BoxReciprocalSetup(self):
+        self.box.box_reciprocal_setup()
+
+    def BoxReciprocalSums(self):
+        self.box.box_reciprocal_sums()
+
+    def BoxReciprocal(self, isNewVolume: bool = False) -> float:
+        return self.box.box_reciprocal(use_ref=False)
+
+    def MolReciprocal(self, molCoords, molIndex: int) -> float:
+        return self.box.mol_reciprocal(molIndex, molCoords)
+
+    def SwapDestRecip(self, newMolCoords, molIndex: int) -> float:
+        return self.box.swap_dest_recip(molIndex, newMolCoords)
+
+    def SwapSourceRecip(self, oldMolCoords, molIndex: int) -> float:
+        return self.box.swap_source_recip(molIndex, oldMolCoords)
+
+    def UpdateRecip(self):
+        self.box.update_recip()
+
+    def CopyRecip(self):
+        self.box.copy_recip()
+
+    def BoxSelf(self) -> float:
+        return self.box.box_self()
+
+    def MolCorrection(self, molIndex: int) -> float:
+        return self.box.mol_correction(molIndex)
+
+    def BoxForceReciprocal(self):
+        return self.box.box_force_reciprocal()
+
+
+class CellList:
+    """src/CellList.h:22-86 on a resident Box."""
+
+    def __init__(self, box: Box):
+        self.box = box
+
+    def GridAll(self):
+        self.box.grid_all()
+
+    def CellMembership(self):
+        return self.box.cell_membership()

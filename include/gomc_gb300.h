@@ -1,0 +1,177 @@
+/* gomc_gb300.h -- C ABI of the GB300 Monte Carlo energy path.
+ *
+ * One gb_box is one orthogonal periodic simulation box whose coordinates,
+ * cell grid, Ewald k-vectors and structure factors, and running energies stay
+ * resident in HBM on one GPU.  Every call returns 0 on success or a gb_status
+ * code; gb_last_error() gives the message.  No call exits the process.
+ * Calls on one box are not re-entrant; separate boxes may be used from
+ * separate threads.  Positions are Angstrom, energies Kelvin, charges e.
+ *
+ * Each entry point names the reference interface it replaces (GOMC 2.80,
+ * file:line within the GOMC source tree).
+ */
+#ifndef GOMC_GB300_H
+#define GOMC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gb_box gb_box;
+
+enum gb_status {
+  GB_OK = 0,
+  GB_ERR_ARG = 1,         /* invalid argument */
+  GB_ERR_CUDA = 2,        /* CUDA runtime error */
+  GB_ERR_NOMEM = 3,       /* device allocation failed */
+  GB_ERR_CAPACITY = 4,    /* a cell ran out of slots */
+  GB_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+  GB_ERR_STATE = 6,       /* call not valid in the current state */
+  GB_ERR_UNSUPPORTED = 7  /* input outside what this build handles */
+};
+
+enum gb_precision { GB_FP64 = 0, GB_MIXED = 1 };
+
+/* The molecular system of one box (what Molecules / MoleculeKind /
+ * Coordinates / FFParticle hold in the reference: src/Molecules.h,
+ * src/MoleculeKind.h, src/Coordinates.cpp:12-22, src/FFParticle.cpp:56-84). */
+typedef struct gb_system_desc {
+  int32_t n_atoms, n_mol, n_kinds;
+  const double *pos;          /* [n_atoms * 3] as read from the PDB */
+  const int32_t *atom_kind;   /* [n_atoms], 0 .. n_kinds-1 */
+  const double *atom_charge;  /* [n_atoms] */
+  const int32_t *mol_start;   /* [n_mol + 1] */
+  const double *kind_epsilon; /* [n_kinds] K */
+  const double *kind_sigma;   /* [n_kinds] A */
+  const double *kind_n;       /* [n_kinds] Mie repulsion exponent */
+  double box[3];              /* orthogonal edge lengths, A */
+} gb_system_desc;
+
+/* The in.conf keys of the energy path (src/ConfigSetup.cpp:222-1409). */
+typedef struct gb_config {
+  double temperature;   /* Temperature */
+  double rcut;          /* Rcut */
+  double rcut_low;      /* RcutLow */
+  double rcut_coulomb;  /* RcutCoulomb (defaults to Rcut when <= 0) */
+  double tolerance;     /* Tolerance */
+  int32_t ewald;        /* Ewald */
+  int32_t electrostatic;/* ElectroStatic */
+  int32_t precision;    /* GB300Precision: GB_FP64 or GB_MIXED */
+  int32_t device;       /* CUDA device ordinal */
+} gb_config;
+
+const char *gb_version(void);
+const char *gb_last_error(const gb_box *box); /* NULL box: last create error */
+
+/* System::Init (src/System.cpp:67-100): wrap coordinates into the box
+ * (Coordinates::WrapCoordinate, src/Coordinates.cpp:24-73), molecule centres
+ * (COM::CalcCOM, src/COM.h:47-68), CellList::GridAll
+ * (src/CellList.cpp:220-237), Ewald::Init (src/Ewald.cpp:100-139) and the
+ * initial CalculateEnergy::SystemTotal (src/CalculateEnergy.cpp:83-138). */
+int gb_box_create(const gb_system_desc *sys, const gb_config *cfg,
+                  gb_box **out);
+void gb_box_destroy(gb_box *box);
+
+/* ---- CalculateEnergy (src/CalculateEnergy.h:48-293) ---- */
+/* SystemTotal: out9 = inter, real, recip, self, correction, tailCorrection,
+ * intraBond, intraNonbond, total; also resets the running energies. */
+int gb_system_total(gb_box *box, double *out9);
+/* BoxInter (src/CalculateEnergy.cpp:157-266): LJ and real-space Coulomb */
+int gb_box_inter(gb_box *box, double *inter, double *real);
+/* MoleculeInter (src/CalculateEnergy.cpp:581-686): energy change of moving
+ * molecule `mol` from its current position to new_pos[n_atoms_of_mol * 3]. */
+int gb_molecule_inter(gb_box *box, int32_t mol, const double *new_pos,
+                      double *lj, double *real, int32_t *overlap);
+/* ParticleInter (src/CalculateEnergy.cpp:727-785): one atom of kind/charge
+ * at each of ntrials positions; atoms of molecule `mol` are excluded. */
+int gb_particle_inter(gb_box *box, int32_t mol, int32_t kind, double charge,
+                      const double *trials, int32_t ntrials, double *en,
+                      double *real, int32_t *overlap);
+/* BoxForce (src/CalculateEnergy.cpp:268-406): energies plus atom and
+ * molecule forces (host arrays may be NULL). */
+int gb_box_force(gb_box *box, double *inter, double *real, double *atom_force,
+                 double *mol_force);
+/* CalculateTorque (src/CalculateEnergy.cpp:1365-1406) from the forces of the
+ * last gb_box_force and gb_box_force_reciprocal calls. */
+int gb_calculate_torque(gb_box *box, double *mol_torque);
+
+/* ---- Ewald (src/Ewald.h:46-228) ---- */
+int gb_num_kvectors(gb_box *box, int32_t *k_count, int32_t *kmax);
+/* k-vector tables and Ref sums: kx, ky, kz, prefact, hsqr, sumRref, sumIref,
+ * seven arrays of k_count doubles (Ewald::RecipInitOrth,
+ * src/Ewald.cpp:847-903) */
+int gb_get_kvectors(gb_box *box, double *out7);
+int gb_get_sums_new(gb_box *box, double *sum_r, double *sum_i);
+/* BoxReciprocalSetup (src/Ewald.cpp:193-274) + SetRecipRef (:1021-1053) */
+int gb_box_reciprocal_setup(gb_box *box);
+/* BoxReciprocalSums (src/Ewald.cpp:281-361) for the current coordinates */
+int gb_box_reciprocal_sums(gb_box *box);
+/* BoxReciprocal (src/Ewald.cpp:375-406) of the New (use_ref = 0) or Ref
+ * (use_ref = 1) sums */
+int gb_box_reciprocal(gb_box *box, int32_t use_ref, double *energy);
+/* MolReciprocal (src/Ewald.cpp:409-473): fills the New sums, returns the
+ * energy difference against the running reciprocal energy */
+int gb_mol_reciprocal(gb_box *box, int32_t mol, const double *new_pos,
+                      double *delta);
+/* SwapDestRecip / SwapSourceRecip (src/Ewald.cpp:478-531, 657-710) */
+int gb_swap_dest_recip(gb_box *box, int32_t mol, const double *pos,
+                       double *delta);
+int gb_swap_source_recip(gb_box *box, int32_t mol, const double *pos,
+                         double *delta);
+int gb_update_recip(gb_box *box);   /* UpdateRecip, src/Ewald.cpp:1420-1434 */
+int gb_copy_recip(gb_box *box);     /* CopyRecip, src/Ewald.cpp:1441-1460 */
+int gb_box_self(gb_box *box, double *self); /* BoxSelf :1125-1163 */
+int gb_mol_correction(gb_box *box, int32_t mol, double *corr); /* :1056-1085 */
+/* BoxForceReciprocal (src/Ewald.cpp:1496-1596) from the New sums */
+int gb_box_force_reciprocal(gb_box *box, double *atom_force_rec,
+                            double *mol_force_rec);
+
+/* ---- CellList (src/CellList.h:22-86) ---- */
+int gb_grid_all(gb_box *box);  /* GridAll, src/CellList.cpp:220-237 */
+/* cell index of every atom (GetCellListNeighbor's mapParticleToCell,
+ * src/CellList.cpp:258-285) and the cells per edge */
+int gb_cell_membership(gb_box *box, int32_t *cell_of_atom, int32_t *edge3);
+
+/* ---- state ---- */
+int gb_get_coords(gb_box *box, double *xyz, double *com);
+int gb_set_coords(gb_box *box, const double *xyz, const double *com);
+/* running energies inter, real, recip, self, correction (SystemPotential) */
+int gb_get_energy(gb_box *box, double *e5);
+int gb_set_energy(gb_box *box, const double *e5);
+
+/* ---- device-resident Monte Carlo loop ----
+ * System::ChooseAndRunMove / RunMove (src/System.cpp:262-302) with the
+ * Translate, Rotate and MultiParticle moves (src/moves/Translate.h,
+ * Rotation.h, MultiParticle.h) and MoveSettings adjustment
+ * (src/MoveSettings.cpp:157-265).  Proposals come from the reference's
+ * MT19937 stream seeded with Random_Seed (src/PRNGSetup.h:28) and the
+ * MultiParticle move from Philox4x64-10 keyed (step, seed). */
+typedef struct gb_mc_params {
+  uint32_t seed;          /* Random_Seed */
+  double frac[3];         /* DisFreq, RotFreq, MultiParticleFreq */
+  int32_t adj_steps;      /* AdjSteps */
+  int32_t use_scales;     /* 1: start from scales[] instead of the defaults */
+  double scales[4];       /* displacement, rotation, MP t_max, MP r_max */
+  int32_t recompute_freq; /* GB300RecomputeFreq (mixed form), 0 = never */
+} gb_mc_params;
+
+int gb_mc_init(gb_box *box, const gb_mc_params *params);
+/* Run steps [first_step, first_step + nsteps).  Trace arrays may be NULL;
+ * otherwise each has nsteps entries (de: 3 per step). */
+int gb_mc_run(gb_box *box, int64_t first_step, int64_t nsteps, int32_t *kind,
+              int32_t *mol, int32_t *accepted, double *de);
+/* scales4: displacement, rotation, MP t_max, MP r_max;
+ * counts6: tries/accepted for displacement, rotation, MultiParticle */
+int gb_mc_state(gb_box *box, double *scales4, int64_t *counts6);
+
+/* Run the same number of steps on several boxes concurrently (one launch
+ * for all single-molecule segments).  Each box must have gb_mc_init. */
+int gb_mc_run_batch(gb_box **boxes, int32_t nboxes, int64_t first_step,
+                    int64_t nsteps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GOMC_GB300_H */

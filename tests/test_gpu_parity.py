@@ -1,0 +1,165 @@
+"""GPU energy path (FP64 plain form) against the reference's golden vectors.
+
+Bars (FP64 plain form): every energy term within 1e-10 relative; cell
+membership, k-vector tables and initial coordinates bit-exact; per-move
+accept/reject sequence identical to the reference's over the golden traces.
+"""
+import numpy as np
+import pytest
+
+from tests.golden_util import NAMES, config_of, load, move_fractions, system_of
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def gb():
+    from gomc_gb300 import engine
+    engine.lib(build_if_missing=True)
+    return engine
+
+
+def close(a, b, rel=REL, scale=None):
+    s = abs(b) if scale is None else scale
+    return abs(a - b) <= rel * max(s, 1e-300)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_initial_state(gb, name):
+    z, meta = load(name)
+    box = gb.Box(system_of(z, meta), config_of(meta))
+    st = box.system_total()
+    for term in ("inter", "real", "recip", "self", "correction", "total"):
+        ref = meta["init"]["box0_" + term]
+        assert close(st[term], ref, scale=max(abs(ref), 1.0)), (term, st[term], ref)
+    np.testing.assert_array_equal(box.coords(), z["coords_init"])
+    np.testing.assert_array_equal(box.com(), z["com_init"].reshape(-1, 3))
+    cells, edge = box.cell_membership()
+    assert list(edge) == meta["init"]["edgeCells"]
+    ref_cells = np.full(box.n_atoms, -1)
+    ref_cells[z["cells"][:, 0]] = z["cells"][:, 1]
+    np.testing.assert_array_equal(cells, ref_cells)
+    if "kvec" in z:
+        kv = box.kvectors()
+        K, _ = box.num_kvectors()
+        assert K == int(meta["init"]["imageSize"])
+        for i, key in enumerate(["kx", "ky", "kz"]):
+            np.testing.assert_array_equal(kv[key], z["kvec"][:, i])
+        np.testing.assert_array_equal(kv["hsqr"], z["kvec"][:, 6])
+        # prefactors go through the host libm's exp(): equal to a few ulp
+        # across x86-64 and aarch64 C libraries
+        np.testing.assert_allclose(kv["prefact"], z["kvec"][:, 3], rtol=1e-14,
+                                   atol=0)
+        smax = np.abs(z["kvec"][:, 4:6]).max()
+        np.testing.assert_allclose(kv["sumRref"], z["kvec"][:, 4], rtol=0,
+                                   atol=REL * smax)
+        np.testing.assert_allclose(kv["sumIref"], z["kvec"][:, 5], rtol=0,
+                                   atol=REL * smax)
+    box.close()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_proposal_deltas(gb, name):
+    z, meta = load(name)
+    box = gb.Box(system_of(z, meta), config_of(meta))
+    st = box.system_total()
+    cur = box.coords()
+    ms = z["mol_start"]
+    ewald = meta["config"]["ewald"]
+    # scale for differences: the box-term magnitude
+    s_lj = abs(meta["init"]["box0_inter"])
+    s_re = abs(meta["init"]["box0_real"]) if ewald else 1.0
+    s_rc = abs(meta["init"]["box0_recip"]) if ewald else 1.0
+    for i, m in enumerate(z["prop_mol"]):
+        ref = z["prop_out"][i]
+        ov, lj, re = box.molecule_inter(int(m), z["prop_pos"][i])
+        assert int(ov) == int(ref[1])
+        assert close(lj, ref[2], scale=s_lj), (i, lj, ref[2])
+        assert close(re, ref[3], scale=s_re), (i, re, ref[3])
+        if ewald:
+            assert close(box.mol_reciprocal(int(m), z["prop_pos"][i]), ref[4],
+                         scale=s_rc)
+            assert close(box.swap_dest_recip(int(m), z["prop_pos"][i]), ref[5],
+                         scale=s_rc)
+            old = cur[ms[m]:ms[m + 1]]
+            assert close(box.swap_source_recip(int(m), old), ref[6], scale=s_rc)
+    box.close()
+
+
+def test_forces(gb):
+    z, meta = load("c0_water_mp")
+    box = gb.Box(system_of(z, meta), config_of(meta))
+    aF, mF, lj, re = box.box_force()
+    box.copy_recip()
+    aR, mR = box.box_force_reciprocal()
+    tq = box.calculate_torque()
+    fa, fm = z["forces_atom"], z["forces_mol"]
+    for got, ref in ((aF, fa[:, 0:3]), (aR, fa[:, 3:6]), (mF, fm[:, 0:3]),
+                     (mR, fm[:, 3:6]), (tq, fm[:, 6:9])):
+        np.testing.assert_allclose(got, ref, rtol=0,
+                                   atol=REL * np.abs(ref).max())
+    assert close(lj, meta["force_energy"]["inter"])
+    assert close(re, meta["force_energy"]["real"])
+    box.close()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_mc_trace_matches_reference(gb, name):
+    z, meta = load(name)
+    box = gb.Box(system_of(z, meta), config_of(meta))
+    box.mc_init(meta["config"]["random_seed"], move_fractions(meta),
+                meta["config"]["adj_steps"])
+    tr = z["trace"]
+    n = tr.shape[0]
+    r = box.mc_run(0, n, trace=True)
+    np.testing.assert_array_equal(r["kind"], tr[:, 1].astype(int))
+    np.testing.assert_array_equal(r["mol"], tr[:, 2].astype(int))
+    np.testing.assert_array_equal(r["accepted"], tr[:, 3].astype(int))
+    scale = np.maximum(np.abs(tr[-1, 8:11]), 1.0)
+    single = tr[:, 1] < 2
+    for j in range(3):
+        np.testing.assert_allclose(r["de"][single, j], tr[single, 5 + j],
+                                   rtol=0, atol=REL * scale[j])
+    mp = ~single
+    if mp.any():
+        for j in range(3):
+            np.testing.assert_allclose(r["de"][mp, j], tr[mp, 5 + j], rtol=0,
+                                       atol=REL * scale[j])
+    e = box.energy()
+    for j in range(3):
+        assert close(e[j], tr[-1, 8 + j], scale=scale[j])
+    np.testing.assert_allclose(box.coords(), z["coords_final"], rtol=0,
+                               atol=1e-9)
+    sc, cnt = box.mc_state()
+    for k in range(3):
+        key = "move%d" % k
+        if key in meta["final"]:
+            tries, acc, scl = meta["final"][key]
+            assert cnt[2 * k] == tries and cnt[2 * k + 1] == acc
+            if k < 2:
+                assert close(sc[k], scl, rel=1e-12)
+    # running totals agree with a fresh recompute
+    st = box.system_total()
+    for j, term in enumerate(("inter", "real", "recip")):
+        assert close(e[j], st[term], scale=scale[j])
+    box.close()
+
+
+def test_particle_inter_against_oracle(gb):
+    from oracle import oracle as O
+    O.set_threads(1)
+    z, meta = load("w1728")
+    sysm, cfg = system_of(z, meta), config_of(meta)
+    box = gb.Box(sysm, cfg)
+    ob = O.OracleBox(sysm, cfg)
+    rng = np.random.default_rng(5)
+    trials = rng.uniform(0, 1, size=(16, 3)) * sysm.box
+    ov, en, re = box.particle_inter(7, 0, -0.8476, trials)
+    for t in range(16):
+        o2, e2, r2 = ob.particle_inter(7, 0, -0.8476, trials[t])
+        assert bool(ov[t]) == o2
+        assert close(en[t], e2, scale=max(abs(e2), 1.0))
+        assert close(re[t], r2, scale=max(abs(r2), 1.0))
+    box.close()
