@@ -1,0 +1,395 @@
+"""Benchmark: Monte Carlo moves per second on the 8,000-water NVT system.
+
+Workload (the GPU configuration the metric is quoted on): 8,000 rigid
+SPC/E-geometry waters (24,000 sites) in a 62.1 A cube at 298 K, Rcut 10 A,
+Ewald tolerance 1e-5 (24,658 k-vectors), seeded lattice with random
+orientations; single-molecule translate/rotate moves 50/50 drawn from the
+reference's MT19937 stream, move sizes starting from 0.3 A / 0.3 rad with the
+reference's adjustment every 1,000 moves.  One step = --moves-per-step moves
+of one Markov chain per GPU, state resident in HBM.
+
+value   : moves/s of the plain FP64 form, device time (CUDA events on the
+          library's stream) summed over the timed steps, L2 flushed between
+          steps; whole job over all ranks (independent replicas per GPU).
+e2e     : the same metric through the public API with host buffers: each step
+          uploads the coordinates from host memory (gb_set_coords), runs the
+          moves (gb_mc_run) and reads back energies and coordinates.
+mixed   : the mixed-precision form (FP32 pair / per-k arithmetic, FP64
+          accumulators), several independent chains batched on one GPU.
+roofline: the dominant kernel (the persistent chain kernel) against the
+          measured FP64 pipe peak of this GPU (float64 GEMM timed here).
+
+--impl reference times the reference algorithm on the host cores instead (the
+C oracle restatement, OpenMP over k-vectors, all host threads), same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+N_MOL = 8000
+BOX = 62.1
+RCUT = 10.0
+TOL = 1e-5
+TEMP = 298.0
+SEED = 20260
+FRAC = (0.5, 0.5, 0.0)
+ADJ = 1000
+SCALES = (0.3, 0.3, 0.02, 0.031415926535897934)
+METRIC = ("MC moves/s, 8k-water NVT: FP64 vs mixed (|dE|<=1e-6 rel); "
+          "job p50/p99 latency")
+WORKLOAD = ("8000 SPC/E waters (24000 sites), L=62.1 A, Rcut 10 A, Ewald tol "
+            "1e-5 (K=24658), T=298 K, translate/rotate 50/50, one chain per "
+            "GPU")
+
+
+def flop_per_move(K: int, na: int = 3, cand: int = 18000, incut: int = 2500):
+    """Algorithmic FP64 flops of one single-molecule move.
+
+    Reciprocal: per k-vector and per old/new atom position two complex
+    products (12 flops) and the charge-weighted accumulate (4), plus the
+    structure-factor update (4) and its energy (4).  Real space: 9 flops per
+    candidate pair (minimum image and r^2) and about 60 per pair inside the
+    cutoff (LJ, erfc-screened Coulomb)."""
+    recip = K * (2 * na * 16 + 8)
+    real = cand * 9 + incut * 60
+    return recip + real
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([v.strip() for v in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[0]))
+                mx.append(float(s[1]))
+                for i, n in enumerate(names):
+                    if s[4 + i].lower().startswith("active"):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks(torch, dev):
+    """HBM/bf16 from MEASURED_PEAKS.json; FP64/FP32 pipe peaks timed here."""
+    out = {}
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            mp = json.load(f)
+        out["hbm_gbs"] = mp.get("hbm_gbs")
+        out["source"] = "MEASURED_PEAKS.json"
+    else:
+        out["hbm_gbs"] = 6800.0
+        out["source"] = "fallback"
+    torch.backends.cuda.matmul.allow_tf32 = False
+    for name, dt, n, reps in (("fp64_tflops", torch.float64, 4096, 3),
+                              ("fp32_tflops", torch.float32, 8192, 5)):
+        a = torch.randn(n, n, device=dev, dtype=dt)
+        b = torch.randn(n, n, device=dev, dtype=dt)
+        torch.matmul(a, b)
+        torch.cuda.synchronize(dev)
+        best = 1e9
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1) / 1e3)
+        out[name] = 2.0 * n ** 3 / best / 1e12
+        del a, b
+    out["pipe_peak_source"] = "float64 / float32 GEMM timed in bench.py"
+    return out
+
+
+SMALL = False  # --small: the 256-water, 19.7 A box (for profiler captures)
+
+
+def make_system(rank: int):
+    from gomc_gb300.config import SimConfig
+    from gomc_gb300.systems import spce_water_box
+    if SMALL:
+        sysm = spce_water_box(256, 19.7, seed=SEED + rank)
+        cfg = SimConfig(temperature=TEMP, rcut=9.0, tolerance=TOL)
+    else:
+        sysm = spce_water_box(N_MOL, BOX, seed=SEED + rank)
+        cfg = SimConfig(temperature=TEMP, rcut=RCUT, tolerance=TOL)
+    return sysm, cfg
+
+
+def cpu_baseline(seconds: float, threads: int):
+    """The oracle port on the host cores: moves/s over a bounded sample."""
+    from oracle import oracle as O
+    O.set_threads(threads)
+    sysm, cfg = make_system(0)
+    ob = O.OracleBox(sysm, cfg)
+    ob.mc_init(SEED, FRAC, ADJ)
+    ob.mc_set_scales(SCALES)
+    step, n = 0, 0
+    t0 = time.time()
+    chunk = 8
+    while time.time() - t0 < seconds:
+        ob.mc_run(step, chunk)
+        step += chunk
+        n += chunk
+    dt = time.time() - t0
+    return {"value": n / dt, "unit": "moves/s", "cores": threads,
+            "kind": "port",
+            "sample": "%d single-molecule moves of the 8000-water system "
+                      "(%.1f s)" % (n, dt)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    steps, warm = args.steps, args.warmup
+    from oracle import oracle as O
+    O.set_threads(threads)
+    sysm, cfg = make_system(0)
+    ob = O.OracleBox(sysm, cfg)
+    ob.mc_init(SEED, FRAC, ADJ)
+    ob.mc_set_scales(SCALES)
+    per_step = args.ref_moves_per_step
+    step = 0
+    for _ in range(warm):
+        ob.mc_run(step, per_step)
+        step += per_step
+    t0 = time.time()
+    for _ in range(steps):
+        ob.mc_run(step, per_step)
+        step += per_step
+    dt = time.time() - t0
+    v = steps * per_step / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "moves/s",
+        "n_gpus": args.gpus, "steps": steps, "warmup": warm,
+        "ms_per_step": dt / steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "moves_per_step": per_step,
+                   "l2": "host run"},
+        "cpu_baseline": {"value": v, "unit": "moves/s", "cores": threads,
+                         "kind": "port",
+                         "sample": "%d steps x %d moves of the same workload"
+                                   % (steps, per_step)},
+        "e2e": {"value": v, "unit": "moves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, rank, world):
+    import torch
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    from gomc_gb300 import engine
+    engine.lib(build_if_missing=True)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+
+    peaks = measured_peaks(torch, dev) if rank == 0 else {}
+    sysm, cfg = make_system(rank)
+    box = engine.Box(sysm, cfg, device=dev)
+    K, kmax = box.num_kvectors()
+    box.mc_init(SEED + rank, FRAC, ADJ, scales=SCALES)
+    stream = torch.cuda.ExternalStream(box.stream_ptr(), device=dev)
+    M = args.moves_per_step
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32,
+                        device=dev)
+    step = 0
+    for _ in range(args.warmup):
+        box.mc_run(step, M)
+        step += M
+    box.mc_timing(reset=True)
+    times = []
+    barrier()
+    with ClockSampler(dev) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            box.mc_run(step, M)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            step += M
+    barrier()
+    timing = box.mc_timing(reset=True)
+    t_total = float(sum(times))
+    if dist:
+        tt = torch.tensor([t_total], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_total = float(tt.item())
+    value = world * args.steps * M / t_total
+
+    # end to end through the public API with host buffers
+    e2e_times = []
+    xyz = box.coords()
+    com = box.com()
+    barrier()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        box.set_coords(xyz, com)
+        box.mc_run(step, M)
+        e = box.energy()
+        xyz = box.coords()
+        com = box.com()
+        e2e_times.append(time.perf_counter() - t0)
+        step += M
+    barrier()
+    t_e2e = float(sum(e2e_times))
+    if dist:
+        tt = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e_value = world * args.steps * M / t_e2e
+    h2d = (sysm.n_atoms + sysm.n_mol) * 3 * 8 + M * 64
+    d2h = 5 * 8 + (sysm.n_atoms + sysm.n_mol) * 3 * 8
+
+    # correctness of the running energies after the timed steps
+    e_run = box.energy()
+    st = box.system_total()
+    drift = {k: abs(e_run[i] - st[k]) / abs(st[k])
+             for i, k in enumerate(["inter", "real", "recip"])}
+
+    mixed = None
+    if not args.no_mixed and hasattr(engine, "run_mixed_bench"):
+        mixed = engine.run_mixed_bench(args, dev, rank, world)
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    launches = timing["chain_launches"] + 10 * timing["mp_moves"]
+    kern_ms = timing["chain_ms"] / max(timing["chain_launches"], 1)
+    moves_per_launch = timing["chain_moves"] / max(timing["chain_launches"], 1)
+    fl = flop_per_move(K)
+    achieved = fl * moves_per_launch / (kern_ms / 1e3) / 1e12
+    roof = {"bound": "fp64", "achieved": achieved,
+            "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
+            "frac": achieved / peaks["fp64_tflops"], "traffic": None,
+            "kernel": "k_chain_fp64",
+            "per_unit": "%.3g FP64 flop per move (%d k-vectors)" % (fl, K),
+            "peak_source": peaks["pipe_peak_source"],
+            "hbm_peak_gbs": peaks["hbm_gbs"], "hbm_peak_source": peaks["source"]}
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_baseline(args.cpu_seconds, os.cpu_count() or 1)
+    line = {
+        "metric": METRIC, "value": value, "unit": "moves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "moves_per_step": M,
+                   "l2": "flushed between steps (512 MB write)",
+                   "precision": "FP64 plain form", "k_vectors": K},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "moves/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+        "running_vs_recompute_rel": drift,
+        "step_ms": [round(t * 1e3, 3) for t in times],
+        "e2e_step_ms": [round(t * 1e3, 3) for t in e2e_times],
+        "chain_kernel_ms_per_launch": kern_ms,
+        "mixed": mixed,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--moves-per-step", type=int, default=1000)
+    ap.add_argument("--ref-moves-per-step", type=int, default=100)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--small", action="store_true",
+                    help="256-water box instead of the 8000-water workload")
+    args = ap.parse_args()
+    global SMALL
+    SMALL = args.small
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gb300(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -97,6 +97,8 @@ SIGNATURES = {
     "gb_mc_state": (C.c_int, [_P, _D, _L]),
     "gb_mc_run_batch": (C.c_int, [C.POINTER(_P), C.c_int32, C.c_int64,
                                   C.c_int64]),
+    "gb_mc_timing": (C.c_int, [_P, C.c_int32, _D, _L, _L, _D, _L]),
+    "gb_box_stream": (C.c_int, [_P, C.POINTER(_P)]),
 }
 
 

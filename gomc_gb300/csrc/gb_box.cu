@@ -265,6 +265,8 @@ int Box::Init(const HostSystem &s0, const BoxConfig &c) {
   for (int k = 0; k < 3; ++k) {
     d.edge[k] = std::max((int)std::floor(s.L[k] / c.rcut), 3);
     d.cellSize[k] = s.L[k] / d.edge[k];
+    d.invCell[k] = 1.0 / d.cellSize[k];
+    d.invL[k] = 1.0 / s.L[k];
   }
   d.ncell = d.edge[0] * d.edge[1] * d.edge[2];
   std::vector<int> nbr((size_t)d.ncell * NB27);

@@ -258,6 +258,24 @@ int gb_mc_state(gb_box *box, double *scales4, int64_t *counts6) {
     return rc;
   return gb::mc_state(*box->b, scales4, counts6);
 }
+int gb_mc_timing(gb_box *box, int32_t reset, double *chain_ms,
+                 int64_t *chain_launches, int64_t *chain_moves, double *mp_ms,
+                 int64_t *mp_moves) {
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  return gb::mc_timing(*box->b, reset, chain_ms, chain_launches, chain_moves,
+                       mp_ms, mp_moves);
+}
+int gb_box_stream(gb_box *box, void **stream) {
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  if (!stream)
+    return gb::ERR_ARG;
+  *stream = (void *)box->b->stream;
+  return gb::OK;
+}
 int gb_mc_run_batch(gb_box **boxes, int32_t nboxes, int64_t first_step,
                     int64_t nsteps) {
   if (!boxes || nboxes <= 0)

@@ -16,7 +16,7 @@ __global__ void k_cell_scatter(DevBox b, const double *__restrict__ x,
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= b.n_atoms)
     return;
-  int c = position_to_cell(b, x[i], y[i], z[i]);
+  int c = position_to_cell_fast(b, x[i], y[i], z[i]);
   if (c < 0 || c >= b.ncell) {
     atomicOr(b.err, DERR_BAD_INPUT);
     return;

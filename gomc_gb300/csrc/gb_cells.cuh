@@ -21,8 +21,8 @@ __device__ __forceinline__ void cell_write_slot(const DevBox &b, int cell,
   b.cell_atom[s] = a;
   b.cell_pos[s] = make_double4_32a(x, y, z, q);
   b.cell_meta[s] = pack_meta(b.mol[a], b.kind[a]);
-  b.cell_fix[s] = make_uint4(to_turns(x, b.L[0]), to_turns(y, b.L[1]),
-                             to_turns(z, b.L[2]), __float_as_uint((float)q));
+  b.cell_fix[s] = make_uint4(to_turns(x, b.invL[0]), to_turns(y, b.invL[1]),
+                             to_turns(z, b.invL[2]), __float_as_uint((float)q));
   b.atom_cell[a] = cell;
   b.atom_slot[a] = slot;
 }
@@ -32,9 +32,8 @@ __device__ __forceinline__ void cell_write_slot(const DevBox &b, int cell,
 // atoms per cell changes exactly as in the reference; the slot order inside a
 // cell is this grid's own (swap-remove, append).  Single-thread use.
 __device__ __forceinline__ bool cell_move_atom(const DevBox &b, int a, double x,
-                                               double y, double z) {
+                                               double y, double z, int c1) {
   int c0 = b.atom_cell[a];
-  int c1 = position_to_cell(b, x, y, z);
   if (c0 == c1) {
     cell_write_slot(b, c0, b.atom_slot[a], a, x, y, z);
     return true;

@@ -382,47 +382,70 @@ __device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
     return;
   __shared__ double oldp[MAX_MOL_ATOMS][3], newp[MAX_MOL_ATOMS][3], com[3],
       newcom[3];
-  if (threadIdx.x == 0) {
-    bool same = prev_acc && prev_hdr && (int)prev_hdr[0] == m;
-    for (int a = 0; a < na; ++a) {
-      if (same) {
-        for (int d = 0; d < 3; ++d)
-          oldp[a][d] = prev_hdr[48 + 3 * a + d];
-      } else {
-        oldp[a][0] = __ldcg(b.x + a0 + a);
-        oldp[a][1] = __ldcg(b.y + a0 + a);
-        oldp[a][2] = __ldcg(b.z + a0 + a);
-      }
-    }
-    if (same && (int)prev_hdr[1] == 0) {
-      for (int d = 0; d < 3; ++d)
-        com[d] = prev_hdr[4 + d];
-    } else {
-      com[0] = __ldcg(b.cx + m);
-      com[1] = __ldcg(b.cy + m);
-      com[2] = __ldcg(b.cz + m);
-    }
-    apply_proposal(b, r.kind, A.prop + (size_t)t * 12, na, oldp, com, newp,
-                   newcom);
+  __shared__ double prop[12];
+  bool same = prev_acc && prev_hdr && (int)prev_hdr[0] == m;
+  if (threadIdx.x < 12)
+    prop[threadIdx.x] = A.prop[(size_t)t * 12 + threadIdx.x];
+  if (threadIdx.x < 3) {
+    int d = threadIdx.x;
+    double *cs[3] = {b.cx, b.cy, b.cz};
+    com[d] = (same && (int)prev_hdr[1] == 0) ? prev_hdr[4 + d]
+                                             : __ldcg(cs[d] + m);
+  }
+  if (threadIdx.x >= 32 && threadIdx.x < 32 + 3 * na) {
+    int i = threadIdx.x - 32, a = i / 3, d = i % 3;
+    double *xs[3] = {b.x, b.y, b.z};
+    oldp[a][d] = same ? prev_hdr[48 + 3 * a + d] : __ldcg(xs[d] + a0 + a);
   }
   __syncthreads();
-  if (header_cta && threadIdx.x == 0) {
-    double *h = A.ctx;
-    h[0] = m;
-    h[1] = r.kind;
-    h[2] = na;
-    h[3] = r.pacc;
-    for (int d = 0; d < 3; ++d)
-      h[4 + d] = newcom[d];
-    for (int a = 0; a < na; ++a) {
-      h[8 + a] = position_to_cell(b, oldp[a][0], oldp[a][1], oldp[a][2]);
-      h[16 + a] = position_to_cell(b, newp[a][0], newp[a][1], newp[a][2]);
+  // one thread per atom applies the proposal (Coordinates::TranslateRand /
+  // RotateRand arithmetic, see apply_proposal)
+  if (threadIdx.x < na) {
+    int a = threadIdx.x;
+    double v[3], w[3];
+    if (r.kind == 0) {
+      for (int d = 0; d < 3; ++d)
+        w[d] = wrap1(__dadd_rn(oldp[a][d], prop[d]), b.L[d]);
+    } else {
       for (int d = 0; d < 3; ++d) {
-        h[24 + 3 * a + d] = oldp[a][d];
-        h[48 + 3 * a + d] = newp[a][d];
+        v[d] = unwrap1(oldp[a][d], com[d], b.L[d], b.half[d]);
+        v[d] = __dadd_rn(v[d], -com[d]);
       }
-      double q = b.q[a0 + a];
-      h[72 + a] = fabs(q) < 0.000000001 ? 0.0 : q;
+      for (int i = 0; i < 3; ++i) {
+        double u = __dadd_rn(__dadd_rn(__dmul_rn(prop[3 * i], v[0]),
+                                       __dmul_rn(prop[3 * i + 1], v[1])),
+                             __dmul_rn(prop[3 * i + 2], v[2]));
+        w[i] = wrap1(__dadd_rn(u, com[i]), b.L[i]);
+      }
+    }
+    for (int d = 0; d < 3; ++d)
+      newp[a][d] = w[d];
+  }
+  if (threadIdx.x >= 32 && threadIdx.x < 35) {
+    int d = threadIdx.x - 32;
+    newcom[d] = r.kind == 0 ? wrap1(__dadd_rn(com[d], prop[d]), b.L[d]) : com[d];
+  }
+  __syncthreads();
+  if (header_cta) {
+    double *h = A.ctx;
+    if (threadIdx.x == 0) {
+      h[0] = m;
+      h[1] = r.kind;
+      h[2] = na;
+      h[3] = r.pacc;
+      for (int d = 0; d < 3; ++d)
+        h[4 + d] = newcom[d];
+    }
+    if (threadIdx.x >= 32 && threadIdx.x < 32 + 2 * na) {
+      int i = threadIdx.x - 32, a = i % na, side = i / na;
+      const double *p = side ? newp[a] : oldp[a];
+      h[(side ? 16 : 8) + a] = position_to_cell_fast(b, p[0], p[1], p[2]);
+      for (int d = 0; d < 3; ++d)
+        h[(side ? 48 : 24) + 3 * a + d] = p[d];
+      if (side == 0) {
+        double q = b.q[a0 + a];
+        h[72 + a] = fabs(q) < 0.000000001 ? 0.0 : q;
+      }
     }
   }
   // phase rows exp(i n 2 pi r_d / L_d), n = 0..kmax, one entry per thread
@@ -589,7 +612,23 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
     // ---------------- phase B ----------------
     if (threadIdx.x < 32) {
       double v[4] = {0, 0, 0, 0};
-      for (int c = threadIdx.x; c < G; c += 32) {
+      constexpr int PF = 8;  // partial slots per lane loaded up front
+      double2 pa[PF], pb[PF];
+#pragma unroll
+      for (int i = 0; i < PF; ++i) {
+        int c = threadIdx.x + 32 * i;
+        const double2 *src = (const double2 *)(A.part + (size_t)c * 4);
+        pa[i] = c < G ? __ldcg(src) : make_double2(0, 0);
+        pb[i] = c < G ? __ldcg(src + 1) : make_double2(0, 0);
+      }
+#pragma unroll
+      for (int i = 0; i < PF; ++i) {
+        v[0] += pa[i].x;
+        v[1] += pa[i].y;
+        v[2] += pb[i].x;
+        v[3] = fmax(v[3], pb[i].y);
+      }
+      for (int c = threadIdx.x + 32 * PF; c < G; c += 32) {
         const double *p = A.part + (size_t)c * 4;
         v[0] += __ldcg(p);
         v[1] += __ldcg(p + 1);
@@ -643,7 +682,7 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
           b.x[a0 + a] = np[0];
           b.y[a0 + a] = np[1];
           b.z[a0 + a] = np[2];
-          cell_move_atom(b, a0 + a, np[0], np[1], np[2]);
+          cell_move_atom(b, a0 + a, np[0], np[1], np[2], (int)S.hdr[16 + a]);
         }
         if ((int)S.hdr[1] == 0) {
           b.cx[m] = S.hdr[4];
@@ -975,12 +1014,15 @@ static int mc_alloc(Box &b, McState &s, T **p, size_t n) {
   return OK;
 }
 
+static void harvest(McState &s);
+
 void mc_destroy(Box &b) {
   if (!b.mc)
     return;
   McState &s = *b.mc;
   if (b.stream)
     cudaStreamSynchronize(b.stream);
+  harvest(s);
   for (void *p : s.allocs)
     cudaFree(p);
   if (s.h_moves)
@@ -1109,6 +1151,64 @@ static void skip_to(McState &s, int64_t step) {
   }
 }
 
+static std::pair<cudaEvent_t, cudaEvent_t> ev_pair() {
+  cudaEvent_t a = nullptr, z = nullptr;
+  cudaEventCreate(&a);
+  cudaEventCreate(&z);
+  return {a, z};
+}
+
+// Fold finished event pairs into the accumulated device times.
+static void harvest(McState &s) {
+  for (size_t i = 0; i < s.chain_ev.size(); ++i) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, s.chain_ev[i].first, s.chain_ev[i].second) ==
+        cudaSuccess)
+      s.chain_ms += ms;
+    s.chain_launches++;
+    s.chain_moves += s.chain_ev_moves[i];
+    cudaEventDestroy(s.chain_ev[i].first);
+    cudaEventDestroy(s.chain_ev[i].second);
+  }
+  for (auto &e : s.mp_ev) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, e.first, e.second) == cudaSuccess)
+      s.mp_ms += ms;
+    s.mp_moves++;
+    cudaEventDestroy(e.first);
+    cudaEventDestroy(e.second);
+  }
+  s.chain_ev.clear();
+  s.chain_ev_moves.clear();
+  s.mp_ev.clear();
+}
+
+int mc_timing(Box &b, int reset, double *chain_ms, int64_t *chain_launches,
+              int64_t *chain_moves, double *mp_ms, int64_t *mp_moves) {
+  if (!b.mc)
+    return b.Fail(ERR_STATE, "gb_mc_init has not been called");
+  int rc = b.Sync();
+  if (rc)
+    return rc;
+  McState &s = *b.mc;
+  harvest(s);
+  if (chain_ms)
+    *chain_ms = s.chain_ms;
+  if (chain_launches)
+    *chain_launches = s.chain_launches;
+  if (chain_moves)
+    *chain_moves = s.chain_moves;
+  if (mp_ms)
+    *mp_ms = s.mp_ms;
+  if (mp_moves)
+    *mp_moves = s.mp_moves;
+  if (reset) {
+    s.chain_ms = s.mp_ms = 0.0;
+    s.chain_launches = s.chain_moves = s.mp_moves = 0;
+  }
+  return OK;
+}
+
 static int run_chain(Box &b, McState &s, const MoveRec *moves, int64_t first,
                      int n, int *tr_i, double *tr_d) {
   ChainArgs A;
@@ -1126,15 +1226,24 @@ static int run_chain(Box &b, McState &s, const MoveRec *moves, int64_t first,
   A.tr_d = tr_d;
   void *args[] = {&A};
   size_t sm = chain_smem(b, s.grid);
-  return b.CudaCheck(cudaLaunchCooperativeKernel((void *)k_chain_fp64,
-                                                 dim3(s.grid), dim3(CT), args,
-                                                 sm, b.stream),
-                     "chain kernel");
+  auto ev = ev_pair();
+  cudaEventRecord(ev.first, b.stream);
+  int rc = b.CudaCheck(cudaLaunchCooperativeKernel((void *)k_chain_fp64,
+                                                   dim3(s.grid), dim3(CT), args,
+                                                   sm, b.stream),
+                       "chain kernel");
+  cudaEventRecord(ev.second, b.stream);
+  s.chain_ev.push_back(ev);
+  s.chain_ev_moves.push_back(n);
+  return rc;
 }
 
 static int run_mp(Box &b, McState &s, int64_t step, int type, int *tr_i,
                   double *tr_d) {
   int rc;
+  auto ev = ev_pair();
+  cudaEventRecord(ev.first, b.stream);
+  s.mp_ev.push_back(ev);
   k_settings_adjust<<<1, 1, 0, b.stream>>>(s.d_set, (long long)step);
   Settings host_set;
   if ((rc = b.CudaCheck(cudaMemcpyAsync(&host_set, s.d_set, sizeof(Settings),
@@ -1231,6 +1340,7 @@ static int run_mp(Box &b, McState &s, int64_t step, int type, int *tr_i,
   C.mRn = s.d_mRn;
   C.tqn = s.d_tqn;
   k_mp_commit<<<2 * b.sm_count, 256, 0, b.stream>>>(C);
+  cudaEventRecord(ev.second, b.stream);
   return b.CudaCheck(cudaGetLastError(), "multiparticle");
 }
 
@@ -1289,6 +1399,7 @@ int mc_run(Box &b, int64_t first, int64_t nsteps, int32_t *kind, int32_t *mol,
   }
   if ((rc = b.Sync()) || (rc = b.CheckError()))
     return rc;
+  harvest(s);
   if (trace) {
     std::vector<int> ti(3 * (size_t)nsteps);
     std::vector<double> td(3 * (size_t)nsteps);

@@ -89,7 +89,15 @@ struct McState {
   double *d_mp = nullptr;    // MultiParticle scalars
   DevBox cells_new{};        // cell grid of the trial state
   std::vector<void *> allocs;
+  // device-time accounting (CUDA events on the box stream)
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> chain_ev, mp_ev;
+  std::vector<int> chain_ev_moves;
+  double chain_ms = 0.0, mp_ms = 0.0;
+  int64_t chain_launches = 0, chain_moves = 0, mp_moves = 0;
 };
+
+int mc_timing(Box &b, int reset, double *chain_ms, int64_t *chain_launches,
+              int64_t *chain_moves, double *mp_ms, int64_t *mp_moves);
 
 int mc_init(Box &b, const gb_mc_params &p);
 int mc_run(Box &b, int64_t first_step, int64_t nsteps, int32_t *kind,

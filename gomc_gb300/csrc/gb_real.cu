@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(RT) k_mol_inter(DevBox b, const FF *__restrict
     py = newpos[3 * a + 1];
     pz = newpos[3 * a + 2];
   }
-  int cell = position_to_cell(b, px, py, pz);
+  int cell = position_to_cell_fast(b, px, py, pz);
   int c2 = b.nbr[cell * NB27 + n];
   int n2 = b.cell_count[c2];
   double qa = b.q[atom];
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(RT) k_particle_inter(DevBox b, const FF *__res
   int u = blockIdx.x;
   int t = u / NB27, n = u % NB27;
   double px = trials[3 * t], py = trials[3 * t + 1], pz = trials[3 * t + 2];
-  int cell = position_to_cell(b, px, py, pz);
+  int cell = position_to_cell_fast(b, px, py, pz);
   int c2 = b.nbr[cell * NB27 + n];
   int n2 = b.cell_count[c2];
   double lj = 0.0, re = 0.0, ovl = 0.0;

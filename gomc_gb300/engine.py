@@ -277,6 +277,20 @@ class Box:
                                   _ip(m), _ip(a), _dp(de)))
         return dict(kind=k, mol=m, accepted=a, de=de)
 
+    def mc_timing(self, reset: bool = False) -> dict:
+        cm, mm = C.c_double(), C.c_double()
+        cl, cn, mn = C.c_int64(), C.c_int64(), C.c_int64()
+        self._chk(lib().gb_mc_timing(self.h, int(reset), C.byref(cm),
+                                     C.byref(cl), C.byref(cn), C.byref(mm),
+                                     C.byref(mn)))
+        return dict(chain_ms=cm.value, chain_launches=cl.value,
+                    chain_moves=cn.value, mp_ms=mm.value, mp_moves=mn.value)
+
+    def stream_ptr(self) -> int:
+        p = C.c_void_p()
+        self._chk(lib().gb_box_stream(self.h, C.byref(p)))
+        return int(p.value or 0)
+
     def mc_state(self):
         sc = np.empty(4)
         cnt = np.empty(6, dtype=np.int64)

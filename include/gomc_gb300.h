@@ -166,6 +166,16 @@ int gb_mc_run(gb_box *box, int64_t first_step, int64_t nsteps, int32_t *kind,
  * counts6: tries/accepted for displacement, rotation, MultiParticle */
 int gb_mc_state(gb_box *box, double *scales4, int64_t *counts6);
 
+/* Device time spent in this box's Monte Carlo kernels since the last reset,
+ * measured with CUDA events on the box's stream: chain kernels (translate /
+ * rotate segments) and MultiParticle kernel sequences.  No reference
+ * counterpart (measurement). */
+int gb_mc_timing(gb_box *box, int32_t reset, double *chain_ms,
+                 int64_t *chain_launches, int64_t *chain_moves, double *mp_ms,
+                 int64_t *mp_moves);
+/* The CUDA stream (cudaStream_t) every call on this machine is ordered on. */
+int gb_box_stream(gb_box *box, void **stream);
+
 /* Run the same number of steps on several boxes concurrently (one launch
  * for all single-molecule segments).  Each box must have gb_mc_init. */
 int gb_mc_run_batch(gb_box **boxes, int32_t nboxes, int64_t first_step,
