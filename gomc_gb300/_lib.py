@@ -51,7 +51,8 @@ class Config(C.Structure):
 class McParams(C.Structure):
     _fields_ = [("seed", C.c_uint32), ("frac", C.c_double * 3),
                 ("adj_steps", C.c_int32), ("use_scales", C.c_int32),
-                ("scales", C.c_double * 4), ("recompute_freq", C.c_int32)]
+                ("scales", C.c_double * 4), ("recompute_freq", C.c_int32),
+                ("cluster_size", C.c_int32), ("flush_every", C.c_int32)]
 
 
 # every function the header declares: name -> (restype, argtypes)
@@ -99,6 +100,7 @@ SIGNATURES = {
                                   C.c_int64]),
     "gb_mc_timing": (C.c_int, [_P, C.c_int32, _D, _L, _L, _D, _L]),
     "gb_box_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "gb_mc_drift": (C.c_int, [_P, _D, _D, _L]),
 }
 
 

@@ -267,6 +267,23 @@ int gb_mc_timing(gb_box *box, int32_t reset, double *chain_ms,
   return gb::mc_timing(*box->b, reset, chain_ms, chain_launches, chain_moves,
                        mp_ms, mp_moves);
 }
+int gb_mc_drift(gb_box *box, double *max4, double *last4, int64_t *n) {
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  if (!box->b->mc)
+    return gb::ERR_STATE;
+  gb::McState &s = *box->b->mc;
+  for (int i = 0; i < 4; ++i) {
+    if (max4)
+      max4[i] = s.drift_max[i];
+    if (last4)
+      last4[i] = s.drift_last[i];
+  }
+  if (n)
+    *n = s.recomputes;
+  return gb::OK;
+}
 int gb_box_stream(gb_box *box, void **stream) {
   int rc = guard(box);
   if (rc)

@@ -26,6 +26,7 @@
 // (step, seed) as in Random123Wrapper (src/Random123Wrapper.cpp:16-84).
 #include "gb_mc.h"
 #include "gb_cells.cuh"
+#include "gb_moves.cuh"
 #include "gb_pair.cuh"
 
 #include <algorithm>
@@ -138,71 +139,7 @@ void MoveStream::Next(MoveRec *r) {
     r->ax[2] = u;
   }
   r->pacc = mt_.rand01();  // Translate/Rotate::Accept prng()
-}
-
-// ===========================================================================
-// Move settings, identical on host and device
-// ===========================================================================
-GB_HD double bound_d(double v, double lo, double hi) {
-  return v < lo ? lo : (v > hi ? hi : v);
-}
-
-// MoveSettings::AdjustMoves / Adjust / AdjustMultiParticle
-// (src/MoveSettings.cpp:157-265), called at the start of every step.
-GB_HD void settings_adjust(Settings &s, long long step) {
-  if ((step + 1) % s.adj != 0)
-    return;
-  for (int mv = 0; mv < 3; ++mv) {
-    if (mv < 2) {
-      if (s.tempTries[mv] > 0) {
-        double currentAccept =
-            (double)s.tempAccepted[mv] / (double)s.tempTries[mv];
-        double fract = currentAccept / 0.5;
-        if (fract > 0.0)
-          s.scale[mv] *= fract;
-        else
-          s.scale[mv] *= 0.5;
-      }
-      if (mv == 0)
-        s.scale[0] = bound_d(s.scale[0], 1.0e-10, (s.amin * 0.5) - 1.0e-7);
-      else
-        s.scale[1] = bound_d(s.scale[1], 1.0e-6, M_PI - 1.0e-7);
-    }
-    s.tempTries[mv] = 0;
-    s.tempAccepted[mv] = 0;
-  }
-  for (int t = 0; t < 2; ++t) {
-    if (s.mp_itries[t] > 0) {
-      s.mp_tries[t] += s.mp_itries[t];
-      s.mp_acc[t] += s.mp_iacc[t];
-      double fTot = ((double)s.mp_acc[t] / (double)s.mp_tries[t]) / 0.3;
-      double fInt = ((double)s.mp_iacc[t] / (double)s.mp_itries[t]) / 0.3;
-      double &mx = (t == 0) ? s.mp_t_max : s.mp_r_max;
-      if (fInt == 0.0)
-        mx *= 0.5;
-      else if (fabs(fInt - 0.3) > 0.1)
-        mx *= ((1.0 - 0.2) * fTot + 0.2 * fInt);
-      if (t == 0)
-        mx = bound_d(mx, 0.001, (s.amin * 0.5) - 0.001);
-      else
-        mx = bound_d(mx, 0.001, M_PI - 0.001);
-      s.mp_iacc[t] = 0;
-      s.mp_itries[t] = 0;
-    }
-  }
-}
-
-// MoveSettings::Update (src/MoveSettings.cpp:100-155), one molecule kind
-GB_HD void settings_update(Settings &s, int mv, int accepted) {
-  s.tries[mv]++;
-  s.tempTries[mv]++;
-  if (accepted) {
-    s.tempAccepted[mv]++;
-    s.accepted[mv]++;
-    s.singleMoveAccepted = 1;
-  }
-  if (mv == 2)
-    s.singleMoveAccepted = 0;
+  r->lpacc = std::log(r->pacc);
 }
 
 // ===========================================================================
@@ -253,22 +190,6 @@ __device__ bool grid_sync(unsigned *bar, unsigned nblocks, unsigned &gen,
   return *s_flag != 0;
 }
 
-// Rotation matrix from an angle and a unit axis
-// (RotationMatrix::FromAxisAngle, src/TransformMatrix.h:165-214).
-__device__ __forceinline__ void axis_angle_matrix(double theta, const double *u,
-                                                  double *r) {
-  double c = cos(theta);
-  double s = sin(theta);
-  double cross[9] = {0.0, -(u[2]), u[1], u[2], 0.0, -(u[0]), -(u[1]), u[0], 0.0};
-  double omc = 1 - c;
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) {
-      double t = __dmul_rn(u[i], u[j]);
-      double add = __dadd_rn(__dmul_rn(s, cross[3 * i + j]), __dmul_rn(omc, t));
-      r[3 * i + j] = __dadd_rn(i == j ? c : 0.0, add);
-    }
-}
-
 // Apply a stored proposal to the atoms of molecule m.
 // kind 0: shift (Coordinates::TranslateRand, src/Coordinates.cpp:83-100)
 // kind 1: rotation about the molecule centre (RotateRand, :103-128)
@@ -300,21 +221,6 @@ __device__ __forceinline__ void apply_proposal(const DevBox &b, int kind,
     }
     for (int d = 0; d < 3; ++d)
       newcom[d] = com[d];
-  }
-}
-
-// Proposal of one move for the current scales: shift (3) or matrix (9).
-__device__ __forceinline__ void make_proposal(const MoveRec &r,
-                                              const Settings &s, double *prop) {
-  if (r.kind == 0) {
-    double bnd = s.scale[0];
-    double b2 = 2.0 * bnd;
-    for (int d = 0; d < 3; ++d)
-      prop[d] = __dadd_rn(__dmul_rn(r.u[d], b2), -bnd);
-  } else if (r.kind == 1) {
-    double mx = s.scale[1];
-    double theta = __dadd_rn(__dmul_rn(r.u[0], 2.0 * mx), -mx);
-    axis_angle_matrix(theta, r.ax, prop);
   }
 }
 
@@ -1027,6 +933,8 @@ void mc_destroy(Box &b) {
     cudaFree(p);
   if (s.h_moves)
     cudaFreeHost(s.h_moves);
+  if (s.h_desc)
+    cudaFreeHost(s.h_desc);
   delete s.stream;
   delete b.mc;
   b.mc = nullptr;
@@ -1109,6 +1017,39 @@ int mc_init(Box &b, const gb_mc_params &p) {
     return rc;
   if ((rc = b.CudaCheck(cudaMemsetAsync(s.d_bar, 0, 32, b.stream), "memset")))
     return rc;
+  if (b.cfg.precision == GB_MIXED) {
+    // FP32 pair terms assume the 12-6 form
+    for (int i = 0; i < b.ff.n_kinds * b.ff.n_kinds; ++i)
+      if (b.ff.eps_cn[i] != 0.0 && b.ff.nexp[i] != 12.0)
+        return b.Fail(ERR_UNSUPPORTED, "mixed form supports Mie n = 12 only");
+    int want = p.cluster_size;
+    if (want != 0 && want != 2 && want != 4 && want != 8 && want != 16)
+      return b.Fail(ERR_ARG, "cluster_size must be 0, 2, 4, 8 or 16");
+    int cands[4] = {16, 8, 4, 2};
+    s.cluster = 0;
+    for (int c : cands) {
+      if (want && c != want)
+        continue;
+      size_t sm = mixed_smem(b.dev.K, b.dev.kmax, c);
+      if (sm > 220 * 1024)
+        continue;
+      if (max_active_clusters(c, sm) >= 1) {
+        s.cluster = c;
+        s.mixed_smem = sm;
+        break;
+      }
+    }
+    if (!s.cluster)
+      return b.Fail(ERR_UNSUPPORTED, "no cluster shape fits this box");
+    s.flush_every = p.flush_every > 0 ? p.flush_every : 64;
+    s.desc_cap = 256;
+    if ((rc = mc_alloc(b, s, &s.d_desc, s.desc_cap)))
+      return rc;
+    if ((rc = b.CudaCheck(cudaMallocHost(&s.h_desc,
+                                         s.desc_cap * sizeof(MixedChain)),
+                          "pinned")))
+      return rc;
+  }
   // MultiParticle trial-state buffers
   int N = b.dev.n_atoms, M = b.dev.n_mol;
   if ((rc = mc_alloc(b, s, &s.d_xn, N)) || (rc = mc_alloc(b, s, &s.d_yn, N)) ||
@@ -1236,6 +1177,77 @@ static int run_chain(Box &b, McState &s, const MoveRec *moves, int64_t first,
   s.chain_ev.push_back(ev);
   s.chain_ev_moves.push_back(n);
   return rc;
+}
+
+static MixedChain fill_mixed(Box &b, McState &s, const MoveRec *moves,
+                             int64_t first, int n, int *tr_i, double *tr_d) {
+  MixedChain c;
+  c.b = b.dev;
+  c.ff = b.d_ff;
+  c.set = s.d_set;
+  c.moves = moves;
+  c.prop = s.d_prop;
+  c.first = first;
+  c.n = n;
+  c.flush_every = s.flush_every;
+  c.tr_i = tr_i;
+  c.tr_d = tr_d;
+  return c;
+}
+
+static int next_desc(Box &b, McState &s) {
+  if (s.desc_next >= s.desc_cap) {
+    int rc = b.Sync();  // every staged descriptor has been copied
+    if (rc)
+      return -1;
+    s.desc_next = 0;
+  }
+  return s.desc_next++;
+}
+
+static int run_chain_mixed(Box &b, McState &s, const MoveRec *moves,
+                           int64_t first, int n, int *tr_i, double *tr_d) {
+  int slot = next_desc(b, s);
+  if (slot < 0)
+    return ERR_CUDA;
+  s.h_desc[slot] = fill_mixed(b, s, moves, first, n, tr_i, tr_d);
+  int rc = b.CudaCheck(cudaMemcpyAsync(s.d_desc + slot, s.h_desc + slot,
+                                       sizeof(MixedChain),
+                                       cudaMemcpyHostToDevice, b.stream),
+                       "descriptor upload");
+  if (rc)
+    return rc;
+  auto ev = ev_pair();
+  cudaEventRecord(ev.first, b.stream);
+  rc = launch_chain_mixed(b.stream, s.d_desc + slot, 1, s.cluster, s.mixed_smem);
+  cudaEventRecord(ev.second, b.stream);
+  s.chain_ev.push_back(ev);
+  s.chain_ev_moves.push_back(n);
+  if (rc)
+    return b.CudaCheck(cudaGetLastError(), "mixed chain kernel");
+  return OK;
+}
+
+// Periodic full FP64 recompute of the mixed form: record how far the running
+// energies drifted, then restart from the FP64 values (the reference's
+// UpdateVectorsAndRecipTerms + SystemTotal, src/Simulation.cpp:170-223).
+static int recompute_fp64(Box &b, McState &s) {
+  double run[5], tot[9];
+  int rc;
+  if ((rc = b.GetEnergy(run)) || (rc = b.SystemTotal(tot)))
+    return rc;
+  double rt = run[0] + run[1] + run[2] + run[3] + run[4];
+  double ft = tot[0] + tot[1] + tot[2] + tot[3] + tot[4];
+  double d[4] = {std::fabs(run[0] - tot[0]) / std::max(std::fabs(tot[0]), 1e-300),
+                 std::fabs(run[1] - tot[1]) / std::max(std::fabs(tot[1]), 1e-300),
+                 std::fabs(run[2] - tot[2]) / std::max(std::fabs(tot[2]), 1e-300),
+                 std::fabs(rt - ft) / std::max(std::fabs(ft), 1e-300)};
+  for (int i = 0; i < 4; ++i) {
+    s.drift_last[i] = d[i];
+    s.drift_max[i] = std::max(s.drift_max[i], d[i]);
+  }
+  s.recomputes++;
+  return OK;
 }
 
 static int run_mp(Box &b, McState &s, int64_t step, int type, int *tr_i,
@@ -1376,7 +1388,10 @@ int mc_run(Box &b, int64_t first, int64_t nsteps, int32_t *kind, int32_t *mol,
                                           cudaMemcpyHostToDevice, b.stream),
                           "upload moves")))
       return rc;
-    // split into chain segments and MultiParticle moves
+    // split into chain segments, MultiParticle moves and (mixed form)
+    // periodic FP64 recomputes
+    const bool mixed = b.cfg.precision == GB_MIXED;
+    const int64_t R = mixed ? s.params.recompute_freq : 0;
     int64_t i = 0;
     while (i < chunk) {
       int64_t step = first + done + i;
@@ -1386,12 +1401,21 @@ int mc_run(Box &b, int64_t first, int64_t nsteps, int32_t *kind, int32_t *mol,
         if ((rc = run_mp(b, s, step, s.h_moves[i].mol, ti, td)))
           return rc;
         ++i;
+        if (R > 0 && (step + 1) % R == 0 && (rc = recompute_fp64(b, s)))
+          return rc;
         continue;
       }
       int64_t j = i;
-      while (j < chunk && s.h_moves[j].kind != 2)
+      while (j < chunk && s.h_moves[j].kind != 2) {
         ++j;
-      if ((rc = run_chain(b, s, s.d_moves + i, step, (int)(j - i), ti, td)))
+        if (R > 0 && (first + done + j) % R == 0)
+          break;
+      }
+      rc = mixed ? run_chain_mixed(b, s, s.d_moves + i, step, (int)(j - i), ti, td)
+                 : run_chain(b, s, s.d_moves + i, step, (int)(j - i), ti, td);
+      if (rc)
+        return rc;
+      if (R > 0 && (first + done + j) % R == 0 && (rc = recompute_fp64(b, s)))
         return rc;
       i = j;
     }
@@ -1451,11 +1475,103 @@ int mc_state(Box &b, double *scales4, int64_t *counts6) {
 
 int mc_run_batch(const std::vector<Box *> &boxes, int64_t first,
                  int64_t nsteps) {
+  // FP64 boxes (or a single box) run one after another.
+  bool all_mixed = boxes.size() > 1;
   for (Box *b : boxes) {
-    int rc = mc_run(*b, first, nsteps, nullptr, nullptr, nullptr, nullptr);
-    if (rc)
+    if (!b->mc)
+      return b->Fail(ERR_STATE, "gb_mc_init has not been called");
+    if (b->cfg.precision != GB_MIXED || b->mc->params.frac[2] > 0)
+      all_mixed = false;
+    if (b->dev.n_atoms > 0 && b->sm_count != boxes[0]->sm_count)
+      all_mixed = false;
+  }
+  if (!all_mixed) {
+    for (Box *b : boxes) {
+      int rc = mc_run(*b, first, nsteps, nullptr, nullptr, nullptr, nullptr);
+      if (rc)
+        return rc;
+    }
+    return OK;
+  }
+  // Mixed boxes without MultiParticle moves: one launch runs every chain.
+  Box &b0 = *boxes[0];
+  int csize = b0.mc->cluster;
+  size_t smem = 0;
+  for (Box *b : boxes)
+    csize = std::min(csize, b->mc->cluster);
+  for (Box *b : boxes)
+    smem = std::max(smem, mixed_smem(b->dev.K, b->dev.kmax, csize));
+  if (smem > 220 * 1024 || max_active_clusters(csize, smem) < 1)
+    return b0.Fail(ERR_UNSUPPORTED,
+                   "boxes of this batch need different cluster shapes");
+  int rc;
+  for (Box *b : boxes) {
+    if (first < b->mc->next_step)
+      return b->Fail(ERR_STATE, "steps must be run in increasing order");
+    skip_to(*b->mc, first);
+    if ((rc = b->Sync()))
       return rc;
   }
+  McState &s0 = *b0.mc;
+  int nb = (int)boxes.size();
+  if (s0.desc_cap < nb) {
+    s0.desc_cap = std::max(nb, 256);
+    if ((rc = mc_alloc(b0, s0, &s0.d_desc, s0.desc_cap)))
+      return rc;
+    if (s0.h_desc)
+      cudaFreeHost(s0.h_desc);
+    if ((rc = b0.CudaCheck(cudaMallocHost(&s0.h_desc,
+                                          s0.desc_cap * sizeof(MixedChain)),
+                           "pinned")))
+      return rc;
+  }
+  int64_t done = 0;
+  while (done < nsteps) {
+    int64_t chunk = std::min<int64_t>(nsteps - done, (int64_t)s0.move_cap);
+    int64_t R = s0.params.recompute_freq;
+    if (R > 0) {
+      int64_t to_boundary = R - ((first + done) % R);
+      chunk = std::min(chunk, to_boundary);
+    }
+    if ((rc = b0.Sync()))
+      return rc;
+    for (int k = 0; k < nb; ++k) {
+      Box &b = *boxes[k];
+      McState &s = *b.mc;
+      for (int64_t i = 0; i < chunk; ++i)
+        s.stream->Next(&s.h_moves[i]);
+      s.next_step += chunk;
+      if ((rc = b.CudaCheck(cudaMemcpyAsync(s.d_moves, s.h_moves,
+                                            chunk * sizeof(MoveRec),
+                                            cudaMemcpyHostToDevice, b0.stream),
+                            "upload moves")))
+        return rc;
+      s0.h_desc[k] = fill_mixed(b, s, s.d_moves, first + done, (int)chunk,
+                                nullptr, nullptr);
+    }
+    if ((rc = b0.CudaCheck(cudaMemcpyAsync(s0.d_desc, s0.h_desc,
+                                           nb * sizeof(MixedChain),
+                                           cudaMemcpyHostToDevice, b0.stream),
+                           "descriptor upload")))
+      return rc;
+    auto ev = ev_pair();
+    cudaEventRecord(ev.first, b0.stream);
+    if ((rc = launch_chain_mixed(b0.stream, s0.d_desc, nb, csize, smem)))
+      return b0.CudaCheck(cudaGetLastError(), "batched mixed chain kernel");
+    cudaEventRecord(ev.second, b0.stream);
+    s0.chain_ev.push_back(ev);
+    s0.chain_ev_moves.push_back((int)(chunk * nb));
+    if ((rc = b0.Sync()))
+      return rc;
+    done += chunk;
+    if (R > 0 && (first + done) % R == 0)
+      for (Box *b : boxes)
+        if ((rc = recompute_fp64(*b, *b->mc)))
+          return rc;
+  }
+  for (Box *b : boxes)
+    if ((rc = b->CheckError()))
+      return rc;
   return OK;
 }
 

@@ -17,6 +17,7 @@ struct MoveRec {
   double u[3];    // displacement: three rand() draws; rotation: u[0] = angle draw
   double ax[3];   // rotation axis (PRNG::PickOnUnitSphere, src/PRNG.h:143-151)
   double pacc;    // Metropolis uniform (Translate::Accept, src/moves/Translate.h:101)
+  double lpacc;   // log(pacc), for the mixed form's log-domain comparison
 };
 
 // MoveSettings state (src/MoveSettings.h:28-160) for one box, one kind.
@@ -64,8 +65,20 @@ class MoveStream {
   bool all_single_;
 };
 
+struct MixedChain;
+
 struct McState {
   gb_mc_params params{};
+  // mixed form: cluster size, descriptor ring, drift records
+  int cluster = 0;
+  size_t mixed_smem = 0;
+  MixedChain *d_desc = nullptr;   // [desc_cap]
+  MixedChain *h_desc = nullptr;   // pinned
+  int desc_cap = 0, desc_next = 0;
+  int flush_every = 64;
+  double drift_max[4] = {0, 0, 0, 0};  // inter, real, recip, total (relative)
+  double drift_last[4] = {0, 0, 0, 0};
+  int64_t recomputes = 0;
   MoveStream *stream = nullptr;
   int64_t next_step = 0;     // step the stream is positioned at
   Settings *d_set = nullptr; // device copy of Settings
@@ -98,6 +111,24 @@ struct McState {
 
 int mc_timing(Box &b, int reset, double *chain_ms, int64_t *chain_launches,
               int64_t *chain_moves, double *mp_ms, int64_t *mp_moves);
+
+// One chain of the mixed-precision chain kernel (gb_mixed.cu).
+struct MixedChain {
+  DevBox b;
+  const FF *ff;
+  Settings *set;
+  const MoveRec *moves;
+  double *prop;
+  int64_t first;
+  int n;
+  int flush_every;
+  int *tr_i;
+  double *tr_d;
+};
+size_t mixed_smem(int K, int kmax, int csize);
+int launch_chain_mixed(cudaStream_t st, const MixedChain *d_chains, int nchains,
+                       int csize, size_t smem);
+int max_active_clusters(int csize, size_t smem);
 
 int mc_init(Box &b, const gb_mc_params &p);
 int mc_run(Box &b, int64_t first_step, int64_t nsteps, int32_t *kind,

@@ -1,0 +1,628 @@
+// Mixed-precision chain kernel: one thread-block cluster runs one Markov
+// chain, many chains per launch.
+//
+// Per move, every CTA of the cluster:
+//   * builds the move header (FP64 old/new positions, exact cell indices,
+//     32-bit fixed-point turns, the midpoint p = (r + r')/2 and the half step
+//     h = (r' - r)/2 of every atom) and per-axis phase rows exp(2 pi i n p/L)
+//     from the exact fixed-point phase;
+//   * evaluates its share of the real-space (atom, old/new, neighbour cell)
+//     units in FP32 from fixed-point coordinates -- the minimum image is the
+//     wrapped 32-bit difference -- with an exact FP64 decision for pairs whose
+//     r^2 lies within 1e-5 of the cutoff;
+//   * evaluates its chunk of k-vectors with
+//       exp(i k.r') - exp(i k.r) = 2i sin(k.h) exp(i k.p),
+//     which keeps the structure-factor change accurate relative to itself,
+//     and dE_k = prefact (2 S.dS + |dS|^2) against its resident accumulators;
+//   * exchanges its partial sums through distributed shared memory; after a
+//     cluster barrier every CTA adds the partials in one order, takes the
+//     same Metropolis decision (FP64 exponent against log u) and, on accept,
+//     folds dS into its accumulators.
+// Structure factors are FP64 accumulators in shared memory; accepted deltas
+// are staged in an FP32 two-sum window and folded into FP64 every
+// `flush_every` accepted moves.  Running energies are FP64.
+#include "gb_cells.cuh"
+#include "gb_f32math.cuh"
+#include "gb_mc.h"
+#include "gb_moves.cuh"
+#include "gb_pair.cuh"
+
+#include <cooperative_groups.h>
+
+namespace cg = cooperative_groups;
+
+namespace gb {
+
+constexpr int MT_THREADS = 256;  // threads per CTA
+constexpr int MAXA = MAX_MOL_ATOMS;
+
+struct MHdr {
+  int m, kind, na, a0;
+  double lpacc;
+  double oldp[MAXA][3], newp[MAXA][3], newcom[3];
+  int cell_old[MAXA], cell_new[MAXA];
+  uint32_t uo[MAXA][3], un[MAXA][3], P[MAXA][3];
+  float hf[MAXA][3];
+  float qf[MAXA];
+  int ka[MAXA];
+};
+
+struct MShared {
+  MHdr h;
+  Settings set;
+  double e_run[5];
+  double part[4];        // this CTA's partial: LJ, real, recip, overlap
+  double tot[4];
+  double wred[MT_THREADS / 32][4];
+  double prop[12];
+  int accept;
+  int nacc;              // accepted moves since the last flush
+};
+
+// Byte offsets of the per-CTA k-chunk arrays in dynamic shared memory; every
+// array starts on a 16-byte boundary whatever the chunk length.
+struct MixedLayout {
+  size_t kcs;  // padded chunk length (multiple of 4)
+  size_t s64, f32, kn, tab;
+};
+__host__ __device__ __forceinline__ MixedLayout mixed_layout(int kc_max) {
+  MixedLayout L;
+  L.kcs = ((size_t)kc_max + 3) & ~(size_t)3;
+  L.s64 = 0;
+  L.f32 = L.s64 + 2 * 8 * L.kcs;
+  L.kn = L.f32 + 9 * 4 * L.kcs;
+  L.tab = L.kn + 4 * L.kcs;
+  return L;
+}
+
+// Whether cells c1 and c2 are in one another's 27-cell neighbourhood (every
+// axis has at least 3 cells, src/CellList.cpp:138-161).
+__device__ __forceinline__ bool cells_adjacent(const DevBox &b, int c1, int c2) {
+  const int e1 = b.edge[1], e2 = b.edge[2];
+  int d[3] = {c2 / (e1 * e2) - c1 / (e1 * e2), (c2 / e2) % e1 - (c1 / e2) % e1,
+              c2 % e2 - c1 % e2};
+  bool ok = true;
+  for (int i = 0; i < 3; ++i) {
+    int v = d[i] < 0 ? -d[i] : d[i];
+    ok = ok && (v <= 1 || v == b.edge[i] - 1);
+  }
+  return ok;
+}
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 tabf(const float2 *row, int n) {
+  float2 v = row[n < 0 ? -n : n];
+  if (n < 0)
+    v.y = -v.y;
+  return v;
+}
+
+// Header of move t (all threads of the CTA call it).
+__device__ void mixed_header(const MixedChain &C, MShared &S, int t,
+                             bool prev_acc, int prev_m, int prev_kind) {
+  const DevBox &b = C.b;
+  const MoveRec &r = C.moves[t];
+  MHdr &h = S.h;
+  int m = r.mol;
+  int a0 = b.mstart[m], na = b.mstart[m + 1] - a0;
+  bool same = prev_acc && prev_m == m;
+  // the previous header still holds that move's new positions
+  __shared__ double oldp[MAXA][3], com[3];
+  if (threadIdx.x < 12)
+    S.prop[threadIdx.x] = C.prop[(size_t)t * 12 + threadIdx.x];
+  if (threadIdx.x < 3) {
+    int d = threadIdx.x;
+    const double *cs[3] = {b.cx, b.cy, b.cz};
+    com[d] = (same && prev_kind == 0) ? h.newcom[d] : __ldcg(cs[d] + m);
+  }
+  if (threadIdx.x >= 32 && threadIdx.x < 32 + 3 * na) {
+    int i = threadIdx.x - 32, a = i / 3, d = i % 3;
+    const double *xs[3] = {b.x, b.y, b.z};
+    oldp[a][d] = same ? h.newp[a][d] : __ldcg(xs[d] + a0 + a);
+  }
+  __syncthreads();
+  if (threadIdx.x < na) {
+    int a = threadIdx.x;
+    double w[3];
+    if (r.kind == 0) {
+      for (int d = 0; d < 3; ++d)
+        w[d] = wrap1(__dadd_rn(oldp[a][d], S.prop[d]), b.L[d]);
+    } else {
+      double v[3];
+      for (int d = 0; d < 3; ++d) {
+        v[d] = unwrap1(oldp[a][d], com[d], b.L[d], b.half[d]);
+        v[d] = __dadd_rn(v[d], -com[d]);
+      }
+      for (int i = 0; i < 3; ++i) {
+        double u = __dadd_rn(__dadd_rn(__dmul_rn(S.prop[3 * i], v[0]),
+                                       __dmul_rn(S.prop[3 * i + 1], v[1])),
+                             __dmul_rn(S.prop[3 * i + 2], v[2]));
+        w[i] = wrap1(__dadd_rn(u, com[i]), b.L[i]);
+      }
+    }
+    for (int d = 0; d < 3; ++d) {
+      h.oldp[a][d] = oldp[a][d];
+      h.newp[a][d] = w[d];
+      uint32_t uo = to_turns(oldp[a][d], b.invL[d]);
+      uint32_t un = to_turns(w[d], b.invL[d]);
+      int32_t D = (int32_t)(un - uo);
+      h.uo[a][d] = uo;
+      h.un[a][d] = un;
+      h.P[a][d] = uo + (uint32_t)(D >> 1);
+      h.hf[a][d] = (float)D * 7.31459039633579840e-10f;  // pi / 2^32
+    }
+    h.cell_old[a] = position_to_cell_fast(b, oldp[a][0], oldp[a][1], oldp[a][2]);
+    h.cell_new[a] = position_to_cell_fast(b, w[0], w[1], w[2]);
+    double q = b.q[a0 + a];
+    h.qf[a] = fabs(q) < 0.000000001 ? 0.0f : (float)q;
+    h.ka[a] = b.kind[a0 + a];
+  }
+  if (threadIdx.x == 64) {
+    h.m = m;
+    h.kind = r.kind;
+    h.na = na;
+    h.a0 = a0;
+    h.lpacc = r.lpacc;
+    for (int d = 0; d < 3; ++d)
+      h.newcom[d] = r.kind == 0 ? wrap1(__dadd_rn(com[d], S.prop[d]), b.L[d])
+                                : com[d];
+  }
+  __syncthreads();
+}
+
+// Phase rows exp(2 pi i n P / 2^32), n = 0..kmax, for every atom and axis.
+__device__ __forceinline__ void mixed_tables(const MixedChain &C, MShared &S,
+                                             float2 *tab) {
+  int stride = C.b.kmax + 1;
+  int rows = 3 * S.h.na;
+  for (int i = threadIdx.x; i < rows * stride; i += MT_THREADS) {
+    int row = i / stride, n = i % stride;
+    uint32_t P = S.h.P[row / 3][row % 3];
+    tab[i] = cis_turns((uint32_t)n * P);
+  }
+}
+
+__global__ void __launch_bounds__(MT_THREADS)
+    k_chain_mixed(const MixedChain *__restrict__ chains) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int csize = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  const int chain_id = blockIdx.x / csize;
+  const MixedChain &C = chains[chain_id];
+  const DevBox &b = C.b;
+  const FF &ff = *C.ff;
+  __shared__ MShared S;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  const int K = b.K;
+  const int kc_max = (K + csize - 1) / csize;
+  const int kbeg = min(K, rank * kc_max);
+  const int kc = min(kc_max, K - kbeg);
+  MixedLayout L = mixed_layout(kc_max);
+  double *s64R = (double *)(dyn + L.s64), *s64I = s64R + L.kcs;
+  float *s32R = (float *)(dyn + L.f32), *s32I = s32R + L.kcs;
+  float *pRh = s32I + L.kcs, *pRl = pRh + L.kcs, *pIh = pRl + L.kcs,
+        *pIl = pIh + L.kcs, *dR = pIl + L.kcs, *dI = dR + L.kcs,
+        *pf = dI + L.kcs;
+  char4 *kn = (char4 *)(dyn + L.kn);
+  float2 *tab = (float2 *)(dyn + L.tab);
+  const int stride = b.kmax + 1;
+
+  for (int i = threadIdx.x; i < kc; i += MT_THREADS) {
+    int k = kbeg + i;
+    double r = b.sumRref[k], im = b.sumIref[k];
+    s64R[i] = r;
+    s64I[i] = im;
+    s32R[i] = (float)r;
+    s32I[i] = (float)im;
+    pRh[i] = pRl[i] = pIh[i] = pIl[i] = 0.0f;
+    pf[i] = b.prefact_f[k];
+    kn[i] = b.kn[k];
+  }
+  if (threadIdx.x == 0) {
+    S.set = *C.set;
+    for (int i = 0; i < 5; ++i)
+      S.e_run[i] = b.energy[i];
+    S.nacc = 0;
+  }
+  __syncthreads();
+  const int tpc = MT_THREADS * csize;
+  const int gt = rank * MT_THREADS + threadIdx.x;
+  auto make_props = [&](int t0) {
+    int t1 = t0;
+    while (t1 < C.n) {
+      long long step = C.first + t1;
+      if (t1 > t0 && (step + 1) % S.set.adj == 0)
+        break;
+      ++t1;
+    }
+    for (int t = t0 + gt; t < t1; t += tpc)
+      make_proposal(C.moves[t], S.set, C.prop + (size_t)t * 12);
+  };
+  auto flush = [&]() {
+    for (int i = threadIdx.x; i < kc; i += MT_THREADS) {
+      s64R[i] += (double)pRh[i] + (double)pRl[i];
+      s64I[i] += (double)pIh[i] + (double)pIl[i];
+      pRh[i] = pRl[i] = pIh[i] = pIl[i] = 0.0f;
+      s32R[i] = (float)s64R[i];
+      s32I[i] = (float)s64I[i];
+    }
+  };
+
+  if (C.n > 0) {
+    if (threadIdx.x == 0)
+      settings_adjust(S.set, C.first);
+    __syncthreads();
+    make_props(0);
+    cluster.sync();
+    mixed_header(C, S, 0, false, -1, 0);
+    mixed_tables(C, S, tab);
+    __syncthreads();
+  }
+  const float rc2 = (float)ff.rcutSq;
+  const float rcc2 = (float)ff.rcutCoulSq;
+  const float rl2 = (float)ff.rcutLowSq;
+  const float alpha = (float)ff.alpha;
+  const float sx = (float)(b.L[0] * 2.3283064365386963e-10);  // L / 2^32
+  const float sy = (float)(b.L[1] * 2.3283064365386963e-10);
+  const float sz = (float)(b.L[2] * 2.3283064365386963e-10);
+  const bool coul_cut = ff.rcutCoulSq < ff.rcutSq;
+  const bool narrow = b.cellSize[0] * b.cellSize[0] < ff.rcutSq ||
+                      b.cellSize[1] * b.cellSize[1] < ff.rcutSq ||
+                      b.cellSize[2] * b.cellSize[2] < ff.rcutSq;
+
+  for (int t = 0; t < C.n; ++t) {
+    const MHdr &h = S.h;
+    const int m = h.m, na = h.na;
+    // ---------------- real space ----------------
+    // Each neighbour j is taken once: from the new position's cells when it
+    // is inside the cutoff there (then as the difference u(r') - u(r) if it
+    // was also inside before), from the old position's cells when it was
+    // inside only before.  Differences use r'^2 - r^2 = delta . (d + d').
+    float lj_h = 0.f, lj_l = 0.f, re_h = 0.f, re_l = 0.f, ovl = 0.f;
+    const int units = na * 2 * NB27;
+    const int lane128 = threadIdx.x & 127, half = threadIdx.x >> 7;
+    for (int ub = rank * 2; ub < units; ub += 2 * csize) {
+      int u = ub + half;
+      if (u >= units)
+        continue;
+      int a = u / (2 * NB27), side = (u / NB27) % 2, nn = u % NB27;
+      int cell = side ? h.cell_new[a] : h.cell_old[a];
+      int c2 = b.nbr[cell * NB27 + nn];
+      int n2 = __ldcg(b.cell_count + c2);
+      const uint32_t *uo = h.uo[a], *un = h.un[a];
+      float ddx = (float)(int32_t)(un[0] - uo[0]) * sx;
+      float ddy = (float)(int32_t)(un[1] - uo[1]) * sy;
+      float ddz = (float)(int32_t)(un[2] - uo[2]) * sz;
+      float qa = h.qf[a];
+      int ka = h.ka[a];
+      for (int j = lane128; j < n2; j += 128) {
+        size_t s = (size_t)c2 * b.cap + j;
+        int mj = __ldcg(b.cell_meta + s);
+        if (meta_mol(mj) == m)
+          continue;
+        uint4 f = __ldcg(b.cell_fix + s);
+        int32_t ox = (int32_t)(uo[0] - f.x), oy = (int32_t)(uo[1] - f.y),
+                oz = (int32_t)(uo[2] - f.z);
+        int32_t nx_ = (int32_t)(un[0] - f.x), ny_ = (int32_t)(un[1] - f.y),
+                nz_ = (int32_t)(un[2] - f.z);
+        float dox = (float)ox * sx, doy = (float)oy * sy, doz = (float)oz * sz;
+        float dnx = (float)nx_ * sx, dny = (float)ny_ * sy, dnz = (float)nz_ * sz;
+        float r2o = fmaf(dox, dox, fmaf(doy, doy, doz * doz));
+        float r2n = fmaf(dnx, dnx, fmaf(dny, dny, dnz * dnz));
+        // inside-cutoff decisions, exact in FP64 within 1e-5 of the cutoff
+        bool in_o = r2o < rc2, in_n = r2n < rc2;
+        bool amb_o = fabsf(r2o - rc2) <= rc2 * 1e-5f;
+        bool amb_n = fabsf(r2n - rc2) <= rc2 * 1e-5f;
+        bool amb_l = side && r2n < rl2 * 1.00001f;
+        if (side ? (!in_n && !amb_n) : (!in_o && !amb_o))
+          continue;
+        if (amb_o || amb_n || amb_l) {
+          const double *pp = (const double *)(b.cell_pos + s);
+          double px = __ldcg(pp), py = __ldcg(pp + 1), pz = __ldcg(pp + 2);
+          if (amb_o) {
+            const double *mp = h.oldp[a];
+            double d2 = dsq3(min_image(mp[0] - px, b.L[0], b.half[0]),
+                             min_image(mp[1] - py, b.L[1], b.half[1]),
+                             min_image(mp[2] - pz, b.L[2], b.half[2]));
+            in_o = ff.rcutSq > d2;
+          }
+          if (amb_n || amb_l) {
+            const double *mp = h.newp[a];
+            double d2 = dsq3(min_image(mp[0] - px, b.L[0], b.half[0]),
+                             min_image(mp[1] - py, b.L[1], b.half[1]),
+                             min_image(mp[2] - pz, b.L[2], b.half[2]));
+            in_n = ff.rcutSq > d2;
+            if (side && in_n && d2 < ff.rcutLowSq)
+              ovl = 1.f;
+          }
+        }
+        // With cells narrower than the cutoff a pair inside it may lie
+        // outside the other position's neighbourhood, where it is not summed.
+        if (narrow && in_o && in_n &&
+            !cells_adjacent(b, c2, side ? h.cell_old[a] : h.cell_new[a])) {
+          if (side)
+            in_o = false;
+          else
+            in_n = false;
+        }
+        int kj = meta_kind(mj);
+        int idx = ka + kj * ff.n_kinds;
+        float qq = qa * __uint_as_float(f.w) * (float)QQ_FACT;
+        bool coul = ff.electrostatic && qq != 0.f;
+        // Coulomb cutoff: the pair cutoff decision when it is the larger one
+        bool cin_o = coul_cut ? r2o <= rcc2 : true;
+        bool cin_n = coul_cut ? r2n <= rcc2 : true;
+        float sg2 = ff.sigmaSq_f[idx], ecn = ff.eps_cn_f[idx];
+        if (side) {
+          if (!in_n)
+            continue;
+          if (in_o) {
+            // difference of the pair terms between r and r'
+            // (d + d') in FP32: the integer sum can leave the int32 range
+            float dr2 = fmaf(ddx, dox + dnx, fmaf(ddy, doy + dny, ddz * (doz + dnz)));
+            float ro = sqrtf(r2o), rn = sqrtf(r2n);
+            float so = sg2 / r2o, sn = sg2 / r2n;
+            float ds = -sg2 * dr2 / (r2o * r2n);
+            float so3 = so * so * so, sn3 = sn * sn * sn;
+            float d3 = ds * fmaf(sn, sn, fmaf(sn, so, so * so));
+            two_sum_add(lj_h, lj_l, ecn * d3 * (sn3 + so3 - 1.0f));
+            if (coul && cin_n && cin_o) {
+              float inv_o = 1.0f / ro, inv_n = 1.0f / rn;
+              float sum_r = ro + rn;
+              float dinv = -dr2 * inv_o * inv_n / sum_r;  // 1/rn - 1/ro
+              float derfc;                                 // erfc(a rn) - erfc(a ro)
+              if (ff.ewald) {
+                float tlo = alpha * ro, thi = alpha * rn;
+                float dt = alpha * dr2 / sum_r;              // thi - tlo
+                if (fabsf(dt) < 0.25f) {
+                  // 3-point Gauss-Legendre of exp(-t^2) over [tlo, thi]
+                  float tm = 0.5f * (tlo + thi), hw = 0.5f * dt;
+                  float t1 = fmaf(-0.774596669f, hw, tm),
+                        t3 = fmaf(0.774596669f, hw, tm);
+                  float g = 0.888888889f * expf(-tm * tm) +
+                            0.555555556f * (expf(-t1 * t1) + expf(-t3 * t3));
+                  derfc = -1.128379167f * hw * g;  // 2/sqrt(pi) * (dt/2) * sum
+                } else {
+                  derfc = erfc_f32(thi) - erfc_f32(tlo);
+                }
+                float en = erfc_f32(thi);
+                two_sum_add(re_h, re_l, qq * fmaf(en, dinv, derfc * inv_o));
+              } else {
+                two_sum_add(re_h, re_l, qq * dinv);
+              }
+            } else if (coul) {
+              if (cin_n) {
+                float rr = sqrtf(r2n);
+                two_sum_add(re_h, re_l, ff.ewald ? qq * erfc_f32(alpha * rr) / rr : qq / rr);
+              }
+              if (cin_o) {
+                float rr = sqrtf(r2o);
+                two_sum_add(re_h, re_l, ff.ewald ? -qq * erfc_f32(alpha * rr) / rr : -qq / rr);
+              }
+            }
+          } else {
+            float rr2 = sg2 / r2n, r6 = rr2 * rr2 * rr2;
+            two_sum_add(lj_h, lj_l, ecn * (r6 * r6 - r6));
+            if (coul && cin_n) {
+              float rr = sqrtf(r2n);
+              two_sum_add(re_h, re_l, ff.ewald ? qq * erfc_f32(alpha * rr) / rr : qq / rr);
+            }
+          }
+        } else {
+          if (!in_o || in_n)
+            continue;  // counted from the new position's cells
+          float rr2 = sg2 / r2o, r6 = rr2 * rr2 * rr2;
+          two_sum_add(lj_h, lj_l, -ecn * (r6 * r6 - r6));
+          if (coul && cin_o) {
+            float rr = sqrtf(r2o);
+            two_sum_add(re_h, re_l, ff.ewald ? -qq * erfc_f32(alpha * rr) / rr : -qq / rr);
+          }
+        }
+      }
+    }
+    // ---------------- reciprocal space ----------------
+    float de_h = 0.f, de_l = 0.f;
+    for (int i = threadIdx.x; i < kc; i += MT_THREADS) {
+      char4 n = kn[i];
+      float fx = (float)n.x, fy = (float)n.y, fz = (float)n.z;
+      float ddR = 0.f, ddI = 0.f;
+      for (int a = 0; a < na; ++a) {
+        float q = h.qf[a];
+        if (q == 0.f)
+          continue;
+        float arg = fmaf(fx, h.hf[a][0], fmaf(fy, h.hf[a][1], fz * h.hf[a][2]));
+        float w = 2.0f * q * sin_f32(arg);
+        const float2 *rx = tab + (size_t)(3 * a) * stride;
+        float2 e = cmulf(cmulf(rx[n.x], tabf(rx + stride, n.y)),
+                         tabf(rx + 2 * stride, n.z));
+        ddR = fmaf(-w, e.y, ddR);
+        ddI = fmaf(w, e.x, ddI);
+      }
+      dR[i] = ddR;
+      dI[i] = ddI;
+      float sr = s32R[i], si = s32I[i];
+      two_sum_add(de_h, de_l, pf[i] * fmaf(2.0f * sr + ddR, ddR, (2.0f * si + ddI) * ddI));
+    }
+    // ---------------- reduce: warp (FP32), CTA (FP64) ----------------
+    // compensated warp reduction, then FP64 across warps
+    float vh[3] = {lj_h, re_h, de_h}, vl[3] = {lj_l, re_l, de_l}, v3 = ovl;
+    for (int o = 16; o > 0; o >>= 1) {
+      for (int c = 0; c < 3; ++c) {
+        float oh = __shfl_down_sync(0xffffffffu, vh[c], o);
+        float ol = __shfl_down_sync(0xffffffffu, vl[c], o);
+        two_sum_add(vh[c], vl[c], oh);
+        vl[c] += ol;
+      }
+      v3 = fmaxf(v3, __shfl_down_sync(0xffffffffu, v3, o));
+    }
+    int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+      for (int c = 0; c < 3; ++c)
+        S.wred[w][c] = (double)vh[c] + (double)vl[c];
+      S.wred[w][3] = v3;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4) {
+      int c = threadIdx.x;
+      double acc = 0.0;
+      for (int i = 0; i < MT_THREADS / 32; ++i)
+        acc = c == 3 ? fmax(acc, S.wred[i][3]) : acc + S.wred[i][c];
+      S.part[c] = acc;
+    }
+    cluster.sync();
+    // ---------------- decision (identical in every CTA) ----------------
+    if (threadIdx.x < 32) {
+      double p[4] = {0, 0, 0, 0};
+      if ((int)threadIdx.x < csize) {
+        const double *rp = cluster.map_shared_rank(S.part, (unsigned)threadIdx.x);
+        for (int c = 0; c < 4; ++c)
+          p[c] = rp[c];
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        p[0] += __shfl_down_sync(0xffffffffu, p[0], o);
+        p[1] += __shfl_down_sync(0xffffffffu, p[1], o);
+        p[2] += __shfl_down_sync(0xffffffffu, p[2], o);
+        p[3] = fmax(p[3], __shfl_down_sync(0xffffffffu, p[3], o));
+      }
+      if (threadIdx.x == 0) {
+        bool over = p[3] > 0;
+        double dLJ = p[0], dRe = p[1], dRc = over ? 0.0 : p[2];
+        double ex = -ff.beta * ((dLJ + dRe) + dRc);
+        int acc = !over && (ex > h.lpacc);
+        if (acc) {
+          S.e_run[0] += dLJ;
+          S.e_run[1] += dRe;
+          S.e_run[2] += dRc;
+          S.nacc++;
+        }
+        settings_update(S.set, h.kind, acc);
+        S.accept = acc;
+        if (rank == 0 && C.tr_i) {
+          C.tr_i[3 * (size_t)t] = h.kind;
+          C.tr_i[3 * (size_t)t + 1] = m;
+          C.tr_i[3 * (size_t)t + 2] = acc;
+          C.tr_d[3 * (size_t)t] = dLJ;
+          C.tr_d[3 * (size_t)t + 1] = dRe;
+          C.tr_d[3 * (size_t)t + 2] = dRc;
+        }
+      }
+    }
+    __syncthreads();
+    const int acc = S.accept;
+    const int prev_m = m, prev_kind = h.kind;
+    if (acc) {
+      for (int i = threadIdx.x; i < kc; i += MT_THREADS) {
+        two_sum_add(pRh[i], pRl[i], dR[i]);
+        two_sum_add(pIh[i], pIl[i], dI[i]);
+        s32R[i] += dR[i];
+        s32I[i] += dI[i];
+      }
+      if (rank == 0 && threadIdx.x == 0) {
+        for (int a = 0; a < na; ++a) {
+          const double *np = h.newp[a];
+          int at = h.a0 + a;
+          b.x[at] = np[0];
+          b.y[at] = np[1];
+          b.z[at] = np[2];
+          cell_move_atom(b, at, np[0], np[1], np[2], h.cell_new[a]);
+        }
+        if (h.kind == 0) {
+          b.cx[m] = h.newcom[0];
+          b.cy[m] = h.newcom[1];
+          b.cz[m] = h.newcom[2];
+        }
+      }
+      if (S.nacc >= C.flush_every) {
+        __syncthreads();
+        flush();
+        if (threadIdx.x == 0)
+          S.nacc = 0;
+      }
+    }
+    if (t + 1 < C.n) {
+      long long step = C.first + t + 1;
+      if ((step + 1) % S.set.adj == 0) {
+        __syncthreads();
+        if (threadIdx.x == 0)
+          settings_adjust(S.set, step);
+        __syncthreads();
+        make_props(t + 1);
+        cluster.sync();
+      }
+      __syncthreads();
+      mixed_header(C, S, t + 1, acc, prev_m, prev_kind);
+      mixed_tables(C, S, tab);
+    }
+    cluster.sync();  // the cell grid committed by rank 0 is visible
+  }
+  __syncthreads();
+  flush();
+  __syncthreads();
+  for (int i = threadIdx.x; i < kc; i += MT_THREADS) {
+    b.sumRref[kbeg + i] = s64R[i];
+    b.sumIref[kbeg + i] = s64I[i];
+  }
+  if (rank == 0 && threadIdx.x == 0) {
+    *C.set = S.set;
+    for (int i = 0; i < 5; ++i)
+      b.energy[i] = S.e_run[i];
+  }
+}
+
+size_t mixed_smem(int K, int kmax, int csize) {
+  int kc_max = (K + csize - 1) / csize;
+  MixedLayout L = mixed_layout(kc_max);
+  return L.tab + sizeof(float2) * (size_t)3 * MAXA * (kmax + 1) + 16;
+}
+
+int launch_chain_mixed(cudaStream_t st, const MixedChain *d_chains, int nchains,
+                       int csize, size_t smem) {
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaFuncSetAttribute(k_chain_mixed,
+                         cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    attr_done = true;
+  }
+  cudaFuncSetAttribute(k_chain_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nchains * csize);
+  cfg.blockDim = dim3(MT_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = csize;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, k_chain_mixed, d_chains);
+  return e == cudaSuccess ? OK : ERR_CUDA;
+}
+
+int max_active_clusters(int csize, size_t smem) {
+  cudaFuncSetAttribute(k_chain_mixed,
+                       cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaFuncSetAttribute(k_chain_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(csize);
+  cfg.blockDim = dim3(MT_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = csize;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_chain_mixed, &cfg) != cudaSuccess)
+    return 0;
+  return n;
+}
+
+}  // namespace gb

@@ -251,7 +251,8 @@ class Box:
     # ---- Monte Carlo ----------------------------------------------------------
     def mc_init(self, seed: int, move_frac: Sequence[float], adj_steps: int,
                 scales: Optional[Sequence[float]] = None,
-                recompute_freq: int = 0) -> None:
+                recompute_freq: int = 0, cluster_size: int = 0,
+                flush_every: int = 0) -> None:
         p = _lib.McParams()
         p.seed = int(seed) & 0xFFFFFFFF
         for i in range(3):
@@ -262,7 +263,17 @@ class Box:
             for i in range(4):
                 p.scales[i] = float(scales[i])
         p.recompute_freq = int(recompute_freq)
+        p.cluster_size = int(cluster_size)
+        p.flush_every = int(flush_every)
         self._chk(lib().gb_mc_init(self.h, C.byref(p)))
+
+    def mc_drift(self):
+        mx, last = np.empty(4), np.empty(4)
+        n = C.c_int64()
+        self._chk(lib().gb_mc_drift(self.h, _dp(mx), _dp(last), C.byref(n)))
+        names = ["inter", "real", "recip", "total"]
+        return dict(max=dict(zip(names, mx.tolist())),
+                    last=dict(zip(names, last.tolist())), recomputes=n.value)
 
     def mc_run(self, first_step: int, nsteps: int, trace: bool = False):
         if not trace:

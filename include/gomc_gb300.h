@@ -155,6 +155,8 @@ typedef struct gb_mc_params {
   int32_t use_scales;     /* 1: start from scales[] instead of the defaults */
   double scales[4];       /* displacement, rotation, MP t_max, MP r_max */
   int32_t recompute_freq; /* GB300RecomputeFreq (mixed form), 0 = never */
+  int32_t cluster_size;   /* mixed form: CTAs per chain (0 = autotuned) */
+  int32_t flush_every;    /* mixed form: accepted moves per FP64 fold (0 = 64) */
 } gb_mc_params;
 
 int gb_mc_init(gb_box *box, const gb_mc_params *params);
@@ -173,6 +175,12 @@ int gb_mc_state(gb_box *box, double *scales4, int64_t *counts6);
 int gb_mc_timing(gb_box *box, int32_t reset, double *chain_ms,
                  int64_t *chain_launches, int64_t *chain_moves, double *mp_ms,
                  int64_t *mp_moves);
+/* Mixed form: relative difference between the running energies and the
+ * periodic full FP64 recompute (inter, real, recip, total), largest and
+ * latest, and the number of recomputes so far.  No reference counterpart
+ * (the reference's check is Simulation::RecalculateAndCheck,
+ * src/Simulation.cpp:170-223, at 1e-3). */
+int gb_mc_drift(gb_box *box, double *max4, double *last4, int64_t *recomputes);
 /* The CUDA stream (cudaStream_t) every call on this machine is ordered on. */
 int gb_box_stream(gb_box *box, void **stream);
 

@@ -1,0 +1,113 @@
+"""Mixed-precision form against the FP64 form on the same move streams.
+
+Bars: every running energy term within 1e-6 relative of a full FP64
+recompute; per-move energy changes within 1e-2 K (3.4e-5 kT at 298 K) or
+1e-4 of the FP64 change, whichever is larger (FP32 rounding of single pair
+changes of a few thousand K, e.g. hydrogen-bonded O-H pairs, leaves a few
+1e-3 K); the same accept/reject sequence as the FP64
+chain over the compared moves; total-energy drift at most 1e-8 relative
+between full FP64 recomputes every 10,000 moves; a box run inside a batched
+launch gives bit-identical state to the same box run alone over the same
+call boundaries (each call ends by folding the FP32 window of accepted
+structure-factor changes into the FP64 accumulators).
+"""
+import numpy as np
+import pytest
+
+from gomc_gb300.config import SimConfig
+from gomc_gb300.systems import spce_water_box
+
+pytestmark = pytest.mark.gpu
+
+TERM_REL = 1e-6      # running energy term vs FP64 recompute
+DE_ABS = 1e-2        # per-move dE, K
+DE_REL = 1e-4
+DRIFT_REL = 1e-8     # total energy between recomputes
+SCALES = [0.3, 0.3, 0.02, 0.03]
+
+# (molecules, box edge A, cutoff A): the 256-water box has cells narrower
+# than the cutoff (3 per axis, 6.57 A); the larger ones have wide cells.
+SYSTEMS = [(256, 19.7, 9.0), (2000, 39.1, 10.0), (8000, 62.1, 10.0)]
+
+
+@pytest.fixture(scope="module")
+def gb():
+    from gomc_gb300 import engine
+    engine.lib(build_if_missing=True)
+    return engine
+
+
+def make(gb, nmol, L, rc, precision, seed=7):
+    s = spce_water_box(nmol, L, seed=seed)
+    return gb.Box(s, SimConfig(temperature=298.0, rcut=rc, tolerance=1e-5),
+                  precision=precision)
+
+
+@pytest.mark.parametrize("nmol,L,rc", SYSTEMS)
+def test_mixed_follows_fp64(gb, nmol, L, rc):
+    n = 600
+    bf = make(gb, nmol, L, rc, gb.GB_FP64)
+    bm = make(gb, nmol, L, rc, gb.GB_MIXED)
+    for b in (bf, bm):
+        b.mc_init(1234, [0.5, 0.5, 0.0], 200, scales=SCALES)
+    rf = bf.mc_run(0, n, trace=True)
+    rm = bm.mc_run(0, n, trace=True)
+    np.testing.assert_array_equal(rm["mol"], rf["mol"])
+    np.testing.assert_array_equal(rm["kind"], rf["kind"])
+    np.testing.assert_array_equal(rm["accepted"], rf["accepted"])
+    err = np.abs(rm["de"] - rf["de"])
+    bound = np.maximum(DE_ABS, DE_REL * np.abs(rf["de"]))
+    ok = err <= bound
+    assert ok.all(), (np.argwhere(~ok)[:5], err.max(axis=0))
+    run = bm.energy()
+    st = bm.system_total()
+    for i, term in enumerate(["inter", "real", "recip"]):
+        rel = abs(run[i] - st[term]) / abs(st[term])
+        assert rel <= TERM_REL, (term, rel)
+    # both chains moved the same molecules to the same places (to FP64
+    # rounding of the shared proposal arithmetic, which is identical)
+    np.testing.assert_array_equal(bm.coords(), bf.coords())
+    bf.close()
+    bm.close()
+
+
+def test_mixed_drift_between_recomputes(gb):
+    b = make(gb, 8000, 62.1, 10.0, gb.GB_MIXED)
+    b.mc_init(99, [0.5, 0.5, 0.0], 1000, scales=SCALES, recompute_freq=10000)
+    b.mc_run(0, 50000)
+    d = b.mc_drift()
+    assert d["recomputes"] == 5
+    assert d["max"]["total"] <= DRIFT_REL, d
+    for term in ("inter", "real", "recip"):
+        assert d["max"][term] <= TERM_REL, d
+    b.close()
+
+
+def test_batch_matches_alone(gb):
+    sizes = [(256, 19.7, 9.0), (2000, 39.1, 10.0), (1000, 31.0, 10.0)]
+
+    def boxes(seed0):
+        out = []
+        for i, (n, L, rc) in enumerate(sizes):
+            b = make(gb, n, L, rc, gb.GB_MIXED, seed=seed0 + i)
+            b.mc_init(500 + i, [0.5, 0.5, 0.0], 300, scales=SCALES,
+                      cluster_size=8)
+            out.append(b)
+        return out
+
+    alone = boxes(11)
+    for b in alone:
+        b.mc_run(0, 400)
+        b.mc_run(400, 300)
+    mixed = boxes(11)
+    gb.mc_run_batch(mixed, 0, 400)
+    gb.mc_run_batch(mixed, 400, 300)
+    for a, m in zip(alone, mixed):
+        np.testing.assert_array_equal(m.coords(), a.coords())
+        np.testing.assert_array_equal(m.energy(), a.energy())
+        sa, ca = a.mc_state()
+        sm, cm = m.mc_state()
+        np.testing.assert_array_equal(sm, sa)
+        np.testing.assert_array_equal(cm, ca)
+    for b in alone + mixed:
+        b.close()
