@@ -101,7 +101,11 @@ SIGNATURES = {
     "gb_mc_timing": (C.c_int, [_P, C.c_int32, _D, _L, _L, _D, _L]),
     "gb_box_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "gb_mc_drift": (C.c_int, [_P, _D, _D, _L]),
+    "gb_recip_energy_noalloc": (C.c_int, [_P, _P, _P, C.c_int32, _P, _P]),
 }
+
+# fixed scratch of gb_recip_energy_noalloc (include/gomc_gb300.h)
+RECIP_NOALLOC_MAX_K = 256 * 1024
 
 
 def lib_path() -> str:

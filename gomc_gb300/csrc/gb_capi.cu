@@ -20,6 +20,11 @@ int guard(gb_box *box) {
 }
 }  // namespace
 
+namespace gb {
+// Message returned by gb_last_error(NULL) for calls that take no box.
+void set_api_error(const char *msg) { g_create_error = msg; }
+}  // namespace gb
+
 extern "C" {
 
 const char *gb_version(void) { return "gomc_gb300 0.1 (sm_103a)"; }

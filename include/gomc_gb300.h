@@ -189,6 +189,31 @@ int gb_box_stream(gb_box *box, void **stream);
 int gb_mc_run_batch(gb_box **boxes, int32_t nboxes, int64_t first_step,
                     int64_t nsteps);
 
+/* ---- Reciprocal energy without device allocation ----
+ * No counterpart in the reference.  It is the reduction behind BoxReciprocal
+ * (src/Ewald.cpp:375-406), E = sum_k prefact[k] (sumR[k]^2 + sumI[k]^2),
+ * over caller-owned device arrays of K doubles, with the result written to
+ * the device double *d_energy, ordered on `stream` (a cudaStream_t; NULL is
+ * the legacy default stream) of the current device.
+ *
+ * For callers that may not allocate device memory once running: a serving
+ * loop that admits jobs by device memory and has committed all of it, or a
+ * host whose device memory belongs to another allocator.  The call issues no
+ * cudaMalloc/cudaFree and no allocating library routine; its scratch is a
+ * fixed 8 KiB device array inside this library, one FP64 partial per 256
+ * k-vectors, hence the limit on K (larger K: GB_ERR_CAPACITY, nothing
+ * launched).  The first call on a device looks up that array's address with
+ * the device current; make it before any stream capture.  Calls that overlap
+ * in time on one device share the array and race: serialise them.  The sum
+ * is taken in the order of gb_box_reciprocal.  Errors: GB_ERR_ARG (null
+ * pointer, K < 0), GB_ERR_CAPACITY, GB_ERR_CUDA; gb_last_error(NULL) gives
+ * the message. */
+#define GB_RECIP_NOALLOC_MAX_PARTIALS 1024
+#define GB_RECIP_NOALLOC_MAX_K (256 * GB_RECIP_NOALLOC_MAX_PARTIALS)
+int gb_recip_energy_noalloc(const double *d_sumR, const double *d_sumI,
+                            const double *d_prefact, int32_t K,
+                            double *d_energy, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
