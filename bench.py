@@ -235,6 +235,182 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
+              fp64_value):
+    """The mixed-precision form on the same workload.
+
+    accuracy: an FP64 chain and a mixed chain from the same seed run the same
+      moves; reported are the share of identical accept decisions, the
+      per-move energy-change errors and the running energy terms of the mixed
+      chain against a full FP64 recompute.
+    single:   one mixed chain, moves/s (device time, L2 flushed between steps).
+    batched:  independent replicas of the box (seeds differ), all chains in one
+      launch per step; moves/s over all chains, device time.
+    e2e:      the batched run through the public API with host buffers:
+      coordinates of every replica uploaded, moves run, energies and
+      coordinates read back, every step.
+    drift:    largest relative difference between the running energies and
+      the periodic FP64 recompute (every 10,000 moves) over the run."""
+    from gomc_gb300._lib import GB_FP64, GB_MIXED
+    out = {}
+    sysm, cfg = make_system(rank)
+    n_cmp = args.mixed_compare_moves
+    bf = engine.Box(sysm, cfg, device=dev, precision=GB_FP64)
+    bm = engine.Box(sysm, cfg, device=dev, precision=GB_MIXED)
+    for b in (bf, bm):
+        b.mc_init(SEED + rank, FRAC, ADJ, scales=SCALES,
+                  cluster_size=args.cluster)
+    rf = bf.mc_run(0, n_cmp, trace=True)
+    rm = bm.mc_run(0, n_cmp, trace=True)
+    same = float(np.mean(rf["accepted"] == rm["accepted"]))
+    sig = rm["de"] - rf["de"]
+    err = np.abs(sig)
+    # running-energy error the mixed chain accumulates over its accepted
+    # moves (both chains take the same decisions), per term, in K
+    accm = rm["accepted"].astype(bool) & rf["accepted"].astype(bool)
+    acc_err = sig[accm].sum(axis=0)
+    tot_f = rf["de"].sum(axis=1)
+    tot_m = rm["de"].sum(axis=1)
+    rel = np.abs(tot_m - tot_f) / np.maximum(np.abs(tot_f), 1e-300)
+    run = bm.energy()
+    st = bm.system_total()
+    term_rel = {k: abs(run[i] - st[k]) / abs(st[k])
+                for i, k in enumerate(["inter", "real", "recip"])}
+    run_tot = float(sum(run[:5]))
+    st_tot = sum(st[k] for k in ("inter", "real", "recip", "self",
+                                 "correction"))
+    term_rel["total"] = abs(run_tot - st_tot) / abs(st_tot)
+    out["accuracy"] = {
+        "moves": n_cmp, "same_decisions": same,
+        "de_abs_max_K": {"inter": float(err[:, 0].max()),
+                         "real": float(err[:, 1].max()),
+                         "recip": float(err[:, 2].max())},
+        "de_rms_K": {"inter": float(np.sqrt(np.mean(sig[:, 0] ** 2))),
+                     "real": float(np.sqrt(np.mean(sig[:, 1] ** 2))),
+                     "recip": float(np.sqrt(np.mean(sig[:, 2] ** 2)))},
+        "accumulated_over_accepted_K": {"inter": float(acc_err[0]),
+                                        "real": float(acc_err[1]),
+                                        "recip": float(acc_err[2])},
+        "accumulated_total_rel": float(abs(acc_err.sum()) / abs(st_tot)),
+        "de_total_rel_median": float(np.median(rel)),
+        "running_vs_fp64_recompute_rel": term_rel,
+        "tolerance": "every running term <= 1e-6 relative of the FP64 "
+                     "recompute; decisions identical"}
+    layout = bm.mc_layout()
+    bf.close()
+
+    M = args.moves_per_step
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32,
+                        device=dev)
+
+    def timed(run_step, stream):
+        times = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            run_step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+        return times
+
+    # single mixed chain (continues from the comparison run)
+    st_single = torch.cuda.ExternalStream(bm.stream_ptr(), device=dev)
+    step = [n_cmp]
+
+    def one():
+        bm.mc_run(step[0], M)
+        step[0] += M
+    for _ in range(args.warmup):
+        one()
+    barrier()
+    t_single = timed(one, st_single)
+    bm.close()
+    single = args.steps * M / sum(t_single)
+    out["single"] = {"value": single, "unit": "moves/s",
+                     "ms_per_step": sum(t_single) / args.steps * 1e3,
+                     "us_per_move": sum(t_single) / (args.steps * M) * 1e6,
+                     "ctas_per_chain": layout["ctas_per_chain"]}
+
+    # batched replicas, one launch per step for every chain
+    B = args.mixed_chains or layout["max_concurrent"]
+    boxes = []
+    for i in range(B):
+        s_i, c_i = make_system(rank * 1000 + i)
+        b = engine.Box(s_i, c_i, device=dev, precision=GB_MIXED)
+        b.mc_init(SEED + rank * 1000 + i, FRAC, ADJ, scales=SCALES,
+                  recompute_freq=10000, cluster_size=args.cluster)
+        boxes.append(b)
+    st_batch = torch.cuda.ExternalStream(boxes[0].stream_ptr(), device=dev)
+    bstep = [0]
+
+    def batch():
+        engine.mc_run_batch(boxes, bstep[0], M)
+        bstep[0] += M
+    for _ in range(args.warmup):
+        batch()
+    barrier()
+    with ClockSampler(dev) as clk:
+        t_batch = timed(batch, st_batch)
+    barrier()
+    t_tot = float(sum(t_batch))
+    if dist:
+        tt = torch.tensor([t_tot], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_tot = float(tt.item())
+    batched = world * args.steps * M * B / t_tot
+    timing = boxes[0].mc_timing(reset=True)
+
+    # end to end through the public API with host buffers
+    host = [(b.coords(), b.com()) for b in boxes]
+    e2e_t = []
+    barrier()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        for b, (xyz, com) in zip(boxes, host):
+            b.set_coords(xyz, com)
+        engine.mc_run_batch(boxes, bstep[0], M)
+        bstep[0] += M
+        host = []
+        for b in boxes:
+            b.energy()
+            host.append((b.coords(), b.com()))
+        e2e_t.append(time.perf_counter() - t0)
+    barrier()
+    t_e2e = float(sum(e2e_t))
+    if dist:
+        tt = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    per_box = (sysm.n_atoms + sysm.n_mol) * 3 * 8
+    drift = {"max": {}, "recomputes": 0}
+    for b in boxes:
+        d = b.mc_drift()
+        drift["recomputes"] += d["recomputes"]
+        for k, v in d["max"].items():
+            drift["max"][k] = max(drift["max"].get(k, 0.0), v)
+    for b in boxes:
+        b.close()
+    out["batched"] = {
+        "value": batched, "unit": "moves/s", "chains": B,
+        "ms_per_step": sum(t_batch) / args.steps * 1e3,
+        "step_ms": [round(t * 1e3, 3) for t in t_batch],
+        "kernel_launches": timing["chain_launches"],
+        "speedup_vs_fp64": batched / fp64_value,
+        "clocks": clk.summary()}
+    out["e2e"] = {"value": world * args.steps * M * B / t_e2e,
+                  "unit": "moves/s",
+                  "h2d_bytes_per_step": B * (per_box + M * 64),
+                  "d2h_bytes_per_step": B * (5 * 8 + per_box)}
+    out["drift"] = dict(drift, recompute_every=10000,
+                        bar="total-energy drift <= 1e-8 relative")
+    out["dtype"] = "f32 pair/k terms, f64 accumulators"
+    return out
+
+
 def run_gb300(args, rank, world):
     import torch
     dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -319,8 +495,10 @@ def run_gb300(args, rank, world):
              for i, k in enumerate(["inter", "real", "recip"])}
 
     mixed = None
-    if not args.no_mixed and hasattr(engine, "run_mixed_bench"):
-        mixed = engine.run_mixed_bench(args, dev, rank, world)
+    if not args.no_mixed:
+        box.close()
+        mixed = run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
+                          value)
 
     if rank != 0:
         if dist:
@@ -378,6 +556,12 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--mixed-chains", type=int, default=0,
+                    help="replicas in the batched mixed run (0: as many as "
+                         "the GPU holds at once)")
+    ap.add_argument("--cluster", type=int, default=0,
+                    help="CTAs per mixed chain (0: autotuned)")
+    ap.add_argument("--mixed-compare-moves", type=int, default=10000)
     ap.add_argument("--small", action="store_true",
                     help="256-water box instead of the 8000-water workload")
     args = ap.parse_args()

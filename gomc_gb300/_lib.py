@@ -52,7 +52,13 @@ class McParams(C.Structure):
     _fields_ = [("seed", C.c_uint32), ("frac", C.c_double * 3),
                 ("adj_steps", C.c_int32), ("use_scales", C.c_int32),
                 ("scales", C.c_double * 4), ("recompute_freq", C.c_int32),
-                ("cluster_size", C.c_int32), ("flush_every", C.c_int32)]
+                ("cluster_size", C.c_int32), ("flush_every", C.c_int32),
+                ("move_buffer", C.c_int32)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("quantum", C.c_int32),
+                ("mem_budget", C.c_int64), ("max_resident", C.c_int32)]
 
 
 # every function the header declares: name -> (restype, argtypes)
@@ -100,8 +106,24 @@ SIGNATURES = {
                                   C.c_int64]),
     "gb_mc_timing": (C.c_int, [_P, C.c_int32, _D, _L, _L, _D, _L]),
     "gb_box_stream": (C.c_int, [_P, C.POINTER(_P)]),
+    "gb_mc_layout": (C.c_int, [_P, _I, _I, _L]),
     "gb_mc_drift": (C.c_int, [_P, _D, _D, _L]),
     "gb_recip_energy_noalloc": (C.c_int, [_P, _P, _P, C.c_int32, _P, _P]),
+    "gb_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P)]),
+    "gb_server_destroy": (None, [_P]),
+    "gb_server_submit": (C.c_int, [_P, C.POINTER(SystemDesc),
+                                   C.POINTER(Config), C.POINTER(McParams),
+                                   C.c_int64, C.c_int64, _L]),
+    "gb_server_estimate": (C.c_int, [_P, C.POINTER(SystemDesc),
+                                     C.POINTER(Config), C.POINTER(McParams),
+                                     _L, _I]),
+    "gb_server_step": (C.c_int, [_P, _I]),
+    "gb_server_start": (C.c_int, [_P]),
+    "gb_server_drain": (C.c_int, [_P, C.c_double]),
+    "gb_server_job": (C.c_int, [_P, C.c_int64, _I, _L, _D]),
+    "gb_server_result": (C.c_int, [_P, C.c_int64, _D, _D, _D]),
+    "gb_server_stats": (C.c_int, [_P, _D]),
+    "gb_server_error": (C.c_char_p, [_P]),
 }
 
 # fixed scratch of gb_recip_energy_noalloc (include/gomc_gb300.h)

@@ -15,6 +15,14 @@ namespace gb {
 void build_ff(const HostSystem &s, const BoxConfig &c, FF *ff) {
   std::memset(ff, 0, sizeof(FF));
   int nk = s.n_kinds;
+  // FP32 turn length of the mixed form: fl(L 2^-32) = (L 2^-32) / (1 + eta)
+  double eta = 0.0;
+  for (int d = 0; d < 3; ++d) {
+    double exact = s.L[d] * 2.3283064365386963e-10;
+    eta += exact / (double)(float)exact - 1.0;
+  }
+  eta /= 3.0;
+  const double len2 = (1.0 + eta) * (1.0 + eta);
   ff->n_kinds = nk;
   for (int i = 0; i < nk; ++i)
     for (int j = 0; j < nk; ++j) {
@@ -34,6 +42,13 @@ void build_ff(const HostSystem &s, const BoxConfig &c, FF *ff) {
       ff->nOver6[idx] = n / 6;
       ff->sigmaSq_f[idx] = (float)ff->sigmaSq[idx];
       ff->eps_cn_f[idx] = (float)ff->eps_cn[idx];
+      double rs = ff->sigmaSq_f[idx] != 0.0f
+                      ? ff->sigmaSq[idx] / (double)ff->sigmaSq_f[idx] / len2
+                      : 1.0;
+      double re = ff->eps_cn_f[idx] != 0.0f
+                      ? ff->eps_cn[idx] / (double)ff->eps_cn_f[idx] : 1.0;
+      ff->lj_k6_f[idx] = (float)(re * std::pow(rs, 6) - 1.0);
+      ff->lj_k3_f[idx] = (float)(re * std::pow(rs, 3) - 1.0);
     }
   ff->rcut = c.rcut;
   ff->rcutSq = c.rcut * c.rcut;
@@ -44,9 +59,25 @@ void build_ff(const HostSystem &s, const BoxConfig &c, FF *ff) {
   if (c.ewald) {
     ff->alpha = std::sqrt(-std::log(c.tolerance)) / c.rcut_coulomb;
     ff->alphaSq = ff->alpha * ff->alpha;
+    ff->alpha_f = (float)ff->alpha;
+    ff->coul_da_f =
+        (float)((ff->alpha * (1.0 + eta) - (double)ff->alpha_f) * M_2_SQRTPI);
     ff->recip_rcut = -2.0 * std::log(c.tolerance) / c.rcut_coulomb;
     ff->recip_rcutSq = ff->recip_rcut * ff->recip_rcut;
   }
+  ff->coul_qfac_f = (float)(1.0 / (1.0 + eta) - 1.0);
+  for (int d = 0; d < 3; ++d) {
+    double t = s.L[d] * 2.3283064365386963e-10;
+    double t2 = t * t;
+    ff->turn2_hi[d] = (float)t2;
+    ff->turn2_lo[d] = (float)(t2 - (double)ff->turn2_hi[d]);
+  }
+  double a3 = ff->alpha * ff->alpha * ff->alpha;
+  ff->alpha2_f = (float)ff->alphaSq;
+  ff->alpha3_hi = (float)a3;
+  ff->alpha3_lo = (float)(a3 - (double)ff->alpha3_hi);
+  // close-pair path: r < 4 A, and alpha r <= 2 (the range of its erf fit)
+  ff->close_r2_f = (float)std::min(16.0, c.ewald ? 0.99 * 4.0 / ff->alphaSq : 16.0);
   ff->beta = 1 / c.temperature;
 }
 
@@ -118,6 +149,7 @@ int Box::Alloc(T **p, size_t n) {
   if (e != cudaSuccess)
     return CudaCheck(e, "cudaMalloc");
   allocs_.push_back(q);
+  dev_bytes += std::max<size_t>(n, 1) * sizeof(T);
   *p = (T *)q;
   return OK;
 }
@@ -306,7 +338,8 @@ int Box::Init(const HostSystem &s0, const BoxConfig &c) {
       (rc = Alloc(&d.mstart, M + 1)) || (rc = Alloc(&d.nbr, nbr.size())) ||
       (rc = Alloc(&d.cell_count, d.ncell)) || (rc = Alloc(&d.cell_atom, NC)) ||
       (rc = Alloc(&d.cell_pos, NC)) || (rc = Alloc(&d.cell_meta, NC)) ||
-      (rc = Alloc(&d.cell_fix, NC)) || (rc = Alloc(&d.atom_cell, N)) ||
+      (rc = Alloc(&d.cell_fix, NC)) || (rc = Alloc(&d.cell_qlo, NC)) ||
+      (rc = Alloc(&d.atom_cell, N)) ||
       (rc = Alloc(&d.atom_slot, N)) || (rc = Alloc(&d.energy, 8)) ||
       (rc = Alloc(&d.err, 4)) || (rc = Alloc(&d_ff, 1)) ||
       (rc = Alloc(&d_small, 4096)) || (rc = Alloc(&d_aF, 3 * (size_t)N)) ||

@@ -69,6 +69,7 @@ class Box {
   int sm_count = 0;
   std::string last_error;
   McState *mc = nullptr;
+  size_t dev_bytes = 0;  // device memory this box allocated (without mc)
 
   // scratch buffers
   double *d_scratch = nullptr;   // reduction partials

@@ -289,6 +289,32 @@ int gb_mc_drift(gb_box *box, double *max4, double *last4, int64_t *n) {
     *n = s.recomputes;
   return gb::OK;
 }
+int gb_mc_layout(gb_box *box, int32_t *ctas_per_chain,
+                 int32_t *max_concurrent, int64_t *smem_bytes) {
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  gb::Box &b = *box->b;
+  if (!b.mc)
+    return b.Fail(gb::ERR_STATE, "gb_mc_init has not been called");
+  gb::McState &s = *b.mc;
+  int per = 1, conc = 1;
+  size_t sm = 0;
+  if (b.cfg.precision == GB_MIXED) {
+    per = s.cluster;
+    sm = s.mixed_smem;
+    conc = gb::max_active_clusters(s.cluster, s.mixed_smem);
+  } else {
+    per = s.grid;
+  }
+  if (ctas_per_chain)
+    *ctas_per_chain = per;
+  if (max_concurrent)
+    *max_concurrent = conc;
+  if (smem_bytes)
+    *smem_bytes = (int64_t)sm;
+  return gb::OK;
+}
 int gb_box_stream(gb_box *box, void **stream) {
   int rc = guard(box);
   if (rc)

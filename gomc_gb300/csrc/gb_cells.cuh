@@ -21,8 +21,11 @@ __device__ __forceinline__ void cell_write_slot(const DevBox &b, int cell,
   b.cell_atom[s] = a;
   b.cell_pos[s] = make_double4_32a(x, y, z, q);
   b.cell_meta[s] = pack_meta(b.mol[a], b.kind[a]);
+  double qs = q * SQRT_QQ_FACT;
+  float qsf = (float)qs;
   b.cell_fix[s] = make_uint4(to_turns(x, b.invL[0]), to_turns(y, b.invL[1]),
-                             to_turns(z, b.invL[2]), __float_as_uint((float)q));
+                             to_turns(z, b.invL[2]), __float_as_uint(qsf));
+  b.cell_qlo[s] = (float)(qs - (double)qsf);
   b.atom_cell[a] = cell;
   b.atom_slot[a] = slot;
 }
@@ -52,6 +55,7 @@ __device__ __forceinline__ bool cell_move_atom(const DevBox &b, int a, double x,
     b.cell_pos[to] = b.cell_pos[from];
     b.cell_meta[to] = b.cell_meta[from];
     b.cell_fix[to] = b.cell_fix[from];
+    b.cell_qlo[to] = b.cell_qlo[from];
     b.atom_slot[moved] = s0;
   }
   b.cell_count[c0] = last;

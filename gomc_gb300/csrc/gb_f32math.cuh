@@ -6,10 +6,16 @@
 //    truncation error below 2e-9.
 //  * sin of an FP32 radian argument: Cody-Waite reduction by pi/2 with a
 //    two-term split of pi/2, then the same octant polynomials.
-//  * erfc for x >= 0: the Chebyshev-fitted form erfc(x) = t exp(-x^2 + P(t)),
-//    t = 1/(1 + x/2), of Press et al., Numerical Recipes (2nd ed., sec. 6.2,
-//    "erfcc"), fractional error < 1.2e-7; x^2 is split into an exact
-//    hi + lo pair so that exp sees the argument to full precision.
+//  * erfc for x >= 0 in the form erfc(x) = t exp(-x^2 + P(s)), t = 1/(1 + x/2),
+//    of Press et al., Numerical Recipes (2nd ed., sec. 6.2, "erfcc"), with P
+//    this project's own degree-12 Chebyshev fit (fit_f32math.py; fit error
+//    below 1e-10 over [0, 5]); x^2 is split into an exact hi + lo pair so
+//    that exp sees the argument to full precision.
+//  * erf(t)/t as a degree-12 polynomial in u = t^2 (fit_f32math.py), used
+//    through its divided difference for close pairs.
+//  * float-float arithmetic (hi + lo pairs, Dekker 1971; Knuth TAOCP 2,
+//    sec. 4.2.2) for the 1/r difference of close pairs from exact integer
+//    squared distances.
 #pragma once
 
 #include <stdint.h>
@@ -37,7 +43,8 @@ __device__ __forceinline__ float2 cis_turns(uint32_t phase) {
   int32_t s = (int32_t)phase;                  // turns in [-1/2, 1/2)
   int32_t q = (s + (1 << 29)) >> 30;           // nearest quarter turn
   int32_t r = s - (int32_t)((uint32_t)q << 30);  // |r| <= 2^29
-  float x = (float)r * 1.46291807926715968e-9f;  // 2 pi / 2^32
+  float rf = (float)r;  // 2 pi / 2^32 as FP32 hi + lo
+  float x = fmaf(rf, -4.07094027e-17f, rf * 1.46291812e-9f);
   float sn, cs;
   sincos_octant(x, &sn, &cs);
   switch (q & 3) {
@@ -66,22 +73,117 @@ __device__ __forceinline__ float sin_f32(float x) {
 
 // erfc(x), x >= 0 (Numerical Recipes erfcc Chebyshev fit).
 __device__ __forceinline__ float erfc_f32(float x) {
+  // P of erfc_f32 in s = 2.8 t - 1.8 (FP32 values of both constants),
+  // highest power first, with the low parts of the two lowest coefficients
+  // (fit_f32math.py)
+  constexpr float ERFC_P[13] = {
+      5.615803502e-07f,  7.088095799e-07f,  -7.537935744e-06f,  2.896570777e-06f,
+      5.682720439e-05f,  -1.166972652e-04f,  -2.909860341e-04f,  1.508955029e-03f,
+      7.936029579e-04f,  -1.847265288e-02f,  2.271960257e-03f,  4.911400974e-01f,
+      -4.768877327e-01f};
+  constexpr float ERFC_P1_LO = -1.094552576e-08f, ERFC_P0_LO = 8.866951617e-09f;
   float t = 1.0f / fmaf(0.5f, x, 1.0f);
-  float p = fmaf(t, 0.17087277f, -0.82215223f);
-  p = fmaf(t, p, 1.48851587f);
-  p = fmaf(t, p, -1.13520398f);
-  p = fmaf(t, p, 0.27886807f);
-  p = fmaf(t, p, -0.18628806f);
-  p = fmaf(t, p, 0.09678418f);
-  p = fmaf(t, p, 0.37409196f);
-  p = fmaf(t, p, 1.00002368f);
-  p = fmaf(t, p, -1.26551223f);
+  float sv = fmaf(t, 2.79999995f, -1.79999995f);  // FP32-exact map
+  float p = ERFC_P[0];
+#pragma unroll
+  for (int k = 1; k < 13; ++k)
+    p = fmaf(sv, p, ERFC_P[k]);
+  p += fmaf(sv, ERFC_P1_LO, ERFC_P0_LO);
   float x2 = x * x;
   float x2lo = fmaf(x, x, -x2);  // x*x = x2 + x2lo exactly
   return t * expf(-x2) * expf(p - x2lo);
 }
 
-// Compensated (two-sum) accumulation: (hi, lo) += v.
+// ---- float-float (value = hi + lo, |lo| <= ulp(hi) / 2) ----
+struct ff2 {
+  float hi, lo;
+};
+__device__ __forceinline__ ff2 ff_quick(float a, float b) {  // |a| >= |b|
+  float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ ff2 ff_two_sum(float a, float b) {
+  float s = a + b;
+  float bp = s - a;
+  return {s, (a - (s - bp)) + (b - bp)};
+}
+__device__ __forceinline__ ff2 ff_from_i64(long long v) {
+  float hi = __ll2float_rn(v);
+  return {hi, __ll2float_rn(v - (long long)hi)};
+}
+__device__ __forceinline__ ff2 ff_mul(ff2 a, ff2 b) {
+  float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e += fmaf(a.hi, b.lo, a.lo * b.hi);
+  return ff_quick(p, e);
+}
+__device__ __forceinline__ ff2 ff_add(ff2 a, ff2 b) {
+  ff2 s = ff_two_sum(a.hi, b.hi);
+  return ff_quick(s.hi, s.lo + (a.lo + b.lo));
+}
+__device__ __forceinline__ ff2 ff_sqrt(ff2 a) {
+  float y = sqrtf(a.hi);
+  float e = fmaf(-y, y, a.hi) + a.lo;
+  return ff_quick(y, e / (2.0f * y));
+}
+__device__ __forceinline__ ff2 ff_div(ff2 a, ff2 b) {
+  float q1 = a.hi / b.hi;
+  ff2 p = ff_mul({q1, 0.0f}, b);
+  ff2 r = ff_add(a, {-p.hi, -p.lo});
+  return ff_quick(q1, r.hi / b.hi);
+}
+
+// Coulomb bracket of a close pair, erfc(a r')/r' - erfc(a r)/r (Ewald) or
+// 1/r' - 1/r, as hi + lo, from the exact integer turn differences o (old)
+// and n (new) of the pair.  turn2[d] = (L_d 2^-32)^2 as float-float,
+// alpha2 = alpha^2 and alpha3 = alpha^3 (float-float) in FP32.  The squared
+// distances are exact integers scaled by turn2, 1/r' - 1/r =
+// -(r'^2 - r^2) / (r r' (r + r')) is taken in float-float, and the smooth
+// part erf(a r)/r = a g(a^2 r^2), g(u) = erf(sqrt u)/sqrt u, enters through
+// the divided difference of g, so neither part loses digits to cancellation.
+// Valid while a^2 r^2 and a^2 r'^2 are at most 4.
+__device__ __forceinline__ ff2 close_coulomb(const int32_t o[3],
+                                            const int32_t n[3],
+                                            const float turn2_hi[3],
+                                            const float turn2_lo[3],
+                                            bool ewald, float alpha2,
+                                            ff2 alpha3) {
+  ff2 Do = {0.0f, 0.0f}, Dn = {0.0f, 0.0f}, dD = {0.0f, 0.0f};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    long long o2 = (long long)o[d] * o[d], n2 = (long long)n[d] * n[d];
+    ff2 s2 = {turn2_hi[d], turn2_lo[d]};
+    Do = ff_add(Do, ff_mul(ff_from_i64(o2), s2));
+    Dn = ff_add(Dn, ff_mul(ff_from_i64(n2), s2));
+    dD = ff_add(dD, ff_mul(ff_from_i64(n2 - o2), s2));
+  }
+  ff2 ro = ff_sqrt(Do), rn = ff_sqrt(Dn);
+  ff2 den = ff_mul(ff_mul(ro, rn), ff_add(ro, rn));
+  ff2 dinv = ff_div({-dD.hi, -dD.lo}, den);
+  if (!ewald)
+    return dinv;
+  // erf(t)/t in v = t^2 / 2 - 1 over t^2 in [0, 4], highest power first
+  constexpr float ERF_OVER_T[13] = {
+      6.529255359e-08f,  -4.334567336e-07f,  2.470110985e-06f,  -1.390969373e-05f,
+      7.180490502e-05f,  -3.351655905e-04f,  1.405090094e-03f,  -5.234869197e-03f,
+      1.712834463e-02f,  -4.866277799e-02f,  1.194791421e-01f,  -2.611118555e-01f,
+      6.749332547e-01f};
+  constexpr float ERF_OVER_T1_LO = -5.395414282e-09f;
+  // [g(u_n) - g(u_o)] / (v_n - v_o) by synthetic division (one Horner pass)
+  float vo = fmaf(alpha2 * Do.hi, 0.5f, -1.0f);
+  float vn = fmaf(alpha2 * Dn.hi, 0.5f, -1.0f);
+  float p = ERF_OVER_T[0], dd = p;
+#pragma unroll
+  for (int k = 1; k < 12; ++k) {
+    p = fmaf(vn, p, ERF_OVER_T[k]);
+    dd = fmaf(dd, vo, p);
+  }
+  dd += ERF_OVER_T1_LO;  // the power-1 coefficient enters dd once
+  // a [g(u_n) - g(u_o)] = a^3 (r'^2 - r^2) dd / 2
+  float w = 0.5f * dD.hi * dd;
+  return ff_add(dinv, {-alpha3.hi * w, -alpha3.lo * w});
+}
+
 __device__ __forceinline__ void two_sum_add(float &hi, float &lo, float v) {
   float s = hi + v;
   float bp = s - hi;

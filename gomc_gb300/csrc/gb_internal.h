@@ -16,6 +16,9 @@
 namespace gb {
 
 constexpr double QQ_FACT = 167103.208067979;  // lib/NumLib.h:22
+// sqrt(QQ_FACT): the mixed form stores charges scaled by it, so that the
+// product of two scaled charges is q_i q_j QQ_FACT
+constexpr double SQRT_QQ_FACT = 408.7825926675193;
 constexpr int NB27 = 27;
 constexpr int MAX_KINDS = 8;
 constexpr int MAX_MOL_ATOMS = 8;   // rigid molecules handled by the move loop
@@ -56,6 +59,27 @@ struct FF {
   // FP32 copies for the mixed form
   float sigmaSq_f[MAX_KINDS * MAX_KINDS];
   float eps_cn_f[MAX_KINDS * MAX_KINDS];
+  // Rounding a constant to FP32 scales every pair of one kind by the same
+  // factor, a bias that adds up over many moves.  The same holds for the
+  // FP32 length of one fixed-point turn, L 2^-32 rounded to FP32: distances
+  // from it are r_f = r / (1 + eta), eta = (L 2^-32) / fl(L 2^-32) - 1 (the
+  // mean over the axes; exact for a cubic box).  With s = sigmaSq_f / r_f^2
+  // the exact 12-6 energy is
+  //   eps_cn_f * [(s^6 - s^3) + (k6 s^6 - k3 s^3)],
+  //   k6 = (eps_cn / eps_cn_f) (sigmaSq / sigmaSq_f / (1 + eta)^2)^6 - 1,
+  // k3 likewise with the third power.
+  float lj_k6_f[MAX_KINDS * MAX_KINDS];
+  float lj_k3_f[MAX_KINDS * MAX_KINDS];
+  // Coulomb: erfc(alpha r) / r = (1 + coul_qfac) [X + coul_da e^{-t^2}-terms]
+  // with X = erfc(alpha_f r_f) / r_f, t = alpha_f r_f,
+  // coul_da = (alpha (1 + eta) - alpha_f) 2 / sqrt(pi) and
+  // coul_qfac = 1 / (1 + eta) - 1, all to first order.
+  float alpha_f, coul_da_f, coul_qfac_f;
+  // close pairs (both distances below sqrt(close_r2)): exact squared
+  // distances from the turn counts, turn2 = (L_d 2^-32)^2 as hi + lo,
+  // alpha^2 and alpha^3 (hi + lo) for close_coulomb (gb_f32math.cuh)
+  float turn2_hi[3], turn2_lo[3];
+  float alpha2_f, alpha3_hi, alpha3_lo, close_r2_f;
 };
 
 // Plain-pointer view of one box, passed by value to kernels.
@@ -79,7 +103,9 @@ struct DevBox {
   int *cell_atom;    // [ncell * cap]
   double4_32a *cell_pos; // [ncell * cap] x, y, z, q
   int *cell_meta;    // [ncell * cap] (mol << 4) | kind
-  uint4 *cell_fix;   // [ncell * cap] fixed-point turns x, y, z; q as float bits
+  uint4 *cell_fix;   // [ncell * cap] fixed-point turns x, y, z; and
+                     // q * SQRT_QQ_FACT rounded to FP32, as float bits
+  float *cell_qlo;   // [ncell * cap] q * SQRT_QQ_FACT minus that FP32 value
   int *atom_cell, *atom_slot;  // [n_atoms]
   // Ewald
   int K, kmax;

@@ -893,6 +893,7 @@ __global__ void k_mp_commit(MpCommitArgs P) {
     b.cell_pos[i] = n.cell_pos[i];
     b.cell_meta[i] = n.cell_meta[i];
     b.cell_fix[i] = n.cell_fix[i];
+    b.cell_qlo[i] = n.cell_qlo[i];
   }
   for (size_t i = tid; i < (size_t)b.ncell; i += stride)
     b.cell_count[i] = n.cell_count[i];
@@ -916,6 +917,7 @@ static int mc_alloc(Box &b, McState &s, T **p, size_t n) {
   if (e != cudaSuccess)
     return b.CudaCheck(e, "cudaMalloc (Monte Carlo state)");
   s.allocs.push_back(q);
+  s.bytes += std::max<size_t>(n, 1) * sizeof(T);
   *p = (T *)q;
   return OK;
 }
@@ -1002,7 +1004,9 @@ int mc_init(Box &b, const gb_mc_params &p) {
   if (per_sm < 1)
     return b.Fail(ERR_UNSUPPORTED, "chain kernel does not fit on an SM");
   s.grid = b.sm_count;
-  s.move_cap = 1 << 16;
+  if (p.move_buffer < 0)
+    return b.Fail(ERR_ARG, "move_buffer must be >= 0");
+  s.move_cap = p.move_buffer > 0 ? (size_t)p.move_buffer : (size_t)1 << 16;
   int stride = b.dev.kmax + 1;
   if ((rc = mc_alloc(b, s, &s.d_moves, s.move_cap)) ||
       (rc = mc_alloc(b, s, &s.d_prop, s.move_cap * 12)) ||
@@ -1025,22 +1029,31 @@ int mc_init(Box &b, const gb_mc_params &p) {
     int want = p.cluster_size;
     if (want != 0 && want != 2 && want != 4 && want != 8 && want != 16)
       return b.Fail(ERR_ARG, "cluster_size must be 0, 2, 4, 8 or 16");
+    // Largest cluster first (shortest move latency); per cluster size the
+    // k-chunk arrays all in shared memory if they fit, else the cold half of
+    // them in a global buffer.
     int cands[4] = {16, 8, 4, 2};
     s.cluster = 0;
+    bool cold_global = false;
     for (int c : cands) {
       if (want && c != want)
         continue;
-      size_t sm = mixed_smem(b.dev.K, b.dev.kmax, c);
-      if (sm > 220 * 1024)
-        continue;
-      if (max_active_clusters(c, sm) >= 1) {
+      for (int cold_smem = 1; cold_smem >= 0 && !s.cluster; --cold_smem) {
+        size_t sm = mixed_smem(b.dev.K, b.dev.kmax, c, cold_smem != 0);
+        if (sm > MIXED_SMEM_MAX || max_active_clusters(c, sm) < 1)
+          continue;
         s.cluster = c;
         s.mixed_smem = sm;
-        break;
+        cold_global = !cold_smem;
       }
+      if (s.cluster)
+        break;
     }
     if (!s.cluster)
       return b.Fail(ERR_UNSUPPORTED, "no cluster shape fits this box");
+    if (cold_global &&
+        (rc = mc_alloc(b, s, &s.d_cold, mixed_cold_buffer(b.dev.K, s.cluster))))
+      return rc;
     s.flush_every = p.flush_every > 0 ? p.flush_every : 64;
     s.desc_cap = 256;
     if ((rc = mc_alloc(b, s, &s.d_desc, s.desc_cap)))
@@ -1077,6 +1090,7 @@ int mc_init(Box &b, const gb_mc_params &p) {
       (rc = mc_alloc(b, s, &n.cell_pos, NC)) ||
       (rc = mc_alloc(b, s, &n.cell_meta, NC)) ||
       (rc = mc_alloc(b, s, &n.cell_fix, NC)) ||
+      (rc = mc_alloc(b, s, &n.cell_qlo, NC)) ||
       (rc = mc_alloc(b, s, &n.atom_cell, N)) ||
       (rc = mc_alloc(b, s, &n.atom_slot, N)))
     return rc;
@@ -1192,6 +1206,7 @@ static MixedChain fill_mixed(Box &b, McState &s, const MoveRec *moves,
   c.flush_every = s.flush_every;
   c.tr_i = tr_i;
   c.tr_d = tr_d;
+  c.cold = s.d_cold;
   return c;
 }
 
@@ -1473,16 +1488,130 @@ int mc_state(Box &b, double *scales4, int64_t *counts6) {
   return OK;
 }
 
+// Launch one segment of several mixed boxes: box i runs n[i] moves (0: not
+// in this launch) from its own next step.  Boxes are grouped by cluster size;
+// each group is one launch on the stream of its first box, and the groups
+// overlap on the device.  Each n[i] must end at or before the box's next
+// recompute boundary and fit its move buffer.  `leaders` receives the box
+// whose stream carries each launch.
+int mixed_launch(const std::vector<Box *> &boxes,
+                 const std::vector<int64_t> &n, std::vector<Box *> *leaders) {
+  leaders->clear();
+  std::vector<int> sizes;
+  for (size_t i = 0; i < boxes.size(); ++i)
+    if (n[i] > 0 &&
+        std::find(sizes.begin(), sizes.end(), boxes[i]->mc->cluster) == sizes.end())
+      sizes.push_back(boxes[i]->mc->cluster);
+  int rc;
+  for (int csize : sizes) {
+    std::vector<size_t> g;
+    size_t smem = 0;
+    for (size_t i = 0; i < boxes.size(); ++i)
+      if (n[i] > 0 && boxes[i]->mc->cluster == csize) {
+        g.push_back(i);
+        smem = std::max(smem, boxes[i]->mc->mixed_smem);
+      }
+    Box &L = *boxes[g[0]];
+    McState &sl = *L.mc;
+    int nb = (int)g.size();
+    if ((rc = L.Sync()))  // the descriptor staging area is free
+      return rc;
+    if (sl.desc_cap < nb) {
+      sl.desc_cap = std::max(nb, 256);
+      if ((rc = mc_alloc(L, sl, &sl.d_desc, sl.desc_cap)))
+        return rc;
+      if (sl.h_desc)
+        cudaFreeHost(sl.h_desc);
+      sl.h_desc = nullptr;
+      if ((rc = L.CudaCheck(cudaMallocHost(&sl.h_desc,
+                                           sl.desc_cap * sizeof(MixedChain)),
+                            "pinned")))
+        return rc;
+    }
+    sl.desc_next = sl.desc_cap;  // a single-box run re-syncs before reuse
+    int64_t total = 0;
+    for (int k = 0; k < nb; ++k) {
+      Box &b = *boxes[g[k]];
+      McState &s = *b.mc;
+      int64_t m = n[g[k]];
+      if (m > (int64_t)s.move_cap)
+        return b.Fail(ERR_ARG, "segment longer than the move buffer");
+      if ((rc = b.Sync()))  // h_moves is free
+        return rc;
+      for (int64_t t = 0; t < m; ++t)
+        s.stream->Next(&s.h_moves[t]);
+      if ((rc = b.CudaCheck(cudaMemcpyAsync(s.d_moves, s.h_moves,
+                                            m * sizeof(MoveRec),
+                                            cudaMemcpyHostToDevice, L.stream),
+                            "upload moves")))
+        return rc;
+      sl.h_desc[k] = fill_mixed(b, s, s.d_moves, s.next_step, (int)m, nullptr,
+                                nullptr);
+      s.next_step += m;
+      total += m;
+    }
+    if ((rc = L.CudaCheck(cudaMemcpyAsync(sl.d_desc, sl.h_desc,
+                                          nb * sizeof(MixedChain),
+                                          cudaMemcpyHostToDevice, L.stream),
+                          "descriptor upload")))
+      return rc;
+    auto ev = ev_pair();
+    cudaEventRecord(ev.first, L.stream);
+    if ((rc = launch_chain_mixed(L.stream, sl.d_desc, nb, csize, smem)))
+      return L.CudaCheck(cudaGetLastError(), "batched mixed chain kernel");
+    cudaEventRecord(ev.second, L.stream);
+    sl.chain_ev.push_back(ev);
+    sl.chain_ev_moves.push_back((int)total);
+    leaders->push_back(&L);
+  }
+  return OK;
+}
+
+// Wait for the launches of mixed_launch, then run the periodic FP64
+// recompute of every box whose step count reached a multiple of its
+// recompute frequency.
+int mixed_complete(const std::vector<Box *> &boxes,
+                   const std::vector<int64_t> &n,
+                   const std::vector<Box *> &leaders) {
+  int rc;
+  for (Box *L : leaders)
+    if ((rc = L->Sync()))
+      return rc;
+  for (size_t i = 0; i < boxes.size(); ++i) {
+    if (n[i] <= 0)
+      continue;
+    Box &b = *boxes[i];
+    McState &s = *b.mc;
+    int64_t R = s.params.recompute_freq;
+    if (R > 0 && s.next_step % R == 0 && (rc = recompute_fp64(b, s)))
+      return rc;
+    if ((rc = b.CheckError()))
+      return rc;
+  }
+  return OK;
+}
+
+// Moves box i can run before its next recompute boundary (at most cap).
+int64_t mixed_segment_limit(Box &b, int64_t cap) {
+  McState &s = *b.mc;
+  int64_t m = std::min<int64_t>(cap, (int64_t)s.move_cap);
+  int64_t R = s.params.recompute_freq;
+  if (R > 0)
+    m = std::min(m, R - s.next_step % R);
+  return m;
+}
+
 int mc_run_batch(const std::vector<Box *> &boxes, int64_t first,
                  int64_t nsteps) {
-  // FP64 boxes (or a single box) run one after another.
+  // FP64 boxes, boxes with MultiParticle moves or a single box run one after
+  // another through mc_run.
   bool all_mixed = boxes.size() > 1;
   for (Box *b : boxes) {
     if (!b->mc)
       return b->Fail(ERR_STATE, "gb_mc_init has not been called");
     if (b->cfg.precision != GB_MIXED || b->mc->params.frac[2] > 0)
       all_mixed = false;
-    if (b->dev.n_atoms > 0 && b->sm_count != boxes[0]->sm_count)
+    if (b->cfg.device != boxes[0]->cfg.device)
       all_mixed = false;
   }
   if (!all_mixed) {
@@ -1493,85 +1622,28 @@ int mc_run_batch(const std::vector<Box *> &boxes, int64_t first,
     }
     return OK;
   }
-  // Mixed boxes without MultiParticle moves: one launch runs every chain.
-  Box &b0 = *boxes[0];
-  int csize = b0.mc->cluster;
-  size_t smem = 0;
-  for (Box *b : boxes)
-    csize = std::min(csize, b->mc->cluster);
-  for (Box *b : boxes)
-    smem = std::max(smem, mixed_smem(b->dev.K, b->dev.kmax, csize));
-  if (smem > 220 * 1024 || max_active_clusters(csize, smem) < 1)
-    return b0.Fail(ERR_UNSUPPORTED,
-                   "boxes of this batch need different cluster shapes");
   int rc;
   for (Box *b : boxes) {
     if (first < b->mc->next_step)
       return b->Fail(ERR_STATE, "steps must be run in increasing order");
     skip_to(*b->mc, first);
-    if ((rc = b->Sync()))
-      return rc;
   }
-  McState &s0 = *b0.mc;
-  int nb = (int)boxes.size();
-  if (s0.desc_cap < nb) {
-    s0.desc_cap = std::max(nb, 256);
-    if ((rc = mc_alloc(b0, s0, &s0.d_desc, s0.desc_cap)))
-      return rc;
-    if (s0.h_desc)
-      cudaFreeHost(s0.h_desc);
-    if ((rc = b0.CudaCheck(cudaMallocHost(&s0.h_desc,
-                                          s0.desc_cap * sizeof(MixedChain)),
-                           "pinned")))
-      return rc;
-  }
-  int64_t done = 0;
-  while (done < nsteps) {
-    int64_t chunk = std::min<int64_t>(nsteps - done, (int64_t)s0.move_cap);
-    int64_t R = s0.params.recompute_freq;
-    if (R > 0) {
-      int64_t to_boundary = R - ((first + done) % R);
-      chunk = std::min(chunk, to_boundary);
+  std::vector<int64_t> left(boxes.size(), nsteps), n(boxes.size());
+  std::vector<Box *> leaders;
+  for (;;) {
+    bool any = false;
+    for (size_t i = 0; i < boxes.size(); ++i) {
+      n[i] = left[i] > 0 ? mixed_segment_limit(*boxes[i], left[i]) : 0;
+      any = any || n[i] > 0;
     }
-    if ((rc = b0.Sync()))
+    if (!any)
+      break;
+    if ((rc = mixed_launch(boxes, n, &leaders)) ||
+        (rc = mixed_complete(boxes, n, leaders)))
       return rc;
-    for (int k = 0; k < nb; ++k) {
-      Box &b = *boxes[k];
-      McState &s = *b.mc;
-      for (int64_t i = 0; i < chunk; ++i)
-        s.stream->Next(&s.h_moves[i]);
-      s.next_step += chunk;
-      if ((rc = b.CudaCheck(cudaMemcpyAsync(s.d_moves, s.h_moves,
-                                            chunk * sizeof(MoveRec),
-                                            cudaMemcpyHostToDevice, b0.stream),
-                            "upload moves")))
-        return rc;
-      s0.h_desc[k] = fill_mixed(b, s, s.d_moves, first + done, (int)chunk,
-                                nullptr, nullptr);
-    }
-    if ((rc = b0.CudaCheck(cudaMemcpyAsync(s0.d_desc, s0.h_desc,
-                                           nb * sizeof(MixedChain),
-                                           cudaMemcpyHostToDevice, b0.stream),
-                           "descriptor upload")))
-      return rc;
-    auto ev = ev_pair();
-    cudaEventRecord(ev.first, b0.stream);
-    if ((rc = launch_chain_mixed(b0.stream, s0.d_desc, nb, csize, smem)))
-      return b0.CudaCheck(cudaGetLastError(), "batched mixed chain kernel");
-    cudaEventRecord(ev.second, b0.stream);
-    s0.chain_ev.push_back(ev);
-    s0.chain_ev_moves.push_back((int)(chunk * nb));
-    if ((rc = b0.Sync()))
-      return rc;
-    done += chunk;
-    if (R > 0 && (first + done) % R == 0)
-      for (Box *b : boxes)
-        if ((rc = recompute_fp64(*b, *b->mc)))
-          return rc;
+    for (size_t i = 0; i < boxes.size(); ++i)
+      left[i] -= n[i];
   }
-  for (Box *b : boxes)
-    if ((rc = b->CheckError()))
-      return rc;
   return OK;
 }
 

@@ -72,6 +72,7 @@ struct McState {
   // mixed form: cluster size, descriptor ring, drift records
   int cluster = 0;
   size_t mixed_smem = 0;
+  unsigned char *d_cold = nullptr;  // cold per-k arrays when not in smem
   MixedChain *d_desc = nullptr;   // [desc_cap]
   MixedChain *h_desc = nullptr;   // pinned
   int desc_cap = 0, desc_next = 0;
@@ -102,6 +103,7 @@ struct McState {
   double *d_mp = nullptr;    // MultiParticle scalars
   DevBox cells_new{};        // cell grid of the trial state
   std::vector<void *> allocs;
+  size_t bytes = 0;          // device memory of the Monte Carlo state
   // device-time accounting (CUDA events on the box stream)
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> chain_ev, mp_ev;
   std::vector<int> chain_ev_moves;
@@ -124,8 +126,12 @@ struct MixedChain {
   int flush_every;
   int *tr_i;
   double *tr_d;
+  unsigned char *cold;  // cold per-k arrays in global memory (NULL: in smem)
 };
-size_t mixed_smem(int K, int kmax, int csize);
+// Dynamic shared memory of one CTA, with or without the cold arrays.
+size_t mixed_smem(int K, int kmax, int csize, bool cold_smem);
+// Bytes of the global buffer that holds the cold arrays of one chain.
+size_t mixed_cold_buffer(int K, int csize);
 int launch_chain_mixed(cudaStream_t st, const MixedChain *d_chains, int nchains,
                        int csize, size_t smem);
 int max_active_clusters(int csize, size_t smem);
@@ -136,6 +142,21 @@ int mc_run(Box &b, int64_t first_step, int64_t nsteps, int32_t *kind,
 int mc_state(Box &b, double *scales4, int64_t *counts6);
 int mc_run_batch(const std::vector<Box *> &boxes, int64_t first_step,
                  int64_t nsteps);
+
+// Largest dynamic shared memory the mixed chain kernel asks for per CTA.
+constexpr size_t MIXED_SMEM_MAX = 220 * 1024;
+// Batched segments of mixed boxes (gb_mc.cu): mixed_launch uploads the next
+// n[i] moves of box i and launches one kernel per cluster size on the stream
+// of that group's first box (`leaders`); mixed_complete waits for them and
+// runs the periodic FP64 recomputes that fall due.  mixed_segment_limit is
+// the longest segment (at most cap) that ends at or before the box's next
+// recompute boundary.
+int mixed_launch(const std::vector<Box *> &boxes,
+                 const std::vector<int64_t> &n, std::vector<Box *> *leaders);
+int mixed_complete(const std::vector<Box *> &boxes,
+                   const std::vector<int64_t> &n,
+                   const std::vector<Box *> &leaders);
+int64_t mixed_segment_limit(Box &b, int64_t cap);
 void mc_destroy(Box &b);
 
 }  // namespace gb

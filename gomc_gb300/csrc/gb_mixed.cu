@@ -43,7 +43,8 @@ struct MHdr {
   int cell_old[MAXA], cell_new[MAXA];
   uint32_t uo[MAXA][3], un[MAXA][3], P[MAXA][3];
   float hf[MAXA][3];
-  float qf[MAXA];
+  float qf[MAXA], qflo[MAXA];  // charge (structure factors) and remainder
+  float qs[MAXA], qslo[MAXA];  // q * SQRT_QQ_FACT: FP32 value and remainder
   int ka[MAXA];
 };
 
@@ -59,20 +60,30 @@ struct MShared {
   int nacc;              // accepted moves since the last flush
 };
 
-// Byte offsets of the per-CTA k-chunk arrays in dynamic shared memory; every
+// Byte offsets of the per-CTA k-chunk arrays.  The hot arrays, read by every
+// move (FP32 structure factors s32R/I, this move's changes dR/dI, prefactors
+// pf, integer k), always live in dynamic shared memory: 24 B per k-vector.
+// The cold arrays, touched only on accept and fold (FP64 accumulators s64R/I,
+// two-sum window pRh/pRl/pIh/pIl), follow them in shared memory when the
+// chunk fits, else in a per-chain global buffer with the same offsets
+// (32 B per k-vector and CTA).  Every array starts on a 16-byte boundary
+// whatever the chunk length.
 // array starts on a 16-byte boundary whatever the chunk length.
 struct MixedLayout {
-  size_t kcs;  // padded chunk length (multiple of 4)
-  size_t s64, f32, kn, tab;
+  size_t kcs;   // padded chunk length (multiple of 4)
+  size_t cold;  // offset of the cold arrays (in shared memory or the buffer)
+  size_t tab;   // offset of the phase rows in shared memory
 };
-__host__ __device__ __forceinline__ MixedLayout mixed_layout(int kc_max) {
+__host__ __device__ __forceinline__ MixedLayout mixed_layout(int kc_max,
+                                                             bool cold_smem) {
   MixedLayout L;
   L.kcs = ((size_t)kc_max + 3) & ~(size_t)3;
-  L.s64 = 0;
-  L.f32 = L.s64 + 2 * 8 * L.kcs;
-  L.kn = L.f32 + 9 * 4 * L.kcs;
-  L.tab = L.kn + 4 * L.kcs;
+  L.cold = 24 * L.kcs;
+  L.tab = cold_smem ? L.cold + 32 * L.kcs : L.cold;
   return L;
+}
+__host__ __device__ __forceinline__ size_t mixed_cold_bytes(int kc_max) {
+  return 32 * (((size_t)kc_max + 3) & ~(size_t)3);
 }
 
 // Whether cells c1 and c2 are in one another's 27-cell neighbourhood (every
@@ -151,12 +162,18 @@ __device__ void mixed_header(const MixedChain &C, MShared &S, int t,
       h.uo[a][d] = uo;
       h.un[a][d] = un;
       h.P[a][d] = uo + (uint32_t)(D >> 1);
-      h.hf[a][d] = (float)D * 7.31459039633579840e-10f;  // pi / 2^32
+      float Df = (float)D;  // pi / 2^32 as FP32 hi + lo
+      h.hf[a][d] = fmaf(Df, -2.03547013e-17f, Df * 7.31459060e-10f);
     }
     h.cell_old[a] = position_to_cell_fast(b, oldp[a][0], oldp[a][1], oldp[a][2]);
     h.cell_new[a] = position_to_cell_fast(b, w[0], w[1], w[2]);
     double q = b.q[a0 + a];
-    h.qf[a] = fabs(q) < 0.000000001 ? 0.0f : (float)q;
+    bool q0 = fabs(q) < 0.000000001;
+    h.qf[a] = q0 ? 0.0f : (float)q;
+    h.qflo[a] = q0 ? 0.0f : (float)(q - (double)(float)q);
+    double qs = q * SQRT_QQ_FACT;
+    h.qs[a] = q0 ? 0.0f : (float)qs;
+    h.qslo[a] = q0 ? 0.0f : (float)(qs - (double)(float)qs);
     h.ka[a] = b.kind[a0 + a];
   }
   if (threadIdx.x == 64) {
@@ -199,13 +216,16 @@ __global__ void __launch_bounds__(MT_THREADS)
   const int kc_max = (K + csize - 1) / csize;
   const int kbeg = min(K, rank * kc_max);
   const int kc = min(kc_max, K - kbeg);
-  MixedLayout L = mixed_layout(kc_max);
-  double *s64R = (double *)(dyn + L.s64), *s64I = s64R + L.kcs;
-  float *s32R = (float *)(dyn + L.f32), *s32I = s32R + L.kcs;
-  float *pRh = s32I + L.kcs, *pRl = pRh + L.kcs, *pIh = pRl + L.kcs,
-        *pIl = pIh + L.kcs, *dR = pIl + L.kcs, *dI = dR + L.kcs,
-        *pf = dI + L.kcs;
-  char4 *kn = (char4 *)(dyn + L.kn);
+  const bool cold_smem = C.cold == nullptr;
+  MixedLayout L = mixed_layout(kc_max, cold_smem);
+  float *s32R = (float *)dyn, *s32I = s32R + L.kcs, *dR = s32I + L.kcs,
+        *dI = dR + L.kcs, *pf = dI + L.kcs;
+  char4 *kn = (char4 *)(pf + L.kcs);
+  unsigned char *cb = cold_smem ? dyn + L.cold
+                                : C.cold + (size_t)rank * mixed_cold_bytes(kc_max);
+  double *s64R = (double *)cb, *s64I = s64R + L.kcs;
+  float *pRh = (float *)(s64I + L.kcs), *pRl = pRh + L.kcs, *pIh = pRl + L.kcs,
+        *pIl = pIh + L.kcs;
   float2 *tab = (float2 *)(dyn + L.tab);
   const int stride = b.kmax + 1;
 
@@ -263,7 +283,8 @@ __global__ void __launch_bounds__(MT_THREADS)
   const float rc2 = (float)ff.rcutSq;
   const float rcc2 = (float)ff.rcutCoulSq;
   const float rl2 = (float)ff.rcutLowSq;
-  const float alpha = (float)ff.alpha;
+  const float alpha = ff.alpha_f;
+  const float coul_da = ff.coul_da_f;
   const float sx = (float)(b.L[0] * 2.3283064365386963e-10);  // L / 2^32
   const float sy = (float)(b.L[1] * 2.3283064365386963e-10);
   const float sz = (float)(b.L[2] * 2.3283064365386963e-10);
@@ -295,7 +316,7 @@ __global__ void __launch_bounds__(MT_THREADS)
       float ddx = (float)(int32_t)(un[0] - uo[0]) * sx;
       float ddy = (float)(int32_t)(un[1] - uo[1]) * sy;
       float ddz = (float)(int32_t)(un[2] - uo[2]) * sz;
-      float qa = h.qf[a];
+      float qa = h.qs[a], qa_lo = h.qslo[a];
       int ka = h.ka[a];
       for (int j = lane128; j < n2; j += 128) {
         size_t s = (size_t)c2 * b.cap + j;
@@ -349,12 +370,22 @@ __global__ void __launch_bounds__(MT_THREADS)
         }
         int kj = meta_kind(mj);
         int idx = ka + kj * ff.n_kinds;
-        float qq = qa * __uint_as_float(f.w) * (float)QQ_FACT;
+        // q_i q_j QQ_FACT / (1 + eta) = qq + qc up to FP32 rounding of the
+        // remainder qc: the pair's charge product carries no systematic FP32
+        // bias, and qc also takes up the FP32 turn length (FF::coul_qfac_f)
+        float qb = __uint_as_float(f.w);
+        float qq = qa * qb;
         bool coul = ff.electrostatic && qq != 0.f;
+        float qres = 0.f, qc = 0.f;
+        if (coul) {
+          qres = fmaf(qa, qb, -qq) + fmaf(qa, __ldcg(b.cell_qlo + s), qa_lo * qb);
+          qc = fmaf(qq, ff.coul_qfac_f, qres);
+        }
         // Coulomb cutoff: the pair cutoff decision when it is the larger one
         bool cin_o = coul_cut ? r2o <= rcc2 : true;
         bool cin_n = coul_cut ? r2n <= rcc2 : true;
         float sg2 = ff.sigmaSq_f[idx], ecn = ff.eps_cn_f[idx];
+        float k6 = ff.lj_k6_f[idx], k3 = ff.lj_k3_f[idx];
         if (side) {
           if (!in_n)
             continue;
@@ -367,12 +398,23 @@ __global__ void __launch_bounds__(MT_THREADS)
             float ds = -sg2 * dr2 / (r2o * r2n);
             float so3 = so * so * so, sn3 = sn * sn * sn;
             float d3 = ds * fmaf(sn, sn, fmaf(sn, so, so * so));
-            two_sum_add(lj_h, lj_l, ecn * d3 * (sn3 + so3 - 1.0f));
-            if (coul && cin_n && cin_o) {
+            float s33 = sn3 + so3;
+            two_sum_add(lj_h, lj_l,
+                        ecn * d3 * ((s33 - 1.0f) + fmaf(s33, k6, -k3)));
+            if (coul && cin_n && cin_o && r2o < ff.close_r2_f &&
+                r2n < ff.close_r2_f) {
+              // close pair: the bracket in float-float from exact distances
+              const int32_t o3[3] = {ox, oy, oz}, n3[3] = {nx_, ny_, nz_};
+              ff2 X = close_coulomb(o3, n3, ff.turn2_hi, ff.turn2_lo, ff.ewald,
+                                    ff.alpha2_f, {ff.alpha3_hi, ff.alpha3_lo});
+              two_sum_add(re_h, re_l,
+                          fmaf(qq, X.hi, fmaf(qres, X.hi, qq * X.lo)));
+            } else if (coul && cin_n && cin_o) {
               float inv_o = 1.0f / ro, inv_n = 1.0f / rn;
               float sum_r = ro + rn;
               float dinv = -dr2 * inv_o * inv_n / sum_r;  // 1/rn - 1/ro
               float derfc;                                 // erfc(a rn) - erfc(a ro)
+              float dal;  // alpha_f -> alpha correction of the bracket
               if (ff.ewald) {
                 float tlo = alpha * ro, thi = alpha * rn;
                 float dt = alpha * dr2 / sum_r;              // thi - tlo
@@ -381,43 +423,57 @@ __global__ void __launch_bounds__(MT_THREADS)
                   float tm = 0.5f * (tlo + thi), hw = 0.5f * dt;
                   float t1 = fmaf(-0.774596669f, hw, tm),
                         t3 = fmaf(0.774596669f, hw, tm);
-                  float g = 0.888888889f * expf(-tm * tm) +
-                            0.555555556f * (expf(-t1 * t1) + expf(-t3 * t3));
-                  derfc = -1.128379167f * hw * g;  // 2/sqrt(pi) * (dt/2) * sum
+                  float em = expf(-tm * tm);
+                  // 2/sqrt(pi) (dt/2) [8/9 e(tm) + 5/9 (e(t1) + e(t3))], the
+                  // weights times 2/sqrt(pi) as FP32 hi + lo pairs
+                  float e13 = expf(-t1 * t1) + expf(-t3 * t3);
+                  float g = fmaf(1.00300372f, em, 0.626877308f * e13) +
+                            fmaf(-1.23839108e-8f, em, 7.16121695e-9f * e13);
+                  derfc = -hw * g;
+                  // exp(-tn^2) - exp(-to^2) = -2 tm dt exp(-tm^2) + O(dt^3)
+                  dal = 2.0f * coul_da * tm * dt * em;
                 } else {
                   derfc = erfc_f32(thi) - erfc_f32(tlo);
+                  dal = -coul_da * (expf(-thi * thi) - expf(-tlo * tlo));
                 }
                 float en = erfc_f32(thi);
-                two_sum_add(re_h, re_l, qq * fmaf(en, dinv, derfc * inv_o));
+                float X = fmaf(en, dinv, derfc * inv_o) + dal;
+                two_sum_add(re_h, re_l, fmaf(qq, X, qc * X));
               } else {
-                two_sum_add(re_h, re_l, qq * dinv);
+                two_sum_add(re_h, re_l, fmaf(qq, dinv, qc * dinv));
               }
             } else if (coul) {
               if (cin_n) {
                 float rr = sqrtf(r2n);
-                two_sum_add(re_h, re_l, ff.ewald ? qq * erfc_f32(alpha * rr) / rr : qq / rr);
+                float X = ff.ewald ? erfc_f32(alpha * rr) / rr : 1.0f / rr;
+                two_sum_add(re_h, re_l, fmaf(qq, X, qc * X));
               }
               if (cin_o) {
                 float rr = sqrtf(r2o);
-                two_sum_add(re_h, re_l, ff.ewald ? -qq * erfc_f32(alpha * rr) / rr : -qq / rr);
+                float X = ff.ewald ? erfc_f32(alpha * rr) / rr : 1.0f / rr;
+                two_sum_add(re_h, re_l, -fmaf(qq, X, qc * X));
               }
             }
           } else {
-            float rr2 = sg2 / r2n, r6 = rr2 * rr2 * rr2;
-            two_sum_add(lj_h, lj_l, ecn * (r6 * r6 - r6));
+            float rr2 = sg2 / r2n, r6 = rr2 * rr2 * rr2, r12 = r6 * r6;
+            two_sum_add(lj_h, lj_l,
+                        ecn * ((r12 - r6) + fmaf(r12, k6, -r6 * k3)));
             if (coul && cin_n) {
               float rr = sqrtf(r2n);
-              two_sum_add(re_h, re_l, ff.ewald ? qq * erfc_f32(alpha * rr) / rr : qq / rr);
+              float X = ff.ewald ? erfc_f32(alpha * rr) / rr : 1.0f / rr;
+              two_sum_add(re_h, re_l, fmaf(qq, X, qc * X));
             }
           }
         } else {
           if (!in_o || in_n)
             continue;  // counted from the new position's cells
-          float rr2 = sg2 / r2o, r6 = rr2 * rr2 * rr2;
-          two_sum_add(lj_h, lj_l, -ecn * (r6 * r6 - r6));
+          float rr2 = sg2 / r2o, r6 = rr2 * rr2 * rr2, r12 = r6 * r6;
+          two_sum_add(lj_h, lj_l,
+                      -ecn * ((r12 - r6) + fmaf(r12, k6, -r6 * k3)));
           if (coul && cin_o) {
             float rr = sqrtf(r2o);
-            two_sum_add(re_h, re_l, ff.ewald ? -qq * erfc_f32(alpha * rr) / rr : -qq / rr);
+            float X = ff.ewald ? erfc_f32(alpha * rr) / rr : 1.0f / rr;
+            two_sum_add(re_h, re_l, -fmaf(qq, X, qc * X));
           }
         }
       }
@@ -433,7 +489,8 @@ __global__ void __launch_bounds__(MT_THREADS)
         if (q == 0.f)
           continue;
         float arg = fmaf(fx, h.hf[a][0], fmaf(fy, h.hf[a][1], fz * h.hf[a][2]));
-        float w = 2.0f * q * sin_f32(arg);
+        float sa = sin_f32(arg);
+        float w = 2.0f * fmaf(h.qflo[a], sa, q * sa);
         const float2 *rx = tab + (size_t)(3 * a) * stride;
         float2 e = cmulf(cmulf(rx[n.x], tabf(rx + stride, n.y)),
                          tabf(rx + 2 * stride, n.z));
@@ -571,10 +628,14 @@ __global__ void __launch_bounds__(MT_THREADS)
   }
 }
 
-size_t mixed_smem(int K, int kmax, int csize) {
+size_t mixed_smem(int K, int kmax, int csize, bool cold_smem) {
   int kc_max = (K + csize - 1) / csize;
-  MixedLayout L = mixed_layout(kc_max);
+  MixedLayout L = mixed_layout(kc_max, cold_smem);
   return L.tab + sizeof(float2) * (size_t)3 * MAXA * (kmax + 1) + 16;
+}
+
+size_t mixed_cold_buffer(int K, int csize) {
+  return (size_t)csize * mixed_cold_bytes((K + csize - 1) / csize);
 }
 
 int launch_chain_mixed(cudaStream_t st, const MixedChain *d_chains, int nchains,

@@ -28,6 +28,64 @@ def _ip(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_int32))
 
 
+def system_desc(sysm):
+    """gb_system_desc of a System, and the arrays it points into (keep them
+    alive while the descriptor is used)."""
+    keep = [np.ascontiguousarray(sysm.pos, dtype=np.float64),
+            np.ascontiguousarray(sysm.atom_kind, dtype=np.int32),
+            np.ascontiguousarray(sysm.atom_charge, dtype=np.float64),
+            np.ascontiguousarray(sysm.mol_start, dtype=np.int32),
+            np.array([k.epsilon for k in sysm.kinds], np.float64),
+            np.array([k.sigma for k in sysm.kinds], np.float64),
+            np.array([k.n for k in sysm.kinds], np.float64)]
+    pos, kind, q, ms, eps, sig, nex = keep
+    d = _lib.SystemDesc()
+    d.n_atoms, d.n_mol, d.n_kinds = sysm.n_atoms, sysm.n_mol, len(sysm.kinds)
+    d.pos, d.atom_kind, d.atom_charge, d.mol_start = _dp(pos), _ip(kind), \
+        _dp(q), _ip(ms)
+    d.kind_epsilon, d.kind_sigma, d.kind_n = _dp(eps), _dp(sig), _dp(nex)
+    for i in range(3):
+        d.box[i] = float(sysm.box[i])
+    return d, keep
+
+
+def config_struct(cfg, precision: int, device: int):
+    """gb_config of a SimConfig (the in.conf keys of the energy path)."""
+    c = _lib.Config()
+    c.temperature = cfg.temperature
+    c.rcut = cfg.rcut
+    c.rcut_low = cfg.rcut_low
+    c.rcut_coulomb = cfg.rcut_coulomb_value
+    c.tolerance = cfg.tolerance
+    c.ewald = int(cfg.ewald)
+    c.electrostatic = int(cfg.electrostatic)
+    c.precision = precision
+    c.device = device
+    return c
+
+
+def mc_params(seed: int, move_frac: Sequence[float], adj_steps: int,
+              scales: Optional[Sequence[float]] = None,
+              recompute_freq: int = 0, cluster_size: int = 0,
+              flush_every: int = 0, move_buffer: int = 0):
+    """gb_mc_params (Random_Seed, DisFreq / RotFreq / MultiParticleFreq,
+    AdjSteps and the mixed form's settings)."""
+    p = _lib.McParams()
+    p.seed = int(seed) & 0xFFFFFFFF
+    for i in range(3):
+        p.frac[i] = float(move_frac[i])
+    p.adj_steps = int(adj_steps)
+    p.use_scales = 0 if scales is None else 1
+    if scales is not None:
+        for i in range(4):
+            p.scales[i] = float(scales[i])
+    p.recompute_freq = int(recompute_freq)
+    p.cluster_size = int(cluster_size)
+    p.flush_every = int(flush_every)
+    p.move_buffer = int(move_buffer)
+    return p
+
+
 class Box:
     """One orthogonal periodic box resident on one GPU."""
 
@@ -39,34 +97,11 @@ class Box:
         self.n_atoms = sysm.n_atoms
         self.n_mol = sysm.n_mol
         self.mol_start = np.ascontiguousarray(sysm.mol_start, dtype=np.int32)
-        self._keep = [np.ascontiguousarray(sysm.pos, dtype=np.float64),
-                      np.ascontiguousarray(sysm.atom_kind, dtype=np.int32),
-                      np.ascontiguousarray(sysm.atom_charge, dtype=np.float64),
-                      self.mol_start,
-                      np.array([k.epsilon for k in sysm.kinds], np.float64),
-                      np.array([k.sigma for k in sysm.kinds], np.float64),
-                      np.array([k.n for k in sysm.kinds], np.float64)]
-        pos, kind, q, ms, eps, sig, nex = self._keep
-        d = _lib.SystemDesc()
-        d.n_atoms, d.n_mol, d.n_kinds = self.n_atoms, self.n_mol, len(sysm.kinds)
-        d.pos, d.atom_kind, d.atom_charge, d.mol_start = _dp(pos), _ip(kind), \
-            _dp(q), _ip(ms)
-        d.kind_epsilon, d.kind_sigma, d.kind_n = _dp(eps), _dp(sig), _dp(nex)
-        for i in range(3):
-            d.box[i] = float(sysm.box[i])
-        c = _lib.Config()
-        c.temperature = cfg.temperature
-        c.rcut = cfg.rcut
-        c.rcut_low = cfg.rcut_low
-        c.rcut_coulomb = cfg.rcut_coulomb_value
-        c.tolerance = cfg.tolerance
-        c.ewald = int(cfg.ewald)
-        c.electrostatic = int(cfg.electrostatic)
+        d, self._keep = system_desc(sysm)
         if precision is None:
             precision = GB_MIXED if getattr(cfg, "precision", "fp64") == "mixed" \
                 else GB_FP64
-        c.precision = precision
-        c.device = device
+        c = config_struct(cfg, precision, device)
         h = C.c_void_p()
         rc = L.gb_box_create(C.byref(d), C.byref(c), C.byref(h))
         if rc != 0:
@@ -252,19 +287,9 @@ class Box:
     def mc_init(self, seed: int, move_frac: Sequence[float], adj_steps: int,
                 scales: Optional[Sequence[float]] = None,
                 recompute_freq: int = 0, cluster_size: int = 0,
-                flush_every: int = 0) -> None:
-        p = _lib.McParams()
-        p.seed = int(seed) & 0xFFFFFFFF
-        for i in range(3):
-            p.frac[i] = float(move_frac[i])
-        p.adj_steps = int(adj_steps)
-        p.use_scales = 0 if scales is None else 1
-        if scales is not None:
-            for i in range(4):
-                p.scales[i] = float(scales[i])
-        p.recompute_freq = int(recompute_freq)
-        p.cluster_size = int(cluster_size)
-        p.flush_every = int(flush_every)
+                flush_every: int = 0, move_buffer: int = 0) -> None:
+        p = mc_params(seed, move_frac, adj_steps, scales, recompute_freq,
+                      cluster_size, flush_every, move_buffer)
         self._chk(lib().gb_mc_init(self.h, C.byref(p)))
 
     def mc_drift(self):
@@ -296,6 +321,14 @@ class Box:
                                      C.byref(mn)))
         return dict(chain_ms=cm.value, chain_launches=cl.value,
                     chain_moves=cn.value, mp_ms=mm.value, mp_moves=mn.value)
+
+    def mc_layout(self) -> dict:
+        c, n = C.c_int32(), C.c_int32()
+        sm = C.c_int64()
+        self._chk(lib().gb_mc_layout(self.h, C.byref(c), C.byref(n),
+                                     C.byref(sm)))
+        return dict(ctas_per_chain=c.value, max_concurrent=n.value,
+                    smem_bytes=sm.value)
 
     def stream_ptr(self) -> int:
         p = C.c_void_p()

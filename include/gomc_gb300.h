@@ -157,6 +157,7 @@ typedef struct gb_mc_params {
   int32_t recompute_freq; /* GB300RecomputeFreq (mixed form), 0 = never */
   int32_t cluster_size;   /* mixed form: CTAs per chain (0 = autotuned) */
   int32_t flush_every;    /* mixed form: accepted moves per FP64 fold (0 = 64) */
+  int32_t move_buffer;    /* moves drawn and uploaded per chunk (0 = 65536) */
 } gb_mc_params;
 
 int gb_mc_init(gb_box *box, const gb_mc_params *params);
@@ -181,6 +182,13 @@ int gb_mc_timing(gb_box *box, int32_t reset, double *chain_ms,
  * (the reference's check is Simulation::RecalculateAndCheck,
  * src/Simulation.cpp:170-223, at 1e-3). */
 int gb_mc_drift(gb_box *box, double *max4, double *last4, int64_t *recomputes);
+/* Launch geometry gb_mc_init chose for this box's chain kernel: CTAs that
+ * run one chain (the thread-block cluster size of the mixed form, the
+ * cooperative grid of the FP64 form), how many such chains the GPU holds at
+ * once, and the dynamic shared memory per CTA (mixed form).  No reference
+ * counterpart. */
+int gb_mc_layout(gb_box *box, int32_t *ctas_per_chain, int32_t *max_concurrent,
+                 int64_t *smem_bytes);
 /* The CUDA stream (cudaStream_t) every call on this machine is ordered on. */
 int gb_box_stream(gb_box *box, void **stream);
 
@@ -188,6 +196,70 @@ int gb_box_stream(gb_box *box, void **stream);
  * for all single-molecule segments).  Each box must have gb_mc_init. */
 int gb_mc_run_batch(gb_box **boxes, int32_t nboxes, int64_t first_step,
                     int64_t nsteps);
+
+/* ---- Continuous-batching job server ----
+ * No counterpart in the reference (it runs one simulation per process,
+ * src/Simulation.cpp:116-168).  A server runs many independent
+ * mixed-precision NVT jobs (translate / rotate moves) on one GPU.  Each
+ * round launches the next segment of every resident job (at most `quantum`
+ * moves, one launch per cluster size, launches overlapping on the device),
+ * admits queued jobs first come first served while their estimated device
+ * memory fits `mem_budget` and their chains fit the GPU's free CTA slots,
+ * and retires finished jobs (their final coordinates and running energies
+ * are kept on the host).  A job's results do not depend on which other jobs
+ * share its rounds.  Rounds run either on the caller's thread
+ * (gb_server_step) or on a worker thread (gb_server_start .. gb_server_drain);
+ * gb_server_submit may be called from any thread at any time. */
+typedef struct gb_server gb_server;
+enum gb_job_status {
+  GB_JOB_QUEUED = 0,
+  GB_JOB_RUNNING = 1,
+  GB_JOB_DONE = 2,
+  GB_JOB_FAILED = 3
+};
+typedef struct gb_server_config {
+  int32_t device;
+  int32_t quantum;       /* moves per job per round (0 = 1000) */
+  int64_t mem_budget;    /* device bytes for job state (0 = 90% of free) */
+  int32_t max_resident;  /* at most this many resident jobs (0 = no cap) */
+} gb_server_config;
+int gb_server_create(const gb_server_config *cfg, gb_server **out);
+/* Stops the worker after its current round; drops queued and resident jobs. */
+void gb_server_destroy(gb_server *srv);
+/* Queue a job of `nsteps` moves; the inputs are copied.  cfg->precision must
+ * be GB_MIXED, mc->frac[2] (MultiParticle) 0; mc->cluster_size 0 lets the
+ * server pick the cluster from the job's k-vector count.  `sweep_moves` (0 =
+ * molecules of the job) defines a sweep for the latency statistics. */
+int gb_server_submit(gb_server *srv, const gb_system_desc *sys,
+                     const gb_config *cfg, const gb_mc_params *mc,
+                     int64_t nsteps, int64_t sweep_moves, int64_t *job_id);
+/* The device bytes the server would reserve for such a job at admission
+ * (its memory estimate) and the CTAs per chain it would give it. */
+int gb_server_estimate(gb_server *srv, const gb_system_desc *sys,
+                       const gb_config *cfg, const gb_mc_params *mc,
+                       int64_t *bytes, int32_t *ctas_per_chain);
+/* One round on the calling thread (GB_ERR_STATE while a worker runs);
+ * *pending = jobs queued or resident afterwards. */
+int gb_server_step(gb_server *srv, int32_t *pending);
+/* Run rounds on a worker thread until gb_server_drain. */
+int gb_server_start(gb_server *srv);
+/* Wait until every submitted job has finished (or failed), then stop the
+ * worker.  timeout_s <= 0 waits without limit; GB_ERR_TIMEOUT otherwise. */
+int gb_server_drain(gb_server *srv, double timeout_s);
+/* status (gb_job_status), moves done, and times (s since server creation)
+ * of submission, admission and completion */
+int gb_server_job(gb_server *srv, int64_t job, int32_t *status,
+                  int64_t *steps_done, double *times3);
+/* Final coordinates [n_atoms * 3], molecule centres [n_mol * 3] and running
+ * energies (inter, real, recip, self, correction) of a finished job. */
+int gb_server_result(gb_server *srv, int64_t job, double *xyz, double *com,
+                     double *energy5);
+/* out10: jobs done, moves run, wall seconds from the first admission to the
+ * last completion, moves/s over that span, per-sweep latency p50 and p99
+ * (ms), job latency (submission to completion) p50 and p99 (s), rounds, mean
+ * resident jobs per round. */
+int gb_server_stats(gb_server *srv, double *out10);
+const char *gb_server_error(const gb_server *srv);
 
 /* ---- Reciprocal energy without device allocation ----
  * No counterpart in the reference.  It is the reduction behind BoxReciprocal
