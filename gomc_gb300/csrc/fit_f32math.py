@@ -7,8 +7,8 @@ erfc_f32: erfc(x) = t exp(-x^2 + P(s)), t = 1 / (1 + x/2) -- the
   least-squares fit of log(erfcx(x) / t) in s = a t + b over x in [0, 5],
   a = fl32(2.8), b = fl32(-1.8) (t0 = 1 / (1 + 5/2) maps to s = -1),
   written in the monomial basis of s.
-erf_over_t: g(u) = erf(sqrt(u)) / sqrt(u), a degree-12 Chebyshev fit over
-  u in [0, 4] in v = u / 2 - 1, monomial basis of v.  It feeds the divided
+erf_over_t: g(u) = erf(sqrt(u)) / sqrt(u), a degree-16 Chebyshev fit over
+  u in [0, 8] in v = u / 4 - 1, monomial basis of v.  It feeds the divided
   difference (g(u_n) - g(u_o)) / (u_n - u_o) of close pairs.
 Both fits are far below FP32 resolution (printed); the two lowest
 coefficients of each are kept as FP32 hi + lo pairs, so what remains is FP32
@@ -42,12 +42,12 @@ def fit_erfc(xmax=5.0):
     return (a, b), cheb.cheb2poly(c), err
 
 
-def fit_erf_over_t(umax=4.0):
+def fit_erf_over_t(umax=8.0, deg=16):
     v = _nodes()
     u = (v + 1.0) * umax / 2.0
     t = np.sqrt(u)
     g = erf(t) / t
-    c = cheb.chebfit(v, g, DEG)
+    c = cheb.chebfit(v, g, deg)
     err = np.abs(cheb.chebval(v, c) - g).max()
     return cheb.cheb2poly(c), err
 

@@ -47,6 +47,9 @@ void build_ff(const HostSystem &s, const BoxConfig &c, FF *ff) {
                       : 1.0;
       double re = ff->eps_cn_f[idx] != 0.0f
                       ? ff->eps_cn[idx] / (double)ff->eps_cn_f[idx] : 1.0;
+      ff->sigmaSq_lo_f[idx] =
+          (float)(ff->sigmaSq[idx] - (double)ff->sigmaSq_f[idx]);
+      ff->eps_cn_lo_f[idx] = (float)(ff->eps_cn[idx] - (double)ff->eps_cn_f[idx]);
       ff->lj_k6_f[idx] = (float)(re * std::pow(rs, 6) - 1.0);
       ff->lj_k3_f[idx] = (float)(re * std::pow(rs, 3) - 1.0);
     }
@@ -60,8 +63,10 @@ void build_ff(const HostSystem &s, const BoxConfig &c, FF *ff) {
     ff->alpha = std::sqrt(-std::log(c.tolerance)) / c.rcut_coulomb;
     ff->alphaSq = ff->alpha * ff->alpha;
     ff->alpha_f = (float)ff->alpha;
+    ff->alpha_lo_f = (float)(ff->alpha - (double)ff->alpha_f);
     ff->coul_da_f =
         (float)((ff->alpha * (1.0 + eta) - (double)ff->alpha_f) * M_2_SQRTPI);
+    ff->far_r2_f = (float)(4.0 / ff->alphaSq);
     ff->recip_rcut = -2.0 * std::log(c.tolerance) / c.rcut_coulomb;
     ff->recip_rcutSq = ff->recip_rcut * ff->recip_rcut;
   }
@@ -76,8 +81,11 @@ void build_ff(const HostSystem &s, const BoxConfig &c, FF *ff) {
   ff->alpha2_f = (float)ff->alphaSq;
   ff->alpha3_hi = (float)a3;
   ff->alpha3_lo = (float)(a3 - (double)ff->alpha3_hi);
-  // close-pair path: r < 4 A, and alpha r <= 2 (the range of its erf fit)
-  ff->close_r2_f = (float)std::min(16.0, c.ewald ? 0.99 * 4.0 / ff->alphaSq : 16.0);
+  // the split 1/r - erf(a r)/r while alpha r < 1.3: beyond it erf(a r)/r
+  // nearly equals 1/r, their difference (erfc) loses the digits the split
+  // gains, and the erfc form on exact distances is the more accurate one;
+  // r < 4 A without Ewald
+  ff->close_r2_f = (float)(c.ewald ? 1.3 * 1.3 / ff->alphaSq : 16.0);
   ff->beta = 1 / c.temperature;
 }
 

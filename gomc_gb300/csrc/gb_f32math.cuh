@@ -11,7 +11,7 @@
 //    this project's own degree-12 Chebyshev fit (fit_f32math.py; fit error
 //    below 1e-10 over [0, 5]); x^2 is split into an exact hi + lo pair so
 //    that exp sees the argument to full precision.
-//  * erf(t)/t as a degree-12 polynomial in u = t^2 (fit_f32math.py), used
+//  * erf(t)/t as a degree-16 polynomial in u = t^2 (fit_f32math.py), used
 //    through its divided difference for close pairs.
 //  * float-float arithmetic (hi + lo pairs, Dekker 1971; Knuth TAOCP 2,
 //    sec. 4.2.2) for the 1/r difference of close pairs from exact integer
@@ -133,54 +133,103 @@ __device__ __forceinline__ ff2 ff_div(ff2 a, ff2 b) {
   return ff_quick(q1, r.hi / b.hi);
 }
 
-// Coulomb bracket of a close pair, erfc(a r')/r' - erfc(a r)/r (Ewald) or
-// 1/r' - 1/r, as hi + lo, from the exact integer turn differences o (old)
-// and n (new) of the pair.  turn2[d] = (L_d 2^-32)^2 as float-float,
-// alpha2 = alpha^2 and alpha3 = alpha^3 (float-float) in FP32.  The squared
-// distances are exact integers scaled by turn2, 1/r' - 1/r =
-// -(r'^2 - r^2) / (r r' (r + r')) is taken in float-float, and the smooth
-// part erf(a r)/r = a g(a^2 r^2), g(u) = erf(sqrt u)/sqrt u, enters through
-// the divided difference of g, so neither part loses digits to cancellation.
-// Valid while a^2 r^2 and a^2 r'^2 are at most 4.
-__device__ __forceinline__ ff2 close_coulomb(const int32_t o[3],
-                                            const int32_t n[3],
-                                            const float turn2_hi[3],
-                                            const float turn2_lo[3],
-                                            bool ewald, float alpha2,
-                                            ff2 alpha3) {
-  ff2 Do = {0.0f, 0.0f}, Dn = {0.0f, 0.0f}, dD = {0.0f, 0.0f};
+// Exact squared distances of a close pair in float-float: Do and Dn from the
+// integer turn differences o (old) and n (new), dD = Dn - Do from the exact
+// integer differences per axis; turn2[d] = (L_d 2^-32)^2 as hi + lo.
+struct ClosePair {
+  ff2 Do, Dn, dD;
+};
+__device__ __forceinline__ ClosePair close_pair(const int32_t o[3],
+                                                const int32_t n[3],
+                                                const float turn2_hi[3],
+                                                const float turn2_lo[3]) {
+  ClosePair c = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     long long o2 = (long long)o[d] * o[d], n2 = (long long)n[d] * n[d];
     ff2 s2 = {turn2_hi[d], turn2_lo[d]};
-    Do = ff_add(Do, ff_mul(ff_from_i64(o2), s2));
-    Dn = ff_add(Dn, ff_mul(ff_from_i64(n2), s2));
-    dD = ff_add(dD, ff_mul(ff_from_i64(n2 - o2), s2));
+    c.Do = ff_add(c.Do, ff_mul(ff_from_i64(o2), s2));
+    c.Dn = ff_add(c.Dn, ff_mul(ff_from_i64(n2), s2));
+    c.dD = ff_add(c.dD, ff_mul(ff_from_i64(n2 - o2), s2));
   }
+  return c;
+}
+
+// 12-6 energy change eps_cn [(s'^6 - s'^3) - (s^6 - s^3)], s = sigma^2 / r^2,
+// of a close pair in float-float (sigma^2 and eps_cn as hi + lo).
+__device__ __forceinline__ ff2 close_lj(const ClosePair &c, ff2 sg2, ff2 ecn) {
+  ff2 so = ff_div(sg2, c.Do), sn = ff_div(sg2, c.Dn);
+  ff2 so3 = ff_mul(ff_mul(so, so), so), sn3 = ff_mul(ff_mul(sn, sn), sn);
+  ff2 uo = ff_add(ff_mul(so3, so3), {-so3.hi, -so3.lo});
+  ff2 un = ff_add(ff_mul(sn3, sn3), {-sn3.hi, -sn3.lo});
+  return ff_mul(ecn, ff_add(un, {-uo.hi, -uo.lo}));
+}
+
+// Ewald bracket erfc(a r')/r' - erfc(a r)/r of a pair beyond the close range
+// from the exact squared distances of close_pair (alpha as hi + lo):
+//   erfc(t') (1/r' - 1/r) + (erfc(t') - erfc(t)) / r,
+// with 1/r' - 1/r in float-float, t = a r and t' - t = a (r'^2 - r^2)/(r + r')
+// accurate to FP32 relative to themselves, erfc(t') corrected for the low
+// part of t', and erfc(t') - erfc(t) as 3-point Gauss-Legendre quadrature of
+// (2/sqrt pi) exp(-s^2) over [t, t'] (the difference of two erfc values when
+// the step is large).  The weights times 2/sqrt(pi) are FP32 hi + lo pairs.
+__device__ __forceinline__ float far_coulomb(const ClosePair &c, ff2 alpha) {
+  ff2 ro = ff_sqrt(c.Do), rn = ff_sqrt(c.Dn), sr = ff_add(ro, rn);
+  ff2 dinv = ff_div({-c.dD.hi, -c.dD.lo}, ff_mul(ff_mul(ro, rn), sr));
+  ff2 to = ff_mul(alpha, ro), tn = ff_mul(alpha, rn);
+  float dt = ff_div(ff_mul(alpha, c.dD), sr).hi;  // t' - t
+  float derfc;
+  if (fabsf(dt) < 0.25f) {
+    float hw = 0.5f * dt, tm = to.hi + (to.lo + hw);
+    float t1 = fmaf(-0.774596669f, hw, tm), t3 = fmaf(0.774596669f, hw, tm);
+    float em = expf(-tm * tm), e13 = expf(-t1 * t1) + expf(-t3 * t3);
+    float g = fmaf(1.00300372f, em, 0.626877308f * e13) +
+              fmaf(-1.23839108e-8f, em, 7.16121695e-9f * e13);
+    derfc = -hw * g;
+  } else {
+    derfc = (erfc_f32(tn.hi) - erfc_f32(to.hi)) -
+            1.12837917f * (expf(-tn.hi * tn.hi) * tn.lo -
+                           expf(-to.hi * to.hi) * to.lo);
+  }
+  float en = fmaf(-1.12837917f * expf(-tn.hi * tn.hi), tn.lo, erfc_f32(tn.hi));
+  return fmaf(en, dinv.hi, fmaf(en, dinv.lo, derfc / ro.hi));
+}
+
+// Coulomb bracket of a close pair, erfc(a r')/r' - erfc(a r)/r (Ewald) or
+// 1/r' - 1/r, as hi + lo, from the exact squared distances of close_pair;
+// alpha2 = alpha^2 in FP32 and alpha3 = alpha^3 as hi + lo.  1/r' - 1/r =
+// -(r'^2 - r^2) / (r r' (r + r')) is taken in float-float, and the smooth
+// part erf(a r)/r = a g(a^2 r^2), g(u) = erf(sqrt u)/sqrt u, enters through
+// the divided difference of g, so neither part loses digits to cancellation.
+// Valid while a^2 r^2 and a^2 r'^2 are at most 8.
+__device__ __forceinline__ ff2 close_coulomb(const ClosePair &c, bool ewald,
+                                            float alpha2, ff2 alpha3) {
+  const ff2 &Do = c.Do, &Dn = c.Dn, &dD = c.dD;
   ff2 ro = ff_sqrt(Do), rn = ff_sqrt(Dn);
   ff2 den = ff_mul(ff_mul(ro, rn), ff_add(ro, rn));
   ff2 dinv = ff_div({-dD.hi, -dD.lo}, den);
   if (!ewald)
     return dinv;
-  // erf(t)/t in v = t^2 / 2 - 1 over t^2 in [0, 4], highest power first
-  constexpr float ERF_OVER_T[13] = {
-      6.529255359e-08f,  -4.334567336e-07f,  2.470110985e-06f,  -1.390969373e-05f,
-      7.180490502e-05f,  -3.351655905e-04f,  1.405090094e-03f,  -5.234869197e-03f,
-      1.712834463e-02f,  -4.866277799e-02f,  1.194791421e-01f,  -2.611118555e-01f,
-      6.749332547e-01f};
-  constexpr float ERF_OVER_T1_LO = -5.395414282e-09f;
+  // erf(t)/t in v = t^2 / 4 - 1 over t^2 in [0, 8], highest power first
+  constexpr float ERF_OVER_T[17] = {
+      2.032793418e-07f,  -8.897155794e-07f,  2.865503120e-06f,  -1.098633129e-05f,
+      4.077676203e-05f,  -1.371821127e-04f,  4.277413827e-04f,  -1.235923497e-03f,
+      3.284808714e-03f,  -7.982767187e-03f,  1.764078625e-02f,  -3.527706116e-02f,
+      6.369094551e-02f,  -1.042822003e-01f,  1.582058221e-01f,  -2.384970784e-01f,
+      4.976611435e-01f};
+  constexpr float ERF_OVER_T1_LO = 4.852327290e-09f;
   // [g(u_n) - g(u_o)] / (v_n - v_o) by synthetic division (one Horner pass)
-  float vo = fmaf(alpha2 * Do.hi, 0.5f, -1.0f);
-  float vn = fmaf(alpha2 * Dn.hi, 0.5f, -1.0f);
+  float vo = fmaf(alpha2 * Do.hi, 0.25f, -1.0f);
+  float vn = fmaf(alpha2 * Dn.hi, 0.25f, -1.0f);
   float p = ERF_OVER_T[0], dd = p;
 #pragma unroll
-  for (int k = 1; k < 12; ++k) {
+  for (int k = 1; k < 16; ++k) {
     p = fmaf(vn, p, ERF_OVER_T[k]);
     dd = fmaf(dd, vo, p);
   }
   dd += ERF_OVER_T1_LO;  // the power-1 coefficient enters dd once
-  // a [g(u_n) - g(u_o)] = a^3 (r'^2 - r^2) dd / 2
-  float w = 0.5f * dD.hi * dd;
+  // a [g(u_n) - g(u_o)] = a^3 (r'^2 - r^2) dd / 4
+  float w = 0.25f * dD.hi * dd;
   return ff_add(dinv, {-alpha3.hi * w, -alpha3.lo * w});
 }
 

@@ -70,15 +70,22 @@ struct FF {
   // k3 likewise with the third power.
   float lj_k6_f[MAX_KINDS * MAX_KINDS];
   float lj_k3_f[MAX_KINDS * MAX_KINDS];
-  // Coulomb: erfc(alpha r) / r = (1 + coul_qfac) [X + coul_da e^{-t^2}-terms]
-  // with X = erfc(alpha_f r_f) / r_f, t = alpha_f r_f,
-  // coul_da = (alpha (1 + eta) - alpha_f) 2 / sqrt(pi) and
-  // coul_qfac = 1 / (1 + eta) - 1, all to first order.
-  float alpha_f, coul_da_f, coul_qfac_f;
-  // close pairs (both distances below sqrt(close_r2)): exact squared
+  // Coulomb of a single position (and FP32 pair brackets): erfc(alpha r)/r =
+  // (1 + coul_qfac) erfc(alpha_f r_f) / r_f to first order in eta, with
+  // coul_qfac = 1 / (1 + eta) - 1 (alpha_lo_f = alpha - alpha_f is below
+  // what those near-cutoff terms can show).  Pair differences use exact
+  // distances and alpha as alpha_f + alpha_lo_f.
+  float alpha_f, alpha_lo_f, coul_qfac_f;
+  // pairs with both alpha r >= 2 (r^2 >= far_r2) take the FP32 bracket on
+  // FP32 distances, with first-order corrections for the turn length (eta)
+  // and alpha_f: coul_da = (alpha (1 + eta) - alpha_f) 2 / sqrt(pi)
+  float far_r2_f, coul_da_f;
+  // close pairs (both distances below sqrt(close_r2), alpha r < 1.3): exact squared
   // distances from the turn counts, turn2 = (L_d 2^-32)^2 as hi + lo,
   // alpha^2 and alpha^3 (hi + lo) for close_coulomb (gb_f32math.cuh)
   float turn2_hi[3], turn2_lo[3];
+  float sigmaSq_lo_f[MAX_KINDS * MAX_KINDS];  // sigmaSq - sigmaSq_f
+  float eps_cn_lo_f[MAX_KINDS * MAX_KINDS];   // eps_cn - eps_cn_f
   float alpha2_f, alpha3_hi, alpha3_lo, close_r2_f;
 };
 

@@ -100,6 +100,38 @@ __device__ __forceinline__ bool cells_adjacent(const DevBox &b, int c1, int c2) 
   return ok;
 }
 
+// Ewald bracket erfc(a r')/r' - erfc(a r)/r of a far pair (alpha r >= 2 at
+// both positions) from the FP32 distances: the FP32 erfc form with the
+// first-order corrections for the FP32 turn length and alpha_f (coul_da;
+// the charge factor carries the 1 / (1 + eta) part).  Cheaper than
+// far_coulomb; at these distances its amplified argument rounding is below
+// the error of the near-cutoff terms.
+__device__ __forceinline__ float fp32_bracket(float r2o, float r2n, float dr2,
+                                              float alpha, float coul_da) {
+  float ro = sqrtf(r2o), rn = sqrtf(r2n);
+  float inv_o = 1.0f / ro, inv_n = 1.0f / rn, sum_r = ro + rn;
+  float dinv = -dr2 * inv_o * inv_n / sum_r;  // 1/rn - 1/ro
+  float tlo = alpha * ro, thi = alpha * rn;
+  float dt = alpha * dr2 / sum_r;             // thi - tlo
+  float derfc, dal;
+  if (fabsf(dt) < 0.25f) {
+    // 3-point Gauss-Legendre of (2/sqrt pi) exp(-t^2) over [tlo, thi], the
+    // weights times 2/sqrt(pi) as FP32 hi + lo pairs
+    float tm = 0.5f * (tlo + thi), hw = 0.5f * dt;
+    float t1 = fmaf(-0.774596669f, hw, tm), t3 = fmaf(0.774596669f, hw, tm);
+    float em = expf(-tm * tm), e13 = expf(-t1 * t1) + expf(-t3 * t3);
+    float g = fmaf(1.00300372f, em, 0.626877308f * e13) +
+              fmaf(-1.23839108e-8f, em, 7.16121695e-9f * e13);
+    derfc = -hw * g;
+    // exp(-tn^2) - exp(-to^2) = -2 tm dt exp(-tm^2) + O(dt^3)
+    dal = 2.0f * coul_da * tm * dt * em;
+  } else {
+    derfc = erfc_f32(thi) - erfc_f32(tlo);
+    dal = -coul_da * (expf(-thi * thi) - expf(-tlo * tlo));
+  }
+  return fmaf(erfc_f32(thi), dinv, derfc * inv_o) + dal;
+}
+
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -284,7 +316,6 @@ __global__ void __launch_bounds__(MT_THREADS)
   const float rcc2 = (float)ff.rcutCoulSq;
   const float rl2 = (float)ff.rcutLowSq;
   const float alpha = ff.alpha_f;
-  const float coul_da = ff.coul_da_f;
   const float sx = (float)(b.L[0] * 2.3283064365386963e-10);  // L / 2^32
   const float sy = (float)(b.L[1] * 2.3283064365386963e-10);
   const float sz = (float)(b.L[2] * 2.3283064365386963e-10);
@@ -390,10 +421,29 @@ __global__ void __launch_bounds__(MT_THREADS)
           if (!in_n)
             continue;
           if (in_o) {
+            const int32_t o3[3] = {ox, oy, oz}, n3[3] = {nx_, ny_, nz_};
+            if (r2o < ff.close_r2_f && r2n < ff.close_r2_f) {
+              // close pair: both differences in float-float from the exact
+              // squared distances, added with their rounding residuals
+              ClosePair cp = close_pair(o3, n3, ff.turn2_hi, ff.turn2_lo);
+              if (ecn != 0.0f) {
+                ff2 du = close_lj(cp, {sg2, ff.sigmaSq_lo_f[idx]},
+                                  {ecn, ff.eps_cn_lo_f[idx]});
+                two_sum_add(lj_h, lj_l, du.hi);
+                lj_l += du.lo;
+              }
+              if (coul && cin_n && cin_o) {
+                ff2 X = close_coulomb(cp, ff.ewald, ff.alpha2_f,
+                                      {ff.alpha3_hi, ff.alpha3_lo});
+                float pr = qq * X.hi;
+                two_sum_add(re_h, re_l, pr);
+                re_l += fmaf(qq, X.hi, -pr) + fmaf(qres, X.hi, qq * X.lo);
+              }
+              continue;
+            }
             // difference of the pair terms between r and r'
             // (d + d') in FP32: the integer sum can leave the int32 range
             float dr2 = fmaf(ddx, dox + dnx, fmaf(ddy, doy + dny, ddz * (doz + dnz)));
-            float ro = sqrtf(r2o), rn = sqrtf(r2n);
             float so = sg2 / r2o, sn = sg2 / r2n;
             float ds = -sg2 * dr2 / (r2o * r2n);
             float so3 = so * so * so, sn3 = sn * sn * sn;
@@ -401,46 +451,18 @@ __global__ void __launch_bounds__(MT_THREADS)
             float s33 = sn3 + so3;
             two_sum_add(lj_h, lj_l,
                         ecn * d3 * ((s33 - 1.0f) + fmaf(s33, k6, -k3)));
-            if (coul && cin_n && cin_o && r2o < ff.close_r2_f &&
-                r2n < ff.close_r2_f) {
-              // close pair: the bracket in float-float from exact distances
-              const int32_t o3[3] = {ox, oy, oz}, n3[3] = {nx_, ny_, nz_};
-              ff2 X = close_coulomb(o3, n3, ff.turn2_hi, ff.turn2_lo, ff.ewald,
-                                    ff.alpha2_f, {ff.alpha3_hi, ff.alpha3_lo});
-              two_sum_add(re_h, re_l,
-                          fmaf(qq, X.hi, fmaf(qres, X.hi, qq * X.lo)));
-            } else if (coul && cin_n && cin_o) {
-              float inv_o = 1.0f / ro, inv_n = 1.0f / rn;
-              float sum_r = ro + rn;
-              float dinv = -dr2 * inv_o * inv_n / sum_r;  // 1/rn - 1/ro
-              float derfc;                                 // erfc(a rn) - erfc(a ro)
-              float dal;  // alpha_f -> alpha correction of the bracket
-              if (ff.ewald) {
-                float tlo = alpha * ro, thi = alpha * rn;
-                float dt = alpha * dr2 / sum_r;              // thi - tlo
-                if (fabsf(dt) < 0.25f) {
-                  // 3-point Gauss-Legendre of exp(-t^2) over [tlo, thi]
-                  float tm = 0.5f * (tlo + thi), hw = 0.5f * dt;
-                  float t1 = fmaf(-0.774596669f, hw, tm),
-                        t3 = fmaf(0.774596669f, hw, tm);
-                  float em = expf(-tm * tm);
-                  // 2/sqrt(pi) (dt/2) [8/9 e(tm) + 5/9 (e(t1) + e(t3))], the
-                  // weights times 2/sqrt(pi) as FP32 hi + lo pairs
-                  float e13 = expf(-t1 * t1) + expf(-t3 * t3);
-                  float g = fmaf(1.00300372f, em, 0.626877308f * e13) +
-                            fmaf(-1.23839108e-8f, em, 7.16121695e-9f * e13);
-                  derfc = -hw * g;
-                  // exp(-tn^2) - exp(-to^2) = -2 tm dt exp(-tm^2) + O(dt^3)
-                  dal = 2.0f * coul_da * tm * dt * em;
-                } else {
-                  derfc = erfc_f32(thi) - erfc_f32(tlo);
-                  dal = -coul_da * (expf(-thi * thi) - expf(-tlo * tlo));
-                }
-                float en = erfc_f32(thi);
-                float X = fmaf(en, dinv, derfc * inv_o) + dal;
+            if (coul && cin_n && cin_o) {
+              if (ff.ewald && r2o >= ff.far_r2_f && r2n >= ff.far_r2_f) {
+                float X = fp32_bracket(r2o, r2n, dr2, alpha, ff.coul_da_f);
                 two_sum_add(re_h, re_l, fmaf(qq, X, qc * X));
               } else {
-                two_sum_add(re_h, re_l, fmaf(qq, dinv, qc * dinv));
+                // the erfc form on the exact distances (float-float r,
+                // alpha r and their differences)
+                ClosePair cp = close_pair(o3, n3, ff.turn2_hi, ff.turn2_lo);
+                float X = ff.ewald
+                              ? far_coulomb(cp, {ff.alpha_f, ff.alpha_lo_f})
+                              : close_coulomb(cp, false, 0.0f, {0.0f, 0.0f}).hi;
+                two_sum_add(re_h, re_l, fmaf(qq, X, qres * X));
               }
             } else if (coul) {
               if (cin_n) {
