@@ -16,6 +16,8 @@ e2e     : the same metric through the public API with host buffers: each step
           moves (gb_mc_run) and reads back energies and coordinates.
 mixed   : the mixed-precision form (FP32 pair / per-k arithmetic, FP64
           accumulators), several independent chains batched on one GPU.
+serving : a stream of water jobs of mixed size through the job server
+          (continuous batching), throughput and p50/p99 per-sweep latency.
 roofline: the dominant kernel (the persistent chain kernel) against the
           measured FP64 pipe peak of this GPU (float64 GEMM timed here).
 
@@ -411,6 +413,51 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
     return out
 
 
+def run_serving(args, dev):
+    """Serving stream on one GPU, scaled down from 256 jobs x 100 sweeps:
+    jobs of N waters, N log-uniform in [500, 20000] at 1 g/cm^3 (SPC/E, Rcut
+    9 A, Ewald tol 1e-5, T = 298 K), seeded lattices, Poisson arrivals at a
+    seeded rate, each asking for --serve-sweeps sweeps (1 sweep = N moves),
+    mixed form with an FP64 recompute every 10,000 moves; jobs are admitted by
+    device memory and chain slots and batched per round while they run."""
+    from gomc_gb300 import serving
+    from gomc_gb300.config import SimConfig
+    from gomc_gb300.systems import spce_water_box, water_box_length
+    rng = np.random.default_rng(SEED)
+    J, sweeps = args.serve_jobs, args.serve_sweeps
+    sizes = np.exp(rng.uniform(np.log(500), np.log(20000), J)).astype(int)
+    gaps = rng.exponential(1.0 / args.serve_rate, J)
+    cfg = SimConfig(temperature=TEMP, rcut=9.0, tolerance=TOL)
+    systems = [spce_water_box(int(n), water_box_length(int(n)), seed=SEED + i)
+               for i, n in enumerate(sizes)]
+    srv = serving.Server(device=dev, quantum=args.serve_quantum)
+    srv.start()
+    t0 = time.perf_counter()
+    for i, (s, n) in enumerate(zip(systems, sizes)):
+        target = t0 + float(np.sum(gaps[:i + 1]))
+        delay = target - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        srv.submit(s, cfg, seed=SEED + i, nsteps=int(n) * sweeps,
+                   scales=SCALES, adj_steps=ADJ, recompute_freq=10000)
+    srv.drain(timeout_s=600)
+    st = srv.stats()
+    srv.close()
+    return {
+        "workload": "%d water jobs, N log-uniform in [500, 20000] (sum %d "
+                    "molecules), %d sweeps each, Poisson arrivals at %.1f "
+                    "jobs/s, quantum %d moves per job per round"
+                    % (J, int(sizes.sum()), sweeps, args.serve_rate,
+                       args.serve_quantum),
+        "moves_per_s": st["moves_per_s"], "moves": st["moves"],
+        "wall_s": st["wall_s"],
+        "sweep_latency_ms": {"p50": st["sweep_p50_ms"],
+                             "p99": st["sweep_p99_ms"]},
+        "job_latency_s": {"p50": st["job_p50_s"], "p99": st["job_p99_s"]},
+        "rounds": st["rounds"], "mean_resident_jobs": st["mean_resident"],
+        "jobs_done": st["jobs_done"]}
+
+
 def run_gb300(args, rank, world):
     import torch
     dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -500,6 +547,10 @@ def run_gb300(args, rank, world):
         mixed = run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
                           value)
 
+    serving_stats = None
+    if not args.no_serving and rank == 0:
+        serving_stats = run_serving(args, dev)
+
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -539,6 +590,7 @@ def run_gb300(args, rank, world):
         "e2e_step_ms": [round(t * 1e3, 3) for t in e2e_times],
         "chain_kernel_ms_per_launch": kern_ms,
         "mixed": mixed,
+        "serving": serving_stats,
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -562,6 +614,12 @@ def main():
     ap.add_argument("--cluster", type=int, default=0,
                     help="CTAs per mixed chain (0: autotuned)")
     ap.add_argument("--mixed-compare-moves", type=int, default=10000)
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-jobs", type=int, default=32)
+    ap.add_argument("--serve-sweeps", type=int, default=2)
+    ap.add_argument("--serve-rate", type=float, default=64.0,
+                    help="job arrivals per second (Poisson)")
+    ap.add_argument("--serve-quantum", type=int, default=1000)
     ap.add_argument("--small", action="store_true",
                     help="256-water box instead of the 8000-water workload")
     args = ap.parse_args()
