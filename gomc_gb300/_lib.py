@@ -45,7 +45,9 @@ class Config(C.Structure):
                 ("rcut_low", C.c_double), ("rcut_coulomb", C.c_double),
                 ("tolerance", C.c_double), ("ewald", C.c_int32),
                 ("electrostatic", C.c_int32), ("precision", C.c_int32),
-                ("device", C.c_int32)]
+                ("device", C.c_int32), ("sc_alpha", C.c_double),
+                ("sc_sigma", C.c_double), ("sc_power", C.c_int32),
+                ("sc_coul", C.c_int32)]
 
 
 class McParams(C.Structure):
@@ -75,6 +77,7 @@ SIGNATURES = {
     "gb_system_total": (C.c_int, [_P, _D]),
     "gb_box_inter": (C.c_int, [_P, _D, _D]),
     "gb_molecule_inter": (C.c_int, [_P, C.c_int32, _D, _D, _D, _I]),
+    "gb_single_molecule_inter": (C.c_int, [_P, C.c_int32, _D, _D]),
     "gb_particle_inter": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_double, _D,
                                     C.c_int32, _D, _D, _I]),
     "gb_box_force": (C.c_int, [_P, _D, _D, _D, _D]),

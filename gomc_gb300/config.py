@@ -40,6 +40,12 @@ class SimConfig:
     multi_particle_freq: float = 0.0
     random_seed: int = 1234
     # build-only keys
+    # soft-core pair terms at lambda < 1 (ScaleAlpha, ScaleSigma, ScalePower,
+    # ScaleCoulomb; 0 when free-energy and NeMTMC moves are off)
+    sc_alpha: float = 0.0
+    sc_sigma: float = 0.0
+    sc_power: int = 0
+    sc_coul: bool = False
     precision: str = "fp64"
     recompute_freq: int = 10000
     autotune: bool = False

@@ -87,6 +87,10 @@ void build_ff(const HostSystem &s, const BoxConfig &c, FF *ff) {
   // r < 4 A without Ewald
   ff->close_r2_f = (float)(c.ewald ? 1.3 * 1.3 / ff->alphaSq : 16.0);
   ff->beta = 1 / c.temperature;
+  ff->sc_alpha = c.sc_alpha;
+  ff->sc_sigma_6 = std::pow(c.sc_sigma, 6.0);
+  ff->sc_power = c.sc_power;
+  ff->sc_coul = c.sc_coul;
 }
 
 // ---------------------------------------------------------------------------
@@ -674,6 +678,29 @@ int Box::MoleculeInter(int m, const double *new_pos, double *lj, double *real,
   *lj = h_pinned[0];
   *real = h_pinned[1];
   *overlap = h_pinned[2] != 0.0;
+  return CheckError();
+}
+
+// CalculateEnergy::SingleMoleculeInter (src/CalculateEnergy.cpp:1494-1556)
+int Box::SingleMoleculeInter(int m, const double lam[4], double out[4]) {
+  if (m < 0 || m >= dev.n_mol)
+    return Fail(ERR_ARG, "molecule index out of range");
+  for (int i = 0; i < 4; ++i)
+    if (!(lam[i] >= 0.0 && lam[i] <= 1.0))
+      return Fail(ERR_ARG, "lambda outside [0, 1]");
+  std::memcpy(h_pinned, lam, 4 * sizeof(double));
+  int rc = CudaCheck(cudaMemcpyAsync(d_small + 1024, h_pinned, 32,
+                                     cudaMemcpyHostToDevice, stream),
+                     "upload");
+  if (rc || (rc = launch_single_mol_inter(*this, m, d_small + 1024, d_small)))
+    return rc;
+  if ((rc = CudaCheck(cudaMemcpyAsync(h_pinned, d_small, 32,
+                                      cudaMemcpyDeviceToHost, stream),
+                      "download")) ||
+      (rc = Sync()))
+    return rc;
+  for (int i = 0; i < 4; ++i)
+    out[i] = h_pinned[i];
   return CheckError();
 }
 

@@ -18,6 +18,8 @@ struct BoxConfig {
   int ewald = 1, electrostatic = 1;
   int precision = 0;  // 0 = FP64 plain form, 1 = mixed
   int device = 0;
+  double sc_alpha = 0.0, sc_sigma = 0.0;  // soft-core settings
+  int sc_power = 0, sc_coul = 0;
 };
 
 class Box {
@@ -35,6 +37,7 @@ class Box {
   int SystemTotal(double out9[9]);               // CalculateEnergy::SystemTotal
   int MoleculeInter(int m, const double *new_pos, double *lj, double *real,
                     int *overlap);
+  int SingleMoleculeInter(int m, const double lam[4], double out[4]);
   int ParticleInter(int m, int kind, double charge, const double *trials,
                     int ntrials, double *en, double *real, int *overlap);
   int MolReciprocal(int m, const double *new_pos, double *de);
@@ -115,6 +118,8 @@ int launch_recip_energy(Box &b, const double *sumR, const double *sumI,
 int launch_mol_recip(Box &b, int m, const double *d_newpos, int sign_mode,
                      double *d_out);
 int launch_mol_inter(Box &b, int m, const double *d_newpos, double *d_out3);
+int launch_single_mol_inter(Box &b, int m, const double *d_lam4,
+                            double *d_out4);
 int launch_particle_inter(Box &b, int m, int kind, double charge,
                           const double *d_trials, int ntrials, double *d_out);
 int launch_correction(Box &b, double *d_out);

@@ -77,6 +77,14 @@ int gb_box_create(const gb_system_desc *sys, const gb_config *cfg,
   c.electrostatic = cfg->electrostatic ? 1 : 0;
   c.precision = cfg->precision;
   c.device = cfg->device;
+  c.sc_alpha = cfg->sc_alpha;
+  c.sc_sigma = cfg->sc_sigma;
+  c.sc_power = cfg->sc_power;
+  c.sc_coul = cfg->sc_coul ? 1 : 0;
+  if (c.sc_power < 0) {
+    g_create_error = "ScalePower must be >= 0";
+    return gb::ERR_ARG;
+  }
   if (c.precision != GB_FP64 && c.precision != GB_MIXED) {
     g_create_error = "precision must be GB_FP64 or GB_MIXED";
     return gb::ERR_ARG;
@@ -130,6 +138,16 @@ int gb_molecule_inter(gb_box *box, int32_t mol, const double *new_pos,
   *overlap = ov;
   return rc;
 }
+int gb_single_molecule_inter(gb_box *box, int32_t mol, const double *lambdas4,
+                             double *out4) {
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  if (!lambdas4 || !out4)
+    return box->b->Fail(gb::ERR_ARG, "null lambdas or output");
+  return box->b->SingleMoleculeInter(mol, lambdas4, out4);
+}
+
 int gb_particle_inter(gb_box *box, int32_t mol, int32_t kind, double charge,
                       const double *trials, int32_t ntrials, double *en,
                       double *real, int32_t *overlap) {

@@ -56,6 +56,10 @@ struct FF {
   double nexp[MAX_KINDS * MAX_KINDS];
   double eps_cn_6[MAX_KINDS * MAX_KINDS];
   double nOver6[MAX_KINDS * MAX_KINDS];
+  // soft-core settings at lambda < 1 (Forcefield::sc_*,
+  // src/Forcefield.cpp:59-75)
+  double sc_alpha, sc_sigma_6;
+  int sc_power, sc_coul;
   // FP32 copies for the mixed form
   float sigmaSq_f[MAX_KINDS * MAX_KINDS];
   float eps_cn_f[MAX_KINDS * MAX_KINDS];

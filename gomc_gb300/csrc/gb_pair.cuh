@@ -58,6 +58,43 @@ __device__ __forceinline__ double coulomb_virial(const FF &ff, double distSq,
   return qq / (distSq * dist);
 }
 
+// Soft-core squared distance at coupling lambda (src/FFParticle.cpp:301-308):
+// cbrt(sc_alpha (1 - lambda)^sc_power max(sigma^6, sc_sigma^6) + r^6).
+__device__ __forceinline__ double soft_rsq(const FF &ff, double distSq,
+                                           int idx, double lambda) {
+  double sigma6 = ff.sigmaSq[idx] * ff.sigmaSq[idx] * ff.sigmaSq[idx];
+  sigma6 = fmax(sigma6, ff.sc_sigma_6);
+  double dist6 = __dmul_rn(__dmul_rn(distSq, distSq), distSq);
+  double lambdaCoef = ff.sc_alpha * pow((1.0 - lambda), (double)ff.sc_power);
+  double softDist6 = __dadd_rn(__dmul_rn(lambdaCoef, sigma6), dist6);
+  return cbrt(softDist6);
+}
+
+// FFParticle::CalcEn at coupling lambda (src/FFParticle.cpp:295-316); the
+// caller has checked r^2 < Rcut^2.
+__device__ __forceinline__ double lj_energy_lambda(const FF &ff, double distSq,
+                                                   int idx, double lambda) {
+  if (lambda >= 0.999999)
+    return lj_energy(ff, distSq, idx);
+  return lambda * lj_energy(ff, soft_rsq(ff, distSq, idx, lambda), idx);
+}
+
+// FFParticle::CalcCoulomb at coupling lambda (src/FFParticle.cpp:361-387):
+// the soft-core distance only with sc_coul.
+__device__ __forceinline__ double coulomb_energy_lambda(const FF &ff,
+                                                        double distSq, int idx,
+                                                        double qq,
+                                                        double lambda) {
+  if (ff.rcutCoulSq < distSq)
+    return 0.0;
+  if (lambda >= 0.999999)
+    return coulomb_energy(ff, distSq, qq);
+  double r2 = ff.sc_coul ? soft_rsq(ff, distSq, idx, lambda) : distSq;
+  double dist = sqrt(r2);
+  double e = ff.ewald ? qq * erfc(ff.alpha * dist) / dist : qq / dist;
+  return lambda * e;
+}
+
 // Block-wide sum of one double, deterministic order; result valid in thread 0.
 template <int NT>
 __device__ __forceinline__ double block_sum(double v, double *sh) {

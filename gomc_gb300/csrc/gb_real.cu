@@ -202,6 +202,72 @@ int launch_mol_inter(Box &bx, int m, const double *d_newpos, double *d_out3) {
 }
 
 // ---------------------------------------------------------------------------
+// SingleMoleculeInter: unit u = atom * 27 + neighbour cell of the atom's
+// current cell; the molecule stays in the cell list and its own atoms are
+// skipped (src/CalculateEnergy.cpp:1494-1556).  lam = old VDW, new VDW, old
+// Coulomb, new Coulomb; partials = old LJ, old real, new LJ, new real.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(RT) k_single_mol_inter(
+    DevBox b, const FF *__restrict__ pff, int m,
+    const double *__restrict__ lam, double *part) {
+  const FF &ff = *pff;
+  int u = blockIdx.x;
+  int a = u / NB27, n = u % NB27;
+  int atom = b.mstart[m] + a;
+  double px = b.x[atom], py = b.y[atom], pz = b.z[atom];
+  int cell = position_to_cell_fast(b, px, py, pz);
+  int c2 = b.nbr[cell * NB27 + n];
+  int n2 = b.cell_count[c2];
+  double qa = b.q[atom];
+  int ka = b.kind[atom];
+  double lov = lam[0], lnv = lam[1], loc = lam[2], lnc = lam[3];
+  double ljo = 0.0, reo = 0.0, ljn = 0.0, ren = 0.0;
+  for (int j = threadIdx.x; j < n2; j += RT) {
+    size_t s = (size_t)c2 * b.cap + j;
+    int mj = b.cell_meta[s];
+    if (meta_mol(mj) == m)
+      continue;
+    double4_32a pj = b.cell_pos[s];
+    double dx = min_image(px - pj.x, b.L[0], b.half[0]);
+    double dy = min_image(py - pj.y, b.L[1], b.half[1]);
+    double dz = min_image(pz - pj.z, b.L[2], b.half[2]);
+    double distSq = dsq3(dx, dy, dz);
+    if (!(ff.rcutSq > distSq))
+      continue;
+    int idx = ka + meta_kind(mj) * ff.n_kinds;
+    if (ff.electrostatic) {
+      double qq = qa * pj.w * QQ_FACT;
+      if (qq != 0.0) {
+        ren += coulomb_energy_lambda(ff, distSq, idx, qq, lnc);
+        reo += coulomb_energy_lambda(ff, distSq, idx, qq, loc);
+      }
+    }
+    ljn += lj_energy_lambda(ff, distSq, idx, lnv);
+    ljo += lj_energy_lambda(ff, distSq, idx, lov);
+  }
+  __shared__ double red[RT / 32];
+  double v[4] = {ljo, reo, ljn, ren};
+  for (int c = 0; c < 4; ++c) {
+    double r = block_sum<RT>(v[c], red);
+    if (threadIdx.x == 0)
+      part[4 * u + c] = r;
+  }
+}
+
+int launch_single_mol_inter(Box &bx, int m, const double *d_lam4,
+                            double *d_out4) {
+  int na = bx.host.mstart[m + 1] - bx.host.mstart[m];
+  int units = na * NB27;
+  int rc = bx.EnsureScratch((size_t)units * 4);
+  if (rc)
+    return rc;
+  k_single_mol_inter<<<units, RT, 0, bx.stream>>>(bx.dev, bx.d_ff, m, d_lam4,
+                                                  bx.d_scratch);
+  k_reduce_partials<<<1, RT, 0, bx.stream>>>(bx.d_scratch, units, 4, d_out4, 0);
+  return bx.CudaCheck(cudaGetLastError(), "single molecule inter");
+}
+
+// ---------------------------------------------------------------------------
 // ParticleInter: unit u = trial * 27 + neighbour; atoms of molecule m are
 // treated as absent from the cell list (the molecule being grown).
 // ---------------------------------------------------------------------------

@@ -203,6 +203,10 @@ Job *make_job(const gb_system_desc *sys, const gb_config *cfg) {
   c.electrostatic = cfg->electrostatic ? 1 : 0;
   c.precision = GB_MIXED;
   c.device = cfg->device;
+  c.sc_alpha = cfg->sc_alpha;
+  c.sc_sigma = cfg->sc_sigma;
+  c.sc_power = cfg->sc_power;
+  c.sc_coul = cfg->sc_coul ? 1 : 0;
   return j;
 }
 

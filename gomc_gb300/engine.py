@@ -61,6 +61,10 @@ def config_struct(cfg, precision: int, device: int):
     c.electrostatic = int(cfg.electrostatic)
     c.precision = precision
     c.device = device
+    c.sc_alpha = float(getattr(cfg, "sc_alpha", 0.0))
+    c.sc_sigma = float(getattr(cfg, "sc_sigma", 0.0))
+    c.sc_power = int(getattr(cfg, "sc_power", 0))
+    c.sc_coul = int(bool(getattr(cfg, "sc_coul", False)))
     return c
 
 
@@ -151,6 +155,15 @@ class Box:
         self._chk(lib().gb_molecule_inter(self.h, int(m), _dp(p), C.byref(a),
                                           C.byref(b), C.byref(o)))
         return bool(o.value), a.value, b.value
+
+    def single_molecule_inter(self, m: int, lambdas):
+        """(old inter, old real, new inter, new real) of molecule m at
+        lambdas = (old VDW, new VDW, old Coulomb, new Coulomb)."""
+        lam = np.ascontiguousarray(lambdas, dtype=np.float64).reshape(4)
+        out = np.empty(4)
+        self._chk(lib().gb_single_molecule_inter(self.h, int(m), _dp(lam),
+                                                 _dp(out)))
+        return out
 
     def particle_inter(self, m: int, kind: int, charge: float, trials):
         t = np.ascontiguousarray(trials, dtype=np.float64).reshape(-1, 3)
@@ -368,6 +381,15 @@ class CalculateEnergy:
     def MoleculeInter(self, molCoords, molIndex: int):
         """Returns (overlap, inter_LJ, inter_coulomb)."""
         return self.box.molecule_inter(molIndex, molCoords)
+
+    def SingleMoleculeInter(self, lambdaOldVDW: float, lambdaNewVDW: float,
+                            lambdaOldCoulomb: float, lambdaNewCoulomb: float,
+                            molIndex: int):
+        """Returns (interEnOld, interEnNew) as {inter, real} dicts."""
+        o = self.box.single_molecule_inter(
+            molIndex, [lambdaOldVDW, lambdaNewVDW, lambdaOldCoulomb,
+                       lambdaNewCoulomb])
+        return (dict(inter=o[0], real=o[1]), dict(inter=o[2], real=o[3]))
 
     def ParticleInter(self, trialPos, partIndex_kind: int, charge: float,
                       molIndex: int):

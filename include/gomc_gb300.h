@@ -60,6 +60,11 @@ typedef struct gb_config {
   int32_t electrostatic;/* ElectroStatic */
   int32_t precision;    /* GB300Precision: GB_FP64 or GB_MIXED */
   int32_t device;       /* CUDA device ordinal */
+  /* soft-core settings of pair terms at lambda < 1 (FreeEnergyCalc /
+   * NeMTMC blocks: ScaleAlpha, ScaleSigma, ScalePower, ScaleCoulomb; all 0
+   * when neither is enabled, src/Forcefield.cpp:59-75) */
+  double sc_alpha, sc_sigma;
+  int32_t sc_power, sc_coul;
 } gb_config;
 
 const char *gb_version(void);
@@ -84,6 +89,12 @@ int gb_box_inter(gb_box *box, double *inter, double *real);
  * molecule `mol` from its current position to new_pos[n_atoms_of_mol * 3]. */
 int gb_molecule_inter(gb_box *box, int32_t mol, const double *new_pos,
                       double *lj, double *real, int32_t *overlap);
+/* SingleMoleculeInter (src/CalculateEnergy.cpp:1494-1556): real-space
+ * energy of molecule `mol` at its current position with its neighbourhood,
+ * at two coupling pairs.  lambdas4 = old VDW, new VDW, old Coulomb, new
+ * Coulomb; out4 = old inter, old real, new inter, new real (K). */
+int gb_single_molecule_inter(gb_box *box, int32_t mol, const double *lambdas4,
+                             double *out4);
 /* ParticleInter (src/CalculateEnergy.cpp:727-785): one atom of kind/charge
  * at each of ntrials positions; atoms of molecule `mol` are excluded. */
 int gb_particle_inter(gb_box *box, int32_t mol, int32_t kind, double charge,

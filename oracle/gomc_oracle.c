@@ -559,6 +559,100 @@ int ora_molecule_inter(ora_sys *s, int m, const double *newpos, double *dlj,
   return overlap;
 }
 
+/* FFParticle::CalcEn / CalcCoulomb at a coupling lambda with the soft-core
+ * distance (src/FFParticle.cpp:295-316, 361-387): below lambda 0.999999 the
+ * pair is evaluated at r_sc^2 = cbrt(sc_alpha (1 - lambda)^sc_power
+ * max(sigma^6, sc_sigma^6) + r^6) and scaled by lambda; Coulomb takes the
+ * soft-core distance only when sc_coul is set. */
+static double soft_rsq(const ora_sys *s, double distSq, int idx,
+                       const ora_softcore *sc, double lambda) {
+  double sigma6 = s->sigmaSq[idx] * s->sigmaSq[idx] * s->sigmaSq[idx];
+  sigma6 = sigma6 > sc->sigma6 ? sigma6 : sc->sigma6;
+  double dist6 = distSq * distSq * distSq;
+  double lambdaCoef = sc->alpha * pow((1.0 - lambda), (double)sc->power);
+  double softDist6 = lambdaCoef * sigma6 + dist6;
+  return cbrt(softDist6);
+}
+static double calc_en_lambda(const ora_sys *s, double distSq, int k1, int k2,
+                             const ora_softcore *sc, double lambda) {
+  if (s->rcutSq < distSq)
+    return 0.0;
+  if (lambda >= 0.999999)
+    return calc_en(s, distSq, k1, k2);
+  int idx = k1 + k2 * s->n_kinds;
+  double softRsq = soft_rsq(s, distSq, idx, sc, lambda);
+  /* FFParticle::CalcEn(distSq, index) has no cutoff test */
+  double rRat2 = s->sigmaSq[idx] / softRsq;
+  double rRat4 = rRat2 * rRat2;
+  double attract = rRat4 * rRat2;
+  double repulse = pow(rRat2, (s->nexp[idx] * 0.5));
+  return lambda * (s->eps_cn[idx] * (repulse - attract));
+}
+static double coulomb_plain(const ora_sys *s, double distSq, double qq) {
+  double dist = sqrt(distSq);
+  if (s->ewald)
+    return qq * erfc(s->alpha * dist) / dist;
+  return qq / dist;
+}
+static double calc_coulomb_lambda(const ora_sys *s, double distSq, int k1,
+                                  int k2, double qq, const ora_softcore *sc,
+                                  double lambda) {
+  if (s->rcutCoulSq < distSq)
+    return 0.0;
+  if (lambda >= 0.999999)
+    return coulomb_plain(s, distSq, qq);
+  if (sc->coul) {
+    int idx = k1 + k2 * s->n_kinds;
+    return lambda * coulomb_plain(s, soft_rsq(s, distSq, idx, sc, lambda), qq);
+  }
+  return lambda * coulomb_plain(s, distSq, qq);
+}
+
+/* SingleMoleculeInter, src/CalculateEnergy.cpp:1494-1556: the real-space
+ * energy of molecule m at its current position, with every other atom of its
+ * 27-cell neighbourhood, at the old and the new lambda pair.
+ * lam = {old VDW, new VDW, old Coulomb, new Coulomb};
+ * out = {old inter, old real, new inter, new real}. */
+void ora_single_molecule_inter(const ora_sys *s, int m, const double *lam,
+                               const ora_softcore *sc, double *out) {
+  double tempREnOld = 0.0, tempLJEnOld = 0.0;
+  double tempREnNew = 0.0, tempLJEnNew = 0.0;
+  int *nb = (int *)malloc(sizeof(int) * (s->n_atoms + 1));
+  int start = s->mstart[m], len = s->mstart[m + 1] - start;
+  for (int p = 0; p < len; ++p) {
+    int atom = start + p;
+    int cell = position_to_cell(s, s->x[atom], s->y[atom], s->z[atom]);
+    int nn = gather_neighbors(s, cell, nb);
+    for (int i = 0; i < nn; i++) {
+      int j = nb[i];
+      if (s->mol[j] == m)
+        continue;
+      double distSq = dist_sq(s, s->x[atom], s->y[atom], s->z[atom], s->x[j],
+                              s->y[j], s->z[j], 0);
+      if (!(s->rcutSq > distSq))
+        continue;
+      if (s->electrostatic) {
+        double qq = s->q[atom] * s->q[j] * QQ_FACT;
+        if (qq != 0.0) {
+          tempREnNew += calc_coulomb_lambda(s, distSq, s->kind[atom],
+                                            s->kind[j], qq, sc, lam[3]);
+          tempREnOld += calc_coulomb_lambda(s, distSq, s->kind[atom],
+                                            s->kind[j], qq, sc, lam[2]);
+        }
+      }
+      tempLJEnNew +=
+          calc_en_lambda(s, distSq, s->kind[atom], s->kind[j], sc, lam[1]);
+      tempLJEnOld +=
+          calc_en_lambda(s, distSq, s->kind[atom], s->kind[j], sc, lam[0]);
+    }
+  }
+  free(nb);
+  out[0] = tempLJEnOld;
+  out[1] = tempREnOld;
+  out[2] = tempLJEnNew;
+  out[3] = tempREnNew;
+}
+
 /* ParticleInter, src/CalculateEnergy.cpp:727-785, one trial */
 int ora_particle_inter(const ora_sys *s, int m, int kindI, double qI,
                        const double *t, double *en, double *real) {

@@ -54,6 +54,17 @@ void ora_set_energy(ora_sys *s, const double *e5);
 void ora_system_total(ora_sys *s, double *out9);
 void ora_grid_all(ora_sys *s);
 
+/* Soft-core settings of FFParticle at lambda < 1 (Forcefield sc_alpha,
+ * sc_sigma_6, sc_power, sc_coul; src/Forcefield.cpp:59-75). */
+typedef struct ora_softcore {
+  double alpha, sigma6;
+  int power, coul;
+} ora_softcore;
+/* CalculateEnergy::SingleMoleculeInter (src/CalculateEnergy.cpp:1494-1556):
+ * lam = old VDW, new VDW, old Coulomb, new Coulomb lambdas;
+ * out = old inter, old real, new inter, new real. */
+void ora_single_molecule_inter(const ora_sys *s, int m, const double *lam,
+                               const ora_softcore *sc, double *out);
 /* CalculateEnergy::MoleculeInter with the molecule removed from the cell list
  * first (as Translate::CalcEn does).  Returns overlap. */
 int ora_molecule_inter(ora_sys *s, int m, const double *newpos, double *dlj,

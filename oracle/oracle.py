@@ -60,6 +60,8 @@ def lib():
             "ora_system_total": (None, [P, dp]),
             "ora_grid_all": (None, [P]),
             "ora_molecule_inter": (I, [P, I, dp, dp, dp]),
+            "ora_single_molecule_inter": (None, [P, I, dp,
+                                                 C.POINTER(SoftCore), dp]),
             "ora_particle_inter": (I, [P, I, I, D, dp, dp, dp]),
             "ora_mol_reciprocal": (D, [P, dp, I]),
             "ora_swap_dest_recip": (D, [P, dp, I]),
@@ -91,6 +93,12 @@ def lib():
             f.argtypes = args
         _lib = L
     return _lib
+
+
+class SoftCore(C.Structure):
+    """ora_softcore: sc_alpha, sc_sigma^6, sc_power, sc_coul."""
+    _fields_ = [("alpha", C.c_double), ("sigma6", C.c_double),
+                ("power", C.c_int), ("coul", C.c_int)]
 
 
 def _dp(a: np.ndarray):
@@ -205,6 +213,18 @@ class OracleBox:
         ov = lib().ora_molecule_inter(self.h, int(m), _dp(p), C.byref(a),
                                       C.byref(b))
         return bool(ov), a.value, b.value
+
+    def single_molecule_inter(self, m: int, lambdas, sc_alpha: float,
+                              sc_sigma: float, sc_power: int, sc_coul: bool):
+        """(old inter, old real, new inter, new real) at lambdas = (old VDW,
+        new VDW, old Coulomb, new Coulomb)."""
+        lam = np.ascontiguousarray(lambdas, dtype=np.float64)
+        sc = SoftCore(float(sc_alpha), float(sc_sigma) ** 6, int(sc_power),
+                      int(bool(sc_coul)))
+        out = np.empty(4)
+        lib().ora_single_molecule_inter(self.h, int(m), _dp(lam), C.byref(sc),
+                                        _dp(out))
+        return out
 
     def particle_inter(self, m: int, kind: int, charge: float, trial):
         t = np.ascontiguousarray(trial, dtype=np.float64)

@@ -123,12 +123,15 @@ int main(int argc, char **argv) {
     return dump_kat(argv[2]);
   if (argc < 4) {
     fprintf(stderr,
-            "usage: ref_probe in.conf outdir nsteps [proposals.txt]\n");
+            "usage: ref_probe in.conf outdir nsteps [proposals.txt|-] "
+            "[lambdas.txt]\n");
     return 1;
   }
   std::string outdir = argv[2];
   long nsteps = atol(argv[3]);
-  const char *propFile = argc > 4 ? argv[4] : nullptr;
+  const char *propFile =
+      argc > 4 && std::string(argv[4]) != "-" ? argv[4] : nullptr;
+  const char *lamFile = argc > 5 ? argv[5] : nullptr;
 
   Simulation sim(argv[1]);
   System &sys = *sim.system;
@@ -247,6 +250,37 @@ int main(int argc, char **argv) {
       }
       fprintf(f, "%u %d %.17g %.17g %.17g %.17g %.17g\n", m, (int)overlap,
               lj.energy, coul.energy, recip, dest, src);
+    }
+    fclose(f);
+  }
+
+  // ---- SingleMoleculeInter at two lambda values ---------------------------
+  // lambdas.txt: "sc_alpha sc_sigma sc_power", n, then n lines
+  // "mol lambdaOldVDW lambdaNewVDW lambdaOldCoulomb lambdaNewCoulomb sc_coul";
+  // the soft-core settings are set on the reference's own Forcefield
+  // (src/Forcefield.cpp:59-75) before each call.
+  if (lamFile) {
+    std::ifstream in(lamFile);
+    double scA, scS;
+    uint scP;
+    int n = 0;
+    in >> scA >> scS >> scP >> n;
+    Forcefield &ffd = stat.forcefield;
+    ffd.sc_alpha = scA;
+    ffd.sc_sigma = scS;
+    ffd.sc_sigma_6 = pow(scS, 6.0);
+    ffd.sc_power = scP;
+    FILE *f = open_out(outdir, "single_mol_out.txt");
+    for (int i = 0; i < n; ++i) {
+      uint m;
+      int scc;
+      double lov, lnv, loc, lnc;
+      in >> m >> lov >> lnv >> loc >> lnc >> scc;
+      ffd.sc_coul = scc != 0;
+      Energy eo, en;
+      sys.calcEnergy.SingleMoleculeInter(eo, en, lov, lnv, loc, lnc, m, box);
+      fprintf(f, "%u %.17g %.17g %.17g %.17g %d %.17g %.17g %.17g %.17g\n", m,
+              lov, lnv, loc, lnc, scc, eo.inter, eo.real, en.inter, en.real);
     }
     fclose(f);
   }

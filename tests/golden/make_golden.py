@@ -180,6 +180,43 @@ def make_one(probe: str, name: str) -> None:
         print("wrote", name)
 
 
+# soft-core settings of the SingleMoleculeInter vectors: ScaleAlpha,
+# ScaleSigma, ScalePower (GOMC's defaults for free-energy runs)
+SOFT_CORE = (0.5, 3.0, 2)
+
+
+def make_single_mol(probe: str, name: str, n: int = 48) -> None:
+    """SingleMoleculeInter (src/CalculateEnergy.cpp:1494-1556) of random
+    molecules at random old/new lambda pairs, with and without soft-core
+    Coulomb, on the fixture's initial state -> smi_<name>.npz."""
+    builder, cfg, _, _ = FIXTURES[name]
+    sysm = builder()
+    rng = np.random.default_rng(2000 + len(name))
+    mols = rng.integers(0, sysm.n_mol, size=n)
+    lam = rng.uniform(0.0, 1.0, size=(n, 4))
+    lam[::6] = 1.0                       # the lambda = 1 shortcut
+    lam[1::6, :2] = 0.0                  # fully decoupled LJ
+    lam[2::6, 1] = 0.9999995             # just inside the shortcut
+    scc = (np.arange(n) % 2).astype(int)
+    with tempfile.TemporaryDirectory() as d:
+        write_reference_inputs(d, sysm, cfg)
+        with open(os.path.join(d, "lam.txt"), "w") as f:
+            f.write("%.17g %.17g %d\n%d\n" % (SOFT_CORE + (n,)))
+            for m, l, c in zip(mols, lam, scc):
+                f.write("%d %s %d\n" % (m, " ".join("%.17g" % v for v in l),
+                                          c))
+        out = os.path.join(d, "out")
+        os.makedirs(out)
+        subprocess.check_call([probe, "in.conf", out, "0", "-", "lam.txt"],
+                              cwd=d, stdout=subprocess.DEVNULL)
+        r = np.loadtxt(os.path.join(out, "single_mol_out.txt")).reshape(n, -1)
+    np.savez_compressed(os.path.join(HERE, "smi_" + name + ".npz"),
+                        mol=r[:, 0].astype(np.int64), lam=r[:, 1:5],
+                        sc_coul=r[:, 5].astype(np.int64), out=r[:, 6:10],
+                        soft_core=np.array(SOFT_CORE, dtype=np.float64))
+    print("wrote smi_" + name)
+
+
 def make_kat(probe: str) -> None:
     """Known-answer vectors of the reference's MT19937 and Philox4x64-10."""
     with tempfile.TemporaryDirectory() as d:
@@ -204,6 +241,9 @@ def main():
         make_kat(probe)
     for n in (a.names or list(FIXTURES)):
         make_one(probe, n)
+    for n in ("c0_water", "w1728", "lj500"):
+        if not a.names or n in a.names:
+            make_single_mol(probe, n)
 
 
 if __name__ == "__main__":

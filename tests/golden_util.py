@@ -48,3 +48,15 @@ def config_of(meta):
 def move_fractions(meta):
     c = meta["config"]
     return [c["dis_freq"], c["rot_freq"], c["multi_particle_freq"]]
+
+
+SMI_NAMES = ["c0_water", "w1728", "lj500"]
+
+
+def load_smi(name):
+    """SingleMoleculeInter vectors of fixture `name` (the reference's
+    CalculateEnergy::SingleMoleculeInter on the fixture's initial state):
+    molecule, lambdas (old VDW, new VDW, old Coulomb, new Coulomb), sc_coul,
+    outputs (old inter, old real, new inter, new real) and the soft-core
+    settings (ScaleAlpha, ScaleSigma, ScalePower)."""
+    return np.load(os.path.join(GOLDEN, "smi_" + name + ".npz"))

@@ -7,7 +7,8 @@ accept/reject sequence identical to the reference's over the golden traces.
 import numpy as np
 import pytest
 
-from tests.golden_util import NAMES, config_of, load, move_fractions, system_of
+from tests.golden_util import (NAMES, SMI_NAMES, config_of, load, load_smi,
+                               move_fractions, system_of)
 
 pytestmark = pytest.mark.gpu
 
@@ -163,3 +164,25 @@ def test_particle_inter_against_oracle(gb):
         assert close(en[t], e2, scale=max(abs(e2), 1.0))
         assert close(re[t], r2, scale=max(abs(r2), 1.0))
     box.close()
+
+
+@pytest.mark.parametrize("name", SMI_NAMES)
+def test_single_molecule_inter(gb, name):
+    """SingleMoleculeInter on the GPU against the reference's vectors: every
+    output within 1e-10 relative (1e-10 K absolute for values near 0)."""
+    import dataclasses
+    z, meta = load(name)
+    g = load_smi(name)
+    a, s, p = g["soft_core"]
+    boxes = {}
+    for c in (0, 1):
+        cfg = dataclasses.replace(config_of(meta), sc_alpha=float(a),
+                                  sc_sigma=float(s), sc_power=int(p),
+                                  sc_coul=bool(c))
+        boxes[c] = gb.Box(system_of(z, meta), cfg)
+    for m, lam, c, ref in zip(g["mol"], g["lam"], g["sc_coul"], g["out"]):
+        got = boxes[int(c)].single_molecule_inter(int(m), lam)
+        for x, y in zip(got, ref):
+            assert abs(x - y) <= REL * max(abs(y), 1.0), (m, lam, c, got, ref)
+    for b in boxes.values():
+        b.close()

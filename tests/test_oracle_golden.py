@@ -11,7 +11,8 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from tests.golden_util import NAMES, config_of, load, move_fractions, system_of
+from tests.golden_util import (NAMES, SMI_NAMES, config_of, load, load_smi,
+                               move_fractions, system_of)
 
 REL = 1e-12
 
@@ -132,3 +133,17 @@ def test_rng_known_answers():
         for d in range(3):
             assert O.u01_64(r[d]) == row_r[d]
             assert 1.0 * O.uneg11_64(r[d]) == row_r[3 + d]
+
+
+@pytest.mark.parametrize("name", SMI_NAMES)
+def test_single_molecule_inter(name):
+    """CalculateEnergy::SingleMoleculeInter at two lambda pairs, soft-core
+    LJ and (every other row) soft-core Coulomb: bit-exact."""
+    z, meta = load(name)
+    ob = O.OracleBox(system_of(z, meta), config_of(meta))
+    g = load_smi(name)
+    a, s, p = g["soft_core"]
+    for m, lam, c, ref in zip(g["mol"], g["lam"], g["sc_coul"], g["out"]):
+        got = ob.single_molecule_inter(int(m), lam, a, s, int(p), bool(c))
+        np.testing.assert_array_equal(got, ref)
+    del ob
