@@ -414,7 +414,8 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
 
 
 def run_serving(args, dev):
-    """Serving stream on one GPU, scaled down from 256 jobs x 100 sweeps:
+    """Serving stream on one GPU, scaled down from 256 jobs x 100 sweeps
+    (the longest job alone then needs 2 x 20,000 sequential moves, the tail):
     jobs of N waters, N log-uniform in [500, 20000] at 1 g/cm^3 (SPC/E, Rcut
     9 A, Ewald tol 1e-5, T = 298 K), seeded lattices, Poisson arrivals at a
     seeded rate, each asking for --serve-sweeps sweeps (1 sweep = N moves),
@@ -446,7 +447,7 @@ def run_serving(args, dev):
     return {
         "workload": "%d water jobs, N log-uniform in [500, 20000] (sum %d "
                     "molecules), %d sweeps each, Poisson arrivals at %.1f "
-                    "jobs/s, quantum %d moves per job per round"
+                    "jobs/s, base quantum %d moves per round"
                     % (J, int(sizes.sum()), sweeps, args.serve_rate,
                        args.serve_quantum),
         "moves_per_s": st["moves_per_s"], "moves": st["moves"],
@@ -455,6 +456,7 @@ def run_serving(args, dev):
                              "p99": st["sweep_p99_ms"]},
         "job_latency_s": {"p50": st["job_p50_s"], "p99": st["job_p99_s"]},
         "rounds": st["rounds"], "mean_resident_jobs": st["mean_resident"],
+        "helper_busy_s": st["helper_busy_s"], "round_busy_s": st["round_busy_s"],
         "jobs_done": st["jobs_done"]}
 
 
@@ -615,7 +617,7 @@ def main():
                     help="CTAs per mixed chain (0: autotuned)")
     ap.add_argument("--mixed-compare-moves", type=int, default=10000)
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--serve-jobs", type=int, default=32)
+    ap.add_argument("--serve-jobs", type=int, default=96)
     ap.add_argument("--serve-sweeps", type=int, default=2)
     ap.add_argument("--serve-rate", type=float, default=64.0,
                     help="job arrivals per second (Poisson)")

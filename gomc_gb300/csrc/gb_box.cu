@@ -4,8 +4,26 @@
 #include <cmath>
 #include <cstring>
 #include <algorithm>
+#include <map>
+#include <mutex>
 
 namespace gb {
+
+void raise_smem_limit(const void *func, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> limit;
+  if (bytes <= 48 * 1024)
+    return;
+  int dev = 0;
+  cudaGetDevice(&dev);  // the attribute belongs to the current device
+  std::lock_guard<std::mutex> g(mu);
+  size_t &cur = limit[{dev, func}];
+  if (bytes > cur) {
+    cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)bytes);
+    cur = bytes;
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Force field: FFSetup::Particle::Read zeroing (src/FFSetup.cpp:246-255),
@@ -394,18 +412,43 @@ int Box::Init(const HostSystem &s0, const BoxConfig &c) {
       return Fail(ERR_UNSUPPORTED, "k-vector index above 127");
     std::vector<float> pff(pf.begin(), pf.end());
     size_t K = d.K;
+    // runs of consecutive n_x per (n_y, n_z) column, k indices ascending
+    std::map<std::pair<int, int>, std::vector<std::pair<int, int>>> cols;
+    for (int k = 0; k < d.K; ++k)
+      cols[{kn[k].y, kn[k].z}].push_back({kn[k].x, k});
+    std::vector<int4> runs;
+    std::vector<int> run_k;
+    for (auto &c : cols) {
+      auto &v = c.second;  // n_x ascending (k vectors are listed x outer)
+      size_t i = 0;
+      while (i < v.size()) {
+        size_t j = i + 1;
+        while (j < v.size() && j - i < (size_t)KRUN &&
+               v[j].first == v[j - 1].first + 1)
+          ++j;
+        runs.push_back(make_int4(c.first.first, c.first.second, v[i].first,
+                                 (int)(j - i)));
+        for (int g = 0; g < KRUN; ++g)
+          run_k.push_back(i + g < j ? v[i + g].second : -1);
+        i = j;
+      }
+    }
+    d.nrun = (int)runs.size();
     if ((rc = Alloc(&d.kx, K)) || (rc = Alloc(&d.ky, K)) ||
         (rc = Alloc(&d.kz, K)) || (rc = Alloc(&d.prefact, K)) ||
         (rc = Alloc(&d.hsqr, K)) || (rc = Alloc(&d.kn, K)) ||
         (rc = Alloc(&d.prefact_f, K)) || (rc = Alloc(&d.sumRref, K)) ||
         (rc = Alloc(&d.sumIref, K)) || (rc = Alloc(&d.sumRnew, K)) ||
-        (rc = Alloc(&d.sumInew, K)))
+        (rc = Alloc(&d.sumInew, K)) || (rc = Alloc(&d.krun, runs.size())) ||
+        (rc = Alloc(&d.krun_k, run_k.size())))
       return rc;
     if ((rc = up(d.kx, kx.data(), K * 8)) || (rc = up(d.ky, ky.data(), K * 8)) ||
         (rc = up(d.kz, kz.data(), K * 8)) ||
         (rc = up(d.prefact, pf.data(), K * 8)) ||
         (rc = up(d.hsqr, hs.data(), K * 8)) ||
         (rc = up(d.kn, kn.data(), K * 4)) ||
+        (rc = up(d.krun, runs.data(), runs.size() * sizeof(int4))) ||
+        (rc = up(d.krun_k, run_k.data(), run_k.size() * sizeof(int))) ||
         (rc = up(d.prefact_f, pff.data(), K * 4)))
       return rc;
   }

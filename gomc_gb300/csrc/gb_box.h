@@ -97,6 +97,11 @@ class Box {
   int Alloc(T **p, size_t n);
 };
 
+// Raise `func`'s dynamic shared-memory limit to at least `bytes`; the limit
+// only ever grows, so launches and occupancy queries from several host
+// threads never see it lowered under them (gb_box.cu).
+void raise_smem_limit(const void *func, size_t bytes);
+
 // host helpers (gb_box.cu)
 void build_ff(const HostSystem &s, const BoxConfig &c, FF *ff);
 void recip_vectors(const double L[3], double volume, double alphaSq,

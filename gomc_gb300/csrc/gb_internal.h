@@ -23,6 +23,7 @@ constexpr int NB27 = 27;
 constexpr int MAX_KINDS = 8;
 constexpr int MAX_MOL_ATOMS = 8;   // rigid molecules handled by the move loop
 constexpr int END_CELL = -1;
+constexpr int KRUN = 8;  // k-vectors per run of the structure-factor kernel
 
 // Status codes of the C ABI (include/gomc_gb300.h).
 enum Status : int {
@@ -122,6 +123,12 @@ struct DevBox {
   int K, kmax;
   double *kx, *ky, *kz, *prefact, *hsqr;  // [K]
   char4 *kn;                              // [K] integer k indices
+  // runs of up to KRUN k-vectors with one (n_y, n_z) and consecutive n_x,
+  // for the full structure factor: (n_y, n_z, first n_x, length) and the
+  // k index of each member (-1 past the length)
+  int nrun;
+  int4 *krun;   // [nrun]
+  int *krun_k;  // [nrun * KRUN]
   float *prefact_f;                       // [K]
   double *sumRref, *sumIref, *sumRnew, *sumInew;  // [K]
   // running energies: inter, real, recip, self, correction

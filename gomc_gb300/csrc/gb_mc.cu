@@ -994,9 +994,7 @@ int mc_init(Box &b, const gb_mc_params &p) {
   // chain-kernel geometry: one CTA per SM (cooperative residency checked)
   int per_sm = 0;
   size_t sm = chain_smem(b, b.sm_count);
-  if (sm > 48 * 1024)
-    cudaFuncSetAttribute(k_chain_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sm);
+  raise_smem_limit((const void *)k_chain_fp64, sm);
   if ((rc = b.CudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                             &per_sm, k_chain_fp64, CT, sm),
                         "occupancy")))
@@ -1572,23 +1570,36 @@ int mixed_launch(const std::vector<Box *> &boxes,
 // recompute frequency.
 int mixed_complete(const std::vector<Box *> &boxes,
                    const std::vector<int64_t> &n,
-                   const std::vector<Box *> &leaders) {
+                   const std::vector<Box *> &leaders,
+                   std::vector<char> *due) {
   int rc;
   for (Box *L : leaders)
     if ((rc = L->Sync()))
       return rc;
+  if (due)
+    due->assign(boxes.size(), 0);
   for (size_t i = 0; i < boxes.size(); ++i) {
     if (n[i] <= 0)
       continue;
     Box &b = *boxes[i];
     McState &s = *b.mc;
     int64_t R = s.params.recompute_freq;
-    if (R > 0 && s.next_step % R == 0 && (rc = recompute_fp64(b, s)))
-      return rc;
+    if (R > 0 && s.next_step % R == 0) {
+      if (due)
+        (*due)[i] = 1;
+      else if ((rc = recompute_fp64(b, s)))
+        return rc;
+    }
     if ((rc = b.CheckError()))
       return rc;
   }
   return OK;
+}
+
+int mc_recompute(Box &b) {
+  if (!b.mc)
+    return b.Fail(ERR_STATE, "gb_mc_init has not been called");
+  return recompute_fp64(b, *b.mc);
 }
 
 // Moves box i can run before its next recompute boundary (at most cap).

@@ -148,14 +148,17 @@ constexpr size_t MIXED_SMEM_MAX = 220 * 1024;
 // Batched segments of mixed boxes (gb_mc.cu): mixed_launch uploads the next
 // n[i] moves of box i and launches one kernel per cluster size on the stream
 // of that group's first box (`leaders`); mixed_complete waits for them and
-// runs the periodic FP64 recomputes that fall due.  mixed_segment_limit is
+// runs the periodic FP64 recomputes that fall due, or, given `due`, marks
+// them there for the caller to run (mc_recompute).  mixed_segment_limit is
 // the longest segment (at most cap) that ends at or before the box's next
 // recompute boundary.
 int mixed_launch(const std::vector<Box *> &boxes,
                  const std::vector<int64_t> &n, std::vector<Box *> *leaders);
 int mixed_complete(const std::vector<Box *> &boxes,
                    const std::vector<int64_t> &n,
-                   const std::vector<Box *> &leaders);
+                   const std::vector<Box *> &leaders,
+                   std::vector<char> *due = nullptr);
+int mc_recompute(Box &b);
 int64_t mixed_segment_limit(Box &b, int64_t cap);
 void mc_destroy(Box &b);
 

@@ -28,6 +28,7 @@
 #include "gb_pair.cuh"
 
 #include <cooperative_groups.h>
+#include <mutex>
 
 namespace cg = cooperative_groups;
 
@@ -660,16 +661,26 @@ size_t mixed_cold_buffer(int K, int csize) {
   return (size_t)csize * mixed_cold_bytes((K + csize - 1) / csize);
 }
 
-int launch_chain_mixed(cudaStream_t st, const MixedChain *d_chains, int nchains,
-                       int csize, size_t smem) {
-  static bool attr_done = false;
-  if (!attr_done) {
+// The kernel's attributes are set once, to the largest shared memory it ever
+// asks for: launches and occupancy queries may then come from several host
+// threads (the job server's round and set-up threads) without one changing
+// the limit under another's launch.
+static void mixed_attrs() {
+  static std::once_flag once;
+  std::call_once(once, [] {
     cudaFuncSetAttribute(k_chain_mixed,
                          cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    attr_done = true;
-  }
-  cudaFuncSetAttribute(k_chain_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem);
+    cudaFuncSetAttribute(k_chain_mixed,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)MIXED_SMEM_MAX);
+  });
+}
+
+int launch_chain_mixed(cudaStream_t st, const MixedChain *d_chains, int nchains,
+                       int csize, size_t smem) {
+  if (smem > MIXED_SMEM_MAX)
+    return ERR_UNSUPPORTED;
+  mixed_attrs();
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nchains * csize);
   cfg.blockDim = dim3(MT_THREADS);
@@ -687,10 +698,9 @@ int launch_chain_mixed(cudaStream_t st, const MixedChain *d_chains, int nchains,
 }
 
 int max_active_clusters(int csize, size_t smem) {
-  cudaFuncSetAttribute(k_chain_mixed,
-                       cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  cudaFuncSetAttribute(k_chain_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)smem);
+  if (smem > MIXED_SMEM_MAX)
+    return 0;
+  mixed_attrs();
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(csize);
   cfg.blockDim = dim3(MT_THREADS);

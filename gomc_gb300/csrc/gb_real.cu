@@ -115,9 +115,7 @@ int launch_box_inter(Box &bx, double *d_out2) {
   if (rc)
     return rc;
   size_t sh = (size_t)b.cap * (sizeof(double4_32a) + 2 * sizeof(int));
-  if (sh > 48 * 1024)
-    cudaFuncSetAttribute(k_box_inter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sh);
+  raise_smem_limit((const void *)k_box_inter, sh);
   k_box_inter<<<tiles, RT, sh, bx.stream>>>(b, bx.d_ff, bx.d_scratch);
   k_reduce_partials<<<1, RT, 0, bx.stream>>>(bx.d_scratch, tiles, 2, d_out2, 0);
   return bx.CudaCheck(cudaGetLastError(), "box inter");
@@ -506,9 +504,7 @@ int launch_box_force(Box &bx, const DevBox &b, double *aF, double *mF,
   double *fpart = bx.d_scratch;
   double *epart = fpart + (size_t)FG * b.n_atoms * 3;
   size_t sh = (size_t)b.cap * (sizeof(double4_32a) + 2 * sizeof(int));
-  if (sh > 48 * 1024)
-    cudaFuncSetAttribute(k_box_force, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sh);
+  raise_smem_limit((const void *)k_box_force, sh);
   k_box_force<<<dim3(b.ncell, FG), RT, sh, bx.stream>>>(b, bx.d_ff, fpart, epart);
   k_force_gather<<<(b.n_mol + 127) / 128, 128, 0, bx.stream>>>(b, fpart, aF,
                                                               mF);

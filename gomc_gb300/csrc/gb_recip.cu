@@ -12,17 +12,17 @@
 //
 // The full-box kernels evaluate exp(i k.r) as a product of per-axis phase
 // factors exp(i n_x t_x) exp(i n_y t_y) exp(i n_z t_z), t = 2 pi r / L, held
-// per atom in shared memory; each CTA owns a chunk of k-vectors and one
-// chunk of atoms, and chunk partials are added in a fixed order.
+// per atom in shared memory; each CTA owns a chunk of k-vectors (the
+// structure factor: runs of consecutive n_x) and one chunk of atoms, and
+// chunk partials are added in a fixed order.
 #include "gb_box.h"
 #include "gb_pair.cuh"
 
 namespace gb {
 
 constexpr int KT = 256;     // threads per reciprocal CTA
-constexpr int KPT = 2;      // k-vectors per thread
 constexpr int TA = 16;      // atoms per shared-memory tile
-constexpr int NCH_MAX = 32; // atom chunks
+constexpr int NCH_MAX = 64; // atom chunks
 
 struct Phase {
   double2 *e;  // [atoms][3][kmax + 1]
@@ -53,6 +53,9 @@ __device__ __forceinline__ double2 pick(const double2 *row, int n) {
   return v;
 }
 
+// One thread per run of up to KRUN k-vectors sharing (n_y, n_z) with
+// consecutive n_x: per atom, exp(i(n_y t_y + n_z t_z)) is formed once and
+// exp(i n_x t_x) advances along the run by multiplying with exp(i t_x).
 __global__ void __launch_bounds__(KT) k_recip_sums(DevBox b, const double *__restrict__ X,
                                                    const double *__restrict__ Y,
                                                    const double *__restrict__ Z,
@@ -60,17 +63,16 @@ __global__ void __launch_bounds__(KT) k_recip_sums(DevBox b, const double *__res
   extern __shared__ double2 tab[];
   __shared__ double qs[TA];
   int stride = b.kmax + 1;
-  int k0 = blockIdx.x * KT * KPT;
+  int run = blockIdx.x * KT + threadIdx.x;
   int ch = blockIdx.y;
   int a_begin = (int)((long long)b.n_atoms * ch / nch);
   int a_end = (int)((long long)b.n_atoms * (ch + 1) / nch);
-  char4 kn[KPT];
-  double sR[KPT], sI[KPT];
-  for (int t = 0; t < KPT; ++t) {
-    int k = k0 + t * KT + threadIdx.x;
-    kn[t] = k < b.K ? b.kn[k] : make_char4(0, 0, 0, 0);
-    sR[t] = 0.0;
-    sI[t] = 0.0;
+  int4 rn = run < b.nrun ? b.krun[run] : make_int4(0, 0, 0, 0);
+  double sR[KRUN], sI[KRUN];
+#pragma unroll
+  for (int g = 0; g < KRUN; ++g) {
+    sR[g] = 0.0;
+    sI[g] = 0.0;
   }
   double cv[3];
   for (int d = 0; d < 3; ++d) {
@@ -98,19 +100,24 @@ __global__ void __launch_bounds__(KT) k_recip_sums(DevBox b, const double *__res
       const double2 *ex = tab + (a * 3 + 0) * stride;
       const double2 *ey = tab + (a * 3 + 1) * stride;
       const double2 *ez = tab + (a * 3 + 2) * stride;
+      double2 step = ex[1];
+      double2 e = cmul(ex[rn.z], cmul(pick(ey, rn.x), pick(ez, rn.y)));
 #pragma unroll
-      for (int t = 0; t < KPT; ++t) {
-        double2 e = cmul(cmul(ex[kn[t].x], pick(ey, kn[t].y)), pick(ez, kn[t].z));
-        sR[t] += q * e.x;
-        sI[t] += q * e.y;
+      for (int g = 0; g < KRUN; ++g) {
+        sR[g] += q * e.x;
+        sI[g] += q * e.y;
+        e = cmul(e, step);
       }
     }
   }
-  for (int t = 0; t < KPT; ++t) {
-    int k = k0 + t * KT + threadIdx.x;
-    if (k < b.K) {
-      part[((size_t)ch * b.K + k) * 2] = sR[t];
-      part[((size_t)ch * b.K + k) * 2 + 1] = sI[t];
+  if (run < b.nrun) {
+#pragma unroll
+    for (int g = 0; g < KRUN; ++g) {
+      if (g < rn.w) {
+        int k = b.krun_k[(size_t)run * KRUN + g];
+        part[((size_t)ch * b.K + k) * 2] = sR[g];
+        part[((size_t)ch * b.K + k) * 2 + 1] = sI[g];
+      }
     }
   }
 }
@@ -130,7 +137,7 @@ __global__ void k_recip_chunk_sum(int K, int nch, const double *__restrict__ par
 }
 
 static int recip_chunks(const Box &bx) {
-  int kb = (bx.dev.K + KT * KPT - 1) / (KT * KPT);
+  int kb = (bx.dev.nrun + KT - 1) / KT;
   int want = (4 * bx.sm_count + kb - 1) / kb;
   int nch = std::max(1, std::min(NCH_MAX, want));
   int maxch = std::max(1, bx.dev.n_atoms / TA);
@@ -144,11 +151,9 @@ int launch_recip_sums(Box &bx, const double *x, const double *y,
   int rc = bx.EnsureScratch((size_t)nch * b.K * 2);
   if (rc)
     return rc;
-  int kb = (b.K + KT * KPT - 1) / (KT * KPT);
+  int kb = (b.nrun + KT - 1) / KT;
   size_t sh = (size_t)TA * 3 * (b.kmax + 1) * sizeof(double2) + 16;
-  if (sh > 48 * 1024)
-    cudaFuncSetAttribute(k_recip_sums, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sh);
+  raise_smem_limit((const void *)k_recip_sums, sh);
   k_recip_sums<<<dim3(kb, nch), KT, sh, bx.stream>>>(b, x, y, z, nch,
                                                      bx.d_scratch);
   k_recip_chunk_sum<<<(b.K + 255) / 256, 256, 0, bx.stream>>>(
@@ -388,9 +393,7 @@ int launch_force_recip(Box &bx, const DevBox &b, const double *sumR,
     return rc;
   int pad = 3 * (b.kmax + 1) + 1;
   size_t sh = (size_t)FA * pad * sizeof(double2) + (size_t)FK * (6 * 8 + 4);
-  if (sh > 48 * 1024)
-    cudaFuncSetAttribute(k_force_recip, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sh);
+  raise_smem_limit((const void *)k_force_recip, sh);
   dim3 grid((b.n_atoms + FA - 1) / FA, FKS);
   k_force_recip<<<grid, FA, sh, bx.stream>>>(b, bx.d_ff, sumR, sumI,
                                              bx.d_scratch);

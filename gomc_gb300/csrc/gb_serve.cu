@@ -2,19 +2,20 @@
 // simulations on one GPU, each resident in HBM from admission to completion.
 //
 // A round (Server::Round) does, in order:
-//   1. launch: every resident job runs its next segment (at most `quantum`
-//      moves, cut at its next FP64 recompute boundary).  Jobs are grouped by
+//   1. launch: every resident job runs its next segment (at most its
+//      quantum of moves, cut at its next FP64 recompute boundary).  Jobs are grouped by
 //      cluster size; each group is one kernel launch, the groups run on
 //      separate streams and overlap on the device (mixed_launch);
 //   2. admission, while those kernels run: queued jobs, first come first
-//      served, get a box (coordinates, cell grid, k-vectors, structure
-//      factors) if their estimated device memory fits the budget and their
-//      chains fit the free CTA slots; their set-up kernels run on their own
-//      streams beside the round's launches;
-//   3. completion: wait for the launches, run the recomputes that fell due
-//      (mixed_complete), record sweep completions, and retire finished jobs
-//      (final coordinates and energies copied to the host, device memory
-//      returned to the budget).
+//      served, are admitted if their estimated device memory fits the budget
+//      and their chains fit the free CTA slots;
+//   3. completion: wait for the launches and record sweep completions.
+// Building an admitted job's box (coordinates, cell grid, k-vectors,
+// structure factors, initial FP64 energies) and the periodic FP64
+// recomputes that fall due run on helper threads, on the jobs' own
+// streams, beside the rounds; a job sits out rounds meanwhile.  Finished
+// jobs are retired at the start of the next round (final coordinates and
+// energies copied to the host, device memory returned to the budget).
 // A job's segment lengths depend only on the job (its quantum, recompute
 // frequency and step count), and its cluster size only on its own size, so
 // it computes the same moves with the same arithmetic alone or in any mix.
@@ -50,7 +51,10 @@ struct Job {
   int64_t nsteps = 0, sweep = 0, done = 0;
   int status = GB_JOB_QUEUED;
   int csize = 0;
-  size_t mem = 0;  // admission estimate, then the box's actual bytes
+  int64_t quantum = 0;  // moves per round
+  size_t smem = 0;      // dynamic shared memory per CTA
+  size_t mem = 0;   // admission estimate, or the box's bytes when larger
+  bool busy = false;  // being set up or recomputed: sits out rounds
   Box *box = nullptr;
   double t_submit = 0, t_admit = 0, t_done = 0, t_last = 0;
   std::vector<double> xyz, com;
@@ -73,12 +77,14 @@ struct Server {
   size_t budget = 0, mem_used = 0;
   std::mutex mu;
   std::condition_variable cv;
-  std::deque<Job *> queue;
-  std::vector<Job *> resident;
+  std::deque<Job *> queue;     // submitted, not yet admitted
+  std::vector<Job *> resident; // admitted (being set up, running, recomputing)
+  std::deque<Job *> tasks;     // set-up and recompute work for the helper
   std::map<int64_t, Job *> jobs;
   int64_t next_id = 1;
   Clock::time_point t0;
   std::thread worker;
+  std::vector<std::thread> helpers;  // set-up / recompute threads
   bool worker_on = false, stop = false, abort = false;
   int worker_rc = OK;
   std::string last_error;
@@ -86,6 +92,7 @@ struct Server {
   std::vector<double> sweep_lat;  // seconds
   int64_t moves = 0, rounds = 0, resident_sum = 0;
   double t_first = -1, t_last_done = 0;
+  double helper_s = 0, round_s = 0;  // time in set-up / recompute, in rounds
 
   double Now() const {
     return std::chrono::duration<double>(Clock::now() - t0).count();
@@ -95,8 +102,13 @@ struct Server {
     last_error = m;
     return code;
   }
-  int Round(int32_t *pending);
+  int Round(int32_t *pending, bool *worked);
+  int Admit();
+  void RunTask(Job *j);
+  void RunTasksInline();
+  void Retire(Job *j);
   void Worker();
+  void Helper();
 };
 
 namespace {
@@ -110,6 +122,17 @@ int job_cluster(const Job &j, int K) {
     if ((K + c - 1) / c <= 2048)
       return c;
   return 16;
+}
+
+// Moves per round of a job: `quantum` scaled by 4,096 over the k-vectors
+// each of its CTAs evaluates per move (the bulk of a move's time), within
+// [quantum / 4, 8 quantum], so small and large jobs spend about the same time
+// per round.  Depends on the job alone.
+int64_t job_quantum(int quantum, int K, int csize) {
+  int64_t per_cta = std::max(K / std::max(csize, 1), 256);
+  int64_t q = (int64_t)quantum * 4096 / per_cta;
+  return std::min<int64_t>(std::max<int64_t>(q, std::max(quantum / 4, 1)),
+                           8 * (int64_t)quantum);
 }
 
 // k-vector count and largest |n| of a box, from the set-up rules of
@@ -217,32 +240,17 @@ size_t job_estimate(const Job &j, int quantum, int *csize_out) {
   int csize = job_cluster(j, K);
   if (csize_out)
     *csize_out = csize;
-  return job_bytes(j, K, kmax, csize, (size_t)quantum);
+  return job_bytes(j, K, kmax, csize,
+                   (size_t)job_quantum(quantum, K, csize));
 }
 
 }  // namespace
 
-// One scheduling round (see the top of this file).  *pending = jobs queued or
-// resident afterwards.
-int Server::Round(int32_t *pending) {
-  int rc;
-  // 1. launch the resident jobs' segments
-  std::vector<Box *> boxes;
-  std::vector<int64_t> n;
-  std::vector<Job *> live;
-  for (Job *j : resident) {
-    int64_t m = mixed_segment_limit(*j->box, std::min<int64_t>(
-                                                 cfg.quantum, j->nsteps - j->done));
-    boxes.push_back(j->box);
-    n.push_back(m);
-    live.push_back(j);
-  }
-  std::vector<Box *> leaders;
-  double t_start = Now();
-  if (!boxes.empty() && (rc = mixed_launch(boxes, n, &leaders)))
-    return Fail(rc, "launch: " + boxes[0]->last_error);
-
-  // 2. admission while the round runs
+// Admission (first come first served): reserve the job's estimated device
+// memory and CTA slots, mark it resident and busy, and queue its set-up for
+// the helpers.  Returns how many jobs were admitted.
+int Server::Admit() {
+  int admitted = 0;
   for (;;) {
     Job *j = nullptr;
     {
@@ -256,23 +264,25 @@ int Server::Round(int32_t *pending) {
     int csize = job_cluster(*j, K);
     bool cold_smem = mixed_smem(K, kmax, csize, true) <= MIXED_SMEM_MAX;
     size_t smem = mixed_smem(K, kmax, csize, cold_smem);
-    size_t est = job_bytes(*j, K, kmax, csize, (size_t)cfg.quantum);
+    size_t est =
+      job_bytes(*j, K, kmax, csize, (size_t)job_quantum(cfg.quantum, K, csize));
+    std::lock_guard<std::mutex> g(mu);
     // CTA slots: shared memory and two CTAs per SM by registers
     size_t used_smem = 0;
     int used_ctas = 0;
     for (Job *r : resident) {
-      used_smem += (size_t)r->csize * (r->box->mc->mixed_smem + 1024);
+      used_smem += (size_t)r->csize * (r->smem + 1024);
       used_ctas += r->csize;
     }
     bool fits_mem = mem_used + est <= budget;
     bool fits_slots =
         used_smem + (size_t)csize * (smem + 1024) <= slots.smem_per_sm * slots.sms &&
         used_ctas + csize <= 2 * slots.sms;
-    bool fits_count = cfg.max_resident <= 0 || (int)resident.size() < cfg.max_resident;
+    bool fits_count =
+        cfg.max_resident <= 0 || (int)resident.size() < cfg.max_resident;
     if (!(fits_mem && fits_slots && fits_count)) {
       if (resident.empty() && est > budget) {
         // can never fit: fail it rather than block the queue
-        std::lock_guard<std::mutex> g(mu);
         queue.pop_front();
         j->status = GB_JOB_FAILED;
         j->msg = "job needs more device memory than the server's budget";
@@ -280,45 +290,160 @@ int Server::Round(int32_t *pending) {
       }
       break;
     }
-    {
-      std::lock_guard<std::mutex> g(mu);
-      queue.pop_front();
-    }
+    queue.pop_front();
+    j->csize = csize;
+    j->quantum = job_quantum(cfg.quantum, K, csize);
+    j->smem = smem;
+    j->mem = est;
+    j->busy = true;
+    mem_used += est;
+    resident.push_back(j);
+    tasks.push_back(j);
+    admitted++;
+  }
+  if (admitted)
+    cv.notify_all();
+  return admitted;
+}
+
+// Set-up of an admitted job (its box: coordinates, cell grid, k-vectors,
+// structure factors and the initial FP64 energies) or its periodic FP64
+// recompute; runs on a helper thread beside the rounds.
+void Server::RunTask(Job *j) {
+  int rc;
+  std::string err;
+  double t0 = Now();
+  if (!j->box) {
     Box *b = nullptr;
-    std::string err;
     gb_mc_params p = j->mc;
-    p.cluster_size = csize;
-    p.move_buffer = cfg.quantum;
+    p.cluster_size = j->csize;
+    p.move_buffer = (int32_t)j->quantum;
     rc = Box::Create(j->host, j->cfg, &b, &err);
-    if (!rc) {
-      rc = mc_init(*b, p);
-      if (rc)
-        err = b->last_error;
-    }
+    if (!rc && (rc = mc_init(*b, p)))
+      err = b->last_error;
     std::lock_guard<std::mutex> g(mu);
     if (rc) {
-      delete b;
+      if (b) {
+        mc_destroy(*b);
+        delete b;
+      }
       j->status = GB_JOB_FAILED;
       j->msg = err;
-      continue;
+      mem_used -= j->mem;
+      resident.erase(std::find(resident.begin(), resident.end(), j));
+    } else {
+      j->box = b;
+      size_t actual = b->dev_bytes + b->mc->bytes;
+      if (actual > j->mem) {
+        mem_used += actual - j->mem;
+        j->mem = actual;
+      }
+      j->smem = b->mc->mixed_smem;
+      j->status = GB_JOB_RUNNING;
+      j->t_admit = j->t_last = Now();
+      if (t_first < 0)
+        t_first = j->t_admit;
+      j->busy = false;
     }
-    j->box = b;
-    j->csize = b->mc->cluster;
-    j->mem = std::max(est, b->dev_bytes + b->mc->bytes);
-    mem_used += j->mem;
-    j->status = GB_JOB_RUNNING;
-    j->t_admit = j->t_last = Now();
-    if (t_first < 0)
-      t_first = j->t_admit;
-    resident.push_back(j);
+    helper_s += Now() - t0;
+    cv.notify_all();
+    return;
+  } else {
+    rc = mc_recompute(*j->box);
+    if (rc)
+      err = j->box->last_error;
+    std::lock_guard<std::mutex> g(mu);
+    if (rc) {
+      j->status = GB_JOB_FAILED;
+      j->msg = err;
+      j->done = j->nsteps;  // retired by the next round
+    }
+    j->busy = false;
   }
+  helper_s += Now() - t0;
+  cv.notify_all();
+}
 
-  // 3. completion
+void Server::RunTasksInline() {
+  for (;;) {
+    Job *j = nullptr;
+    {
+      std::lock_guard<std::mutex> g(mu);
+      if (tasks.empty())
+        return;
+      j = tasks.front();
+      tasks.pop_front();
+    }
+    RunTask(j);
+  }
+}
+
+// A finished job: final coordinates and running energies to the host, device
+// memory back to the budget.
+void Server::Retire(Job *j) {
+  j->xyz.resize(3 * (size_t)j->host.n_atoms);
+  j->com.resize(3 * (size_t)j->host.n_mol);
+  int rc = OK;
+  if (j->status != GB_JOB_FAILED) {
+    rc = j->box->GetCoords(j->xyz.data(), j->com.data());
+    if (!rc)
+      rc = j->box->GetEnergy(j->e5);
+  }
+  std::string err = rc ? j->box->last_error : std::string();
+  mc_destroy(*j->box);
+  delete j->box;
+  std::lock_guard<std::mutex> g(mu);
+  j->box = nullptr;
+  mem_used -= j->mem;
+  j->t_done = Now();
+  t_last_done = j->t_done;
+  if (j->status != GB_JOB_FAILED) {
+    j->status = rc ? GB_JOB_FAILED : GB_JOB_DONE;
+    j->msg = err;
+  }
+  resident.erase(std::find(resident.begin(), resident.end(), j));
+  cv.notify_all();
+}
+
+// One scheduling round (see the top of this file).  *pending = jobs queued or
+// resident afterwards; *worked = whether anything was launched or admitted.
+int Server::Round(int32_t *pending, bool *worked) {
+  int rc;
+  bool inline_tasks;
+  std::vector<Job *> live, finished;
+  {
+    std::lock_guard<std::mutex> g(mu);
+    inline_tasks = helpers.empty();
+    for (Job *j : resident)
+      if (!j->busy)
+        (j->done >= j->nsteps ? finished : live).push_back(j);
+  }
+  for (Job *j : finished)
+    Retire(j);
+  // 1. launch the segments of the jobs that are ready
+  std::vector<Box *> boxes;
+  std::vector<int64_t> n;
+  for (Job *j : live) {
+    boxes.push_back(j->box);
+    n.push_back(mixed_segment_limit(
+        *j->box, std::min<int64_t>(j->quantum, j->nsteps - j->done)));
+  }
+  std::vector<Box *> leaders;
+  double t_start = Now();
+  if (!boxes.empty() && (rc = mixed_launch(boxes, n, &leaders)))
+    return Fail(rc, "launch: " + boxes[0]->last_error);
+  // 2. admission while they run
+  int admitted = Admit();
+  if (inline_tasks)
+    RunTasksInline();
+  // 3. completion; due recomputes go to the helpers
   if (!boxes.empty()) {
-    if ((rc = mixed_complete(boxes, n, leaders)))
+    std::vector<char> due;
+    if ((rc = mixed_complete(boxes, n, leaders, &due)))
       return Fail(rc, "round: " + boxes[0]->last_error);
     double t_end = Now();
     std::lock_guard<std::mutex> g(mu);
+    round_s += t_end - t_start;
     rounds++;
     resident_sum += (int64_t)live.size();
     for (size_t i = 0; i < live.size(); ++i) {
@@ -333,38 +458,20 @@ int Server::Round(int32_t *pending) {
       }
       j->done = after;
       moves += n[i];
+      if (due[i]) {
+        j->busy = true;
+        tasks.push_back(j);
+      }
     }
+    cv.notify_all();
   }
-  if (!boxes.empty()) {
-    std::vector<Job *> finished;
-    {
-      std::lock_guard<std::mutex> g(mu);
-      for (Job *j : live)
-        if (j->done >= j->nsteps)
-          finished.push_back(j);
-    }
-    for (Job *j : finished) {
-      j->xyz.resize(3 * (size_t)j->host.n_atoms);
-      j->com.resize(3 * (size_t)j->host.n_mol);
-      rc = j->box->GetCoords(j->xyz.data(), j->com.data());
-      if (!rc)
-        rc = j->box->GetEnergy(j->e5);
-      std::string err = rc ? j->box->last_error : std::string();
-      mc_destroy(*j->box);
-      delete j->box;
-      std::lock_guard<std::mutex> g(mu);
-      j->box = nullptr;
-      mem_used -= j->mem;
-      j->t_done = Now();
-      t_last_done = j->t_done;
-      j->status = rc ? GB_JOB_FAILED : GB_JOB_DONE;
-      j->msg = err;
-      resident.erase(std::find(resident.begin(), resident.end(), j));
-    }
-  }
+  if (inline_tasks)
+    RunTasksInline();
   std::lock_guard<std::mutex> g(mu);
   if (pending)
     *pending = (int32_t)(queue.size() + resident.size());
+  if (worked)
+    *worked = !boxes.empty() || admitted > 0 || !finished.empty();
   cv.notify_all();
   return OK;
 }
@@ -374,21 +481,37 @@ void Server::Worker() {
   for (;;) {
     {
       std::unique_lock<std::mutex> lk(mu);
-      cv.wait(lk, [&] {
-        return abort || stop || !queue.empty() || !resident.empty();
-      });
       if (abort || (stop && queue.empty() && resident.empty()))
         return;
     }
     int32_t pending = 0;
-    int rc = Round(&pending);
+    bool worked = false;
+    int rc = Round(&pending, &worked);
+    std::unique_lock<std::mutex> lk(mu);
     if (rc) {
-      std::lock_guard<std::mutex> g(mu);
       worker_rc = rc;
-      stop = true;
+      abort = true;
       cv.notify_all();
       return;
     }
+    if (!worked)  // everything resident is being set up or recomputed
+      cv.wait_for(lk, std::chrono::milliseconds(2));
+  }
+}
+
+void Server::Helper() {
+  cudaSetDevice(cfg.device);
+  for (;;) {
+    Job *j = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      cv.wait(lk, [&] { return abort || !tasks.empty() || !worker_on; });
+      if (abort || (tasks.empty() && !worker_on))
+        return;
+      j = tasks.front();
+      tasks.pop_front();
+    }
+    RunTask(j);
   }
 }
 
@@ -467,15 +590,17 @@ void gb_server_destroy(gb_server *srv) {
     s.queue.clear();
   }
   s.cv.notify_all();
-  // a running round finishes; resident jobs are dropped after it
-  if (s.worker.joinable()) {
-    {
-      std::lock_guard<std::mutex> g(s.mu);
-      s.abort = true;
-    }
-    s.cv.notify_all();
-    s.worker.join();
+  // a running round or task finishes; resident jobs are dropped after it
+  {
+    std::lock_guard<std::mutex> g(s.mu);
+    s.abort = true;
   }
+  s.cv.notify_all();
+  if (s.worker.joinable())
+    s.worker.join();
+  for (auto &h : s.helpers)
+    h.join();
+  s.helpers.clear();
   for (auto &kv : s.jobs) {
     gb::Job *j = kv.second;
     if (j->box) {
@@ -540,7 +665,7 @@ int gb_server_step(gb_server *srv, int32_t *pending) {
       return gb::ERR_STATE;
   }
   cudaSetDevice(s.cfg.device);
-  return s.Round(pending);
+  return s.Round(pending, nullptr);
 }
 
 int gb_server_start(gb_server *srv) {
@@ -553,6 +678,10 @@ int gb_server_start(gb_server *srv) {
   s.worker_on = true;
   s.stop = false;
   s.worker = std::thread([&s] { s.Worker(); });
+  // two helpers: a small job's set-up leaves most of the GPU idle, so two
+  // overlap; more only contend for the FP64 units
+  for (int i = 0; i < 2; ++i)
+    s.helpers.emplace_back([&s] { s.Helper(); });
   return gb::OK;
 }
 
@@ -565,7 +694,7 @@ int gb_server_drain(gb_server *srv, double timeout_s) {
     if (!s.worker_on)
       return gb::ERR_STATE;
     auto done = [&] {
-      return (s.queue.empty() && s.resident.empty()) || s.worker_rc != gb::OK;
+      return (s.queue.empty() && s.resident.empty()) || s.abort;
     };
     if (timeout_s > 0) {
       if (!s.cv.wait_for(lk, std::chrono::duration<double>(timeout_s), done))
@@ -577,8 +706,15 @@ int gb_server_drain(gb_server *srv, double timeout_s) {
   }
   s.cv.notify_all();
   s.worker.join();
+  {
+    std::lock_guard<std::mutex> g(s.mu);
+    s.worker_on = false;  // the helpers return once the queue is empty
+  }
+  s.cv.notify_all();
+  for (auto &h : s.helpers)
+    h.join();
+  s.helpers.clear();
   std::lock_guard<std::mutex> g(s.mu);
-  s.worker_on = false;
   return s.worker_rc;
 }
 
@@ -625,9 +761,10 @@ int gb_server_result(gb_server *srv, int64_t job, double *xyz, double *com,
   return gb::OK;
 }
 
-int gb_server_stats(gb_server *srv, double *out10) {
-  if (!srv || !out10)
+int gb_server_stats(gb_server *srv, double *out12) {
+  if (!srv || !out12)
     return gb::ERR_ARG;
+  double *out10 = out12;
   gb::Server &s = srv->s;
   std::lock_guard<std::mutex> g(s.mu);
   std::vector<double> lat = s.sweep_lat, jl;
@@ -655,6 +792,8 @@ int gb_server_stats(gb_server *srv, double *out10) {
   out10[7] = pct(jl, 0.99);
   out10[8] = (double)s.rounds;
   out10[9] = s.rounds ? (double)s.resident_sum / (double)s.rounds : 0.0;
+  out12[10] = s.helper_s;
+  out12[11] = s.round_s;
   return gb::OK;
 }
 

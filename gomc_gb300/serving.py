@@ -21,7 +21,7 @@ STATUS_NAMES = {QUEUED: "queued", RUNNING: "running", DONE: "done",
                 FAILED: "failed"}
 STATS_KEYS = ["jobs_done", "moves", "wall_s", "moves_per_s",
               "sweep_p50_ms", "sweep_p99_ms", "job_p50_s", "job_p99_s",
-              "rounds", "mean_resident"]
+              "rounds", "mean_resident", "helper_busy_s", "round_busy_s"]
 
 
 class Server:
@@ -130,7 +130,7 @@ class Server:
         return dict(xyz=xyz, com=com, energy=e)
 
     def stats(self) -> dict:
-        o = np.zeros(10)
+        o = np.zeros(12)
         self._chk(lib().gb_server_stats(self.h,
                                         o.ctypes.data_as(C.POINTER(C.c_double))))
         return dict(zip(STATS_KEYS, o.tolist()))

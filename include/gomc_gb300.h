@@ -230,7 +230,10 @@ enum gb_job_status {
 };
 typedef struct gb_server_config {
   int32_t device;
-  int32_t quantum;       /* moves per job per round (0 = 1000) */
+  int32_t quantum;       /* moves per round of a job with 4,096 k-vectors per
+                            CTA (0 = 1000); a job's own quantum scales
+                            inversely with its k-vectors per CTA, within
+                            [quantum/4, 8 quantum] */
   int64_t mem_budget;    /* device bytes for job state (0 = 90% of free) */
   int32_t max_resident;  /* at most this many resident jobs (0 = no cap) */
 } gb_server_config;
@@ -265,11 +268,13 @@ int gb_server_job(gb_server *srv, int64_t job, int32_t *status,
  * energies (inter, real, recip, self, correction) of a finished job. */
 int gb_server_result(gb_server *srv, int64_t job, double *xyz, double *com,
                      double *energy5);
-/* out10: jobs done, moves run, wall seconds from the first admission to the
+/* out12: jobs done, moves run, wall seconds from the first admission to the
  * last completion, moves/s over that span, per-sweep latency p50 and p99
  * (ms), job latency (submission to completion) p50 and p99 (s), rounds, mean
- * resident jobs per round. */
-int gb_server_stats(gb_server *srv, double *out10);
+ * resident jobs per round, helper-thread seconds (summed over the helper
+ * threads) spent on set-ups and FP64 recomputes, seconds spent in rounds
+ * (launch to completion). */
+int gb_server_stats(gb_server *srv, double *out12);
 const char *gb_server_error(const gb_server *srv);
 
 /* ---- Reciprocal energy without device allocation ----
