@@ -724,6 +724,42 @@ int Box::MoleculeInter(int m, const double *new_pos, double *lj, double *real,
   return CheckError();
 }
 
+// CalculateEnergy::VirialCalc (src/CalculateEnergy.cpp:411-579, LRC off)
+// with Ewald::VirialReciprocal (src/Ewald.cpp:1168-1305): inter, real,
+// recip, total, then the diagonals of interTens, realTens, recipTens,
+// totalTens (the reference computes no off-diagonal components).
+int Box::VirialCalc(double out[16]) {
+  int rc;
+  if ((rc = launch_box_virial(*this, d_small)))
+    return rc;
+  if (cfg.ewald && (rc = launch_virial_recip(*this, d_small + 8)))
+    return rc;
+  if ((rc = CudaCheck(cudaMemcpyAsync(h_pinned, d_small, 14 * 8,
+                                      cudaMemcpyDeviceToHost, stream),
+                      "download")) ||
+      (rc = Sync()))
+    return rc;
+  double vt[3], rt[3], wt[3];
+  for (int d = 0; d < 3; ++d) {
+    vt[d] = h_pinned[d];
+    rt[d] = cfg.electrostatic ? h_pinned[3 + d] * QQ_FACT : 0.0;
+    wt[d] = cfg.ewald ? h_pinned[8 + d] + h_pinned[11 + d] : 0.0;
+  }
+  out[0] = vt[0] + vt[1] + vt[2];
+  out[1] = cfg.electrostatic
+               ? (h_pinned[3] + h_pinned[4] + h_pinned[5]) * QQ_FACT
+               : 0.0;
+  out[2] = wt[0] + wt[1] + wt[2];
+  out[3] = out[0] + out[1] + out[2];
+  for (int d = 0; d < 3; ++d) {
+    out[4 + d] = vt[d];
+    out[7 + d] = rt[d];
+    out[10 + d] = wt[d];
+    out[13 + d] = vt[d] + rt[d] + wt[d];
+  }
+  return CheckError();
+}
+
 // CalculateEnergy::SingleMoleculeInter (src/CalculateEnergy.cpp:1494-1556)
 int Box::SingleMoleculeInter(int m, const double lam[4], double out[4]) {
   if (m < 0 || m >= dev.n_mol)

@@ -38,6 +38,7 @@ class Box {
   int MoleculeInter(int m, const double *new_pos, double *lj, double *real,
                     int *overlap);
   int SingleMoleculeInter(int m, const double lam[4], double out[4]);
+  int VirialCalc(double out16[16]);              // CalculateEnergy::VirialCalc
   int ParticleInter(int m, int kind, double charge, const double *trials,
                     int ntrials, double *en, double *real, int *overlap);
   int MolReciprocal(int m, const double *new_pos, double *de);
@@ -116,6 +117,8 @@ void recip_vectors(const double L[3], double volume, double alphaSq,
 // the MultiParticle move evaluate its trial state in separate buffers.
 int launch_grid_all(Box &b, const DevBox &d);
 int launch_box_inter(Box &b, double *d_out2);
+int launch_box_virial(Box &b, double *d_out6);
+int launch_virial_recip(Box &b, double *d_out6);
 int launch_recip_sums(Box &b, const double *x, const double *y,
                       const double *z, double *sumR, double *sumI);
 int launch_recip_energy(Box &b, const double *sumR, const double *sumI,

@@ -138,6 +138,12 @@ int gb_molecule_inter(gb_box *box, int32_t mol, const double *new_pos,
   *overlap = ov;
   return rc;
 }
+int gb_virial(gb_box *box, double *out16) {
+  if (!out16)
+    return gb::ERR_ARG;
+  BOX_CALL(VirialCalc(out16));
+}
+
 int gb_single_molecule_inter(gb_box *box, int32_t mol, const double *lambdas4,
                              double *out4) {
   int rc = guard(box);

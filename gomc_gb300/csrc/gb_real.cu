@@ -108,6 +108,87 @@ __global__ void __launch_bounds__(RT) k_box_inter(DevBox b, const FF *__restrict
   }
 }
 
+// ---------------------------------------------------------------------------
+// Pair virial (CalculateEnergy::VirialCalc CPU branch,
+// src/CalculateEnergy.cpp:458-519): the BoxInter tiles, each pair's force
+// factor times the product of its atom separation and the molecule-centre
+// separation, diagonal components; partials = LJ xx, yy, zz, then the
+// Coulomb factor (q_i q_j, without qqFact) xx, yy, zz.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(RT) k_box_virial(DevBox b, const FF *__restrict__ pff,
+                                                   double *part) {
+  extern __shared__ __align__(32) unsigned char smem[];
+  const FF &ff = *pff;
+  int tile = blockIdx.x;
+  int c = tile / NB27, n = tile % NB27;
+  int c2 = b.nbr[c * NB27 + n];
+  int n1 = b.cell_count[c], n2 = b.cell_count[c2];
+  double4_32a *sp = (double4_32a *)smem;
+  int *sm = (int *)(sp + b.cap);
+  int *sa = sm + b.cap;
+  for (int j = threadIdx.x; j < n2; j += RT) {
+    size_t s = (size_t)c2 * b.cap + j;
+    sp[j] = b.cell_pos[s];
+    sm[j] = b.cell_meta[s];
+    sa[j] = b.cell_atom[s];
+  }
+  __syncthreads();
+  double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int i = threadIdx.x; i < n1; i += RT) {
+    size_t si = (size_t)c * b.cap + i;
+    double4_32a pi = b.cell_pos[si];
+    int mi = b.cell_meta[si], ai = b.cell_atom[si];
+    int moli = meta_mol(mi), ki = meta_kind(mi);
+    for (int j = 0; j < n2; ++j) {
+      int aj = sa[j];
+      int mj = sm[j];
+      int molj = meta_mol(mj);
+      if (!(ai < aj && moli != molj))
+        continue;
+      double4_32a pj = sp[j];
+      double vc[3] = {min_image(pi.x - pj.x, b.L[0], b.half[0]),
+                      min_image(pi.y - pj.y, b.L[1], b.half[1]),
+                      min_image(pi.z - pj.z, b.L[2], b.half[2])};
+      double distSq = dsq3(vc[0], vc[1], vc[2]);
+      if (!(ff.rcutSq > distSq))
+        continue;
+      double cc[3] = {min_image(b.cx[moli] - b.cx[molj], b.L[0], b.half[0]),
+                      min_image(b.cy[moli] - b.cy[molj], b.L[1], b.half[1]),
+                      min_image(b.cz[moli] - b.cz[molj], b.L[2], b.half[2])};
+      if (ff.electrostatic) {
+        double qi_qj = pi.w * pj.w;
+        if (qi_qj != 0.0) {
+          double pRF = coulomb_virial(ff, distSq, qi_qj);
+          for (int d = 0; d < 3; ++d)
+            v[3 + d] += pRF * (vc[d] * cc[d]);
+        }
+      }
+      double pVF = lj_virial(ff, distSq, ki + meta_kind(mj) * ff.n_kinds);
+      for (int d = 0; d < 3; ++d)
+        v[d] += pVF * (vc[d] * cc[d]);
+    }
+  }
+  __shared__ double red[RT / 32];
+  for (int d = 0; d < 6; ++d) {
+    double r = block_sum<RT>(v[d], red);
+    if (threadIdx.x == 0)
+      part[6 * tile + d] = r;
+  }
+}
+
+int launch_box_virial(Box &bx, double *d_out6) {
+  DevBox &b = bx.dev;
+  int tiles = b.ncell * NB27;
+  int rc = bx.EnsureScratch((size_t)tiles * 6);
+  if (rc)
+    return rc;
+  size_t sh = (size_t)b.cap * (sizeof(double4_32a) + 2 * sizeof(int));
+  raise_smem_limit((const void *)k_box_virial, sh);
+  k_box_virial<<<tiles, RT, sh, bx.stream>>>(b, bx.d_ff, bx.d_scratch);
+  k_reduce_partials<<<1, RT, 0, bx.stream>>>(bx.d_scratch, tiles, 6, d_out6, 0);
+  return bx.CudaCheck(cudaGetLastError(), "box virial");
+}
+
 int launch_box_inter(Box &bx, double *d_out2) {
   DevBox &b = bx.dev;
   int tiles = b.ncell * NB27;

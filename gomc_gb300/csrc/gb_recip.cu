@@ -275,7 +275,7 @@ constexpr int FKS = 4;      // k splits
 __global__ void __launch_bounds__(FA) k_force_recip(DevBox b, const FF *__restrict__ pff,
                                                     const double *__restrict__ sR,
                                                     const double *__restrict__ sI,
-                                                    double *fpart) {
+                                                    int intra, double *fpart) {
   extern __shared__ double2 tab[];
   const FF &ff = *pff;
   int stride = b.kmax + 1;
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(FA) k_force_recip(DevBox b, const FF *__restri
     phase_row(my, cv[0] * b.x[a], b.kmax);
     phase_row(my + stride, cv[1] * b.y[a], b.kmax);
     phase_row(my + 2 * stride, cv[2] * b.z[a], b.kmax);
-    if (blockIdx.y == 0 && fabs(q) >= 0.000000001 && ff.ewald) {
+    if (intra && blockIdx.y == 0 && fabs(q) >= 0.000000001 && ff.ewald) {
       // intramolecular correction (src/Ewald.cpp:1556-1575)
       double constValue = ff.alpha * M_2_SQRTPI;
       int m = b.mol[a];
@@ -395,11 +395,106 @@ int launch_force_recip(Box &bx, const DevBox &b, const double *sumR,
   size_t sh = (size_t)FA * pad * sizeof(double2) + (size_t)FK * (6 * 8 + 4);
   raise_smem_limit((const void *)k_force_recip, sh);
   dim3 grid((b.n_atoms + FA - 1) / FA, FKS);
-  k_force_recip<<<grid, FA, sh, bx.stream>>>(b, bx.d_ff, sumR, sumI,
+  k_force_recip<<<grid, FA, sh, bx.stream>>>(b, bx.d_ff, sumR, sumI, 1,
                                              bx.d_scratch);
   k_force_recip_gather<<<(b.n_mol + 127) / 128, 128, 0, bx.stream>>>(
       b, bx.d_scratch, aR, mR);
   return bx.CudaCheck(cudaGetLastError(), "force recip");
+}
+
+}  // namespace gb
+
+namespace gb {
+
+// ---------------------------------------------------------------------------
+// Reciprocal virial (Ewald::VirialReciprocal, src/Ewald.cpp:1168-1305) from
+// the Ref structure factors: the k-space sum, one thread per k-vector,
+//   w_d += prefact |S|^2 (1 - 2 (1/(4 alpha^2) + 1/k^2) k_d^2),
+// and the intramolecular part, one thread per atom,
+//   w_d += -F_d (r_d - com_d),
+// F the reciprocal force of the atom without the intramolecular correction
+// (k_force_recip with intra = 0): sum_k 2 q prefact (S_I cos - S_R sin) k_d
+// is -F_d.  Partials per CTA, three per row.
+// ---------------------------------------------------------------------------
+constexpr int VT = 256;
+__global__ void k_virial_k(DevBox b, const FF *__restrict__ pff,
+                           double *part) {
+  const FF &ff = *pff;
+  int k = blockIdx.x * VT + threadIdx.x;
+  double w[3] = {0.0, 0.0, 0.0};
+  if (k < b.K) {
+    double constVal = 1.0 / (4.0 * ff.alphaSq);
+    double factor = b.prefact[k] * (b.sumRref[k] * b.sumRref[k] +
+                                    b.sumIref[k] * b.sumIref[k]);
+    double c = 2.0 * (constVal + 1.0 / b.hsqr[k]);
+    double kv[3] = {b.kx[k], b.ky[k], b.kz[k]};
+    for (int d = 0; d < 3; ++d)
+      w[d] = factor * (1.0 - c * kv[d] * kv[d]);
+  }
+  __shared__ double red[VT / 32];
+  for (int d = 0; d < 3; ++d) {
+    double r = block_sum<VT>(w[d], red);
+    if (threadIdx.x == 0)
+      part[3 * blockIdx.x + d] = r;
+  }
+}
+
+__global__ void k_virial_intra(DevBox b, const double *__restrict__ fpart,
+                               int nchunk, double *part) {
+  int a = blockIdx.x * VT + threadIdx.x;
+  double w[3] = {0.0, 0.0, 0.0};
+  if (a < b.n_atoms && fabs(b.q[a]) >= 0.000000001) {
+    int m = b.mol[a];
+    double com[3] = {b.cx[m], b.cy[m], b.cz[m]};
+    double pos[3] = {b.x[a], b.y[a], b.z[a]};
+    for (int d = 0; d < 3; ++d) {
+      double F = 0.0;
+      for (int c = 0; c < nchunk; ++c)
+        F += fpart[((size_t)c * b.n_atoms + a) * 3 + d];
+      double diff = unwrap1(pos[d], com[d], b.L[d], b.half[d]) - com[d];
+      w[d] = -F * diff;
+    }
+  }
+  __shared__ double red[VT / 32];
+  for (int d = 0; d < 3; ++d) {
+    double r = block_sum<VT>(w[d], red);
+    if (threadIdx.x == 0)
+      part[3 * blockIdx.x + d] = r;
+  }
+}
+
+__global__ void k_sum3(const double *__restrict__ part, int n, double *out) {
+  __shared__ double red[VT / 32];
+  for (int d = 0; d < 3; ++d) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += VT)
+      v += part[3 * i + d];
+    double r = block_sum<VT>(v, red);
+    if (threadIdx.x == 0)
+      out[d] = r;
+  }
+}
+
+// d_out6: k-space sum (xx, yy, zz), then the intramolecular part
+int launch_virial_recip(Box &bx, double *d_out6) {
+  DevBox &b = bx.dev;
+  int nkb = (b.K + VT - 1) / VT, nab = (b.n_atoms + VT - 1) / VT;
+  size_t fp = (size_t)FKS * b.n_atoms * 3;
+  int rc = bx.EnsureScratch(fp + 3 * (size_t)(nkb + nab));
+  if (rc)
+    return rc;
+  double *kpart = bx.d_scratch + fp, *ipart = kpart + 3 * (size_t)nkb;
+  int pad = 3 * (b.kmax + 1) + 1;
+  size_t sh = (size_t)FA * pad * sizeof(double2) + (size_t)FK * (6 * 8 + 4);
+  raise_smem_limit((const void *)k_force_recip, sh);
+  dim3 grid((b.n_atoms + FA - 1) / FA, FKS);
+  k_force_recip<<<grid, FA, sh, bx.stream>>>(b, bx.d_ff, b.sumRref, b.sumIref,
+                                             0, bx.d_scratch);
+  k_virial_k<<<nkb, VT, 0, bx.stream>>>(b, bx.d_ff, kpart);
+  k_virial_intra<<<nab, VT, 0, bx.stream>>>(b, bx.d_scratch, FKS, ipart);
+  k_sum3<<<1, VT, 0, bx.stream>>>(kpart, nkb, d_out6);
+  k_sum3<<<1, VT, 0, bx.stream>>>(ipart, nab, d_out6 + 3);
+  return bx.CudaCheck(cudaGetLastError(), "virial recip");
 }
 
 }  // namespace gb

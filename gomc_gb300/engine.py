@@ -156,6 +156,21 @@ class Box:
                                           C.byref(b), C.byref(o)))
         return bool(o.value), a.value, b.value
 
+    def virial(self) -> np.ndarray:
+        """VirialCalc: inter, real, recip, total (K), then the xx/yy/zz
+        diagonals of interTens, realTens, recipTens, totalTens."""
+        out = np.empty(16)
+        self._chk(lib().gb_virial(self.h, _dp(out)))
+        return out
+
+    def pressure(self) -> float:
+        """Pressure in bar from the virial and the ideal-gas term
+        (OutputVars::CalcAndConvert, src/OutputVars.cpp:129-180)."""
+        v = self.virial()
+        vol = float(np.prod(self.sysm.box))
+        return 138.0649 * (self.n_mol * self.cfg.temperature +
+                           v[3] / 3.0) / vol
+
     def single_molecule_inter(self, m: int, lambdas):
         """(old inter, old real, new inter, new real) of molecule m at
         lambdas = (old VDW, new VDW, old Coulomb, new Coulomb)."""
@@ -398,6 +413,9 @@ class CalculateEnergy:
 
     def BoxForce(self):
         return self.box.box_force()
+
+    def VirialCalc(self):
+        return self.box.virial()
 
     def CalculateTorque(self):
         return self.box.calculate_torque()

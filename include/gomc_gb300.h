@@ -89,6 +89,13 @@ int gb_box_inter(gb_box *box, double *inter, double *real);
  * molecule `mol` from its current position to new_pos[n_atoms_of_mol * 3]. */
 int gb_molecule_inter(gb_box *box, int32_t mol, const double *new_pos,
                       double *lj, double *real, int32_t *overlap);
+/* VirialCalc (src/CalculateEnergy.cpp:411-579) with Ewald::VirialReciprocal
+ * (src/Ewald.cpp:1168-1305), long-range correction off: out16 = inter,
+ * real, recip, total virial (K), then the xx, yy, zz diagonals of
+ * interTens, realTens, recipTens, totalTens (the reference computes no
+ * off-diagonal components).  Pressure (bar) = 138.0649 (N_mol T + total/3)
+ * / V (OutputVars::CalcAndConvert, src/OutputVars.cpp:129-180). */
+int gb_virial(gb_box *box, double *out16);
 /* SingleMoleculeInter (src/CalculateEnergy.cpp:1494-1556): real-space
  * energy of molecule `mol` at its current position with its neighbourhood,
  * at two coupling pairs.  lambdas4 = old VDW, new VDW, old Coulomb, new

@@ -488,6 +488,114 @@ static void box_pairs(ora_sys *s, const double *X, const double *Y,
   *outReal = tempREn;
 }
 
+/* CalculateEnergy::VirialCalc, src/CalculateEnergy.cpp:411-579 (CPU
+ * branch :458-519; LRC off) with Ewald::VirialReciprocal,
+ * src/Ewald.cpp:1168-1305 (CPU branch :1228-1283).  out16 = inter, real,
+ * recip, total, then the diagonals (xx, yy, zz) of interTens, realTens,
+ * recipTens, totalTens; the reference leaves the off-diagonals at zero. */
+void ora_virial(ora_sys *s, double *out) {
+  int n = s->n_atoms;
+  int *cv = (int *)malloc(sizeof(int) * n);
+  int *cs = (int *)malloc(sizeof(int) * (s->ncell + 1));
+  int *mp = (int *)malloc(sizeof(int) * n);
+  cell_vectors(s, cv, cs, mp);
+  double vT11 = 0.0, vT22 = 0.0, vT33 = 0.0;
+  double rT11 = 0.0, rT22 = 0.0, rT33 = 0.0;
+  int nv = cs[s->ncell];
+  for (int ci = 0; ci < nv; ci++) {
+    int cur = cv[ci];
+    int cell = mp[cur];
+    for (int nc = 0; nc < NB27; nc++) {
+      int ncell = s->nbr[cell * NB27 + nc];
+      for (int ni = cs[ncell]; ni < cs[ncell + 1]; ni++) {
+        int np = cv[ni];
+        if (!(cur < np && s->mol[cur] != s->mol[np]))
+          continue;
+        double virC[3];
+        double distSq = dist_sq(s, s->x[cur], s->y[cur], s->z[cur], s->x[np],
+                                s->y[np], s->z[np], virC);
+        if (!(s->rcutSq > distSq))
+          continue;
+        int mc = s->mol[cur], mn = s->mol[np];
+        double comC[3] = {min_image(s->cx[mc] - s->cx[mn], s->box[0], s->half[0]),
+                          min_image(s->cy[mc] - s->cy[mn], s->box[1], s->half[1]),
+                          min_image(s->cz[mc] - s->cz[mn], s->box[2], s->half[2])};
+        if (s->electrostatic) {
+          double qi_qj = s->q[cur] * s->q[np];
+          if (qi_qj != 0.0) {
+            double pRF = calc_coulomb_vir(s, distSq, qi_qj);
+            rT11 += pRF * (virC[0] * comC[0]);
+            rT22 += pRF * (virC[1] * comC[1]);
+            rT33 += pRF * (virC[2] * comC[2]);
+          }
+        }
+        double pVF = calc_vir(s, distSq, s->kind[cur], s->kind[np]);
+        vT11 += pVF * (virC[0] * comC[0]);
+        vT22 += pVF * (virC[1] * comC[1]);
+        vT33 += pVF * (virC[2] * comC[2]);
+      }
+    }
+  }
+  free(cv);
+  free(cs);
+  free(mp);
+  double wT11 = 0.0, wT22 = 0.0, wT33 = 0.0;
+  if (s->ewald) {
+    double constVal = 1.0 / (4.0 * s->alphaSq);
+    for (int i = 0; i < s->K; i++) {
+      double factor = s->prefact[i] * (s->sumRref[i] * s->sumRref[i] +
+                                       s->sumIref[i] * s->sumIref[i]);
+      wT11 += factor * (1.0 - 2.0 * (constVal + 1.0 / s->hsqr[i]) * s->kx[i] *
+                                  s->kx[i]);
+      wT22 += factor * (1.0 - 2.0 * (constVal + 1.0 / s->hsqr[i]) * s->ky[i] *
+                                  s->ky[i]);
+      wT33 += factor * (1.0 - 2.0 * (constVal + 1.0 / s->hsqr[i]) * s->kz[i] *
+                                  s->kz[i]);
+    }
+    for (int m = 0; m < s->n_mol; ++m) {
+      for (int atom = s->mstart[m]; atom < s->mstart[m + 1]; ++atom) {
+        if (s->no_charge[atom])
+          continue;
+        double ac[3] = {unwrap1(s->x[atom], s->cx[m], s->box[0], s->half[0]),
+                        unwrap1(s->y[atom], s->cy[m], s->box[1], s->half[1]),
+                        unwrap1(s->z[atom], s->cz[m], s->box[2], s->half[2])};
+        double diffC[3] = {ac[0] - s->cx[m], ac[1] - s->cy[m], ac[2] - s->cz[m]};
+        double charge = s->q[atom] * 1.0;
+        for (int i = 0; i < s->K; i++) {
+          double arg = s->x[atom] * s->kx[i] + s->y[atom] * s->ky[i] +
+                       s->z[atom] * s->kz[i];
+          double factor = s->prefact[i] * 2.0 *
+                          (s->sumIref[i] * cos(arg) - s->sumRref[i] * sin(arg)) *
+                          charge;
+          wT11 += factor * (s->kx[i] * diffC[0]);
+          wT22 += factor * (s->ky[i] * diffC[1]);
+          wT33 += factor * (s->kz[i] * diffC[2]);
+        }
+      }
+    }
+  }
+  double inter = vT11 + vT22 + vT33;
+  double real = s->electrostatic ? (rT11 + rT22 + rT33) * QQ_FACT : 0.0;
+  double rt[3] = {0, 0, 0};
+  if (s->electrostatic) {
+    rt[0] = rT11 * QQ_FACT;
+    rt[1] = rT22 * QQ_FACT;
+    rt[2] = rT33 * QQ_FACT;
+  }
+  double recip = wT11 + wT22 + wT33;
+  double vt[3] = {vT11, vT22, vT33}, wt[3] = {wT11, wT22, wT33};
+  out[0] = inter;
+  out[1] = real;
+  out[2] = recip;
+  out[3] = inter + 0.0 + real + recip + 0.0 + 0.0;
+  for (int d = 0; d < 3; ++d) {
+    out[4 + d] = vt[d];
+    out[7 + d] = rt[d];
+    out[10 + d] = wt[d];
+    out[13 + d] = vt[d] + rt[d] + wt[d] + 0.0;
+  }
+}
+
 void ora_box_force(ora_sys *s, const double *coords, double *aF, double *mF,
                    double *inter, double *real) {
   memset(aF, 0, sizeof(double) * 3 * s->n_atoms);

@@ -65,6 +65,11 @@ typedef struct ora_softcore {
  * out = old inter, old real, new inter, new real. */
 void ora_single_molecule_inter(const ora_sys *s, int m, const double *lam,
                                const ora_softcore *sc, double *out);
+/* CalculateEnergy::VirialCalc + Ewald::VirialReciprocal
+ * (src/CalculateEnergy.cpp:411-579, src/Ewald.cpp:1168-1305), LRC off.
+ * out16 = inter, real, recip, total, diagonals of interTens, realTens,
+ * recipTens, totalTens. */
+void ora_virial(ora_sys *s, double *out16);
 /* CalculateEnergy::MoleculeInter with the molecule removed from the cell list
  * first (as Translate::CalcEn does).  Returns overlap. */
 int ora_molecule_inter(ora_sys *s, int m, const double *newpos, double *dlj,

@@ -60,6 +60,7 @@ def lib():
             "ora_system_total": (None, [P, dp]),
             "ora_grid_all": (None, [P]),
             "ora_molecule_inter": (I, [P, I, dp, dp, dp]),
+            "ora_virial": (None, [P, dp]),
             "ora_single_molecule_inter": (None, [P, I, dp,
                                                  C.POINTER(SoftCore), dp]),
             "ora_particle_inter": (I, [P, I, I, D, dp, dp, dp]),
@@ -213,6 +214,13 @@ class OracleBox:
         ov = lib().ora_molecule_inter(self.h, int(m), _dp(p), C.byref(a),
                                       C.byref(b))
         return bool(ov), a.value, b.value
+
+    def virial(self) -> np.ndarray:
+        """VirialCalc: inter, real, recip, total, then the xx/yy/zz diagonals
+        of interTens, realTens, recipTens, totalTens."""
+        out = np.empty(16)
+        lib().ora_virial(self.h, _dp(out))
+        return out
 
     def single_molecule_inter(self, m: int, lambdas, sc_alpha: float,
                               sc_sigma: float, sc_power: int, sc_coul: bool):

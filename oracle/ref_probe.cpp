@@ -162,6 +162,19 @@ int main(int argc, char **argv) {
   dump_coords(outdir, "coords_init.txt", sys.coordinates);
   dump_coords(outdir, "com_init.txt", sys.com);
 
+  // CalculateEnergy::VirialCalc on the initial state
+  // (src/CalculateEnergy.cpp:411-579): scalars and tensor diagonals
+  {
+    Virial v = sys.calcEnergy.VirialCalc(box);
+    FILE *f = open_out(outdir, "virial.txt");
+    fprintf(f, "%.17g %.17g %.17g %.17g\n", v.inter, v.real, v.recip,
+            v.total);
+    for (int d = 0; d < 3; ++d)
+      fprintf(f, "%.17g %.17g %.17g %.17g\n", v.interTens[d][d],
+              v.realTens[d][d], v.recipTens[d][d], v.totalTens[d][d]);
+    fclose(f);
+  }
+
   if (stat.forcefield.ewald) {
     FILE *f = open_out(outdir, "kvec.txt");
     for (uint i = 0; i < ew->imageSizeRef[box]; ++i)

@@ -217,6 +217,26 @@ def make_single_mol(probe: str, name: str, n: int = 48) -> None:
     print("wrote smi_" + name)
 
 
+def make_virial(probe: str, name: str) -> None:
+    """CalculateEnergy::VirialCalc (src/CalculateEnergy.cpp:411-579) of the
+    fixture's initial state -> vir_<name>.npz: out16 = inter, real, recip,
+    total, then the xx/yy/zz diagonals of interTens, realTens, recipTens,
+    totalTens."""
+    builder, cfg, _, _ = FIXTURES[name]
+    sysm = builder()
+    with tempfile.TemporaryDirectory() as d:
+        write_reference_inputs(d, sysm, cfg)
+        out = os.path.join(d, "out")
+        os.makedirs(out)
+        subprocess.check_call([probe, "in.conf", out, "0"], cwd=d,
+                              stdout=subprocess.DEVNULL)
+        v = np.loadtxt(os.path.join(out, "virial.txt"))
+    out16 = np.concatenate([v[0], v[1:, 0], v[1:, 1], v[1:, 2], v[1:, 3]])
+    np.savez_compressed(os.path.join(HERE, "vir_" + name + ".npz"),
+                        out16=out16)
+    print("wrote vir_" + name)
+
+
 def make_kat(probe: str) -> None:
     """Known-answer vectors of the reference's MT19937 and Philox4x64-10."""
     with tempfile.TemporaryDirectory() as d:
@@ -244,6 +264,8 @@ def main():
     for n in ("c0_water", "w1728", "lj500"):
         if not a.names or n in a.names:
             make_single_mol(probe, n)
+    for n in (a.names or list(FIXTURES)):
+        make_virial(probe, n)
 
 
 if __name__ == "__main__":

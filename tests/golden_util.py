@@ -60,3 +60,10 @@ def load_smi(name):
     outputs (old inter, old real, new inter, new real) and the soft-core
     settings (ScaleAlpha, ScaleSigma, ScalePower)."""
     return np.load(os.path.join(GOLDEN, "smi_" + name + ".npz"))
+
+
+def load_virial(name):
+    """The reference's CalculateEnergy::VirialCalc of fixture `name`'s
+    initial state: inter, real, recip, total, then the xx/yy/zz diagonals of
+    interTens, realTens, recipTens, totalTens."""
+    return np.load(os.path.join(GOLDEN, "vir_" + name + ".npz"))["out16"]

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from tests.golden_util import (NAMES, SMI_NAMES, config_of, load, load_smi,
+                               load_virial,
                                move_fractions, system_of)
 
 pytestmark = pytest.mark.gpu
@@ -186,3 +187,19 @@ def test_single_molecule_inter(gb, name):
             assert abs(x - y) <= REL * max(abs(y), 1.0), (m, lam, c, got, ref)
     for b in boxes.values():
         b.close()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_virial(gb, name):
+    """VirialCalc on the GPU against the reference: every scalar and tensor
+    component within 1e-10 of the largest virial term (the components are
+    sums of cancelling terms, so each is held to the scale of the whole)."""
+    z, meta = load(name)
+    box = gb.Box(system_of(z, meta), config_of(meta))
+    got, ref = box.virial(), load_virial(name)
+    scale = np.abs(ref[:4]).max()
+    for i, (x, y) in enumerate(zip(got, ref)):
+        assert abs(x - y) <= REL * scale, (i, x, y)
+    p = box.pressure()
+    assert np.isfinite(p)
+    box.close()

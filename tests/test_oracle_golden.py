@@ -12,6 +12,7 @@ import pytest
 
 from oracle import oracle as O
 from tests.golden_util import (NAMES, SMI_NAMES, config_of, load, load_smi,
+                               load_virial,
                                move_fractions, system_of)
 
 REL = 1e-12
@@ -146,4 +147,13 @@ def test_single_molecule_inter(name):
     for m, lam, c, ref in zip(g["mol"], g["lam"], g["sc_coul"], g["out"]):
         got = ob.single_molecule_inter(int(m), lam, a, s, int(p), bool(c))
         np.testing.assert_array_equal(got, ref)
+    del ob
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_virial(name):
+    """VirialCalc + VirialReciprocal of the initial state: bit-exact."""
+    z, meta = load(name)
+    ob = O.OracleBox(system_of(z, meta), config_of(meta))
+    np.testing.assert_array_equal(ob.virial(), load_virial(name))
     del ob
