@@ -79,6 +79,9 @@ SIGNATURES = {
     "gb_molecule_inter": (C.c_int, [_P, C.c_int32, _D, _D, _D, _I]),
     "gb_single_molecule_inter": (C.c_int, [_P, C.c_int32, _D, _D]),
     "gb_virial": (C.c_int, [_P, _D]),
+    "gb_checkpoint_size": (C.c_int, [_P, _L]),
+    "gb_checkpoint_save": (C.c_int, [_P, _P, C.c_int64]),
+    "gb_checkpoint_load": (C.c_int, [_P, _P, C.c_int64]),
     "gb_particle_inter": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_double, _D,
                                     C.c_int32, _D, _D, _I]),
     "gb_box_force": (C.c_int, [_P, _D, _D, _D, _D]),

@@ -138,6 +138,31 @@ int gb_molecule_inter(gb_box *box, int32_t mol, const double *new_pos,
   *overlap = ov;
   return rc;
 }
+int gb_checkpoint_size(gb_box *box, int64_t *bytes) {
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  if (!bytes)
+    return gb::ERR_ARG;
+  return gb::checkpoint_size(*box->b, bytes);
+}
+int gb_checkpoint_save(gb_box *box, void *buf, int64_t bytes) {
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  if (!buf)
+    return gb::ERR_ARG;
+  return gb::checkpoint_save(*box->b, buf, bytes);
+}
+int gb_checkpoint_load(gb_box *box, const void *buf, int64_t bytes) {
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  if (!buf)
+    return gb::ERR_ARG;
+  return gb::checkpoint_load(*box->b, buf, bytes);
+}
+
 int gb_virial(gb_box *box, double *out16) {
   if (!out16)
     return gb::ERR_ARG;

@@ -66,6 +66,20 @@ uint32_t MT19937::u32() {
   return y ^ (y >> 18);
 }
 
+void MT19937::Save(uint32_t st[624], int32_t *left, int32_t *next) const {
+  for (int i = 0; i < 624; ++i)
+    st[i] = st_[i];
+  *left = left_;
+  *next = next_;
+}
+
+void MT19937::Load(const uint32_t st[624], int32_t left, int32_t next) {
+  for (int i = 0; i < 624; ++i)
+    st_[i] = st[i];
+  left_ = left;
+  next_ = next;
+}
+
 uint32_t MT19937::randInt(uint32_t n) {
   uint32_t used = n;
   used |= used >> 1;

@@ -41,6 +41,9 @@ class MT19937 {
   double rand01() { return (double)u32() * (1.0 / 4294967295.0); }
   double randExc01() { return (double)u32() * (1.0 / 4294967296.0); }
   uint32_t randInt(uint32_t n);
+  // the generator's full state (checkpoints)
+  void Save(uint32_t st[624], int32_t *left, int32_t *next) const;
+  void Load(const uint32_t st[624], int32_t left, int32_t next);
 
  private:
   void reload();
@@ -56,6 +59,7 @@ class MoveStream {
   MoveStream(uint32_t seed, const double frac[3], int n_mol,
              const std::vector<int> &mol_len);
   void Next(MoveRec *r);
+  MT19937 &mt() { return mt_; }
 
  private:
   MT19937 mt_;
@@ -161,5 +165,10 @@ int mixed_complete(const std::vector<Box *> &boxes,
 int mc_recompute(Box &b);
 int64_t mixed_segment_limit(Box &b, int64_t cap);
 void mc_destroy(Box &b);
+
+// Checkpoints of a box's dynamic state (gb_ckpt.cu)
+int checkpoint_size(Box &b, int64_t *bytes);
+int checkpoint_save(Box &b, void *buf, int64_t bytes);
+int checkpoint_load(Box &b, const void *buf, int64_t bytes);
 
 }  // namespace gb

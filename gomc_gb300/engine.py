@@ -320,6 +320,22 @@ class Box:
                       cluster_size, flush_every, move_buffer)
         self._chk(lib().gb_mc_init(self.h, C.byref(p)))
 
+    def checkpoint(self) -> bytes:
+        """The box's dynamic state (and its Monte Carlo state after
+        mc_init) as bytes; see gb_checkpoint_save."""
+        n = C.c_int64()
+        self._chk(lib().gb_checkpoint_size(self.h, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        self._chk(lib().gb_checkpoint_save(self.h, buf, n.value))
+        return buf.raw
+
+    def restore(self, blob: bytes) -> None:
+        """Load a checkpoint written by a box of the same system and
+        configuration (call mc_init first when it holds Monte Carlo
+        state)."""
+        buf = C.create_string_buffer(blob, len(blob))
+        self._chk(lib().gb_checkpoint_load(self.h, buf, len(blob)))
+
     def mc_drift(self):
         mx, last = np.empty(4), np.empty(4)
         n = C.c_int64()

@@ -215,6 +215,22 @@ int gb_box_stream(gb_box *box, void **stream);
 int gb_mc_run_batch(gb_box **boxes, int32_t nboxes, int64_t first_step,
                     int64_t nsteps);
 
+/* ---- Checkpoints ----
+ * The role of the reference's Checkpoint (src/Checkpoint.h:27-120) in a
+ * format of this library's own: a run that loads a checkpoint continues with
+ * the same moves, decisions and coordinates, bit for bit, as a run that
+ * never stopped (the reference's restart tests pin the same property,
+ * test/src/CheckpointTest.cpp).  Saved: coordinates, molecule centres, the
+ * cell grid's slot order, the FP64 structure factors, the running energies
+ * and, after gb_mc_init, the step, the MT19937 state of the move stream,
+ * the move settings and the drift records.  A checkpoint loads into a box
+ * created from the same system and configuration (and gb_mc_init'ed first
+ * when it holds Monte Carlo state); anything else is GB_ERR_ARG /
+ * GB_ERR_STATE. */
+int gb_checkpoint_size(gb_box *box, int64_t *bytes);
+int gb_checkpoint_save(gb_box *box, void *buf, int64_t bytes);
+int gb_checkpoint_load(gb_box *box, const void *buf, int64_t bytes);
+
 /* ---- Continuous-batching job server ----
  * No counterpart in the reference (it runs one simulation per process,
  * src/Simulation.cpp:116-168).  A server runs many independent

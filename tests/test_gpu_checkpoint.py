@@ -1,0 +1,82 @@
+"""Checkpoint and resume (gb_checkpoint_*): a run that stops, saves, and
+continues in a fresh box from the saved state ends bit-identical to a run
+that never stopped -- coordinates, molecule centres, running energies and
+move statistics -- for the FP64 form (with MultiParticle moves) and the
+mixed form.  The reference's restart tests pin the same property for its
+own checkpoint format (test/src/CheckpointTest.cpp)."""
+import numpy as np
+import pytest
+
+from gomc_gb300.config import SimConfig
+from gomc_gb300.systems import spce_water_box
+from tests.golden_util import config_of, load, move_fractions, system_of
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gb():
+    from gomc_gb300 import engine
+    engine.lib(build_if_missing=True)
+    return engine
+
+
+def _state(box):
+    sc, cnt = box.mc_state()
+    return box.coords(), box.com(), box.energy(), sc, cnt
+
+
+def _resume_equals_straight(gb, make, init, first, more):
+    straight = make()
+    init(straight)
+    straight.mc_run(0, first)
+    blob = straight.checkpoint()
+    straight.mc_run(first, more)
+    want = _state(straight)
+    straight.close()
+    resumed = make()
+    init(resumed)
+    resumed.restore(blob)
+    resumed.mc_run(first, more)
+    got = _state(resumed)
+    resumed.close()
+    for a, b in zip(got, want):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_fp64_with_multiparticle(gb):
+    z, meta = load("c0_water_mp")
+    seed = meta["config"]["random_seed"]
+
+    def make():
+        return gb.Box(system_of(z, meta), config_of(meta))
+
+    def init(b):
+        b.mc_init(seed, move_fractions(meta), meta["config"]["adj_steps"])
+    _resume_equals_straight(gb, make, init, 150, 200)
+
+
+def test_mixed(gb):
+    def make():
+        return gb.Box(spce_water_box(2000, 39.1, seed=21),
+                      SimConfig(temperature=298.0, rcut=10.0, tolerance=1e-5),
+                      precision=gb.GB_MIXED)
+
+    def init(b):
+        b.mc_init(77, [0.5, 0.5, 0.0], 300, scales=[0.3, 0.3, 0.02, 0.03],
+                  recompute_freq=500)
+    _resume_equals_straight(gb, make, init, 700, 900)
+
+
+def test_rejects_other_system(gb):
+    from gomc_gb300._lib import GbError
+    cfg = SimConfig(temperature=298.0, rcut=9.0, tolerance=1e-5)
+    a = gb.Box(spce_water_box(256, 19.7, seed=1), cfg)
+    blob = a.checkpoint()
+    a.close()
+    b = gb.Box(spce_water_box(300, 20.8, seed=1), cfg)
+    with pytest.raises(GbError):
+        b.restore(blob)
+    with pytest.raises(GbError):
+        b.restore(b"not a checkpoint at all, just some bytes")
+    b.close()
