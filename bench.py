@@ -262,6 +262,9 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
     for b in (bf, bm):
         b.mc_init(SEED + rank, FRAC, ADJ, scales=SCALES,
                   cluster_size=args.cluster)
+    tune_single = None
+    if not args.cluster:
+        tune_single = bm.mc_autotune("latency")
     rf = bf.mc_run(0, n_cmp, trace=True)
     rm = bm.mc_run(0, n_cmp, trace=True)
     same = float(np.mean(rf["accepted"] == rm["accepted"]))
@@ -335,16 +338,30 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
     out["single"] = {"value": single, "unit": "moves/s",
                      "ms_per_step": sum(t_single) / args.steps * 1e3,
                      "us_per_move": sum(t_single) / (args.steps * M) * 1e6,
-                     "ctas_per_chain": layout["ctas_per_chain"]}
+                     "ctas_per_chain": layout["ctas_per_chain"],
+                     "autotune_us_per_move": tune_single and {
+                         str(k): v for k, v in
+                         tune_single["us_per_move"].items()}}
 
-    # batched replicas, one launch per step for every chain
-    B = args.mixed_chains or layout["max_concurrent"]
+    # batched replicas, one launch per step for every chain; the cluster
+    # size from the autotuner's throughput objective on the first replica
     boxes = []
-    for i in range(B):
+    s0, c0 = make_system(rank * 1000)
+    b0 = engine.Box(s0, c0, device=dev, precision=GB_MIXED)
+    b0.mc_init(SEED + rank * 1000, FRAC, ADJ, scales=SCALES,
+               recompute_freq=10000, cluster_size=args.cluster)
+    tune_batch = None
+    if not args.cluster:
+        tune_batch = b0.mc_autotune("throughput")
+    lay0 = b0.mc_layout()
+    csize = lay0["ctas_per_chain"]
+    boxes.append(b0)
+    B = args.mixed_chains or lay0["max_concurrent"]
+    for i in range(1, B):
         s_i, c_i = make_system(rank * 1000 + i)
         b = engine.Box(s_i, c_i, device=dev, precision=GB_MIXED)
         b.mc_init(SEED + rank * 1000 + i, FRAC, ADJ, scales=SCALES,
-                  recompute_freq=10000, cluster_size=args.cluster)
+                  recompute_freq=10000, cluster_size=csize)
         boxes.append(b)
     st_batch = torch.cuda.ExternalStream(boxes[0].stream_ptr(), device=dev)
     bstep = [0]
@@ -402,6 +419,9 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
         "step_ms": [round(t * 1e3, 3) for t in t_batch],
         "kernel_launches": timing["chain_launches"],
         "speedup_vs_fp64": batched / fp64_value,
+        "ctas_per_chain": csize,
+        "autotune_us_per_move": tune_batch and {str(k): v for k, v in
+                                                tune_batch["us_per_move"].items()},
         "clocks": clk.summary()}
     out["e2e"] = {"value": world * args.steps * M * B / t_e2e,
                   "unit": "moves/s",

@@ -114,6 +114,7 @@ SIGNATURES = {
     "gb_mc_timing": (C.c_int, [_P, C.c_int32, _D, _L, _L, _D, _L]),
     "gb_box_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "gb_mc_layout": (C.c_int, [_P, _I, _I, _L]),
+    "gb_mc_autotune": (C.c_int, [_P, C.c_int32, C.c_int32, _I, _D]),
     "gb_mc_drift": (C.c_int, [_P, _D, _D, _L]),
     "gb_recip_energy_noalloc": (C.c_int, [_P, _P, _P, C.c_int32, _P, _P]),
     "gb_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P)]),

@@ -138,6 +138,18 @@ int gb_molecule_inter(gb_box *box, int32_t mol, const double *new_pos,
   *overlap = ov;
   return rc;
 }
+int gb_mc_autotune(gb_box *box, int32_t objective, int32_t trial_moves,
+                   int32_t *cluster_size, double *us_per_move4) {
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  int c = 0;
+  rc = gb::mc_autotune(*box->b, objective, trial_moves, &c, us_per_move4);
+  if (!rc && cluster_size)
+    *cluster_size = c;
+  return rc;
+}
+
 int gb_checkpoint_size(gb_box *box, int64_t *bytes) {
   int rc = guard(box);
   if (rc)

@@ -166,6 +166,10 @@ int mc_recompute(Box &b);
 int64_t mixed_segment_limit(Box &b, int64_t cap);
 void mc_destroy(Box &b);
 
+// Timed choice of the mixed chain's cluster size (gb_tune.cu)
+int mc_autotune(Box &b, int objective, int trial_moves, int *chosen,
+                double *us_per_move4);
+
 // Checkpoints of a box's dynamic state (gb_ckpt.cu)
 int checkpoint_size(Box &b, int64_t *bytes);
 int checkpoint_save(Box &b, void *buf, int64_t bytes);

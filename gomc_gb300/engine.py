@@ -374,6 +374,19 @@ class Box:
         return dict(ctas_per_chain=c.value, max_concurrent=n.value,
                     smem_bytes=sm.value)
 
+    def mc_autotune(self, objective: str = "latency",
+                    trial_moves: int = 0) -> dict:
+        """Time each fitting cluster size on this machine's own state and keep
+        the best ('latency': one chain; 'throughput': as many chains as the
+        GPU holds); the Monte Carlo state is unchanged."""
+        c = C.c_int32()
+        us = np.zeros(4)
+        self._chk(lib().gb_mc_autotune(
+            self.h, 0 if objective == "latency" else 1, int(trial_moves),
+            C.byref(c), _dp(us)))
+        return dict(cluster_size=c.value,
+                    us_per_move={2: us[0], 4: us[1], 8: us[2], 16: us[3]})
+
     def stream_ptr(self) -> int:
         p = C.c_void_p()
         self._chk(lib().gb_box_stream(self.h, C.byref(p)))

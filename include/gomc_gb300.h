@@ -207,6 +207,18 @@ int gb_mc_drift(gb_box *box, double *max4, double *last4, int64_t *recomputes);
  * counterpart. */
 int gb_mc_layout(gb_box *box, int32_t *ctas_per_chain, int32_t *max_concurrent,
                  int64_t *smem_bytes);
+/* Autotuner of the mixed form's chain geometry (no reference counterpart):
+ * times a trial segment of `trial_moves` moves (0 = 200) for each cluster
+ * size 2, 4, 8, 16 that fits the box -- it fixes the k-vectors per CTA and
+ * the threads per molecule move -- on the box's own state, which is
+ * checkpointed and restored around every trial, and keeps the best for the
+ * objective: 0 = shortest move latency of one chain, 1 = most moves/s with
+ * as many chains as the GPU holds at once.  The Monte Carlo state after the
+ * call is the state before it; gb_mc_layout shows the choice.
+ * us_per_move4 (may be NULL) receives each candidate's latency (0 where a
+ * shape does not fit). */
+int gb_mc_autotune(gb_box *box, int32_t objective, int32_t trial_moves,
+                   int32_t *cluster_size, double *us_per_move4);
 /* The CUDA stream (cudaStream_t) every call on this machine is ordered on. */
 int gb_box_stream(gb_box *box, void **stream);
 

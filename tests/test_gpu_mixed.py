@@ -111,3 +111,35 @@ def test_batch_matches_alone(gb):
         np.testing.assert_array_equal(cm, ca)
     for b in alone + mixed:
         b.close()
+
+
+def test_autotune_keeps_state_and_matches_fixed_shape(gb):
+    """The autotuner restores the state it found, and a box it tuned runs
+    exactly as a box initialised with the chosen cluster size."""
+    params = dict(scales=SCALES, recompute_freq=0)
+    tuned = make(gb, 2000, 39.1, 10.0, gb.GB_MIXED, seed=31)
+    tuned.mc_init(41, [0.5, 0.5, 0.0], 300, **params)
+    tuned.mc_run(0, 300)
+    before = (tuned.coords(), tuned.energy(), tuned.mc_state())
+    res = tuned.mc_autotune("throughput", 120)
+    c = res["cluster_size"]
+    assert c in (2, 4, 8, 16) and res["us_per_move"][c] > 0
+    assert tuned.mc_layout()["ctas_per_chain"] == c
+    after = (tuned.coords(), tuned.energy(), tuned.mc_state())
+    np.testing.assert_array_equal(before[0], after[0])
+    np.testing.assert_array_equal(before[1], after[1])
+    for x, y in zip(before[2], after[2]):
+        np.testing.assert_array_equal(x, y)
+    # the same first 300 moves, then the chosen shape from the same state
+    fixed = make(gb, 2000, 39.1, 10.0, gb.GB_MIXED, seed=31)
+    fixed.mc_init(41, [0.5, 0.5, 0.0], 300, **params)
+    fixed.mc_run(0, 300)
+    blob = fixed.checkpoint()
+    fixed.mc_init(41, [0.5, 0.5, 0.0], 300, cluster_size=c, **params)
+    fixed.restore(blob)
+    tuned.mc_run(300, 400)
+    fixed.mc_run(300, 400)
+    np.testing.assert_array_equal(tuned.coords(), fixed.coords())
+    np.testing.assert_array_equal(tuned.energy(), fixed.energy())
+    tuned.close()
+    fixed.close()
