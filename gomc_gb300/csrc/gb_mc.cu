@@ -238,6 +238,45 @@ __device__ __forceinline__ void apply_proposal(const DevBox &b, int kind,
   }
 }
 
+// exp(2 pi i phase / 2^64) in FP64 for a phase given as an exact 64-bit
+// fraction of a turn: the reduction to |x| <= pi/4 is integer arithmetic,
+// sin and cos of the remainder are their Taylor series to x^19 / x^20
+// (truncation below 1e-19 there).
+__device__ __forceinline__ double2 cis_turns64(uint64_t phase) {
+  int64_t s = (int64_t)phase;                       // [-1/2, 1/2) turn
+  int64_t q = (s + (1LL << 61)) >> 62;              // nearest quarter turn
+  int64_t r = s - (int64_t)((uint64_t)q << 62);     // |r| <= 2^61
+  double x = (double)r * 3.4061215800865545e-19;    // 2 pi / 2^64
+  double x2 = x * x;
+  double ps = -1.0 / 121645100408832000.0;          // -1/19!
+  ps = fma(x2, ps, 1.0 / 355687428096000.0);        //  1/17!
+  ps = fma(x2, ps, -1.0 / 1307674368000.0);         // -1/15!
+  ps = fma(x2, ps, 1.0 / 6227020800.0);             //  1/13!
+  ps = fma(x2, ps, -1.0 / 39916800.0);              // -1/11!
+  ps = fma(x2, ps, 1.0 / 362880.0);                 //  1/9!
+  ps = fma(x2, ps, -1.0 / 5040.0);                  // -1/7!
+  ps = fma(x2, ps, 1.0 / 120.0);                    //  1/5!
+  ps = fma(x2, ps, -1.0 / 6.0);                     // -1/3!
+  double sn = fma(x * x2, ps, x);
+  double pc = 1.0 / 2432902008176640000.0;          //  1/20!
+  pc = fma(x2, pc, -1.0 / 6402373705728000.0);      // -1/18!
+  pc = fma(x2, pc, 1.0 / 20922789888000.0);         //  1/16!
+  pc = fma(x2, pc, -1.0 / 87178291200.0);           // -1/14!
+  pc = fma(x2, pc, 1.0 / 479001600.0);              //  1/12!
+  pc = fma(x2, pc, -1.0 / 3628800.0);               // -1/10!
+  pc = fma(x2, pc, 1.0 / 40320.0);                  //  1/8!
+  pc = fma(x2, pc, -1.0 / 720.0);                   // -1/6!
+  pc = fma(x2, pc, 1.0 / 24.0);                     //  1/4!
+  pc = fma(x2, pc, -0.5);
+  double cs = fma(x2, pc, 1.0);
+  switch ((int)(q & 3)) {
+    case 0: return make_double2(cs, sn);
+    case 1: return make_double2(-sn, cs);
+    case 2: return make_double2(-cs, -sn);
+    default: return make_double2(sn, -cs);
+  }
+}
+
 __device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -253,10 +292,12 @@ __device__ __forceinline__ double2 tab_at(const double2 *row, int n) {
 // ===========================================================================
 constexpr int CT = 256;
 constexpr int HDR = 96;  // doubles in the move-context header
+constexpr int ICL_MAX = 256;  // in-cutoff pairs a CTA lists per move
 
 // Context header layout (doubles):
 //  0 m, 1 kind, 2 na, 3 pacc, 4..6 newcom, 8..15 cell old, 16..23 cell new,
-//  24..47 old positions [8][3], 48..71 new positions [8][3], 72..79 charges
+//  24..47 old positions [8][3], 48..71 new positions [8][3], 72..79 charges,
+//  80 log(pacc)
 struct ChainArgs {
   DevBox b;
   const FF *ff;
@@ -282,11 +323,23 @@ struct ChainShared {
   unsigned gen;
 };
 
+// Synchronise the threads [first, first + count) of the CTA: the whole CTA
+// through __syncthreads, a group of whole warps through named barrier 1.
+__device__ __forceinline__ void group_sync(int count) {
+  if (count == (int)blockDim.x)
+    __syncthreads();
+  else
+    asm volatile("bar.sync 1, %0;" ::"r"(count) : "memory");
+}
+
 // Build the next move's header and phase tables (designated CTAs), using the
 // committed state plus the just-decided move when it touched the same
-// molecule.
+// molecule.  The threads [first, first + count) of the CTA take part (whole
+// warps; count >= 64).
 __device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
-                          const double *prev_hdr, int prev_acc) {
+                          const double *prev_hdr, int prev_acc, int first,
+                          int count) {
+  const int tid = (int)threadIdx.x - first;
   const DevBox &b = A.b;
   const MoveRec &r = A.moves[t];
   int m = r.mol;
@@ -304,24 +357,24 @@ __device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
       newcom[3];
   __shared__ double prop[12];
   bool same = prev_acc && prev_hdr && (int)prev_hdr[0] == m;
-  if (threadIdx.x < 12)
-    prop[threadIdx.x] = A.prop[(size_t)t * 12 + threadIdx.x];
-  if (threadIdx.x < 3) {
-    int d = threadIdx.x;
+  if (tid < 12)
+    prop[tid] = A.prop[(size_t)t * 12 + tid];
+  if (tid < 3) {
+    int d = tid;
     double *cs[3] = {b.cx, b.cy, b.cz};
     com[d] = (same && (int)prev_hdr[1] == 0) ? prev_hdr[4 + d]
                                              : __ldcg(cs[d] + m);
   }
-  if (threadIdx.x >= 32 && threadIdx.x < 32 + 3 * na) {
-    int i = threadIdx.x - 32, a = i / 3, d = i % 3;
+  if (tid >= 32 && tid < 32 + 3 * na) {
+    int i = tid - 32, a = i / 3, d = i % 3;
     double *xs[3] = {b.x, b.y, b.z};
     oldp[a][d] = same ? prev_hdr[48 + 3 * a + d] : __ldcg(xs[d] + a0 + a);
   }
-  __syncthreads();
+  group_sync(count);
   // one thread per atom applies the proposal (Coordinates::TranslateRand /
   // RotateRand arithmetic, see apply_proposal)
-  if (threadIdx.x < na) {
-    int a = threadIdx.x;
+  if (tid < na) {
+    int a = tid;
     double v[3], w[3];
     if (r.kind == 0) {
       for (int d = 0; d < 3; ++d)
@@ -341,23 +394,24 @@ __device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
     for (int d = 0; d < 3; ++d)
       newp[a][d] = w[d];
   }
-  if (threadIdx.x >= 32 && threadIdx.x < 35) {
-    int d = threadIdx.x - 32;
+  if (tid >= 32 && tid < 35) {
+    int d = tid - 32;
     newcom[d] = r.kind == 0 ? wrap1(__dadd_rn(com[d], prop[d]), b.L[d]) : com[d];
   }
-  __syncthreads();
+  group_sync(count);
   if (header_cta) {
     double *h = A.ctx;
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
       h[0] = m;
       h[1] = r.kind;
       h[2] = na;
       h[3] = r.pacc;
+      h[80] = r.lpacc;
       for (int d = 0; d < 3; ++d)
         h[4 + d] = newcom[d];
     }
-    if (threadIdx.x >= 32 && threadIdx.x < 32 + 2 * na) {
-      int i = threadIdx.x - 32, a = i % na, side = i / na;
+    if (tid >= 32 && tid < 32 + 2 * na) {
+      int i = tid - 32, a = i % na, side = i / na;
       const double *p = side ? newp[a] : oldp[a];
       h[(side ? 16 : 8) + a] = position_to_cell_fast(b, p[0], p[1], p[2]);
       for (int d = 0; d < 3; ++d)
@@ -368,19 +422,19 @@ __device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
       }
     }
   }
-  // phase rows exp(i n 2 pi r_d / L_d), n = 0..kmax, one entry per thread
+  // phase rows exp(i n 2 pi r_d / L_d), n = 0..kmax, one entry per thread:
+  // the coordinate as a 64-bit fraction of the box edge, n times it exact
+  // modulo one turn
   double2 *tab = (double2 *)(A.ctx + HDR);
   for (int rr = blockIdx.x; rr < nrows; rr += G) {
     int p = rr / 3, d = rr % 3;
     double coord = p < na ? oldp[p][d] : newp[p - na][d];
-    double cv = 1.0 / b.L[d];
-    cv *= 2.0 * M_PI;
-    double th = cv * coord;
-    for (int n = threadIdx.x; n < stride; n += blockDim.x) {
-      double s, c;
-      sincos(th * (double)n, &s, &c);
-      tab[(size_t)rr * stride + n] = make_double2(c, s);
-    }
+    double t = coord * b.invL[d];
+    if (t >= 1.0)
+      t -= 1.0;
+    uint64_t u = __double2ull_rn(t * 18446744073709551616.0);  // 2^64
+    for (int n = tid; n < stride; n += count)
+      tab[(size_t)rr * stride + n] = cis_turns64((uint64_t)n * u);
   }
 }
 
@@ -435,7 +489,7 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
   make_props(0);
   if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
     return;
-  build_ctx(A, S, 0, nullptr, 0);
+  build_ctx(A, S, 0, nullptr, 0, 0, CT);
   if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
     return;
 
@@ -451,70 +505,182 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
       tab[i] = __ldcg((const double2 *)(A.ctx + HDR) + i);
     __syncthreads();
     double lj = 0.0, re = 0.0, ovl = 0.0, er = 0.0;
+    // Real space: the candidates of all (atom, old/new, neighbour cell)
+    // units, numbered through a prefix sum of the units' slot counts and
+    // dealt out over the whole grid, so the in-cutoff pair terms (the
+    // FP64-heavy part) land evenly on the SMs.
     int units = na * 2 * NB27;
-    for (int u = cta; u < units; u += G) {
+    __shared__ int u_cell[MAX_MOL_ATOMS * 2 * NB27];
+    __shared__ int u_off[MAX_MOL_ATOMS * 2 * NB27 + 1];
+    for (int u = threadIdx.x; u < units; u += CT) {
       int a = u / (2 * NB27), side = (u / NB27) % 2, nn = u % NB27;
-      const double *pp = S.hdr + (side ? 48 : 24) + 3 * a;
       int cell = (int)S.hdr[(side ? 16 : 8) + a];
       int c2 = b.nbr[cell * NB27 + nn];
-      int n2 = __ldcg(b.cell_count + c2);
-      double qa = b.q[b.mstart[m] + a];
-      int ka = b.kind[b.mstart[m] + a];
-      for (int j = threadIdx.x; j < n2; j += CT) {
-        size_t s = (size_t)c2 * b.cap + j;
+      u_cell[u] = c2;
+      u_off[u + 1] = __ldcg(b.cell_count + c2);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      // inclusive scan of the counts: each lane a contiguous run of units
+      int per = (units + 31) / 32;
+      int lo = threadIdx.x * per, hi = min(units, lo + per);
+      int run = 0;
+      for (int u = lo; u < hi; ++u)
+        run += u_off[u + 1];
+      int incl = run;
+      for (int o = 1; o < 32; o <<= 1) {
+        int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)threadIdx.x >= o)
+          incl += v;
+      }
+      int acc0 = incl - run;
+      for (int u = lo; u < hi; ++u) {
+        acc0 += u_off[u + 1];
+        u_off[u + 1] = acc0;
+      }
+      if (threadIdx.x == 0)
+        u_off[0] = 0;
+    }
+    __syncthreads();
+    const int total = u_off[units];
+    // (1) Every warp tests candidates against the cutoff -- consecutive
+    //     candidates to different CTAs -- and the pairs inside it are
+    //     compacted, in candidate order, into a shared list (ballot and a
+    //     scan over the warps, so the order and every sum stay fixed).
+    __shared__ int icl_slot[ICL_MAX];
+    __shared__ short icl_unit[ICL_MAX];
+    __shared__ double icl_d2[ICL_MAX];
+    __shared__ int icl_warp[CT / 32 + 1];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int icl_n = 0;
+    for (int base = cta; base < total; base += total_threads) {
+      int idx = base + threadIdx.x * G;
+      bool in = false;
+      int u = 0, s = 0;
+      double distSq = 0.0;
+      if (idx < total) {
+        int lo = 0, hi = units - 1;  // last unit whose offset <= idx
+        while (lo < hi) {
+          int mid = (lo + hi + 1) >> 1;
+          if (u_off[mid] <= idx)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        u = lo;
+        int a = u / (2 * NB27), side = (u / NB27) % 2;
+        const double *pp = S.hdr + (side ? 48 : 24) + 3 * a;
+        s = u_cell[u] * b.cap + (idx - u_off[u]);
         int mj = __ldcg(b.cell_meta + s);
-        if (meta_mol(mj) == m)
-          continue;
-        const double *pq = (const double *)(b.cell_pos + s);
-        double4_32a pj = make_double4_32a(__ldcg(pq), __ldcg(pq + 1),
-                                          __ldcg(pq + 2), __ldcg(pq + 3));
-        double dx = min_image(pp[0] - pj.x, b.L[0], b.half[0]);
-        double dy = min_image(pp[1] - pj.y, b.L[1], b.half[1]);
-        double dz = min_image(pp[2] - pj.z, b.L[2], b.half[2]);
-        double distSq = dsq3(dx, dy, dz);
-        if (ff.rcutSq > distSq) {
-          if (side && distSq < ff.rcutLowSq)
+        if (meta_mol(mj) != m) {
+          const double *pq = (const double *)(b.cell_pos + s);
+          double dx = min_image(pp[0] - __ldcg(pq), b.L[0], b.half[0]);
+          double dy = min_image(pp[1] - __ldcg(pq + 1), b.L[1], b.half[1]);
+          double dz = min_image(pp[2] - __ldcg(pq + 2), b.L[2], b.half[2]);
+          distSq = dsq3(dx, dy, dz);
+          in = ff.rcutSq > distSq;
+          if (in && side && distSq < ff.rcutLowSq)
             ovl = 1.0;
+        }
+      }
+      unsigned mask = __ballot_sync(0xffffffffu, in);
+      if (lane == 0)
+        icl_warp[warp] = __popc(mask);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        int run = icl_n;
+        for (int w = 0; w < CT / 32; ++w) {
+          int c = icl_warp[w];
+          icl_warp[w] = run;
+          run += c;
+        }
+        icl_warp[CT / 32] = run;
+      }
+      __syncthreads();
+      if (in) {
+        int pos = icl_warp[warp] + __popc(mask & ((1u << lane) - 1u));
+        if (pos < ICL_MAX) {
+          icl_slot[pos] = s;
+          icl_unit[pos] = (short)u;
+          icl_d2[pos] = distSq;
+        } else {
+          // past the list (not met at liquid densities): evaluated here
+          int a = u / (2 * NB27), side = (u / NB27) % 2;
+          int mj = __ldcg(b.cell_meta + s);
+          double qa = b.q[b.mstart[m] + a];
+          int ka = b.kind[b.mstart[m] + a];
           double e = 0.0;
           if (ff.electrostatic) {
-            double qq = qa * pj.w * QQ_FACT;
+            double qq =
+                qa * __ldcg((const double *)(b.cell_pos + s) + 3) * QQ_FACT;
             if (qq != 0.0)
               e = coulomb_energy(ff, distSq, qq);
           }
           double l = lj_energy(ff, distSq, ka + meta_kind(mj) * ff.n_kinds);
-          if (side) {
-            re += e;
-            lj += l;
-          } else {
-            re += -e;
-            lj += -l;
-          }
+          re += side ? e : -e;
+          lj += side ? l : -l;
+        }
+      }
+      icl_n = icl_warp[CT / 32];
+      __syncthreads();
+    }
+    // (2) Warp 3 evaluates the listed pairs (the FP64-heavy LJ and
+    //     erfc-screened Coulomb terms) while warps 0, 1, 2, 4, 5, 6 take the
+    //     k-vectors: with warps issued to the SM's four sub-partitions by
+    //     warp index modulo 4, the pair terms run beside the k-vectors
+    //     instead of after them.
+    const int n_eval = min(icl_n, ICL_MAX);
+    if (warp == 3) {
+      for (int i = lane; i < n_eval; i += 32) {
+        int u = icl_unit[i], s = icl_slot[i];
+        int a = u / (2 * NB27), side = (u / NB27) % 2;
+        double qa = b.q[b.mstart[m] + a];
+        int ka = b.kind[b.mstart[m] + a];
+        int mj = __ldcg(b.cell_meta + s);
+        double qj = __ldcg((const double *)(b.cell_pos + s) + 3);
+        double d2 = icl_d2[i];
+        double e = 0.0;
+        if (ff.electrostatic) {
+          double qq = qa * qj * QQ_FACT;
+          if (qq != 0.0)
+            e = coulomb_energy(ff, d2, qq);
+        }
+        double l = lj_energy(ff, d2, ka + meta_kind(mj) * ff.n_kinds);
+        if (side) {
+          re += e;
+          lj += l;
+        } else {
+          re += -e;
+          lj += -l;
         }
       }
     }
-    for (int i = threadIdx.x; i < kc; i += CT) {
-      char4 n = kn[i];
-      double rN = 0, iN = 0, rO = 0, iO = 0;
-      for (int a = 0; a < na; ++a) {
-        double q = S.hdr[72 + a];
-        if (q == 0.0)
-          continue;
-        const double2 *ro = tab + (size_t)(a * 3) * stride;
-        const double2 *rn = tab + (size_t)((na + a) * 3) * stride;
-        double2 eo = cmul2(cmul2(ro[n.x], tab_at(ro + stride, n.y)),
-                           tab_at(ro + 2 * stride, n.z));
-        double2 en = cmul2(cmul2(rn[n.x], tab_at(rn + stride, n.y)),
-                           tab_at(rn + 2 * stride, n.z));
-        rN += q * en.x;
-        iN += q * en.y;
-        rO += q * eo.x;
-        iO += q * eo.y;
+    if (warp != 3 && warp != 7) {
+      const int kw = warp < 3 ? warp : warp - 1;  // 0..5
+      for (int i = kw * 32 + lane; i < kc; i += 6 * 32) {
+        char4 n = kn[i];
+        double rN = 0, iN = 0, rO = 0, iO = 0;
+        for (int a = 0; a < na; ++a) {
+          double q = S.hdr[72 + a];
+          if (q == 0.0)
+            continue;
+          const double2 *ro = tab + (size_t)(a * 3) * stride;
+          const double2 *rn = tab + (size_t)((na + a) * 3) * stride;
+          double2 eo = cmul2(cmul2(ro[n.x], tab_at(ro + stride, n.y)),
+                             tab_at(ro + 2 * stride, n.z));
+          double2 en = cmul2(cmul2(rn[n.x], tab_at(rn + stride, n.y)),
+                             tab_at(rn + 2 * stride, n.z));
+          rN += q * en.x;
+          iN += q * en.y;
+          rO += q * eo.x;
+          iO += q * eo.y;
+        }
+        double srn = sR[i] + 1.0 * (rN - rO);
+        double sin_ = sI[i] + 1.0 * (iN - iO);
+        nR[i] = srn;
+        nI[i] = sin_;
+        er += (srn * srn + sin_ * sin_) * pf[i];
       }
-      double srn = sR[i] + 1.0 * (rN - rO);
-      double sin_ = sI[i] + 1.0 * (iN - iO);
-      nR[i] = srn;
-      nI[i] = sin_;
-      er += (srn * srn + sin_ * sin_) * pf[i];
     }
     double LJ = block_sum<CT>(lj, S.red);
     double RE = block_sum<CT>(re, S.red);
@@ -530,7 +696,16 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
     if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
       return;
     // ---------------- phase B ----------------
-    if (threadIdx.x < 32) {
+    // While warp 0 reduces the partials and decides, warps 1..7 build the
+    // next move's context: it does not depend on this decision unless the
+    // next move touches the same molecule or follows a settings adjustment
+    // (then it is built after the decision, as in the prologue).
+    const bool spec = t + 1 < A.n && A.moves[t + 1].mol != m &&
+                      (A.first + t + 2) % S.set.adj != 0;
+    if (threadIdx.x >= 32) {
+      if (spec)
+        build_ctx(A, S, t + 1, nullptr, 0, 32, CT - 32);
+    } else {
       double v[4] = {0, 0, 0, 0};
       constexpr int PF = 8;  // partial slots per lane loaded up front
       double2 pa[PF], pb[PF];
@@ -569,7 +744,17 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
         if (!over && b.K == 0)
           dRc = 0.0;
         double ex = __dmul_rn(-ff.beta, __dadd_rn(__dadd_rn(dLJ, dRe), dRc));
-        int res = S.hdr[3] < exp(ex);
+        // pacc < exp(ex), decided on logarithms unless the two sides are
+        // within 1e-9 (or pacc is 0): the outcome of the exp comparison
+        // without its FP64 exp on the critical path
+        double lp = S.hdr[80];
+        int res;
+        if (S.hdr[3] > 0.0 && ex > lp + 1e-9)
+          res = 1;
+        else if (S.hdr[3] > 0.0 && ex < lp - 1e-9)
+          res = 0;
+        else
+          res = S.hdr[3] < exp(ex);
         int acc = res && !over;
         if (acc) {
           S.e_run[0] += dLJ;
@@ -595,19 +780,39 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
         sR[i] = nR[i];
         sI[i] = nI[i];
       }
-      if (cta == 0 && threadIdx.x == 0) {
-        int a0 = b.mstart[m];
-        for (int a = 0; a < na; ++a) {
+      // The last CTA commits (coordinates, centre, cell slots) while CTA 0
+      // builds the next move's header.  Atoms that stay in their cell are
+      // rewritten in place by one lane each; then the atoms that change
+      // cell are relinked one after another, in atom order -- the slot
+      // layout that relinking every atom in order would give.
+      if (cta == G - 1 && threadIdx.x < 32) {
+        int a0 = b.mstart[m], a = threadIdx.x;
+        bool stay = false;
+        if (a < na) {
           const double *np = S.hdr + 48 + 3 * a;
           b.x[a0 + a] = np[0];
           b.y[a0 + a] = np[1];
           b.z[a0 + a] = np[2];
-          cell_move_atom(b, a0 + a, np[0], np[1], np[2], (int)S.hdr[16 + a]);
+          int c1 = (int)S.hdr[16 + a];
+          stay = __ldcg(b.atom_cell + a0 + a) == c1;
+          if (stay)
+            cell_write_slot(b, c1, __ldcg(b.atom_slot + a0 + a), a0 + a,
+                            np[0], np[1], np[2]);
         }
-        if ((int)S.hdr[1] == 0) {
-          b.cx[m] = S.hdr[4];
-          b.cy[m] = S.hdr[5];
-          b.cz[m] = S.hdr[6];
+        unsigned moving = __ballot_sync(0xffffffffu, a < na && !stay);
+        __syncwarp();
+        if (a == 0) {
+          for (int i = 0; i < na; ++i)
+            if (moving & (1u << i)) {
+              const double *np = S.hdr + 48 + 3 * i;
+              cell_move_atom(b, a0 + i, np[0], np[1], np[2],
+                             (int)S.hdr[16 + i]);
+            }
+          if ((int)S.hdr[1] == 0) {
+            b.cx[m] = S.hdr[4];
+            b.cy[m] = S.hdr[5];
+            b.cz[m] = S.hdr[6];
+          }
         }
       }
     }
@@ -621,7 +826,8 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
         if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
           return;
       }
-      build_ctx(A, S, t + 1, S.hdr, acc);
+      if (!spec)
+        build_ctx(A, S, t + 1, S.hdr, acc, 0, CT);
       if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
         return;
     }
