@@ -318,6 +318,8 @@ struct ChainShared {
   double e_run[5];
   double hdr[HDR];
   double red[CT / 32];
+  double red3[3][CT / 32];
+  int ovl_any;
   double tot[4];
   int accept, flag, ok;
   unsigned gen;
@@ -682,16 +684,31 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
         er += (srn * srn + sin_ * sin_) * pf[i];
       }
     }
-    double LJ = block_sum<CT>(lj, S.red);
-    double RE = block_sum<CT>(re, S.red);
-    double ER = block_sum<CT>(er, S.red);
-    double OV = block_sum<CT>(ovl, S.red);
-    if (threadIdx.x == 0) {
-      double *p = A.part + (size_t)cta * 4;
-      p[0] = LJ;
-      p[1] = RE;
-      p[2] = ER;
-      p[3] = OV > 0 ? 1.0 : 0.0;
+    // CTA partials: the three sums in one pass (warp shuffles, then lanes
+    // 0..2 of warp 0 each add one quantity over the warps, fixed order);
+    // the overlap flag by vote
+    {
+      double v0 = lj, v1 = re, v2 = er;
+      for (int o = 16; o > 0; o >>= 1) {
+        v0 += __shfl_down_sync(0xffffffffu, v0, o);
+        v1 += __shfl_down_sync(0xffffffffu, v1, o);
+        v2 += __shfl_down_sync(0xffffffffu, v2, o);
+      }
+      int any = __syncthreads_or(ovl > 0.0);
+      if (lane == 0) {
+        S.red3[0][warp] = v0;
+        S.red3[1][warp] = v1;
+        S.red3[2][warp] = v2;
+      }
+      __syncthreads();
+      if (threadIdx.x < 3) {
+        double r = 0.0;
+        for (int w = 0; w < CT / 32; ++w)
+          r += S.red3[threadIdx.x][w];
+        A.part[(size_t)cta * 4 + threadIdx.x] = r;
+        if (threadIdx.x == 0)
+          A.part[(size_t)cta * 4 + 3] = any ? 1.0 : 0.0;
+      }
     }
     if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
       return;
