@@ -433,6 +433,42 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
     return out
 
 
+def run_drift(args, dev, engine):
+    """One mixed chain over `--drift-moves` moves of the same workload with
+    the FP64 recompute every 10,000 moves; each window's relative difference
+    between the running energies and the recompute is recorded.  The chain
+    starts from the seeded lattice, so the first windows cover the melt of
+    the lattice (large energy changes, small |E|)."""
+    from gomc_gb300._lib import GB_MIXED
+    sysm, cfg = make_system(0)
+    b = engine.Box(sysm, cfg, device=dev, precision=GB_MIXED)
+    R = 10000
+    b.mc_init(SEED + 77, FRAC, ADJ, scales=SCALES, recompute_freq=R)
+    n = (args.drift_moves + R - 1) // R
+    t0 = time.perf_counter()
+    win = []
+    for w in range(n):
+        b.mc_run(w * R, R)
+        d = b.mc_drift()["last"]
+        win.append([d["inter"], d["real"], d["recip"], d["total"]])
+    wall = time.perf_counter() - t0
+    e = b.energy()
+    b.close()
+    win = np.array(win)
+    after = win[10:] if len(win) > 10 else win[-1:]
+    return {"moves": n * R, "recompute_every": R, "windows": n,
+            "wall_s": wall,
+            "total_max": float(win[:, 3].max()),
+            "total_first_window": float(win[0, 3]),
+            "total_max_after_100k_moves": float(after[:, 3].max()),
+            "windows_above_1e-8": int((win[:, 3] > 1e-8).sum()),
+            "term_max": {"inter": float(win[:, 0].max()),
+                         "real": float(win[:, 1].max()),
+                         "recip": float(win[:, 2].max())},
+            "energy_end_K": float(sum(e[:5])),
+            "bar": "total-energy drift <= 1e-8 relative between recomputes"}
+
+
 def run_serving(args, dev):
     """Serving stream on one GPU, scaled down from 256 jobs x 100 sweeps
     (the longest job alone then needs 2 x 20,000 sequential moves, the tail):
@@ -572,6 +608,9 @@ def run_gb300(args, rank, world):
     serving_stats = None
     if not args.no_serving and rank == 0:
         serving_stats = run_serving(args, dev)
+    drift_run = None
+    if args.drift_moves > 0 and rank == 0:
+        drift_run = run_drift(args, dev, engine)
 
     if rank != 0:
         if dist:
@@ -614,6 +653,8 @@ def run_gb300(args, rank, world):
         "mixed": mixed,
         "serving": serving_stats,
     }
+    if drift_run:
+        line["mixed_drift_run"] = drift_run
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -642,6 +683,9 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=64.0,
                     help="job arrivals per second (Poisson)")
     ap.add_argument("--serve-quantum", type=int, default=1000)
+    ap.add_argument("--drift-moves", type=int, default=0,
+                    help="also run one mixed chain this many moves and "
+                         "report the drift of every 10,000-move window")
     ap.add_argument("--small", action="store_true",
                     help="256-water box instead of the 8000-water workload")
     args = ap.parse_args()

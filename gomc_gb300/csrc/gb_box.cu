@@ -440,8 +440,29 @@ int Box::Init(const HostSystem &s0, const BoxConfig &c) {
         (rc = Alloc(&d.prefact_f, K)) || (rc = Alloc(&d.sumRref, K)) ||
         (rc = Alloc(&d.sumIref, K)) || (rc = Alloc(&d.sumRnew, K)) ||
         (rc = Alloc(&d.sumInew, K)) || (rc = Alloc(&d.krun, runs.size())) ||
-        (rc = Alloc(&d.krun_k, run_k.size())))
+        (rc = Alloc(&d.krun_k, run_k.size())) || (rc = Alloc(&d.cis256, 256)))
       return rc;
+    // exp(2 pi i j / 256) from the first octant by symmetry, each value
+    // split into FP32 hi + lo
+    std::vector<float4> cis(256);
+    for (int j = 0; j < 256; ++j) {
+      int o = j & 63;  // angle within its quarter turn, in 1/256 turns
+      bool flip = o > 32;
+      long double a = (flip ? 64 - o : o) * (3.14159265358979323846264338327950L / 128.0L);
+      double c = (double)cosl(a), sn = (double)sinl(a);
+      if (flip)
+        std::swap(c, sn);
+      double re, im;
+      switch (j >> 6) {
+        case 0: re = c; im = sn; break;
+        case 1: re = -sn; im = c; break;
+        case 2: re = -c; im = -sn; break;
+        default: re = sn; im = -c; break;
+      }
+      float rh = (float)re, ih = (float)im;
+      cis[j] = make_float4(rh, (float)(re - (double)rh), ih,
+                           (float)(im - (double)ih));
+    }
     if ((rc = up(d.kx, kx.data(), K * 8)) || (rc = up(d.ky, ky.data(), K * 8)) ||
         (rc = up(d.kz, kz.data(), K * 8)) ||
         (rc = up(d.prefact, pf.data(), K * 8)) ||
@@ -449,7 +470,8 @@ int Box::Init(const HostSystem &s0, const BoxConfig &c) {
         (rc = up(d.kn, kn.data(), K * 4)) ||
         (rc = up(d.krun, runs.data(), runs.size() * sizeof(int4))) ||
         (rc = up(d.krun_k, run_k.data(), run_k.size() * sizeof(int))) ||
-        (rc = up(d.prefact_f, pff.data(), K * 4)))
+        (rc = up(d.prefact_f, pff.data(), K * 4)) ||
+        (rc = up(d.cis256, cis.data(), 256 * sizeof(float4))))
       return rc;
   }
   if ((rc = GridAll()))
@@ -503,6 +525,8 @@ int Box::BoxInter(double *inter, double *real) {
 int Box::RecipSums(const double *x, const double *y, const double *z) {
   if (!cfg.ewald)
     return OK;
+  if (cfg.precision == 1)  // mixed form: float-float structure factor
+    return launch_recip_sums_ff(*this, x, y, z, dev.sumRnew, dev.sumInew);
   return launch_recip_sums(*this, x, y, z, dev.sumRnew, dev.sumInew);
 }
 

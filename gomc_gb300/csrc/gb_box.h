@@ -121,6 +121,8 @@ int launch_box_virial(Box &b, double *d_out6);
 int launch_virial_recip(Box &b, double *d_out6);
 int launch_recip_sums(Box &b, const double *x, const double *y,
                       const double *z, double *sumR, double *sumI);
+int launch_recip_sums_ff(Box &b, const double *x, const double *y,
+                         const double *z, double *sumR, double *sumI);
 int launch_recip_energy(Box &b, const double *sumR, const double *sumI,
                         double *d_out);
 int launch_mol_recip(Box &b, int m, const double *d_newpos, int sign_mode,

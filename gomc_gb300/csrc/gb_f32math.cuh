@@ -95,24 +95,27 @@ __device__ __forceinline__ float erfc_f32(float x) {
 }
 
 // ---- float-float (value = hi + lo, |lo| <= ulp(hi) / 2) ----
+// The error-free steps (the rounded sum or product whose error is recovered
+// next) use the _rn intrinsics, which the compiler never contracts into an
+// FMA with a neighbouring product.
 struct ff2 {
   float hi, lo;
 };
 __device__ __forceinline__ ff2 ff_quick(float a, float b) {  // |a| >= |b|
-  float s = a + b;
-  return {s, b - (s - a)};
+  float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
 }
 __device__ __forceinline__ ff2 ff_two_sum(float a, float b) {
-  float s = a + b;
-  float bp = s - a;
-  return {s, (a - (s - bp)) + (b - bp)};
+  float s = __fadd_rn(a, b);
+  float bp = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp))};
 }
 __device__ __forceinline__ ff2 ff_from_i64(long long v) {
   float hi = __ll2float_rn(v);
   return {hi, __ll2float_rn(v - (long long)hi)};
 }
 __device__ __forceinline__ ff2 ff_mul(ff2 a, ff2 b) {
-  float p = a.hi * b.hi;
+  float p = __fmul_rn(a.hi, b.hi);
   float e = fmaf(a.hi, b.hi, -p);
   e += fmaf(a.hi, b.lo, a.lo * b.hi);
   return ff_quick(p, e);
@@ -234,11 +237,67 @@ __device__ __forceinline__ ff2 close_coulomb(const ClosePair &c, bool ewald,
 }
 
 __device__ __forceinline__ void two_sum_add(float &hi, float &lo, float v) {
-  float s = hi + v;
-  float bp = s - hi;
-  float e = (hi - (s - bp)) + (v - bp);
-  hi = s;
-  lo += e;
+  ff2 s = ff_two_sum(hi, v);
+  hi = s.hi;
+  lo += s.lo;
+}
+
+// ---- complex float-float: float4 (re hi, re lo, im hi, im lo) ----
+__device__ __forceinline__ float4 ffc_mul(float4 a, float4 b) {
+  // re = a.re b.re - a.im b.im, im = a.re b.im + a.im b.re; the two leading
+  // products and their sum are error-free, the low-order cross terms are
+  // added in FP32.
+  float p1 = __fmul_rn(a.x, b.x), p2 = __fmul_rn(a.z, b.z);
+  float e1 = fmaf(a.x, b.x, -p1), e2 = fmaf(a.z, b.z, -p2);
+  ff2 s = ff_two_sum(p1, -p2);
+  float t = (e1 - e2) + s.lo;
+  t += fmaf(a.x, b.y, a.y * b.x) - fmaf(a.z, b.w, a.w * b.z);
+  ff2 re = ff_quick(s.hi, t);
+  float p3 = __fmul_rn(a.x, b.z), p4 = __fmul_rn(a.z, b.x);
+  float e3 = fmaf(a.x, b.z, -p3), e4 = fmaf(a.z, b.x, -p4);
+  ff2 u = ff_two_sum(p3, p4);
+  float v = (e3 + e4) + u.lo;
+  v += fmaf(a.x, b.w, a.y * b.z) + fmaf(a.z, b.y, a.w * b.x);
+  ff2 im = ff_quick(u.hi, v);
+  return make_float4(re.hi, re.lo, im.hi, im.lo);
+}
+__device__ __forceinline__ float4 ffc_conj_if(float4 a, bool neg) {
+  return neg ? make_float4(a.x, a.y, -a.z, -a.w) : a;
+}
+// (hi, lo) += v (float-float), renormalised
+__device__ __forceinline__ void ff_acc(float &hi, float &lo, float vh, float vl) {
+  ff2 s = ff_two_sum(hi, vh);
+  ff2 r = ff_quick(s.hi, s.lo + (lo + vl));
+  hi = r.hi;
+  lo = r.lo;
+}
+
+// exp(2 pi i u / 2^64) in float-float for a phase u given as an exact 64-bit
+// fraction of a turn.  u is rounded to the nearest 1/256 turn, whose cosine
+// and sine come from `tab` (256 entries, double values split into hi + lo);
+// the remainder |x| <= pi/256 takes the Taylor series
+// sin x = x - x^3 (1/6 - x^2/120) and cos x = 1 - x^2/2 + x^4/24 - x^6/720
+// (truncation below 1e-17): x, x^2, x^3 and 1/6 in float-float; x^2/120,
+// x^4/24 and x^6/720 in FP32 (their size is at most 1.3e-6 relative to the
+// term they correct, or 1e-9 absolute, so FP32 rounding stays below 1e-16).
+__device__ __forceinline__ float4 cis_turns64_ff(uint64_t u, const float4 *tab) {
+  uint64_t up = u + (1ULL << 55);
+  uint32_t j = (uint32_t)(up >> 56);
+  int64_t r = (int64_t)(u - ((uint64_t)j << 56));  // |r| <= 2^55
+  constexpr double TP = 6.283185307179586476925286766559 / 18446744073709551616.0;
+  constexpr float TP_HI = (float)TP;
+  constexpr float TP_LO = (float)(TP - (double)TP_HI);
+  constexpr float S6_HI = (float)(1.0 / 6.0);
+  constexpr float S6_LO = (float)(1.0 / 6.0 - (double)S6_HI);
+  ff2 x = ff_mul(ff_from_i64(r), {TP_HI, TP_LO});
+  ff2 x2 = ff_mul(x, x);
+  float h = x2.hi;
+  ff2 s3 = ff_mul(ff_mul(x, x2), ff_quick(S6_HI, S6_LO - h * (1.0f / 120.0f)));
+  ff2 sn = ff_add(x, {-s3.hi, -s3.lo});
+  float c4 = h * h * fmaf(h, -1.0f / 720.0f, 1.0f / 24.0f);
+  ff2 cs = ff_quick(1.0f, -0.5f * x2.hi);
+  cs = ff_quick(cs.hi, cs.lo + (c4 - 0.5f * x2.lo));
+  return ffc_mul(tab[j & 255], make_float4(cs.hi, cs.lo, sn.hi, sn.lo));
 }
 
 }  // namespace gb

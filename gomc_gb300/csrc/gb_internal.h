@@ -130,6 +130,7 @@ struct DevBox {
   int4 *krun;   // [nrun]
   int *krun_k;  // [nrun * KRUN]
   float *prefact_f;                       // [K]
+  float4 *cis256;  // [256] exp(2 pi i j / 256) as float-float (re, im)
   double *sumRref, *sumIref, *sumRnew, *sumInew;  // [K]
   // running energies: inter, real, recip, self, correction
   double *energy;

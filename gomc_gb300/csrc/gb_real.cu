@@ -54,51 +54,111 @@ __global__ void k_reduce_partials(const double *__restrict__ part, int n, int w,
 // ---------------------------------------------------------------------------
 // BoxInter
 // ---------------------------------------------------------------------------
+// A warp scans its 32 atoms of cell c against the neighbour cell with an
+// FP32 distance pre-filter (its radius padded beyond FP32 position
+// rounding) and queues the candidate pairs (i < j atom ids, other molecule)
+// in shared memory; every 32 queued pairs are evaluated in FP64 by the full
+// warp, with the exact FP64 cutoff test.  The FP64 energy work then scales
+// with the pairs inside the cutoff, not with the pairs scanned.
+constexpr int QW = 64;  // queue slots per warp
+
 __global__ void __launch_bounds__(RT) k_box_inter(DevBox b, const FF *__restrict__ pff,
                                                   double *part) {
   extern __shared__ __align__(32) unsigned char smem[];
+  __shared__ int2 queue[RT / 32][QW];
   const FF &ff = *pff;
   int tile = blockIdx.x;
   int c = tile / NB27, n = tile % NB27;
   int c2 = b.nbr[c * NB27 + n];
   int n1 = b.cell_count[c], n2 = b.cell_count[c2];
   double4_32a *sp = (double4_32a *)smem;
-  int *sm = (int *)(sp + b.cap);
+  float4 *sf = (float4 *)(sp + b.cap);
+  int *sm = (int *)(sf + b.cap);
   int *sa = sm + b.cap;
   for (int j = threadIdx.x; j < n2; j += RT) {
     size_t s = (size_t)c2 * b.cap + j;
-    sp[j] = b.cell_pos[s];
+    double4_32a p = b.cell_pos[s];
+    sp[j] = p;
+    sf[j] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.0f);
     sm[j] = b.cell_meta[s];
     sa[j] = b.cell_atom[s];
   }
   __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const float Lf[3] = {(float)b.L[0], (float)b.L[1], (float)b.L[2]};
+  const float Hf[3] = {(float)b.half[0], (float)b.half[1], (float)b.half[2]};
+  // FP32 positions are within L 2^-24 of the FP64 ones; the pre-filter
+  // radius covers twice that per axis plus 1e-4 of Rcut^2
+  const double lmax = fmax(b.L[0], fmax(b.L[1], b.L[2]));
+  const double rpad = ff.rcut + 1e-6 * lmax;
+  const float cut_f = (float)(rpad * rpad * 1.0001);
+  int2 *q = queue[warp];
   double lj = 0.0, re = 0.0;
-  for (int i = threadIdx.x; i < n1; i += RT) {
-    size_t si = (size_t)c * b.cap + i;
-    double4_32a pi = b.cell_pos[si];
-    int mi = b.cell_meta[si], ai = b.cell_atom[si];
-    int moli = meta_mol(mi), ki = meta_kind(mi);
+  // FP64 energy of queued pair e (slot of cell c, slot of the neighbour cell)
+  auto eval = [&](int2 e) {
+    double4_32a pi = b.cell_pos[(size_t)c * b.cap + e.x];
+    double4_32a pj = sp[e.y];
+    double dx = min_image(pi.x - pj.x, b.L[0], b.half[0]);
+    double dy = min_image(pi.y - pj.y, b.L[1], b.half[1]);
+    double dz = min_image(pi.z - pj.z, b.L[2], b.half[2]);
+    double distSq = dsq3(dx, dy, dz);
+    if (ff.rcutSq > distSq) {
+      int ki = meta_kind(b.cell_meta[(size_t)c * b.cap + e.x]);
+      int kj = meta_kind(sm[e.y]);
+      if (ff.electrostatic) {
+        double qq = pi.w * pj.w * QQ_FACT;
+        if (qq != 0.0)
+          re += coulomb_energy(ff, distSq, qq);
+      }
+      lj += lj_energy(ff, distSq, ki + kj * ff.n_kinds);
+    }
+  };
+  int qn = 0;  // warp-uniform queue fill
+  for (int i0 = warp * 32; i0 < n1; i0 += RT) {
+    int i = i0 + lane;
+    bool act = i < n1;
+    int ai = -1, moli = -1;
+    float px = 0.0f, py = 0.0f, pz = 0.0f;
+    if (act) {
+      size_t si = (size_t)c * b.cap + i;
+      double4_32a p = b.cell_pos[si];
+      px = (float)p.x;
+      py = (float)p.y;
+      pz = (float)p.z;
+      ai = b.cell_atom[si];
+      moli = meta_mol(b.cell_meta[si]);
+    }
     for (int j = 0; j < n2; ++j) {
-      int aj = sa[j];
-      int mj = sm[j];
-      if (ai < aj && moli != meta_mol(mj)) {
-        double4_32a pj = sp[j];
-        double dx = min_image(pi.x - pj.x, b.L[0], b.half[0]);
-        double dy = min_image(pi.y - pj.y, b.L[1], b.half[1]);
-        double dz = min_image(pi.z - pj.z, b.L[2], b.half[2]);
-        double distSq = dsq3(dx, dy, dz);
-        if (ff.rcutSq > distSq) {
-          int kj = meta_kind(mj);
-          if (ff.electrostatic) {
-            double qq = pi.w * pj.w * QQ_FACT;
-            if (qq != 0.0)
-              re += coulomb_energy(ff, distSq, qq);
-          }
-          lj += lj_energy(ff, distSq, ki + kj * ff.n_kinds);
-        }
+      bool in = false;
+      if (act && ai < sa[j] && moli != meta_mol(sm[j])) {
+        float4 pj = sf[j];
+        float dx = px - pj.x, dy = py - pj.y, dz = pz - pj.z;
+        dx = dx > Hf[0] ? dx - Lf[0] : dx < -Hf[0] ? dx + Lf[0] : dx;
+        dy = dy > Hf[1] ? dy - Lf[1] : dy < -Hf[1] ? dy + Lf[1] : dy;
+        dz = dz > Hf[2] ? dz - Lf[2] : dz < -Hf[2] ? dz + Lf[2] : dz;
+        in = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < cut_f;
+      }
+      unsigned m = __ballot_sync(0xffffffffu, in);
+      if (in)
+        q[qn + __popc(m & lt)] = make_int2(i, j);
+      qn += __popc(m);
+      if (qn >= 32) {
+        __syncwarp();
+        eval(q[lane]);
+        int rest = qn - 32;
+        int2 mv = lane < rest ? q[32 + lane] : make_int2(0, 0);
+        __syncwarp();
+        if (lane < rest)
+          q[lane] = mv;
+        __syncwarp();
+        qn = rest;
       }
     }
   }
+  __syncwarp();
+  if (lane < qn)
+    eval(q[lane]);
   __shared__ double red[RT / 32];
   double a = block_sum<RT>(lj, red);
   double r = block_sum<RT>(re, red);
@@ -195,7 +255,8 @@ int launch_box_inter(Box &bx, double *d_out2) {
   int rc = bx.EnsureScratch((size_t)tiles * 2);
   if (rc)
     return rc;
-  size_t sh = (size_t)b.cap * (sizeof(double4_32a) + 2 * sizeof(int));
+  size_t sh = (size_t)b.cap * (sizeof(double4_32a) + sizeof(float4) +
+                                2 * sizeof(int));
   raise_smem_limit((const void *)k_box_inter, sh);
   k_box_inter<<<tiles, RT, sh, bx.stream>>>(b, bx.d_ff, bx.d_scratch);
   k_reduce_partials<<<1, RT, 0, bx.stream>>>(bx.d_scratch, tiles, 2, d_out2, 0);

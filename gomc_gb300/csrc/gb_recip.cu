@@ -16,6 +16,7 @@
 // structure factor: runs of consecutive n_x) and one chunk of atoms, and
 // chunk partials are added in a fixed order.
 #include "gb_box.h"
+#include "gb_f32math.cuh"
 #include "gb_pair.cuh"
 
 namespace gb {
@@ -136,6 +137,105 @@ __global__ void k_recip_chunk_sum(int K, int nch, const double *__restrict__ par
   sumI[k] = i;
 }
 
+// Structure factor in float-float arithmetic, the set-up and periodic
+// recompute of the mixed form.  Positions enter as exact 64-bit fractions of
+// a turn (u = r / L 2^64), so every phase n u is exact integer arithmetic;
+// each CTA tile builds the rows exp(2 pi i n u / 2^64), n = 0..kmax, of its
+// atoms directly from the phase (no recurrence), the x row scaled by the
+// atom's charge, and a thread's run of k-vectors takes
+// q exp(i n_x t_x) * (exp(i n_y t_y) exp(i n_z t_z)) per member, summed in
+// float-float.  Each term carries a relative error of a few 2^-48, about
+// 1e-14, against 1e-16 for the FP64 kernel above, at the FP32 rate.
+constexpr int TAF = 16;  // atoms per tile
+
+__global__ void __launch_bounds__(KT) k_recip_sums_ff(DevBox b,
+                                                      const double *__restrict__ X,
+                                                      const double *__restrict__ Y,
+                                                      const double *__restrict__ Z,
+                                                      int nch, double *part) {
+  extern __shared__ float4 rows[];  // [TAF][3][kmax + 1]
+  __shared__ float4 ctab[256];
+  __shared__ unsigned long long tu[TAF * 3];
+  __shared__ float2 qs[TAF];
+  const int stride = b.kmax + 1;
+  for (int i = threadIdx.x; i < 256; i += KT)
+    ctab[i] = b.cis256[i];
+  const int run = blockIdx.x * KT + threadIdx.x;
+  const int ch = blockIdx.y;
+  const int a_begin = (int)((long long)b.n_atoms * ch / nch);
+  const int a_end = (int)((long long)b.n_atoms * (ch + 1) / nch);
+  const int4 rn = run < b.nrun ? b.krun[run] : make_int4(0, 0, 0, 0);
+  float rh[KRUN], rl[KRUN], ih[KRUN], il[KRUN];
+#pragma unroll
+  for (int g = 0; g < KRUN; ++g) {
+    rh[g] = 0.0f;
+    rl[g] = 0.0f;
+    ih[g] = 0.0f;
+    il[g] = 0.0f;
+  }
+  const int per_atom = 3 * stride;
+  for (int a0 = a_begin; a0 < a_end; a0 += TAF) {
+    const int na = min(TAF, a_end - a0);
+    __syncthreads();
+    if (threadIdx.x < na * 3) {
+      int a = threadIdx.x / 3, d = threadIdx.x % 3;
+      int atom = a0 + a;
+      double coord = d == 0 ? X[atom] : d == 1 ? Y[atom] : Z[atom];
+      double t = coord * b.invL[d];
+      t -= floor(t);
+      tu[threadIdx.x] = __double2ull_rn(t * 18446744073709551616.0);  // 2^64
+    }
+    if (threadIdx.x < na) {
+      double q = b.q[a0 + threadIdx.x];
+      if (fabs(q) < 0.000000001)
+        q = 0.0;
+      float hi = (float)q;
+      qs[threadIdx.x] = make_float2(hi, (float)(q - (double)hi));
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < na * per_atom; e += KT) {
+      int a = e / per_atom;
+      int r = e - a * per_atom;
+      int d = r / stride;
+      int n = r - d * stride;
+      float4 v = cis_turns64_ff(tu[a * 3 + d] * (unsigned long long)n, ctab);
+      if (d == 0) {
+        float2 q = qs[a];
+        ff2 re = ff_mul({v.x, v.y}, {q.x, q.y});
+        ff2 im = ff_mul({v.z, v.w}, {q.x, q.y});
+        v = make_float4(re.hi, re.lo, im.hi, im.lo);
+      }
+      rows[e] = v;
+    }
+    __syncthreads();
+    for (int a = 0; a < na; ++a) {
+      if (qs[a].x == 0.0f)
+        continue;
+      const float4 *ex = rows + a * per_atom;
+      const float4 *ey = ex + stride;
+      const float4 *ez = ey + stride;
+      float4 eyz = ffc_mul(ffc_conj_if(ey[abs(rn.x)], rn.x < 0),
+                           ffc_conj_if(ez[abs(rn.y)], rn.y < 0));
+#pragma unroll
+      for (int g = 0; g < KRUN; ++g) {
+        float4 v = ffc_mul(ex[min(rn.z + g, b.kmax)], eyz);
+        ff_acc(rh[g], rl[g], v.x, v.y);
+        ff_acc(ih[g], il[g], v.z, v.w);
+      }
+    }
+  }
+  if (run < b.nrun) {
+#pragma unroll
+    for (int g = 0; g < KRUN; ++g) {
+      if (g < rn.w) {
+        int k = b.krun_k[(size_t)run * KRUN + g];
+        part[((size_t)ch * b.K + k) * 2] = (double)rh[g] + (double)rl[g];
+        part[((size_t)ch * b.K + k) * 2 + 1] = (double)ih[g] + (double)il[g];
+      }
+    }
+  }
+}
+
 static int recip_chunks(const Box &bx) {
   int kb = (bx.dev.nrun + KT - 1) / KT;
   int want = (4 * bx.sm_count + kb - 1) / kb;
@@ -159,6 +259,25 @@ int launch_recip_sums(Box &bx, const double *x, const double *y,
   k_recip_chunk_sum<<<(b.K + 255) / 256, 256, 0, bx.stream>>>(
       b.K, nch, bx.d_scratch, sumR, sumI);
   return bx.CudaCheck(cudaGetLastError(), "recip sums");
+}
+
+int launch_recip_sums_ff(Box &bx, const double *x, const double *y,
+                         const double *z, double *sumR, double *sumI) {
+  DevBox &b = bx.dev;
+  int kb = (b.nrun + KT - 1) / KT;
+  int want = (4 * bx.sm_count + kb - 1) / kb;
+  int nch = std::max(1, std::min(NCH_MAX, want));
+  nch = std::min(nch, std::max(1, b.n_atoms / TAF));
+  int rc = bx.EnsureScratch((size_t)nch * b.K * 2);
+  if (rc)
+    return rc;
+  size_t sh = (size_t)TAF * 3 * (b.kmax + 1) * sizeof(float4);
+  raise_smem_limit((const void *)k_recip_sums_ff, sh);
+  k_recip_sums_ff<<<dim3(kb, nch), KT, sh, bx.stream>>>(b, x, y, z, nch,
+                                                        bx.d_scratch);
+  k_recip_chunk_sum<<<(b.K + 255) / 256, 256, 0, bx.stream>>>(
+      b.K, nch, bx.d_scratch, sumR, sumI);
+  return bx.CudaCheck(cudaGetLastError(), "recip sums (float-float)");
 }
 
 // ---------------------------------------------------------------------------

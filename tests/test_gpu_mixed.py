@@ -6,7 +6,9 @@ recompute; per-move energy changes within 1e-2 K (3.4e-5 kT at 298 K) or
 changes of a few thousand K, e.g. hydrogen-bonded O-H pairs, leaves a few
 1e-3 K); the same accept/reject sequence as the FP64
 chain over the compared moves; total-energy drift at most 1e-8 relative
-between full FP64 recomputes every 10,000 moves; a box run inside a batched
+between full FP64 recomputes every 10,000 moves; the mixed box's own
+recompute (float-float structure factor) within 1e-11 of the FP64 box's on
+the same coordinates; a box run inside a batched
 launch gives bit-identical state to the same box run alone over the same
 call boundaries (each call ends by folding the FP32 window of accepted
 structure-factor changes into the FP64 accumulators).
@@ -23,6 +25,7 @@ TERM_REL = 1e-6      # running energy term vs FP64 recompute
 DE_ABS = 1e-2        # per-move dE, K
 DE_REL = 1e-4
 DRIFT_REL = 1e-8     # total energy between recomputes
+RECOMP_REL = 1e-11   # mixed-box recompute vs FP64 recompute, reciprocal term
 SCALES = [0.3, 0.3, 0.02, 0.03]
 
 # (molecules, box edge A, cutoff A): the 256-water box has cells narrower
@@ -64,6 +67,12 @@ def test_mixed_follows_fp64(gb, nmol, L, rc):
     for i, term in enumerate(["inter", "real", "recip"]):
         rel = abs(run[i] - st[term]) / abs(st[term])
         assert rel <= TERM_REL, (term, rel)
+    # the mixed box's recompute (float-float structure factor from exact
+    # 64-bit phases) against the FP64 box's on the same coordinates
+    sf = bf.system_total()
+    for term, tol in (("inter", 1e-13), ("real", 1e-13), ("recip", RECOMP_REL)):
+        rel = abs(st[term] - sf[term]) / abs(sf[term])
+        assert rel <= tol, (term, rel)
     # both chains moved the same molecules to the same places (to FP64
     # rounding of the shared proposal arithmetic, which is identical)
     np.testing.assert_array_equal(bm.coords(), bf.coords())
