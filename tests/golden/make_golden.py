@@ -60,6 +60,25 @@ FIXTURES = {
                         adj_steps=10, dis_freq=1.0, rot_freq=0.0,
                         random_seed=777),
               1500, 32),
+    # the two boxes of the GEMC configuration, each as its own NVT box: the
+    # energy calls its moves make (BoxInter, GridAll, ParticleInter, single
+    # particle displacements).  Liquid: 2,400 spheres in 40 A (3 cells per
+    # axis); vapour: 300 in 90 A (7 cells per axis).  Random placement at
+    # the liquid's density needs a closest approach below sigma.
+    "c3_liquid": (lambda: lj_sphere_box(2400, 40.0, seed=31, epsilon=148.0,
+                                        sigma=3.73, min_sep=2.4, name="LJ"),
+                  SimConfig(temperature=150.0, rcut=12.0, ewald=False,
+                            electrostatic=False, run_steps=1000, eq_steps=500,
+                            adj_steps=10, dis_freq=1.0, rot_freq=0.0,
+                            random_seed=3131),
+                  1000, 32),
+    "c3_vapour": (lambda: lj_sphere_box(300, 90.0, seed=32, epsilon=148.0,
+                                        sigma=3.73, min_sep=3.5, name="LJ"),
+                  SimConfig(temperature=150.0, rcut=12.0, ewald=False,
+                            electrostatic=False, run_steps=1500, eq_steps=1000,
+                            adj_steps=10, dis_freq=1.0, rot_freq=0.0,
+                            random_seed=3232),
+                  1500, 32),
 }
 
 

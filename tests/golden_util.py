@@ -8,7 +8,7 @@ from gomc_gb300.config import SimConfig
 from gomc_gb300.systems import AtomKind, MoleculeType, MolSystem
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-NAMES = ["c0_water", "c0_water_mp", "w1728", "lj500"]
+NAMES = ["c0_water", "c0_water_mp", "w1728", "lj500", "c3_liquid", "c3_vapour"]
 
 
 def load(name):
