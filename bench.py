@@ -405,12 +405,15 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_e2e = float(tt.item())
     per_box = (sysm.n_atoms + sysm.n_mol) * 3 * 8
-    drift = {"max": {}, "recomputes": 0}
+    drift = {"max": {}, "latest_window_max": {}, "recomputes": 0}
     for b in boxes:
         d = b.mc_drift()
         drift["recomputes"] += d["recomputes"]
         for k, v in d["max"].items():
             drift["max"][k] = max(drift["max"].get(k, 0.0), v)
+        for k, v in d["last"].items():
+            drift["latest_window_max"][k] = max(
+                drift["latest_window_max"].get(k, 0.0), v)
     for b in boxes:
         b.close()
     out["batched"] = {
@@ -428,7 +431,9 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
                   "h2d_bytes_per_step": B * (per_box + M * 64),
                   "d2h_bytes_per_step": B * (5 * 8 + per_box)}
     out["drift"] = dict(drift, recompute_every=10000,
-                        bar="total-energy drift <= 1e-8 relative")
+                        bar="total-energy drift <= 1e-8 relative",
+                        note="every replica starts from its own lattice; "
+                             "max includes the first window (lattice melt)")
     out["dtype"] = "f32 pair/k terms, f64 accumulators"
     return out
 

@@ -10,10 +10,10 @@
 namespace gb {
 
 void raise_smem_limit(const void *func, size_t bytes) {
+  // The opt-in is needed whenever static plus dynamic shared memory passes
+  // 48 KiB, so it is set for every size (once per device, kernel and size).
   static std::mutex mu;
   static std::map<std::pair<int, const void *>, size_t> limit;
-  if (bytes <= 48 * 1024)
-    return;
   int dev = 0;
   cudaGetDevice(&dev);  // the attribute belongs to the current device
   std::lock_guard<std::mutex> g(mu);
@@ -109,6 +109,64 @@ void build_ff(const HostSystem &s, const BoxConfig &c, FF *ff) {
   ff->sc_sigma_6 = std::pow(c.sc_sigma, 6.0);
   ff->sc_power = c.sc_power;
   ff->sc_coul = c.sc_coul;
+}
+
+// ---------------------------------------------------------------------------
+// Table of erfc(alpha r) / r over r^2 in [0.5, 2^e1) A^2, 2^e1 > s_max: per
+// segment (64 per binade) the degree-8 Chebyshev interpolant at 9 first-kind
+// Chebyshev nodes, computed in long double and stored as monomial
+// coefficients in u = 2 (s - a) / h - 1.  Interpolation error below 1.1e-16
+// relative on [0.5, 100] for alpha = 0.339 (degree 6 reached only 2e-14 in
+// the widest segments, where exp(-alpha^2 r^2) bends most per segment).
+// ---------------------------------------------------------------------------
+static void erfc_table(double alpha, double s_max, std::vector<double> &tab,
+                       int *key0, int *nseg) {
+  constexpr int D = ETAB_DEG, NC = ETAB_DEG + 1;
+  const int E0 = -1;
+  int e1 = E0;
+  while (std::ldexp(1.0, e1) <= s_max)
+    ++e1;
+  *nseg = (e1 - E0) * 64;
+  *key0 = (1023 + E0) << 6;
+  tab.assign((size_t)*nseg * NC, 0.0);
+  const long double al = alpha;
+  const long double pi = 3.14159265358979323846264338327950288L;
+  long double node[NC], tk[NC][NC];  // nodes; T_k(node_i)
+  for (int i = 0; i < NC; ++i) {
+    node[i] = cosl(pi * (i + 0.5L) / NC);
+    for (int k = 0; k < NC; ++k)
+      tk[k][i] = cosl(pi * k * (i + 0.5L) / NC);
+  }
+  // power-basis coefficients of T_0..T_D
+  long double mono[NC][NC] = {};
+  mono[0][0] = 1.0L;
+  mono[1][1] = 1.0L;
+  for (int k = 1; k < D; ++k)
+    for (int m = 0; m < NC; ++m)
+      mono[k + 1][m] = (m > 0 ? 2.0L * mono[k][m - 1] : 0.0L) - mono[k - 1][m];
+  for (int seg = 0; seg < *nseg; ++seg) {
+    int bin = seg / 64, j = seg % 64;
+    long double w = ldexpl(1.0L, E0 + bin);
+    long double a = w * (1.0L + j / 64.0L), h = w / 64.0L;
+    long double f[NC], c[NC];
+    for (int i = 0; i < NC; ++i) {
+      long double sv = a + h * (node[i] + 1.0L) * 0.5L;
+      long double r = sqrtl(sv);
+      f[i] = erfcl(al * r) / r;
+    }
+    for (int k = 0; k < NC; ++k) {
+      long double acc = 0.0L;
+      for (int i = 0; i < NC; ++i)
+        acc += f[i] * tk[k][i];
+      c[k] = acc * (2.0L / NC) * (k == 0 ? 0.5L : 1.0L);
+    }
+    for (int m = 0; m < NC; ++m) {
+      long double p = 0.0L;
+      for (int k = 0; k < NC; ++k)
+        p += c[k] * mono[k][m];
+      tab[(size_t)seg * NC + m] = (double)p;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -394,8 +452,20 @@ int Box::Init(const HostSystem &s0, const BoxConfig &c) {
       (rc = up(d.kind, s.kind.data(), N * 4)) ||
       (rc = up(d.mol, s.mol.data(), N * 4)) ||
       (rc = up(d.mstart, s.mstart.data(), (M + 1) * 4)) ||
-      (rc = up(d.nbr, nbr.data(), nbr.size() * 4)) ||
-      (rc = up(d_ff, &ff, sizeof(FF))))
+      (rc = up(d.nbr, nbr.data(), nbr.size() * 4)))
+    return rc;
+  ff.erfc_tab = nullptr;
+  ff.etab_key0 = ff.etab_nseg = 0;
+  if (c.ewald) {
+    std::vector<double> et;
+    double *d_et = nullptr;
+    erfc_table(ff.alpha, ff.rcutCoulSq, et, &ff.etab_key0, &ff.etab_nseg);
+    if ((rc = Alloc(&d_et, et.size())) ||
+        (rc = up(d_et, et.data(), et.size() * sizeof(double))))
+      return rc;
+    ff.erfc_tab = d_et;
+  }
+  if ((rc = up(d_ff, &ff, sizeof(FF))))
     return rc;
   if ((rc = CudaCheck(cudaMemsetAsync(d.err, 0, 16, stream), "memset")) ||
       (rc = CudaCheck(cudaMemsetAsync(d.energy, 0, 64, stream), "memset")))

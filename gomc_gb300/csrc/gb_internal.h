@@ -21,6 +21,7 @@ constexpr double QQ_FACT = 167103.208067979;  // lib/NumLib.h:22
 constexpr double SQRT_QQ_FACT = 408.7825926675193;
 constexpr int NB27 = 27;
 constexpr int MAX_KINDS = 8;
+constexpr int ETAB_DEG = 8;  // degree of the erfc(alpha r)/r segments
 constexpr int MAX_MOL_ATOMS = 8;   // rigid molecules handled by the move loop
 constexpr int END_CELL = -1;
 constexpr int KRUN = 8;  // k-vectors per run of the structure-factor kernel
@@ -57,6 +58,11 @@ struct FF {
   double nexp[MAX_KINDS * MAX_KINDS];
   double eps_cn_6[MAX_KINDS * MAX_KINDS];
   double nOver6[MAX_KINDS * MAX_KINDS];
+  // erfc(alpha r) / r as piecewise degree-8 polynomials in r^2 (Ewald
+  // only): 64 segments per binade of r^2 from 0.5 A^2, 9 coefficients each;
+  // segment of r^2 = (its IEEE exponent and top 6 mantissa bits) - key0
+  const double *erfc_tab;
+  int etab_key0, etab_nseg;
   // soft-core settings at lambda < 1 (Forcefield::sc_*,
   // src/Forcefield.cpp:59-75)
   double sc_alpha, sc_sigma_6;

@@ -204,6 +204,66 @@ __device__ bool grid_sync(unsigned *bar, unsigned nblocks, unsigned &gen,
   return *s_flag != 0;
 }
 
+// Wait (one thread) until *p >= target; bounded like grid_sync.  Returns
+// false when the wait gives up (DERR_BARRIER_TIMEOUT) or another CTA has
+// reported an error.
+__device__ bool wait_geq(const unsigned *p, unsigned target, int *err,
+                         bool backoff = false) {
+  unsigned it = 0;
+  while ((int)(ld_acquire(p) - target) < 0) {
+    if (backoff)
+      __nanosleep(64);
+    if (++it > SPIN_LIMIT) {
+      atomicOr(err, DERR_BARRIER_TIMEOUT);
+      return false;
+    }
+    if ((it & 255u) == 0 && *(volatile int *)err)
+      return false;
+  }
+  __threadfence();
+  return *(volatile int *)err == 0;
+}
+
+__global__ void k_fill_u64(unsigned long long *p, int n, unsigned long long v) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    p[i] = v;
+}
+
+// Wait (one warp) until flags[c] >= target for every c < n: each lane
+// loads its flags together, then the warp votes, so a round of checks costs
+// one memory round trip.  Bounded like grid_sync.
+__device__ bool warp_wait_all(const unsigned *flags, int n, unsigned target,
+                              int *err) {
+  const int lane = threadIdx.x & 31;
+  unsigned it = 0;
+  for (;;) {
+    bool mine = true;
+#pragma unroll 4
+    for (int c = lane; c < n; c += 32)
+      mine &= (int)(*(const volatile unsigned *)(flags + c) - target) >= 0;
+    if (__all_sync(0xffffffffu, mine))
+      break;
+    int bad = 0;
+    if (lane == 0) {
+      if (++it > SPIN_LIMIT) {
+        atomicOr(err, DERR_BARRIER_TIMEOUT);
+        bad = 1;
+      } else if ((it & 255u) == 0 && *(volatile int *)err) {
+        bad = 1;
+      }
+    }
+    if (__shfl_sync(0xffffffffu, bad, 0))
+      return false;
+  }
+  __threadfence();
+  return true;
+}
+
+__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // Apply a stored proposal to the atoms of molecule m.
 // kind 0: shift (Coordinates::TranslateRand, src/Coordinates.cpp:83-100)
 // kind 1: rotation about the molecule centre (RotateRand, :103-128)
@@ -293,6 +353,21 @@ __device__ __forceinline__ double2 tab_at(const double2 *row, int n) {
 constexpr int CT = 256;
 constexpr int HDR = 96;  // doubles in the move-context header
 constexpr int ICL_MAX = 256;  // in-cutoff pairs a CTA lists per move
+constexpr int SEQ_PART = 32;      // words; the decision word has its own line
+// A CTA's partial slots hold this NaN pattern until written: the leader
+// polls the values themselves (each 8-byte store is single-copy atomic), so
+// no separate arrival flag, fence or atomic is needed
+constexpr unsigned long long PART_EMPTY = 0x7FF4C0DE7FF4C0DEULL;
+constexpr int PART_MAX_GRID = 256;  // partial slots the leader holds per lane: 8
+constexpr int SEQ_STRIDE = 1024;  // words per per-CTA flag array (grid <= 1024)
+constexpr int NPAIR_CAP = 64; // (n_x, n_y) columns a CTA's k-chunk may span
+                              // for the shared x-y phase products
+
+// doubles of one move context: the header and 2 MAX_MOL_ATOMS x 3 phase
+// rows of kmax + 1 double2 entries
+__host__ __device__ constexpr size_t chain_ctx_len(int stride) {
+  return HDR + 2 * (size_t)(2 * MAX_MOL_ATOMS * 3) * stride;
+}
 
 // Context header layout (doubles):
 //  0 m, 1 kind, 2 na, 3 pacc, 4..6 newcom, 8..15 cell old, 16..23 cell new,
@@ -306,9 +381,14 @@ struct ChainArgs {
   double *prop;   // [n][12]
   int64_t first;
   int n;
-  double *part;   // [grid][4]
-  unsigned *bar;
-  double *ctx;    // HDR + tables
+  double *part;   // [2][grid][4], by move parity
+  unsigned *bar;  // [0..1] grid barrier
+  unsigned *seq;  // [0] decision published (2 (t + 1) + accept); from
+                  // SEQ_PART: per CTA, partials of move t written (t + 1);
+                  // from SEQ_PART + SEQ_STRIDE: per CTA, its part of the
+                  // context of move t written (t)
+  double *ctx;    // [2][ctx_len], by move parity: HDR + tables
+  size_t ctx_len;
   int *tr_i;      // [n][3] or null
   double *tr_d;   // [n][3] or null
 };
@@ -340,7 +420,7 @@ __device__ __forceinline__ void group_sync(int count) {
 // warps; count >= 64).
 __device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
                           const double *prev_hdr, int prev_acc, int first,
-                          int count) {
+                          int count, bool report = false) {
   const int tid = (int)threadIdx.x - first;
   const DevBox &b = A.b;
   const MoveRec &r = A.moves[t];
@@ -401,8 +481,9 @@ __device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
     newcom[d] = r.kind == 0 ? wrap1(__dadd_rn(com[d], prop[d]), b.L[d]) : com[d];
   }
   group_sync(count);
+  double *const ctx = A.ctx + (size_t)(t & 1) * A.ctx_len;
   if (header_cta) {
-    double *h = A.ctx;
+    double *h = ctx;
     if (tid == 0) {
       h[0] = m;
       h[1] = r.kind;
@@ -427,7 +508,7 @@ __device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
   // phase rows exp(i n 2 pi r_d / L_d), n = 0..kmax, one entry per thread:
   // the coordinate as a 64-bit fraction of the box edge, n times it exact
   // modulo one turn
-  double2 *tab = (double2 *)(A.ctx + HDR);
+  double2 *tab = (double2 *)(ctx + HDR);
   for (int rr = blockIdx.x; rr < nrows; rr += G) {
     int p = rr / 3, d = rr % 3;
     double coord = p < na ? oldp[p][d] : newp[p - na][d];
@@ -438,9 +519,26 @@ __device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
     for (int n = tid; n < stride; n += count)
       tab[(size_t)rr * stride + n] = cis_turns64((uint64_t)n * u);
   }
+  if (report) {
+    // this CTA's part of the context is written: flag it for the leader
+    group_sync(count);
+    if (tid == 0) {
+      __threadfence();
+      st_release(A.seq + SEQ_PART + SEQ_STRIDE + blockIdx.x, (unsigned)t);
+    }
+  }
 }
 
-__global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
+// CTAs that write part of move t's context: CTA 0 (header) and one CTA
+// per phase row.
+__device__ __forceinline__ unsigned ctx_builders(const ChainArgs &A, int t) {
+  int m = A.moves[t].mol;
+  int na = A.b.mstart[m + 1] - A.b.mstart[m];
+  int nrows = A.b.K > 0 ? 2 * na * 3 : 0;
+  return (unsigned)max(1, min((int)gridDim.x, nrows));
+}
+
+__global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
   extern __shared__ double dyn[];
   __shared__ ChainShared S;
   const DevBox &b = A.b;
@@ -454,6 +552,15 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
   char4 *kn = (char4 *)(pf + kc_max);
   int stride = b.kmax + 1;
   double2 *tab = (double2 *)(dyn + ((5 * kc_max + (kc_max + 1) / 2 + 1) & ~1));
+  // The k-chunk lists k-vectors x outer, y, z inner, so it spans a few
+  // (n_x, n_y) columns; per move the products exp(i n_x t_x) exp(i n_y t_y)
+  // are formed once per column and atom, and each k-vector multiplies in
+  // its exp(i n_z t_z) -- the same products, in the same order, as forming
+  // all three per k-vector.
+  double2 *exy = tab + (size_t)(2 * MAX_MOL_ATOMS * 3) * (b.kmax + 1);
+  unsigned short *pidx = (unsigned short *)(exy + NPAIR_CAP * 2 * MAX_MOL_ATOMS);
+  __shared__ char2 pair_n[NPAIR_CAP];
+  __shared__ int npair;
   for (int i = threadIdx.x; i < kc; i += CT) {
     int k = kbeg + i;
     sR[i] = b.sumRref[k];
@@ -466,6 +573,22 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
     for (int i = 0; i < 5; ++i)
       S.e_run[i] = b.energy[i];
     S.gen = ld_acquire(&A.bar[1]);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int np = 0;
+    for (int i = 0; i < kc && np >= 0; ++i) {
+      char4 n = kn[i];
+      if (np == 0 || pair_n[np - 1].x != n.x || pair_n[np - 1].y != n.y) {
+        if (np == NPAIR_CAP) {
+          np = -1;  // too many columns: form all three products per k
+          break;
+        }
+        pair_n[np++] = make_char2(n.x, n.y);
+      }
+      pidx[i] = (unsigned short)(np - 1);
+    }
+    npair = np;
   }
   __syncthreads();
 
@@ -497,14 +620,15 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
 
   for (int t = 0; t < A.n; ++t) {
     // ---------------- phase A ----------------
+    const double *ctx_t = A.ctx + (size_t)(t & 1) * A.ctx_len;
     for (int i = threadIdx.x; i < HDR; i += CT)
-      S.hdr[i] = __ldcg(A.ctx + i);
+      S.hdr[i] = __ldcg(ctx_t + i);
     __syncthreads();
     int m = (int)S.hdr[0];
     int na = (int)S.hdr[2];
     int nrows = b.K > 0 ? 2 * na * 3 : 0;
     for (int i = threadIdx.x; i < nrows * stride; i += CT)
-      tab[i] = __ldcg((const double2 *)(A.ctx + HDR) + i);
+      tab[i] = __ldcg((const double2 *)(ctx_t + HDR) + i);
     __syncthreads();
     double lj = 0.0, re = 0.0, ovl = 0.0, er = 0.0;
     // Real space: the candidates of all (atom, old/new, neighbour cell)
@@ -520,6 +644,12 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
       int c2 = b.nbr[cell * NB27 + nn];
       u_cell[u] = c2;
       u_off[u + 1] = __ldcg(b.cell_count + c2);
+    }
+    // x-y column products, one per (column, old/new atom)
+    for (int e = threadIdx.x; e < npair * 2 * na; e += CT) {
+      int p = e / (2 * na), r = e - p * 2 * na;
+      const double2 *rx = tab + (size_t)(r * 3) * stride;
+      exy[e] = cmul2(rx[pair_n[p].x], tab_at(rx + stride, pair_n[p].y));
     }
     __syncthreads();
     if (threadIdx.x < 32) {
@@ -662,16 +792,18 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
       for (int i = kw * 32 + lane; i < kc; i += 6 * 32) {
         char4 n = kn[i];
         double rN = 0, iN = 0, rO = 0, iO = 0;
+        const double2 *col = npair > 0 ? exy + (size_t)pidx[i] * 2 * na : nullptr;
         for (int a = 0; a < na; ++a) {
           double q = S.hdr[72 + a];
           if (q == 0.0)
             continue;
           const double2 *ro = tab + (size_t)(a * 3) * stride;
           const double2 *rn = tab + (size_t)((na + a) * 3) * stride;
-          double2 eo = cmul2(cmul2(ro[n.x], tab_at(ro + stride, n.y)),
-                             tab_at(ro + 2 * stride, n.z));
-          double2 en = cmul2(cmul2(rn[n.x], tab_at(rn + stride, n.y)),
-                             tab_at(rn + 2 * stride, n.z));
+          double2 xo = col ? col[a] : cmul2(ro[n.x], tab_at(ro + stride, n.y));
+          double2 xn = col ? col[na + a]
+                           : cmul2(rn[n.x], tab_at(rn + stride, n.y));
+          double2 eo = cmul2(xo, tab_at(ro + 2 * stride, n.z));
+          double2 en = cmul2(xn, tab_at(rn + 2 * stride, n.z));
           rN += q * en.x;
           iN += q * en.y;
           rO += q * eo.x;
@@ -701,141 +833,212 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
         S.red3[2][warp] = v2;
       }
       __syncthreads();
+      double *part_t = A.part + (size_t)(t & 1) * G * 4;
       if (threadIdx.x < 3) {
         double r = 0.0;
         for (int w = 0; w < CT / 32; ++w)
           r += S.red3[threadIdx.x][w];
-        A.part[(size_t)cta * 4 + threadIdx.x] = r;
+        __stcg(part_t + (size_t)cta * 4 + threadIdx.x, r);
         if (threadIdx.x == 0)
-          A.part[(size_t)cta * 4 + 3] = any ? 1.0 : 0.0;
+          __stcg(part_t + (size_t)cta * 4 + 3, any ? 1.0 : 0.0);
       }
     }
-    if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
-      return;
     // ---------------- phase B ----------------
-    // While warp 0 reduces the partials and decides, warps 1..7 build the
-    // next move's context: it does not depend on this decision unless the
-    // next move touches the same molecule or follows a settings adjustment
-    // (then it is built after the decision, as in the prologue).
+    // The last CTA (the leader) waits for every CTA's partials, reduces them
+    // in a fixed order, decides, commits an accepted move (coordinates,
+    // centre, cell slots) and publishes the decision; the other CTAs wait
+    // for that one word.  Meanwhile warps 1..7 of the context-building CTAs
+    // build the next move's context (into the other parity buffer): it does
+    // not depend on this decision unless the next move touches the same
+    // molecule or follows a settings adjustment (then it is built after the
+    // decision, behind a grid barrier, as in the prologue).  The leader
+    // publishes only after those builds are counted in, so one published
+    // word orders the decision, the commit and the next context before
+    // every CTA's next phase A.
     const bool spec = t + 1 < A.n && A.moves[t + 1].mol != m &&
                       (A.first + t + 2) % S.set.adj != 0;
+    const bool leader = cta == G - 1;
     if (threadIdx.x >= 32) {
       if (spec)
-        build_ctx(A, S, t + 1, nullptr, 0, 32, CT - 32);
-    } else {
-      double v[4] = {0, 0, 0, 0};
-      constexpr int PF = 8;  // partial slots per lane loaded up front
+        build_ctx(A, S, t + 1, nullptr, 0, 32, CT - 32, true);
+    } else if (leader) {
+      // poll every CTA's partial values (and, when the next context is
+      // built speculatively, the builders' flags) until all are present;
+      // lane l holds CTAs l, l + 32, ...
+      double *part_t = A.part + (size_t)(t & 1) * G * 4;
+      constexpr int PF = PART_MAX_GRID / 32;
       double2 pa[PF], pb[PF];
+      const int nb = spec ? (int)ctx_builders(A, t + 1) : 0;
+      const unsigned *bsq = A.seq + SEQ_PART + SEQ_STRIDE;
+      int ok = 1;
+      unsigned it = 0;
+      for (;;) {
+        bool mine = true;
 #pragma unroll
-      for (int i = 0; i < PF; ++i) {
-        int c = threadIdx.x + 32 * i;
-        const double2 *src = (const double2 *)(A.part + (size_t)c * 4);
-        pa[i] = c < G ? __ldcg(src) : make_double2(0, 0);
-        pb[i] = c < G ? __ldcg(src + 1) : make_double2(0, 0);
+        for (int i = 0; i < PF; ++i) {
+          int c = threadIdx.x + 32 * i;
+          if (c < G) {
+            const double2 *src = (const double2 *)(part_t + (size_t)c * 4);
+            pa[i] = __ldcg(src);
+            pb[i] = __ldcg(src + 1);
+            mine &= __double_as_longlong(pa[i].x) != (long long)PART_EMPTY &&
+                    __double_as_longlong(pa[i].y) != (long long)PART_EMPTY &&
+                    __double_as_longlong(pb[i].x) != (long long)PART_EMPTY &&
+                    __double_as_longlong(pb[i].y) != (long long)PART_EMPTY;
+          } else {
+            pa[i] = make_double2(0, 0);
+            pb[i] = make_double2(0, 0);
+          }
+        }
+        for (int c = threadIdx.x; c < nb; c += 32)
+          mine &= (int)(*(const volatile unsigned *)(bsq + c) -
+                        (unsigned)(t + 1)) >= 0;
+        if (__all_sync(0xffffffffu, mine))
+          break;
+        int bad = 0;
+        if (threadIdx.x == 0) {
+          if (++it > SPIN_LIMIT) {
+            atomicOr(b.err, DERR_BARRIER_TIMEOUT);
+            bad = 1;
+          } else if ((it & 255u) == 0 && *(volatile int *)b.err) {
+            bad = 1;
+          }
+        }
+        if (__shfl_sync(0xffffffffu, bad, 0)) {
+          ok = 0;
+          break;
+        }
       }
+      int acc = 0;
+      if (ok) {
+        // the slots are read: mark them empty for move t + 2 (ordered before
+        // the decision word that every later writer waits for)
+        const double2 empty = make_double2(__longlong_as_double(PART_EMPTY),
+                                           __longlong_as_double(PART_EMPTY));
 #pragma unroll
-      for (int i = 0; i < PF; ++i) {
-        v[0] += pa[i].x;
-        v[1] += pa[i].y;
-        v[2] += pb[i].x;
-        v[3] = fmax(v[3], pb[i].y);
-      }
-      for (int c = threadIdx.x + 32 * PF; c < G; c += 32) {
-        const double *p = A.part + (size_t)c * 4;
-        v[0] += __ldcg(p);
-        v[1] += __ldcg(p + 1);
-        v[2] += __ldcg(p + 2);
-        v[3] = fmax(v[3], __ldcg(p + 3));
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        v[0] += __shfl_down_sync(0xffffffffu, v[0], o);
-        v[1] += __shfl_down_sync(0xffffffffu, v[1], o);
-        v[2] += __shfl_down_sync(0xffffffffu, v[2], o);
-        v[3] = fmax(v[3], __shfl_down_sync(0xffffffffu, v[3], o));
+        for (int i = 0; i < PF; ++i) {
+          int c = threadIdx.x + 32 * i;
+          if (c < G) {
+            __stcg((double2 *)(part_t + (size_t)c * 4), empty);
+            __stcg((double2 *)(part_t + (size_t)c * 4) + 1, empty);
+          }
+        }
+        double v[4] = {0, 0, 0, 0};
+#pragma unroll
+        for (int i = 0; i < PF; ++i) {
+          v[0] += pa[i].x;
+          v[1] += pa[i].y;
+          v[2] += pb[i].x;
+          v[3] = fmax(v[3], pb[i].y);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          v[0] += __shfl_down_sync(0xffffffffu, v[0], o);
+          v[1] += __shfl_down_sync(0xffffffffu, v[1], o);
+          v[2] += __shfl_down_sync(0xffffffffu, v[2], o);
+          v[3] = fmax(v[3], __shfl_down_sync(0xffffffffu, v[3], o));
+        }
+        if (threadIdx.x == 0) {
+          int kind = (int)S.hdr[1];
+          bool over = v[3] > 0;
+          double dLJ = v[0], dRe = v[1];
+          double dRc = (!over && b.K > 0) ? v[2] - S.e_run[2] : 0.0;
+          if (!over && b.K == 0)
+            dRc = 0.0;
+          double ex = __dmul_rn(-ff.beta, __dadd_rn(__dadd_rn(dLJ, dRe), dRc));
+          // pacc < exp(ex), decided on logarithms unless the two sides are
+          // within 1e-9 (or pacc is 0): the outcome of the exp comparison
+          // without its FP64 exp on the critical path
+          double lp = S.hdr[80];
+          int res;
+          if (S.hdr[3] > 0.0 && ex > lp + 1e-9)
+            res = 1;
+          else if (S.hdr[3] > 0.0 && ex < lp - 1e-9)
+            res = 0;
+          else
+            res = S.hdr[3] < exp(ex);
+          acc = res && !over;
+          if (acc) {
+            S.e_run[0] += dLJ;
+            S.e_run[1] += dRe;
+            S.e_run[2] += dRc;
+          }
+          if (A.tr_i) {
+            A.tr_i[3 * (size_t)t] = kind;
+            A.tr_i[3 * (size_t)t + 1] = m;
+            A.tr_i[3 * (size_t)t + 2] = acc;
+            A.tr_d[3 * (size_t)t] = dLJ;
+            A.tr_d[3 * (size_t)t + 1] = dRe;
+            A.tr_d[3 * (size_t)t + 2] = dRc;
+          }
+        }
+        acc = __shfl_sync(0xffffffffu, acc, 0);
+        if (acc) {
+          // Atoms that stay in their cell are rewritten in place by one
+          // lane each; then the atoms that change cell are relinked one
+          // after another, in atom order -- the slot layout that relinking
+          // every atom in order would give.
+          int a0 = b.mstart[m], a = threadIdx.x;
+          bool stay = false;
+          if (a < na) {
+            const double *np = S.hdr + 48 + 3 * a;
+            b.x[a0 + a] = np[0];
+            b.y[a0 + a] = np[1];
+            b.z[a0 + a] = np[2];
+            int c1 = (int)S.hdr[16 + a];
+            stay = __ldcg(b.atom_cell + a0 + a) == c1;
+            if (stay)
+              cell_write_slot(b, c1, __ldcg(b.atom_slot + a0 + a), a0 + a,
+                              np[0], np[1], np[2]);
+          }
+          unsigned moving = __ballot_sync(0xffffffffu, a < na && !stay);
+          __syncwarp();
+          if (a == 0) {
+            for (int i = 0; i < na; ++i)
+              if (moving & (1u << i)) {
+                const double *np = S.hdr + 48 + 3 * i;
+                cell_move_atom(b, a0 + i, np[0], np[1], np[2],
+                               (int)S.hdr[16 + i]);
+              }
+            if ((int)S.hdr[1] == 0) {
+              b.cx[m] = S.hdr[4];
+              b.cy[m] = S.hdr[5];
+              b.cz[m] = S.hdr[6];
+            }
+          }
+          __syncwarp();
+        }
+        if (threadIdx.x == 0 && ok) {
+          __threadfence();
+          st_release(A.seq, 2u * (unsigned)(t + 1) + (unsigned)acc);
+        }
       }
       if (threadIdx.x == 0) {
-        int kind = (int)S.hdr[1];
-        bool over = v[3] > 0;
-        double dLJ = v[0], dRe = v[1];
-        double dRc = (!over && b.K > 0) ? v[2] - S.e_run[2] : 0.0;
-        if (!over && b.K == 0)
-          dRc = 0.0;
-        double ex = __dmul_rn(-ff.beta, __dadd_rn(__dadd_rn(dLJ, dRe), dRc));
-        // pacc < exp(ex), decided on logarithms unless the two sides are
-        // within 1e-9 (or pacc is 0): the outcome of the exp comparison
-        // without its FP64 exp on the critical path
-        double lp = S.hdr[80];
-        int res;
-        if (S.hdr[3] > 0.0 && ex > lp + 1e-9)
-          res = 1;
-        else if (S.hdr[3] > 0.0 && ex < lp - 1e-9)
-          res = 0;
-        else
-          res = S.hdr[3] < exp(ex);
-        int acc = res && !over;
-        if (acc) {
-          S.e_run[0] += dLJ;
-          S.e_run[1] += dRe;
-          S.e_run[2] += dRc;
-        }
-        settings_update(S.set, kind, acc);
         S.accept = acc;
-        if (cta == 0 && A.tr_i) {
-          A.tr_i[3 * (size_t)t] = kind;
-          A.tr_i[3 * (size_t)t + 1] = m;
-          A.tr_i[3 * (size_t)t + 2] = acc;
-          A.tr_d[3 * (size_t)t] = dLJ;
-          A.tr_d[3 * (size_t)t + 1] = dRe;
-          A.tr_d[3 * (size_t)t + 2] = dRc;
-        }
+        S.ok = ok;
+      }
+    } else {
+      if (threadIdx.x == 0) {
+        int ok = wait_geq(A.seq, 2u * (unsigned)(t + 1), b.err, true);
+        S.accept = ok ? (int)(ld_acquire(A.seq) & 1u) : 0;
+        S.ok = ok;
       }
     }
     __syncthreads();
-    int acc = S.accept;
+    if (!S.ok)
+      return;
+    const int acc = S.accept;
+    if (threadIdx.x == 0)
+      settings_update(S.set, (int)S.hdr[1], acc);
     if (acc) {
       for (int i = threadIdx.x; i < kc; i += CT) {
         sR[i] = nR[i];
         sI[i] = nI[i];
       }
-      // The last CTA commits (coordinates, centre, cell slots) while CTA 0
-      // builds the next move's header.  Atoms that stay in their cell are
-      // rewritten in place by one lane each; then the atoms that change
-      // cell are relinked one after another, in atom order -- the slot
-      // layout that relinking every atom in order would give.
-      if (cta == G - 1 && threadIdx.x < 32) {
-        int a0 = b.mstart[m], a = threadIdx.x;
-        bool stay = false;
-        if (a < na) {
-          const double *np = S.hdr + 48 + 3 * a;
-          b.x[a0 + a] = np[0];
-          b.y[a0 + a] = np[1];
-          b.z[a0 + a] = np[2];
-          int c1 = (int)S.hdr[16 + a];
-          stay = __ldcg(b.atom_cell + a0 + a) == c1;
-          if (stay)
-            cell_write_slot(b, c1, __ldcg(b.atom_slot + a0 + a), a0 + a,
-                            np[0], np[1], np[2]);
-        }
-        unsigned moving = __ballot_sync(0xffffffffu, a < na && !stay);
-        __syncwarp();
-        if (a == 0) {
-          for (int i = 0; i < na; ++i)
-            if (moving & (1u << i)) {
-              const double *np = S.hdr + 48 + 3 * i;
-              cell_move_atom(b, a0 + i, np[0], np[1], np[2],
-                             (int)S.hdr[16 + i]);
-            }
-          if ((int)S.hdr[1] == 0) {
-            b.cx[m] = S.hdr[4];
-            b.cy[m] = S.hdr[5];
-            b.cz[m] = S.hdr[6];
-          }
-        }
-      }
     }
     if (t + 1 < A.n) {
       long long step = A.first + t + 1;
       if ((step + 1) % S.set.adj == 0) {
+        __syncthreads();
         if (threadIdx.x == 0)
           settings_adjust(S.set, step);
         __syncthreads();
@@ -843,18 +1046,20 @@ __global__ void __launch_bounds__(CT) k_chain_fp64(ChainArgs A) {
         if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
           return;
       }
-      if (!spec)
+      if (!spec) {
         build_ctx(A, S, t + 1, S.hdr, acc, 0, CT);
-      if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
-        return;
+        if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
+          return;
+      }
     }
   }
-  // write back this CTA's structure factors; CTA 0 the settings and energies
+  // write back this CTA's structure factors; the leader the settings and
+  // the running energies
   for (int i = threadIdx.x; i < kc; i += CT) {
     b.sumRref[kbeg + i] = sR[i];
     b.sumIref[kbeg + i] = sI[i];
   }
-  if (cta == 0 && threadIdx.x == 0) {
+  if (cta == G - 1 && threadIdx.x == 0) {
     *A.set = S.set;
     for (int i = 0; i < 5; ++i)
       b.energy[i] = S.e_run[i];
@@ -1183,7 +1388,8 @@ static size_t chain_smem(const Box &b, int grid) {
   int kc_max = (b.dev.K + grid - 1) / grid;
   return sizeof(double) * ((5 * (size_t)kc_max + (kc_max + 1) / 2 + 1) & ~(size_t)1) +
          sizeof(double2) * (size_t)(2 * MAX_MOL_ATOMS * 3) * (b.dev.kmax + 1) +
-         64;
+         sizeof(double2) * (size_t)NPAIR_CAP * 2 * MAX_MOL_ATOMS +
+         sizeof(unsigned short) * (size_t)kc_max + 64;
 }
 
 int mc_init(Box &b, const gb_mc_params &p) {
@@ -1239,16 +1445,18 @@ int mc_init(Box &b, const gb_mc_params &p) {
   if (per_sm < 1)
     return b.Fail(ERR_UNSUPPORTED, "chain kernel does not fit on an SM");
   s.grid = b.sm_count;
+  if (s.grid > PART_MAX_GRID)
+    return b.Fail(ERR_UNSUPPORTED, "more SMs than the chain's leader holds");
   if (p.move_buffer < 0)
     return b.Fail(ERR_ARG, "move_buffer must be >= 0");
   s.move_cap = p.move_buffer > 0 ? (size_t)p.move_buffer : (size_t)1 << 16;
   int stride = b.dev.kmax + 1;
   if ((rc = mc_alloc(b, s, &s.d_moves, s.move_cap)) ||
       (rc = mc_alloc(b, s, &s.d_prop, s.move_cap * 12)) ||
-      (rc = mc_alloc(b, s, &s.d_part, (size_t)s.grid * 4)) ||
+      (rc = mc_alloc(b, s, &s.d_part, 2 * (size_t)s.grid * 4)) ||
       (rc = mc_alloc(b, s, &s.d_bar, 8)) ||
-      (rc = mc_alloc(b, s, &s.d_ctx,
-                     HDR + 2 * (size_t)(2 * MAX_MOL_ATOMS * 3) * stride)) ||
+      (rc = mc_alloc(b, s, &s.d_seq, SEQ_PART + 2 * SEQ_STRIDE)) ||
+      (rc = mc_alloc(b, s, &s.d_ctx, 2 * chain_ctx_len(stride))) ||
       (rc = mc_alloc(b, s, &s.d_mp, 16)))
     return rc;
   if ((rc = b.CudaCheck(cudaMallocHost(&s.h_moves, s.move_cap * sizeof(MoveRec)),
@@ -1411,14 +1619,26 @@ static int run_chain(Box &b, McState &s, const MoveRec *moves, int64_t first,
   A.n = n;
   A.part = s.d_part;
   A.bar = s.d_bar;
+  A.seq = s.d_seq;
   A.ctx = s.d_ctx;
+  A.ctx_len = chain_ctx_len(b.dev.kmax + 1);
   A.tr_i = tr_i;
   A.tr_d = tr_d;
   void *args[] = {&A};
   size_t sm = chain_smem(b, s.grid);
+  // the per-launch counters of the decision protocol start from zero
+  int rc = b.CudaCheck(cudaMemsetAsync(s.d_seq, 0,
+                                       (SEQ_PART + 2 * SEQ_STRIDE) *
+                                           sizeof(unsigned),
+                                       b.stream),
+                       "memset");
+  if (rc)
+    return rc;
+  k_fill_u64<<<(2 * s.grid * 4 + 255) / 256, 256, 0, b.stream>>>(
+      (unsigned long long *)s.d_part, 2 * s.grid * 4, PART_EMPTY);
   auto ev = ev_pair();
   cudaEventRecord(ev.first, b.stream);
-  int rc = b.CudaCheck(cudaLaunchCooperativeKernel((void *)k_chain_fp64,
+  rc = b.CudaCheck(cudaLaunchCooperativeKernel((void *)k_chain_fp64,
                                                    dim3(s.grid), dim3(CT), args,
                                                    sm, b.stream),
                        "chain kernel");

@@ -95,6 +95,7 @@ struct McState {
   double *d_trace_d = nullptr;
   size_t trace_cap = 0;
   double *d_part = nullptr;  // per-CTA partials
+  unsigned *d_seq = nullptr; // FP64 chain decision and per-CTA flags
   unsigned *d_bar = nullptr; // grid barrier words
   double *d_ctx = nullptr;   // per-move context (positions, tables)
   int grid = 0, kchunk = 0;

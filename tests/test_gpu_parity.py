@@ -121,9 +121,15 @@ def test_mc_trace_matches_reference(gb, name):
     np.testing.assert_array_equal(r["accepted"], tr[:, 3].astype(int))
     scale = np.maximum(np.abs(tr[-1, 8:11]), 1.0)
     single = tr[:, 1] < 2
+    # 1e-10 of the box energy, or of the move's own change where that is
+    # larger (near-overlap proposals of the sparse LJ box change the energy
+    # by up to 1e11 K)
     for j in range(3):
-        np.testing.assert_allclose(r["de"][single, j], tr[single, 5 + j],
-                                   rtol=0, atol=REL * scale[j])
+        ref = tr[single, 5 + j]
+        bound = REL * np.maximum(scale[j], np.abs(ref))
+        err = np.abs(r["de"][single, j] - ref)
+        assert (err <= bound).all(), (j, np.argwhere(err > bound)[:5].ravel(),
+                                      err.max())
     mp = ~single
     if mp.any():
         for j in range(3):
