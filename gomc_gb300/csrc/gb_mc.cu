@@ -372,7 +372,7 @@ __host__ __device__ constexpr size_t chain_ctx_len(int stride) {
 // Context header layout (doubles):
 //  0 m, 1 kind, 2 na, 3 pacc, 4..6 newcom, 8..15 cell old, 16..23 cell new,
 //  24..47 old positions [8][3], 48..71 new positions [8][3], 72..79 charges,
-//  80 log(pacc)
+//  80 log(pacc), 81 log(pacc) + 1e-9, 82 log(pacc) - 1e-9
 struct ChainArgs {
   DevBox b;
   const FF *ff;
@@ -490,6 +490,8 @@ __device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
       h[2] = na;
       h[3] = r.pacc;
       h[80] = r.lpacc;
+      h[81] = r.lpacc + 1e-9;  // the decision's margins, precomputed
+      h[82] = r.lpacc - 1e-9;
       for (int d = 0; d < 3; ++d)
         h[4 + d] = newcom[d];
     }
@@ -858,45 +860,39 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     const bool spec = t + 1 < A.n && A.moves[t + 1].mol != m &&
                       (A.first + t + 2) % S.set.adj != 0;
     const bool leader = cta == G - 1;
-    if (threadIdx.x >= 32) {
+    // threads of this CTA that build its part of the next context (when it
+    // is a builder): warps 1..7, or warps 4..7 in the leader
+    const int bfirst = leader ? 128 : 32;
+    if ((int)threadIdx.x >= bfirst) {
       if (spec)
-        build_ctx(A, S, t + 1, nullptr, 0, 32, CT - 32, true);
+        build_ctx(A, S, t + 1, nullptr, 0, bfirst, CT - bfirst, true);
     } else if (leader) {
-      // poll every CTA's partial values (and, when the next context is
-      // built speculatively, the builders' flags) until all are present;
-      // lane l holds CTAs l, l + 32, ...
+      // Warps 0..3 of the leader each gather one quantity over all CTAs
+      // (LJ, real space, reciprocal energy, overlap), polling the values
+      // until every CTA's is present, so the FP64 additions run on four
+      // SM sub-partitions at once.  Lane l adds CTAs l, l + 32, ... in
+      // order, then the warp tree: a fixed order.
+      const int q = warp;
       double *part_t = A.part + (size_t)(t & 1) * G * 4;
       constexpr int PF = PART_MAX_GRID / 32;
-      double2 pa[PF], pb[PF];
-      const int nb = spec ? (int)ctx_builders(A, t + 1) : 0;
-      const unsigned *bsq = A.seq + SEQ_PART + SEQ_STRIDE;
+      double pv[PF];
       int ok = 1;
       unsigned it = 0;
       for (;;) {
         bool mine = true;
 #pragma unroll
         for (int i = 0; i < PF; ++i) {
-          int c = threadIdx.x + 32 * i;
+          int c = lane + 32 * i;
+          pv[i] = 0.0;
           if (c < G) {
-            const double2 *src = (const double2 *)(part_t + (size_t)c * 4);
-            pa[i] = __ldcg(src);
-            pb[i] = __ldcg(src + 1);
-            mine &= __double_as_longlong(pa[i].x) != (long long)PART_EMPTY &&
-                    __double_as_longlong(pa[i].y) != (long long)PART_EMPTY &&
-                    __double_as_longlong(pb[i].x) != (long long)PART_EMPTY &&
-                    __double_as_longlong(pb[i].y) != (long long)PART_EMPTY;
-          } else {
-            pa[i] = make_double2(0, 0);
-            pb[i] = make_double2(0, 0);
+            pv[i] = __ldcg(part_t + (size_t)c * 4 + q);
+            mine &= __double_as_longlong(pv[i]) != (long long)PART_EMPTY;
           }
         }
-        for (int c = threadIdx.x; c < nb; c += 32)
-          mine &= (int)(*(const volatile unsigned *)(bsq + c) -
-                        (unsigned)(t + 1)) >= 0;
         if (__all_sync(0xffffffffu, mine))
           break;
         int bad = 0;
-        if (threadIdx.x == 0) {
+        if (lane == 0) {
           if (++it > SPIN_LIMIT) {
             atomicOr(b.err, DERR_BARRIER_TIMEOUT);
             bad = 1;
@@ -909,67 +905,59 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
           break;
         }
       }
-      int acc = 0;
       if (ok) {
-        // the slots are read: mark them empty for move t + 2 (ordered before
-        // the decision word that every later writer waits for)
-        const double2 empty = make_double2(__longlong_as_double(PART_EMPTY),
-                                           __longlong_as_double(PART_EMPTY));
+        // read: mark this quantity's slots empty for move t + 2 (ordered
+        // before the decision word that every later writer waits for)
 #pragma unroll
         for (int i = 0; i < PF; ++i) {
-          int c = threadIdx.x + 32 * i;
-          if (c < G) {
-            __stcg((double2 *)(part_t + (size_t)c * 4), empty);
-            __stcg((double2 *)(part_t + (size_t)c * 4) + 1, empty);
-          }
+          int c = lane + 32 * i;
+          if (c < G)
+            __stcg(part_t + (size_t)c * 4 + q, __longlong_as_double(PART_EMPTY));
         }
-        double v[4] = {0, 0, 0, 0};
+        if (q < 3) {
+          double v = 0.0;
 #pragma unroll
-        for (int i = 0; i < PF; ++i) {
-          v[0] += pa[i].x;
-          v[1] += pa[i].y;
-          v[2] += pb[i].x;
-          v[3] = fmax(v[3], pb[i].y);
+          for (int i = 0; i < PF; ++i)
+            v += pv[i];
+          for (int o = 16; o > 0; o >>= 1)
+            v += __shfl_down_sync(0xffffffffu, v, o);
+          if (lane == 0)
+            S.tot[q] = v;
+        } else {
+          bool any = false;
+#pragma unroll
+          for (int i = 0; i < PF; ++i)
+            any |= __double_as_longlong(pv[i]) != 0;
+          any = __any_sync(0xffffffffu, any);
+          if (lane == 0)
+            S.tot[3] = any ? 1.0 : 0.0;
         }
-        for (int o = 16; o > 0; o >>= 1) {
-          v[0] += __shfl_down_sync(0xffffffffu, v[0], o);
-          v[1] += __shfl_down_sync(0xffffffffu, v[1], o);
-          v[2] += __shfl_down_sync(0xffffffffu, v[2], o);
-          v[3] = fmax(v[3], __shfl_down_sync(0xffffffffu, v[3], o));
-        }
-        if (threadIdx.x == 0) {
-          int kind = (int)S.hdr[1];
-          bool over = v[3] > 0;
-          double dLJ = v[0], dRe = v[1];
-          double dRc = (!over && b.K > 0) ? v[2] - S.e_run[2] : 0.0;
-          if (!over && b.K == 0)
-            dRc = 0.0;
+      }
+      if (lane == 0)
+        S.red3[0][q] = ok;  // per-warp status
+      asm volatile("bar.sync 2, 128;" ::: "memory");
+      ok = S.red3[0][0] != 0.0 && S.red3[0][1] != 0.0 && S.red3[0][2] != 0.0 &&
+           S.red3[0][3] != 0.0;
+      int acc = 0;
+      if (warp == 0 && ok) {
+        double dLJ = 0.0, dRe = 0.0, dRc = 0.0;
+        if (lane == 0) {
+          bool over = S.tot[3] > 0;
+          dLJ = S.tot[0];
+          dRe = S.tot[1];
+          dRc = (!over && b.K > 0) ? S.tot[2] - S.e_run[2] : 0.0;
           double ex = __dmul_rn(-ff.beta, __dadd_rn(__dadd_rn(dLJ, dRe), dRc));
           // pacc < exp(ex), decided on logarithms unless the two sides are
           // within 1e-9 (or pacc is 0): the outcome of the exp comparison
           // without its FP64 exp on the critical path
-          double lp = S.hdr[80];
           int res;
-          if (S.hdr[3] > 0.0 && ex > lp + 1e-9)
+          if (S.hdr[3] > 0.0 && ex > S.hdr[81])
             res = 1;
-          else if (S.hdr[3] > 0.0 && ex < lp - 1e-9)
+          else if (S.hdr[3] > 0.0 && ex < S.hdr[82])
             res = 0;
           else
             res = S.hdr[3] < exp(ex);
           acc = res && !over;
-          if (acc) {
-            S.e_run[0] += dLJ;
-            S.e_run[1] += dRe;
-            S.e_run[2] += dRc;
-          }
-          if (A.tr_i) {
-            A.tr_i[3 * (size_t)t] = kind;
-            A.tr_i[3 * (size_t)t + 1] = m;
-            A.tr_i[3 * (size_t)t + 2] = acc;
-            A.tr_d[3 * (size_t)t] = dLJ;
-            A.tr_d[3 * (size_t)t + 1] = dRe;
-            A.tr_d[3 * (size_t)t + 2] = dRc;
-          }
         }
         acc = __shfl_sync(0xffffffffu, acc, 0);
         if (acc) {
@@ -977,7 +965,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
           // lane each; then the atoms that change cell are relinked one
           // after another, in atom order -- the slot layout that relinking
           // every atom in order would give.
-          int a0 = b.mstart[m], a = threadIdx.x;
+          int a0 = b.mstart[m], a = lane;
           bool stay = false;
           if (a < na) {
             const double *np = S.hdr + 48 + 3 * a;
@@ -1007,14 +995,36 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
           }
           __syncwarp();
         }
-        if (threadIdx.x == 0 && ok) {
+        // the next context must be complete before the word goes out
+        if (spec)
+          ok = warp_wait_all(A.seq + SEQ_PART + SEQ_STRIDE,
+                             (int)ctx_builders(A, t + 1), (unsigned)(t + 1),
+                             b.err);
+        if (lane == 0 && ok) {
           __threadfence();
           st_release(A.seq, 2u * (unsigned)(t + 1) + (unsigned)acc);
         }
-      }
-      if (threadIdx.x == 0) {
-        S.accept = acc;
-        S.ok = ok;
+        if (lane == 0) {
+          // off the critical path: running energies and the trace
+          if (acc) {
+            S.e_run[0] += dLJ;
+            S.e_run[1] += dRe;
+            S.e_run[2] += dRc;
+          }
+          if (A.tr_i) {
+            A.tr_i[3 * (size_t)t] = (int)S.hdr[1];
+            A.tr_i[3 * (size_t)t + 1] = m;
+            A.tr_i[3 * (size_t)t + 2] = acc;
+            A.tr_d[3 * (size_t)t] = dLJ;
+            A.tr_d[3 * (size_t)t + 1] = dRe;
+            A.tr_d[3 * (size_t)t + 2] = dRc;
+          }
+          S.accept = acc;
+          S.ok = ok;
+        }
+      } else if (warp == 0 && lane == 0) {
+        S.accept = 0;
+        S.ok = 0;
       }
     } else {
       if (threadIdx.x == 0) {
