@@ -351,7 +351,7 @@ __device__ __forceinline__ double2 tab_at(const double2 *row, int n) {
 // The FP64 chain kernel
 // ===========================================================================
 constexpr int CT = 256;
-constexpr int HDR = 96;  // doubles in the move-context header
+constexpr int HDR = 112;  // doubles in the move-context header
 constexpr int ICL_MAX = 256;  // in-cutoff pairs a CTA lists per move
 constexpr int SEQ_PART = 32;      // words; the decision word has its own line
 // A CTA's partial slots hold this NaN pattern until written: the leader
@@ -372,7 +372,8 @@ __host__ __device__ constexpr size_t chain_ctx_len(int stride) {
 // Context header layout (doubles):
 //  0 m, 1 kind, 2 na, 3 pacc, 4..6 newcom, 8..15 cell old, 16..23 cell new,
 //  24..47 old positions [8][3], 48..71 new positions [8][3], 72..79 charges,
-//  80 log(pacc), 81 log(pacc) + 1e-9, 82 log(pacc) - 1e-9
+//  80 log(pacc), 81 log(pacc) + 1e-9, 82 log(pacc) - 1e-9,
+//  84..107 fixed-point turns of the positions as uint32 [side][atom][3]
 struct ChainArgs {
   DevBox b;
   const FF *ff;
@@ -403,6 +404,11 @@ struct ChainShared {
   double tot[4];
   int accept, flag, ok;
   unsigned gen;
+  // inputs and new positions of the context being built
+  double b_oldp[MAX_MOL_ATOMS][3], b_newp[MAX_MOL_ATOMS][3];
+  double b_com[3], b_newcom[3], b_prop[12], b_q[MAX_MOL_ATOMS];
+  double b_pacc, b_lpacc;
+  int b_m, b_a0, b_na, b_kind, b_writer;
 };
 
 // Synchronise the threads [first, first + count) of the CTA: the whole CTA
@@ -414,112 +420,98 @@ __device__ __forceinline__ void group_sync(int count) {
     asm volatile("bar.sync 1, %0;" ::"r"(count) : "memory");
 }
 
-// Build the next move's header and phase tables (designated CTAs), using the
-// committed state plus the just-decided move when it touched the same
-// molecule.  The threads [first, first + count) of the CTA take part (whole
-// warps; count >= 64).
-__device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
-                          const double *prev_hdr, int prev_acc, int first,
-                          int count, bool report = false) {
-  const int tid = (int)threadIdx.x - first;
-  const DevBox &b = A.b;
-  const MoveRec &r = A.moves[t];
-  int m = r.mol;
-  int a0 = b.mstart[m], na = b.mstart[m + 1] - a0;
-  int G = gridDim.x;
-  int stride = b.kmax + 1;
+// Is this CTA one of the writers of a move's context: CTA 0 (header) and
+// one CTA per phase row.
+__device__ __forceinline__ bool ctx_writer(const ChainArgs &A, int na) {
   int nrows = A.b.K > 0 ? 2 * na * 3 : 0;
-  bool header_cta = blockIdx.x == 0;
-  bool row_cta = false;
-  for (int rr = blockIdx.x; rr < nrows; rr += G)
-    row_cta = true;
-  if (!header_cta && !row_cta)
-    return;
-  __shared__ double oldp[MAX_MOL_ATOMS][3], newp[MAX_MOL_ATOMS][3], com[3],
-      newcom[3];
-  __shared__ double prop[12];
-  bool same = prev_acc && prev_hdr && (int)prev_hdr[0] == m;
-  if (tid < 12)
-    prop[tid] = A.prop[(size_t)t * 12 + tid];
-  if (tid < 3) {
-    int d = tid;
-    double *cs[3] = {b.cx, b.cy, b.cz};
-    com[d] = (same && (int)prev_hdr[1] == 0) ? prev_hdr[4 + d]
-                                             : __ldcg(cs[d] + m);
-  }
-  if (tid >= 32 && tid < 32 + 3 * na) {
-    int i = tid - 32, a = i / 3, d = i % 3;
-    double *xs[3] = {b.x, b.y, b.z};
-    oldp[a][d] = same ? prev_hdr[48 + 3 * a + d] : __ldcg(xs[d] + a0 + a);
-  }
-  group_sync(count);
-  // one thread per atom applies the proposal (Coordinates::TranslateRand /
-  // RotateRand arithmetic, see apply_proposal)
+  return blockIdx.x == 0 || (int)blockIdx.x < nrows;
+}
+
+// Second half of building move t's context from the inputs in S.b_*
+// (threads tid = 0..count-1 of the CTA, count >= 128; the tasks sit on
+// different warps so that they overlap): the proposal applied
+// (Coordinates::TranslateRand / RotateRand arithmetic, see apply_proposal),
+// the header (CTA 0), this CTA's phase row, and -- with `report` -- this
+// CTA's flag for the leader.
+__device__ void build_ctx_rest(const ChainArgs &A, ChainShared &S, int t,
+                               int tid, int count, bool report) {
+  const DevBox &b = A.b;
+  const int m = S.b_m, na = S.b_na, kind = S.b_kind;
+  const int G = gridDim.x;
+  const int stride = b.kmax + 1;
+  const int nrows = b.K > 0 ? 2 * na * 3 : 0;
+  const double *prop = S.b_prop;
   if (tid < na) {
     int a = tid;
     double v[3], w[3];
-    if (r.kind == 0) {
+    if (kind == 0) {
       for (int d = 0; d < 3; ++d)
-        w[d] = wrap1(__dadd_rn(oldp[a][d], prop[d]), b.L[d]);
+        w[d] = wrap1(__dadd_rn(S.b_oldp[a][d], prop[d]), b.L[d]);
     } else {
       for (int d = 0; d < 3; ++d) {
-        v[d] = unwrap1(oldp[a][d], com[d], b.L[d], b.half[d]);
-        v[d] = __dadd_rn(v[d], -com[d]);
+        v[d] = unwrap1(S.b_oldp[a][d], S.b_com[d], b.L[d], b.half[d]);
+        v[d] = __dadd_rn(v[d], -S.b_com[d]);
       }
       for (int i = 0; i < 3; ++i) {
         double u = __dadd_rn(__dadd_rn(__dmul_rn(prop[3 * i], v[0]),
                                        __dmul_rn(prop[3 * i + 1], v[1])),
                              __dmul_rn(prop[3 * i + 2], v[2]));
-        w[i] = wrap1(__dadd_rn(u, com[i]), b.L[i]);
+        w[i] = wrap1(__dadd_rn(u, S.b_com[i]), b.L[i]);
       }
     }
     for (int d = 0; d < 3; ++d)
-      newp[a][d] = w[d];
-  }
-  if (tid >= 32 && tid < 35) {
+      S.b_newp[a][d] = w[d];
+  } else if (tid >= 32 && tid < 35) {
     int d = tid - 32;
-    newcom[d] = r.kind == 0 ? wrap1(__dadd_rn(com[d], prop[d]), b.L[d]) : com[d];
+    S.b_newcom[d] = kind == 0 ? wrap1(__dadd_rn(S.b_com[d], prop[d]), b.L[d])
+                              : S.b_com[d];
   }
   group_sync(count);
   double *const ctx = A.ctx + (size_t)(t & 1) * A.ctx_len;
-  if (header_cta) {
+  if (blockIdx.x == 0) {
     double *h = ctx;
-    if (tid == 0) {
+    if (tid == 64) {
       h[0] = m;
-      h[1] = r.kind;
+      h[1] = kind;
       h[2] = na;
-      h[3] = r.pacc;
-      h[80] = r.lpacc;
-      h[81] = r.lpacc + 1e-9;  // the decision's margins, precomputed
-      h[82] = r.lpacc - 1e-9;
+      h[3] = S.b_pacc;
+      h[80] = S.b_lpacc;
+      h[81] = S.b_lpacc + 1e-9;  // the decision's margins, precomputed
+      h[82] = S.b_lpacc - 1e-9;
       for (int d = 0; d < 3; ++d)
-        h[4 + d] = newcom[d];
-    }
-    if (tid >= 32 && tid < 32 + 2 * na) {
-      int i = tid - 32, a = i % na, side = i / na;
-      const double *p = side ? newp[a] : oldp[a];
+        h[4 + d] = S.b_newcom[d];
+    } else if (tid >= 96 && tid < 96 + 2 * na) {
+      int i = tid - 96, a = i % na, side = i / na;
+      const double *p = side ? S.b_newp[a] : S.b_oldp[a];
       h[(side ? 16 : 8) + a] = position_to_cell_fast(b, p[0], p[1], p[2]);
       for (int d = 0; d < 3; ++d)
         h[(side ? 48 : 24) + 3 * a + d] = p[d];
       if (side == 0) {
-        double q = b.q[a0 + a];
+        double q = S.b_q[a];
         h[72 + a] = fabs(q) < 0.000000001 ? 0.0 : q;
       }
+    } else if (tid >= 128 && tid < 128 + 6 * na) {
+      int i = tid - 128, pa = i / 3, d = i % 3;  // pa = side * na + atom
+      const double *p = pa < na ? S.b_oldp[pa] : S.b_newp[pa - na];
+      ((uint32_t *)(h + 84))[i] = to_turns(p[d], b.invL[d]);
     }
   }
   // phase rows exp(i n 2 pi r_d / L_d), n = 0..kmax, one entry per thread:
   // the coordinate as a 64-bit fraction of the box edge, n times it exact
-  // modulo one turn
+  // modulo one turn; in CTA 0 on the threads the header leaves free
   double2 *tab = (double2 *)(ctx + HDR);
-  for (int rr = blockIdx.x; rr < nrows; rr += G) {
-    int p = rr / 3, d = rr % 3;
-    double coord = p < na ? oldp[p][d] : newp[p - na][d];
-    double t = coord * b.invL[d];
-    if (t >= 1.0)
-      t -= 1.0;
-    uint64_t u = __double2ull_rn(t * 18446744073709551616.0);  // 2^64
-    for (int n = tid; n < stride; n += count)
-      tab[(size_t)rr * stride + n] = cis_turns64((uint64_t)n * u);
+  const int rfirst = blockIdx.x == 0 ? 160 : 0;
+  if (tid >= rfirst) {
+    for (int rr = blockIdx.x; rr < nrows; rr += G) {
+      int p = rr / 3, d = rr % 3;
+      double coord = p < na ? S.b_oldp[p][d] : S.b_newp[p - na][d];
+      double tt = coord * b.invL[d];
+      if (tt >= 1.0)
+        tt -= 1.0;
+      uint64_t u = __double2ull_rn(tt * 18446744073709551616.0);  // 2^64
+      for (int n = tid - rfirst; n < stride; n += count - rfirst)
+        tab[(size_t)rr * stride + n] = cis_turns64((uint64_t)n * u);
+    }
   }
   if (report) {
     // this CTA's part of the context is written: flag it for the leader
@@ -531,6 +523,106 @@ __device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
   }
 }
 
+// Build move t's context with threads [first, first + count) of the CTA,
+// count >= 192 (all of them after a decision; prev_hdr / prev_acc: the
+// previous move's header and outcome, whose new positions are the current
+// ones when the same molecule moves again).
+__device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
+                          const double *prev_hdr, int prev_acc, int first,
+                          int count) {
+  const int tid = (int)threadIdx.x - first;
+  const DevBox &b = A.b;
+  const MoveRec &r = A.moves[t];
+  int m = r.mol;
+  int a0 = b.mstart[m], na = b.mstart[m + 1] - a0;
+  if (!ctx_writer(A, na))
+    return;
+  bool same = prev_acc && prev_hdr && (int)prev_hdr[0] == m;
+  if (tid == 0) {
+    S.b_m = m;
+    S.b_a0 = a0;
+    S.b_na = na;
+    S.b_kind = r.kind;
+    S.b_pacc = r.pacc;
+    S.b_lpacc = r.lpacc;
+  }
+  for (int i = tid; i < 12; i += count)
+    S.b_prop[i] = A.prop[(size_t)t * 12 + i];
+  for (int d = tid; d < 3; d += count) {
+    double *cs[3] = {b.cx, b.cy, b.cz};
+    S.b_com[d] = (same && (int)prev_hdr[1] == 0) ? prev_hdr[4 + d]
+                                                 : __ldcg(cs[d] + m);
+  }
+  for (int i = tid; i < 3 * na; i += count) {
+    int a = i / 3, d = i % 3;
+    double *xs[3] = {b.x, b.y, b.z};
+    S.b_oldp[a][d] = same ? prev_hdr[48 + 3 * a + d] : __ldcg(xs[d] + a0 + a);
+  }
+  for (int a = tid; a < na; a += count)
+    S.b_q[a] = b.q[a0 + a];
+  group_sync(count);
+  build_ctx_rest(A, S, t, tid, count, false);
+}
+
+// Inputs of move t's context gathered by one warp in registers, in two
+// steps so that each load has a stretch of other work to arrive in: step 1
+// the move record and the molecule's atom range, step 2 the proposal
+// (lanes 0..11), the centre (12..14), the old coordinates (lanes < 3 na)
+// and the charges (lanes < na).
+struct CtxPre {
+  int m, a0, na, kind;
+  double pacc, lpacc;
+  double v0, v1, q;
+  bool writer;
+};
+__device__ __forceinline__ void ctx_pre1(const ChainArgs &A, int t, CtxPre &c) {
+  const MoveRec &r = A.moves[t];
+  c.m = r.mol;
+  c.kind = r.kind;
+  c.pacc = r.pacc;
+  c.lpacc = r.lpacc;
+  c.a0 = A.b.mstart[c.m];
+  c.na = A.b.mstart[c.m + 1] - c.a0;
+}
+__device__ __forceinline__ void ctx_pre2(const ChainArgs &A, int t, CtxPre &c) {
+  const DevBox &b = A.b;
+  const int lane = threadIdx.x & 31;
+  c.writer = ctx_writer(A, c.na);
+  c.v0 = c.v1 = c.q = 0.0;
+  if (!c.writer)
+    return;
+  if (lane < 12)
+    c.v0 = A.prop[(size_t)t * 12 + lane];
+  else if (lane < 15)
+    c.v0 = __ldcg((lane == 12 ? b.cx : lane == 13 ? b.cy : b.cz) + c.m);
+  if (lane < 3 * c.na) {
+    int a = lane / 3, d = lane % 3;
+    c.v1 = __ldcg((d == 0 ? b.x : d == 1 ? b.y : b.z) + c.a0 + a);
+  }
+  if (lane < c.na)
+    c.q = b.q[c.a0 + lane];
+}
+// Stage the gathered inputs in shared memory (by the loading warp).
+__device__ __forceinline__ void ctx_pre_store(ChainShared &S, const CtxPre &c) {
+  const int lane = threadIdx.x & 31;
+  if (lane == 0) {
+    S.b_m = c.m;
+    S.b_a0 = c.a0;
+    S.b_na = c.na;
+    S.b_kind = c.kind;
+    S.b_pacc = c.pacc;
+    S.b_lpacc = c.lpacc;
+  }
+  if (lane < 12)
+    S.b_prop[lane] = c.v0;
+  else if (lane < 15)
+    S.b_com[lane - 12] = c.v0;
+  if (lane < 3 * c.na)
+    S.b_oldp[lane / 3][lane % 3] = c.v1;
+  if (lane < c.na)
+    S.b_q[lane] = c.q;
+}
+
 // CTAs that write part of move t's context: CTA 0 (header) and one CTA
 // per phase row.
 __device__ __forceinline__ unsigned ctx_builders(const ChainArgs &A, int t) {
@@ -538,6 +630,46 @@ __device__ __forceinline__ unsigned ctx_builders(const ChainArgs &A, int t) {
   int na = A.b.mstart[m + 1] - A.b.mstart[m];
   int nrows = A.b.K > 0 ? 2 * na * 3 : 0;
   return (unsigned)max(1, min((int)gridDim.x, nrows));
+}
+
+// FP64 term of one candidate pair of the chain: unit u (atom, old/new side,
+// neighbour cell) against cell slot s: the exact minimum-image distance and
+// cutoff test, the overlap flag for new positions, and the LJ and
+// erfc-screened Coulomb terms, old positions subtracted.
+__device__ __forceinline__ void pair_term(const ChainArgs &A,
+                                          const ChainShared &S, int m, int u,
+                                          int s, double &lj, double &re,
+                                          double &ovl) {
+  const DevBox &b = A.b;
+  const FF &ff = *A.ff;
+  int a = u / (2 * NB27), side = (u / NB27) % 2;
+  const double *pp = S.hdr + (side ? 48 : 24) + 3 * a;
+  const double *pq = (const double *)(b.cell_pos + s);
+  double dx = min_image(pp[0] - __ldcg(pq), b.L[0], b.half[0]);
+  double dy = min_image(pp[1] - __ldcg(pq + 1), b.L[1], b.half[1]);
+  double dz = min_image(pp[2] - __ldcg(pq + 2), b.L[2], b.half[2]);
+  double d2 = dsq3(dx, dy, dz);
+  if (!(ff.rcutSq > d2))
+    return;
+  if (side && d2 < ff.rcutLowSq)
+    ovl = 1.0;
+  double qa = b.q[b.mstart[m] + a];
+  int ka = b.kind[b.mstart[m] + a];
+  int mj = __ldcg(b.cell_meta + s);
+  double e = 0.0;
+  if (ff.electrostatic) {
+    double qq = qa * __ldcg(pq + 3) * QQ_FACT;
+    if (qq != 0.0)
+      e = coulomb_energy(ff, d2, qq);
+  }
+  double l = lj_energy(ff, d2, ka + meta_kind(mj) * ff.n_kinds);
+  if (side) {
+    re += e;
+    lj += l;
+  } else {
+    re += -e;
+    lj += -l;
+  }
 }
 
 __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
@@ -596,6 +728,12 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
 
   const int total_threads = G * CT;
   const int gtid = cta * CT + threadIdx.x;
+  // FP32 candidate pre-test: turn lengths and a cutoff padded by 1e-4 of
+  // Rcut^2 (FP32 and fixed-point rounding stay below 1e-6 of it)
+  const float turn_f[3] = {(float)(b.L[0] * 2.3283064365386963e-10),
+                           (float)(b.L[1] * 2.3283064365386963e-10),
+                           (float)(b.L[2] * 2.3283064365386963e-10)};
+  const float cut_f = (float)(ff.rcutSq * 1.0001);
   // proposals from move t to the next adjustment boundary
   auto make_props = [&](int t0) {
     int t1 = t0;
@@ -628,6 +766,20 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     __syncthreads();
     int m = (int)S.hdr[0];
     int na = (int)S.hdr[2];
+    // The next move's context does not depend on this move's outcome unless
+    // the next move touches the same molecule or follows a settings
+    // adjustment; then it is built after the decision, behind a grid
+    // barrier.  Otherwise warp 7 of each context writer gathers its inputs
+    // during this phase (the loads overlap it) and the writer builds it
+    // right after its partials are out.
+    const bool spec = t + 1 < A.n && A.moves[t + 1].mol != m &&
+                      (A.first + t + 2) % S.set.adj != 0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    CtxPre pre;
+    pre.writer = false;
+    const bool wload = spec && warp == 7;
+    if (wload)
+      ctx_pre1(A, t + 1, pre);
     int nrows = b.K > 0 ? 2 * na * 3 : 0;
     for (int i = threadIdx.x; i < nrows * stride; i += CT)
       tab[i] = __ldcg((const double2 *)(ctx_t + HDR) + i);
@@ -654,6 +806,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
       exy[e] = cmul2(rx[pair_n[p].x], tab_at(rx + stride, pair_n[p].y));
     }
     __syncthreads();
+    if (wload)
+      ctx_pre2(A, t + 1, pre);
     if (threadIdx.x < 32) {
       // inclusive scan of the counts: each lane a contiguous run of units
       int per = (units + 31) / 32;
@@ -683,15 +837,12 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     //     scan over the warps, so the order and every sum stay fixed).
     __shared__ int icl_slot[ICL_MAX];
     __shared__ short icl_unit[ICL_MAX];
-    __shared__ double icl_d2[ICL_MAX];
     __shared__ int icl_warp[CT / 32 + 1];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int icl_n = 0;
     for (int base = cta; base < total; base += total_threads) {
       int idx = base + threadIdx.x * G;
       bool in = false;
       int u = 0, s = 0;
-      double distSq = 0.0;
       if (idx < total) {
         int lo = 0, hi = units - 1;  // last unit whose offset <= idx
         while (lo < hi) {
@@ -703,18 +854,19 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
         }
         u = lo;
         int a = u / (2 * NB27), side = (u / NB27) % 2;
-        const double *pp = S.hdr + (side ? 48 : 24) + 3 * a;
         s = u_cell[u] * b.cap + (idx - u_off[u]);
         int mj = __ldcg(b.cell_meta + s);
         if (meta_mol(mj) != m) {
-          const double *pq = (const double *)(b.cell_pos + s);
-          double dx = min_image(pp[0] - __ldcg(pq), b.L[0], b.half[0]);
-          double dy = min_image(pp[1] - __ldcg(pq + 1), b.L[1], b.half[1]);
-          double dz = min_image(pp[2] - __ldcg(pq + 2), b.L[2], b.half[2]);
-          distSq = dsq3(dx, dy, dz);
-          in = ff.rcutSq > distSq;
-          if (in && side && distSq < ff.rcutLowSq)
-            ovl = 1.0;
+          // FP32 pre-test on the fixed-point turns (the wrapped integer
+          // difference is the minimum image); the exact FP64 test is made
+          // where the listed pairs are evaluated
+          const uint32_t *pt =
+              (const uint32_t *)(S.hdr + 84) + (side * na + a) * 3;
+          uint4 f = __ldcg(b.cell_fix + s);
+          float dx = (float)(int)(pt[0] - f.x) * turn_f[0];
+          float dy = (float)(int)(pt[1] - f.y) * turn_f[1];
+          float dz = (float)(int)(pt[2] - f.z) * turn_f[2];
+          in = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < cut_f;
         }
       }
       unsigned mask = __ballot_sync(0xffffffffu, in);
@@ -736,23 +888,9 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
         if (pos < ICL_MAX) {
           icl_slot[pos] = s;
           icl_unit[pos] = (short)u;
-          icl_d2[pos] = distSq;
         } else {
           // past the list (not met at liquid densities): evaluated here
-          int a = u / (2 * NB27), side = (u / NB27) % 2;
-          int mj = __ldcg(b.cell_meta + s);
-          double qa = b.q[b.mstart[m] + a];
-          int ka = b.kind[b.mstart[m] + a];
-          double e = 0.0;
-          if (ff.electrostatic) {
-            double qq =
-                qa * __ldcg((const double *)(b.cell_pos + s) + 3) * QQ_FACT;
-            if (qq != 0.0)
-              e = coulomb_energy(ff, distSq, qq);
-          }
-          double l = lj_energy(ff, distSq, ka + meta_kind(mj) * ff.n_kinds);
-          re += side ? e : -e;
-          lj += side ? l : -l;
+          pair_term(A, S, m, u, s, lj, re, ovl);
         }
       }
       icl_n = icl_warp[CT / 32];
@@ -765,29 +903,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     //     instead of after them.
     const int n_eval = min(icl_n, ICL_MAX);
     if (warp == 3) {
-      for (int i = lane; i < n_eval; i += 32) {
-        int u = icl_unit[i], s = icl_slot[i];
-        int a = u / (2 * NB27), side = (u / NB27) % 2;
-        double qa = b.q[b.mstart[m] + a];
-        int ka = b.kind[b.mstart[m] + a];
-        int mj = __ldcg(b.cell_meta + s);
-        double qj = __ldcg((const double *)(b.cell_pos + s) + 3);
-        double d2 = icl_d2[i];
-        double e = 0.0;
-        if (ff.electrostatic) {
-          double qq = qa * qj * QQ_FACT;
-          if (qq != 0.0)
-            e = coulomb_energy(ff, d2, qq);
-        }
-        double l = lj_energy(ff, d2, ka + meta_kind(mj) * ff.n_kinds);
-        if (side) {
-          re += e;
-          lj += l;
-        } else {
-          re += -e;
-          lj += -l;
-        }
-      }
+      for (int i = lane; i < n_eval; i += 32)
+        pair_term(A, S, m, icl_unit[i], icl_slot[i], lj, re, ovl);
     }
     if (warp != 3 && warp != 7) {
       const int kw = warp < 3 ? warp : warp - 1;  // 0..5
@@ -857,15 +974,24 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     // publishes only after those builds are counted in, so one published
     // word orders the decision, the commit and the next context before
     // every CTA's next phase A.
-    const bool spec = t + 1 < A.n && A.moves[t + 1].mol != m &&
-                      (A.first + t + 2) % S.set.adj != 0;
     const bool leader = cta == G - 1;
     // threads of this CTA that build its part of the next context (when it
-    // is a builder): warps 1..7, or warps 4..7 in the leader
+    // is a writer): warps 1..7, or warps 4..7 in the leader, from the inputs
+    // warp 7 gathered during phase A, with the FP64 pipes free
     const int bfirst = leader ? 128 : 32;
     if ((int)threadIdx.x >= bfirst) {
-      if (spec)
-        build_ctx(A, S, t + 1, nullptr, 0, bfirst, CT - bfirst, true);
+      if (spec) {
+        if (warp == 7) {
+          if (pre.writer)
+            ctx_pre_store(S, pre);
+          if (lane == 0)
+            S.b_writer = pre.writer;
+        }
+        group_sync(CT - bfirst);
+        if (S.b_writer)
+          build_ctx_rest(A, S, t + 1, (int)threadIdx.x - bfirst, CT - bfirst,
+                         true);
+      }
     } else if (leader) {
       // Warps 0..3 of the leader each gather one quantity over all CTAs
       // (LJ, real space, reciprocal energy, overlap), polling the values
@@ -976,7 +1102,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
             stay = __ldcg(b.atom_cell + a0 + a) == c1;
             if (stay)
               cell_write_slot(b, c1, __ldcg(b.atom_slot + a0 + a), a0 + a,
-                              np[0], np[1], np[2]);
+                              np[0], np[1], np[2],
+                              (const uint32_t *)(S.hdr + 84) + (na + a) * 3);
           }
           unsigned moving = __ballot_sync(0xffffffffu, a < na && !stay);
           __syncwarp();
@@ -985,7 +1112,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
               if (moving & (1u << i)) {
                 const double *np = S.hdr + 48 + 3 * i;
                 cell_move_atom(b, a0 + i, np[0], np[1], np[2],
-                               (int)S.hdr[16 + i]);
+                               (int)S.hdr[16 + i],
+                               (const uint32_t *)(S.hdr + 84) + (na + i) * 3);
               }
             if ((int)S.hdr[1] == 0) {
               b.cx[m] = S.hdr[4];
@@ -1455,8 +1583,8 @@ int mc_init(Box &b, const gb_mc_params &p) {
   if (per_sm < 1)
     return b.Fail(ERR_UNSUPPORTED, "chain kernel does not fit on an SM");
   s.grid = b.sm_count;
-  if (s.grid > PART_MAX_GRID)
-    return b.Fail(ERR_UNSUPPORTED, "more SMs than the chain's leader holds");
+  if (s.grid > PART_MAX_GRID || s.grid < 2)
+    return b.Fail(ERR_UNSUPPORTED, "the chain needs 2 to 256 SMs");
   if (p.move_buffer < 0)
     return b.Fail(ERR_ARG, "move_buffer must be >= 0");
   s.move_cap = p.move_buffer > 0 ? (size_t)p.move_buffer : (size_t)1 << 16;
