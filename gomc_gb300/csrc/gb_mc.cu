@@ -1001,22 +1001,39 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
       const int q = warp;
       double *part_t = A.part + (size_t)(t & 1) * G * 4;
       constexpr int PF = PART_MAX_GRID / 32;
-      double pv[PF];
-      int ok = 1;
-      unsigned it = 0;
-      for (;;) {
-        bool mine = true;
+      // two polls in flight, staggered, so that a check comes about every
+      // half memory round trip
+      double pv[PF], pw[PF];
+      auto issue = [&](double *dst) {
 #pragma unroll
         for (int i = 0; i < PF; ++i) {
           int c = lane + 32 * i;
-          pv[i] = 0.0;
-          if (c < G) {
-            pv[i] = __ldcg(part_t + (size_t)c * 4 + q);
-            mine &= __double_as_longlong(pv[i]) != (long long)PART_EMPTY;
-          }
+          dst[i] = c < G ? __ldcg(part_t + (size_t)c * 4 + q) : 0.0;
         }
-        if (__all_sync(0xffffffffu, mine))
+      };
+      auto present = [&](const double *src) {
+        bool mine = true;
+#pragma unroll
+        for (int i = 0; i < PF; ++i)
+          mine &= __double_as_longlong(src[i]) != (long long)PART_EMPTY;
+        return __all_sync(0xffffffffu, mine);
+      };
+      issue(pv);
+      __nanosleep(200);
+      issue(pw);
+      int ok = 1;
+      unsigned it = 0;
+      for (;;) {
+        if (present(pv))
           break;
+        issue(pv);
+        if (present(pw)) {
+#pragma unroll
+          for (int i = 0; i < PF; ++i)
+            pv[i] = pw[i];
+          break;
+        }
+        issue(pw);
         int bad = 0;
         if (lane == 0) {
           if (++it > SPIN_LIMIT) {
@@ -1065,6 +1082,17 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
       ok = S.red3[0][0] != 0.0 && S.red3[0][1] != 0.0 && S.red3[0][2] != 0.0 &&
            S.red3[0][3] != 0.0;
       int acc = 0;
+      if (warp == 1 && ok) {
+        // the writers' flags of the next context, checked while warp 0
+        // decides and commits
+        int bok = spec ? warp_wait_all(A.seq + SEQ_PART + SEQ_STRIDE,
+                                       (int)ctx_builders(A, t + 1),
+                                       (unsigned)(t + 1), b.err)
+                       : 1;
+        if (lane == 0)
+          S.red3[1][0] = bok;
+        asm volatile("bar.sync 3, 64;" ::: "memory");
+      }
       if (warp == 0 && ok) {
         double dLJ = 0.0, dRe = 0.0, dRc = 0.0;
         if (lane == 0) {
@@ -1124,10 +1152,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
           __syncwarp();
         }
         // the next context must be complete before the word goes out
-        if (spec)
-          ok = warp_wait_all(A.seq + SEQ_PART + SEQ_STRIDE,
-                             (int)ctx_builders(A, t + 1), (unsigned)(t + 1),
-                             b.err);
+        asm volatile("bar.sync 3, 64;" ::: "memory");
+        ok = S.red3[1][0] != 0.0;
         if (lane == 0 && ok) {
           __threadfence();
           st_release(A.seq, 2u * (unsigned)(t + 1) + (unsigned)acc);
