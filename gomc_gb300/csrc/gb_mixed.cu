@@ -18,9 +18,10 @@
 //     cluster barrier every CTA adds the partials in one order, takes the
 //     same Metropolis decision (FP64 exponent against log u) and, on accept,
 //     folds dS into its accumulators.
-// Structure factors are FP64 accumulators in shared memory; accepted deltas
-// are staged in an FP32 two-sum window and folded into FP64 every
-// `flush_every` accepted moves.  Running energies are FP64.
+// Structure factors are float-float accumulators (an FP32 value and its
+// FP32 remainder, about 48 bits) in shared memory, updated by an error-free
+// sum on every accepted move; they are read from and written back to the
+// box's FP64 arrays at launch boundaries.  Running energies are FP64.
 #include "gb_cells.cuh"
 #include "gb_f32math.cuh"
 #include "gb_mc.h"
@@ -58,21 +59,21 @@ struct MShared {
   double wred[MT_THREADS / 32][4];
   double prop[12];
   int accept;
-  int nacc;              // accepted moves since the last flush
 };
 
-// Byte offsets of the per-CTA k-chunk arrays.  The hot arrays, read by every
-// move (FP32 structure factors s32R/I, this move's changes dR/dI, prefactors
-// pf, integer k), always live in dynamic shared memory: 24 B per k-vector.
-// The cold arrays, touched only on accept and fold (FP64 accumulators s64R/I,
-// two-sum window pRh/pRl/pIh/pIl), follow them in shared memory when the
-// chunk fits, else in a per-chain global buffer with the same offsets
-// (32 B per k-vector and CTA).  Every array starts on a 16-byte boundary
-// whatever the chunk length.
-// array starts on a 16-byte boundary whatever the chunk length.
+// Byte offsets of the per-CTA k-chunk arrays.  The structure factor of each
+// k-vector is held in float-float: s32 (its FP32 value, read by every move)
+// plus lo (the remainder), updated on every accepted move by an error-free
+// sum and renormalised, so it carries about 48 bits without FP64 storage.
+// The arrays read by every move (s32R/I, this move's changes dR/dI,
+// prefactors pf, integer k) always live in dynamic shared memory, 24 B per
+// k-vector; the remainders loR/I (8 B, touched on accept) follow them when
+// the chunk fits, else they sit in a per-chain global buffer with the same
+// offsets.  Every array starts on a 16-byte boundary whatever the chunk
+// length.
 struct MixedLayout {
   size_t kcs;   // padded chunk length (multiple of 4)
-  size_t cold;  // offset of the cold arrays (in shared memory or the buffer)
+  size_t cold;  // offset of the remainders (in shared memory or the buffer)
   size_t tab;   // offset of the phase rows in shared memory
 };
 __host__ __device__ __forceinline__ MixedLayout mixed_layout(int kc_max,
@@ -80,11 +81,11 @@ __host__ __device__ __forceinline__ MixedLayout mixed_layout(int kc_max,
   MixedLayout L;
   L.kcs = ((size_t)kc_max + 3) & ~(size_t)3;
   L.cold = 24 * L.kcs;
-  L.tab = cold_smem ? L.cold + 32 * L.kcs : L.cold;
+  L.tab = cold_smem ? L.cold + 8 * L.kcs : L.cold;
   return L;
 }
 __host__ __device__ __forceinline__ size_t mixed_cold_bytes(int kc_max) {
-  return 32 * (((size_t)kc_max + 3) & ~(size_t)3);
+  return 8 * (((size_t)kc_max + 3) & ~(size_t)3);
 }
 
 // Whether cells c1 and c2 are in one another's 27-cell neighbourhood (every
@@ -256,20 +257,17 @@ __global__ void __launch_bounds__(MT_THREADS)
   char4 *kn = (char4 *)(pf + L.kcs);
   unsigned char *cb = cold_smem ? dyn + L.cold
                                 : C.cold + (size_t)rank * mixed_cold_bytes(kc_max);
-  double *s64R = (double *)cb, *s64I = s64R + L.kcs;
-  float *pRh = (float *)(s64I + L.kcs), *pRl = pRh + L.kcs, *pIh = pRl + L.kcs,
-        *pIl = pIh + L.kcs;
+  float *loR = (float *)cb, *loI = loR + L.kcs;
   float2 *tab = (float2 *)(dyn + L.tab);
   const int stride = b.kmax + 1;
 
   for (int i = threadIdx.x; i < kc; i += MT_THREADS) {
     int k = kbeg + i;
     double r = b.sumRref[k], im = b.sumIref[k];
-    s64R[i] = r;
-    s64I[i] = im;
     s32R[i] = (float)r;
     s32I[i] = (float)im;
-    pRh[i] = pRl[i] = pIh[i] = pIl[i] = 0.0f;
+    loR[i] = (float)(r - (double)s32R[i]);
+    loI[i] = (float)(im - (double)s32I[i]);
     pf[i] = b.prefact_f[k];
     kn[i] = b.kn[k];
   }
@@ -277,7 +275,6 @@ __global__ void __launch_bounds__(MT_THREADS)
     S.set = *C.set;
     for (int i = 0; i < 5; ++i)
       S.e_run[i] = b.energy[i];
-    S.nacc = 0;
   }
   __syncthreads();
   const int tpc = MT_THREADS * csize;
@@ -292,15 +289,6 @@ __global__ void __launch_bounds__(MT_THREADS)
     }
     for (int t = t0 + gt; t < t1; t += tpc)
       make_proposal(C.moves[t], S.set, C.prop + (size_t)t * 12);
-  };
-  auto flush = [&]() {
-    for (int i = threadIdx.x; i < kc; i += MT_THREADS) {
-      s64R[i] += (double)pRh[i] + (double)pRl[i];
-      s64I[i] += (double)pIh[i] + (double)pIl[i];
-      pRh[i] = pRl[i] = pIh[i] = pIl[i] = 0.0f;
-      s32R[i] = (float)s64R[i];
-      s32I[i] = (float)s64I[i];
-    }
   };
 
   if (C.n > 0) {
@@ -575,7 +563,6 @@ __global__ void __launch_bounds__(MT_THREADS)
           S.e_run[0] += dLJ;
           S.e_run[1] += dRe;
           S.e_run[2] += dRc;
-          S.nacc++;
         }
         settings_update(S.set, h.kind, acc);
         S.accept = acc;
@@ -594,10 +581,15 @@ __global__ void __launch_bounds__(MT_THREADS)
     const int prev_m = m, prev_kind = h.kind;
     if (acc) {
       for (int i = threadIdx.x; i < kc; i += MT_THREADS) {
-        two_sum_add(pRh[i], pRl[i], dR[i]);
-        two_sum_add(pIh[i], pIl[i], dI[i]);
-        s32R[i] += dR[i];
-        s32I[i] += dI[i];
+        // (s32 + lo) += d, error-free sum then renormalised
+        ff2 r = ff_two_sum(s32R[i], dR[i]);
+        ff2 im = ff_two_sum(s32I[i], dI[i]);
+        r = ff_quick(r.hi, r.lo + loR[i]);
+        im = ff_quick(im.hi, im.lo + loI[i]);
+        s32R[i] = r.hi;
+        loR[i] = r.lo;
+        s32I[i] = im.hi;
+        loI[i] = im.lo;
       }
       if (rank == 0 && threadIdx.x == 0) {
         for (int a = 0; a < na; ++a) {
@@ -613,12 +605,6 @@ __global__ void __launch_bounds__(MT_THREADS)
           b.cy[m] = h.newcom[1];
           b.cz[m] = h.newcom[2];
         }
-      }
-      if (S.nacc >= C.flush_every) {
-        __syncthreads();
-        flush();
-        if (threadIdx.x == 0)
-          S.nacc = 0;
       }
     }
     if (t + 1 < C.n) {
@@ -638,11 +624,9 @@ __global__ void __launch_bounds__(MT_THREADS)
     cluster.sync();  // the cell grid committed by rank 0 is visible
   }
   __syncthreads();
-  flush();
-  __syncthreads();
   for (int i = threadIdx.x; i < kc; i += MT_THREADS) {
-    b.sumRref[kbeg + i] = s64R[i];
-    b.sumIref[kbeg + i] = s64I[i];
+    b.sumRref[kbeg + i] = (double)s32R[i] + (double)loR[i];
+    b.sumIref[kbeg + i] = (double)s32I[i] + (double)loI[i];
   }
   if (rank == 0 && threadIdx.x == 0) {
     *C.set = S.set;

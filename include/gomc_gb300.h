@@ -174,7 +174,9 @@ typedef struct gb_mc_params {
   double scales[4];       /* displacement, rotation, MP t_max, MP r_max */
   int32_t recompute_freq; /* GB300RecomputeFreq (mixed form), 0 = never */
   int32_t cluster_size;   /* mixed form: CTAs per chain (0 = autotuned) */
-  int32_t flush_every;    /* mixed form: accepted moves per FP64 fold (0 = 64) */
+  int32_t flush_every;    /* not used (kept for layout): the mixed form's
+                             structure factors are float-float and need no
+                             periodic FP64 fold */
   int32_t move_buffer;    /* moves drawn and uploaded per chunk (0 = 65536) */
 } gb_mc_params;
 
