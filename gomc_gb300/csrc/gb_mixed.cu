@@ -51,7 +51,7 @@ struct MHdr {
 };
 
 struct MShared {
-  MHdr h;
+  MHdr hh[2];  // this move's header and the next one's, by move parity
   Settings set;
   double e_run[5];
   double part[4];        // this CTA's partial: LJ, real, recip, overlap
@@ -144,12 +144,14 @@ __device__ __forceinline__ float2 tabf(const float2 *row, int n) {
   return v;
 }
 
-// Header of move t (all threads of the CTA call it).
+// Header of move t into h (all threads of the CTA call it); prev is the
+// previous move's header, whose new positions are the current ones when
+// that move was accepted and touched the same molecule.
 __device__ void mixed_header(const MixedChain &C, MShared &S, int t,
-                             bool prev_acc, int prev_m, int prev_kind) {
+                             bool prev_acc, int prev_m, int prev_kind,
+                             const MHdr &prev, MHdr &h) {
   const DevBox &b = C.b;
   const MoveRec &r = C.moves[t];
-  MHdr &h = S.h;
   int m = r.mol;
   int a0 = b.mstart[m], na = b.mstart[m + 1] - a0;
   bool same = prev_acc && prev_m == m;
@@ -160,12 +162,12 @@ __device__ void mixed_header(const MixedChain &C, MShared &S, int t,
   if (threadIdx.x < 3) {
     int d = threadIdx.x;
     const double *cs[3] = {b.cx, b.cy, b.cz};
-    com[d] = (same && prev_kind == 0) ? h.newcom[d] : __ldcg(cs[d] + m);
+    com[d] = (same && prev_kind == 0) ? prev.newcom[d] : __ldcg(cs[d] + m);
   }
   if (threadIdx.x >= 32 && threadIdx.x < 32 + 3 * na) {
     int i = threadIdx.x - 32, a = i / 3, d = i % 3;
     const double *xs[3] = {b.x, b.y, b.z};
-    oldp[a][d] = same ? h.newp[a][d] : __ldcg(xs[d] + a0 + a);
+    oldp[a][d] = same ? prev.newp[a][d] : __ldcg(xs[d] + a0 + a);
   }
   __syncthreads();
   if (threadIdx.x < na) {
@@ -224,13 +226,13 @@ __device__ void mixed_header(const MixedChain &C, MShared &S, int t,
 }
 
 // Phase rows exp(2 pi i n P / 2^32), n = 0..kmax, for every atom and axis.
-__device__ __forceinline__ void mixed_tables(const MixedChain &C, MShared &S,
-                                             float2 *tab) {
+__device__ __forceinline__ void mixed_tables(const MixedChain &C,
+                                             const MHdr &h, float2 *tab) {
   int stride = C.b.kmax + 1;
-  int rows = 3 * S.h.na;
+  int rows = 3 * h.na;
   for (int i = threadIdx.x; i < rows * stride; i += MT_THREADS) {
     int row = i / stride, n = i % stride;
-    uint32_t P = S.h.P[row / 3][row % 3];
+    uint32_t P = h.P[row / 3][row % 3];
     tab[i] = cis_turns((uint32_t)n * P);
   }
 }
@@ -258,7 +260,9 @@ __global__ void __launch_bounds__(MT_THREADS)
   unsigned char *cb = cold_smem ? dyn + L.cold
                                 : C.cold + (size_t)rank * mixed_cold_bytes(kc_max);
   float *loR = (float *)cb, *loI = loR + L.kcs;
-  float2 *tab = (float2 *)(dyn + L.tab);
+  // phase rows of this move and the next, by move parity
+  float2 *const tabs = (float2 *)(dyn + L.tab);
+  const size_t tab_len = (size_t)3 * MAXA * (b.kmax + 1);
   const int stride = b.kmax + 1;
 
   for (int i = threadIdx.x; i < kc; i += MT_THREADS) {
@@ -297,8 +301,8 @@ __global__ void __launch_bounds__(MT_THREADS)
     __syncthreads();
     make_props(0);
     cluster.sync();
-    mixed_header(C, S, 0, false, -1, 0);
-    mixed_tables(C, S, tab);
+    mixed_header(C, S, 0, false, -1, 0, S.hh[1], S.hh[0]);
+    mixed_tables(C, S.hh[0], tabs);
     __syncthreads();
   }
   const float rc2 = (float)ff.rcutSq;
@@ -314,8 +318,14 @@ __global__ void __launch_bounds__(MT_THREADS)
                       b.cellSize[2] * b.cellSize[2] < ff.rcutSq;
 
   for (int t = 0; t < C.n; ++t) {
-    const MHdr &h = S.h;
+    const MHdr &h = S.hh[t & 1];
+    const float2 *const tab = tabs + (t & 1) * tab_len;
     const int m = h.m, na = h.na;
+    // The next header does not depend on this move's outcome unless the
+    // next move touches the same molecule or follows a settings adjustment:
+    // then it is built during the cluster barrier before the decision.
+    const bool spec = t + 1 < C.n && C.moves[t + 1].mol != m &&
+                      (C.first + t + 2) % S.set.adj != 0;
     // ---------------- real space ----------------
     // Each neighbour j is taken once: from the new position's cells when it
     // is inside the cutoff there (then as the difference u(r') - u(r) if it
@@ -324,170 +334,204 @@ __global__ void __launch_bounds__(MT_THREADS)
     float lj_h = 0.f, lj_l = 0.f, re_h = 0.f, re_l = 0.f, ovl = 0.f;
     const int units = na * 2 * NB27;
     const int lane128 = threadIdx.x & 127, half = threadIdx.x >> 7;
-    for (int ub = rank * 2; ub < units; ub += 2 * csize) {
-      int u = ub + half;
-      if (u >= units)
-        continue;
+    // the units' neighbour cells and slot counts, all at once
+    __shared__ int mu_c2[2 * MAXA * NB27], mu_n2[2 * MAXA * NB27];
+    for (int u = threadIdx.x; u < units; u += MT_THREADS) {
       int a = u / (2 * NB27), side = (u / NB27) % 2, nn = u % NB27;
       int cell = side ? h.cell_new[a] : h.cell_old[a];
       int c2 = b.nbr[cell * NB27 + nn];
-      int n2 = __ldcg(b.cell_count + c2);
+      mu_c2[u] = c2;
+      mu_n2[u] = __ldcg(b.cell_count + c2);
+    }
+    __syncthreads();
+    // one candidate: unit u against cell slot s (meta mj, fixed-point slot f)
+    auto pair = [&](int u, size_t s, int mj, uint4 f) {
+      if (meta_mol(mj) == m)
+        return;
+      const int a = u / (2 * NB27), side = (u / NB27) % 2;
+      const int c2 = mu_c2[u];
       const uint32_t *uo = h.uo[a], *un = h.un[a];
-      float ddx = (float)(int32_t)(un[0] - uo[0]) * sx;
-      float ddy = (float)(int32_t)(un[1] - uo[1]) * sy;
-      float ddz = (float)(int32_t)(un[2] - uo[2]) * sz;
-      float qa = h.qs[a], qa_lo = h.qslo[a];
-      int ka = h.ka[a];
-      for (int j = lane128; j < n2; j += 128) {
-        size_t s = (size_t)c2 * b.cap + j;
-        int mj = __ldcg(b.cell_meta + s);
-        if (meta_mol(mj) == m)
-          continue;
-        uint4 f = __ldcg(b.cell_fix + s);
-        int32_t ox = (int32_t)(uo[0] - f.x), oy = (int32_t)(uo[1] - f.y),
-                oz = (int32_t)(uo[2] - f.z);
-        int32_t nx_ = (int32_t)(un[0] - f.x), ny_ = (int32_t)(un[1] - f.y),
-                nz_ = (int32_t)(un[2] - f.z);
-        float dox = (float)ox * sx, doy = (float)oy * sy, doz = (float)oz * sz;
-        float dnx = (float)nx_ * sx, dny = (float)ny_ * sy, dnz = (float)nz_ * sz;
-        float r2o = fmaf(dox, dox, fmaf(doy, doy, doz * doz));
-        float r2n = fmaf(dnx, dnx, fmaf(dny, dny, dnz * dnz));
-        // inside-cutoff decisions, exact in FP64 within 1e-5 of the cutoff
-        bool in_o = r2o < rc2, in_n = r2n < rc2;
-        bool amb_o = fabsf(r2o - rc2) <= rc2 * 1e-5f;
-        bool amb_n = fabsf(r2n - rc2) <= rc2 * 1e-5f;
-        bool amb_l = side && r2n < rl2 * 1.00001f;
-        if (side ? (!in_n && !amb_n) : (!in_o && !amb_o))
-          continue;
-        if (amb_o || amb_n || amb_l) {
-          const double *pp = (const double *)(b.cell_pos + s);
-          double px = __ldcg(pp), py = __ldcg(pp + 1), pz = __ldcg(pp + 2);
-          if (amb_o) {
-            const double *mp = h.oldp[a];
-            double d2 = dsq3(min_image(mp[0] - px, b.L[0], b.half[0]),
-                             min_image(mp[1] - py, b.L[1], b.half[1]),
-                             min_image(mp[2] - pz, b.L[2], b.half[2]));
-            in_o = ff.rcutSq > d2;
-          }
-          if (amb_n || amb_l) {
-            const double *mp = h.newp[a];
-            double d2 = dsq3(min_image(mp[0] - px, b.L[0], b.half[0]),
-                             min_image(mp[1] - py, b.L[1], b.half[1]),
-                             min_image(mp[2] - pz, b.L[2], b.half[2]));
-            in_n = ff.rcutSq > d2;
-            if (side && in_n && d2 < ff.rcutLowSq)
-              ovl = 1.f;
-          }
+      const float ddx = (float)(int32_t)(un[0] - uo[0]) * sx;
+      const float ddy = (float)(int32_t)(un[1] - uo[1]) * sy;
+      const float ddz = (float)(int32_t)(un[2] - uo[2]) * sz;
+      const float qa = h.qs[a], qa_lo = h.qslo[a];
+      const int ka = h.ka[a];
+      int32_t ox = (int32_t)(uo[0] - f.x), oy = (int32_t)(uo[1] - f.y),
+              oz = (int32_t)(uo[2] - f.z);
+      int32_t nx_ = (int32_t)(un[0] - f.x), ny_ = (int32_t)(un[1] - f.y),
+              nz_ = (int32_t)(un[2] - f.z);
+      float dox = (float)ox * sx, doy = (float)oy * sy, doz = (float)oz * sz;
+      float dnx = (float)nx_ * sx, dny = (float)ny_ * sy, dnz = (float)nz_ * sz;
+      float r2o = fmaf(dox, dox, fmaf(doy, doy, doz * doz));
+      float r2n = fmaf(dnx, dnx, fmaf(dny, dny, dnz * dnz));
+      // inside-cutoff decisions, exact in FP64 within 1e-5 of the cutoff
+      bool in_o = r2o < rc2, in_n = r2n < rc2;
+      bool amb_o = fabsf(r2o - rc2) <= rc2 * 1e-5f;
+      bool amb_n = fabsf(r2n - rc2) <= rc2 * 1e-5f;
+      bool amb_l = side && r2n < rl2 * 1.00001f;
+      if (side ? (!in_n && !amb_n) : (!in_o && !amb_o))
+        return;
+      if (amb_o || amb_n || amb_l) {
+        const double *pp = (const double *)(b.cell_pos + s);
+        double px = __ldcg(pp), py = __ldcg(pp + 1), pz = __ldcg(pp + 2);
+        if (amb_o) {
+          const double *mp = h.oldp[a];
+          double d2 = dsq3(min_image(mp[0] - px, b.L[0], b.half[0]),
+                           min_image(mp[1] - py, b.L[1], b.half[1]),
+                           min_image(mp[2] - pz, b.L[2], b.half[2]));
+          in_o = ff.rcutSq > d2;
         }
-        // With cells narrower than the cutoff a pair inside it may lie
-        // outside the other position's neighbourhood, where it is not summed.
-        if (narrow && in_o && in_n &&
-            !cells_adjacent(b, c2, side ? h.cell_old[a] : h.cell_new[a])) {
-          if (side)
-            in_o = false;
-          else
-            in_n = false;
+        if (amb_n || amb_l) {
+          const double *mp = h.newp[a];
+          double d2 = dsq3(min_image(mp[0] - px, b.L[0], b.half[0]),
+                           min_image(mp[1] - py, b.L[1], b.half[1]),
+                           min_image(mp[2] - pz, b.L[2], b.half[2]));
+          in_n = ff.rcutSq > d2;
+          if (side && in_n && d2 < ff.rcutLowSq)
+            ovl = 1.f;
         }
-        int kj = meta_kind(mj);
-        int idx = ka + kj * ff.n_kinds;
-        // q_i q_j QQ_FACT / (1 + eta) = qq + qc up to FP32 rounding of the
-        // remainder qc: the pair's charge product carries no systematic FP32
-        // bias, and qc also takes up the FP32 turn length (FF::coul_qfac_f)
-        float qb = __uint_as_float(f.w);
-        float qq = qa * qb;
-        bool coul = ff.electrostatic && qq != 0.f;
-        float qres = 0.f, qc = 0.f;
-        if (coul) {
-          qres = fmaf(qa, qb, -qq) + fmaf(qa, __ldcg(b.cell_qlo + s), qa_lo * qb);
-          qc = fmaf(qq, ff.coul_qfac_f, qres);
-        }
-        // Coulomb cutoff: the pair cutoff decision when it is the larger one
-        bool cin_o = coul_cut ? r2o <= rcc2 : true;
-        bool cin_n = coul_cut ? r2n <= rcc2 : true;
-        float sg2 = ff.sigmaSq_f[idx], ecn = ff.eps_cn_f[idx];
-        float k6 = ff.lj_k6_f[idx], k3 = ff.lj_k3_f[idx];
-        if (side) {
-          if (!in_n)
-            continue;
-          if (in_o) {
-            const int32_t o3[3] = {ox, oy, oz}, n3[3] = {nx_, ny_, nz_};
-            if (r2o < ff.close_r2_f && r2n < ff.close_r2_f) {
-              // close pair: both differences in float-float from the exact
-              // squared distances, added with their rounding residuals
-              ClosePair cp = close_pair(o3, n3, ff.turn2_hi, ff.turn2_lo);
-              if (ecn != 0.0f) {
-                ff2 du = close_lj(cp, {sg2, ff.sigmaSq_lo_f[idx]},
-                                  {ecn, ff.eps_cn_lo_f[idx]});
-                two_sum_add(lj_h, lj_l, du.hi);
-                lj_l += du.lo;
-              }
-              if (coul && cin_n && cin_o) {
-                ff2 X = close_coulomb(cp, ff.ewald, ff.alpha2_f,
-                                      {ff.alpha3_hi, ff.alpha3_lo});
-                float pr = qq * X.hi;
-                two_sum_add(re_h, re_l, pr);
-                re_l += fmaf(qq, X.hi, -pr) + fmaf(qres, X.hi, qq * X.lo);
-              }
-              continue;
+      }
+      // With cells narrower than the cutoff a pair inside it may lie
+      // outside the other position's neighbourhood, where it is not summed.
+      if (narrow && in_o && in_n &&
+          !cells_adjacent(b, c2, side ? h.cell_old[a] : h.cell_new[a])) {
+        if (side)
+          in_o = false;
+        else
+          in_n = false;
+      }
+      int kj = meta_kind(mj);
+      int idx = ka + kj * ff.n_kinds;
+      // q_i q_j QQ_FACT / (1 + eta) = qq + qc up to FP32 rounding of the
+      // remainder qc: the pair's charge product carries no systematic FP32
+      // bias, and qc also takes up the FP32 turn length (FF::coul_qfac_f)
+      float qb = __uint_as_float(f.w);
+      float qq = qa * qb;
+      bool coul = ff.electrostatic && qq != 0.f;
+      float qres = 0.f, qc = 0.f;
+      if (coul) {
+        qres = fmaf(qa, qb, -qq) + fmaf(qa, __ldcg(b.cell_qlo + s), qa_lo * qb);
+        qc = fmaf(qq, ff.coul_qfac_f, qres);
+      }
+      // Coulomb cutoff: the pair cutoff decision when it is the larger one
+      bool cin_o = coul_cut ? r2o <= rcc2 : true;
+      bool cin_n = coul_cut ? r2n <= rcc2 : true;
+      float sg2 = ff.sigmaSq_f[idx], ecn = ff.eps_cn_f[idx];
+      float k6 = ff.lj_k6_f[idx], k3 = ff.lj_k3_f[idx];
+      if (side) {
+        if (!in_n)
+          return;
+        if (in_o) {
+          const int32_t o3[3] = {ox, oy, oz}, n3[3] = {nx_, ny_, nz_};
+          if (r2o < ff.close_r2_f && r2n < ff.close_r2_f) {
+            // close pair: both differences in float-float from the exact
+            // squared distances, added with their rounding residuals
+            ClosePair cp = close_pair(o3, n3, ff.turn2_hi, ff.turn2_lo);
+            if (ecn != 0.0f) {
+              ff2 du = close_lj(cp, {sg2, ff.sigmaSq_lo_f[idx]},
+                                {ecn, ff.eps_cn_lo_f[idx]});
+              two_sum_add(lj_h, lj_l, du.hi);
+              lj_l += du.lo;
             }
-            // difference of the pair terms between r and r'
-            // (d + d') in FP32: the integer sum can leave the int32 range
-            float dr2 = fmaf(ddx, dox + dnx, fmaf(ddy, doy + dny, ddz * (doz + dnz)));
-            float so = sg2 / r2o, sn = sg2 / r2n;
-            float ds = -sg2 * dr2 / (r2o * r2n);
-            float so3 = so * so * so, sn3 = sn * sn * sn;
-            float d3 = ds * fmaf(sn, sn, fmaf(sn, so, so * so));
-            float s33 = sn3 + so3;
-            two_sum_add(lj_h, lj_l,
-                        ecn * d3 * ((s33 - 1.0f) + fmaf(s33, k6, -k3)));
             if (coul && cin_n && cin_o) {
-              if (ff.ewald && r2o >= ff.far_r2_f && r2n >= ff.far_r2_f) {
-                float X = fp32_bracket(r2o, r2n, dr2, alpha, ff.coul_da_f);
-                two_sum_add(re_h, re_l, fmaf(qq, X, qc * X));
-              } else {
-                // the erfc form on the exact distances (float-float r,
-                // alpha r and their differences)
-                ClosePair cp = close_pair(o3, n3, ff.turn2_hi, ff.turn2_lo);
-                float X = ff.ewald
-                              ? far_coulomb(cp, {ff.alpha_f, ff.alpha_lo_f})
-                              : close_coulomb(cp, false, 0.0f, {0.0f, 0.0f}).hi;
-                two_sum_add(re_h, re_l, fmaf(qq, X, qres * X));
-              }
-            } else if (coul) {
-              if (cin_n) {
-                float rr = sqrtf(r2n);
-                float X = ff.ewald ? erfc_f32(alpha * rr) / rr : 1.0f / rr;
-                two_sum_add(re_h, re_l, fmaf(qq, X, qc * X));
-              }
-              if (cin_o) {
-                float rr = sqrtf(r2o);
-                float X = ff.ewald ? erfc_f32(alpha * rr) / rr : 1.0f / rr;
-                two_sum_add(re_h, re_l, -fmaf(qq, X, qc * X));
-              }
+              ff2 X = close_coulomb(cp, ff.ewald, ff.alpha2_f,
+                                    {ff.alpha3_hi, ff.alpha3_lo});
+              float pr = qq * X.hi;
+              two_sum_add(re_h, re_l, pr);
+              re_l += fmaf(qq, X.hi, -pr) + fmaf(qres, X.hi, qq * X.lo);
             }
-          } else {
-            float rr2 = sg2 / r2n, r6 = rr2 * rr2 * rr2, r12 = r6 * r6;
-            two_sum_add(lj_h, lj_l,
-                        ecn * ((r12 - r6) + fmaf(r12, k6, -r6 * k3)));
-            if (coul && cin_n) {
+            return;
+          }
+          // difference of the pair terms between r and r'
+          // (d + d') in FP32: the integer sum can leave the int32 range
+          float dr2 = fmaf(ddx, dox + dnx, fmaf(ddy, doy + dny, ddz * (doz + dnz)));
+          float so = sg2 / r2o, sn = sg2 / r2n;
+          float ds = -sg2 * dr2 / (r2o * r2n);
+          float so3 = so * so * so, sn3 = sn * sn * sn;
+          float d3 = ds * fmaf(sn, sn, fmaf(sn, so, so * so));
+          float s33 = sn3 + so3;
+          two_sum_add(lj_h, lj_l,
+                      ecn * d3 * ((s33 - 1.0f) + fmaf(s33, k6, -k3)));
+          if (coul && cin_n && cin_o) {
+            if (ff.ewald && r2o >= ff.far_r2_f && r2n >= ff.far_r2_f) {
+              float X = fp32_bracket(r2o, r2n, dr2, alpha, ff.coul_da_f);
+              two_sum_add(re_h, re_l, fmaf(qq, X, qc * X));
+            } else {
+              // the erfc form on the exact distances (float-float r,
+              // alpha r and their differences)
+              ClosePair cp = close_pair(o3, n3, ff.turn2_hi, ff.turn2_lo);
+              float X = ff.ewald
+                            ? far_coulomb(cp, {ff.alpha_f, ff.alpha_lo_f})
+                            : close_coulomb(cp, false, 0.0f, {0.0f, 0.0f}).hi;
+              two_sum_add(re_h, re_l, fmaf(qq, X, qres * X));
+            }
+          } else if (coul) {
+            if (cin_n) {
               float rr = sqrtf(r2n);
               float X = ff.ewald ? erfc_f32(alpha * rr) / rr : 1.0f / rr;
               two_sum_add(re_h, re_l, fmaf(qq, X, qc * X));
             }
+            if (cin_o) {
+              float rr = sqrtf(r2o);
+              float X = ff.ewald ? erfc_f32(alpha * rr) / rr : 1.0f / rr;
+              two_sum_add(re_h, re_l, -fmaf(qq, X, qc * X));
+            }
           }
         } else {
-          if (!in_o || in_n)
-            continue;  // counted from the new position's cells
-          float rr2 = sg2 / r2o, r6 = rr2 * rr2 * rr2, r12 = r6 * r6;
+          float rr2 = sg2 / r2n, r6 = rr2 * rr2 * rr2, r12 = r6 * r6;
           two_sum_add(lj_h, lj_l,
-                      -ecn * ((r12 - r6) + fmaf(r12, k6, -r6 * k3)));
-          if (coul && cin_o) {
-            float rr = sqrtf(r2o);
+                      ecn * ((r12 - r6) + fmaf(r12, k6, -r6 * k3)));
+          if (coul && cin_n) {
+            float rr = sqrtf(r2n);
             float X = ff.ewald ? erfc_f32(alpha * rr) / rr : 1.0f / rr;
-            two_sum_add(re_h, re_l, -fmaf(qq, X, qc * X));
+            two_sum_add(re_h, re_l, fmaf(qq, X, qc * X));
           }
         }
+      } else {
+        if (!in_o || in_n)
+          return;  // counted from the new position's cells
+        float rr2 = sg2 / r2o, r6 = rr2 * rr2 * rr2, r12 = r6 * r6;
+        two_sum_add(lj_h, lj_l,
+                    -ecn * ((r12 - r6) + fmaf(r12, k6, -r6 * k3)));
+        if (coul && cin_o) {
+          float rr = sqrtf(r2o);
+          float X = ff.ewald ? erfc_f32(alpha * rr) / rr : 1.0f / rr;
+          two_sum_add(re_h, re_l, -fmaf(qq, X, qc * X));
+        }
       }
+    };
+    // This CTA takes units rank*2 + half, stepping 2 csize; a thread takes
+    // slot lane128 of its unit (and lane128 + 128, ... in fuller cells).
+    // The next unit's slot data are loaded while this one is evaluated.
+    const int ustep = 2 * csize;
+    int pu = -1, pmj = 0;
+    size_t ps = 0;
+    uint4 pfix = make_uint4(0, 0, 0, 0);
+    auto fetch = [&](int ub) {
+      int u = ub + half;
+      pu = -1;
+      if (u < units && lane128 < mu_n2[u]) {
+        ps = (size_t)mu_c2[u] * b.cap + lane128;
+        pmj = __ldcg(b.cell_meta + ps);
+        pfix = __ldcg(b.cell_fix + ps);
+        pu = u;
+      }
+    };
+    fetch(rank * 2);
+    for (int ub = rank * 2; ub < units; ub += ustep) {
+      const int u = pu, mj = pmj;
+      const size_t s = ps;
+      const uint4 f = pfix;
+      if (ub + ustep < units)
+        fetch(ub + ustep);
+      if (u >= 0)
+        pair(u, s, mj, f);
+      const int uu = ub + half;
+      if (uu < units)
+        for (int j = lane128 + 128; j < mu_n2[uu]; j += 128) {
+          size_t s2 = (size_t)mu_c2[uu] * b.cap + j;
+          pair(uu, s2, __ldcg(b.cell_meta + s2), __ldcg(b.cell_fix + s2));
+        }
     }
     // ---------------- reciprocal space ----------------
     float de_h = 0.f, de_l = 0.f;
@@ -539,7 +583,14 @@ __global__ void __launch_bounds__(MT_THREADS)
         acc = c == 3 ? fmax(acc, S.wred[i][3]) : acc + S.wred[i][c];
       S.part[c] = acc;
     }
-    cluster.sync();
+    // split cluster barrier: arrive with this CTA's partial, build the next
+    // header meanwhile, wait before reading the other CTAs' partials
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    if (spec) {
+      mixed_header(C, S, t + 1, false, -1, 0, h, S.hh[(t + 1) & 1]);
+      mixed_tables(C, S.hh[(t + 1) & 1], tabs + ((t + 1) & 1) * tab_len);
+    }
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
     // ---------------- decision (identical in every CTA) ----------------
     if (threadIdx.x < 32) {
       double p[4] = {0, 0, 0, 0};
@@ -617,9 +668,12 @@ __global__ void __launch_bounds__(MT_THREADS)
         make_props(t + 1);
         cluster.sync();
       }
-      __syncthreads();
-      mixed_header(C, S, t + 1, acc, prev_m, prev_kind);
-      mixed_tables(C, S, tab);
+      if (!spec) {
+        __syncthreads();
+        mixed_header(C, S, t + 1, acc, prev_m, prev_kind, h,
+                     S.hh[(t + 1) & 1]);
+        mixed_tables(C, S.hh[(t + 1) & 1], tabs + ((t + 1) & 1) * tab_len);
+      }
     }
     cluster.sync();  // the cell grid committed by rank 0 is visible
   }
@@ -638,7 +692,7 @@ __global__ void __launch_bounds__(MT_THREADS)
 size_t mixed_smem(int K, int kmax, int csize, bool cold_smem) {
   int kc_max = (K + csize - 1) / csize;
   MixedLayout L = mixed_layout(kc_max, cold_smem);
-  return L.tab + sizeof(float2) * (size_t)3 * MAXA * (kmax + 1) + 16;
+  return L.tab + 2 * sizeof(float2) * (size_t)3 * MAXA * (kmax + 1) + 16;
 }
 
 size_t mixed_cold_buffer(int K, int csize) {
