@@ -503,6 +503,26 @@ int Box::Init(const HostSystem &s0, const BoxConfig &c) {
         i = j;
       }
     }
+    // longest runs first: neighbouring threads then take runs of equal
+    // length, and a warp skips the members none of its runs has (each
+    // run's sums do not depend on which thread takes it)
+    {
+      std::vector<int> order(runs.size());
+      for (size_t r = 0; r < runs.size(); ++r)
+        order[r] = (int)r;
+      std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return runs[x].w > runs[y].w;
+      });
+      std::vector<int4> r2(runs.size());
+      std::vector<int> k2(run_k.size());
+      for (size_t r = 0; r < runs.size(); ++r) {
+        r2[r] = runs[order[r]];
+        for (int g = 0; g < KRUN; ++g)
+          k2[r * KRUN + g] = run_k[(size_t)order[r] * KRUN + g];
+      }
+      runs.swap(r2);
+      run_k.swap(k2);
+    }
     d.nrun = (int)runs.size();
     if ((rc = Alloc(&d.kx, K)) || (rc = Alloc(&d.ky, K)) ||
         (rc = Alloc(&d.kz, K)) || (rc = Alloc(&d.prefact, K)) ||

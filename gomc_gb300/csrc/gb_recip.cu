@@ -69,6 +69,8 @@ __global__ void __launch_bounds__(KT) k_recip_sums(DevBox b, const double *__res
   int a_begin = (int)((long long)b.n_atoms * ch / nch);
   int a_end = (int)((long long)b.n_atoms * (ch + 1) / nch);
   int4 rn = run < b.nrun ? b.krun[run] : make_int4(0, 0, 0, 0);
+  // members of this warp's longest run (runs are sorted longest first)
+  const int wlen = __reduce_max_sync(0xffffffffu, rn.w);
   double sR[KRUN], sI[KRUN];
 #pragma unroll
   for (int g = 0; g < KRUN; ++g) {
@@ -105,9 +107,11 @@ __global__ void __launch_bounds__(KT) k_recip_sums(DevBox b, const double *__res
       double2 e = cmul(ex[rn.z], cmul(pick(ey, rn.x), pick(ez, rn.y)));
 #pragma unroll
       for (int g = 0; g < KRUN; ++g) {
-        sR[g] += q * e.x;
-        sI[g] += q * e.y;
-        e = cmul(e, step);
+        if (g < wlen) {
+          sR[g] += q * e.x;
+          sI[g] += q * e.y;
+          e = cmul(e, step);
+        }
       }
     }
   }
@@ -165,6 +169,8 @@ __global__ void __launch_bounds__(KT) k_recip_sums_ff(DevBox b,
   const int a_begin = (int)((long long)b.n_atoms * ch / nch);
   const int a_end = (int)((long long)b.n_atoms * (ch + 1) / nch);
   const int4 rn = run < b.nrun ? b.krun[run] : make_int4(0, 0, 0, 0);
+  // members of this warp's longest run (runs are sorted longest first)
+  const int wlen = __reduce_max_sync(0xffffffffu, rn.w);
   float rh[KRUN], rl[KRUN], ih[KRUN], il[KRUN];
 #pragma unroll
   for (int g = 0; g < KRUN; ++g) {
@@ -218,10 +224,28 @@ __global__ void __launch_bounds__(KT) k_recip_sums_ff(DevBox b,
                            ffc_conj_if(ez[abs(rn.y)], rn.y < 0));
 #pragma unroll
       for (int g = 0; g < KRUN; ++g) {
-        float4 v = ffc_mul(ex[min(rn.z + g, b.kmax)], eyz);
-        ff_acc(rh[g], rl[g], v.x, v.y);
-        ff_acc(ih[g], il[g], v.z, v.w);
+        if (g < wlen) {
+          // (hi, lo) += v without renormalising: the error-free sum's
+          // remainder and v's low part collect in lo, which the end of
+          // the tile folds back (lo stays within a few ulp of hi)
+          float4 v = ffc_mul(ex[min(rn.z + g, b.kmax)], eyz);
+          ff2 sr = ff_two_sum(rh[g], v.x);
+          ff2 si = ff_two_sum(ih[g], v.z);
+          rh[g] = sr.hi;
+          rl[g] += sr.lo + v.y;
+          ih[g] = si.hi;
+          il[g] += si.lo + v.w;
+        }
       }
+    }
+#pragma unroll
+    for (int g = 0; g < KRUN; ++g) {
+      ff2 r = ff_quick(rh[g], rl[g]);
+      ff2 i = ff_quick(ih[g], il[g]);
+      rh[g] = r.hi;
+      rl[g] = r.lo;
+      ih[g] = i.hi;
+      il[g] = i.lo;
     }
   }
   if (run < b.nrun) {
@@ -265,14 +289,21 @@ int launch_recip_sums_ff(Box &bx, const double *x, const double *y,
                          const double *z, double *sumR, double *sumI) {
   DevBox &b = bx.dev;
   int kb = (b.nrun + KT - 1) / KT;
-  int want = (4 * bx.sm_count + kb - 1) / kb;
-  int nch = std::max(1, std::min(NCH_MAX, want));
+  size_t sh = (size_t)TAF * 3 * (b.kmax + 1) * sizeof(float4);
+  raise_smem_limit((const void *)k_recip_sums_ff, sh);
+  // atom chunks: as many CTAs as the GPU holds at once (whole waves, no
+  // tail), each chunk at least one atom tile
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_recip_sums_ff,
+                                                    KT, sh) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  int nch = std::max(1, bx.sm_count * per_sm / kb);
+  nch = std::min(nch, NCH_MAX);
   nch = std::min(nch, std::max(1, b.n_atoms / TAF));
   int rc = bx.EnsureScratch((size_t)nch * b.K * 2);
   if (rc)
     return rc;
-  size_t sh = (size_t)TAF * 3 * (b.kmax + 1) * sizeof(float4);
-  raise_smem_limit((const void *)k_recip_sums_ff, sh);
   k_recip_sums_ff<<<dim3(kb, nch), KT, sh, bx.stream>>>(b, x, y, z, nch,
                                                         bx.d_scratch);
   k_recip_chunk_sum<<<(b.K + 255) / 256, 256, 0, bx.stream>>>(
