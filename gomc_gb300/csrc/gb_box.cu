@@ -19,9 +19,13 @@ void raise_smem_limit(const void *func, size_t bytes) {
   std::lock_guard<std::mutex> g(mu);
   size_t &cur = limit[{dev, func}];
   if (bytes > cur) {
-    cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)bytes);
-    cur = bytes;
+    // a refused size must not surface later as another call's error; the
+    // launch that needs it reports the problem
+    if (cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bytes) == cudaSuccess)
+      cur = bytes;
+    else
+      cudaGetLastError();
   }
 }
 

@@ -149,7 +149,7 @@ int mc_run_batch(const std::vector<Box *> &boxes, int64_t first_step,
                  int64_t nsteps);
 
 // Largest dynamic shared memory the mixed chain kernel asks for per CTA.
-constexpr size_t MIXED_SMEM_MAX = 220 * 1024;
+constexpr size_t MIXED_SMEM_MAX = 214 * 1024;  // plus ~11 KB static: under 227 KB
 // Batched segments of mixed boxes (gb_mc.cu): mixed_launch uploads the next
 // n[i] moves of box i and launches one kernel per cluster size on the stream
 // of that group's first box (`leaders`); mixed_complete waits for them and

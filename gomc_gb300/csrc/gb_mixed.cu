@@ -711,6 +711,9 @@ static void mixed_attrs() {
     cudaFuncSetAttribute(k_chain_mixed,
                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)MIXED_SMEM_MAX);
+    // a refused attribute must not surface later as another call's error;
+    // the launch itself then reports the problem
+    cudaGetLastError();
   });
 }
 
