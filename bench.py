@@ -197,6 +197,16 @@ def cpu_baseline(seconds: float, threads: int):
                       "(%.1f s)" % (n, dt)}
 
 
+def max_over_ranks(value, dist, torch, device):
+    """The largest of every rank's value (the slowest rank's time); the value
+    itself in a single-process run."""
+    if not dist:
+        return value
+    tt = torch.tensor([value], device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -376,10 +386,7 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
         t_batch = timed(batch, st_batch)
     barrier()
     t_tot = float(sum(t_batch))
-    if dist:
-        tt = torch.tensor([t_tot], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_tot = float(tt.item())
+    t_tot = max_over_ranks(t_tot, dist, torch, dev)
     batched = world * args.steps * M * B / t_tot
     timing = boxes[0].mc_timing(reset=True)
 
@@ -401,10 +408,7 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
             e2e_t.append(time.perf_counter() - t0)
     barrier()
     t_e2e = float(sum(e2e_t))
-    if dist:
-        tt = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt.item())
+    t_e2e = max_over_ranks(t_e2e, dist, torch, dev)
     per_box = (sysm.n_atoms + sysm.n_mol) * 3 * 8
     drift = {"max": {}, "latest_window_max": {}, "recomputes": 0}
     for b in boxes:
@@ -569,10 +573,7 @@ def run_gb300(args, rank, world):
     barrier()
     timing = box.mc_timing(reset=True)
     t_total = float(sum(times))
-    if dist:
-        tt = torch.tensor([t_total], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_total = float(tt.item())
+    t_total = max_over_ranks(t_total, dist, torch, dev)
     value = world * args.steps * M / t_total
 
     # end to end through the public API with host buffers
@@ -592,10 +593,7 @@ def run_gb300(args, rank, world):
         step += M
     barrier()
     t_e2e = float(sum(e2e_times))
-    if dist:
-        tt = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt.item())
+    t_e2e = max_over_ranks(t_e2e, dist, torch, dev)
     e2e_value = world * args.steps * M / t_e2e
     h2d = (sysm.n_atoms + sysm.n_mol) * 3 * 8 + M * 64
     d2h = 5 * 8 + (sysm.n_atoms + sysm.n_mol) * 3 * 8
