@@ -390,6 +390,7 @@ struct ChainArgs {
                   // context of move t written (t)
   double *ctx;    // [2][ctx_len], by move parity: HDR + tables
   size_t ctx_len;
+  int nrows_max;  // phase rows of the largest molecule (6 x its atoms)
   int *tr_i;      // [n][3] or null
   double *tr_d;   // [n][3] or null
 };
@@ -760,9 +761,12 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
 
   for (int t = 0; t < A.n; ++t) {
     // ---------------- phase A ----------------
+    // the header and the rows of the largest molecule in one round trip
     const double *ctx_t = A.ctx + (size_t)(t & 1) * A.ctx_len;
     for (int i = threadIdx.x; i < HDR; i += CT)
       S.hdr[i] = __ldcg(ctx_t + i);
+    for (int i = threadIdx.x; i < A.nrows_max * stride; i += CT)
+      tab[i] = __ldcg((const double2 *)(ctx_t + HDR) + i);
     __syncthreads();
     int m = (int)S.hdr[0];
     int na = (int)S.hdr[2];
@@ -780,10 +784,6 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     const bool wload = spec && warp == 7;
     if (wload)
       ctx_pre1(A, t + 1, pre);
-    int nrows = b.K > 0 ? 2 * na * 3 : 0;
-    for (int i = threadIdx.x; i < nrows * stride; i += CT)
-      tab[i] = __ldcg((const double2 *)(ctx_t + HDR) + i);
-    __syncthreads();
     double lj = 0.0, re = 0.0, ovl = 0.0, er = 0.0;
     // Real space: the candidates of all (atom, old/new, neighbour cell)
     // units, numbered through a prefix sum of the units' slot counts and
@@ -1565,14 +1565,17 @@ int mc_init(Box &b, const gb_mc_params &p) {
     return b.Fail(ERR_ARG, "move frequencies must be non-negative, not all 0");
   const HostSystem &h = b.host;
   std::vector<int> len(h.n_mol);
+  int na_max = 1;
   for (int m = 0; m < h.n_mol; ++m) {
     len[m] = h.mstart[m + 1] - h.mstart[m];
+    na_max = std::max(na_max, len[m]);
     if (len[m] > MAX_MOL_ATOMS)
       return b.Fail(ERR_UNSUPPORTED, "molecules above 8 atoms in the move loop");
   }
   b.mc = new McState();
   McState &s = *b.mc;
   s.params = p;
+  s.na_max = na_max;
   s.stream = new MoveStream(p.seed, p.frac, h.n_mol, len);
   s.next_step = 0;
   int rc;
@@ -1786,6 +1789,7 @@ static int run_chain(Box &b, McState &s, const MoveRec *moves, int64_t first,
   A.seq = s.d_seq;
   A.ctx = s.d_ctx;
   A.ctx_len = chain_ctx_len(b.dev.kmax + 1);
+  A.nrows_max = b.dev.K > 0 ? 6 * s.na_max : 0;
   A.tr_i = tr_i;
   A.tr_d = tr_d;
   void *args[] = {&A};

@@ -96,6 +96,7 @@ struct McState {
   size_t trace_cap = 0;
   double *d_part = nullptr;  // per-CTA partials
   unsigned *d_seq = nullptr; // FP64 chain decision and per-CTA flags
+  int na_max = 1;            // atoms of the largest molecule
   unsigned *d_bar = nullptr; // grid barrier words
   double *d_ctx = nullptr;   // per-move context (positions, tables)
   int grid = 0, kchunk = 0;
