@@ -353,13 +353,15 @@ __device__ __forceinline__ double2 tab_at(const double2 *row, int n) {
 constexpr int CT = 256;
 constexpr int HDR = 112;  // doubles in the move-context header
 constexpr int ICL_MAX = 256;  // in-cutoff pairs a CTA lists per move
-constexpr int SEQ_PART = 32;      // words; the decision word has its own line
+// Words of the chain's flag array: [0] the decision word, alone on its
+// 128-byte line; from SEQ_CTX, one word per CTA: its part of a move's
+// context written (grid <= PART_MAX_GRID).
+constexpr int SEQ_CTX = 32;
 // A CTA's partial slots hold this NaN pattern until written: the leader
 // polls the values themselves (each 8-byte store is single-copy atomic), so
 // no separate arrival flag, fence or atomic is needed
 constexpr unsigned long long PART_EMPTY = 0x7FF4C0DE7FF4C0DEULL;
 constexpr int PART_MAX_GRID = 256;  // partial slots the leader holds per lane: 8
-constexpr int SEQ_STRIDE = 1024;  // words per per-CTA flag array (grid <= 1024)
 constexpr int NPAIR_CAP = 64; // (n_x, n_y) columns a CTA's k-chunk may span
                               // for the shared x-y phase products
 
@@ -385,9 +387,8 @@ struct ChainArgs {
   double *part;   // [2][grid][4], by move parity
   unsigned *bar;  // [0..1] grid barrier
   unsigned *seq;  // [0] decision published (2 (t + 1) + accept); from
-                  // SEQ_PART: per CTA, partials of move t written (t + 1);
-                  // from SEQ_PART + SEQ_STRIDE: per CTA, its part of the
-                  // context of move t written (t)
+                  // SEQ_CTX: per CTA, its part of the context of move t
+                  // written (t)
   double *ctx;    // [2][ctx_len], by move parity: HDR + tables
   size_t ctx_len;
   int nrows_max;  // phase rows of the largest molecule (6 x its atoms)
@@ -519,7 +520,7 @@ __device__ void build_ctx_rest(const ChainArgs &A, ChainShared &S, int t,
     group_sync(count);
     if (tid == 0) {
       __threadfence();
-      st_release(A.seq + SEQ_PART + SEQ_STRIDE + blockIdx.x, (unsigned)t);
+      st_release(A.seq + SEQ_CTX + blockIdx.x, (unsigned)t);
     }
   }
 }
@@ -1085,7 +1086,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
       if (warp == 1 && ok) {
         // the writers' flags of the next context, checked while warp 0
         // decides and commits
-        int bok = spec ? warp_wait_all(A.seq + SEQ_PART + SEQ_STRIDE,
+        int bok = spec ? warp_wait_all(A.seq + SEQ_CTX,
                                        (int)ctx_builders(A, t + 1),
                                        (unsigned)(t + 1), b.err)
                        : 1;
@@ -1622,7 +1623,7 @@ int mc_init(Box &b, const gb_mc_params &p) {
       (rc = mc_alloc(b, s, &s.d_prop, s.move_cap * 12)) ||
       (rc = mc_alloc(b, s, &s.d_part, 2 * (size_t)s.grid * 4)) ||
       (rc = mc_alloc(b, s, &s.d_bar, 8)) ||
-      (rc = mc_alloc(b, s, &s.d_seq, SEQ_PART + 2 * SEQ_STRIDE)) ||
+      (rc = mc_alloc(b, s, &s.d_seq, SEQ_CTX + PART_MAX_GRID)) ||
       (rc = mc_alloc(b, s, &s.d_ctx, 2 * chain_ctx_len(stride))) ||
       (rc = mc_alloc(b, s, &s.d_mp, 16)))
     return rc;
@@ -1796,7 +1797,7 @@ static int run_chain(Box &b, McState &s, const MoveRec *moves, int64_t first,
   size_t sm = chain_smem(b, s.grid);
   // the per-launch counters of the decision protocol start from zero
   int rc = b.CudaCheck(cudaMemsetAsync(s.d_seq, 0,
-                                       (SEQ_PART + 2 * SEQ_STRIDE) *
+                                       (SEQ_CTX + PART_MAX_GRID) *
                                            sizeof(unsigned),
                                        b.stream),
                        "memset");
