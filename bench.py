@@ -522,6 +522,10 @@ def run_serving(args, dev):
                              "p99": st["sweep_p99_ms"]},
         "job_latency_s": {"p50": st["job_p50_s"], "p99": st["job_p99_s"]},
         "rounds": st["rounds"], "mean_resident_jobs": st["mean_resident"],
+        "occupancy": {k: st[k] for k in ("mean_admitted", "mean_in_round",
+                                         "cta_slot_frac", "smem_frac",
+                                         "mean_queued", "stops_mem",
+                                         "stops_smem", "stops_ctas")},
         "helper_busy_s": st["helper_busy_s"], "round_busy_s": st["round_busy_s"],
         "jobs_done": st["jobs_done"]}
 

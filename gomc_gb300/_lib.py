@@ -131,6 +131,7 @@ SIGNATURES = {
     "gb_server_job": (C.c_int, [_P, C.c_int64, _I, _L, _D]),
     "gb_server_result": (C.c_int, [_P, C.c_int64, _D, _D, _D]),
     "gb_server_stats": (C.c_int, [_P, _D]),
+    "gb_server_occupancy": (C.c_int, [_P, _D]),
     "gb_server_error": (C.c_char_p, [_P]),
 }
 

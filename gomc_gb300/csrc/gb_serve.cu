@@ -91,6 +91,13 @@ struct Server {
   // statistics
   std::vector<double> sweep_lat;  // seconds
   int64_t moves = 0, rounds = 0, resident_sum = 0;
+  // occupancy sums over rounds, taken after each round's admission: jobs
+  // admitted, CTA-slot and shared-memory fractions in use, jobs queued
+  double occ_admitted = 0, occ_ctas = 0, occ_smem = 0, occ_queued = 0;
+  int64_t occ_rounds = 0;
+  // admissions stopped at the queue's head by device memory, by shared
+  // memory, by CTA count
+  int64_t stop_mem = 0, stop_smem = 0, stop_ctas = 0;
   double t_first = -1, t_last_done = 0;
   double helper_s = 0, round_s = 0;  // time in set-up / recompute, in rounds
 
@@ -104,6 +111,7 @@ struct Server {
   }
   int Round(int32_t *pending, bool *worked);
   int Admit();
+  void SlotUse(size_t *smem, int *ctas) const;
   void RunTask(Job *j);
   void RunTasksInline();
   void Retire(Job *j);
@@ -246,6 +254,17 @@ size_t job_estimate(const Job &j, int quantum, int *csize_out) {
 
 }  // namespace
 
+// Shared memory (with the runtime's 1 KB per CTA) and CTAs held by the
+// resident jobs' chains; the caller holds `mu`.
+void Server::SlotUse(size_t *smem, int *ctas) const {
+  *smem = 0;
+  *ctas = 0;
+  for (const Job *r : resident) {
+    *smem += (size_t)r->csize * (r->smem + 1024);
+    *ctas += r->csize;
+  }
+}
+
 // Admission (first come first served): reserve the job's estimated device
 // memory and CTA slots, mark it resident and busy, and queue its set-up for
 // the helpers.  Returns how many jobs were admitted.
@@ -270,14 +289,12 @@ int Server::Admit() {
     // CTA slots: shared memory and two CTAs per SM by registers
     size_t used_smem = 0;
     int used_ctas = 0;
-    for (Job *r : resident) {
-      used_smem += (size_t)r->csize * (r->smem + 1024);
-      used_ctas += r->csize;
-    }
+    SlotUse(&used_smem, &used_ctas);
     bool fits_mem = mem_used + est <= budget;
-    bool fits_slots =
-        used_smem + (size_t)csize * (smem + 1024) <= slots.smem_per_sm * slots.sms &&
-        used_ctas + csize <= 2 * slots.sms;
+    bool fits_smem = used_smem + (size_t)csize * (smem + 1024) <=
+                     slots.smem_per_sm * slots.sms;
+    bool fits_ctas = used_ctas + csize <= 2 * slots.sms;
+    bool fits_slots = fits_smem && fits_ctas;
     bool fits_count =
         cfg.max_resident <= 0 || (int)resident.size() < cfg.max_resident;
     if (!(fits_mem && fits_slots && fits_count)) {
@@ -288,6 +305,9 @@ int Server::Admit() {
         j->msg = "job needs more device memory than the server's budget";
         continue;
       }
+      stop_mem += fits_mem ? 0 : 1;
+      stop_smem += fits_smem ? 0 : 1;
+      stop_ctas += fits_ctas ? 0 : 1;
       break;
     }
     queue.pop_front();
@@ -434,6 +454,17 @@ int Server::Round(int32_t *pending, bool *worked) {
     return Fail(rc, "launch: " + boxes[0]->last_error);
   // 2. admission while they run
   int admitted = Admit();
+  {
+    std::lock_guard<std::mutex> g(mu);
+    size_t used_smem;
+    int used_ctas;
+    SlotUse(&used_smem, &used_ctas);
+    occ_admitted += (double)resident.size();
+    occ_ctas += (double)used_ctas / (double)(2 * slots.sms);
+    occ_smem += (double)used_smem / (double)(slots.smem_per_sm * slots.sms);
+    occ_queued += (double)queue.size();
+    occ_rounds++;
+  }
   if (inline_tasks)
     RunTasksInline();
   // 3. completion; due recomputes go to the helpers
@@ -794,6 +825,24 @@ int gb_server_stats(gb_server *srv, double *out12) {
   out10[9] = s.rounds ? (double)s.resident_sum / (double)s.rounds : 0.0;
   out12[10] = s.helper_s;
   out12[11] = s.round_s;
+  return gb::OK;
+}
+
+int gb_server_occupancy(gb_server *srv, double *out8) {
+  if (!srv || !out8)
+    return gb::ERR_ARG;
+  gb::Server &s = srv->s;
+  std::lock_guard<std::mutex> g(s.mu);
+  double n = s.occ_rounds ? (double)s.occ_rounds : 1.0;
+  double *out5 = out8;
+  out5[0] = s.occ_admitted / n;
+  out5[1] = s.rounds ? (double)s.resident_sum / (double)s.rounds : 0.0;
+  out5[2] = s.occ_ctas / n;
+  out5[3] = s.occ_smem / n;
+  out5[4] = s.occ_queued / n;
+  out8[5] = (double)s.stop_mem;
+  out8[6] = (double)s.stop_smem;
+  out8[7] = (double)s.stop_ctas;
   return gb::OK;
 }
 

@@ -22,6 +22,9 @@ STATUS_NAMES = {QUEUED: "queued", RUNNING: "running", DONE: "done",
 STATS_KEYS = ["jobs_done", "moves", "wall_s", "moves_per_s",
               "sweep_p50_ms", "sweep_p99_ms", "job_p50_s", "job_p99_s",
               "rounds", "mean_resident", "helper_busy_s", "round_busy_s"]
+OCCUPANCY_KEYS = ["mean_admitted", "mean_in_round", "cta_slot_frac",
+                  "smem_frac", "mean_queued", "stops_mem", "stops_smem",
+                  "stops_ctas"]
 
 
 class Server:
@@ -133,4 +136,9 @@ class Server:
         o = np.zeros(12)
         self._chk(lib().gb_server_stats(self.h,
                                         o.ctypes.data_as(C.POINTER(C.c_double))))
-        return dict(zip(STATS_KEYS, o.tolist()))
+        d = dict(zip(STATS_KEYS, o.tolist()))
+        occ = np.zeros(8)
+        self._chk(lib().gb_server_occupancy(
+            self.h, occ.ctypes.data_as(C.POINTER(C.c_double))))
+        d.update(zip(OCCUPANCY_KEYS, occ.tolist()))
+        return d

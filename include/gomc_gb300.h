@@ -312,6 +312,13 @@ int gb_server_result(gb_server *srv, int64_t job, double *xyz, double *com,
  * threads) spent on set-ups and FP64 recomputes, seconds spent in rounds
  * (launch to completion). */
 int gb_server_stats(gb_server *srv, double *out12);
+/* out8: means over the rounds so far, taken after each round's admission,
+ * of the jobs admitted (set up, running or recomputing), the jobs in the
+ * round's launches, the fraction of the GPU's chain CTA slots held (two per
+ * SM), the fraction of the GPU's shared memory held and the jobs still
+ * queued; then how many admission passes stopped at the queue's head for
+ * want of device memory, of shared memory, of CTA slots. */
+int gb_server_occupancy(gb_server *srv, double *out8);
 const char *gb_server_error(const gb_server *srv);
 
 /* ---- Reciprocal energy without device allocation ----
