@@ -525,7 +525,8 @@ def run_serving(args, dev):
         "occupancy": {k: st[k] for k in ("mean_admitted", "mean_in_round",
                                          "cta_slot_frac", "smem_frac",
                                          "mean_queued", "stops_mem",
-                                         "stops_smem", "stops_ctas")},
+                                         "stops_smem", "stops_ctas",
+                                         "launch_balance", "round_gap_s")},
         "helper_busy_s": st["helper_busy_s"], "round_busy_s": st["round_busy_s"],
         "jobs_done": st["jobs_done"]}
 

@@ -98,6 +98,10 @@ struct Server {
   // admissions stopped at the queue's head by device memory, by shared
   // memory, by CTA count
   int64_t stop_mem = 0, stop_smem = 0, stop_ctas = 0;
+  // launch balance: per round, the chain CTAs' kernel time over the time
+  // they were held (the longest launch of the round), CTA-weighted; and the
+  // round's wall time outside its longest launch (host work, launch gaps)
+  double bal_sum = 0, gap_s = 0;
   double t_first = -1, t_last_done = 0;
   double helper_s = 0, round_s = 0;  // time in set-up / recompute, in rounds
 
@@ -132,13 +136,17 @@ int job_cluster(const Job &j, int K) {
   return 16;
 }
 
-// Moves per round of a job: `quantum` scaled by 4,096 over the k-vectors
-// each of its CTAs evaluates per move (the bulk of a move's time), within
-// [quantum / 4, 8 quantum], so small and large jobs spend about the same time
-// per round.  Depends on the job alone.
+// Moves per round of a job: `quantum` scaled by the time of a move of a
+// chain with 4,096 k-vectors per CTA over the time of one of this job's, so
+// that every resident job's segment takes about the same time and no chain
+// idles while the round waits for the slowest.  A move costs a fixed part
+// (the cluster barriers, the header, the real-space pairs: about as long as
+// 2,560 k-vectors of one CTA's reciprocal work on GB300) plus its k-vectors
+// per CTA.  Within [quantum / 4, 8 quantum]; depends on the job alone.
 int64_t job_quantum(int quantum, int K, int csize) {
+  constexpr int64_t FIXED = 2560, REF = 4096;
   int64_t per_cta = std::max(K / std::max(csize, 1), 256);
-  int64_t q = (int64_t)quantum * 4096 / per_cta;
+  int64_t q = (int64_t)quantum * (FIXED + REF) / (FIXED + per_cta);
   return std::min<int64_t>(std::max<int64_t>(q, std::max(quantum / 4, 1)),
                            8 * (int64_t)quantum);
 }
@@ -473,7 +481,25 @@ int Server::Round(int32_t *pending, bool *worked) {
     if ((rc = mixed_complete(boxes, n, leaders, &due)))
       return Fail(rc, "round: " + boxes[0]->last_error);
     double t_end = Now();
+    // each leader's launch time this round (and its events released)
+    double ms_max = 0, cta_ms = 0;
+    int64_t ctas = 0;
+    for (Box *L : leaders) {
+      double ms = 0;
+      if ((rc = mc_timing(*L, 1, &ms, nullptr, nullptr, nullptr, nullptr)))
+        return Fail(rc, "round: " + L->last_error);
+      int c = L->mc->cluster, nb = 0;
+      for (Box *b : boxes)
+        nb += b->mc->cluster == c ? 1 : 0;
+      ms_max = std::max(ms_max, ms);
+      cta_ms += ms * c * nb;
+      ctas += (int64_t)c * nb;
+    }
     std::lock_guard<std::mutex> g(mu);
+    if (ms_max > 0 && ctas > 0) {
+      bal_sum += cta_ms / (ms_max * (double)ctas);
+      gap_s += std::max(0.0, t_end - t_start - 1e-3 * ms_max);
+    }
     round_s += t_end - t_start;
     rounds++;
     resident_sum += (int64_t)live.size();
@@ -828,13 +854,13 @@ int gb_server_stats(gb_server *srv, double *out12) {
   return gb::OK;
 }
 
-int gb_server_occupancy(gb_server *srv, double *out8) {
-  if (!srv || !out8)
+int gb_server_occupancy(gb_server *srv, double *out10) {
+  if (!srv || !out10)
     return gb::ERR_ARG;
   gb::Server &s = srv->s;
   std::lock_guard<std::mutex> g(s.mu);
   double n = s.occ_rounds ? (double)s.occ_rounds : 1.0;
-  double *out5 = out8;
+  double *out5 = out10, *out8 = out10;
   out5[0] = s.occ_admitted / n;
   out5[1] = s.rounds ? (double)s.resident_sum / (double)s.rounds : 0.0;
   out5[2] = s.occ_ctas / n;
@@ -843,6 +869,8 @@ int gb_server_occupancy(gb_server *srv, double *out8) {
   out8[5] = (double)s.stop_mem;
   out8[6] = (double)s.stop_smem;
   out8[7] = (double)s.stop_ctas;
+  out10[8] = s.rounds ? s.bal_sum / (double)s.rounds : 0.0;
+  out10[9] = s.gap_s;
   return gb::OK;
 }
 

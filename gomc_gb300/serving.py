@@ -24,7 +24,7 @@ STATS_KEYS = ["jobs_done", "moves", "wall_s", "moves_per_s",
               "rounds", "mean_resident", "helper_busy_s", "round_busy_s"]
 OCCUPANCY_KEYS = ["mean_admitted", "mean_in_round", "cta_slot_frac",
                   "smem_frac", "mean_queued", "stops_mem", "stops_smem",
-                  "stops_ctas"]
+                  "stops_ctas", "launch_balance", "round_gap_s"]
 
 
 class Server:
@@ -137,7 +137,7 @@ class Server:
         self._chk(lib().gb_server_stats(self.h,
                                         o.ctypes.data_as(C.POINTER(C.c_double))))
         d = dict(zip(STATS_KEYS, o.tolist()))
-        occ = np.zeros(8)
+        occ = np.zeros(10)
         self._chk(lib().gb_server_occupancy(
             self.h, occ.ctypes.data_as(C.POINTER(C.c_double))))
         d.update(zip(OCCUPANCY_KEYS, occ.tolist()))

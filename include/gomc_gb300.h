@@ -269,7 +269,8 @@ typedef struct gb_server_config {
   int32_t device;
   int32_t quantum;       /* moves per round of a job with 4,096 k-vectors per
                             CTA (0 = 1000); a job's own quantum scales
-                            inversely with its k-vectors per CTA, within
+                            inversely with its time per move, modelled as
+                            2,560 + its k-vectors per CTA, within
                             [quantum/4, 8 quantum] */
   int64_t mem_budget;    /* device bytes for job state (0 = 90% of free) */
   int32_t max_resident;  /* at most this many resident jobs (0 = no cap) */
@@ -312,13 +313,17 @@ int gb_server_result(gb_server *srv, int64_t job, double *xyz, double *com,
  * threads) spent on set-ups and FP64 recomputes, seconds spent in rounds
  * (launch to completion). */
 int gb_server_stats(gb_server *srv, double *out12);
-/* out8: means over the rounds so far, taken after each round's admission,
+/* out10: means over the rounds so far, taken after each round's admission,
  * of the jobs admitted (set up, running or recomputing), the jobs in the
  * round's launches, the fraction of the GPU's chain CTA slots held (two per
  * SM), the fraction of the GPU's shared memory held and the jobs still
  * queued; then how many admission passes stopped at the queue's head for
- * want of device memory, of shared memory, of CTA slots. */
-int gb_server_occupancy(gb_server *srv, double *out8);
+ * want of device memory, of shared memory, of CTA slots; then the mean
+ * launch balance of a round (its launches' device time weighted by their
+ * CTAs, over its longest launch's time those CTAs were held: 1 = every chain
+ * ran until the round's end) and the seconds of round wall time outside
+ * each round's longest launch. */
+int gb_server_occupancy(gb_server *srv, double *out10);
 const char *gb_server_error(const gb_server *srv);
 
 /* ---- Reciprocal energy without device allocation ----
