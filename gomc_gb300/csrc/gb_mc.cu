@@ -351,7 +351,7 @@ __device__ __forceinline__ double2 tab_at(const double2 *row, int n) {
 // The FP64 chain kernel
 // ===========================================================================
 constexpr int CT = 256;
-constexpr int HDR = 112;  // doubles in the move-context header
+constexpr int HDR = 128;  // doubles in the move-context header
 constexpr int ICL_MAX = 256;  // in-cutoff pairs a CTA lists per move
 // Words of the chain's flag array: [0] the decision word, alone on its
 // 128-byte line; from SEQ_CTX, one word per CTA: its part of a move's
@@ -410,7 +410,7 @@ struct ChainShared {
   double b_oldp[MAX_MOL_ATOMS][3], b_newp[MAX_MOL_ATOMS][3];
   double b_com[3], b_newcom[3], b_prop[12], b_q[MAX_MOL_ATOMS];
   double b_pacc, b_lpacc;
-  int b_m, b_a0, b_na, b_kind, b_writer;
+  int b_m, b_a0, b_na, b_kind, b_writer, b_ka[MAX_MOL_ATOMS];
 };
 
 // Synchronise the threads [first, first + count) of the CTA: the whole CTA
@@ -491,6 +491,8 @@ __device__ void build_ctx_rest(const ChainArgs &A, ChainShared &S, int t,
       if (side == 0) {
         double q = S.b_q[a];
         h[72 + a] = fabs(q) < 0.000000001 ? 0.0 : q;
+        h[108 + a] = q;  // the charge and kind of the real-space terms
+        ((int *)(h + 116))[a] = S.b_ka[a];
       }
     } else if (tid >= 128 && tid < 128 + 6 * na) {
       int i = tid - 128, pa = i / 3, d = i % 3;  // pa = side * na + atom
@@ -560,8 +562,10 @@ __device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
     double *xs[3] = {b.x, b.y, b.z};
     S.b_oldp[a][d] = same ? prev_hdr[48 + 3 * a + d] : __ldcg(xs[d] + a0 + a);
   }
-  for (int a = tid; a < na; a += count)
+  for (int a = tid; a < na; a += count) {
     S.b_q[a] = b.q[a0 + a];
+    S.b_ka[a] = b.kind[a0 + a];
+  }
   group_sync(count);
   build_ctx_rest(A, S, t, tid, count, false);
 }
@@ -572,7 +576,7 @@ __device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
 // (lanes 0..11), the centre (12..14), the old coordinates (lanes < 3 na)
 // and the charges (lanes < na).
 struct CtxPre {
-  int m, a0, na, kind;
+  int m, a0, na, kind, ka;
   double pacc, lpacc;
   double v0, v1, q;
   bool writer;
@@ -591,6 +595,7 @@ __device__ __forceinline__ void ctx_pre2(const ChainArgs &A, int t, CtxPre &c) {
   const int lane = threadIdx.x & 31;
   c.writer = ctx_writer(A, c.na);
   c.v0 = c.v1 = c.q = 0.0;
+  c.ka = 0;
   if (!c.writer)
     return;
   if (lane < 12)
@@ -601,8 +606,10 @@ __device__ __forceinline__ void ctx_pre2(const ChainArgs &A, int t, CtxPre &c) {
     int a = lane / 3, d = lane % 3;
     c.v1 = __ldcg((d == 0 ? b.x : d == 1 ? b.y : b.z) + c.a0 + a);
   }
-  if (lane < c.na)
+  if (lane < c.na) {
     c.q = b.q[c.a0 + lane];
+    c.ka = b.kind[c.a0 + lane];
+  }
 }
 // Stage the gathered inputs in shared memory (by the loading warp).
 __device__ __forceinline__ void ctx_pre_store(ChainShared &S, const CtxPre &c) {
@@ -621,8 +628,10 @@ __device__ __forceinline__ void ctx_pre_store(ChainShared &S, const CtxPre &c) {
     S.b_com[lane - 12] = c.v0;
   if (lane < 3 * c.na)
     S.b_oldp[lane / 3][lane % 3] = c.v1;
-  if (lane < c.na)
+  if (lane < c.na) {
     S.b_q[lane] = c.q;
+    S.b_ka[lane] = c.ka;
+  }
 }
 
 // CTAs that write part of move t's context: CTA 0 (header) and one CTA
@@ -638,29 +647,30 @@ __device__ __forceinline__ unsigned ctx_builders(const ChainArgs &A, int t) {
 // neighbour cell) against cell slot s: the exact minimum-image distance and
 // cutoff test, the overlap flag for new positions, and the LJ and
 // erfc-screened Coulomb terms, old positions subtracted.
+// The neighbour's position and charge (p: x, y, z, q) and meta word come
+// from the caller's loads; the moved atom's from the move header.
 __device__ __forceinline__ void pair_term(const ChainArgs &A,
-                                          const ChainShared &S, int m, int u,
-                                          int s, double &lj, double &re,
+                                          const ChainShared &S, int u,
+                                          double2 pxy, double2 pzq, int mj,
+                                          double &lj, double &re,
                                           double &ovl) {
   const DevBox &b = A.b;
   const FF &ff = *A.ff;
   int a = u / (2 * NB27), side = (u / NB27) % 2;
   const double *pp = S.hdr + (side ? 48 : 24) + 3 * a;
-  const double *pq = (const double *)(b.cell_pos + s);
-  double dx = min_image(pp[0] - __ldcg(pq), b.L[0], b.half[0]);
-  double dy = min_image(pp[1] - __ldcg(pq + 1), b.L[1], b.half[1]);
-  double dz = min_image(pp[2] - __ldcg(pq + 2), b.L[2], b.half[2]);
+  double dx = min_image(pp[0] - pxy.x, b.L[0], b.half[0]);
+  double dy = min_image(pp[1] - pxy.y, b.L[1], b.half[1]);
+  double dz = min_image(pp[2] - pzq.x, b.L[2], b.half[2]);
   double d2 = dsq3(dx, dy, dz);
   if (!(ff.rcutSq > d2))
     return;
   if (side && d2 < ff.rcutLowSq)
     ovl = 1.0;
-  double qa = b.q[b.mstart[m] + a];
-  int ka = b.kind[b.mstart[m] + a];
-  int mj = __ldcg(b.cell_meta + s);
+  double qa = S.hdr[108 + a];
+  int ka = ((const int *)(S.hdr + 116))[a];
   double e = 0.0;
   if (ff.electrostatic) {
-    double qq = qa * __ldcg(pq + 3) * QQ_FACT;
+    double qq = qa * pzq.y * QQ_FACT;
     if (qq != 0.0)
       e = coulomb_energy(ff, d2, qq);
   }
@@ -800,11 +810,14 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
       u_cell[u] = c2;
       u_off[u + 1] = __ldcg(b.cell_count + c2);
     }
-    // x-y column products, one per (column, old/new atom)
+    // x-y column products times the atom's charge, one per (column,
+    // old/new atom)
     for (int e = threadIdx.x; e < npair * 2 * na; e += CT) {
       int p = e / (2 * na), r = e - p * 2 * na;
       const double2 *rx = tab + (size_t)(r * 3) * stride;
-      exy[e] = cmul2(rx[pair_n[p].x], tab_at(rx + stride, pair_n[p].y));
+      double q = S.hdr[72 + (r < na ? r : r - na)];
+      double2 v = cmul2(rx[pair_n[p].x], tab_at(rx + stride, pair_n[p].y));
+      exy[e] = make_double2(q * v.x, q * v.y);
     }
     __syncthreads();
     if (wload)
@@ -836,14 +849,15 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     //     candidates to different CTAs -- and the pairs inside it are
     //     compacted, in candidate order, into a shared list (ballot and a
     //     scan over the warps, so the order and every sum stay fixed).
-    __shared__ int icl_slot[ICL_MAX];
+    __shared__ double2 icl_pos[ICL_MAX][2];  // neighbour x, y | z, q
+    __shared__ int icl_meta[ICL_MAX];
     __shared__ short icl_unit[ICL_MAX];
     __shared__ int icl_warp[CT / 32 + 1];
     int icl_n = 0;
     for (int base = cta; base < total; base += total_threads) {
       int idx = base + threadIdx.x * G;
       bool in = false;
-      int u = 0, s = 0;
+      int u = 0, s = 0, mj = 0;
       if (idx < total) {
         int lo = 0, hi = units - 1;  // last unit whose offset <= idx
         while (lo < hi) {
@@ -856,19 +870,26 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
         u = lo;
         int a = u / (2 * NB27), side = (u / NB27) % 2;
         s = u_cell[u] * b.cap + (idx - u_off[u]);
-        int mj = __ldcg(b.cell_meta + s);
+        mj = __ldcg(b.cell_meta + s);
+        uint4 f = __ldcg(b.cell_fix + s);
         if (meta_mol(mj) != m) {
           // FP32 pre-test on the fixed-point turns (the wrapped integer
           // difference is the minimum image); the exact FP64 test is made
           // where the listed pairs are evaluated
           const uint32_t *pt =
               (const uint32_t *)(S.hdr + 84) + (side * na + a) * 3;
-          uint4 f = __ldcg(b.cell_fix + s);
           float dx = (float)(int)(pt[0] - f.x) * turn_f[0];
           float dy = (float)(int)(pt[1] - f.y) * turn_f[1];
           float dz = (float)(int)(pt[2] - f.z) * turn_f[2];
           in = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < cut_f;
         }
+      }
+      // the listed pairs' neighbour data, loaded while the list is formed
+      double2 pxy = make_double2(0.0, 0.0), pzq = pxy;
+      if (in) {
+        const double2 *pq = (const double2 *)(b.cell_pos + s);
+        pxy = __ldcg(pq);
+        pzq = __ldcg(pq + 1);
       }
       unsigned mask = __ballot_sync(0xffffffffu, in);
       if (lane == 0)
@@ -887,11 +908,13 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
       if (in) {
         int pos = icl_warp[warp] + __popc(mask & ((1u << lane) - 1u));
         if (pos < ICL_MAX) {
-          icl_slot[pos] = s;
+          icl_pos[pos][0] = pxy;
+          icl_pos[pos][1] = pzq;
+          icl_meta[pos] = mj;
           icl_unit[pos] = (short)u;
         } else {
           // past the list (not met at liquid densities): evaluated here
-          pair_term(A, S, m, u, s, lj, re, ovl);
+          pair_term(A, S, u, pxy, pzq, mj, lj, re, ovl);
         }
       }
       icl_n = icl_warp[CT / 32];
@@ -905,13 +928,16 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     const int n_eval = min(icl_n, ICL_MAX);
     if (warp == 3) {
       for (int i = lane; i < n_eval; i += 32)
-        pair_term(A, S, m, icl_unit[i], icl_slot[i], lj, re, ovl);
+        pair_term(A, S, icl_unit[i], icl_pos[i][0], icl_pos[i][1],
+                  icl_meta[i], lj, re, ovl);
     }
     if (warp != 3 && warp != 7) {
       const int kw = warp < 3 ? warp : warp - 1;  // 0..5
       for (int i = kw * 32 + lane; i < kc; i += 6 * 32) {
         char4 n = kn[i];
-        double rN = 0, iN = 0, rO = 0, iO = 0;
+        // sum over the atoms of q (e^{i k.r_new} - e^{i k.r_old}), the
+        // charge already in the x-y product: four FMAs per (atom, side)
+        double dR = 0, dI = 0;
         const double2 *col = npair > 0 ? exy + (size_t)pidx[i] * 2 * na : nullptr;
         for (int a = 0; a < na; ++a) {
           double q = S.hdr[72 + a];
@@ -919,18 +945,29 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
             continue;
           const double2 *ro = tab + (size_t)(a * 3) * stride;
           const double2 *rn = tab + (size_t)((na + a) * 3) * stride;
-          double2 xo = col ? col[a] : cmul2(ro[n.x], tab_at(ro + stride, n.y));
-          double2 xn = col ? col[na + a]
-                           : cmul2(rn[n.x], tab_at(rn + stride, n.y));
-          double2 eo = cmul2(xo, tab_at(ro + 2 * stride, n.z));
-          double2 en = cmul2(xn, tab_at(rn + 2 * stride, n.z));
-          rN += q * en.x;
-          iN += q * en.y;
-          rO += q * eo.x;
-          iO += q * eo.y;
+          double2 xo, xn;
+          if (col) {
+            xo = col[a];
+            xn = col[na + a];
+          } else {
+            double2 vo = cmul2(ro[n.x], tab_at(ro + stride, n.y));
+            double2 vn = cmul2(rn[n.x], tab_at(rn + stride, n.y));
+            xo = make_double2(q * vo.x, q * vo.y);
+            xn = make_double2(q * vn.x, q * vn.y);
+          }
+          double2 zo = tab_at(ro + 2 * stride, n.z);
+          double2 zn = tab_at(rn + 2 * stride, n.z);
+          dR = fma(xn.x, zn.x, dR);
+          dR = fma(-xn.y, zn.y, dR);
+          dR = fma(-xo.x, zo.x, dR);
+          dR = fma(xo.y, zo.y, dR);
+          dI = fma(xn.x, zn.y, dI);
+          dI = fma(xn.y, zn.x, dI);
+          dI = fma(-xo.x, zo.y, dI);
+          dI = fma(-xo.y, zo.x, dI);
         }
-        double srn = sR[i] + 1.0 * (rN - rO);
-        double sin_ = sI[i] + 1.0 * (iN - iO);
+        double srn = sR[i] + dR;
+        double sin_ = sI[i] + dI;
         nR[i] = srn;
         nI[i] = sin_;
         er += (srn * srn + sin_ * sin_) * pf[i];
