@@ -1220,7 +1220,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
       }
     } else {
       if (threadIdx.x == 0) {
-        int ok = wait_geq(A.seq, 2u * (unsigned)(t + 1), b.err, true);
+        int ok = wait_geq(A.seq, 2u * (unsigned)(t + 1), b.err, false);
         S.accept = ok ? (int)(ld_acquire(A.seq) & 1u) : 0;
         S.ok = ok;
       }
