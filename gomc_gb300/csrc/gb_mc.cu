@@ -337,6 +337,21 @@ __device__ __forceinline__ double2 cis_turns64(uint64_t phase) {
   }
 }
 
+// Neighbour nn of a cell (offsets dx, dy, dz in -1..1, dz fastest, each
+// axis wrapped): the entry of the 27-neighbour table Box::Init builds
+// (CellList::RebuildNeighbors order), computed instead of loaded.
+__device__ __forceinline__ int nbr_cell(const int *e, int cell, int nn) {
+  int z = cell % e[2], xy = cell / e[2];
+  int y = xy % e[1], x = xy / e[1];
+  x += nn / 9 - 1;
+  y += (nn / 3) % 3 - 1;
+  z += nn % 3 - 1;
+  x += x < 0 ? e[0] : (x >= e[0] ? -e[0] : 0);
+  y += y < 0 ? e[1] : (y >= e[1] ? -e[1] : 0);
+  z += z < 0 ? e[2] : (z >= e[2] ? -e[2] : 0);
+  return (x * e[1] + y) * e[2] + z;
+}
+
 __device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -806,7 +821,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     for (int u = threadIdx.x; u < units; u += CT) {
       int a = u / (2 * NB27), side = (u / NB27) % 2, nn = u % NB27;
       int cell = (int)S.hdr[(side ? 16 : 8) + a];
-      int c2 = b.nbr[cell * NB27 + nn];
+      int c2 = nbr_cell(b.edge, cell, nn);
       u_cell[u] = c2;
       u_off[u + 1] = __ldcg(b.cell_count + c2);
     }
@@ -1039,9 +1054,10 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
       const int q = warp;
       double *part_t = A.part + (size_t)(t & 1) * G * 4;
       constexpr int PF = PART_MAX_GRID / 32;
-      // two polls in flight, staggered, so that a check comes about every
-      // half memory round trip
-      double pv[PF], pw[PF];
+      // three polls in flight, staggered, so that a check comes about
+      // every third of a memory round trip
+      constexpr int NPOLL = 3;
+      double pp[NPOLL][PF];
       auto issue = [&](double *dst) {
 #pragma unroll
         for (int i = 0; i < PF; ++i) {
@@ -1056,22 +1072,26 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
           mine &= __double_as_longlong(src[i]) != (long long)PART_EMPTY;
         return __all_sync(0xffffffffu, mine);
       };
-      issue(pv);
-      __nanosleep(200);
-      issue(pw);
-      int ok = 1;
+#pragma unroll
+      for (int j = 0; j < NPOLL; ++j) {
+        if (j)
+          __nanosleep(150);
+        issue(pp[j]);
+      }
+      int ok = 1, got = -1;
       unsigned it = 0;
       for (;;) {
-        if (present(pv))
-          break;
-        issue(pv);
-        if (present(pw)) {
 #pragma unroll
-          for (int i = 0; i < PF; ++i)
-            pv[i] = pw[i];
-          break;
+        for (int j = 0; j < NPOLL; ++j) {
+          if (got < 0) {
+            if (present(pp[j]))
+              got = j;  // warp-uniform
+            else
+              issue(pp[j]);
+          }
         }
-        issue(pw);
+        if (got >= 0)
+          break;
         int bad = 0;
         if (lane == 0) {
           if (++it > SPIN_LIMIT) {
@@ -1086,6 +1106,10 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
           break;
         }
       }
+      double pv[PF];
+#pragma unroll
+      for (int i = 0; i < PF; ++i)
+        pv[i] = got == 0 ? pp[0][i] : got == 1 ? pp[1][i] : pp[2][i];
       if (ok) {
         // read: mark this quantity's slots empty for move t + 2 (ordered
         // before the decision word that every later writer waits for)
