@@ -160,6 +160,7 @@ def measured_peaks(torch, dev):
     return out
 
 
+CHAIN_FP64_DRAM_BYTES_1000 = 3.32e6
 SMALL = False  # --small: the 256-water, 19.7 A box (for profiler captures)
 
 
@@ -631,9 +632,16 @@ def run_gb300(args, rank, world):
     moves_per_launch = timing["chain_moves"] / max(timing["chain_launches"], 1)
     fl = flop_per_move(K)
     achieved = fl * moves_per_launch / (kern_ms / 1e3) / 1e12
+    # DRAM bytes (read + write) of one 1,000-move k_chain_fp64 launch of
+    # this workload after the L2 flush, from an ncu capture of this command
+    # (profiles/k_chain_fp64_8000water_full.md); other move counts: null
+    traffic = (CHAIN_FP64_DRAM_BYTES_1000
+               if not SMALL and round(moves_per_launch) == 1000 else None)
     roof = {"bound": "fp64", "achieved": achieved,
             "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
-            "frac": achieved / peaks["fp64_tflops"], "traffic": None,
+            "frac": achieved / peaks["fp64_tflops"], "traffic": traffic,
+            "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + "
+                            "dram__bytes_write.sum)",
             "kernel": "k_chain_fp64",
             "per_unit": "%.3g FP64 flop per move (%d k-vectors)" % (fl, K),
             "peak_source": peaks["pipe_peak_source"],
