@@ -2260,9 +2260,11 @@ int mixed_complete(const std::vector<Box *> &boxes,
                    const std::vector<Box *> &leaders,
                    std::vector<char> *due) {
   int rc;
-  for (Box *L : leaders)
+  for (Box *L : leaders) {
     if ((rc = L->Sync()))
       return rc;
+    harvest(*L->mc);  // the launch's events folded into its device time
+  }
   if (due)
     due->assign(boxes.size(), 0);
   for (size_t i = 0; i < boxes.size(); ++i) {

@@ -55,6 +55,7 @@ struct Job {
   size_t smem = 0;      // dynamic shared memory per CTA
   size_t mem = 0;   // admission estimate, or the box's bytes when larger
   bool busy = false;  // being set up or recomputed: sits out rounds
+  int K = -1, kmax = 0;  // k-vectors and largest |n|, once known
   Box *box = nullptr;
   double t_submit = 0, t_admit = 0, t_done = 0, t_last = 0;
   std::vector<double> xyz, com;
@@ -286,8 +287,9 @@ int Server::Admit() {
         break;
       j = queue.front();
     }
-    int K, kmax;
-    job_kvectors(*j, &K, &kmax);
+    if (j->K < 0)  // host work, done once per job
+      job_kvectors(*j, &j->K, &j->kmax);
+    const int K = j->K, kmax = j->kmax;
     int csize = job_cluster(*j, K);
     bool cold_smem = mixed_smem(K, kmax, csize, true) <= MIXED_SMEM_MAX;
     size_t smem = mixed_smem(K, kmax, csize, cold_smem);
