@@ -55,6 +55,13 @@ def test_alone_equals_mixed(srv_mod):
     assert st["jobs_done"] == len(JOBS)
     assert st["moves"] == sum(j[2] for j in JOBS)
     assert st["mean_resident"] > 1.0  # the jobs did share rounds
+    # occupancy statistics: fractions in [0, 1], counts non-negative
+    assert st["mean_admitted"] > 0.0 and st["mean_in_round"] > 0.0
+    assert 0.0 < st["cta_slot_frac"] <= 1.0
+    assert 0.0 < st["smem_frac"] <= 1.0
+    assert 0.0 < st["launch_balance"] <= 1.0 + 1e-9
+    assert min(st["stops_mem"], st["stops_smem"], st["stops_ctas"],
+               st["round_gap_s"], st["mean_queued"]) >= 0.0
     res_mixed = [mixed.result(i) for i in ids]
     mixed.close()
     for job, rm in zip(JOBS, res_mixed):
