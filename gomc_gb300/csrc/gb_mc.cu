@@ -420,10 +420,6 @@ struct ChainShared {
   int ovl_any;
   double tot[4];
   int accept, flag, ok;
-  // the next move's header, read during this move's phase B; pre_t: the
-  // move it belongs to (its phase rows are then already in the row table)
-  double nhdr[HDR];
-  int pre_t;
   unsigned gen;
   // inputs and new positions of the context being built
   double b_oldp[MAX_MOL_ATOMS][3], b_newp[MAX_MOL_ATOMS][3];
@@ -738,7 +734,6 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     for (int i = 0; i < 5; ++i)
       S.e_run[i] = b.energy[i];
     S.gen = ld_acquire(&A.bar[1]);
-    S.pre_t = -1;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -794,16 +789,10 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     // ---------------- phase A ----------------
     // the header and the rows of the largest molecule in one round trip
     const double *ctx_t = A.ctx + (size_t)(t & 1) * A.ctx_len;
-    if (S.pre_t == t) {
-      // read while the previous decision was pending
-      for (int i = threadIdx.x; i < HDR; i += CT)
-        S.hdr[i] = S.nhdr[i];
-    } else {
-      for (int i = threadIdx.x; i < HDR; i += CT)
-        S.hdr[i] = __ldcg(ctx_t + i);
-      for (int i = threadIdx.x; i < A.nrows_max * stride; i += CT)
-        tab[i] = __ldcg((const double2 *)(ctx_t + HDR) + i);
-    }
+    for (int i = threadIdx.x; i < HDR; i += CT)
+      S.hdr[i] = __ldcg(ctx_t + i);
+    for (int i = threadIdx.x; i < A.nrows_max * stride; i += CT)
+      tab[i] = __ldcg((const double2 *)(ctx_t + HDR) + i);
     __syncthreads();
     int m = (int)S.hdr[0];
     int na = (int)S.hdr[2];
@@ -1055,27 +1044,6 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
         if (S.b_writer)
           build_ctx_rest(A, S, t + 1, (int)threadIdx.x - bfirst, CT - bfirst,
                          true);
-        // The next move's header and phase rows are final once their
-        // writers have flagged them (the leader publishes this decision
-        // only after the same flags): read them now, while the decision is
-        // pending, the header into a second buffer (this move's is still
-        // read after the decision), the rows into the row table (read only
-        // in phase A).
-        if (warp == 7) {
-          int pok = warp_wait_all(A.seq + SEQ_CTX, (int)ctx_builders(A, t + 1),
-                                  (unsigned)(t + 1), b.err);
-          if (lane == 0)
-            S.pre_t = pok ? t + 1 : -1;
-        }
-        group_sync(CT - bfirst);
-        if (S.pre_t == t + 1) {
-          const double *nctx = A.ctx + (size_t)((t + 1) & 1) * A.ctx_len;
-          const int tid = (int)threadIdx.x - bfirst, cnt = CT - bfirst;
-          for (int i = tid; i < HDR; i += cnt)
-            S.nhdr[i] = __ldcg(nctx + i);
-          for (int i = tid; i < A.nrows_max * stride; i += cnt)
-            tab[i] = __ldcg((const double2 *)(nctx + HDR) + i);
-        }
       }
     } else if (leader) {
       // Warps 0..3 of the leader each gather one quantity over all CTAs
