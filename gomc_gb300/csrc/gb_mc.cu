@@ -30,8 +30,10 @@
 #include "gb_pair.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <thread>
 
 namespace gb {
 
@@ -2267,20 +2269,45 @@ int mixed_complete(const std::vector<Box *> &boxes,
   }
   if (due)
     due->assign(boxes.size(), 0);
+  std::vector<Box *> rec;
   for (size_t i = 0; i < boxes.size(); ++i) {
     if (n[i] <= 0)
       continue;
     Box &b = *boxes[i];
     McState &s = *b.mc;
+    if ((rc = b.CheckError()))
+      return rc;
     int64_t R = s.params.recompute_freq;
     if (R > 0 && s.next_step % R == 0) {
       if (due)
         (*due)[i] = 1;
-      else if ((rc = recompute_fp64(b, s)))
-        return rc;
+      else
+        rec.push_back(&b);
     }
-    if ((rc = b.CheckError()))
-      return rc;
+  }
+  // The due recomputes, several boxes at once: each runs on its own box's
+  // stream and waits on that stream only, so one box's kernels fill the
+  // tails and host gaps of another's.  Boxes are independent; the order
+  // changes no result.
+  if (rec.size() == 1)
+    return recompute_fp64(*rec[0], *rec[0]->mc);
+  if (!rec.empty()) {
+    const int dev = rec[0]->cfg.device;
+    const int nt = (int)std::min<size_t>(rec.size(), 4);
+    std::vector<int> rcs(rec.size(), OK);
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> th;
+    for (int k = 0; k < nt; ++k)
+      th.emplace_back([&] {
+        cudaSetDevice(dev);
+        for (size_t i; (i = next++) < rec.size();)
+          rcs[i] = recompute_fp64(*rec[i], *rec[i]->mc);
+      });
+    for (auto &x : th)
+      x.join();
+    for (int r : rcs)
+      if (r)
+        return r;
   }
   return OK;
 }
