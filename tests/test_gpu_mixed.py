@@ -99,8 +99,10 @@ def test_batch_matches_alone(gb):
         out = []
         for i, (n, L, rc) in enumerate(sizes):
             b = make(gb, n, L, rc, gb.GB_MIXED, seed=seed0 + i)
+            # an FP64 recompute every 200 moves: the batched run makes
+            # several boxes' recomputes at once
             b.mc_init(500 + i, [0.5, 0.5, 0.0], 300, scales=SCALES,
-                      cluster_size=8)
+                      cluster_size=8, recompute_freq=200)
             out.append(b)
         return out
 
@@ -118,6 +120,8 @@ def test_batch_matches_alone(gb):
         sm, cm = m.mc_state()
         np.testing.assert_array_equal(sm, sa)
         np.testing.assert_array_equal(cm, ca)
+        dm, da = m.mc_drift(), a.mc_drift()
+        assert dm == da and dm["recomputes"] == 3
     for b in alone + mixed:
         b.close()
 
