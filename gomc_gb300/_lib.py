@@ -82,8 +82,10 @@ SIGNATURES = {
     "gb_checkpoint_size": (C.c_int, [_P, _L]),
     "gb_checkpoint_save": (C.c_int, [_P, _P, C.c_int64]),
     "gb_checkpoint_load": (C.c_int, [_P, _P, C.c_int64]),
-    "gb_particle_inter": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_double, _D,
+    "gb_particle_inter": (C.c_int, [_P, C.c_int32, C.c_int32, _D,
                                     C.c_int32, _D, _D, _I]),
+    "gb_cell_remove_mol": (C.c_int, [_P, C.c_int32]),
+    "gb_cell_add_mol": (C.c_int, [_P, C.c_int32]),
     "gb_box_force": (C.c_int, [_P, _D, _D, _D, _D]),
     "gb_calculate_torque": (C.c_int, [_P, _D]),
     "gb_num_kvectors": (C.c_int, [_P, _I, _I]),
@@ -92,6 +94,16 @@ SIGNATURES = {
     "gb_box_reciprocal_setup": (C.c_int, [_P]),
     "gb_box_reciprocal_sums": (C.c_int, [_P]),
     "gb_box_reciprocal": (C.c_int, [_P, C.c_int32, _D]),
+    "gb_box_reciprocal_sums_coords": (C.c_int, [_P, _D]),
+    "gb_box_reciprocal_setup_coords": (C.c_int, [_P, _D]),
+    "gb_recip_init": (C.c_int, [_P, _D, _I]),
+    "gb_update_recip_vec": (C.c_int, [_P]),
+    "gb_set_box": (C.c_int, [_P, _D, _D, _D]),
+    "gb_box_edges": (C.c_int, [_P, _D]),
+    "gb_box_inter_coords": (C.c_int, [_P, _D, _D, _D, _D]),
+    "gb_box_force_coords": (C.c_int, [_P, _D, _D, _D, _D, _D]),
+    "gb_swap_self": (C.c_int, [_P, C.c_int32, _D]),
+    "gb_swap_correction": (C.c_int, [_P, C.c_int32, _D, _D]),
     "gb_mol_reciprocal": (C.c_int, [_P, C.c_int32, _D, _D]),
     "gb_swap_dest_recip": (C.c_int, [_P, C.c_int32, _D, _D]),
     "gb_swap_source_recip": (C.c_int, [_P, C.c_int32, _D, _D]),

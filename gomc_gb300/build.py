@@ -3,8 +3,6 @@
 Each CUDA translation unit under ``gomc_gb300/csrc`` is compiled by nvcc in
 parallel for ``compute_103a/sm_103a`` and linked into
 ``gomc_gb300/_build/libgomc_gb300.so`` (the C ABI of include/gomc_gb300.h).
-A C++ example that drives the library through the header-only C++ layer
-(include/gomc_gb300.hpp) is built beside it.
 """
 from __future__ import annotations
 
@@ -80,25 +78,7 @@ def build(force: bool = False, verbose: bool = False, extra=None) -> str:
         if p.returncode != 0:
             raise RuntimeError("link failed:\n%s" % p.stderr[-4000:])
         os.replace(tmp, LIB)
-    _build_example()
     return LIB
-
-
-def _build_example() -> None:
-    """C++ example over the header-only C++ layer (include/gomc_gb300.hpp)."""
-    src = os.path.join(HERE, "examples", "cpp_energy_path.cpp")
-    if not os.path.exists(src):
-        return
-    exe = os.path.join(OUT, "cpp_energy_path")
-    hpp = os.path.join(ROOT, "include", "gomc_gb300.hpp")
-    if not _stale(exe, [src, hpp, LIB]):
-        return
-    cmd = ["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"),
-           src, "-o", exe, "-L" + OUT, "-lgomc_gb300",
-           "-Wl,-rpath," + OUT]
-    p = subprocess.run(cmd, capture_output=True, text=True)
-    if p.returncode != 0:
-        raise RuntimeError("example build failed:\n%s" % p.stderr[-4000:])
 
 
 if __name__ == "__main__":

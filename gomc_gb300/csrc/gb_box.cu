@@ -219,6 +219,44 @@ void recip_vectors(const double L[3], double volume, double alphaSq,
   }
 }
 
+// COM::CalcCOM (src/COM.h:47-68), including its unwrap / re-wrap of the
+// atom coordinates: each molecule is unwrapped against its first atom,
+// averaged, and its atoms and centre wrapped back into the box.
+static void calc_com(HostSystem &s) {
+  const int M = s.n_mol;
+  double half[3] = {s.L[0] * 0.5, s.L[1] * 0.5, s.L[2] * 0.5};
+  s.cx.assign(M, 0);
+  s.cy.assign(M, 0);
+  s.cz.assign(M, 0);
+  for (int m = 0; m < M; ++m) {
+    int a0 = s.mstart[m], a1 = s.mstart[m + 1];
+    double rx = s.x[a0], ry = s.y[a0], rz = s.z[a0];
+    for (int p = a0; p < a1; ++p) {
+      s.x[p] = unwrap1(s.x[p], rx, s.L[0], half[0]);
+      s.y[p] = unwrap1(s.y[p], ry, s.L[1], half[1]);
+      s.z[p] = unwrap1(s.z[p], rz, s.L[2], half[2]);
+    }
+    double cx = 0, cy = 0, cz = 0;
+    for (int p = a0; p < a1; ++p) {
+      cx += s.x[p];
+      cy += s.y[p];
+      cz += s.z[p];
+    }
+    for (int p = a0; p < a1; ++p) {
+      s.x[p] = wrap1(s.x[p], s.L[0]);
+      s.y[p] = wrap1(s.y[p], s.L[1]);
+      s.z[p] = wrap1(s.z[p], s.L[2]);
+    }
+    double inv = 1.0 / (double)(a1 - a0);
+    cx *= inv;
+    cy *= inv;
+    cz *= inv;
+    s.cx[m] = wrap1(cx, s.L[0]);
+    s.cy[m] = wrap1(cy, s.L[1]);
+    s.cz[m] = wrap1(cz, s.L[2]);
+  }
+}
+
 // ---------------------------------------------------------------------------
 Box::~Box() { FreeAll(); }
 
@@ -252,12 +290,248 @@ void Box::FreeAll() {
   for (void *p : allocs_)
     cudaFree(p);
   allocs_.clear();
+  for (void *p : trial.allocs)
+    cudaFree(p);
+  trial.allocs.clear();
   if (h_pinned)
     cudaFreeHost(h_pinned);
   h_pinned = nullptr;
   if (own_stream && stream)
     cudaStreamDestroy(stream);
   stream = nullptr;
+}
+
+
+// (Re)allocate *p to hold `bytes`, dropping its old contents; the pointer is
+// owned by `allocs`.
+static int regrow(Box &b, void **p, size_t bytes, std::vector<void *> &allocs) {
+  if (*p) {
+    cudaFree(*p);
+    allocs.erase(std::remove(allocs.begin(), allocs.end(), *p), allocs.end());
+    *p = nullptr;
+  }
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(bytes, 1));
+  if (e != cudaSuccess)
+    return b.CudaCheck(e, "cudaMalloc");
+  allocs.push_back(q);
+  b.dev_bytes += bytes;
+  *p = q;
+  return OK;
+}
+
+// CellList::ResizeGrid / RebuildNeighbors (src/CellList.cpp:138-218) for
+// edges L: cells per axis max(floor(L / Rcut), 3), the 27-neighbour table in
+// the reference's order, and the slot capacity (three times the fullest cell
+// of the given coordinates, at least 32, a multiple of 32).  The cell arrays
+// grow when the grid needs more slots than they hold.
+int Box::GridGeometry(const double L[3], const double *x, const double *y,
+                      const double *z, DevBox &d, size_t *cell_cap,
+                      size_t *nbr_cap, std::vector<void *> &allocs) {
+  for (int k = 0; k < 3; ++k) {
+    d.L[k] = L[k];
+    d.half[k] = L[k] * 0.5;
+    d.edge[k] = std::max((int)std::floor(L[k] / cfg.rcut), 3);
+    d.cellSize[k] = L[k] / d.edge[k];
+    d.invCell[k] = 1.0 / d.cellSize[k];
+    d.invL[k] = 1.0 / L[k];
+  }
+  d.volume = L[0] * L[1] * L[2];
+  d.ncell = d.edge[0] * d.edge[1] * d.edge[2];
+  std::vector<int> nbr((size_t)d.ncell * NB27);
+  {
+    int *e = d.edge;
+    for (int x = 0; x < e[0]; ++x)
+      for (int y = 0; y < e[1]; ++y)
+        for (int z = 0; z < e[2]; ++z) {
+          int cell = x * e[2] * e[1] + y * e[2] + z;
+          int n = 0;
+          for (int dx = -1; dx <= 1; ++dx)
+            for (int dy = -1; dy <= 1; ++dy)
+              for (int dz = -1; dz <= 1; ++dz)
+                nbr[(size_t)cell * NB27 + n++] =
+                    ((x + dx + e[0]) % e[0]) * e[2] * e[1] +
+                    ((y + dy + e[1]) % e[1]) * e[2] + ((z + dz + e[2]) % e[2]);
+        }
+  }
+  {
+    std::vector<int> cnt(d.ncell, 0);
+    int mx = 0;
+    for (int i = 0; i < d.n_atoms; ++i) {
+      int cc = position_to_cell(d, x[i], y[i], z[i]);
+      if (cc < 0 || cc >= d.ncell)
+        return Fail(ERR_ARG, "coordinates must lie inside the box");
+      mx = std::max(mx, ++cnt[cc]);
+    }
+    int cap = std::max(3 * mx, 32);
+    d.cap = (cap + 31) / 32 * 32;
+  }
+  int rc;
+  size_t NC = (size_t)d.ncell * d.cap;
+  if (NC > *cell_cap) {
+    if ((rc = regrow(*this, (void **)&d.cell_atom, NC * 4, allocs)) ||
+        (rc = regrow(*this, (void **)&d.cell_pos, NC * sizeof(double4_32a),
+                     allocs)) ||
+        (rc = regrow(*this, (void **)&d.cell_meta, NC * 4, allocs)) ||
+        (rc = regrow(*this, (void **)&d.cell_fix, NC * sizeof(uint4),
+                     allocs)) ||
+        (rc = regrow(*this, (void **)&d.cell_qlo, NC * 4, allocs)))
+      return rc;
+    *cell_cap = NC;
+  }
+  if ((size_t)d.ncell * NB27 > *nbr_cap) {
+    if ((rc = regrow(*this, (void **)&d.nbr, nbr.size() * 4, allocs)) ||
+        (rc = regrow(*this, (void **)&d.cell_count, (size_t)d.ncell * 4,
+                     allocs)))
+      return rc;
+    *nbr_cap = (size_t)d.ncell * NB27;
+  }
+  return CudaCheck(cudaMemcpyAsync(d.nbr, nbr.data(), nbr.size() * 4,
+                                   cudaMemcpyHostToDevice, stream),
+                   "upload");
+}
+
+// Ewald::RecipInit (src/Ewald.cpp:835-903) for edges L into `ks`: the
+// k-vectors with their prefactors, the integer indices, and runs of up to
+// KRUN consecutive n_x per (n_y, n_z) column for the structure-factor
+// kernels (longest runs first).
+int Box::BuildKSet(const double L[3], KSet &ks) {
+  std::vector<double> kx, ky, kz, hs, pf;
+  std::vector<char4> kn;
+  int kmax = 0;
+  recip_vectors(L, L[0] * L[1] * L[2], ff.alphaSq, ff.recip_rcutSq,
+                ff.recip_rcut, kx, ky, kz, hs, pf, kn, &kmax);
+  if (kmax > 127)
+    return Fail(ERR_UNSUPPORTED, "k-vector index above 127");
+  const int K = (int)kx.size();
+  std::vector<float> pff(pf.begin(), pf.end());
+  std::map<std::pair<int, int>, std::vector<std::pair<int, int>>> cols;
+  for (int k = 0; k < K; ++k)
+    cols[{kn[k].y, kn[k].z}].push_back({kn[k].x, k});
+  std::vector<int4> runs;
+  std::vector<int> run_k;
+  for (auto &c : cols) {
+    auto &v = c.second;  // n_x ascending (k vectors are listed x outer)
+    size_t i = 0;
+    while (i < v.size()) {
+      size_t j = i + 1;
+      while (j < v.size() && j - i < (size_t)KRUN &&
+             v[j].first == v[j - 1].first + 1)
+        ++j;
+      runs.push_back(make_int4(c.first.first, c.first.second, v[i].first,
+                               (int)(j - i)));
+      for (int g = 0; g < KRUN; ++g)
+        run_k.push_back(i + g < j ? v[i + g].second : -1);
+      i = j;
+    }
+  }
+  // longest runs first: neighbouring threads then take runs of equal
+  // length, and a warp skips the members none of its runs has (each run's
+  // sums do not depend on which thread takes it)
+  {
+    std::vector<int> order(runs.size());
+    for (size_t r = 0; r < runs.size(); ++r)
+      order[r] = (int)r;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+      return runs[x].w > runs[y].w;
+    });
+    std::vector<int4> r2(runs.size());
+    std::vector<int> k2(run_k.size());
+    for (size_t r = 0; r < runs.size(); ++r) {
+      r2[r] = runs[order[r]];
+      for (int g = 0; g < KRUN; ++g)
+        k2[r * KRUN + g] = run_k[(size_t)order[r] * KRUN + g];
+    }
+    runs.swap(r2);
+    run_k.swap(k2);
+  }
+  int rc;
+  if ((size_t)K > ks.cap) {
+    if ((rc = regrow(*this, (void **)&ks.kx, (size_t)K * 8, allocs_)) ||
+        (rc = regrow(*this, (void **)&ks.ky, (size_t)K * 8, allocs_)) ||
+        (rc = regrow(*this, (void **)&ks.kz, (size_t)K * 8, allocs_)) ||
+        (rc = regrow(*this, (void **)&ks.prefact, (size_t)K * 8, allocs_)) ||
+        (rc = regrow(*this, (void **)&ks.hsqr, (size_t)K * 8, allocs_)) ||
+        (rc = regrow(*this, (void **)&ks.kn, (size_t)K * 4, allocs_)) ||
+        (rc = regrow(*this, (void **)&ks.prefact_f, (size_t)K * 4, allocs_)))
+      return rc;
+    ks.cap = K;
+  }
+  if (runs.size() > ks.run_cap) {
+    if ((rc = regrow(*this, (void **)&ks.krun, runs.size() * sizeof(int4),
+                     allocs_)) ||
+        (rc = regrow(*this, (void **)&ks.krun_k, run_k.size() * sizeof(int),
+                     allocs_)))
+      return rc;
+    ks.run_cap = runs.size();
+  }
+  auto up = [&](void *dst, const void *src, size_t bytes) {
+    return CudaCheck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice,
+                                     stream),
+                     "upload");
+  };
+  if ((rc = up(ks.kx, kx.data(), (size_t)K * 8)) ||
+      (rc = up(ks.ky, ky.data(), (size_t)K * 8)) ||
+      (rc = up(ks.kz, kz.data(), (size_t)K * 8)) ||
+      (rc = up(ks.prefact, pf.data(), (size_t)K * 8)) ||
+      (rc = up(ks.hsqr, hs.data(), (size_t)K * 8)) ||
+      (rc = up(ks.kn, kn.data(), (size_t)K * 4)) ||
+      (rc = up(ks.krun, runs.data(), runs.size() * sizeof(int4))) ||
+      (rc = up(ks.krun_k, run_k.data(), run_k.size() * sizeof(int))) ||
+      (rc = up(ks.prefact_f, pff.data(), (size_t)K * 4)))
+    return rc;
+  // the host vectors go out of scope: wait for the copies
+  if ((rc = Sync()))
+    return rc;
+  ks.K = K;
+  ks.kmax = kmax;
+  ks.nrun = (int)runs.size();
+  for (int d = 0; d < 3; ++d)
+    ks.L[d] = L[d];
+  return OK;
+}
+
+// The four structure-factor arrays hold at least K entries; growing them
+// keeps the Ref sums (their first entries).
+int Box::EnsureSums(size_t K) {
+  if (K <= sums_cap)
+    return OK;
+  double **arr[4] = {&dev.sumRref, &dev.sumIref, &dev.sumRnew, &dev.sumInew};
+  for (int i = 0; i < 4; ++i) {
+    double *old = *arr[i];
+    double *q = nullptr;
+    int rc = Alloc(&q, K);
+    if (rc)
+      return rc;
+    if (old && sums_cap) {
+      if ((rc = CudaCheck(cudaMemcpyAsync(q, old, sums_cap * 8,
+                                          cudaMemcpyDeviceToDevice, stream),
+                          "copy")) ||
+          (rc = Sync()))
+        return rc;
+      cudaFree(old);
+      allocs_.erase(std::remove(allocs_.begin(), allocs_.end(), (void *)old),
+                    allocs_.end());
+    }
+    *arr[i] = q;
+  }
+  sums_cap = K;
+  return OK;
+}
+
+void Box::MirrorKRef() {
+  dev.K = kref.K;
+  dev.kmax = kref.kmax;
+  dev.nrun = kref.nrun;
+  dev.kx = kref.kx;
+  dev.ky = kref.ky;
+  dev.kz = kref.kz;
+  dev.prefact = kref.prefact;
+  dev.hsqr = kref.hsqr;
+  dev.kn = kref.kn;
+  dev.prefact_f = kref.prefact_f;
+  dev.krun = kref.krun;
+  dev.krun_k = kref.krun_k;
 }
 
 int Box::EnsureScratch(size_t n) {
@@ -340,40 +614,8 @@ int Box::Init(const HostSystem &s0, const BoxConfig &c) {
           s.z[i] >= 0 && s.z[i] <= s.L[2]))
       return Fail(ERR_ARG, "an atom lies outside the box after wrapping");
   }
-  // COM::CalcCOM (src/COM.h:47-68), including its unwrap / re-wrap of the
-  // atom coordinates.
   double half[3] = {s.L[0] * 0.5, s.L[1] * 0.5, s.L[2] * 0.5};
-  s.cx.assign(M, 0);
-  s.cy.assign(M, 0);
-  s.cz.assign(M, 0);
-  for (int m = 0; m < M; ++m) {
-    int a0 = s.mstart[m], a1 = s.mstart[m + 1];
-    double rx = s.x[a0], ry = s.y[a0], rz = s.z[a0];
-    for (int p = a0; p < a1; ++p) {
-      s.x[p] = unwrap1(s.x[p], rx, s.L[0], half[0]);
-      s.y[p] = unwrap1(s.y[p], ry, s.L[1], half[1]);
-      s.z[p] = unwrap1(s.z[p], rz, s.L[2], half[2]);
-    }
-    double cx = 0, cy = 0, cz = 0;
-    for (int p = a0; p < a1; ++p) {
-      cx += s.x[p];
-      cy += s.y[p];
-      cz += s.z[p];
-    }
-    for (int p = a0; p < a1; ++p) {
-      s.x[p] = wrap1(s.x[p], s.L[0]);
-      s.y[p] = wrap1(s.y[p], s.L[1]);
-      s.z[p] = wrap1(s.z[p], s.L[2]);
-    }
-    double inv = 1.0 / (double)(a1 - a0);
-    cx *= inv;
-    cy *= inv;
-    cz *= inv;
-    s.cx[m] = wrap1(cx, s.L[0]);
-    s.cy[m] = wrap1(cy, s.L[1]);
-    s.cz[m] = wrap1(cz, s.L[2]);
-  }
-
+  calc_com(s);
   build_ff(s, c, &ff);
   DevBox &d = dev;
   for (int k = 0; k < 3; ++k) {
@@ -384,59 +626,22 @@ int Box::Init(const HostSystem &s0, const BoxConfig &c) {
   d.n_atoms = N;
   d.n_mol = M;
 
-  // cell grid (CellList::ResizeGrid / RebuildNeighbors,
-  // src/CellList.cpp:138-218)
-  for (int k = 0; k < 3; ++k) {
-    d.edge[k] = std::max((int)std::floor(s.L[k] / c.rcut), 3);
-    d.cellSize[k] = s.L[k] / d.edge[k];
-    d.invCell[k] = 1.0 / d.cellSize[k];
-    d.invL[k] = 1.0 / s.L[k];
-  }
-  d.ncell = d.edge[0] * d.edge[1] * d.edge[2];
-  std::vector<int> nbr((size_t)d.ncell * NB27);
-  {
-    int *e = d.edge;
-    for (int x = 0; x < e[0]; ++x)
-      for (int y = 0; y < e[1]; ++y)
-        for (int z = 0; z < e[2]; ++z) {
-          int cell = x * e[2] * e[1] + y * e[2] + z;
-          int n = 0;
-          for (int dx = -1; dx <= 1; ++dx)
-            for (int dy = -1; dy <= 1; ++dy)
-              for (int dz = -1; dz <= 1; ++dz)
-                nbr[(size_t)cell * NB27 + n++] =
-                    ((x + dx + e[0]) % e[0]) * e[2] * e[1] +
-                    ((y + dy + e[1]) % e[1]) * e[2] + ((z + dz + e[2]) % e[2]);
-        }
-  }
-  // capacity: three times the fullest cell at set-up, at least 32 slots
-  {
-    std::vector<int> cnt(d.ncell, 0);
-    int mx = 0;
-    for (int i = 0; i < N; ++i) {
-      int cc = position_to_cell(d, s.x[i], s.y[i], s.z[i]);
-      mx = std::max(mx, ++cnt[cc]);
-    }
-    int cap = std::max(3 * mx, 32);
-    d.cap = (cap + 31) / 32 * 32;
-  }
-
-  // device allocations
-  size_t NC = (size_t)d.ncell * d.cap;
+  // device allocations; the cell grid (CellList::ResizeGrid /
+  // RebuildNeighbors, src/CellList.cpp:138-218) and its arrays
   if ((rc = Alloc(&d.x, N)) || (rc = Alloc(&d.y, N)) || (rc = Alloc(&d.z, N)) ||
       (rc = Alloc(&d.cx, M)) || (rc = Alloc(&d.cy, M)) ||
       (rc = Alloc(&d.cz, M)) || (rc = Alloc(&d.q, N)) ||
       (rc = Alloc(&d.kind, N)) || (rc = Alloc(&d.mol, N)) ||
-      (rc = Alloc(&d.mstart, M + 1)) || (rc = Alloc(&d.nbr, nbr.size())) ||
-      (rc = Alloc(&d.cell_count, d.ncell)) || (rc = Alloc(&d.cell_atom, NC)) ||
-      (rc = Alloc(&d.cell_pos, NC)) || (rc = Alloc(&d.cell_meta, NC)) ||
-      (rc = Alloc(&d.cell_fix, NC)) || (rc = Alloc(&d.cell_qlo, NC)) ||
+      (rc = Alloc(&d.mstart, M + 1)) ||
       (rc = Alloc(&d.atom_cell, N)) ||
       (rc = Alloc(&d.atom_slot, N)) || (rc = Alloc(&d.energy, 8)) ||
       (rc = Alloc(&d.err, 4)) || (rc = Alloc(&d_ff, 1)) ||
       (rc = Alloc(&d_small, 4096)) || (rc = Alloc(&d_aF, 3 * (size_t)N)) ||
       (rc = Alloc(&d_mF, 3 * (size_t)M)) || (rc = Alloc(&d_aR, 3 * (size_t)N)) ||
       (rc = Alloc(&d_mR, 3 * (size_t)M)) || (rc = Alloc(&d_tq, 3 * (size_t)M)))
+    return rc;
+  if ((rc = GridGeometry(s.L, s.x.data(), s.y.data(), s.z.data(), d,
+                         &grid_cell_cap_, &grid_nbr_cap_, allocs_)))
     return rc;
   rc = CudaCheck(cudaMallocHost(&h_pinned, 4096 * sizeof(double)), "pinned");
   if (rc)
@@ -455,8 +660,7 @@ int Box::Init(const HostSystem &s0, const BoxConfig &c) {
       (rc = up(d.q, s.q.data(), N * 8)) ||
       (rc = up(d.kind, s.kind.data(), N * 4)) ||
       (rc = up(d.mol, s.mol.data(), N * 4)) ||
-      (rc = up(d.mstart, s.mstart.data(), (M + 1) * 4)) ||
-      (rc = up(d.nbr, nbr.data(), nbr.size() * 4)))
+      (rc = up(d.mstart, s.mstart.data(), (M + 1) * 4)))
     return rc;
   ff.erfc_tab = nullptr;
   ff.etab_key0 = ff.etab_nseg = 0;
@@ -475,66 +679,13 @@ int Box::Init(const HostSystem &s0, const BoxConfig &c) {
       (rc = CudaCheck(cudaMemsetAsync(d.energy, 0, 64, stream), "memset")))
     return rc;
 
-  // Ewald tables
+  // Ewald tables: the k-vector set of the box edges and its structure
+  // factors; exp(2 pi i j / 256) (float-float) for the mixed form's phases
   if (c.ewald) {
-    std::vector<double> kx, ky, kz, hs, pf;
-    std::vector<char4> kn;
-    recip_vectors(s.L, d.volume, ff.alphaSq, ff.recip_rcutSq, ff.recip_rcut,
-                  kx, ky, kz, hs, pf, kn, &d.kmax);
-    d.K = (int)kx.size();
-    if (d.kmax > 127)
-      return Fail(ERR_UNSUPPORTED, "k-vector index above 127");
-    std::vector<float> pff(pf.begin(), pf.end());
-    size_t K = d.K;
-    // runs of consecutive n_x per (n_y, n_z) column, k indices ascending
-    std::map<std::pair<int, int>, std::vector<std::pair<int, int>>> cols;
-    for (int k = 0; k < d.K; ++k)
-      cols[{kn[k].y, kn[k].z}].push_back({kn[k].x, k});
-    std::vector<int4> runs;
-    std::vector<int> run_k;
-    for (auto &c : cols) {
-      auto &v = c.second;  // n_x ascending (k vectors are listed x outer)
-      size_t i = 0;
-      while (i < v.size()) {
-        size_t j = i + 1;
-        while (j < v.size() && j - i < (size_t)KRUN &&
-               v[j].first == v[j - 1].first + 1)
-          ++j;
-        runs.push_back(make_int4(c.first.first, c.first.second, v[i].first,
-                                 (int)(j - i)));
-        for (int g = 0; g < KRUN; ++g)
-          run_k.push_back(i + g < j ? v[i + g].second : -1);
-        i = j;
-      }
-    }
-    // longest runs first: neighbouring threads then take runs of equal
-    // length, and a warp skips the members none of its runs has (each
-    // run's sums do not depend on which thread takes it)
-    {
-      std::vector<int> order(runs.size());
-      for (size_t r = 0; r < runs.size(); ++r)
-        order[r] = (int)r;
-      std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
-        return runs[x].w > runs[y].w;
-      });
-      std::vector<int4> r2(runs.size());
-      std::vector<int> k2(run_k.size());
-      for (size_t r = 0; r < runs.size(); ++r) {
-        r2[r] = runs[order[r]];
-        for (int g = 0; g < KRUN; ++g)
-          k2[r * KRUN + g] = run_k[(size_t)order[r] * KRUN + g];
-      }
-      runs.swap(r2);
-      run_k.swap(k2);
-    }
-    d.nrun = (int)runs.size();
-    if ((rc = Alloc(&d.kx, K)) || (rc = Alloc(&d.ky, K)) ||
-        (rc = Alloc(&d.kz, K)) || (rc = Alloc(&d.prefact, K)) ||
-        (rc = Alloc(&d.hsqr, K)) || (rc = Alloc(&d.kn, K)) ||
-        (rc = Alloc(&d.prefact_f, K)) || (rc = Alloc(&d.sumRref, K)) ||
-        (rc = Alloc(&d.sumIref, K)) || (rc = Alloc(&d.sumRnew, K)) ||
-        (rc = Alloc(&d.sumInew, K)) || (rc = Alloc(&d.krun, runs.size())) ||
-        (rc = Alloc(&d.krun_k, run_k.size())) || (rc = Alloc(&d.cis256, 256)))
+    if ((rc = BuildKSet(s.L, kref)) || (rc = EnsureSums(kref.K)))
+      return rc;
+    MirrorKRef();
+    if ((rc = Alloc(&d.cis256, 256)))
       return rc;
     // exp(2 pi i j / 256) from the first octant by symmetry, each value
     // split into FP32 hi + lo
@@ -557,15 +708,7 @@ int Box::Init(const HostSystem &s0, const BoxConfig &c) {
       cis[j] = make_float4(rh, (float)(re - (double)rh), ih,
                            (float)(im - (double)ih));
     }
-    if ((rc = up(d.kx, kx.data(), K * 8)) || (rc = up(d.ky, ky.data(), K * 8)) ||
-        (rc = up(d.kz, kz.data(), K * 8)) ||
-        (rc = up(d.prefact, pf.data(), K * 8)) ||
-        (rc = up(d.hsqr, hs.data(), K * 8)) ||
-        (rc = up(d.kn, kn.data(), K * 4)) ||
-        (rc = up(d.krun, runs.data(), runs.size() * sizeof(int4))) ||
-        (rc = up(d.krun_k, run_k.data(), run_k.size() * sizeof(int))) ||
-        (rc = up(d.prefact_f, pff.data(), K * 4)) ||
-        (rc = up(d.cis256, cis.data(), 256 * sizeof(float4))))
+    if ((rc = up(d.cis256, cis.data(), 256 * sizeof(float4))))
       return rc;
   }
   if ((rc = GridAll()))
@@ -599,6 +742,34 @@ int Box::GridAll() {
   int rc = launch_grid_all(*this, dev);
   if (rc)
     return rc;
+  cell_out.assign(dev.n_mol, 0);
+  n_cell_out = 0;
+  return OK;
+}
+
+int Box::CellRemoveMol(int m) {
+  if (m < 0 || m >= dev.n_mol)
+    return Fail(ERR_ARG, "molecule index out of range");
+  if (cell_out[m])
+    return Fail(ERR_STATE, "molecule is not in the cell list");
+  int rc = launch_cell_remove_mol(*this, m);
+  if (rc)
+    return rc;
+  cell_out[m] = 1;
+  ++n_cell_out;
+  return OK;
+}
+
+int Box::CellAddMol(int m) {
+  if (m < 0 || m >= dev.n_mol)
+    return Fail(ERR_ARG, "molecule index out of range");
+  if (!cell_out[m])
+    return Fail(ERR_STATE, "molecule is already in the cell list");
+  int rc = launch_cell_add_mol(*this, m);
+  if (rc || (rc = CheckError()))
+    return rc;
+  cell_out[m] = 0;
+  --n_cell_out;
   return OK;
 }
 
@@ -901,18 +1072,24 @@ int Box::SingleMoleculeInter(int m, const double lam[4], double out[4]) {
   return CheckError();
 }
 
-int Box::ParticleInter(int m, int kind, double charge, const double *trials,
-                       int ntrials, double *en, double *real, int *overlap) {
-  if (m < 0 || m >= dev.n_mol || kind < 0 || kind >= ff.n_kinds ||
-      ntrials <= 0 || ntrials > 256)
+// CalculateEnergy::ParticleInter (src/CalculateEnergy.cpp:727-785): atom
+// `part` of molecule m (its kind and charge) at each trial position, against
+// the atoms in the cell grid.
+int Box::ParticleInter(int m, int part, const double *trials, int ntrials,
+                       double *en, double *real, int *overlap) {
+  if (m < 0 || m >= dev.n_mol || part < 0 ||
+      part >= host.mstart[m + 1] - host.mstart[m] || ntrials <= 0 ||
+      ntrials > 256)
     return Fail(ERR_ARG, "ParticleInter arguments out of range");
+  const int kind = host.kind[host.mstart[m] + part];
+  const double charge = host.q[host.mstart[m] + part];
   if (check_newpos(*this, m, trials, ntrials))
     return Fail(ERR_ARG, "trial coordinates must lie inside the box");
   std::memcpy(h_pinned, trials, 3 * ntrials * sizeof(double));
   int rc = CudaCheck(cudaMemcpyAsync(d_small + 1024, h_pinned, 3 * ntrials * 8,
                                      cudaMemcpyHostToDevice, stream),
                      "upload");
-  if (rc || (rc = launch_particle_inter(*this, m, kind, charge, d_small + 1024,
+  if (rc || (rc = launch_particle_inter(*this, kind, charge, d_small + 1024,
                                         ntrials, d_small)))
     return rc;
   if ((rc = CudaCheck(cudaMemcpyAsync(h_pinned, d_small, 3 * ntrials * 8,
@@ -1005,6 +1182,12 @@ int Box::BoxForce(double *inter, double *real, double *h_aF, double *h_mF) {
   int rc = launch_box_force(*this, dev, d_aF, d_mF, d_small);
   if (rc)
     return rc;
+  return ForceDownload(inter, real, h_aF, h_mF);
+}
+
+int Box::ForceDownload(double *inter, double *real, double *h_aF,
+                       double *h_mF) {
+  int rc;
   if ((rc = CudaCheck(cudaMemcpyAsync(h_pinned, d_small, 16,
                                       cudaMemcpyDeviceToHost, stream),
                       "download")))
@@ -1090,41 +1273,351 @@ int Box::GetCoords(double *xyz, double *com) {
   return OK;
 }
 
+// Replace the coordinates (and molecule centres) and bring every derived
+// quantity in line, as System::Init does after reading coordinates
+// (src/System.cpp:67-100): CellList::GridAll, the Ewald structure factors
+// (BoxReciprocalSetup + SetRecipRef) and the running energies
+// (CalculateEnergy::SystemTotal).  Without `com` the centres are computed
+// the way COM::CalcCOM does (which also re-wraps the atoms).
 int Box::SetCoords(const double *xyz, const double *com) {
   int N = dev.n_atoms, M = dev.n_mol;
-  std::vector<double> t(3 * (size_t)std::max(N, M));
-  double *dst[3] = {dev.x, dev.y, dev.z};
-  double *cdst[3] = {dev.cx, dev.cy, dev.cz};
-  int rc;
   for (int i = 0; i < N; ++i)
     for (int d = 0; d < 3; ++d) {
       double v = xyz[3 * i + d];
       if (!(v >= 0.0 && v <= dev.L[d]))
         return Fail(ERR_ARG, "coordinates must lie inside the box");
-      t[(size_t)d * N + i] = v;
     }
+  HostSystem s = host;
+  for (int i = 0; i < N; ++i) {
+    s.x[i] = xyz[3 * i];
+    s.y[i] = xyz[3 * i + 1];
+    s.z[i] = xyz[3 * i + 2];
+  }
+  if (com) {
+    for (int m = 0; m < M; ++m) {
+      s.cx[m] = com[3 * m];
+      s.cy[m] = com[3 * m + 1];
+      s.cz[m] = com[3 * m + 2];
+    }
+  } else {
+    calc_com(s);
+  }
+  const double *src[6] = {s.x.data(), s.y.data(), s.z.data(),
+                          s.cx.data(), s.cy.data(), s.cz.data()};
+  double *dst[6] = {dev.x, dev.y, dev.z, dev.cx, dev.cy, dev.cz};
+  int rc;
+  for (int d = 0; d < 6; ++d)
+    if ((rc = CudaCheck(cudaMemcpyAsync(dst[d], src[d],
+                                        (size_t)(d < 3 ? N : M) * 8,
+                                        cudaMemcpyHostToDevice, stream),
+                        "upload")))
+      return rc;
+  if ((rc = Sync()) || (rc = GridAll()))
+    return rc;
+  double tot[9];
+  return SystemTotal(tot);
+}
+
+
+// ---------------------------------------------------------------------------
+// Box edges that change (VolumeTransfer, src/moves/VolumeTransfer.h:143-190)
+// ---------------------------------------------------------------------------
+static bool inside(const double *xyz, int n, const double L[3]) {
+  for (int i = 0; i < n; ++i)
+    for (int d = 0; d < 3; ++d) {
+      double v = xyz[3 * i + d];
+      if (!(v >= 0.0 && v <= L[d]))
+        return false;
+    }
+  return true;
+}
+
+// Trial coordinates [N * 3] at edges L in the trial state's own buffers
+// (atom back-pointers included, so the box's grid is untouched); with
+// `grid`, also the trial cell grid.
+int Box::TrialCoords(const double L[3], const double *xyz, bool grid) {
+  const int N = dev.n_atoms, M = dev.n_mol;
+  if (!inside(xyz, N, L))
+    return Fail(ERR_ARG, "coordinates must lie inside the box edges");
+  DevBox &v = trial.v;
+  int rc;
+  if (!trial.v.x) {
+    v = dev;
+    v.x = v.y = v.z = v.cx = v.cy = v.cz = nullptr;
+    v.atom_cell = v.atom_slot = nullptr;
+    v.nbr = v.cell_count = v.cell_atom = v.cell_meta = nullptr;
+    v.cell_pos = nullptr;
+    v.cell_fix = nullptr;
+    v.cell_qlo = nullptr;
+    if ((rc = regrow(*this, (void **)&v.x, (size_t)N * 8, trial.allocs)) ||
+        (rc = regrow(*this, (void **)&v.y, (size_t)N * 8, trial.allocs)) ||
+        (rc = regrow(*this, (void **)&v.z, (size_t)N * 8, trial.allocs)) ||
+        (rc = regrow(*this, (void **)&v.cx, (size_t)M * 8, trial.allocs)) ||
+        (rc = regrow(*this, (void **)&v.cy, (size_t)M * 8, trial.allocs)) ||
+        (rc = regrow(*this, (void **)&v.cz, (size_t)M * 8, trial.allocs)) ||
+        (rc = regrow(*this, (void **)&v.atom_cell, (size_t)N * 4,
+                     trial.allocs)) ||
+        (rc = regrow(*this, (void **)&v.atom_slot, (size_t)N * 4,
+                     trial.allocs)))
+      return rc;
+  }
+  std::vector<double> t(3 * (size_t)N);
+  for (int i = 0; i < N; ++i)
+    for (int d = 0; d < 3; ++d)
+      t[(size_t)d * N + i] = xyz[3 * i + d];
+  double *dst[3] = {v.x, v.y, v.z};
   for (int d = 0; d < 3; ++d)
     if ((rc = CudaCheck(cudaMemcpyAsync(dst[d], t.data() + (size_t)d * N,
                                         (size_t)N * 8, cudaMemcpyHostToDevice,
                                         stream),
                         "upload")))
       return rc;
-  if ((rc = Sync()))
-    return rc;
-  if (com) {
-    for (int i = 0; i < M; ++i)
-      for (int d = 0; d < 3; ++d)
-        t[(size_t)d * M + i] = com[3 * i + d];
-    for (int d = 0; d < 3; ++d)
-      if ((rc = CudaCheck(cudaMemcpyAsync(cdst[d], t.data() + (size_t)d * M,
-                                          (size_t)M * 8, cudaMemcpyHostToDevice,
-                                          stream),
-                          "upload")))
-        return rc;
-    if ((rc = Sync()))
+  if (grid) {
+    if ((rc = GridGeometry(L, t.data(), t.data() + N, t.data() + 2 * (size_t)N,
+                           v, &trial.cell_cap, &trial.nbr_cap, trial.allocs)) ||
+        (rc = launch_grid_all(*this, v)))
       return rc;
+  } else {
+    for (int d = 0; d < 3; ++d) {
+      v.L[d] = L[d];
+      v.half[d] = L[d] * 0.5;
+      v.invL[d] = 1.0 / L[d];
+    }
+    v.volume = L[0] * L[1] * L[2];
   }
-  return GridAll();
+  return Sync();  // `t` goes out of scope
+}
+
+int Box::BoxInterAt(const double L[3], const double *xyz, double *inter,
+                    double *real) {
+  int rc = TrialCoords(L, xyz, true);
+  if (rc || (rc = launch_box_inter_view(*this, trial.v, d_small)))
+    return rc;
+  if ((rc = CudaCheck(cudaMemcpyAsync(h_pinned, d_small, 16,
+                                      cudaMemcpyDeviceToHost, stream),
+                      "download")) ||
+      (rc = Sync()))
+    return rc;
+  *inter = h_pinned[0];
+  *real = h_pinned[1];
+  return CheckError();
+}
+
+int Box::BoxForceAt(const double *xyz, double *inter, double *real,
+                    double *h_aF, double *h_mF) {
+  int rc = TrialCoords(dev.L, xyz, true);
+  if (rc || (rc = launch_box_force(*this, trial.v, d_aF, d_mF, d_small)))
+    return rc;
+  return ForceDownload(inter, real, h_aF, h_mF);
+}
+
+int Box::RecipInit(const double L[3]) {
+  if (!cfg.ewald)
+    return OK;
+  for (int d = 0; d < 3; ++d)
+    if (!(L[d] > 0))
+      return Fail(ERR_ARG, "box edge must be positive");
+  int rc = BuildKSet(L, knew);
+  if (rc || (rc = EnsureSums(knew.K)))
+    return rc;
+  return OK;
+}
+
+int Box::UpdateRecipVec() {
+  if (!cfg.ewald)
+    return OK;
+  if (mc)
+    return Fail(ERR_STATE,
+                "the Monte Carlo loop of this box runs at fixed box edges");
+  if (!knew.K)
+    return Fail(ERR_STATE, "no k-vector set from gb_recip_init to swap in");
+  std::swap(kref, knew);
+  MirrorKRef();
+  return OK;
+}
+
+bool Box::KSetMatchesEdges() const {
+  if (!cfg.ewald)
+    return true;
+  for (int d = 0; d < 3; ++d)
+    if (kref.L[d] != dev.L[d])
+      return false;
+  return true;
+}
+
+int Box::RecipSumsCoords(const double *xyz, bool new_set) {
+  if (!cfg.ewald)
+    return OK;
+  const KSet &ks = new_set ? knew : kref;
+  if (new_set && !knew.K)
+    return Fail(ERR_STATE, "gb_recip_init has not built a k-vector set");
+  int rc = TrialCoords(ks.L, xyz, false);
+  if (rc)
+    return rc;
+  DevBox v = trial.v;
+  v.K = ks.K;
+  v.kmax = ks.kmax;
+  v.nrun = ks.nrun;
+  v.kx = ks.kx;
+  v.ky = ks.ky;
+  v.kz = ks.kz;
+  v.prefact = ks.prefact;
+  v.hsqr = ks.hsqr;
+  v.kn = ks.kn;
+  v.prefact_f = ks.prefact_f;
+  v.krun = ks.krun;
+  v.krun_k = ks.krun_k;
+  if ((rc = launch_recip_sums_view(*this, v, v.x, v.y, v.z, dev.sumRnew,
+                                   dev.sumInew)))
+    return rc;
+  new_sums_set_ = new_set ? 1 : 0;
+  return Sync();
+}
+
+int Box::RecipEnergyNew(double *e, bool new_volume) {
+  if (!cfg.ewald) {
+    *e = 0;
+    return OK;
+  }
+  const KSet &ks = new_volume ? knew : kref;
+  if (new_volume && !knew.K)
+    return Fail(ERR_STATE, "gb_recip_init has not built a k-vector set");
+  DevBox v = dev;
+  v.K = ks.K;
+  v.prefact = ks.prefact;
+  int rc = launch_recip_energy_view(*this, v, dev.sumRnew, dev.sumInew,
+                                    d_small);
+  if (rc)
+    return rc;
+  if ((rc = CudaCheck(cudaMemcpyAsync(h_pinned, d_small, 8,
+                                      cudaMemcpyDeviceToHost, stream),
+                      "download")) ||
+      (rc = Sync()))
+    return rc;
+  *e = h_pinned[0];
+  return OK;
+}
+
+// New box edges with coordinates and centres: what VolumeTransfer::Accept
+// leaves (src/moves/VolumeTransfer.h:241-270: the new coordinates, box
+// dimensions, UpdateRecip and UpdateRecipVec), here with every derived
+// quantity recomputed as System::Init does: the cell grid of the new edges,
+// the k-vector set of the new edges (the one gb_recip_init built for them, or
+// a new one), the structure factors and the running energies.
+int Box::SetBox(const double L[3], const double *xyz, const double *com) {
+  if (mc)
+    return Fail(ERR_STATE,
+                "the Monte Carlo loop of this box runs at fixed box edges");
+  for (int d = 0; d < 3; ++d)
+    if (!(L[d] > 0))
+      return Fail(ERR_ARG, "box edge must be positive");
+  const int N = dev.n_atoms, M = dev.n_mol;
+  if (!inside(xyz, N, L))
+    return Fail(ERR_ARG, "coordinates must lie inside the box edges");
+  HostSystem s = host;
+  for (int d = 0; d < 3; ++d)
+    s.L[d] = L[d];
+  for (int i = 0; i < N; ++i) {
+    s.x[i] = xyz[3 * i];
+    s.y[i] = xyz[3 * i + 1];
+    s.z[i] = xyz[3 * i + 2];
+  }
+  if (com) {
+    for (int m = 0; m < M; ++m) {
+      s.cx[m] = com[3 * m];
+      s.cy[m] = com[3 * m + 1];
+      s.cz[m] = com[3 * m + 2];
+    }
+  } else {
+    calc_com(s);
+  }
+  int rc;
+  if ((rc = Sync()) ||
+      (rc = GridGeometry(L, s.x.data(), s.y.data(), s.z.data(), dev,
+                         &grid_cell_cap_, &grid_nbr_cap_, allocs_)))
+    return rc;
+  // force-field constants that depend on the edges (the mixed form's FP32
+  // turn length); the erfc table does not
+  const double *etab = ff.erfc_tab;
+  int key0 = ff.etab_key0, nseg = ff.etab_nseg;
+  build_ff(s, cfg, &ff);
+  ff.erfc_tab = etab;
+  ff.etab_key0 = key0;
+  ff.etab_nseg = nseg;
+  if ((rc = CudaCheck(cudaMemcpyAsync(d_ff, &ff, sizeof(FF),
+                                      cudaMemcpyHostToDevice, stream),
+                      "upload")))
+    return rc;
+  if (cfg.ewald && !KSetMatchesEdges()) {
+    bool built = knew.K > 0;
+    for (int d = 0; d < 3 && built; ++d)
+      built = knew.L[d] == L[d];
+    if (built)
+      std::swap(kref, knew);
+    else if ((rc = BuildKSet(L, kref)))
+      return rc;
+    if ((rc = EnsureSums(kref.K)))
+      return rc;
+    MirrorKRef();
+  }
+  const double *src[6] = {s.x.data(), s.y.data(), s.z.data(),
+                          s.cx.data(), s.cy.data(), s.cz.data()};
+  double *dst[6] = {dev.x, dev.y, dev.z, dev.cx, dev.cy, dev.cz};
+  for (int d = 0; d < 6; ++d)
+    if ((rc = CudaCheck(cudaMemcpyAsync(dst[d], src[d],
+                                        (size_t)(d < 3 ? N : M) * 8,
+                                        cudaMemcpyHostToDevice, stream),
+                        "upload")))
+      return rc;
+  host.L[0] = L[0];
+  host.L[1] = L[1];
+  host.L[2] = L[2];
+  if ((rc = Sync()) || (rc = GridAll()))
+    return rc;
+  double tot[9];
+  return SystemTotal(tot);
+}
+
+// Ewald::SwapSelf (src/Ewald.cpp:1375-1391): self energy of molecule m.
+int Box::SwapSelf(int m, double *e) {
+  if (m < 0 || m >= dev.n_mol)
+    return Fail(ERR_ARG, "molecule index out of range");
+  if (!cfg.ewald) {
+    *e = 0;
+    return OK;
+  }
+  double en_self = 0.0;
+  for (int a = host.mstart[m]; a < host.mstart[m + 1]; ++a)
+    en_self -= (host.q[a] * host.q[a]);
+  *e = (en_self * ff.alpha * QQ_FACT * M_2_SQRTPI * 0.5);
+  return OK;
+}
+
+// Ewald::SwapCorrection (src/Ewald.cpp:1311-1333): intramolecular
+// correction of molecule m at positions pos [n_atoms_of_m * 3] in this box.
+int Box::SwapCorrection(int m, const double *pos, double *e) {
+  if (m < 0 || m >= dev.n_mol)
+    return Fail(ERR_ARG, "molecule index out of range");
+  if (!cfg.ewald) {
+    *e = 0;
+    return OK;
+  }
+  int a0 = host.mstart[m], n = host.mstart[m + 1] - a0;
+  double correction = 0.0;
+  for (int i = 0; i < n; i++)
+    for (int j = i + 1; j < n; j++) {
+      double dx = min_image(pos[3 * i] - pos[3 * j], dev.L[0], dev.half[0]);
+      double dy = min_image(pos[3 * i + 1] - pos[3 * j + 1], dev.L[1],
+                            dev.half[1]);
+      double dz = min_image(pos[3 * i + 2] - pos[3 * j + 2], dev.L[2],
+                            dev.half[2]);
+      double distSq = dx * dx + dy * dy + dz * dz;
+      double dist = std::sqrt(distSq);
+      correction -= (host.q[a0 + i] * host.q[a0 + j] *
+                     std::erf(ff.alpha * dist) / dist);
+    }
+  *e = QQ_FACT * correction;
+  return OK;
 }
 
 int Box::GetCells(int *cell_of_atom, int edge[3]) {

@@ -13,9 +13,34 @@ struct gb_box {
 namespace {
 thread_local std::string g_create_error;
 
-int guard(gb_box *box) {
+int guard_box(gb_box *box) {
   if (!box || !box->b)
     return gb::ERR_ARG;
+  return gb::OK;
+}
+
+// Every call that works on the box's coordinates needs its k-vector set to
+// be the one of its edges; after gb_update_recip_vec swapped in a set for
+// other edges, only gb_set_box (with those edges) and the calls below that
+// use guard_box are valid.
+int guard(gb_box *box) {
+  int rc = guard_box(box);
+  if (rc)
+    return rc;
+  if (!box->b->KSetMatchesEdges())
+    return box->b->Fail(gb::ERR_STATE,
+                        "the k-vector set is for other box edges: call "
+                        "gb_set_box with them");
+  return gb::OK;
+}
+
+// Calls that move molecules or save the cell grid need every molecule in the
+// grid (a molecule taken out by gb_cell_remove_mol goes back with
+// gb_cell_add_mol or gb_grid_all).
+int all_in_grid(gb::Box &b) {
+  if (b.n_cell_out)
+    return b.Fail(gb::ERR_STATE,
+                  "a molecule is out of the cell list (gb_cell_remove_mol)");
   return gb::OK;
 }
 }  // namespace
@@ -143,6 +168,8 @@ int gb_mc_autotune(gb_box *box, int32_t objective, int32_t trial_moves,
   int rc = guard(box);
   if (rc)
     return rc;
+  if ((rc = all_in_grid(*box->b)))
+    return rc;
   int c = 0;
   rc = gb::mc_autotune(*box->b, objective, trial_moves, &c, us_per_move4);
   if (!rc && cluster_size)
@@ -164,6 +191,8 @@ int gb_checkpoint_save(gb_box *box, void *buf, int64_t bytes) {
     return rc;
   if (!buf)
     return gb::ERR_ARG;
+  if ((rc = all_in_grid(*box->b)))
+    return rc;
   return gb::checkpoint_save(*box->b, buf, bytes);
 }
 int gb_checkpoint_load(gb_box *box, const void *buf, int64_t bytes) {
@@ -172,6 +201,8 @@ int gb_checkpoint_load(gb_box *box, const void *buf, int64_t bytes) {
     return rc;
   if (!buf)
     return gb::ERR_ARG;
+  if ((rc = all_in_grid(*box->b)))
+    return rc;
   return gb::checkpoint_load(*box->b, buf, bytes);
 }
 
@@ -191,7 +222,7 @@ int gb_single_molecule_inter(gb_box *box, int32_t mol, const double *lambdas4,
   return box->b->SingleMoleculeInter(mol, lambdas4, out4);
 }
 
-int gb_particle_inter(gb_box *box, int32_t mol, int32_t kind, double charge,
+int gb_particle_inter(gb_box *box, int32_t mol, int32_t part,
                       const double *trials, int32_t ntrials, double *en,
                       double *real, int32_t *overlap) {
   if (!trials || !en || !real || !overlap)
@@ -200,12 +231,13 @@ int gb_particle_inter(gb_box *box, int32_t mol, int32_t kind, double charge,
   if (rc)
     return rc;
   std::vector<int> ov(ntrials > 0 ? ntrials : 1, 0);
-  rc = box->b->ParticleInter(mol, kind, charge, trials, ntrials, en, real,
-                             ov.data());
+  rc = box->b->ParticleInter(mol, part, trials, ntrials, en, real, ov.data());
   for (int t = 0; t < ntrials && !rc; ++t)
     overlap[t] = ov[t];
   return rc;
 }
+int gb_cell_remove_mol(gb_box *box, int32_t mol) { BOX_CALL(CellRemoveMol(mol)); }
+int gb_cell_add_mol(gb_box *box, int32_t mol) { BOX_CALL(CellAddMol(mol)); }
 int gb_box_force(gb_box *box, double *inter, double *real, double *atom_force,
                  double *mol_force) {
   if (!inter || !real)
@@ -239,10 +271,87 @@ int gb_box_reciprocal_setup(gb_box *box) { BOX_CALL(RecipSetup()); }
 int gb_box_reciprocal_sums(gb_box *box) {
   BOX_CALL(RecipSums(box->b->dev.x, box->b->dev.y, box->b->dev.z));
 }
-int gb_box_reciprocal(gb_box *box, int32_t use_ref, double *energy) {
+int gb_box_reciprocal(gb_box *box, int32_t is_new_volume, double *energy) {
   if (!energy)
     return gb::ERR_ARG;
-  BOX_CALL(RecipEnergy(energy, use_ref != 0));
+  int rc = guard_box(box);
+  if (rc)
+    return rc;
+  return box->b->RecipEnergyNew(energy, is_new_volume != 0);
+}
+int gb_box_reciprocal_sums_coords(gb_box *box, const double *xyz) {
+  if (!xyz)
+    return gb::ERR_ARG;
+  BOX_CALL(RecipSumsCoords(xyz, false));
+}
+int gb_box_reciprocal_setup_coords(gb_box *box, const double *xyz) {
+  if (!xyz)
+    return gb::ERR_ARG;
+  int rc = guard_box(box);
+  if (rc)
+    return rc;
+  return box->b->RecipSumsCoords(xyz, true);
+}
+int gb_recip_init(gb_box *box, const double *edges3, int32_t *k_count) {
+  if (!edges3)
+    return gb::ERR_ARG;
+  int rc = guard_box(box);
+  if (rc || (rc = box->b->RecipInit(edges3)))
+    return rc;
+  if (k_count)
+    *k_count = box->b->cfg.ewald ? box->b->knew.K : 0;
+  return gb::OK;
+}
+int gb_update_recip_vec(gb_box *box) {
+  int rc = guard_box(box);
+  if (rc)
+    return rc;
+  return box->b->UpdateRecipVec();
+}
+int gb_set_box(gb_box *box, const double *edges3, const double *xyz,
+               const double *com) {
+  if (!edges3 || !xyz)
+    return gb::ERR_ARG;
+  int rc = guard_box(box);
+  if (rc)
+    return rc;
+  return box->b->SetBox(edges3, xyz, com);
+}
+int gb_box_edges(gb_box *box, double *edges3) {
+  if (!edges3)
+    return gb::ERR_ARG;
+  int rc = guard_box(box);
+  if (rc)
+    return rc;
+  for (int d = 0; d < 3; ++d)
+    edges3[d] = box->b->dev.L[d];
+  return gb::OK;
+}
+int gb_box_inter_coords(gb_box *box, const double *edges3, const double *xyz,
+                        double *inter, double *real) {
+  if (!edges3 || !xyz || !inter || !real)
+    return gb::ERR_ARG;
+  int rc = guard_box(box);
+  if (rc)
+    return rc;
+  return box->b->BoxInterAt(edges3, xyz, inter, real);
+}
+int gb_box_force_coords(gb_box *box, const double *xyz, double *inter,
+                        double *real, double *atom_force, double *mol_force) {
+  if (!xyz || !inter || !real)
+    return gb::ERR_ARG;
+  BOX_CALL(BoxForceAt(xyz, inter, real, atom_force, mol_force));
+}
+int gb_swap_self(gb_box *box, int32_t mol, double *self) {
+  if (!self)
+    return gb::ERR_ARG;
+  BOX_CALL(SwapSelf(mol, self));
+}
+int gb_swap_correction(gb_box *box, int32_t mol, const double *pos,
+                       double *corr) {
+  if (!pos || !corr)
+    return gb::ERR_ARG;
+  BOX_CALL(SwapCorrection(mol, pos, corr));
 }
 int gb_mol_reciprocal(gb_box *box, int32_t mol, const double *new_pos,
                       double *delta) {
@@ -295,12 +404,18 @@ int gb_set_coords(gb_box *box, const double *xyz, const double *com) {
 int gb_get_energy(gb_box *box, double *e5) {
   if (!e5)
     return gb::ERR_ARG;
-  BOX_CALL(GetEnergy(e5));
+  int rc = guard_box(box);
+  if (rc)
+    return rc;
+  return box->b->GetEnergy(e5);
 }
 int gb_set_energy(gb_box *box, const double *e5) {
   if (!e5)
     return gb::ERR_ARG;
-  BOX_CALL(SetEnergy(e5));
+  int rc = guard_box(box);
+  if (rc)
+    return rc;
+  return box->b->SetEnergy(e5);
 }
 
 int gb_mc_init(gb_box *box, const gb_mc_params *p) {
@@ -314,7 +429,7 @@ int gb_mc_init(gb_box *box, const gb_mc_params *p) {
 int gb_mc_run(gb_box *box, int64_t first_step, int64_t nsteps, int32_t *kind,
               int32_t *mol, int32_t *accepted, double *de) {
   int rc = guard(box);
-  if (rc)
+  if (rc || (rc = all_in_grid(*box->b)))
     return rc;
   return gb::mc_run(*box->b, first_step, nsteps, kind, mol, accepted, de);
 }
@@ -393,6 +508,9 @@ int gb_mc_run_batch(gb_box **boxes, int32_t nboxes, int64_t first_step,
   for (int i = 0; i < nboxes; ++i) {
     if (!boxes[i] || !boxes[i]->b)
       return gb::ERR_ARG;
+    int rc = all_in_grid(*boxes[i]->b);
+    if (rc)
+      return rc;
     v.push_back(boxes[i]->b);
   }
   return gb::mc_run_batch(v, first_step, nsteps);

@@ -66,6 +66,64 @@ __global__ void k_cell_sort_fill(DevBox b, const double *__restrict__ x,
   }
 }
 
+// CellList::RemoveMol (src/CellList.cpp:81-113): take molecule m's atoms out
+// of their cells (the cell's last slot fills each hole); an atom out of the
+// grid has atom_cell = -1.  One thread: a molecule has a few atoms.
+__global__ void k_cell_remove_mol(DevBox b, int m) {
+  for (int a = b.mstart[m]; a < b.mstart[m + 1]; ++a) {
+    int c0 = b.atom_cell[a];
+    if (c0 < 0)
+      continue;
+    int s0 = b.atom_slot[a];
+    int last = b.cell_count[c0] - 1;
+    if (s0 != last) {
+      size_t from = (size_t)c0 * b.cap + last, to = (size_t)c0 * b.cap + s0;
+      int moved = b.cell_atom[from];
+      b.cell_atom[to] = moved;
+      b.cell_pos[to] = b.cell_pos[from];
+      b.cell_meta[to] = b.cell_meta[from];
+      b.cell_fix[to] = b.cell_fix[from];
+      b.cell_qlo[to] = b.cell_qlo[from];
+      b.atom_slot[moved] = s0;
+    }
+    b.cell_count[c0] = last;
+    b.atom_cell[a] = -1;
+    b.atom_slot[a] = -1;
+  }
+}
+
+// CellList::AddMol (src/CellList.cpp:115-135): put molecule m's atoms, at
+// their current coordinates, into the cells PositionToCell gives.
+__global__ void k_cell_add_mol(DevBox b, int m) {
+  for (int a = b.mstart[m]; a < b.mstart[m + 1]; ++a) {
+    if (b.atom_cell[a] >= 0)
+      continue;
+    double x = b.x[a], y = b.y[a], z = b.z[a];
+    int c = position_to_cell_fast(b, x, y, z);
+    if (c < 0 || c >= b.ncell) {
+      atomicOr(b.err, DERR_BAD_INPUT);
+      return;
+    }
+    int s = b.cell_count[c];
+    if (s >= b.cap) {
+      atomicOr(b.err, DERR_CELL_OVERFLOW);
+      return;
+    }
+    b.cell_count[c] = s + 1;
+    cell_write_slot(b, c, s, a, x, y, z);
+  }
+}
+
+int launch_cell_remove_mol(Box &bx, int m) {
+  k_cell_remove_mol<<<1, 1, 0, bx.stream>>>(bx.dev, m);
+  return bx.CudaCheck(cudaGetLastError(), "cell remove");
+}
+
+int launch_cell_add_mol(Box &bx, int m) {
+  k_cell_add_mol<<<1, 1, 0, bx.stream>>>(bx.dev, m);
+  return bx.CudaCheck(cudaGetLastError(), "cell add");
+}
+
 int launch_grid_all(Box &bx, const DevBox &b) {
   cudaStream_t st = bx.stream;
   int rc = bx.CudaCheck(cudaMemsetAsync(b.cell_count, 0, b.ncell * 4, st),

@@ -144,16 +144,42 @@ int checkpoint_load(Box &b, const void *buf, int64_t bytes) {
                            (h.has_mc ? sizeof(McBlock) : 0));
   if (bytes < need)
     return b.Fail(ERR_ARG, "checkpoint truncated");
-  int rc = b.Sync();
-  if (rc)
-    return rc;
+  // Every check of the buffer comes before the first copy, so a rejected
+  // checkpoint leaves the box as it was.
   size_t N = d.n_atoms, M = d.n_mol, K = d.K, NC = (size_t)d.ncell * d.cap;
-  // slot counts must fit the grid before they are used on the device
-  std::vector<int32_t> cnt(d.ncell);
-  std::memcpy(cnt.data(), p + 8 * (3 * N + 3 * M + 5 + 2 * K), 4 * cnt.size());
+  const unsigned char *grid = p + 8 * (3 * N + 3 * M + 5 + 2 * K);
+  // slot counts must fit the grid, and the occupied slots must hold every
+  // atom id of this box exactly once
+  std::vector<int32_t> cnt(d.ncell), slot_atom(NC);
+  std::memcpy(cnt.data(), grid, 4 * cnt.size());
+  std::memcpy(slot_atom.data(), grid + 4 * cnt.size(), 4 * NC);
   for (int32_t c : cnt)
     if (c < 0 || c > d.cap)
       return b.Fail(ERR_ARG, "checkpoint cell counts out of range");
+  {
+    std::vector<char> seen(N, 0);
+    size_t placed = 0;
+    for (int c = 0; c < d.ncell; ++c)
+      for (int j = 0; j < cnt[c]; ++j) {
+        int32_t a = slot_atom[(size_t)c * d.cap + j];
+        if (a < 0 || a >= d.n_atoms || seen[a])
+          return b.Fail(ERR_ARG, "checkpoint cell slots out of range");
+        seen[a] = 1;
+        ++placed;
+      }
+    if (placed != N)
+      return b.Fail(ERR_ARG, "checkpoint cell slots do not hold every atom");
+  }
+  McBlock m;
+  if (h.has_mc) {
+    std::memcpy(&m, grid + 4 * (cnt.size() + NC), sizeof m);
+    // MT19937 position: `left` words remain of the current block of 624
+    if (m.mt_left < 0 || m.mt_left > 624 || m.mt_next + m.mt_left != 624)
+      return b.Fail(ERR_ARG, "checkpoint random-stream state out of range");
+  }
+  int rc = b.Sync();
+  if (rc)
+    return rc;
   struct Part {
     void *dst;
     size_t n;
@@ -168,15 +194,6 @@ int checkpoint_load(Box &b, const void *buf, int64_t bytes) {
       return rc;
     p += q.n;
   }
-  // slot atoms must be atom ids of this box
-  std::vector<int32_t> slot_atom(NC);
-  std::memcpy(slot_atom.data(), p - 4 * NC, 4 * NC);
-  for (int c = 0; c < d.ncell; ++c)
-    for (int j = 0; j < cnt[c]; ++j) {
-      int32_t a = slot_atom[(size_t)c * d.cap + j];
-      if (a < 0 || a >= d.n_atoms)
-        return b.Fail(ERR_ARG, "checkpoint cell slots out of range");
-    }
   if (K && ((rc = b.CudaCheck(cudaMemcpy(d.sumRnew, d.sumRref, 8 * K,
                                          cudaMemcpyDeviceToDevice),
                               "copy")) ||
@@ -190,8 +207,6 @@ int checkpoint_load(Box &b, const void *buf, int64_t bytes) {
     return rc;
   if (h.has_mc) {
     McState &s = *b.mc;
-    McBlock m;
-    std::memcpy(&m, p, sizeof m);
     s.stream->mt().Load(m.mt, m.mt_left, m.mt_next);
     s.next_step = h.next_step;
     if ((rc = b.CudaCheck(cudaMemcpy(s.d_set, &m.set, sizeof(Settings),

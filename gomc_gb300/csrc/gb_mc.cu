@@ -33,6 +33,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <system_error>
 #include <thread>
 
 namespace gb {
@@ -2296,13 +2297,24 @@ int mixed_complete(const std::vector<Box *> &boxes,
     const int nt = (int)std::min<size_t>(rec.size(), 4);
     std::vector<int> rcs(rec.size(), OK);
     std::atomic<size_t> next{0};
+    auto worker = [&] {
+      cudaError_t e = cudaSetDevice(dev);
+      for (size_t i; (i = next++) < rec.size();)
+        rcs[i] = e != cudaSuccess ? rec[i]->CudaCheck(e, "cudaSetDevice")
+                                  : recompute_fp64(*rec[i], *rec[i]->mc);
+    };
     std::vector<std::thread> th;
-    for (int k = 0; k < nt; ++k)
-      th.emplace_back([&] {
-        cudaSetDevice(dev);
-        for (size_t i; (i = next++) < rec.size();)
-          rcs[i] = recompute_fp64(*rec[i], *rec[i]->mc);
-      });
+    for (int k = 0; k < nt; ++k) {
+      // a thread that cannot be started leaves its share to the others and,
+      // with none started, to this thread
+      try {
+        th.emplace_back(worker);
+      } catch (const std::system_error &) {
+        break;
+      }
+    }
+    if (th.empty())
+      worker();
     for (auto &x : th)
       x.join();
     for (int r : rcs)

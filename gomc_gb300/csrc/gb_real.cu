@@ -250,7 +250,11 @@ int launch_box_virial(Box &bx, double *d_out6) {
 }
 
 int launch_box_inter(Box &bx, double *d_out2) {
-  DevBox &b = bx.dev;
+  return launch_box_inter_view(bx, bx.dev, d_out2);
+}
+
+// BoxInter on a view (its coordinates, cell grid and edges).
+int launch_box_inter_view(Box &bx, const DevBox &b, double *d_out2) {
   int tiles = b.ncell * NB27;
   int rc = bx.EnsureScratch((size_t)tiles * 2);
   if (rc)
@@ -408,11 +412,12 @@ int launch_single_mol_inter(Box &bx, int m, const double *d_lam4,
 }
 
 // ---------------------------------------------------------------------------
-// ParticleInter: unit u = trial * 27 + neighbour; atoms of molecule m are
-// treated as absent from the cell list (the molecule being grown).
+// ParticleInter: unit u = trial * 27 + neighbour, against every atom the
+// cell grid holds (a molecule being grown by CBMC is taken out of the grid
+// first, as in the reference).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(RT) k_particle_inter(DevBox b, const FF *__restrict__ pff,
-                                                       int m, int ka, double qa,
+                                                       int ka, double qa,
                                                        const double *__restrict__ trials,
                                                        double *part) {
   const FF &ff = *pff;
@@ -426,8 +431,6 @@ __global__ void __launch_bounds__(RT) k_particle_inter(DevBox b, const FF *__res
   for (int j = threadIdx.x; j < n2; j += RT) {
     size_t s = (size_t)c2 * b.cap + j;
     int mj = b.cell_meta[s];
-    if (meta_mol(mj) == m)
-      continue;
     double4_32a pj = b.cell_pos[s];
     double dx = min_image(px - pj.x, b.L[0], b.half[0]);
     double dy = min_image(py - pj.y, b.L[1], b.half[1]);
@@ -472,13 +475,13 @@ __global__ void k_reduce_trials(const double *__restrict__ part, int ntrials,
   out[3 * t + 2] = o;
 }
 
-int launch_particle_inter(Box &bx, int m, int kind, double charge,
+int launch_particle_inter(Box &bx, int kind, double charge,
                           const double *d_trials, int ntrials, double *d_out) {
   int units = ntrials * NB27;
   int rc = bx.EnsureScratch((size_t)units * 3);
   if (rc)
     return rc;
-  k_particle_inter<<<units, RT, 0, bx.stream>>>(bx.dev, bx.d_ff, m, kind, charge,
+  k_particle_inter<<<units, RT, 0, bx.stream>>>(bx.dev, bx.d_ff, kind, charge,
                                                 d_trials, bx.d_scratch);
   k_reduce_trials<<<(ntrials + 127) / 128, 128, 0, bx.stream>>>(bx.d_scratch,
                                                                ntrials, d_out);

@@ -260,18 +260,25 @@ __global__ void __launch_bounds__(KT) k_recip_sums_ff(DevBox b,
   }
 }
 
-static int recip_chunks(const Box &bx) {
-  int kb = (bx.dev.nrun + KT - 1) / KT;
+static int recip_chunks(const Box &bx, const DevBox &b) {
+  int kb = (b.nrun + KT - 1) / KT;
   int want = (4 * bx.sm_count + kb - 1) / kb;
   int nch = std::max(1, std::min(NCH_MAX, want));
-  int maxch = std::max(1, bx.dev.n_atoms / TA);
+  int maxch = std::max(1, b.n_atoms / TA);
   return std::min(nch, maxch);
 }
 
 int launch_recip_sums(Box &bx, const double *x, const double *y,
                       const double *z, double *sumR, double *sumI) {
-  DevBox &b = bx.dev;
-  int nch = recip_chunks(bx);
+  return launch_recip_sums_view(bx, bx.dev, x, y, z, sumR, sumI);
+}
+
+// The structure factor on a view: its k-vector set, its edges (the phases
+// are 2 pi n x / L) and the given coordinates.
+int launch_recip_sums_view(Box &bx, const DevBox &b, const double *x,
+                           const double *y, const double *z, double *sumR,
+                           double *sumI) {
+  int nch = recip_chunks(bx, b);
   int rc = bx.EnsureScratch((size_t)nch * b.K * 2);
   if (rc)
     return rc;
@@ -340,7 +347,13 @@ __global__ void k_sum_in_order(const double *__restrict__ part, int n,
 
 int launch_recip_energy(Box &bx, const double *sumR, const double *sumI,
                         double *d_out) {
-  DevBox &b = bx.dev;
+  return launch_recip_energy_view(bx, bx.dev, sumR, sumI, d_out);
+}
+
+// The energy of sums with the prefactors and k count of a view (the New
+// k-vector set for a trial volume).
+int launch_recip_energy_view(Box &bx, const DevBox &b, const double *sumR,
+                             const double *sumI, double *d_out) {
   int nb = (b.K + ET - 1) / ET;
   int rc = bx.EnsureScratch(nb);
   if (rc)

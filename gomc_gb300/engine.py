@@ -180,15 +180,24 @@ class Box:
                                                  _dp(out)))
         return out
 
-    def particle_inter(self, m: int, kind: int, charge: float, trials):
+    def particle_inter(self, m: int, part: int, trials):
+        """ParticleInter of atom `part` of molecule m at each trial position
+        against the atoms in the cell list: (overlap, LJ, real) arrays."""
         t = np.ascontiguousarray(trials, dtype=np.float64).reshape(-1, 3)
         n = t.shape[0]
         en, re = np.empty(n), np.empty(n)
         ov = np.empty(n, dtype=np.int32)
-        self._chk(lib().gb_particle_inter(self.h, int(m), int(kind),
-                                          float(charge), _dp(t), n, _dp(en),
-                                          _dp(re), _ip(ov)))
+        self._chk(lib().gb_particle_inter(self.h, int(m), int(part), _dp(t),
+                                          n, _dp(en), _dp(re), _ip(ov)))
         return ov.astype(bool), en, re
+
+    def cell_remove_mol(self, m: int) -> None:
+        """CellList::RemoveMol: take molecule m out of the cell list."""
+        self._chk(lib().gb_cell_remove_mol(self.h, int(m)))
+
+    def cell_add_mol(self, m: int) -> None:
+        """CellList::AddMol: put molecule m back at its coordinates."""
+        self._chk(lib().gb_cell_add_mol(self.h, int(m)))
 
     def box_force(self):
         a, b = C.c_double(), C.c_double()
@@ -226,12 +235,84 @@ class Box:
     def box_reciprocal_setup(self) -> None:
         self._chk(lib().gb_box_reciprocal_setup(self.h))
 
-    def box_reciprocal_sums(self) -> None:
-        self._chk(lib().gb_box_reciprocal_sums(self.h))
+    def box_reciprocal_sums(self, coords=None) -> None:
+        """BoxReciprocalSums: New sums of the box's coordinates or of
+        `coords` [n_atoms, 3], with the current k-vector set."""
+        if coords is None:
+            self._chk(lib().gb_box_reciprocal_sums(self.h))
+            return
+        x = np.ascontiguousarray(coords, dtype=np.float64).reshape(-1, 3)
+        self._chk(lib().gb_box_reciprocal_sums_coords(self.h, _dp(x)))
 
-    def box_reciprocal(self, use_ref: bool = False) -> float:
+    def box_reciprocal(self, is_new_volume: bool = False) -> float:
+        """BoxReciprocal: energy of the New sums with the New k-vector set's
+        prefactors (is_new_volume) or the current set's."""
         e = C.c_double()
-        self._chk(lib().gb_box_reciprocal(self.h, int(use_ref), C.byref(e)))
+        self._chk(lib().gb_box_reciprocal(self.h, int(is_new_volume),
+                                          C.byref(e)))
+        return e.value
+
+    def recip_init(self, edges) -> int:
+        """RecipInit for trial edges: builds the New k-vector set; returns
+        its size."""
+        L = np.ascontiguousarray(edges, dtype=np.float64).reshape(3)
+        k = C.c_int32()
+        self._chk(lib().gb_recip_init(self.h, _dp(L), C.byref(k)))
+        return k.value
+
+    def box_reciprocal_setup_coords(self, coords) -> None:
+        """BoxReciprocalSetup(box, molCoords): New sums of `coords` with the
+        New k-vector set."""
+        x = np.ascontiguousarray(coords, dtype=np.float64).reshape(-1, 3)
+        self._chk(lib().gb_box_reciprocal_setup_coords(self.h, _dp(x)))
+
+    def update_recip_vec(self) -> None:
+        self._chk(lib().gb_update_recip_vec(self.h))
+
+    def edges(self) -> np.ndarray:
+        L = np.empty(3)
+        self._chk(lib().gb_box_edges(self.h, _dp(L)))
+        return L
+
+    def set_box(self, edges, coords, com=None) -> None:
+        """New box edges with coordinates (and centres): grid, k-vectors,
+        structure factors and running energies follow."""
+        L = np.ascontiguousarray(edges, dtype=np.float64).reshape(3)
+        x = np.ascontiguousarray(coords, dtype=np.float64).reshape(-1, 3)
+        c = None if com is None else np.ascontiguousarray(com, np.float64)
+        self._chk(lib().gb_set_box(self.h, _dp(L), _dp(x),
+                                   None if c is None else _dp(c)))
+
+    def box_inter_coords(self, edges, coords):
+        """BoxInter of `coords` at `edges`: (LJ, real)."""
+        L = np.ascontiguousarray(edges, dtype=np.float64).reshape(3)
+        x = np.ascontiguousarray(coords, dtype=np.float64).reshape(-1, 3)
+        a, b = C.c_double(), C.c_double()
+        self._chk(lib().gb_box_inter_coords(self.h, _dp(L), _dp(x),
+                                            C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def box_force_coords(self, coords):
+        """BoxForce of `coords` at the box's edges: (atom forces, molecule
+        forces, LJ, real)."""
+        x = np.ascontiguousarray(coords, dtype=np.float64).reshape(-1, 3)
+        a, b = C.c_double(), C.c_double()
+        aF = np.empty((self.n_atoms, 3))
+        mF = np.empty((self.n_mol, 3))
+        self._chk(lib().gb_box_force_coords(self.h, _dp(x), C.byref(a),
+                                            C.byref(b), _dp(aF), _dp(mF)))
+        return aF, mF, a.value, b.value
+
+    def swap_self(self, m: int) -> float:
+        e = C.c_double()
+        self._chk(lib().gb_swap_self(self.h, int(m), C.byref(e)))
+        return e.value
+
+    def swap_correction(self, m: int, pos) -> float:
+        p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        e = C.c_double()
+        self._chk(lib().gb_swap_correction(self.h, int(m), _dp(p),
+                                           C.byref(e)))
         return e.value
 
     def mol_reciprocal(self, m: int, new_pos) -> float:
@@ -435,10 +516,9 @@ class CalculateEnergy:
                        lambdaNewCoulomb])
         return (dict(inter=o[0], real=o[1]), dict(inter=o[2], real=o[3]))
 
-    def ParticleInter(self, trialPos, partIndex_kind: int, charge: float,
-                      molIndex: int):
-        return self.box.particle_inter(molIndex, partIndex_kind, charge,
-                                       trialPos)
+    def ParticleInter(self, trialPos, partIndex: int, molIndex: int):
+        """Returns (overlap, en, real) per trial position."""
+        return self.box.particle_inter(molIndex, partIndex, trialPos)
 
     def BoxForce(self):
         return self.box.box_force()
@@ -459,11 +539,23 @@ class Ewald:
     def BoxReciprocalSetup(self):
         self.box.box_reciprocal_setup()
 
-    def BoxReciprocalSums(self):
-        self.box.box_reciprocal_sums()
+    def BoxReciprocalSums(self, molCoords=None):
+        self.box.box_reciprocal_sums(molCoords)
 
     def BoxReciprocal(self, isNewVolume: bool = False) -> float:
-        return self.box.box_reciprocal(use_ref=False)
+        return self.box.box_reciprocal(is_new_volume=isNewVolume)
+
+    def RecipInit(self, boxAxes) -> int:
+        return self.box.recip_init(boxAxes)
+
+    def UpdateRecipVec(self):
+        self.box.update_recip_vec()
+
+    def SwapSelf(self, molIndex: int) -> float:
+        return self.box.swap_self(molIndex)
+
+    def SwapCorrection(self, molCoords, molIndex: int) -> float:
+        return self.box.swap_correction(molIndex, molCoords)
 
     def MolReciprocal(self, molCoords, molIndex: int) -> float:
         return self.box.mol_reciprocal(molIndex, molCoords)
@@ -498,6 +590,12 @@ class CellList:
 
     def GridAll(self):
         self.box.grid_all()
+
+    def RemoveMol(self, molIndex: int):
+        self.box.cell_remove_mol(molIndex)
+
+    def AddMol(self, molIndex: int):
+        self.box.cell_add_mol(molIndex)
 
     def CellMembership(self):
         return self.box.cell_membership()

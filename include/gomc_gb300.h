@@ -102,15 +102,31 @@ int gb_virial(gb_box *box, double *out16);
  * Coulomb; out4 = old inter, old real, new inter, new real (K). */
 int gb_single_molecule_inter(gb_box *box, int32_t mol, const double *lambdas4,
                              double *out4);
-/* ParticleInter (src/CalculateEnergy.cpp:727-785): one atom of kind/charge
- * at each of ntrials positions; atoms of molecule `mol` are excluded. */
-int gb_particle_inter(gb_box *box, int32_t mol, int32_t kind, double charge,
+/* ParticleInter (src/CalculateEnergy.cpp:727-785): atom `part` of molecule
+ * `mol` (its kind and charge) at each of ntrials positions (1..256), LJ and
+ * real-space energies and the RcutLow overlap flag against every atom in the
+ * cell list.  As in the reference nothing is excluded: a CBMC caller takes
+ * the molecule out of the cell list first (gb_cell_remove_mol, as
+ * MoleculeTransfer::Transform does, src/moves/MoleculeTransfer.h:100-106). */
+int gb_particle_inter(gb_box *box, int32_t mol, int32_t part,
                       const double *trials, int32_t ntrials, double *en,
                       double *real, int32_t *overlap);
 /* BoxForce (src/CalculateEnergy.cpp:268-406): energies plus atom and
  * molecule forces (host arrays may be NULL). */
 int gb_box_force(gb_box *box, double *inter, double *real, double *atom_force,
                  double *mol_force);
+/* BoxForce(potential, coords, ...) of the given coordinates xyz [n_atoms * 3]
+ * at the box's edges, as MultiParticle::CalcEn calls it on its trial
+ * coordinates (src/moves/MultiParticle.h:424-428); the box's own state is
+ * untouched. */
+int gb_box_force_coords(gb_box *box, const double *xyz, double *inter,
+                        double *real, double *atom_force, double *mol_force);
+/* BoxInter(potential, coords, boxAxes, box) (src/CalculateEnergy.cpp:
+ * 157-266) of coordinates xyz [n_atoms * 3] at edges edges3[3], on a cell
+ * grid of those edges built for the call (VolumeTransfer::CalcEn,
+ * src/moves/VolumeTransfer.h:150-178); the box's own state is untouched. */
+int gb_box_inter_coords(gb_box *box, const double *edges3, const double *xyz,
+                        double *inter, double *real);
 /* CalculateTorque (src/CalculateEnergy.cpp:1365-1406) from the forces of the
  * last gb_box_force and gb_box_force_reciprocal calls. */
 int gb_calculate_torque(gb_box *box, double *mol_torque);
@@ -126,9 +142,31 @@ int gb_get_sums_new(gb_box *box, double *sum_r, double *sum_i);
 int gb_box_reciprocal_setup(gb_box *box);
 /* BoxReciprocalSums (src/Ewald.cpp:281-361) for the current coordinates */
 int gb_box_reciprocal_sums(gb_box *box);
-/* BoxReciprocal (src/Ewald.cpp:375-406) of the New (use_ref = 0) or Ref
- * (use_ref = 1) sums */
-int gb_box_reciprocal(gb_box *box, int32_t use_ref, double *energy);
+/* BoxReciprocalSums(box, molCoords) (src/Ewald.cpp:281-361): the New sums of
+ * the given coordinates xyz [n_atoms * 3] with the current (Ref) k-vector
+ * set, as MultiParticle::CalcEn calls it on its trial coordinates
+ * (src/moves/MultiParticle.h:424-431). */
+int gb_box_reciprocal_sums_coords(gb_box *box, const double *xyz);
+/* BoxReciprocal(box, isNewVolume) (src/Ewald.cpp:375-406): the energy of the
+ * New sums with the prefactors of the New k-vector set (is_new_volume = 1,
+ * after gb_recip_init for trial edges) or of the current Ref set (0). */
+int gb_box_reciprocal(gb_box *box, int32_t is_new_volume, double *energy);
+/* RecipInit(box, boxAxes) (src/Ewald.cpp:835-903) for trial edges
+ * edges3[3]: builds the New k-vector set (imageSize, kx/ky/kz, hsqr,
+ * prefact); k_count (may be NULL) receives its size.  The current set is
+ * untouched. */
+int gb_recip_init(gb_box *box, const double *edges3, int32_t *k_count);
+/* BoxReciprocalSetup(box, molCoords) (src/Ewald.cpp:193-274): the New sums
+ * of coordinates xyz [n_atoms * 3] with the New k-vector set, the coordinates
+ * lying inside the edges that set was built for (VolumeTransfer::CalcEn,
+ * src/moves/VolumeTransfer.h:160-176). */
+int gb_box_reciprocal_setup_coords(gb_box *box, const double *xyz);
+/* UpdateRecipVec (src/Ewald.cpp:1462-1487): swap the New and Ref k-vector
+ * sets.  Until gb_set_box gives the box the edges of its new Ref set, only
+ * gb_set_box, gb_recip_init, gb_box_reciprocal, gb_box_reciprocal_setup_coords,
+ * gb_box_inter_coords, gb_box_edges and the energy accessors are valid
+ * (others return GB_ERR_STATE).  Not for a box with a Monte Carlo loop. */
+int gb_update_recip_vec(gb_box *box);
 /* MolReciprocal (src/Ewald.cpp:409-473): fills the New sums, returns the
  * energy difference against the running reciprocal energy */
 int gb_mol_reciprocal(gb_box *box, int32_t mol, const double *new_pos,
@@ -142,18 +180,52 @@ int gb_update_recip(gb_box *box);   /* UpdateRecip, src/Ewald.cpp:1420-1434 */
 int gb_copy_recip(gb_box *box);     /* CopyRecip, src/Ewald.cpp:1441-1460 */
 int gb_box_self(gb_box *box, double *self); /* BoxSelf :1125-1163 */
 int gb_mol_correction(gb_box *box, int32_t mol, double *corr); /* :1056-1085 */
+/* SwapSelf (src/Ewald.cpp:1375-1391): self energy of molecule `mol`;
+ * SwapCorrection (src/Ewald.cpp:1311-1333): its intramolecular correction at
+ * positions pos [n_atoms_of_mol * 3] in this box (MoleculeTransfer::CalcEn,
+ * src/moves/MoleculeTransfer.h:112-128). */
+int gb_swap_self(gb_box *box, int32_t mol, double *self);
+int gb_swap_correction(gb_box *box, int32_t mol, const double *pos,
+                       double *corr);
 /* BoxForceReciprocal (src/Ewald.cpp:1496-1596) from the New sums */
 int gb_box_force_reciprocal(gb_box *box, double *atom_force_rec,
                             double *mol_force_rec);
 
 /* ---- CellList (src/CellList.h:22-86) ---- */
 int gb_grid_all(gb_box *box);  /* GridAll, src/CellList.cpp:220-237 */
+/* RemoveMol / AddMol (src/CellList.cpp:81-135): take molecule `mol` out of
+ * the cell list, or put it back at its current coordinates.  While any
+ * molecule is out, the Monte Carlo and checkpoint calls return GB_ERR_STATE;
+ * gb_grid_all puts every molecule back. */
+int gb_cell_remove_mol(gb_box *box, int32_t mol);
+int gb_cell_add_mol(gb_box *box, int32_t mol);
 /* cell index of every atom (GetCellListNeighbor's mapParticleToCell,
  * src/CellList.cpp:258-285) and the cells per edge */
 int gb_cell_membership(gb_box *box, int32_t *cell_of_atom, int32_t *edge3);
 
 /* ---- state ---- */
+int gb_box_edges(gb_box *box, double *edges3);  /* BoxDimensions axes */
+/* New box edges edges3[3] with coordinates xyz [n_atoms * 3] (inside them)
+ * and centres com [n_mol * 3] (may be NULL: computed as COM::CalcCOM does):
+ * what VolumeTransfer::Accept leaves after an accepted move
+ * (src/moves/VolumeTransfer.h:241-270: coordinates, BoxDimensions,
+ * UpdateRecip, UpdateRecipVec), with the derived state rebuilt as
+ * System::Init does: CellList::ResizeGrid + GridAll (src/CellList.cpp:
+ * 138-237), the k-vector set of the edges (the one gb_recip_init built for
+ * them, else a new one), the structure factors and the running energies.
+ * Not for a box with a Monte Carlo loop (GB_ERR_STATE). */
+int gb_set_box(gb_box *box, const double *edges3, const double *xyz,
+               const double *com);
 int gb_get_coords(gb_box *box, double *xyz, double *com);
+/* Replace the coordinates [n_atoms * 3] (inside the box) and molecule
+ * centres [n_mol * 3] and bring every derived quantity in line, as
+ * System::Init does after reading coordinates (src/System.cpp:67-100):
+ * CellList::GridAll, the Ewald structure factors (BoxReciprocalSetup +
+ * SetRecipRef) and the running energies (SystemTotal).  com may be NULL: the
+ * centres are then computed as COM::CalcCOM does (src/COM.h:47-68), which
+ * re-wraps each molecule's atoms.  The Monte Carlo state (step, move
+ * settings) is kept; the next gb_mc_run scores moves against the new
+ * state. */
 int gb_set_coords(gb_box *box, const double *xyz, const double *com);
 /* running energies inter, real, recip, self, correction (SystemPotential) */
 int gb_get_energy(gb_box *box, double *e5);
@@ -340,7 +412,10 @@ const char *gb_server_error(const gb_server *srv);
  * fixed 8 KiB device array inside this library, one FP64 partial per 256
  * k-vectors, hence the limit on K (larger K: GB_ERR_CAPACITY, nothing
  * launched).  The first call on a device looks up that array's address with
- * the device current; make it before any stream capture.  Calls that overlap
+ * the device current and keeps it for the life of the process; make it
+ * before any stream capture, and do not call this entry point again on a
+ * device after cudaDeviceReset there (the kept address belonged to the
+ * context the reset destroyed).  Calls that overlap
  * in time on one device share the array and race: serialise them.  The sum
  * is taken in the order of gb_box_reciprocal.  Errors: GB_ERR_ARG (null
  * pointer, K < 0), GB_ERR_CAPACITY, GB_ERR_CUDA; gb_last_error(NULL) gives

@@ -761,18 +761,23 @@ void ora_single_molecule_inter(const ora_sys *s, int m, const double *lam,
   out[3] = tempREnNew;
 }
 
-/* ParticleInter, src/CalculateEnergy.cpp:727-785, one trial */
-int ora_particle_inter(const ora_sys *s, int m, int kindI, double qI,
-                       const double *t, double *en, double *real) {
+/* ParticleInter, src/CalculateEnergy.cpp:727-785, one trial: atom `part` of
+ * molecule m (its kind and charge) at position t against every atom the cell
+ * list holds.  Like the reference it excludes nothing: callers that build a
+ * molecule by CBMC take it out of the cell list first (ora_cell_remove_mol,
+ * as MoleculeTransfer::Transform does, src/moves/MoleculeTransfer.h:100-106). */
+int ora_particle_inter(const ora_sys *s, int m, int part, const double *t,
+                       double *en, double *real) {
   int overlap = 0;
+  int a = s->mstart[m] + part;
+  int kindI = s->kind[a];
+  double qI = s->q[a];
   int *nb = (int *)malloc(sizeof(int) * (s->n_atoms + 1));
   int cell = position_to_cell(s, t[0], t[1], t[2]);
   int nn = gather_neighbors(s, cell, nb);
   double tempLJ = 0.0, tempReal = 0.0;
   for (int i = 0; i < nn; i++) {
     int j = nb[i];
-    if (s->mol[j] == m)
-      continue; /* the molecule being built is not in the list */
     double distSq = dist_sq(s, t[0], t[1], t[2], s->x[j], s->y[j], s->z[j], 0);
     if (s->rcutSq > distSq) {
       if (distSq < s->rcutLowSq)
@@ -786,10 +791,14 @@ int ora_particle_inter(const ora_sys *s, int m, int kindI, double qI,
     }
   }
   free(nb);
-  *en = tempLJ;
-  *real = tempReal;
+  *en = 0.0 + tempLJ;
+  *real = 0.0 + tempReal;
   return overlap;
 }
+
+/* CellList::RemoveMol / AddMol, src/CellList.cpp:81-135 */
+void ora_cell_remove_mol(ora_sys *s, int m) { remove_mol(s, m); }
+void ora_cell_add_mol(ora_sys *s, int m) { add_mol(s, m); }
 
 /* MolReciprocal, src/Ewald.cpp:409-473 (CPU branch) */
 double ora_mol_reciprocal(ora_sys *s, const double *newpos, int m) {

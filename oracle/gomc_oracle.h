@@ -74,11 +74,14 @@ void ora_virial(ora_sys *s, double *out16);
  * first (as Translate::CalcEn does).  Returns overlap. */
 int ora_molecule_inter(ora_sys *s, int m, const double *newpos, double *dlj,
                        double *dreal);
-/* CalculateEnergy::ParticleInter for one trial position of atom kind/charge
- * of molecule m (src/CalculateEnergy.cpp:727-785). */
-int ora_particle_inter(const ora_sys *s, int m, int atom_kind,
-                       double atom_charge, const double *trial, double *en,
-                       double *real);
+/* CalculateEnergy::ParticleInter for one trial position of atom `part` of
+ * molecule m against the atoms in the cell list (src/CalculateEnergy.cpp:
+ * 727-785); nothing is excluded, as in the reference. */
+int ora_particle_inter(const ora_sys *s, int m, int part, const double *trial,
+                       double *en, double *real);
+/* CellList::RemoveMol / AddMol (src/CellList.cpp:81-135) */
+void ora_cell_remove_mol(ora_sys *s, int m);
+void ora_cell_add_mol(ora_sys *s, int m);
 double ora_mol_reciprocal(ora_sys *s, const double *newpos, int m);
 double ora_swap_dest_recip(ora_sys *s, const double *newpos, int m);
 double ora_swap_source_recip(ora_sys *s, const double *oldpos, int m);

@@ -63,7 +63,9 @@ def lib():
             "ora_virial": (None, [P, dp]),
             "ora_single_molecule_inter": (None, [P, I, dp,
                                                  C.POINTER(SoftCore), dp]),
-            "ora_particle_inter": (I, [P, I, I, D, dp, dp, dp]),
+            "ora_particle_inter": (I, [P, I, I, dp, dp, dp]),
+            "ora_cell_remove_mol": (None, [P, I]),
+            "ora_cell_add_mol": (None, [P, I]),
             "ora_mol_reciprocal": (D, [P, dp, I]),
             "ora_swap_dest_recip": (D, [P, dp, I]),
             "ora_swap_source_recip": (D, [P, dp, I]),
@@ -234,12 +236,20 @@ class OracleBox:
                                         _dp(out))
         return out
 
-    def particle_inter(self, m: int, kind: int, charge: float, trial):
+    def particle_inter(self, m: int, part: int, trial):
+        """ParticleInter of atom `part` of molecule m at one trial position
+        against the atoms in the cell list: (overlap, LJ, real)."""
         t = np.ascontiguousarray(trial, dtype=np.float64)
         a, b = C.c_double(), C.c_double()
-        ov = lib().ora_particle_inter(self.h, int(m), int(kind), float(charge),
-                                      _dp(t), C.byref(a), C.byref(b))
+        ov = lib().ora_particle_inter(self.h, int(m), int(part), _dp(t),
+                                      C.byref(a), C.byref(b))
         return bool(ov), a.value, b.value
+
+    def cell_remove_mol(self, m: int) -> None:
+        lib().ora_cell_remove_mol(self.h, int(m))
+
+    def cell_add_mol(self, m: int) -> None:
+        lib().ora_cell_add_mol(self.h, int(m))
 
     def mol_reciprocal(self, m: int, newpos) -> float:
         p = np.ascontiguousarray(newpos, dtype=np.float64)

@@ -13,6 +13,11 @@
 //     src/Ewald.cpp:409-531,657-710),
 //   - BoxForce / BoxForceReciprocal / CalculateTorque outputs when the
 //     fixture enables the MultiParticle move,
+//   - ParticleInter trial energies (src/CalculateEnergy.cpp:727-785) with
+//     and without the molecule in the cell list,
+//   - trial-volume energies (VolumeTransfer's energy calls: RecipInit,
+//     BoxReciprocalSetup, BoxInter at new axes) and the state after one
+//     accepted volume change,
 //   - a per-step trace of the reference Monte Carlo loop
 //     (src/Simulation.cpp:94-96 without output, src/System.cpp:262-302).
 // It is test infrastructure: it runs only in the build container.
@@ -124,14 +129,18 @@ int main(int argc, char **argv) {
   if (argc < 4) {
     fprintf(stderr,
             "usage: ref_probe in.conf outdir nsteps [proposals.txt|-] "
-            "[lambdas.txt]\n");
+            "[lambdas.txt|-] [particles.txt|-] [volumes.txt]\n");
     return 1;
   }
   std::string outdir = argv[2];
   long nsteps = atol(argv[3]);
   const char *propFile =
       argc > 4 && std::string(argv[4]) != "-" ? argv[4] : nullptr;
-  const char *lamFile = argc > 5 ? argv[5] : nullptr;
+  const char *lamFile =
+      argc > 5 && std::string(argv[5]) != "-" ? argv[5] : nullptr;
+  const char *partFile =
+      argc > 6 && std::string(argv[6]) != "-" ? argv[6] : nullptr;
+  const char *volFile = argc > 7 ? argv[7] : nullptr;
 
   Simulation sim(argv[1]);
   System &sys = *sim.system;
@@ -296,6 +305,115 @@ int main(int argc, char **argv) {
               lov, lnv, loc, lnc, scc, eo.inter, eo.real, en.inter, en.real);
     }
     fclose(f);
+  }
+
+  // ---- ParticleInter, the CBMC first-atom trial energies ------------------
+  // particles.txt: n, then n lines "mol part remove ntrials x y z ...".
+  // With remove = 1 the molecule leaves the cell list around the call, as
+  // MoleculeTransfer::Transform does before DCSingle::BuildOld/BuildNew
+  // (src/moves/MoleculeTransfer.h:100-106, src/cbmc/DCSingle.cpp:23-90);
+  // with remove = 0 the call sees the cell list as it stands.
+  if (partFile) {
+    std::ifstream in(partFile);
+    int n = 0;
+    in >> n;
+    FILE *f = open_out(outdir, "particles_out.txt");
+    for (int i = 0; i < n; ++i) {
+      uint m, part, nt;
+      int remove;
+      in >> m >> part >> remove >> nt;
+      XYZArray pos(nt);
+      for (uint t = 0; t < nt; ++t) in >> pos.x[t] >> pos.y[t] >> pos.z[t];
+      std::vector<double> en(nt, 0.0), re(nt, 0.0);
+      std::unique_ptr<bool[]> ov(new bool[nt]);
+      for (uint t = 0; t < nt; ++t) ov[t] = false;
+      if (remove) sys.cellList.RemoveMol(m, box, sys.coordinates);
+      sys.calcEnergy.ParticleInter(en.data(), re.data(), pos, ov.get(), part,
+                                   m, box, nt);
+      if (remove) sys.cellList.AddMol(m, box, sys.coordinates);
+      fprintf(f, "%u %u %d %u", m, part, remove, nt);
+      for (uint t = 0; t < nt; ++t)
+        fprintf(f, " %.17g %.17g %d", en[t], re[t], (int)ov[t]);
+      fprintf(f, "\n");
+    }
+    fclose(f);
+  }
+
+  // ---- trial volumes (the NPT branch of VolumeTransfer) -------------------
+  // volumes.txt: n, then n volume changes (A^3).  Each is evaluated from the
+  // initial state as VolumeTransfer::Transform / CalcEn do
+  // (src/moves/VolumeTransfer.h:96-190): ShiftVolume, TranslateOneBox,
+  // GridAll on the new axes, RecipInit + BoxReciprocalSetup on the new
+  // coordinates, BoxInter and BoxReciprocal(box, true).  The last one is
+  // then accepted (new coordinates, centres and axes, UpdateRecip,
+  // UpdateRecipVec) and the state recomputed as System::Init does
+  // (GridAll, UpdateVectorsAndRecipTerms, SystemTotal).
+  if (volFile) {
+    std::ifstream in(volFile);
+    int n = 0;
+    in >> n;
+    FILE *f = open_out(outdir, "volume_out.txt");
+    const uint N = sys.coordinates.Count();
+    XYZArray scratch(N);
+    COM newCOM(sys.boxDimRef, scratch, sys.molLookupRef, stat.mol);
+    newCOM.Init(stat.mol.count);
+    Coordinates newPos(sys.boxDimRef, newCOM, sys.molLookupRef, sys.prng,
+                       stat.mol);
+    newPos.Init(N);
+    BoxDimensions newDim;
+    for (int i = 0; i < n; ++i) {
+      double delta;
+      in >> delta;
+      newDim = sys.boxDimRef;
+      sys.coordinates.CopyRange(newPos, 0, 0, N);
+      sys.com.CopyRange(newCOM, 0, 0, sys.com.Count());
+      XYZ scale;
+      sys.boxDimRef.ShiftVolume(newDim, scale, box, delta);
+      sys.coordinates.TranslateOneBox(newPos, newCOM, sys.com, newDim, box,
+                                      scale);
+      sys.cellList.GridAll(newDim, newPos, sys.molLookupRef);
+      SystemPotential pNew = sys.potential;
+      double recip = 0.0;
+      uint knew = 0;
+      if (stat.forcefield.ewald) {
+        ew->RecipInit(box, newDim);
+        ew->BoxReciprocalSetup(box, newPos);
+      }
+      pNew = sys.calcEnergy.BoxInter(pNew, newPos, newDim, box);
+      if (stat.forcefield.ewald) {
+        recip = ew->BoxReciprocal(box, true);
+        knew = ew->imageSize[box];
+      }
+      XYZ ax = newDim.GetAxis(box);
+      fprintf(f, "%.17g %.17g %.17g %.17g %u %.17g %.17g %.17g\n", delta,
+              ax.x, ax.y, ax.z, knew, pNew.boxEnergy[box].inter,
+              pNew.boxEnergy[box].real, recip);
+      char name[64];
+      snprintf(name, sizeof name, "volume_pos_%d.txt", i);
+      dump_coords(outdir, name, newPos);
+      snprintf(name, sizeof name, "volume_com_%d.txt", i);
+      dump_coords(outdir, name, newCOM);
+    }
+    fclose(f);
+    if (n > 0) {
+      // accept the last trial volume
+      newPos.CopyRange(sys.coordinates, 0, 0, N);
+      newCOM.CopyRange(sys.com, 0, 0, sys.com.Count());
+      sys.boxDimRef = newDim;
+      if (stat.forcefield.ewald) {
+        ew->UpdateRecip(box);
+        ew->UpdateRecipVec(box);
+      }
+      sys.cellList.GridAll(sys.boxDimRef, sys.coordinates, sys.molLookupRef);
+      if (stat.forcefield.ewald)
+        ew->UpdateVectorsAndRecipTerms(false);
+      SystemPotential pot = sys.calcEnergy.SystemTotal();
+      f = open_out(outdir, "volume_accept.txt");
+      dump_energy(f, "box0", pot.boxEnergy[box]);
+      if (stat.forcefield.ewald)
+        fprintf(f, "imageSize %u\n", ew->imageSizeRef[box]);
+      fclose(f);
+    }
   }
 
   // ---- Monte Carlo trace ---------------------------------------------------

@@ -1,9 +1,9 @@
 """Generate the golden vectors that pin the oracle and the GPU path.
 
-Run in a container that has the reference sources (read-only) at
-``/root/reference``::
+Run in a container that has the reference sources (read-only), given by
+``--ref`` or the ``GOMC_REFERENCE`` environment variable::
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    GOMC_REFERENCE=/root/reference python tests/golden/make_golden.py [names]
 
 It builds the reference CPU path from its own sources with ``oracle/ref.mk``
 (outputs in ``oracle/_ref/``), writes seeded fixtures in the reference's input
@@ -79,6 +79,22 @@ FIXTURES = {
                             adj_steps=10, dis_freq=1.0, rot_freq=0.0,
                             random_seed=3232),
                   1500, 32),
+    # the 8,000-water system the benchmark runs (same generator seed): 62.1 A,
+    # Rcut 10, Ewald tolerance 1e-5 (K = 24,658), 6 cells per axis; moves
+    # adjusted every 1,000 steps like the benchmark's chain
+    "c1_water": (lambda: spce_water_box(8000, 62.1, seed=20260),
+                 SimConfig(temperature=298.0, rcut=10.0, tolerance=1e-5,
+                           run_steps=2000, eq_steps=1000, adj_steps=1000,
+                           dis_freq=0.5, rot_freq=0.5, random_seed=20260),
+                 2000, 64),
+    # the same system with the MultiParticle move in the mix (BoxForce,
+    # BoxForceReciprocal and the full structure factor at 8,000 waters)
+    "c1_water_mp": (lambda: spce_water_box(8000, 62.1, seed=20261),
+                    SimConfig(temperature=298.0, rcut=10.0, tolerance=1e-5,
+                              run_steps=60, eq_steps=30, adj_steps=10,
+                              dis_freq=0.45, rot_freq=0.45,
+                              multi_particle_freq=0.1, random_seed=20261),
+                    60, 8),
 }
 
 
@@ -256,6 +272,108 @@ def make_virial(probe: str, name: str) -> None:
     print("wrote vir_" + name)
 
 
+def make_particles(probe: str, name: str, ncase: int = 24,
+                   ntrials: int = 10) -> None:
+    """CalculateEnergy::ParticleInter (src/CalculateEnergy.cpp:727-785), the
+    CBMC first-atom trial energies, on the fixture's initial state ->
+    pi_<name>.npz.  Two thirds of the cases take the molecule out of the cell
+    list around the call, as MoleculeTransfer does before DCSingle builds the
+    old and new trial sets (src/moves/MoleculeTransfer.h:100-106,
+    src/cbmc/DCSingle.cpp:23-90), with trial 0 at the atom's own position
+    (DCSingle::BuildOld); the rest call it on the full cell list at random
+    positions.  Cases run in order in one process, so each removal and
+    re-insertion relinks the molecule as the reference does."""
+    builder, cfg, _, _ = FIXTURES[name]
+    sysm = builder()
+    z = np.load(os.path.join(HERE, name + ".npz"))
+    c0 = z["coords_init"].reshape(-1, 3)
+    rng = np.random.default_rng(3000 + len(name))
+    ms = sysm.mol_start
+    rows = []
+    for i in range(ncase):
+        m = int(rng.integers(0, sysm.n_mol))
+        na = int(ms[m + 1] - ms[m])
+        part = int(rng.integers(0, na))
+        remove = int(i % 3 != 2)
+        t = rng.uniform(0.0, 1.0, size=(ntrials, 3)) * sysm.box
+        if remove:
+            t[0] = c0[ms[m] + part]
+        rows.append((m, part, remove, t))
+    with tempfile.TemporaryDirectory() as d:
+        write_reference_inputs(d, sysm, cfg)
+        with open(os.path.join(d, "part.txt"), "w") as f:
+            f.write("%d\n" % ncase)
+            for m, part, remove, t in rows:
+                f.write("%d %d %d %d %s\n" % (m, part, remove, ntrials,
+                                             " ".join("%.17g" % v
+                                                      for v in t.ravel())))
+        out = os.path.join(d, "out")
+        os.makedirs(out)
+        subprocess.check_call([probe, "in.conf", out, "0", "-", "-",
+                               "part.txt"], cwd=d, stdout=subprocess.DEVNULL)
+        r = np.loadtxt(os.path.join(out, "particles_out.txt")).reshape(ncase,
+                                                                       -1)
+    res = r[:, 4:].reshape(ncase, ntrials, 3)
+    np.savez_compressed(os.path.join(HERE, "pi_" + name + ".npz"),
+                        mol=r[:, 0].astype(np.int64),
+                        part=r[:, 1].astype(np.int64),
+                        remove=r[:, 2].astype(np.int64),
+                        trials=np.stack([t for _, _, _, t in rows]),
+                        en=res[:, :, 0], real=res[:, :, 1],
+                        overlap=res[:, :, 2].astype(np.int64))
+    print("wrote pi_" + name)
+
+
+PI_NAMES = ("c0_water", "w1728", "lj500", "c3_liquid", "c3_vapour",
+            "c1_water")
+
+# trial volume changes as fractions of the volume.  The reference's NVT
+# build sizes its k-vector arrays for the initial box (no spare capacity), so
+# the Ewald fixtures only shrink; ShiftVolume refuses edges below 2 Rcut.
+VOLUME_FRACS = {"c0_water": (-0.004, -0.012), "w1728": (-0.01, -0.003),
+                "lj500": (0.03, -0.025), "c3_liquid": (0.02, -0.015),
+                "c3_vapour": (-0.05, 0.04)}
+
+
+def make_volumes(probe: str, name: str) -> None:
+    """The energy calls of a volume move (VolumeTransfer::Transform / CalcEn,
+    src/moves/VolumeTransfer.h:96-190, NPT branch) on the fixture's initial
+    state for each trial volume change, and the state after accepting the
+    last one -> vol_<name>.npz: volume change, new edges, New k-vector count,
+    BoxInter (LJ, real) and BoxReciprocal(box, true) of the trial, its
+    coordinates and centres; then the accepted state's energies (inter,
+    real, recip, self, correction, total) and k-vector count."""
+    builder, cfg, _, _ = FIXTURES[name]
+    sysm = builder()
+    vol = float(np.prod(sysm.box))
+    deltas = [f * vol for f in VOLUME_FRACS[name]]
+    with tempfile.TemporaryDirectory() as d:
+        write_reference_inputs(d, sysm, cfg)
+        with open(os.path.join(d, "vol.txt"), "w") as f:
+            f.write("%d\n%s\n" % (len(deltas),
+                                   " ".join("%.17g" % v for v in deltas)))
+        out = os.path.join(d, "out")
+        os.makedirs(out)
+        subprocess.check_call([probe, "in.conf", out, "0", "-", "-", "-",
+                               "vol.txt"], cwd=d, stdout=subprocess.DEVNULL)
+        r = np.loadtxt(os.path.join(out, "volume_out.txt")).reshape(
+            len(deltas), -1)
+        pos = np.stack([np.loadtxt(os.path.join(out, "volume_pos_%d.txt" % i))
+                        for i in range(len(deltas))])
+        com = np.stack([np.loadtxt(os.path.join(out, "volume_com_%d.txt" % i))
+                        .reshape(-1, 3) for i in range(len(deltas))])
+        acc = _energies(os.path.join(out, "volume_accept.txt"))
+    np.savez_compressed(
+        os.path.join(HERE, "vol_" + name + ".npz"), delta=r[:, 0],
+        edges=r[:, 1:4], k_new=r[:, 4].astype(np.int64), inter=r[:, 5],
+        real=r[:, 6], recip=r[:, 7], pos=pos, com=com,
+        accepted=np.array([acc["box0_" + t] for t in
+                           ("inter", "real", "recip", "self", "correction",
+                            "total")]),
+        accepted_k=np.int64(acc.get("imageSize", 0)))
+    print("wrote vol_" + name)
+
+
 def make_kat(probe: str) -> None:
     """Known-answer vectors of the reference's MT19937 and Philox4x64-10."""
     with tempfile.TemporaryDirectory() as d:
@@ -272,10 +390,22 @@ def make_kat(probe: str) -> None:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("GOMC_REFERENCE"))
+    ap.add_argument("--only", choices=("particles", "volumes"), default=None,
+                    help="only the ParticleInter or the volume-move vectors")
     ap.add_argument("names", nargs="*")
     a = ap.parse_args()
+    if not a.ref or not os.path.isdir(os.path.join(a.ref, "src")):
+        ap.error("give the reference source tree with --ref or GOMC_REFERENCE")
     probe = build_reference(a.ref)
+    if a.only == "particles":
+        for n in (a.names or PI_NAMES):
+            make_particles(probe, n)
+        return
+    if a.only == "volumes":
+        for n in (a.names or list(VOLUME_FRACS)):
+            make_volumes(probe, n)
+        return
     if not a.names:
         make_kat(probe)
     for n in (a.names or list(FIXTURES)):
@@ -285,6 +415,12 @@ def main():
             make_single_mol(probe, n)
     for n in (a.names or list(FIXTURES)):
         make_virial(probe, n)
+    for n in PI_NAMES:
+        if not a.names or n in a.names:
+            make_particles(probe, n)
+    for n in VOLUME_FRACS:
+        if not a.names or n in a.names:
+            make_volumes(probe, n)
 
 
 if __name__ == "__main__":

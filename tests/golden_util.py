@@ -8,7 +8,11 @@ from gomc_gb300.config import SimConfig
 from gomc_gb300.systems import AtomKind, MoleculeType, MolSystem
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-NAMES = ["c0_water", "c0_water_mp", "w1728", "lj500", "c3_liquid", "c3_vapour"]
+NAMES = ["c0_water", "c0_water_mp", "w1728", "lj500", "c3_liquid", "c3_vapour",
+         "c1_water", "c1_water_mp"]
+# fixtures of the 8,000-water system: the oracle takes tens of seconds per
+# full structure factor on one core, so its CPU tests cover them in part
+LARGE = ("c1_water", "c1_water_mp")
 
 
 def load(name):
@@ -67,3 +71,15 @@ def load_virial(name):
     initial state: inter, real, recip, total, then the xx/yy/zz diagonals of
     interTens, realTens, recipTens, totalTens."""
     return np.load(os.path.join(GOLDEN, "vir_" + name + ".npz"))["out16"]
+
+
+PI_NAMES = ["c0_water", "w1728", "lj500", "c3_liquid", "c3_vapour", "c1_water"]
+
+
+def load_pi(name):
+    """ParticleInter vectors of fixture `name` (the reference's
+    CalculateEnergy::ParticleInter on the fixture's initial state, cases in
+    order): molecule, atom within it, whether the molecule was taken out of
+    the cell list around the call, trial positions [case, trial, 3], and the
+    outputs en, real, overlap [case, trial]."""
+    return np.load(os.path.join(GOLDEN, "pi_" + name + ".npz"))

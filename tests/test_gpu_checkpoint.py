@@ -80,3 +80,52 @@ def test_rejects_other_system(gb):
     with pytest.raises(GbError):
         b.restore(b"not a checkpoint at all, just some bytes")
     b.close()
+
+
+def test_rejected_load_leaves_box_unchanged(gb):
+    """A checkpoint whose random-stream position or cell slots are out of
+    range is refused before anything reaches the device: the box keeps its
+    coordinates, energies and move stream (the next moves equal those of a
+    box that never saw the bad checkpoint)."""
+    from gomc_gb300._lib import GbError
+    import struct
+    z, meta = load("c0_water")
+    seed = meta["config"]["random_seed"]
+
+    def make():
+        b = gb.Box(system_of(z, meta), config_of(meta))
+        b.mc_init(seed, move_fractions(meta), meta["config"]["adj_steps"])
+        return b
+    src = make()
+    src.mc_run(0, 300)
+    good = bytearray(src.checkpoint())
+    src.close()
+    n_atoms, n_mol = len(z["pos"]), len(z["mol_start"]) - 1
+    hdr = 48  # magic, eight int32 fields, int64 step
+    K, ncell, cap = struct.unpack_from("<iii", good, 8 + 12)
+    body = 8 * (3 * n_atoms + 3 * n_mol + 5 + 2 * K)
+    counts = hdr + body
+    slots = counts + 4 * ncell
+    mc = slots + 4 * ncell * cap
+    bad_mt = bytearray(good)
+    struct.pack_into("<i", bad_mt, mc + 4 * 624, 700)       # mt_left
+    bad_slot = bytearray(good)
+    struct.pack_into("<i", bad_slot, slots, n_atoms + 5)    # slot 0 of cell 0
+    dup_slot = bytearray(good)
+    first, second = struct.unpack_from("<ii", good, slots)
+    struct.pack_into("<i", dup_slot, slots + 4, first)      # an atom twice
+    ref = make()
+    ref.mc_run(0, 200)
+    want = _state(ref)
+    ref.close()
+    box = make()
+    before = (box.coords(), box.energy())
+    for blob in (bad_mt, bad_slot, dup_slot):
+        with pytest.raises(GbError):
+            box.restore(bytes(blob))
+        np.testing.assert_array_equal(box.coords(), before[0])
+        np.testing.assert_array_equal(box.energy(), before[1])
+    box.mc_run(0, 200)
+    for a, b in zip(_state(box), want):
+        np.testing.assert_array_equal(a, b)
+    box.close()

@@ -7,8 +7,8 @@ accept/reject sequence identical to the reference's over the golden traces.
 import numpy as np
 import pytest
 
-from tests.golden_util import (NAMES, SMI_NAMES, config_of, load, load_smi,
-                               load_virial,
+from tests.golden_util import (NAMES, PI_NAMES, SMI_NAMES, config_of, load,
+                               load_pi, load_smi, load_virial,
                                move_fractions, system_of)
 
 pytestmark = pytest.mark.gpu
@@ -155,21 +155,36 @@ def test_mc_trace_matches_reference(gb, name):
     box.close()
 
 
-def test_particle_inter_against_oracle(gb):
-    from oracle import oracle as O
-    O.set_threads(1)
-    z, meta = load("w1728")
-    sysm, cfg = system_of(z, meta), config_of(meta)
-    box = gb.Box(sysm, cfg)
-    ob = O.OracleBox(sysm, cfg)
-    rng = np.random.default_rng(5)
-    trials = rng.uniform(0, 1, size=(16, 3)) * sysm.box
-    ov, en, re = box.particle_inter(7, 0, -0.8476, trials)
-    for t in range(16):
-        o2, e2, r2 = ob.particle_inter(7, 0, -0.8476, trials[t])
-        assert bool(ov[t]) == o2
-        assert close(en[t], e2, scale=max(abs(e2), 1.0))
-        assert close(re[t], r2, scale=max(abs(r2), 1.0))
+@pytest.mark.parametrize("name", PI_NAMES)
+def test_particle_inter(gb, name):
+    """ParticleInter (the CBMC first-atom trial energies) against the
+    reference's vectors, cases in the reference's order: with the molecule
+    taken out of the cell list around the call (as MoleculeTransfer does) or
+    left in.  Each energy within 1e-10 of max(|value|, 1 K); overlap flags
+    equal."""
+    z, meta = load(name)
+    g = load_pi(name)
+    box = gb.Box(system_of(z, meta), config_of(meta))
+    for c in range(len(g["mol"])):
+        m, part, rm = int(g["mol"][c]), int(g["part"][c]), int(g["remove"][c])
+        if rm:
+            box.cell_remove_mol(m)
+        ov, en, re = box.particle_inter(m, part, g["trials"][c])
+        if rm:
+            box.cell_add_mol(m)
+        np.testing.assert_array_equal(ov.astype(int), g["overlap"][c])
+        for got, ref in ((en, g["en"][c]), (re, g["real"][c])):
+            err = np.abs(got - ref)
+            assert (err <= REL * np.maximum(np.abs(ref), 1.0)).all(), (
+                c, got, ref)
+    # a molecule out of the cell list blocks the Monte Carlo loop until it
+    # is back
+    box.cell_remove_mol(0)
+    box.mc_init(1, [0.5, 0.5, 0.0], 1000)
+    with pytest.raises(RuntimeError):
+        box.mc_run(0, 10)
+    box.cell_add_mol(0)
+    box.mc_run(0, 10)
     box.close()
 
 

@@ -11,8 +11,8 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from tests.golden_util import (NAMES, SMI_NAMES, config_of, load, load_smi,
-                               load_virial,
+from tests.golden_util import (LARGE, NAMES, PI_NAMES, SMI_NAMES, config_of,
+                               load, load_pi, load_smi, load_virial,
                                move_fractions, system_of)
 
 REL = 1e-12
@@ -27,11 +27,37 @@ def rel(a, b):
     return abs(a - b) / max(abs(b), 1e-300)
 
 
-@pytest.mark.parametrize("name", NAMES)
+# The 8,000-water MultiParticle fixture pins the GPU path; the oracle's
+# MultiParticle moves at that size take tens of seconds each on the host, and
+# the oracle is pinned on the same system by c1_water and on MultiParticle by
+# c0_water_mp.
+ORACLE_NAMES = [n for n in NAMES if n != "c1_water_mp"]
+
+
+def oracle_box(name, z, meta):
+    """OracleBox of a fixture.  The set-up's structure factor is summed per
+    k-vector in atom order whatever the thread count, so the large fixtures
+    build it on several threads; everything after runs on one thread."""
+    if name in LARGE:
+        O.set_threads(8)
+    try:
+        return O.OracleBox(system_of(z, meta), config_of(meta))
+    finally:
+        O.set_threads(1)
+
+
+@pytest.mark.parametrize("name", ORACLE_NAMES)
 def test_initial_state(name):
     z, meta = load(name)
-    box = O.OracleBox(system_of(z, meta), config_of(meta))
-    st = box.system_total()
+    box = oracle_box(name, z, meta)
+    # the recompute sums the structure factor per k-vector (any thread
+    # count gives the same bits) and the energies on one thread
+    if name in LARGE:
+        O.set_threads(8)
+    try:
+        st = box.system_total()
+    finally:
+        O.set_threads(1)
     for term in ("inter", "real", "recip", "self", "correction", "total"):
         ref = meta["init"]["box0_" + term]
         assert rel(st[term], ref) <= REL or abs(st[term] - ref) < 1e-9, term
@@ -50,10 +76,10 @@ def test_initial_state(name):
             np.testing.assert_array_equal(kv[key], z["kvec"][:, i])
 
 
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", ORACLE_NAMES)
 def test_proposal_deltas(name):
     z, meta = load(name)
-    box = O.OracleBox(system_of(z, meta), config_of(meta))
+    box = oracle_box(name, z, meta)
     cur = box.coords()
     ms = z["mol_start"]
     for i, m in enumerate(z["prop_mol"]):
@@ -68,10 +94,10 @@ def test_proposal_deltas(name):
             assert box.swap_source_recip(int(m), old) == ref[6]
 
 
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", ORACLE_NAMES)
 def test_mc_trace(name):
     z, meta = load(name)
-    box = O.OracleBox(system_of(z, meta), config_of(meta))
+    box = oracle_box(name, z, meta)
     box.mc_init(meta["config"]["random_seed"], move_fractions(meta),
                 meta["config"]["adj_steps"])
     tr = z["trace"]
@@ -150,10 +176,33 @@ def test_single_molecule_inter(name):
     del ob
 
 
-@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("name", ORACLE_NAMES)
 def test_virial(name):
     """VirialCalc + VirialReciprocal of the initial state: bit-exact."""
     z, meta = load(name)
-    ob = O.OracleBox(system_of(z, meta), config_of(meta))
+    ob = oracle_box(name, z, meta)
     np.testing.assert_array_equal(ob.virial(), load_virial(name))
+    del ob
+
+
+@pytest.mark.parametrize("name", PI_NAMES)
+def test_particle_inter(name):
+    """ParticleInter against the reference's vectors, bit-exact: the same
+    cases in the same order, the molecule taken out of the cell list around
+    the call where the reference took it out (each removal and re-insertion
+    relinks the molecule at the head of its cells, as in the reference, so
+    later cases sum in the reference's order too)."""
+    z, meta = load(name)
+    g = load_pi(name)
+    ob = oracle_box(name, z, meta)
+    for c in range(len(g["mol"])):
+        m, part, rm = int(g["mol"][c]), int(g["part"][c]), int(g["remove"][c])
+        if rm:
+            ob.cell_remove_mol(m)
+        for t in range(g["trials"].shape[1]):
+            ov, en, re = ob.particle_inter(m, part, g["trials"][c, t])
+            assert int(ov) == g["overlap"][c, t]
+            assert en == g["en"][c, t] and re == g["real"][c, t], (c, t)
+        if rm:
+            ob.cell_add_mol(m)
     del ob
