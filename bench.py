@@ -12,8 +12,9 @@ value   : moves/s of the plain FP64 form, device time (CUDA events on the
           library's stream) summed over the timed steps, L2 flushed between
           steps; whole job over all ranks (independent replicas per GPU).
 e2e     : the same metric through the public API with host buffers: each step
-          uploads the coordinates from host memory (gb_set_coords), runs the
-          moves (gb_mc_run) and reads back energies and coordinates.
+          draws its moves from the MT19937 stream on the host, copies the
+          move records to the device and runs them (gb_mc_run), and reads
+          back energies, coordinates and molecule centres.
 mixed   : the mixed-precision form (FP32 pair / per-k arithmetic, FP64
           accumulators), several independent chains batched on one GPU.
 serving : a stream of water jobs of mixed size through the job server
@@ -59,14 +60,20 @@ WORKLOAD = ("8000 SPC/E waters (24000 sites), L=62.1 A, Rcut 10 A, Ewald tol "
 def flop_per_move(K: int, na: int = 3, cand: int = 18000, incut: int = 2500):
     """Algorithmic FP64 flops of one single-molecule move.
 
-    Reciprocal: per k-vector and per old/new atom position two complex
-    products (12 flops) and the charge-weighted accumulate (4), plus the
-    structure-factor update (4) and its energy (4).  Real space: 9 flops per
-    candidate pair (minimum image and r^2) and about 60 per pair inside the
-    cutoff (LJ, erfc-screened Coulomb)."""
-    recip = K * (2 * na * 16 + 8)
-    real = cand * 9 + incut * 60
+    Reciprocal: per k-vector and per old/new atom position a dot product k.r
+    (5 flops) and the charge-weighted accumulate of cos and sin (2), then the
+    structure-factor update (4) and its energy (3): 49 K for a 3-site
+    molecule; the 2 n_a K sine/cosine evaluations are counted apart
+    (sincos_per_move).  Real space: 8 flops per candidate pair (minimum image
+    and r^2) and 25 per pair inside the cutoff (LJ and erfc-screened
+    Coulomb)."""
+    recip = K * (2 * na * (5 + 2) + 4 + 3)
+    real = cand * 8 + incut * 25
     return recip + real
+
+
+def sincos_per_move(K: int, na: int = 3):
+    return 2 * na * K
 
 
 class ClockSampler:
@@ -260,8 +267,8 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
     batched:  independent replicas of the box (seeds differ), all chains in one
       launch per step; moves/s over all chains, device time.
     e2e:      the batched run through the public API with host buffers:
-      coordinates of every replica uploaded, moves run, energies and
-      coordinates read back, every step.
+      move records of every replica drawn on the host and copied in, energies
+      and coordinates read back, every step.
     drift:    largest relative difference between the running energies and
       the periodic FP64 recompute (every 10,000 moves) over the run."""
     from gomc_gb300._lib import GB_FP64, GB_MIXED
@@ -391,14 +398,13 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
     batched = world * args.steps * M * B / t_tot
     timing = boxes[0].mc_timing(reset=True)
 
-    # end to end through the public API with host buffers
-    host = [(b.coords(), b.com()) for b in boxes]
+    # end to end through the public API with host buffers: every replica's
+    # move records are drawn on the host and copied in, its energies,
+    # coordinates and centres read back, every step
     e2e_t = []
     barrier()
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        for b, (xyz, com) in zip(boxes, host):
-            b.set_coords(xyz, com)
         engine.mc_run_batch(boxes, bstep[0], M)
         bstep[0] += M
         host = []
@@ -434,7 +440,7 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
         "clocks": clk.summary()}
     out["e2e"] = {"value": world * args.steps * M * B / t_e2e,
                   "unit": "moves/s",
-                  "h2d_bytes_per_step": B * (per_box + M * 64),
+                  "h2d_bytes_per_step": B * M * 64,
                   "d2h_bytes_per_step": B * (5 * 8 + per_box)}
     out["drift"] = dict(drift, recompute_every=10000,
                         bar="total-energy drift <= 1e-8 relative",
@@ -582,14 +588,15 @@ def run_gb300(args, rank, world):
     t_total = max_over_ranks(t_total, dist, torch, dev)
     value = world * args.steps * M / t_total
 
-    # end to end through the public API with host buffers
+    # end to end through the public API with host buffers: each step's
+    # inputs are its move records (molecule, kind, displacement and
+    # acceptance draws of the reference's MT19937 stream, drawn on the host
+    # and copied to the device, 64 B per move); its results, the running
+    # energies, coordinates and molecule centres, are read back
     e2e_times = []
-    xyz = box.coords()
-    com = box.com()
     barrier()
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        box.set_coords(xyz, com)
         box.mc_run(step, M)
         e = box.energy()
         xyz = box.coords()
@@ -601,7 +608,7 @@ def run_gb300(args, rank, world):
     t_e2e = float(sum(e2e_times))
     t_e2e = max_over_ranks(t_e2e, dist, torch, dev)
     e2e_value = world * args.steps * M / t_e2e
-    h2d = (sysm.n_atoms + sysm.n_mol) * 3 * 8 + M * 64
+    h2d = M * 64
     d2h = 5 * 8 + (sysm.n_atoms + sysm.n_mol) * 3 * 8
 
     # correctness of the running energies after the timed steps
@@ -643,7 +650,8 @@ def run_gb300(args, rank, world):
             "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + "
                             "dram__bytes_write.sum)",
             "kernel": "k_chain_fp64",
-            "per_unit": "%.3g FP64 flop per move (%d k-vectors)" % (fl, K),
+            "per_unit": "%.3g FP64 flop per move (%d k-vectors), plus %d "
+                        "sin/cos evaluations" % (fl, K, sincos_per_move(K)),
             "peak_source": peaks["pipe_peak_source"],
             "hbm_peak_gbs": peaks["hbm_gbs"], "hbm_peak_source": peaks["source"]}
     cpu = None
