@@ -373,3 +373,54 @@ def write_reference_inputs(dirpath: str, sysm: MolSystem, cfg) -> str:
     conf = os.path.join(dirpath, "in.conf")
     write_inconf(conf, sysm, cfg, names)
     return conf
+
+
+def write_gemc_inputs(dirpath: str, box0: MolSystem, box1: MolSystem, *,
+                      temperature: float, rcut: float, random_seed: int,
+                      dis_freq: float, vol_freq: float, swap_freq: float,
+                      run_steps: int, eq_steps: int, adj_steps: int,
+                      cbmc_first: int = 10, rcut_low: float = 0.0) -> str:
+    """Inputs of a two-box NVT Gibbs-ensemble run of the reference (GEMC
+    NVT: one PDB / PSF per box, ``Coordinates 0/1``, ``Structure 0/1``,
+    ``CellBasisVector*`` of both boxes, ``DisFreq`` / ``VolFreq`` /
+    ``SwapFreq``), LJ particles without charges; returns the in.conf path.
+    The two systems share one molecule and atom kind."""
+    os.makedirs(dirpath, exist_ok=True)
+    for b, s in enumerate((box0, box1)):
+        write_pdb(os.path.join(dirpath, "box%d.pdb" % b), s)
+        write_psf(os.path.join(dirpath, "box%d.psf" % b), s)
+    write_mie_par(os.path.join(dirpath, "system.par"), box0)
+    rows = [
+        ("Restart", "false"), ("ExpertMode", "true"), ("PRNG", "INTSEED"),
+        ("Random_Seed", str(random_seed)), ("ParaTypeCHARMM", "off"),
+        ("ParaTypeEXOTIC", "on"), ("Parameters", "system.par"),
+        ("Coordinates 0", "box0.pdb"), ("Coordinates 1", "box1.pdb"),
+        ("Structure 0", "box0.psf"), ("Structure 1", "box1.psf"),
+        ("GEMC", "NVT"), ("Temperature", repr(temperature)),
+        ("Potential", "VDW"), ("LRC", "false"), ("Rcut", repr(rcut)),
+        ("RcutLow", repr(rcut_low)), ("Exclude", "1-4"), ("Ewald", "false"),
+        ("ElectroStatic", "false"), ("CachedFourier", "false"),
+        ("RunSteps", str(run_steps)), ("EqSteps", str(eq_steps)),
+        ("AdjSteps", str(adj_steps)), ("DisFreq", repr(dis_freq)),
+        ("VolFreq", repr(vol_freq)), ("SwapFreq", repr(swap_freq)),
+        ("CBMC_First", str(cbmc_first)), ("CBMC_Nth", "4"),
+        ("CBMC_Ang", "50"), ("CBMC_Dih", "20"),
+    ]
+    for b, s in enumerate((box0, box1)):
+        L = s.box
+        rows += [("CellBasisVector1 %d" % b, "%r 0.00 0.00" % float(L[0])),
+                 ("CellBasisVector2 %d" % b, "0.00 %r 0.00" % float(L[1])),
+                 ("CellBasisVector3 %d" % b, "0.00 0.00 %r" % float(L[2]))]
+    rows += [
+        ("OutputName", "out"), ("CoordinatesFreq", "false 1000000"),
+        ("RestartFreq", "false 1000000"), ("CheckpointFreq", "false 1000000"),
+        ("ConsoleFreq", "true 1000000"), ("BlockAverageFreq", "false 1000000"),
+        ("DCDFreq", "false 1000000"), ("OutEnergy", "true true"),
+        ("OutPressure", "false false"), ("OutMolNum", "false false"),
+        ("OutDensity", "false false"), ("PressureCalc", "false"),
+    ]
+    conf = os.path.join(dirpath, "in.conf")
+    with open(conf, "w") as f:
+        for k, v in rows:
+            f.write("%-20s %s\n" % (k, v))
+    return conf

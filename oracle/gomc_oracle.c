@@ -1780,3 +1780,666 @@ void ora_mc_run(ora_mc *mc, long first, long nsteps, int *o_kind, int *o_mol,
   }
   free(np);
 }
+
+/* ======================================================================== */
+/* Gibbs ensemble, NVT (GEMC): two boxes of single-site LJ particles with    */
+/* displacement, molecule-transfer (CBMC) and volume-exchange moves.         */
+/* Restates System::PickMove / RunMove (src/System.cpp:262-302) with         */
+/* Translate (src/moves/Translate.h:52-138), MoleculeTransfer                */
+/* (src/moves/MoleculeTransfer.h:71-245) building through DCLinear /         */
+/* DCSingle (src/cbmc/DCLinear.cpp:44-55, src/cbmc/DCSingle.cpp:23-90),      */
+/* VolumeTransfer (src/moves/VolumeTransfer.h:71-318), the PRNG picks        */
+/* (src/PRNG.h:48-470), BoxDimensions::ExchangeVolume / SetVolume            */
+/* (src/BoxDimensions.cpp:124-227), Coordinates::TranslateRand /             */
+/* TranslateOneBox (src/Coordinates.cpp:83-180), MoleculeLookup::Shift       */
+/* (src/MoleculeLookup.cpp:165-200) and MoveSettings (src/MoveSettings.cpp:  */
+/* 19-265).  Pair sums run over each box's particles in lookup order (the    */
+/* reference sums in cell-list order: the same pairs, another rounding).     */
+/* ======================================================================== */
+#define G_KINDS 14
+#define G_DISPLACE 0
+#define G_ROTATE 1
+#define G_MOL_TRANSFER 10
+#define G_VOL_TRANSFER 13
+#define G_TARGET 0.5    /* MoveSettings::TARGET_ACCEPT_FRACT */
+#define G_TINY 1.0e-7   /* MoveSettings::TINY_AMOUNT */
+#define G_SMALL_WEIGHT 1.0e-38
+
+struct ora_gemc {
+  int n;
+  double ax[2][3], half[2][3], vol[2], volInv[2], minVol[2];
+  double *x, *y, *z, *cx, *cy, *cz;
+  int *lookup, start1; /* box 0: lookup[0, start1), box 1: [start1, n) */
+  double e[2];         /* running inter energies */
+  double sigmaSq, eps_cn, nexp, rcut, rcutSq, rcutLowSq, beta;
+  int ntrials;
+  double perc[G_KINDS];
+  double scale[2][G_KINDS];
+  long tries[2][G_KINDS], acc[2][G_KINDS], ttries[2][G_KINDS],
+      tacc[2][G_KINDS];
+  int adj;
+  int err; /* 1: a volume change would shrink a box below 2 Rcut */
+  ora_mt *mt;
+};
+
+static inline int g_first(const ora_gemc *g, int b) {
+  return b == 0 ? 0 : g->start1;
+}
+static inline int g_count(const ora_gemc *g, int b) {
+  return b == 0 ? g->start1 : g->n - g->start1;
+}
+static inline double g_min_image(double raw, double ax, double half) {
+  if (raw > half)
+    raw -= ax;
+  else if (raw < -half)
+    raw += ax;
+  return raw;
+}
+static inline double g_dist_sq(const double ax[3], const double half[3],
+                               double x1, double y1, double z1, double x2,
+                               double y2, double z2) {
+  double dx = g_min_image(x1 - x2, ax[0], half[0]);
+  double dy = g_min_image(y1 - y2, ax[1], half[1]);
+  double dz = g_min_image(z1 - z2, ax[2], half[2]);
+  return dx * dx + dy * dy + dz * dz;
+}
+/* FFParticle::CalcEn (src/FFParticle.cpp:295-325), lambda = 1 */
+static inline double g_calc_en(const ora_gemc *g, double distSq) {
+  if (g->rcutSq < distSq)
+    return 0.0;
+  double rRat2 = g->sigmaSq / distSq;
+  double rRat4 = rRat2 * rRat2;
+  double attract = rRat4 * rRat2;
+  double repulse = pow(rRat2, (g->nexp * 0.5));
+  return (g->eps_cn * (repulse - attract));
+}
+/* LJ energy of a particle at (px, py, pz) in box b against the box's
+ * particles other than `skip` (CalculateEnergy::ParticleInter /
+ * MoleculeInter's sums, src/CalculateEnergy.cpp:581-785); *ovl set when a
+ * pair is closer than RcutLow */
+static void g_accum(const ora_gemc *g, int b, double px, double py,
+                    double pz, int skip, double sign, double *acc, int *ovl) {
+  int a0 = g_first(g, b), n = g_count(g, b);
+  for (int i = 0; i < n; ++i) {
+    int j = g->lookup[a0 + i];
+    if (j == skip)
+      continue;
+    double d2 = g_dist_sq(g->ax[b], g->half[b], px, py, pz, g->x[j], g->y[j],
+                          g->z[j]);
+    if (d2 < g->rcutSq) {
+      if (ovl && d2 < g->rcutLowSq)
+        *ovl = 1;
+      *acc += sign * g_calc_en(g, d2);
+    }
+  }
+}
+static double g_particle(const ora_gemc *g, int b, double px, double py,
+                         double pz, int skip, int *ovl) {
+  double e = 0.0;
+  g_accum(g, b, px, py, pz, skip, 1.0, &e, ovl);
+  return e;
+}
+/* CalculateEnergy::BoxInter (src/CalculateEnergy.cpp:157-266) of box b for
+ * coordinates X, Y, Z at edges ax / half */
+static double g_box_inter(const ora_gemc *g, int b, const double *X,
+                          const double *Y, const double *Z,
+                          const double ax[3], const double half[3]) {
+  double e = 0.0;
+  int a0 = g_first(g, b), n = g_count(g, b);
+  for (int i = 0; i < n; ++i) {
+    int p = g->lookup[a0 + i];
+    for (int k = i + 1; k < n; ++k) {
+      int q = g->lookup[a0 + k];
+      double d2 = g_dist_sq(ax, half, X[p], Y[p], Z[p], X[q], Y[q], Z[q]);
+      if (d2 < g->rcutSq)
+        e += g_calc_en(g, d2);
+    }
+  }
+  return e;
+}
+static inline double g_wrap(double v, double ax) {
+  if (v >= ax)
+    v -= ax;
+  else if (v < 0)
+    v += ax;
+  return v;
+}
+static inline double g_unwrap(double v, double ref, double ax, double half) {
+  if (fabs(ref - v) > half) {
+    if (ref < half)
+      v -= ax;
+    else
+      v += ax;
+  }
+  return v;
+}
+
+ora_gemc *ora_gemc_create(int n0, const double *pos0, int n1,
+                          const double *pos1, const double *L0,
+                          const double *L1, double eps, double sigma,
+                          double nmie, double temperature, double rcut,
+                          double rcut_low, uint32_t seed,
+                          const double *frac3, int adj_steps, int ntrials) {
+  ora_gemc *g = (ora_gemc *)calloc(1, sizeof(ora_gemc));
+  int n = n0 + n1;
+  g->n = n;
+  g->x = (double *)malloc(sizeof(double) * n);
+  g->y = (double *)malloc(sizeof(double) * n);
+  g->z = (double *)malloc(sizeof(double) * n);
+  g->cx = (double *)malloc(sizeof(double) * n);
+  g->cy = (double *)malloc(sizeof(double) * n);
+  g->cz = (double *)malloc(sizeof(double) * n);
+  g->lookup = (int *)malloc(sizeof(int) * n);
+  g->start1 = n0;
+  for (int d = 0; d < 3; ++d) {
+    g->ax[0][d] = L0[d];
+    g->ax[1][d] = L1[d];
+    g->half[0][d] = L0[d] * 0.5;
+    g->half[1][d] = L1[d] * 0.5;
+  }
+  for (int b = 0; b < 2; ++b) {
+    g->vol[b] = g->ax[b][0] * g->ax[b][1] * g->ax[b][2];
+    g->volInv[b] = 1.0 / g->vol[b];
+    /* BoxDimensions::Init (src/BoxDimensions.cpp:19) */
+    g->minVol[b] = 8.0 * (rcut * rcut) * rcut + 0.001;
+  }
+  /* molecules of box 0 then box 1, as the two PDBs are read; coordinates
+   * wrapped (Coordinates::WrapCoordinate) and centres from COM::CalcCOM
+   * (one atom: the wrapped position) */
+  for (int i = 0; i < n; ++i) {
+    const double *p = i < n0 ? pos0 + 3 * i : pos1 + 3 * (i - n0);
+    int b = i < n0 ? 0 : 1;
+    g->x[i] = g_wrap(p[0], g->ax[b][0]);
+    g->y[i] = g_wrap(p[1], g->ax[b][1]);
+    g->z[i] = g_wrap(p[2], g->ax[b][2]);
+    g->cx[i] = g_wrap(g->x[i] * (1.0 / 1.0), g->ax[b][0]);
+    g->cy[i] = g_wrap(g->y[i] * (1.0 / 1.0), g->ax[b][1]);
+    g->cz[i] = g_wrap(g->z[i] * (1.0 / 1.0), g->ax[b][2]);
+    g->lookup[i] = i;
+  }
+  /* FFParticle::Blend for one kind (src/FFParticle.cpp:200-242) */
+  double cn = nmie / (nmie - 6.0) * pow(nmie / 6.0, (6.0 / (nmie - 6.0)));
+  g->nexp = nmie;
+  g->sigmaSq = sigma * sigma;
+  g->eps_cn = cn * sqrt(eps * eps);
+  g->rcut = rcut;
+  g->rcutSq = rcut * rcut;
+  g->rcutLowSq = rcut_low * rcut_low;
+  g->beta = 1 / temperature;
+  g->ntrials = ntrials;
+  /* StaticVals::InitMovePercents (src/StaticVals.cpp:35-94) */
+  double raw[G_KINDS] = {0};
+  raw[G_DISPLACE] = frac3[0];
+  raw[G_VOL_TRANSFER] = frac3[1];
+  raw[G_MOL_TRANSFER] = frac3[2];
+  double tot = 0.0;
+  for (int m = 0; m < G_KINDS; ++m)
+    tot += raw[m];
+  for (int m = 0; m < G_KINDS; ++m)
+    g->perc[m] = raw[m] / tot;
+  /* MoveSettings::Init (src/MoveSettings.cpp:19-90) runs before
+   * BoxDimensions::Init (src/System.cpp:72-81) and reads a zero-filled axis:
+   * the initial displacement scale is 0 */
+  for (int b = 0; b < 2; ++b) {
+    g->scale[b][G_DISPLACE] = 0.0 * 0.25;
+    g->scale[b][G_ROTATE] = M_PI_4;
+    g->scale[b][G_VOL_TRANSFER] = 500;
+  }
+  g->adj = adj_steps;
+  g->mt = ora_mt_create(seed);
+  for (int b = 0; b < 2; ++b)
+    g->e[b] = g_box_inter(g, b, g->x, g->y, g->z, g->ax[b], g->half[b]);
+  return g;
+}
+
+void ora_gemc_destroy(ora_gemc *g) {
+  if (!g)
+    return;
+  free(g->x); free(g->y); free(g->z);
+  free(g->cx); free(g->cy); free(g->cz);
+  free(g->lookup);
+  ora_mt_destroy(g->mt);
+  free(g);
+}
+
+/* MoveSettings::Update (src/MoveSettings.cpp:94-137), one kind */
+static void g_update(ora_gemc *g, int move, int accepted, int b) {
+  g->tries[b][move]++;
+  g->ttries[b][move]++;
+  if (accepted) {
+    g->tacc[b][move]++;
+    g->acc[b][move]++;
+  }
+}
+/* MoveSettings::AdjustMoves / Adjust (src/MoveSettings.cpp:147-238) */
+static void g_adjust(ora_gemc *g, long step) {
+  if ((step + 1) % g->adj != 0)
+    return;
+  for (int b = 0; b < 2; ++b)
+    for (int m = 0; m < G_KINDS; ++m) {
+      if (m == G_DISPLACE || m == G_ROTATE || m == G_VOL_TRANSFER) {
+        if (g->ttries[b][m] > 0) {
+          double currentAccept =
+              (double)(g->tacc[b][m]) / (double)(g->ttries[b][m]);
+          double fractOfTargetAccept = currentAccept / G_TARGET;
+          if (fractOfTargetAccept > 0.0)
+            g->scale[b][m] *= fractOfTargetAccept;
+          else
+            g->scale[b][m] *= 0.5;
+        }
+        double lo, hi;
+        if (m == G_DISPLACE) {
+          double mn = g->ax[b][0];
+          if (mn > g->ax[b][1])
+            mn = g->ax[b][1];
+          if (mn > g->ax[b][2])
+            mn = g->ax[b][2];
+          lo = 1.0e-10;
+          hi = (mn * 0.5) - G_TINY;
+        } else if (m == G_ROTATE) {
+          lo = 1.0e-6;
+          hi = M_PI - G_TINY;
+        } else {
+          double maxVolExchange = g->vol[b] - g->minVol[b];
+          lo = 0.001;
+          hi = 0.34 * maxVolExchange;
+        }
+        if (g->scale[b][m] < lo)
+          g->scale[b][m] = lo;
+        if (g->scale[b][m] > hi)
+          g->scale[b][m] = hi;
+      }
+      g->tacc[b][m] = 0;
+      g->ttries[b][m] = 0;
+    }
+}
+/* PRNG::PickBox with the sub-draw remainder (src/PRNG.h:215-230) */
+static int g_pick_box(double *subDraw, double *boxDiv, double movPerc) {
+  *boxDiv = movPerc / 2;
+  int b = (int)(unsigned)(*subDraw / *boxDiv);
+  if (b >= 2)
+    b--;
+  *subDraw -= b * *boxDiv;
+  return b;
+}
+/* PRNG::PickMol / PickMol2 with one molecule kind (src/PRNG.h:267-300,
+ * 336-365): -1 when the box is empty */
+static int g_pick_mol(ora_gemc *g, int b) {
+  int nb = g_count(g, b);
+  if (nb == 0)
+    return -1;
+  uint32_t off = mt_randInt(g->mt, (uint32_t)nb - 1u);
+  return g->lookup[g_first(g, b) + off];
+}
+/* MoleculeLookup::Shift (src/MoleculeLookup.cpp:178-200), one kind */
+static void g_shift(ora_gemc *g, int m, int from) {
+  int a0 = g_first(g, from), n = g_count(g, from), idx = -1;
+  for (int i = 0; i < n; ++i)
+    if (g->lookup[a0 + i] == m) {
+      idx = a0 + i;
+      break;
+    }
+  int t;
+  if (from == 0) { /* into box 1: the boundary moves down */
+    int ni = --g->start1;
+    t = g->lookup[idx];
+    g->lookup[idx] = g->lookup[ni];
+    g->lookup[ni] = t;
+  } else { /* into box 0: the boundary moves up */
+    int ni = g->start1++;
+    t = g->lookup[idx];
+    g->lookup[idx] = g->lookup[ni];
+    g->lookup[ni] = t;
+  }
+}
+
+static void g_displace(ora_gemc *g, double subDraw, double movPerc, int *o_b,
+                       int *o_m, int *o_acc, double *o_d) {
+  double boxDiv;
+  int b = g_pick_box(&subDraw, &boxDiv, movPerc);
+  /* PickMol: kind chunk from subDraw (one kind) */
+  int m = g_pick_mol(g, b);
+  *o_b = b;
+  *o_m = m;
+  if (m < 0) {
+    g_update(g, G_DISPLACE, 0, b);
+    return;
+  }
+  /* Coordinates::TranslateRand, PRNG::SymXYZ */
+  double bound = g->scale[b][G_DISPLACE], bound2 = 2.0 * bound;
+  double sx = mt_rand(g->mt) * bound2 - bound;
+  double sy = mt_rand(g->mt) * bound2 - bound;
+  double sz = mt_rand(g->mt) * bound2 - bound;
+  double nx = g_wrap(g->x[m] + sx, g->ax[b][0]);
+  double ny = g_wrap(g->y[m] + sy, g->ax[b][1]);
+  double nz = g_wrap(g->z[m] + sz, g->ax[b][2]);
+  double ncx = g_wrap(g->cx[m] + sx, g->ax[b][0]);
+  double ncy = g_wrap(g->cy[m] + sy, g->ax[b][1]);
+  double ncz = g_wrap(g->cz[m] + sz, g->ax[b][2]);
+  /* MoleculeInter: old pairs subtracted, new pairs added */
+  int ovl = 0;
+  double tempLJ = 0.0;
+  g_accum(g, b, g->x[m], g->y[m], g->z[m], m, -1.0, &tempLJ, NULL);
+  g_accum(g, b, nx, ny, nz, m, 1.0, &tempLJ, &ovl);
+  double pr = mt_rand(g->mt);
+  int res = pr < exp(-g->beta * (tempLJ + 0.0 + 0.0));
+  int result = res && !ovl;
+  if (result) {
+    g->e[b] += tempLJ;
+    g->x[m] = nx; g->y[m] = ny; g->z[m] = nz;
+    g->cx[m] = ncx; g->cy[m] = ncy; g->cz[m] = ncz;
+  }
+  g_update(g, G_DISPLACE, result, b);
+  *o_acc = result;
+  o_d[0] = tempLJ;
+  o_d[1] = ovl;
+}
+
+/* PRNG::PickWeighted (src/PRNG.h:167-200) */
+static int g_pick_weighted(ora_gemc *g, const double *w, int n, double tot,
+                           int *err) {
+  double draw = mt_rand(g->mt) * tot;
+  double sum = 0.0;
+  for (int i = 0; i < n; ++i) {
+    sum += w[i];
+    if (sum >= draw)
+      return i;
+  }
+  int lastZero = n;
+  for (int i = n - 1; i > 0 && w[i] == 0.0; --i)
+    lastZero = i;
+  lastZero--;
+  if (fabs(draw - tot) < 0.001)
+    return lastZero;
+  *err = 2;
+  return 0;
+}
+
+static void g_transfer(ora_gemc *g, double subDraw, double movPerc, int *o_b,
+                       int *o_m, int *o_acc, double *o_d) {
+  double boxDiv;
+  int src = g_pick_box(&subDraw, &boxDiv, movPerc);
+  int dest = src == 0 ? 1 : 0;
+  int m = g_pick_mol(g, src);
+  *o_b = src;
+  *o_m = m;
+  if (m < 0) {
+    g_update(g, G_MOL_TRANSFER, 0, dest);
+    return;
+  }
+  const int nt = g->ntrials;
+  double tx[64], ty[64], tz[64], en[64], w[64];
+  int ov[64];
+  /* DCLinear::Build: direction draw, then BuildNew and BuildOld */
+  (void)mt_randInt(g->mt, 1);
+  /* DCSingle::BuildNew in the destination box */
+  for (int t = 0; t < nt; ++t) {
+    tx[t] = mt_randExc(g->mt) * g->ax[dest][0];
+    ty[t] = mt_randExc(g->mt) * g->ax[dest][1];
+    tz[t] = mt_randExc(g->mt) * g->ax[dest][2];
+  }
+  double stepWeight = 0;
+  for (int t = 0; t < nt; ++t) {
+    ov[t] = 0;
+    en[t] = 0.0 + g_particle(g, dest, tx[t], ty[t], tz[t], m, &ov[t]);
+    w[t] = exp(-1 * g->beta * (en[t] + 0.0));
+    stepWeight += w[t];
+  }
+  int winner = g_pick_weighted(g, w, nt, stepWeight, &g->err);
+  int overlap = ov[winner];
+  double Wn = 1.0 * (stepWeight / nt);
+  double e_new = en[winner];
+  double nx = tx[winner], ny = ty[winner], nz = tz[winner];
+  /* DCSingle::BuildOld in the source box, trial 0 at the particle */
+  for (int t = 0; t < nt; ++t) {
+    tx[t] = mt_randExc(g->mt) * g->ax[src][0];
+    ty[t] = mt_randExc(g->mt) * g->ax[src][1];
+    tz[t] = mt_randExc(g->mt) * g->ax[src][2];
+  }
+  tx[0] = g_wrap(g->x[m], g->ax[src][0]);
+  ty[0] = g_wrap(g->y[m], g->ax[src][1]);
+  tz[0] = g_wrap(g->z[m], g->ax[src][2]);
+  double stepWeightOld = 0;
+  for (int t = 0; t < nt; ++t) {
+    ov[t] = 0;
+    en[t] = 0.0 + g_particle(g, src, tx[t], ty[t], tz[t], m, &ov[t]);
+    stepWeightOld += exp(-1 * g->beta * (en[t] + 0.0));
+  }
+  double Wo = 1.0 * (stepWeightOld / nt);
+  double e_old = en[0];
+  /* MoleculeTransfer::GetCoeff / Accept (GEMC) */
+  int nsrc = g_count(g, src), ndest = g_count(g, dest);
+  double coeff = (double)(nsrc) / (double)(ndest + 1) * g->vol[dest] *
+                 g->volInv[src];
+  double Wrat = Wn / Wo * 1.0 * 1.0;
+  int result = 0;
+  if (Wn > G_SMALL_WEIGHT && !overlap)
+    result = mt_rand(g->mt) < coeff * Wrat;
+  if (result) {
+    g->e[src] -= e_old;
+    g->e[dest] += e_new;
+    g->x[m] = nx; g->y[m] = ny; g->z[m] = nz;
+    /* COM::SetNew of one atom: its wrapped position */
+    g->cx[m] = g_wrap(nx * (1.0 / 1.0), g->ax[dest][0]);
+    g->cy[m] = g_wrap(ny * (1.0 / 1.0), g->ax[dest][1]);
+    g->cz[m] = g_wrap(nz * (1.0 / 1.0), g->ax[dest][2]);
+    g_shift(g, m, src);
+    if (g_count(g, src) == 0 || g_count(g, src) == 1)
+      g->e[src] = 0.0;
+  }
+  g_update(g, G_MOL_TRANSFER, result, dest);
+  *o_acc = result;
+  o_d[0] = Wn;
+  o_d[1] = Wo;
+  o_d[2] = e_new;
+  o_d[3] = e_old;
+}
+
+/* BoxDimensions::SetVolume, cubic scaling (src/BoxDimensions.cpp:215-227) */
+static void g_set_volume(double ax[3], double half[3], double *vol,
+                         double *volInv, double v) {
+  double ratio = cbrt(v / *vol);
+  for (int d = 0; d < 3; ++d) {
+    ax[d] *= ratio;
+    half[d] *= ratio;
+  }
+  *vol = v;
+  *volInv = 1.0 / v;
+}
+
+static void g_volume(ora_gemc *g, double subDraw, double movPerc, int *o_b,
+                     int *o_acc, double *o_d) {
+  double boxDiv = movPerc / 2;
+  int b0 = (int)(unsigned)(subDraw / boxDiv);
+  if (b0 >= 2)
+    b0--;
+  int b1 = b0 == 0 ? 1 : 0;
+  *o_b = b0;
+  int bp[2] = {b0, b1};
+  double max = g->scale[b0][G_VOL_TRANSFER];
+  if (g->scale[b1][G_VOL_TRANSFER] < max)
+    max = g->scale[b1][G_VOL_TRANSFER];
+  double transfer = mt_rand(g->mt) * (2.0 * max) - max;
+  /* BoxDimensions::ExchangeVolume */
+  double nax[2][3], nhalf[2][3], nvol[2], nvolInv[2], sc[2][3];
+  for (int b = 0; b < 2; ++b) {
+    for (int d = 0; d < 3; ++d) {
+      nax[b][d] = g->ax[b][d];
+      nhalf[b][d] = g->half[b][d];
+    }
+    nvol[b] = g->vol[b];
+    nvolInv[b] = g->volInv[b];
+  }
+  double vTot = (g->vol[bp[0]] + g->vol[bp[1]]);
+  g_set_volume(nax[bp[0]], nhalf[bp[0]], &nvol[bp[0]], &nvolInv[bp[0]],
+               g->vol[bp[0]] + transfer);
+  g_set_volume(nax[bp[1]], nhalf[bp[1]], &nvol[bp[1]], &nvolInv[bp[1]],
+               vTot - nvol[bp[0]]);
+  for (int i = 0; i < 2; ++i) {
+    int b = bp[i];
+    for (int d = 0; d < 3; ++d)
+      sc[b][d] = nax[b][d] / g->ax[b][d];
+    if (nhalf[b][0] < g->rcut || nhalf[b][1] < g->rcut ||
+        nhalf[b][2] < g->rcut || nvol[b] < g->minVol[b]) {
+      g->err = 1; /* the reference exits here */
+      return;
+    }
+  }
+  /* Coordinates::TranslateOneBox for both boxes */
+  int n = g->n;
+  double *X = (double *)malloc(sizeof(double) * 6 * n);
+  double *Y = X + n, *Z = X + 2 * n, *CX = X + 3 * n, *CY = X + 4 * n,
+         *CZ = X + 5 * n;
+  for (int i = 0; i < n; ++i) {
+    X[i] = g->x[i]; Y[i] = g->y[i]; Z[i] = g->z[i];
+    CX[i] = g->cx[i]; CY[i] = g->cy[i]; CZ[i] = g->cz[i];
+  }
+  for (int b = 0; b < 2; ++b) {
+    int a0 = g_first(g, b), nb = g_count(g, b);
+    for (int i = 0; i < nb; ++i) {
+      int m = g->lookup[a0 + i];
+      double ux = CX[m] * sc[b][0], uy = CY[m] * sc[b][1],
+             uz = CZ[m] * sc[b][2];
+      CX[m] = ux; CY[m] = uy; CZ[m] = uz;
+      double shx = CX[m] - g->cx[m], shy = CY[m] - g->cy[m],
+             shz = CZ[m] - g->cz[m];
+      double px = g_unwrap(X[m], g->cx[m], g->ax[b][0], g->half[b][0]);
+      double py = g_unwrap(Y[m], g->cy[m], g->ax[b][1], g->half[b][1]);
+      double pz = g_unwrap(Z[m], g->cz[m], g->ax[b][2], g->half[b][2]);
+      X[m] = g_wrap(px + shx, nax[b][0]);
+      Y[m] = g_wrap(py + shy, nax[b][1]);
+      Z[m] = g_wrap(pz + shz, nax[b][2]);
+    }
+  }
+  /* VolumeTransfer::CalcEn: BoxInter of both boxes at the new axes */
+  double en[2];
+  en[0] = g->e[0];
+  en[1] = g->e[1];
+  for (int i = 0; i < 2; ++i) {
+    int b = bp[i];
+    en[b] = g_box_inter(g, b, X, Y, Z, nax[b], nhalf[b]);
+  }
+  /* VolumeTransfer::GetCoeff / Accept */
+  double coeff = 1.0;
+  for (int i = 0; i < 2; ++i) {
+    int b = bp[i];
+    coeff *= pow(nvol[b] / g->vol[b], (double)g_count(g, b));
+  }
+  double tNew = (0.0 + en[0]) + en[1];
+  double tRef = (0.0 + g->e[0]) + g->e[1];
+  double uBoltz = exp(-g->beta * (tNew - tRef));
+  double accept = coeff * uBoltz;
+  int result = mt_rand(g->mt) < accept;
+  if (result) {
+    g->e[0] = en[0];
+    g->e[1] = en[1];
+    for (int i = 0; i < n; ++i) {
+      g->x[i] = X[i]; g->y[i] = Y[i]; g->z[i] = Z[i];
+      g->cx[i] = CX[i]; g->cy[i] = CY[i]; g->cz[i] = CZ[i];
+    }
+    for (int b = 0; b < 2; ++b) {
+      for (int d = 0; d < 3; ++d) {
+        g->ax[b][d] = nax[b][d];
+        g->half[b][d] = nhalf[b][d];
+      }
+      g->vol[b] = nvol[b];
+      g->volInv[b] = nvolInv[b];
+    }
+  }
+  free(X);
+  g_update(g, G_VOL_TRANSFER, result, bp[0]);
+  g_update(g, G_VOL_TRANSFER, result, bp[1]);
+  *o_acc = result;
+  o_d[0] = en[0];
+  o_d[1] = en[1];
+}
+
+/* Run steps [first, first + nsteps).  Per step: kind, box, molecule,
+ * accepted, and four move values (as the reference probe's trace). */
+int ora_gemc_run(ora_gemc *g, long first, long nsteps, int *o_kind, int *o_box,
+                 int *o_mol, int *o_acc, double *o_d4, double *o_state5) {
+  for (long t = 0; t < nsteps; ++t) {
+    long step = first + t;
+    g_adjust(g, step);
+    /* System::PickMove: PRNG::PickArbDist over the GEMC move kinds */
+    double sum = 0.0, prevSum = 0.0, draw = mt_rand(g->mt) * 1.0;
+    int pick;
+    for (pick = 0; pick < G_KINDS && sum < draw; ++pick) {
+      prevSum = sum;
+      sum += g->perc[pick];
+    }
+    if (pick != 0)
+      --pick;
+    double subDraw = draw - prevSum;
+    int b = -1, m = -1, acc = 0;
+    double d[4] = {0, 0, 0, 0};
+    if (pick == G_DISPLACE)
+      g_displace(g, subDraw, g->perc[pick], &b, &m, &acc, d);
+    else if (pick == G_MOL_TRANSFER)
+      g_transfer(g, subDraw, g->perc[pick], &b, &m, &acc, d);
+    else if (pick == G_VOL_TRANSFER)
+      g_volume(g, subDraw, g->perc[pick], &b, &acc, d);
+    if (g->err)
+      return g->err;
+    if (o_kind) o_kind[t] = pick;
+    if (o_box) o_box[t] = b;
+    if (o_mol) o_mol[t] = m;
+    if (o_acc) o_acc[t] = acc;
+    if (o_d4)
+      for (int k = 0; k < 4; ++k)
+        o_d4[4 * t + k] = d[k];
+    if (o_state5) {
+      o_state5[5 * t] = g->e[0];
+      o_state5[5 * t + 1] = g->e[1];
+      o_state5[5 * t + 2] = g->vol[0];
+      o_state5[5 * t + 3] = g->vol[1];
+      o_state5[5 * t + 4] = g->start1;
+    }
+  }
+  return 0;
+}
+
+/* coordinates [n * 3], centres [n * 3], lookup [n], molecules in box 0,
+ * running energies [2], axes [2 * 3] */
+void ora_gemc_get(const ora_gemc *g, double *xyz, double *com, int *lookup,
+                  int *n0, double *e2, double *axes6) {
+  for (int i = 0; i < g->n; ++i) {
+    if (xyz) {
+      xyz[3 * i] = g->x[i]; xyz[3 * i + 1] = g->y[i]; xyz[3 * i + 2] = g->z[i];
+    }
+    if (com) {
+      com[3 * i] = g->cx[i]; com[3 * i + 1] = g->cy[i];
+      com[3 * i + 2] = g->cz[i];
+    }
+    if (lookup)
+      lookup[i] = g->lookup[i];
+  }
+  if (n0)
+    *n0 = g->start1;
+  if (e2) {
+    e2[0] = g->e[0];
+    e2[1] = g->e[1];
+  }
+  if (axes6)
+    for (int b = 0; b < 2; ++b)
+      for (int d = 0; d < 3; ++d)
+        axes6[3 * b + d] = g->ax[b][d];
+}
+/* full recompute of both boxes' inter energies */
+void ora_gemc_system_total(const ora_gemc *g, double *e2) {
+  for (int b = 0; b < 2; ++b)
+    e2[b] = g_box_inter(g, b, g->x, g->y, g->z, g->ax[b], g->half[b]);
+}
+/* scales: displacement and volume per box; counts: tries and accepted of
+ * displacement, transfer, volume per box */
+void ora_gemc_settings(const ora_gemc *g, double *scale4, long *counts12) {
+  for (int b = 0; b < 2; ++b) {
+    scale4[2 * b] = g->scale[b][G_DISPLACE];
+    scale4[2 * b + 1] = g->scale[b][G_VOL_TRANSFER];
+    const int mv[3] = {G_DISPLACE, G_MOL_TRANSFER, G_VOL_TRANSFER};
+    for (int k = 0; k < 3; ++k) {
+      counts12[6 * b + 2 * k] = g->tries[b][mv[k]];
+      counts12[6 * b + 2 * k + 1] = g->acc[b][mv[k]];
+    }
+  }
+}

@@ -124,6 +124,27 @@ void ora_mc_run(ora_mc *mc, long first_step, long nsteps, int *kind, int *mol,
 void ora_mc_state(const ora_mc *mc, double *scales4, long *counts6);
 void ora_mc_set_scales(ora_mc *mc, const double *scales4);
 
+/* Gibbs ensemble (NVT) of single-site LJ particles in two boxes:
+ * displacement, CBMC molecule transfer and volume exchange moves. */
+typedef struct ora_gemc ora_gemc;
+ora_gemc *ora_gemc_create(int n0, const double *pos0, int n1,
+                          const double *pos1, const double *L0,
+                          const double *L1, double eps, double sigma,
+                          double nmie, double temperature, double rcut,
+                          double rcut_low, uint32_t seed,
+                          const double *frac3, int adj_steps, int ntrials);
+void ora_gemc_destroy(ora_gemc *g);
+/* frac3 = DisFreq, VolFreq, SwapFreq.  Per step: kind (0 displacement, 10
+ * transfer, 13 volume), box, molecule, accepted, four move values and the
+ * state after it (energies of both boxes, volumes, molecules in box 0).
+ * Returns non-zero if a volume change would shrink a box below 2 Rcut. */
+int ora_gemc_run(ora_gemc *g, long first, long nsteps, int *kind, int *box,
+                 int *mol, int *acc, double *d4, double *state5);
+void ora_gemc_get(const ora_gemc *g, double *xyz, double *com, int *lookup,
+                  int *n0, double *e2, double *axes6);
+void ora_gemc_system_total(const ora_gemc *g, double *e2);
+void ora_gemc_settings(const ora_gemc *g, double *scale4, long *counts12);
+
 #ifdef __cplusplus
 }
 #endif

@@ -77,6 +77,14 @@ def lib():
             "ora_box_reciprocal_sums": (D, [P, dp]),
             "ora_box_force_recip": (None, [P, dp, dp, dp]),
             "ora_torque": (None, [P, dp, dp, dp, dp, dp]),
+            "ora_gemc_create": (P, [I, dp, I, dp, dp, dp, D, D, D, D, D, D,
+                                    U32, dp, I, I]),
+            "ora_gemc_destroy": (None, [P]),
+            "ora_gemc_run": (I, [P, C.c_long, C.c_long, ip, ip, ip, ip, dp,
+                                 dp]),
+            "ora_gemc_get": (None, [P, dp, dp, ip, ip, dp, dp]),
+            "ora_gemc_system_total": (None, [P, dp]),
+            "ora_gemc_settings": (None, [P, dp, lp]),
             "ora_mt_create": (P, [U32]),
             "ora_mt_destroy": (None, [P]),
             "ora_mt_u32": (U32, [P]),
@@ -357,3 +365,65 @@ def u01_64(v: int) -> float:
 
 def uneg11_64(v: int) -> float:
     return lib().ora_uneg11_64(int(v))
+
+
+class OracleGemc:
+    """Gibbs-ensemble NVT Monte Carlo of single-site LJ particles in two
+    boxes (displacement, CBMC molecule transfer, volume exchange), restating
+    the reference's moves on the host (test infrastructure)."""
+
+    def __init__(self, pos0, pos1, box0, box1, eps, sigma, nmie, temperature,
+                 rcut, seed, frac3, adj_steps, ntrials=10, rcut_low=0.0):
+        p0 = np.ascontiguousarray(pos0, dtype=np.float64)
+        p1 = np.ascontiguousarray(pos1, dtype=np.float64)
+        L0 = np.ascontiguousarray(box0, dtype=np.float64)
+        L1 = np.ascontiguousarray(box1, dtype=np.float64)
+        fr = np.ascontiguousarray(frac3, dtype=np.float64)
+        self.n = len(p0) + len(p1)
+        self.h = lib().ora_gemc_create(len(p0), _dp(p0), len(p1), _dp(p1),
+                                       _dp(L0), _dp(L1), float(eps),
+                                       float(sigma), float(nmie),
+                                       float(temperature), float(rcut),
+                                       float(rcut_low), int(seed), _dp(fr),
+                                       int(adj_steps), int(ntrials))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ora_gemc_destroy(self.h)
+            self.h = None
+
+    def run(self, first: int, n: int) -> dict:
+        kind, box, mol, acc = (np.empty(n, np.int32) for _ in range(4))
+        d4 = np.empty((n, 4))
+        st = np.empty((n, 5))
+        ip = C.POINTER(C.c_int)
+        rc = lib().ora_gemc_run(self.h, int(first), int(n),
+                                kind.ctypes.data_as(ip),
+                                box.ctypes.data_as(ip),
+                                mol.ctypes.data_as(ip),
+                                acc.ctypes.data_as(ip), _dp(d4), _dp(st))
+        if rc:
+            raise RuntimeError("oracle GEMC stopped (code %d)" % rc)
+        return dict(kind=kind, box=box, mol=mol, accepted=acc, d=d4,
+                    energy=st[:, :2], volume=st[:, 2:4],
+                    n0=st[:, 4].astype(int))
+
+    def state(self) -> dict:
+        xyz = np.empty((self.n, 3))
+        com = np.empty((self.n, 3))
+        lk = np.empty(self.n, np.int32)
+        n0 = C.c_int()
+        e = np.empty(2)
+        ax = np.empty((2, 3))
+        lib().ora_gemc_get(self.h, _dp(xyz), _dp(com),
+                           lk.ctypes.data_as(C.POINTER(C.c_int)),
+                           C.byref(n0), _dp(e), _dp(ax))
+        sc = np.empty(4)
+        cnt = np.empty(12, dtype=np.int64)
+        lib().ora_gemc_settings(self.h, _dp(sc),
+                                cnt.ctypes.data_as(C.POINTER(C.c_long)))
+        tot = np.empty(2)
+        lib().ora_gemc_system_total(self.h, _dp(tot))
+        return dict(xyz=xyz, com=com, lookup=lk, n0=n0.value, energy=e,
+                    axes=ax, scales=sc.reshape(2, 2),
+                    counts=cnt.reshape(2, 3, 2), recompute=tot)

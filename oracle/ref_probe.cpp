@@ -57,6 +57,10 @@
 #include "Rotation.h"
 #include "MultiParticle.h"
 #include "TrialMol.h"
+#if ENSEMBLE == GEMC
+#include "MoleculeTransfer.h"
+#include "VolumeTransfer.h"
+#endif
 #undef private
 #undef protected
 
@@ -415,6 +419,97 @@ int main(int argc, char **argv) {
       fclose(f);
     }
   }
+
+#if ENSEMBLE == GEMC
+  // ---- GEMC Monte Carlo trace ----------------------------------------------
+  // One line per step: step, move kind, box (displacement: its box; swap:
+  // source box; volume: first box of the pair), molecule (-1 when none was
+  // picked or for a volume move), accepted, the running inter energies and
+  // volumes of both boxes, molecules in box 0, then four move values:
+  // displacement: dLJ, overlap, 0, 0; swap: new and old Rosenbluth weights,
+  // new and old trial energies; volume: the trial inter energies of both
+  // boxes, 0, 0.
+  if (nsteps > 0) {
+    FILE *f = open_out(outdir, "trace.txt");
+    MoveSettings &ms = sys.moveSettings;
+    MoleculeLookup &ml = sys.molLookupRef;
+    for (long step = 0; step < nsteps; ++step) {
+      ms.AdjustMoves(step);
+      sys.r123wrapper.SetStep(step);
+      double draw = 0;
+      uint kind = 0;
+      sys.PickMove(kind, draw);
+      uint acc0 = 0, acc1 = 0;
+      for (uint b = 0; b < BOX_TOTAL; ++b)
+        for (uint k = 0; k < mv::MOVE_KINDS_TOTAL; ++k)
+          acc0 += ms.GetAcceptTot(b, k);
+      uint n_before[2] = {ml.NumInBox(0), ml.NumInBox(1)};
+      sys.RunMove(kind, draw, step);
+      for (uint b = 0; b < BOX_TOTAL; ++b)
+        for (uint k = 0; k < mv::MOVE_KINDS_TOTAL; ++k)
+          acc1 += ms.GetAcceptTot(b, k);
+      int accepted = acc1 > acc0;
+      long bx = -1, m = -1;
+      double d[4] = {0, 0, 0, 0};
+      if (kind == mv::DISPLACE) {
+        Translate *t = static_cast<Translate *>(sys.moves[kind]);
+        bx = t->b;
+        if (n_before[bx] > 0) {
+          m = t->m;
+          d[0] = t->inter_LJ.energy;
+          d[1] = t->overlap;
+        }
+      } else if (kind == mv::MOL_TRANSFER) {
+        MoleculeTransfer *t = static_cast<MoleculeTransfer *>(sys.moves[kind]);
+        bx = t->sourceBox;
+        if (n_before[bx] > 0) {
+          m = t->molIndex;
+          d[0] = t->newMol.GetWeight();
+          d[1] = t->oldMol.GetWeight();
+          d[2] = t->newMol.GetEnergy().inter;
+          d[3] = t->oldMol.GetEnergy().inter;
+        }
+      } else if (kind == mv::VOL_TRANSFER) {
+        VolumeTransfer *v = static_cast<VolumeTransfer *>(sys.moves[kind]);
+        bx = v->bPick[0];
+        d[0] = v->sysPotNew.boxEnergy[0].inter;
+        d[1] = v->sysPotNew.boxEnergy[1].inter;
+      }
+      fprintf(f,
+              "%ld %u %ld %ld %d %.17g %.17g %.17g %.17g %u %.17g %.17g "
+              "%.17g %.17g\n",
+              step, kind, bx, m, accepted, sys.potential.boxEnergy[0].inter,
+              sys.potential.boxEnergy[1].inter, sys.boxDimRef.volume[0],
+              sys.boxDimRef.volume[1], ml.NumInBox(0), d[0], d[1], d[2], d[3]);
+    }
+    fclose(f);
+    f = open_out(outdir, "energies_final.txt");
+    sys.potential.Total();
+    dump_energy(f, "running0", sys.potential.boxEnergy[0]);
+    dump_energy(f, "running1", sys.potential.boxEnergy[1]);
+    SystemPotential pot = sys.calcEnergy.SystemTotal();
+    dump_energy(f, "recalc0", pot.boxEnergy[0]);
+    dump_energy(f, "recalc1", pot.boxEnergy[1]);
+    for (uint b = 0; b < BOX_TOTAL; ++b) {
+      XYZ ax = sys.boxDimRef.GetAxis(b);
+      fprintf(f, "axis %u %.17g %.17g %.17g\n", b, ax.x, ax.y, ax.z);
+      const uint kinds[3] = {mv::DISPLACE, mv::MOL_TRANSFER, mv::VOL_TRANSFER};
+      for (uint k : kinds)
+        fprintf(f, "settings %u %u %u %u %.17g\n", b, k,
+                ms.GetTrialTot(b, k), ms.GetAcceptTot(b, k),
+                ms.GetScaleTot(b, k));
+    }
+    fclose(f);
+    dump_coords(outdir, "coords_final.txt", sys.coordinates);
+    dump_coords(outdir, "com_final.txt", sys.com);
+    f = open_out(outdir, "lookup_final.txt");
+    fprintf(f, "%u %u\n", ml.NumInBox(0), ml.NumInBox(1));
+    for (uint i = 0; i < ml.NumInBox(0) + ml.NumInBox(1); ++i)
+      fprintf(f, "%u\n", ml.molLookup[i]);
+    fclose(f);
+  }
+  return 0;
+#endif
 
   // ---- Monte Carlo trace ---------------------------------------------------
   if (nsteps > 0) {

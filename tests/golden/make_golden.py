@@ -28,7 +28,8 @@ sys.path.insert(0, ROOT)
 
 from gomc_gb300.config import SimConfig  # noqa: E402
 from gomc_gb300.systems import (lj_sphere_box, spce_water_box,  # noqa: E402
-                                water_box_length, write_reference_inputs)
+                                water_box_length, write_gemc_inputs,
+                                write_reference_inputs)
 
 # name -> (system builder, config, MC steps, number of proposals)
 FIXTURES = {
@@ -374,6 +375,73 @@ def make_volumes(probe: str, name: str) -> None:
     print("wrote vol_" + name)
 
 
+# The Gibbs-ensemble configuration: LJ spheres (eps/kB 148 K, sigma 3.73 A,
+# Rcut 12 A) at 150 K, the liquid box of c3_liquid (2,400 in 40 A) and the
+# vapour box of c3_vapour (300 in 90 A), displacement / volume exchange /
+# molecule swap 0.8 / 0.01 / 0.19, 10 CBMC trials
+GEMC = dict(temperature=150.0, rcut=12.0, random_seed=3333, dis_freq=0.8,
+            vol_freq=0.01, swap_freq=0.19, adj_steps=100, cbmc_first=10)
+GEMC_STEPS = 6000
+
+
+def make_gemc(ref: str, name: str = "c3_gemc") -> None:
+    """A reference GEMC NVT trace (probe built with ENSEMBLE=GEMC) ->
+    c3_gemc.npz: the two boxes as generated, the initial energies, the
+    per-step trace, and the final coordinates, centres, molecule lookup,
+    energies and move settings."""
+    subprocess.check_call(["make", "-s", "-f", os.path.join(ROOT, "oracle",
+                                                             "ref.mk"),
+                           "REF=" + ref, "OUT=" + os.path.join(ROOT, "oracle",
+                                                               "_ref"),
+                           "ENSEMBLE=2", "-j8"], cwd=ROOT)
+    probe = os.path.join(ROOT, "oracle", "_ref", "ref_probe_ens2")
+    s0 = FIXTURES["c3_liquid"][0]()
+    s1 = FIXTURES["c3_vapour"][0]()
+    with tempfile.TemporaryDirectory() as d:
+        write_gemc_inputs(d, s0, s1, run_steps=GEMC_STEPS,
+                          eq_steps=GEMC_STEPS // 2, **GEMC)
+        out = os.path.join(d, "out")
+        os.makedirs(out)
+        subprocess.check_call([probe, "in.conf", out, str(GEMC_STEPS)],
+                              cwd=d, stdout=subprocess.DEVNULL)
+
+        def ld(fn, **kw):
+            return np.loadtxt(os.path.join(out, fn), **kw)
+        init, fin = {}, {}
+        for line in open(os.path.join(out, "energies_init.txt")):
+            t = line.split()
+            if len(t) == 3:
+                init[t[0] + "_" + t[1]] = float(t[2])
+        settings, axes = [], []
+        for line in open(os.path.join(out, "energies_final.txt")):
+            t = line.split()
+            if len(t) == 3:
+                fin[t[0] + "_" + t[1]] = float(t[2])
+            elif t and t[0] == "axis":
+                axes.append([float(v) for v in t[2:5]])
+            elif t and t[0] == "settings":
+                settings.append([float(v) for v in t[1:]])
+        with open(os.path.join(out, "lookup_final.txt")) as fh:
+            lk = [np.array(line.split(), dtype=np.int64) for line in fh]
+        lk = [lk[0], np.concatenate(lk[1:])]
+        arrays = dict(
+            pos0=s0.pos, pos1=s1.pos, box0=s0.box, box1=s1.box,
+            kind_eps=np.array([s0.kinds[0].epsilon]),
+            kind_sigma=np.array([s0.kinds[0].sigma]),
+            kind_n=np.array([s0.kinds[0].n]),
+            coords_init=ld("coords_init.txt"), trace=ld("trace.txt"),
+            coords_final=ld("coords_final.txt"),
+            com_final=ld("com_final.txt"),
+            lookup_counts=lk[0], lookup_final=lk[1],
+            axes_final=np.array(axes), settings_final=np.array(settings))
+        meta = dict(name=name, gemc=GEMC, steps=GEMC_STEPS,
+                    init=init, final=fin)
+        arrays["meta_json"] = np.frombuffer(json.dumps(meta).encode(),
+                                            dtype=np.uint8)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+        print("wrote", name)
+
+
 def make_kat(probe: str) -> None:
     """Known-answer vectors of the reference's MT19937 and Philox4x64-10."""
     with tempfile.TemporaryDirectory() as d:
@@ -391,8 +459,9 @@ def make_kat(probe: str) -> None:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("GOMC_REFERENCE"))
-    ap.add_argument("--only", choices=("particles", "volumes"), default=None,
-                    help="only the ParticleInter or the volume-move vectors")
+    ap.add_argument("--only", choices=("particles", "volumes", "gemc"),
+                    default=None,
+                    help="only the ParticleInter, volume-move or GEMC vectors")
     ap.add_argument("names", nargs="*")
     a = ap.parse_args()
     if not a.ref or not os.path.isdir(os.path.join(a.ref, "src")):
@@ -401,6 +470,9 @@ def main():
     if a.only == "particles":
         for n in (a.names or PI_NAMES):
             make_particles(probe, n)
+        return
+    if a.only == "gemc":
+        make_gemc(a.ref)
         return
     if a.only == "volumes":
         for n in (a.names or list(VOLUME_FRACS)):
@@ -421,6 +493,8 @@ def main():
     for n in VOLUME_FRACS:
         if not a.names or n in a.names:
             make_volumes(probe, n)
+    if not a.names or "c3_gemc" in a.names:
+        make_gemc(a.ref)
 
 
 if __name__ == "__main__":

@@ -83,3 +83,15 @@ def load_pi(name):
     the cell list around the call, trial positions [case, trial, 3], and the
     outputs en, real, overlap [case, trial]."""
     return np.load(os.path.join(GOLDEN, "pi_" + name + ".npz"))
+
+
+def load_gemc(name="c3_gemc"):
+    """The reference's GEMC NVT run of the LJ-sphere configuration: both
+    boxes as generated (pos0/pos1, box0/box1), the Mie parameters, the
+    per-step trace (step, move kind, box, molecule, accepted, running inter
+    energies of both boxes, volumes of both boxes, molecules in box 0, four
+    move values) and the final coordinates, centres, molecule lookup, axes
+    and move settings; meta holds the configuration and energies."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    meta = json.loads(bytes(z["meta_json"]).decode())
+    return z, meta

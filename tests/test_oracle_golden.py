@@ -12,7 +12,7 @@ import pytest
 
 from oracle import oracle as O
 from tests.golden_util import (LARGE, NAMES, PI_NAMES, SMI_NAMES, config_of,
-                               load, load_pi, load_smi, load_virial,
+                               load, load_gemc, load_pi, load_smi, load_virial,
                                move_fractions, system_of)
 
 REL = 1e-12
@@ -206,3 +206,50 @@ def test_particle_inter(name):
         if rm:
             ob.cell_add_mol(m)
     del ob
+
+
+def test_gemc_trace():
+    """The Gibbs-ensemble restatement against the reference's own GEMC NVT
+    run (6,000 steps: displacement, CBMC molecule transfer, volume exchange):
+    every move kind, box, molecule and decision identical; volumes, final
+    coordinates, centres, molecule lookup order, move scales and counts
+    bit-identical; running energies within 1e-12 (the sums run in another
+    order than the reference's cell lists)."""
+    z, meta = load_gemc()
+    g = meta["gemc"]
+    ob = O.OracleGemc(z["pos0"], z["pos1"], z["box0"], z["box1"],
+                      z["kind_eps"][0], z["kind_sigma"][0], z["kind_n"][0],
+                      g["temperature"], g["rcut"], g["random_seed"],
+                      [g["dis_freq"], g["vol_freq"], g["swap_freq"]],
+                      g["adj_steps"], g["cbmc_first"])
+    tr = z["trace"]
+    r = ob.run(0, len(tr))
+    np.testing.assert_array_equal(r["kind"], tr[:, 1].astype(int))
+    np.testing.assert_array_equal(r["box"], tr[:, 2].astype(int))
+    vol = r["kind"] == 13
+    np.testing.assert_array_equal(r["mol"][~vol], tr[~vol, 3].astype(int))
+    np.testing.assert_array_equal(r["accepted"], tr[:, 4].astype(int))
+    np.testing.assert_array_equal(r["volume"], tr[:, 7:9])
+    np.testing.assert_array_equal(r["n0"], tr[:, 9].astype(int))
+    ref = tr[:, 5:7]
+    assert (np.abs(r["energy"] - ref) <= 1e-12 * np.maximum(np.abs(ref), 1.0)
+            ).all()
+    st = ob.state()
+    np.testing.assert_array_equal(st["xyz"], z["coords_final"])
+    np.testing.assert_array_equal(st["com"], z["com_final"])
+    np.testing.assert_array_equal(st["lookup"], z["lookup_final"])
+    assert st["n0"] == int(z["lookup_counts"][0])
+    np.testing.assert_array_equal(st["axes"], z["axes_final"])
+    sf = z["settings_final"]  # box, move, tries, accepted, scale
+    for row in sf:
+        b, mv = int(row[0]), int(row[1])
+        k = {0: 0, 10: 1, 13: 2}[mv]
+        assert st["counts"][b, k, 0] == row[2] and st["counts"][b, k, 1] == row[3]
+        if mv == 0:
+            assert st["scales"][b, 0] == row[4]
+        elif mv == 13:
+            assert st["scales"][b, 1] == row[4]
+    fin = meta["final"]
+    for b in range(2):
+        assert abs(st["recompute"][b] - fin["recalc%d_inter" % b]) <= (
+            1e-12 * abs(fin["recalc%d_inter" % b]))
