@@ -64,6 +64,25 @@ class ServerConfig(C.Structure):
 
 
 # every function the header declares: name -> (restype, argtypes)
+class GemcDesc(C.Structure):
+    """gb_gemc_desc (include/gomc_gb300.h)."""
+    _fields_ = [("n0", C.c_int32), ("n1", C.c_int32),
+                ("pos0", C.POINTER(C.c_double)),
+                ("pos1", C.POINTER(C.c_double)),
+                ("box0", C.c_double * 3), ("box1", C.c_double * 3),
+                ("epsilon", C.c_double), ("sigma", C.c_double),
+                ("n_mie", C.c_double)]
+
+
+class GemcConfig(C.Structure):
+    """gb_gemc_config (include/gomc_gb300.h)."""
+    _fields_ = [("temperature", C.c_double), ("rcut", C.c_double),
+                ("rcut_low", C.c_double), ("frac", C.c_double * 3),
+                ("adj_steps", C.c_int32), ("cbmc_first", C.c_int32),
+                ("precision", C.c_int32), ("device", C.c_int32),
+                ("cluster_size", C.c_int32), ("seed", C.c_uint32)]
+
+
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int32)
@@ -129,6 +148,14 @@ SIGNATURES = {
     "gb_mc_autotune": (C.c_int, [_P, C.c_int32, C.c_int32, _I, _D]),
     "gb_mc_drift": (C.c_int, [_P, _D, _D, _L]),
     "gb_recip_energy_noalloc": (C.c_int, [_P, _P, _P, C.c_int32, _P, _P]),
+    "gb_gemc_create": (C.c_int, [C.POINTER(GemcDesc), C.POINTER(GemcConfig),
+                                 C.POINTER(_P)]),
+    "gb_gemc_destroy": (None, [_P]),
+    "gb_gemc_error": (C.c_char_p, [_P]),
+    "gb_gemc_run": (C.c_int, [_P, C.c_int64, C.c_int64, _I, _D]),
+    "gb_gemc_state": (C.c_int, [_P, _D, _D, _I, _D, _L, _D]),
+    "gb_gemc_coords": (C.c_int, [_P, _D, _D, _I]),
+    "gb_gemc_system_total": (C.c_int, [_P, _D]),
     "gb_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P)]),
     "gb_server_destroy": (None, [_P]),
     "gb_server_submit": (C.c_int, [_P, C.POINTER(SystemDesc),

@@ -1,0 +1,1438 @@
+// Gibbs ensemble (GEMC NVT) of single-site LJ particles: both boxes in one
+// persistent launch of one thread-block cluster.
+//
+// The move loop follows the reference's System::PickMove / RunMove
+// (src/System.cpp:262-302) with Translate (src/moves/Translate.h:52-138),
+// MoleculeTransfer building its trial sets through DCLinear / DCSingle
+// (src/moves/MoleculeTransfer.h:71-245, src/cbmc/DCLinear.cpp:44-55,
+// src/cbmc/DCSingle.cpp:23-90) and VolumeTransfer for GEMC-NVT
+// (src/moves/VolumeTransfer.h:71-318), the picks of src/PRNG.h:48-470, the
+// box arithmetic of BoxDimensions::ExchangeVolume / SetVolume
+// (src/BoxDimensions.cpp:124-227) and Coordinates::TranslateRand /
+// TranslateOneBox (src/Coordinates.cpp:83-180), the lookup reordering of
+// MoleculeLookup::Shift (src/MoleculeLookup.cpp:178-200) and the move-size
+// adjustment of MoveSettings (src/MoveSettings.cpp:94-238).
+//
+// Every CTA of the cluster holds the whole two-box system in shared memory
+// (positions in FP64 with FP32 copies, or 32-bit fixed-point turns in the
+// mixed form, and the molecule lookup) and runs its own copy of the
+// reference's MT19937 stream: warp 0 draws a move's random numbers (their
+// count depends on the state -- molecule counts of the boxes, rejection
+// loops -- so they are drawn on the device), every CTA takes a slice of the
+// move's pair energies, the partials are exchanged through distributed
+// shared memory, and every CTA adds them in rank order, decides and commits
+// the same way: one cluster barrier per move (two for a volume exchange).
+// The molecule centres live in global memory and are kept by CTA 0 alone;
+// the positions go back to global memory at the end of the launch.
+//
+// Pair sums cover each box's particles in lookup order (all pairs inside the
+// cutoff; the reference's cell lists enumerate the same pairs), FP64 pairs
+// behind an FP32 distance pre-filter in the plain form, FP32 pair energies on
+// exact fixed-point separations with FP64 accumulation in the mixed form.
+#include "gb_gemc.h"
+#include "gb_pair.cuh"
+
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+namespace cg = cooperative_groups;
+
+namespace gb {
+
+namespace {
+
+constexpr int PMAX = 3 * GEMC_NTMAX;  // partial values per CTA
+constexpr int NW = GEMC_THREADS / 32;
+constexpr double SMALL_WEIGHT = 1.0e-38;  // lib/NumLib.h:19
+constexpr double TARGET = 0.5;            // MoveSettings::TARGET_ACCEPT_FRACT
+constexpr double TINY = 1.0e-7;           // MoveSettings::TINY_AMOUNT
+constexpr double TURN = 4294967296.0;
+
+// One move as warp 0 drew it.
+struct Move {
+  int kind, b, b1, m, ok;
+  double u_acc;            // acceptance uniform (displacement, volume)
+  unsigned pick_word;      // raw word of PickWeighted (transfer)
+  double nx, ny, nz, ncx, ncy, ncz;  // displacement: new position, centre
+  double tr[2 * GEMC_NTMAX][3];     // transfer: new trials, then old trials
+  double nax[2][3], nhalf[2][3], nvol[2], nvolInv[2], sc[2][3];  // volume
+  double d[4];             // values reported in the trace
+  double tot[PMAX];        // cluster sums of the partials
+};
+
+struct GemcShared {
+  GemcCtl c;
+  Move mv;
+  double part[2][PMAX];       // this CTA's partials, by move parity
+  double wred[NW][PMAX];
+  int accept;
+};
+
+__device__ __forceinline__ double wrapd(double v, double ax) {
+  if (v >= ax)
+    v -= ax;
+  else if (v < 0)
+    v += ax;
+  return v;
+}
+__device__ __forceinline__ double unwrapd(double v, double ref, double ax,
+                                          double half) {
+  if (fabs(ref - v) > half) {
+    if (ref < half)
+      v -= ax;
+    else
+      v += ax;
+  }
+  return v;
+}
+__device__ __forceinline__ double mimg(double raw, double ax, double half) {
+  if (raw > half)
+    raw -= ax;
+  else if (raw < -half)
+    raw += ax;
+  return raw;
+}
+__device__ __forceinline__ float mimgf(float raw, float ax, float half) {
+  if (raw > half)
+    raw -= ax;
+  else if (raw < -half)
+    raw += ax;
+  return raw;
+}
+// FFParticle::CalcEn, lambda = 1 (src/FFParticle.cpp:295-325), inside Rcut
+__device__ __forceinline__ double lj64(const GemcParams &p, double d2) {
+  double rRat2 = p.sigmaSq / d2;
+  double rRat4 = rRat2 * rRat2;
+  double attract = rRat4 * rRat2;
+  double repulse = p.nexp == 12.0 ? attract * attract
+                                  : pow(rRat2, p.nexp * 0.5);
+  return p.eps_cn * (repulse - attract);
+}
+__device__ __forceinline__ float lj32(const GemcParams &p, float d2) {
+  float s = __fdividef(p.sigmaSq_f, d2);
+  float s3 = s * s * s;
+  float rep = p.nexp == 12.0 ? s3 * s3 : __powf(s, (float)(p.nexp * 0.5));
+  return p.eps_cn_f * (rep - s3);
+}
+__device__ __forceinline__ unsigned turns(double v, double invL) {
+  double t = v * invL;
+  t -= floor(t);
+  double s = t * TURN;
+  unsigned long long u = (unsigned long long)(s + 0.5);
+  return (unsigned)(u & 0xffffffffULL);
+}
+
+// ---------------------------------------------------------------------------
+// MT19937 (Matsumoto & Nishimura 1998) with the output of MTRand
+// (src/MersenneTwister.h:320-372), run by the 32 lanes of warp 0: every lane
+// holds the same cursor; a block of 624 words is regenerated in four
+// dependency phases (the recurrence reads word i + 1 and word i + 397 mod
+// 624, which are already new past the first 227 words).
+// ---------------------------------------------------------------------------
+__device__ void mt_phase(unsigned *st, int lo, int hi) {
+  const int lane = threadIdx.x & 31;
+  unsigned v[8];
+  int c = 0;
+  for (int i = lo + lane; i < hi; i += 32) {
+    unsigned a = st[i], b = st[(i + 1) % 624], m = st[(i + 397) % 624];
+    unsigned y = (a & 0x80000000u) | (b & 0x7fffffffu);
+    v[c++] = m ^ (y >> 1) ^ ((b & 1u) ? 0x9908b0dfu : 0u);
+  }
+  __syncwarp();
+  c = 0;
+  for (int i = lo + lane; i < hi; i += 32)
+    st[i] = v[c++];
+  __syncwarp();
+}
+struct MtCursor {
+  unsigned *st;
+  int left, next;
+  __device__ unsigned u32() {
+    if (left == 0) {
+      mt_phase(st, 0, 227);
+      mt_phase(st, 227, 454);
+      mt_phase(st, 454, 623);
+      mt_phase(st, 623, 624);
+      left = 624;
+      next = 0;
+    }
+    --left;
+    unsigned y = st[next++];
+    y ^= (y >> 11);
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    return y ^ (y >> 18);
+  }
+  __device__ double rand01() { return (double)u32() * (1.0 / 4294967295.0); }
+  __device__ double randExc01() {
+    return (double)u32() * (1.0 / 4294967296.0);
+  }
+  __device__ unsigned randInt(unsigned n) {
+    unsigned used = n;
+    used |= used >> 1;
+    used |= used >> 2;
+    used |= used >> 4;
+    used |= used >> 8;
+    used |= used >> 16;
+    unsigned i;
+    do
+      i = u32() & used;
+    while (i > n);
+    return i;
+  }
+};
+
+__device__ __forceinline__ int first_of(const GemcCtl &c, int b) {
+  return b == 0 ? 0 : c.start1;
+}
+__device__ __forceinline__ int count_of(const GemcCtl &c, int n, int b) {
+  return b == 0 ? c.start1 : n - c.start1;
+}
+
+// MoveSettings::Update (src/MoveSettings.cpp:94-137), counter slot k
+__device__ void settings_update(GemcCtl &c, int k, int acc, int b) {
+  c.tries[b][k]++;
+  c.ttries[b][k]++;
+  if (acc) {
+    c.tacc[b][k]++;
+    c.acc[b][k]++;
+  }
+}
+
+// MoveSettings::AdjustMoves / Adjust (src/MoveSettings.cpp:147-238)
+__device__ void settings_adjust(GemcCtl &c, long long step, int adj) {
+  if ((step + 1) % adj != 0)
+    return;
+  for (int b = 0; b < 2; ++b)
+    for (int k = 0; k < 3; ++k) {
+      // slots: displacement (counter 0), rotation (no tries), volume (2)
+      int cnt = k == 0 ? 0 : k == 2 ? 2 : -1;
+      if (cnt >= 0 && c.ttries[b][cnt] > 0) {
+        double currentAccept =
+            (double)(c.tacc[b][cnt]) / (double)(c.ttries[b][cnt]);
+        double f = currentAccept / TARGET;
+        if (f > 0.0)
+          c.scale[b][k] *= f;
+        else
+          c.scale[b][k] *= 0.5;
+      }
+      double lo, hi;
+      if (k == 0) {
+        double mn = c.ax[b][0];
+        if (mn > c.ax[b][1])
+          mn = c.ax[b][1];
+        if (mn > c.ax[b][2])
+          mn = c.ax[b][2];
+        lo = 1.0e-10;
+        hi = (mn * 0.5) - TINY;
+      } else if (k == 1) {
+        lo = 1.0e-6;
+        hi = M_PI - TINY;
+      } else {
+        lo = 0.001;
+        hi = 0.34 * (c.vol[b] - c.minVol[b]);
+      }
+      if (c.scale[b][k] < lo)
+        c.scale[b][k] = lo;
+      if (c.scale[b][k] > hi)
+        c.scale[b][k] = hi;
+    }
+  for (int b = 0; b < 2; ++b)
+    for (int k = 0; k < 3; ++k)
+      c.ttries[b][k] = c.tacc[b][k] = 0;
+}
+
+// Shared-memory arrays after GemcShared: lookup [n]; positions px, py, pz
+// and trial positions qx, qy, qz (FP64); the plain form adds FP32 copies
+// fx, fy, fz of the positions, the mixed form fixed-point turns tx, ty, tz
+// of the positions and ux, uy, uz of the trial positions (uint32).
+template <bool MIXED>
+struct Arrays {
+  int *lookup;
+  double *px, *py, *pz, *qx, *qy, *qz;
+  float *fx, *fy, *fz;
+  unsigned *tx, *ty, *tz, *ux, *uy, *uz;
+  __device__ Arrays(unsigned char *base, int n) {
+    lookup = (int *)base;
+    size_t off = ((size_t)n * 4 + 15) / 16 * 16;
+    px = (double *)(base + off);
+    py = px + n;
+    pz = py + n;
+    qx = pz + n;
+    qy = qx + n;
+    qz = qy + n;
+    if (!MIXED) {
+      fx = (float *)(qz + n);
+      fy = fx + n;
+      fz = fy + n;
+    } else {
+      tx = (unsigned *)(qz + n);
+      ty = tx + n;
+      tz = ty + n;
+      ux = tz + n;
+      uy = ux + n;
+      uz = uy + n;
+    }
+  }
+};
+
+// Pair energy of particle j (box b) with a point given by FP64 position
+// (sx, sy, sz) / FP32 copy / turns; adds to acc, counts RcutLow overlaps.
+template <bool MIXED>
+__device__ __forceinline__ void pair_point(const GemcParams &p,
+                                           const GemcCtl &c, const Arrays<MIXED> &A,
+                                           int b, int j, double sx, double sy,
+                                           double sz, float fxp, float fyp,
+                                           float fzp, unsigned txp,
+                                           unsigned typ, unsigned tzp,
+                                           const float *lt, double &acc,
+                                           int &ovl) {
+  if (!MIXED) {
+    float dx = mimgf(fxp - A.fx[j], (float)c.ax[b][0], (float)c.half[b][0]);
+    float dy = mimgf(fyp - A.fy[j], (float)c.ax[b][1], (float)c.half[b][1]);
+    float dz = mimgf(fzp - A.fz[j], (float)c.ax[b][2], (float)c.half[b][2]);
+    float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (r2 < p.rcutSq_f) {
+      double ex = mimg(sx - A.px[j], c.ax[b][0], c.half[b][0]);
+      double ey = mimg(sy - A.py[j], c.ax[b][1], c.half[b][1]);
+      double ez = mimg(sz - A.pz[j], c.ax[b][2], c.half[b][2]);
+      double d2 = ex * ex + ey * ey + ez * ez;
+      if (d2 < p.rcutSq) {
+        if (d2 < p.rcutLowSq)
+          ++ovl;
+        acc += lj64(p, d2);
+      }
+    }
+  } else {
+    float dx = (float)(int)(txp - A.tx[j]) * lt[0];
+    float dy = (float)(int)(typ - A.ty[j]) * lt[1];
+    float dz = (float)(int)(tzp - A.tz[j]) * lt[2];
+    float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (r2 < p.rcutSq_f) {
+      if (r2 < (float)p.rcutLowSq)
+        ++ovl;
+      acc += (double)lj32(p, r2);
+    }
+  }
+}
+
+// Warp sum, then the CTA's warps in order into wred[.][slot] (lane 0).
+__device__ __forceinline__ void warp_put(GemcShared &S, int slot, double v) {
+  for (int o = 16; o > 0; o >>= 1)
+    v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0)
+    S.wred[threadIdx.x >> 5][slot] = v;
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(GEMC_THREADS)
+    k_gemc(const GemcParams p) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  GemcShared &S = *(GemcShared *)dyn;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int gt = rank * GEMC_THREADS + tid, G = C * GEMC_THREADS;
+  const int n = p.n, nt = p.nt;
+  Arrays<MIXED> A(dyn + (sizeof(GemcShared) + 15) / 16 * 16, n);
+  GemcCtl &c = S.c;
+
+  // ---- load the state ----
+  {
+    const unsigned *src = (const unsigned *)p.ctl;
+    unsigned *dst = (unsigned *)&S.c;
+    for (int i = tid; i < (int)(sizeof(GemcCtl) / 4); i += GEMC_THREADS)
+      dst[i] = src[i];
+  }
+  __syncthreads();
+  for (int i = tid; i < n; i += GEMC_THREADS) {
+    A.lookup[i] = p.lookup[i];
+  }
+  __syncthreads();
+  for (int i = tid; i < n; i += GEMC_THREADS) {
+    int j = A.lookup[i];
+    int b = i < c.start1 ? 0 : 1;
+    A.px[j] = p.x[j];
+    A.py[j] = p.y[j];
+    A.pz[j] = p.z[j];
+    if (!MIXED) {
+      A.fx[j] = (float)p.x[j];
+      A.fy[j] = (float)p.y[j];
+      A.fz[j] = (float)p.z[j];
+    } else {
+      A.tx[j] = turns(p.x[j], 1.0 / c.ax[b][0]);
+      A.ty[j] = turns(p.y[j], 1.0 / c.ax[b][1]);
+      A.tz[j] = turns(p.z[j], 1.0 / c.ax[b][2]);
+    }
+  }
+  __syncthreads();
+  cluster.sync();
+
+  for (int t = 0; t < p.nsteps; ++t) {
+    const long long step = p.first + t;
+    const int par = t & 1;
+    Move &M = S.mv;
+    // ---------------- draw the move (warp 0) ----------------
+    if (warp == 0) {
+      if (lane == 0)
+        settings_adjust(c, step, p.adj);
+      __syncwarp();
+      MtCursor R{c.mt, c.mt_left, c.mt_next};
+      // System::PickMove: PRNG::PickArbDist, Wt = 1
+      double sum = 0.0, prevSum = 0.0, draw = R.rand01() * 1.0;
+      int pick;
+      for (pick = 0; pick < GEMC_KINDS && sum < draw; ++pick) {
+        prevSum = sum;
+        sum += p.perc[pick];
+      }
+      if (pick != 0)
+        --pick;
+      double subDraw = draw - prevSum;
+      double movPerc = p.perc[pick];
+      int kind = pick, b = -1, b1 = -1, m = -1, ok = 0;
+      double u_acc = 0.0;
+      unsigned pick_word = 0;
+      if (kind == GEMC_DISPLACE || kind == GEMC_TRANSFER) {
+        // PRNG::PickMolAndBox / PickMolAndBoxPair2: box from the sub-draw,
+        // then a molecule of the (single) kind in it
+        double boxDiv = movPerc / 2;
+        b = (int)(unsigned)(subDraw / boxDiv);
+        if (b >= 2)
+          b--;
+        b1 = b == 0 ? 1 : 0;
+        int nb = count_of(c, n, b);
+        if (nb > 0) {
+          unsigned off = R.randInt((unsigned)nb - 1u);
+          m = A.lookup[first_of(c, b) + off];
+          ok = 1;
+        }
+      } else if (kind == GEMC_VOLUME) {
+        double boxDiv = movPerc / 2;
+        b = (int)(unsigned)(subDraw / boxDiv);
+        if (b >= 2)
+          b--;
+        b1 = b == 0 ? 1 : 0;
+        ok = 1;
+      }
+      if (kind == GEMC_DISPLACE && ok) {
+        // Coordinates::TranslateRand with PRNG::SymXYZ
+        double bound = c.scale[b][0], bound2 = 2.0 * bound;
+        double sx = R.rand01() * bound2 - bound;
+        double sy = R.rand01() * bound2 - bound;
+        double sz = R.rand01() * bound2 - bound;
+        u_acc = R.rand01();
+        if (lane == 0) {
+          M.nx = wrapd(A.px[m] + sx, c.ax[b][0]);
+          M.ny = wrapd(A.py[m] + sy, c.ax[b][1]);
+          M.nz = wrapd(A.pz[m] + sz, c.ax[b][2]);
+          // the centres are kept by CTA 0 alone (global memory)
+          if (rank == 0) {
+            M.ncx = wrapd(p.cx[m] + sx, c.ax[b][0]);
+            M.ncy = wrapd(p.cy[m] + sy, c.ax[b][1]);
+            M.ncz = wrapd(p.cz[m] + sz, c.ax[b][2]);
+          }
+        }
+      } else if (kind == GEMC_TRANSFER && ok) {
+        // DCLinear::Build: direction, DCSingle::BuildNew (trials in the
+        // destination box, PickWeighted), DCSingle::BuildOld (trials in the
+        // source box, trial 0 at the molecule)
+        (void)R.randInt(1);
+        for (int k = 0; k < nt; ++k) {
+          double vx = R.randExc01() * c.ax[b1][0];
+          double vy = R.randExc01() * c.ax[b1][1];
+          double vz = R.randExc01() * c.ax[b1][2];
+          if (lane == 0) {
+            M.tr[k][0] = vx;
+            M.tr[k][1] = vy;
+            M.tr[k][2] = vz;
+          }
+        }
+        pick_word = R.u32();
+        for (int k = 0; k < nt; ++k) {
+          double vx = R.randExc01() * c.ax[b][0];
+          double vy = R.randExc01() * c.ax[b][1];
+          double vz = R.randExc01() * c.ax[b][2];
+          if (lane == 0) {
+            M.tr[nt + k][0] = vx;
+            M.tr[nt + k][1] = vy;
+            M.tr[nt + k][2] = vz;
+          }
+        }
+        if (lane == 0) {
+          M.tr[nt][0] = wrapd(A.px[m], c.ax[b][0]);
+          M.tr[nt][1] = wrapd(A.py[m], c.ax[b][1]);
+          M.tr[nt][2] = wrapd(A.pz[m], c.ax[b][2]);
+        }
+      } else if (kind == GEMC_VOLUME) {
+        // Coordinates::VolumeTransferTranslate: PRNG::Sym, then
+        // BoxDimensions::ExchangeVolume
+        double max = c.scale[b][2];
+        if (c.scale[b1][2] < max)
+          max = c.scale[b1][2];
+        double transfer = R.rand01() * (2.0 * max) - max;
+        if (lane == 0) {
+          for (int bb = 0; bb < 2; ++bb) {
+            for (int d = 0; d < 3; ++d) {
+              M.nax[bb][d] = c.ax[bb][d];
+              M.nhalf[bb][d] = c.half[bb][d];
+            }
+            M.nvol[bb] = c.vol[bb];
+            M.nvolInv[bb] = c.volInv[bb];
+          }
+          const int bp[2] = {b, b1};
+          double vTot = (c.vol[bp[0]] + c.vol[bp[1]]);
+          double target[2] = {c.vol[bp[0]] + transfer, 0.0};
+          for (int i = 0; i < 2; ++i) {
+            int bb = bp[i];
+            double v = i == 0 ? target[0] : vTot - M.nvol[bp[0]];
+            double ratio = cbrt(v / M.nvol[bb]);
+            for (int d = 0; d < 3; ++d) {
+              M.nax[bb][d] *= ratio;
+              M.nhalf[bb][d] *= ratio;
+            }
+            M.nvol[bb] = v;
+            M.nvolInv[bb] = 1.0 / v;
+          }
+          for (int i = 0; i < 2; ++i) {
+            int bb = bp[i];
+            for (int d = 0; d < 3; ++d)
+              M.sc[bb][d] = M.nax[bb][d] / c.ax[bb][d];
+            if (M.nhalf[bb][0] < p.rcut || M.nhalf[bb][1] < p.rcut ||
+                M.nhalf[bb][2] < p.rcut || M.nvol[bb] < c.minVol[bb])
+              c.err = 1;
+          }
+        }
+        __syncwarp();
+        if (!c.err)
+          u_acc = R.rand01();
+      }
+      if (lane == 0) {
+        M.kind = kind;
+        M.b = b;
+        M.b1 = b1;
+        M.m = m;
+        M.ok = ok;
+        M.u_acc = u_acc;
+        M.pick_word = pick_word;
+        c.mt_left = R.left;
+        c.mt_next = R.next;
+      }
+    }
+    __syncthreads();
+    if (c.err)
+      break;  // every CTA drew the same volume change
+    const int kind = M.kind, b = M.b, b1 = M.b1, m = M.m;
+    int nval = 0;
+    // ---------------- energy phase (all CTAs) ----------------
+    float lt[2][3];
+    if (MIXED)
+      for (int bb = 0; bb < 2; ++bb)
+        for (int d = 0; d < 3; ++d)
+          lt[bb][d] = (float)(c.ax[bb][d] / TURN);
+    if (kind == GEMC_DISPLACE && M.ok) {
+      // Translate::CalcEn -> MoleculeInter (molecule out of the cell list)
+      nval = 2;
+      double acc = 0.0;
+      int ovl = 0, ovl_old = 0;
+      const int a0 = first_of(c, b), nb = count_of(c, n, b);
+      unsigned ntx = 0, nty = 0, ntz = 0;
+      if (MIXED) {
+        ntx = turns(M.nx, 1.0 / c.ax[b][0]);
+        nty = turns(M.ny, 1.0 / c.ax[b][1]);
+        ntz = turns(M.nz, 1.0 / c.ax[b][2]);
+      }
+      for (int i = gt; i < nb; i += G) {
+        int j = A.lookup[a0 + i];
+        if (j == m)
+          continue;
+        double eo = 0.0, en = 0.0;
+        if (!MIXED) {
+          pair_point<MIXED>(p, c, A, b, j, A.px[m], A.py[m], A.pz[m], A.fx[m],
+                            A.fy[m], A.fz[m], 0, 0, 0, nullptr, eo, ovl_old);
+          pair_point<MIXED>(p, c, A, b, j, M.nx, M.ny, M.nz, (float)M.nx,
+                            (float)M.ny, (float)M.nz, 0, 0, 0, nullptr, en,
+                            ovl);
+        } else {
+          pair_point<MIXED>(p, c, A, b, j, 0, 0, 0, 0, 0, 0, A.tx[m], A.ty[m],
+                            A.tz[m], lt[b], eo, ovl_old);
+          pair_point<MIXED>(p, c, A, b, j, 0, 0, 0, 0, 0, 0, ntx, nty, ntz,
+                            lt[b], en, ovl);
+        }
+        acc += en - eo;
+      }
+      warp_put(S, 0, acc);
+      warp_put(S, 1, (double)ovl);
+    } else if (kind == GEMC_TRANSFER && M.ok) {
+      // CalculateEnergy::ParticleInter of each trial (the molecule is out of
+      // its box's cell list): new trials in the destination box, old trials
+      // in the source box
+      nval = 3 * nt;
+      for (int k = 0; k < 2 * nt; ++k) {
+        const int bb = k < nt ? b1 : b;
+        const int a0 = first_of(c, bb), nb = count_of(c, n, bb);
+        double sx = M.tr[k][0], sy = M.tr[k][1], sz = M.tr[k][2];
+        unsigned ux = 0, uy = 0, uz = 0;
+        if (MIXED) {
+          ux = turns(sx, 1.0 / c.ax[bb][0]);
+          uy = turns(sy, 1.0 / c.ax[bb][1]);
+          uz = turns(sz, 1.0 / c.ax[bb][2]);
+        }
+        double acc = 0.0;
+        int ovl = 0;
+        for (int i = gt; i < nb; i += G) {
+          int j = A.lookup[a0 + i];
+          if (j == m)
+            continue;
+          pair_point<MIXED>(p, c, A, bb, j, sx, sy, sz, (float)sx, (float)sy,
+                            (float)sz, ux, uy, uz, MIXED ? lt[bb] : nullptr,
+                            acc, ovl);
+        }
+        warp_put(S, k, acc);
+        if (k < nt)
+          warp_put(S, 2 * nt + k, (double)ovl);
+      }
+    } else if (kind == GEMC_VOLUME) {
+      // Coordinates::TranslateOneBox for both boxes into the trial arrays,
+      // then BoxInter of both boxes at the new axes.  The centres are CTA
+      // 0's (global memory): a cluster barrier first makes its latest
+      // writes visible to every CTA.
+      nval = 2;
+      asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+      asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+      for (int i = tid; i < n; i += GEMC_THREADS) {
+        int j = A.lookup[i];
+        int bb = i < c.start1 ? 0 : 1;
+        double ocx = p.cx[j], ocy = p.cy[j], ocz = p.cz[j];
+        double ncx = ocx * M.sc[bb][0], ncy = ocy * M.sc[bb][1],
+               ncz = ocz * M.sc[bb][2];
+        double ux = unwrapd(A.px[j], ocx, c.ax[bb][0], c.half[bb][0]);
+        double uy = unwrapd(A.py[j], ocy, c.ax[bb][1], c.half[bb][1]);
+        double uz = unwrapd(A.pz[j], ocz, c.ax[bb][2], c.half[bb][2]);
+        double nx = wrapd(ux + (ncx - ocx), M.nax[bb][0]);
+        double ny = wrapd(uy + (ncy - ocy), M.nax[bb][1]);
+        double nz = wrapd(uz + (ncz - ocz), M.nax[bb][2]);
+        A.qx[j] = nx;
+        A.qy[j] = ny;
+        A.qz[j] = nz;
+        if (MIXED) {
+          A.ux[j] = turns(nx, 1.0 / M.nax[bb][0]);
+          A.uy[j] = turns(ny, 1.0 / M.nax[bb][1]);
+          A.uz[j] = turns(nz, 1.0 / M.nax[bb][2]);
+        }
+      }
+      __syncthreads();
+      double eb[2] = {0.0, 0.0};
+      float nlt[2][3];
+      for (int bb = 0; bb < 2; ++bb)
+        for (int d = 0; d < 3; ++d)
+          nlt[bb][d] = (float)(M.nax[bb][d] / TURN);
+      // pair tiles of 32 x 32 (block row <= block column) dealt to the
+      // cluster's warps; lane l takes row i of its tile
+      const int gw = rank * NW + warp, GW = C * NW;
+      for (int bb = 0; bb < 2; ++bb) {
+        const int a0 = first_of(c, bb), nb = count_of(c, n, bb);
+        const int nbt = (nb + 31) / 32;
+        const int ntile = nbt * (nbt + 1) / 2;
+        const float ax0 = (float)M.nax[bb][0], ax1 = (float)M.nax[bb][1],
+                    ax2 = (float)M.nax[bb][2];
+        const float hf0 = (float)M.nhalf[bb][0], hf1 = (float)M.nhalf[bb][1],
+                    hf2 = (float)M.nhalf[bb][2];
+        double acc = 0.0;
+        for (int tl = gw; tl < ntile; tl += GW) {
+          // tile index -> (ib, jb), jb >= ib
+          int ib = 0, rem = tl;
+          while (rem >= nbt - ib) {
+            rem -= nbt - ib;
+            ++ib;
+          }
+          int jb = ib + rem;
+          int i = ib * 32 + lane;
+          bool act = i < nb;
+          int pi = act ? A.lookup[a0 + i] : 0;
+          double xi = 0, yi = 0, zi = 0;
+          float fxi = 0, fyi = 0, fzi = 0;
+          unsigned txi = 0, tyi = 0, tzi = 0;
+          if (act) {
+            if (!MIXED) {
+              xi = A.qx[pi];
+              yi = A.qy[pi];
+              zi = A.qz[pi];
+              fxi = (float)xi;
+              fyi = (float)yi;
+              fzi = (float)zi;
+            } else {
+              txi = A.ux[pi];
+              tyi = A.uy[pi];
+              tzi = A.uz[pi];
+            }
+          }
+          const int j0 = jb * 32, j1 = min(nb, j0 + 32);
+          for (int jj = j0; jj < j1; ++jj) {
+            if (!act || jj <= i)
+              continue;
+            int pj = A.lookup[a0 + jj];
+            if (!MIXED) {
+              double xj = A.qx[pj], yj = A.qy[pj], zj = A.qz[pj];
+              float dx = mimgf(fxi - (float)xj, ax0, hf0);
+              float dy = mimgf(fyi - (float)yj, ax1, hf1);
+              float dz = mimgf(fzi - (float)zj, ax2, hf2);
+              float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+              if (r2 < p.rcutSq_f) {
+                double ex = mimg(xi - xj, M.nax[bb][0], M.nhalf[bb][0]);
+                double ey = mimg(yi - yj, M.nax[bb][1], M.nhalf[bb][1]);
+                double ez = mimg(zi - zj, M.nax[bb][2], M.nhalf[bb][2]);
+                double d2 = ex * ex + ey * ey + ez * ez;
+                if (d2 < p.rcutSq)
+                  acc += lj64(p, d2);
+              }
+            } else {
+              float dx = (float)(int)(txi - A.ux[pj]) * nlt[bb][0];
+              float dy = (float)(int)(tyi - A.uy[pj]) * nlt[bb][1];
+              float dz = (float)(int)(tzi - A.uz[pj]) * nlt[bb][2];
+              float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+              if (r2 < p.rcutSq_f)
+                acc += (double)lj32(p, r2);
+            }
+          }
+        }
+        eb[bb] = acc;
+      }
+      warp_put(S, 0, eb[0]);
+      warp_put(S, 1, eb[1]);
+    }
+    __syncthreads();
+    // this CTA's partials, warps in order
+    if (tid < nval) {
+      double v = 0.0;
+      for (int w = 0; w < NW; ++w)
+        v += S.wred[w][tid];
+      S.part[par][tid] = v;
+    }
+    // ---------------- exchange: one cluster barrier ----------------
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+    if (tid < nval) {
+      double v = 0.0;
+      for (int r = 0; r < C; ++r)
+        v += cluster.map_shared_rank(&S.part[par][0], (unsigned)r)[tid];
+      M.tot[tid] = v;
+    }
+    __syncthreads();
+    // ---------------- decision (identical in every CTA) ----------------
+    if (warp == 0) {
+      MtCursor R{c.mt, c.mt_left, c.mt_next};
+      int acc = 0;
+      if (kind == GEMC_DISPLACE) {
+        if (M.ok) {
+          double dLJ = M.tot[0];
+          bool ovl = M.tot[1] > 0.0;
+          int res = M.u_acc < exp(-p.beta * (dLJ + 0.0 + 0.0));
+          acc = res && !ovl;
+          if (lane == 0) {
+            if (acc)
+              c.e[b] += dLJ;
+            M.d[0] = dLJ;
+            M.d[1] = ovl ? 1.0 : 0.0;
+            M.d[2] = M.d[3] = 0.0;
+          }
+          if (lane == 0)
+            settings_update(c, 0, acc, b);
+        } else if (lane == 0) {
+          settings_update(c, 0, 0, b);
+          M.d[0] = M.d[1] = M.d[2] = M.d[3] = 0.0;
+        }
+      } else if (kind == GEMC_TRANSFER) {
+        if (M.ok) {
+          double stepWeight = 0.0, w[GEMC_NTMAX];
+          for (int k = 0; k < nt; ++k) {
+            w[k] = exp(-1 * p.beta * ((0.0 + M.tot[k]) + 0.0));
+            stepWeight += w[k];
+          }
+          // PRNG::PickWeighted (src/PRNG.h:167-200)
+          double draw = ((double)M.pick_word * (1.0 / 4294967295.0)) *
+                        stepWeight;
+          double s = 0.0;
+          int winner = -1;
+          for (int k = 0; k < nt; ++k) {
+            s += w[k];
+            if (s >= draw) {
+              winner = k;
+              break;
+            }
+          }
+          if (winner < 0) {
+            int lastZero = nt;
+            for (int k = nt - 1; k > 0 && w[k] == 0.0; --k)
+              lastZero = k;
+            winner = lastZero - 1;  // |draw - total| < 0.001 in practice
+          }
+          bool overlap = M.tot[2 * nt + winner] > 0.0;
+          double Wn = 1.0 * (stepWeight / nt);
+          double sumOld = 0.0;
+          for (int k = 0; k < nt; ++k)
+            sumOld += exp(-1 * p.beta * ((0.0 + M.tot[nt + k]) + 0.0));
+          double Wo = 1.0 * (sumOld / nt);
+          double eNew = 0.0 + M.tot[winner], eOld = 0.0 + M.tot[nt];
+          int nsrc = count_of(c, n, b), ndest = count_of(c, n, b1);
+          double coeff = (double)(nsrc) / (double)(ndest + 1) * c.vol[b1] *
+                         c.volInv[b];
+          double Wrat = Wn / Wo * 1.0 * 1.0;
+          if (Wn > SMALL_WEIGHT && !overlap)
+            acc = R.rand01() < coeff * Wrat;
+          if (lane == 0) {
+            M.d[0] = Wn;
+            M.d[1] = Wo;
+            M.d[2] = eNew;
+            M.d[3] = eOld;
+            if (acc) {
+              c.e[b] -= eOld;
+              c.e[b1] += eNew;
+              M.nx = M.tr[winner][0];
+              M.ny = M.tr[winner][1];
+              M.nz = M.tr[winner][2];
+            }
+            settings_update(c, 1, acc, b1);
+          }
+        } else if (lane == 0) {
+          settings_update(c, 1, 0, b1);
+          M.d[0] = M.d[1] = M.d[2] = M.d[3] = 0.0;
+        }
+      } else if (kind == GEMC_VOLUME) {
+        double en0 = M.tot[0], en1 = M.tot[1];
+        double coeff = 1.0;
+        const int bp[2] = {b, b1};
+        for (int i = 0; i < 2; ++i) {
+          int bb = bp[i];
+          coeff *= pow(M.nvol[bb] / c.vol[bb], (double)count_of(c, n, bb));
+        }
+        double tNew = (0.0 + en0) + en1;
+        double tRef = (0.0 + c.e[0]) + c.e[1];
+        double uBoltz = exp(-p.beta * (tNew - tRef));
+        acc = M.u_acc < coeff * uBoltz;
+        if (lane == 0) {
+          M.d[0] = en0;
+          M.d[1] = en1;
+          M.d[2] = M.d[3] = 0.0;
+          settings_update(c, 2, acc, b);
+          settings_update(c, 2, acc, b1);
+        }
+      }
+      if (lane == 0) {
+        S.accept = acc;
+        c.mt_left = R.left;
+        c.mt_next = R.next;
+      }
+    }
+    __syncthreads();
+    // ---------------- commit ----------------
+    const int acc = S.accept;
+    if (acc && kind == GEMC_DISPLACE) {
+      if (tid == 0) {
+        A.px[m] = M.nx;
+        A.py[m] = M.ny;
+        A.pz[m] = M.nz;
+        if (!MIXED) {
+          A.fx[m] = (float)M.nx;
+          A.fy[m] = (float)M.ny;
+          A.fz[m] = (float)M.nz;
+        } else {
+          A.tx[m] = turns(M.nx, 1.0 / c.ax[b][0]);
+          A.ty[m] = turns(M.ny, 1.0 / c.ax[b][1]);
+          A.tz[m] = turns(M.nz, 1.0 / c.ax[b][2]);
+        }
+        if (rank == 0) {
+          p.cx[m] = M.ncx;
+          p.cy[m] = M.ncy;
+          p.cz[m] = M.ncz;
+        }
+      }
+    } else if (acc && kind == GEMC_TRANSFER) {
+      if (tid == 0) {
+        // new coordinates; COM::SetNew of one atom; MoleculeLookup::Shift
+        A.px[m] = M.nx;
+        A.py[m] = M.ny;
+        A.pz[m] = M.nz;
+        if (!MIXED) {
+          A.fx[m] = (float)M.nx;
+          A.fy[m] = (float)M.ny;
+          A.fz[m] = (float)M.nz;
+        } else {
+          A.tx[m] = turns(M.nx, 1.0 / c.ax[b1][0]);
+          A.ty[m] = turns(M.ny, 1.0 / c.ax[b1][1]);
+          A.tz[m] = turns(M.nz, 1.0 / c.ax[b1][2]);
+        }
+        if (rank == 0) {
+          p.cx[m] = wrapd(M.nx * (1.0 / 1.0), c.ax[b1][0]);
+          p.cy[m] = wrapd(M.ny * (1.0 / 1.0), c.ax[b1][1]);
+          p.cz[m] = wrapd(M.nz * (1.0 / 1.0), c.ax[b1][2]);
+        }
+        int a0 = first_of(c, b), nb = count_of(c, n, b), idx = a0;
+        for (int i = 0; i < nb; ++i)
+          if (A.lookup[a0 + i] == m) {
+            idx = a0 + i;
+            break;
+          }
+        int ni = b == 0 ? --c.start1 : c.start1++;
+        int tmp = A.lookup[idx];
+        A.lookup[idx] = A.lookup[ni];
+        A.lookup[ni] = tmp;
+        int left = count_of(c, n, b);
+        if (left == 0 || left == 1)
+          c.e[b] = 0.0;
+      }
+    } else if (acc && kind == GEMC_VOLUME) {
+      // new positions, centres and axes
+      for (int i = tid; i < n; i += GEMC_THREADS) {
+        int j = A.lookup[i];
+        int bb = i < c.start1 ? 0 : 1;
+        A.px[j] = A.qx[j];
+        A.py[j] = A.qy[j];
+        A.pz[j] = A.qz[j];
+        if (!MIXED) {
+          A.fx[j] = (float)A.qx[j];
+          A.fy[j] = (float)A.qy[j];
+          A.fz[j] = (float)A.qz[j];
+        } else {
+          A.tx[j] = A.ux[j];
+          A.ty[j] = A.uy[j];
+          A.tz[j] = A.uz[j];
+        }
+        if (rank == 0) {
+          p.cx[j] = p.cx[j] * M.sc[bb][0];
+          p.cy[j] = p.cy[j] * M.sc[bb][1];
+          p.cz[j] = p.cz[j] * M.sc[bb][2];
+        }
+      }
+      __syncthreads();
+      if (tid == 0) {
+        c.e[0] = M.tot[0];
+        c.e[1] = M.tot[1];
+        for (int bb = 0; bb < 2; ++bb) {
+          for (int d = 0; d < 3; ++d) {
+            c.ax[bb][d] = M.nax[bb][d];
+            c.half[bb][d] = M.nhalf[bb][d];
+          }
+          c.vol[bb] = M.nvol[bb];
+          c.volInv[bb] = M.nvolInv[bb];
+        }
+      }
+    }
+    if (rank == 0 && tid == 0 && p.tr_i) {
+      int *ti = p.tr_i + 5 * (size_t)t;
+      double *td = p.tr_d + 8 * (size_t)t;
+      ti[0] = kind;
+      ti[1] = b;
+      ti[2] = kind == GEMC_VOLUME ? -1 : m;
+      ti[3] = acc;
+      ti[4] = c.start1;
+      for (int k = 0; k < 4; ++k)
+        td[k] = M.d[k];
+      td[4] = c.e[0];
+      td[5] = c.e[1];
+      td[6] = c.vol[0];
+      td[7] = c.vol[1];
+    }
+    __syncthreads();
+  }
+  // ---- write the state back (CTA 0) ----
+  __syncthreads();
+  if (rank == 0) {
+    for (int i = tid; i < n; i += GEMC_THREADS) {
+      p.x[i] = A.px[i];
+      p.y[i] = A.py[i];
+      p.z[i] = A.pz[i];
+    }
+    for (int i = tid; i < n; i += GEMC_THREADS)
+      p.lookup[i] = A.lookup[i];
+    const unsigned *src = (const unsigned *)&S.c;
+    unsigned *dst = (unsigned *)p.ctl;
+    for (int i = tid; i < (int)(sizeof(GemcCtl) / 4); i += GEMC_THREADS)
+      dst[i] = src[i];
+  }
+  cluster.sync();  // no CTA leaves while another may read its partials
+}
+
+// BoxInter of both boxes from the FP64 masters (the periodic check of the
+// running energies): one CTA per pair tile row block, partials in order.
+__global__ void __launch_bounds__(256)
+    k_gemc_box_energy(const GemcParams p, double *part) {
+  const GemcCtl &c = *p.ctl;
+  int bb = blockIdx.y;
+  int a0 = bb == 0 ? 0 : c.start1;
+  int nb = bb == 0 ? c.start1 : p.n - c.start1;
+  double acc = 0.0;
+  for (int i = blockIdx.x; i < nb; i += gridDim.x) {
+    int pi = p.lookup[a0 + i];
+    for (int jj = i + 1 + threadIdx.x; jj < nb; jj += blockDim.x) {
+      int pj = p.lookup[a0 + jj];
+      double ex = mimg(p.x[pi] - p.x[pj], c.ax[bb][0], c.half[bb][0]);
+      double ey = mimg(p.y[pi] - p.y[pj], c.ax[bb][1], c.half[bb][1]);
+      double ez = mimg(p.z[pi] - p.z[pj], c.ax[bb][2], c.half[bb][2]);
+      double d2 = ex * ex + ey * ey + ez * ez;
+      if (d2 < p.rcutSq)
+        acc += lj64(p, d2);
+    }
+  }
+  __shared__ double red[8];
+  double s = block_sum<256>(acc, red);
+  if (threadIdx.x == 0)
+    part[bb * gridDim.x + blockIdx.x] = s;
+}
+
+__global__ void k_gemc_sum(const double *part, int nblk, double *out) {
+  int bb = threadIdx.x;
+  if (bb < 2) {
+    double s = 0.0;
+    for (int i = 0; i < nblk; ++i)
+      s += part[bb * nblk + i];
+    out[bb] = s;
+  }
+}
+
+template <bool MIXED>
+void gemc_attrs(size_t smem) {
+  static std::mutex mu;
+  static size_t set = 0;
+  std::lock_guard<std::mutex> g(mu);
+  if (smem > set) {
+    cudaFuncSetAttribute(k_gemc<MIXED>,
+                         cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (cudaFuncSetAttribute(k_gemc<MIXED>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) == cudaSuccess)
+      set = smem;
+    cudaGetLastError();
+  }
+}
+
+}  // namespace
+
+size_t gemc_smem(int n, int mixed) {
+  size_t head = (sizeof(GemcShared) + 15) / 16 * 16;
+  size_t lk = ((size_t)n * 4 + 15) / 16 * 16;
+  size_t per = 6 * sizeof(double) +
+               (mixed ? 6 * sizeof(unsigned) : 3 * sizeof(float));
+  return head + lk + per * (size_t)n;
+}
+
+int gemc_launch(Gemc &g, int nsteps, cudaEvent_t e0, cudaEvent_t e1) {
+  g.p.nsteps = nsteps;
+  const bool mixed = g.precision == GB_MIXED;
+  if (mixed)
+    gemc_attrs<true>(g.smem);
+  else
+    gemc_attrs<false>(g.smem);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(g.cluster);
+  cfg.blockDim = dim3(GEMC_THREADS);
+  cfg.dynamicSmemBytes = g.smem;
+  cfg.stream = g.stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = g.cluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (e0)
+    cudaEventRecord(e0, g.stream);
+  cudaError_t e = mixed ? cudaLaunchKernelEx(&cfg, k_gemc<true>, g.p)
+                        : cudaLaunchKernelEx(&cfg, k_gemc<false>, g.p);
+  if (e1)
+    cudaEventRecord(e1, g.stream);
+  return g.CudaCheck(e, "GEMC chain launch");
+}
+
+int gemc_recompute(Gemc &g, double *e2) {
+  const int nblk = 304;
+  int rc = OK;
+  if (!g.d_tot) {
+    void *q = nullptr;
+    if ((rc = g.CudaCheck(cudaMalloc(&q, (2 * nblk + 2) * sizeof(double)),
+                          "cudaMalloc")))
+      return rc;
+    g.allocs.push_back(q);
+    g.d_tot = (double *)q;
+  }
+  k_gemc_box_energy<<<dim3(nblk, 2), 256, 0, g.stream>>>(g.p, g.d_tot);
+  k_gemc_sum<<<1, 32, 0, g.stream>>>(g.d_tot, nblk, g.d_tot + 2 * nblk);
+  if ((rc = g.CudaCheck(cudaGetLastError(), "GEMC recompute")) ||
+      (rc = g.CudaCheck(cudaMemcpyAsync(e2, g.d_tot + 2 * nblk,
+                                        2 * sizeof(double),
+                                        cudaMemcpyDeviceToHost, g.stream),
+                        "download")) ||
+      (rc = g.CudaCheck(cudaStreamSynchronize(g.stream), "sync")))
+    return rc;
+  return OK;
+}
+
+}  // namespace gb
+
+// ===========================================================================
+// Host side and C ABI
+// ===========================================================================
+#include "gb_mc.h"  // MT19937
+
+struct gb_gemc {
+  gb::Gemc g;
+};
+
+namespace {
+thread_local std::string g_gemc_create_error;
+
+int gemc_fail_create(int code, const char *msg) {
+  g_gemc_create_error = msg;
+  return code;
+}
+
+template <class T>
+int gemc_alloc(gb::Gemc &g, T **p, size_t n) {
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+  if (e != cudaSuccess)
+    return g.CudaCheck(e, "cudaMalloc");
+  g.allocs.push_back(q);
+  *p = (T *)q;
+  return gb::OK;
+}
+
+void gemc_free(gb::Gemc &g) {
+  if (g.stream)
+    cudaStreamSynchronize(g.stream);
+  for (void *p : g.allocs)
+    cudaFree(p);
+  g.allocs.clear();
+  if (g.stream)
+    cudaStreamDestroy(g.stream);
+  g.stream = nullptr;
+}
+
+inline double host_wrap(double v, double ax) {
+  if (v >= ax)
+    v -= ax;
+  else if (v < 0)
+    v += ax;
+  return v;
+}
+}  // namespace
+
+extern "C" {
+
+int gb_gemc_create(const gb_gemc_desc *d, const gb_gemc_config *cfg,
+                   gb_gemc **out) {
+  using namespace gb;
+  if (!d || !cfg || !out || (d->n0 > 0 && !d->pos0) ||
+      (d->n1 > 0 && !d->pos1))
+    return gemc_fail_create(ERR_ARG, "null argument");
+  const int n = d->n0 + d->n1;
+  if (d->n0 < 0 || d->n1 < 0 || n <= 0)
+    return gemc_fail_create(ERR_ARG, "molecule counts out of range");
+  for (int k = 0; k < 3; ++k)
+    if (!(d->box0[k] > 0) || !(d->box1[k] > 0))
+      return gemc_fail_create(ERR_ARG, "box edges must be positive");
+  if (!(cfg->rcut > 0) || !(cfg->temperature > 0) || !(d->sigma > 0) ||
+      !(d->epsilon >= 0) || !(d->n_mie > 6))
+    return gemc_fail_create(ERR_ARG,
+                            "Rcut, Temperature and the Mie parameters must "
+                            "be positive (exponent above 6)");
+  if (cfg->cbmc_first < 1 || cfg->cbmc_first > GEMC_NTMAX)
+    return gemc_fail_create(ERR_UNSUPPORTED,
+                            "CBMC_First must lie in 1..16 on this engine");
+  if (cfg->adj_steps < 1)
+    return gemc_fail_create(ERR_ARG, "AdjSteps must be positive");
+  double ftot = cfg->frac[0] + cfg->frac[1] + cfg->frac[2];
+  if (!(cfg->frac[0] >= 0 && cfg->frac[1] >= 0 && cfg->frac[2] >= 0 &&
+        ftot > 0))
+    return gemc_fail_create(ERR_ARG, "move frequencies must not be negative");
+  int csize = cfg->cluster_size ? cfg->cluster_size : 16;
+  if (csize != 1 && csize != 2 && csize != 4 && csize != 8 && csize != 16)
+    return gemc_fail_create(ERR_ARG, "cluster size must be 1, 2, 4, 8 or 16");
+  if (cfg->precision != GB_FP64 && cfg->precision != GB_MIXED)
+    return gemc_fail_create(ERR_ARG, "precision must be GB_FP64 or GB_MIXED");
+
+  gb_gemc *h = new gb_gemc();
+  Gemc &g = h->g;
+  g.device = cfg->device;
+  g.precision = cfg->precision;
+  g.cluster = csize;
+  int rc;
+  auto fail = [&](int code) {
+    g_gemc_create_error = g.last_error;
+    gemc_free(g);
+    delete h;
+    return code;
+  };
+  if ((rc = g.CudaCheck(cudaSetDevice(g.device), "cudaSetDevice")))
+    return fail(rc);
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                         g.device);
+  g.smem = gemc_smem(n, g.precision == GB_MIXED);
+  if ((int)g.smem > optin) {
+    g.last_error = "both boxes do not fit one CTA's shared memory (" +
+                   std::to_string(g.smem) + " bytes)";
+    return fail(ERR_UNSUPPORTED);
+  }
+  if ((rc = g.CudaCheck(cudaStreamCreateWithFlags(&g.stream,
+                                                  cudaStreamNonBlocking),
+                        "stream")))
+    return fail(rc);
+
+  // System::Init for two boxes: coordinates wrapped, centres of one-atom
+  // molecules, the molecule lookup of box 0 then box 1
+  std::vector<double> x(n), y(n), z(n), cx(n), cy(n), cz(n);
+  std::vector<int> lookup(n);
+  GemcCtl &c = g.h_ctl;
+  std::memset(&c, 0, sizeof c);
+  for (int k = 0; k < 3; ++k) {
+    c.ax[0][k] = d->box0[k];
+    c.ax[1][k] = d->box1[k];
+    c.half[0][k] = d->box0[k] * 0.5;
+    c.half[1][k] = d->box1[k] * 0.5;
+  }
+  for (int b = 0; b < 2; ++b) {
+    c.vol[b] = c.ax[b][0] * c.ax[b][1] * c.ax[b][2];
+    c.volInv[b] = 1.0 / c.vol[b];
+    c.minVol[b] = 8.0 * (cfg->rcut * cfg->rcut) * cfg->rcut + 0.001;
+  }
+  for (int i = 0; i < n; ++i) {
+    const double *q = i < d->n0 ? d->pos0 + 3 * i : d->pos1 + 3 * (i - d->n0);
+    int b = i < d->n0 ? 0 : 1;
+    x[i] = host_wrap(q[0], c.ax[b][0]);
+    y[i] = host_wrap(q[1], c.ax[b][1]);
+    z[i] = host_wrap(q[2], c.ax[b][2]);
+    if (!(x[i] >= 0 && x[i] <= c.ax[b][0] && y[i] >= 0 &&
+          y[i] <= c.ax[b][1] && z[i] >= 0 && z[i] <= c.ax[b][2])) {
+      g.last_error = "a particle lies outside its box after wrapping";
+      return fail(ERR_ARG);
+    }
+    cx[i] = host_wrap(x[i] * (1.0 / 1.0), c.ax[b][0]);
+    cy[i] = host_wrap(y[i] * (1.0 / 1.0), c.ax[b][1]);
+    cz[i] = host_wrap(z[i] * (1.0 / 1.0), c.ax[b][2]);
+    lookup[i] = i;
+  }
+  c.start1 = d->n0;
+  // MoveSettings::Init: the displacement scale reads the axes before they
+  // are set (0), rotation pi/4, volume exchange 500 A^3
+  for (int b = 0; b < 2; ++b) {
+    c.scale[b][0] = 0.0 * 0.25;
+    c.scale[b][1] = M_PI_4;
+    c.scale[b][2] = 500;
+  }
+  MT19937 mt(cfg->seed);
+  int32_t left = 0, next = 0;
+  mt.Save(c.mt, &left, &next);
+  c.mt_left = left;
+  c.mt_next = next;
+
+  GemcParams &p = g.p;
+  p.n = n;
+  p.nt = cfg->cbmc_first;
+  p.adj = cfg->adj_steps;
+  p.cluster = csize;
+  // StaticVals::InitMovePercents over the GEMC move kinds
+  double raw[GEMC_KINDS] = {0};
+  raw[GEMC_DISPLACE] = cfg->frac[0];
+  raw[GEMC_VOLUME] = cfg->frac[1];
+  raw[GEMC_TRANSFER] = cfg->frac[2];
+  double tot = 0.0;
+  for (int k = 0; k < GEMC_KINDS; ++k)
+    tot += raw[k];
+  for (int k = 0; k < GEMC_KINDS; ++k)
+    p.perc[k] = raw[k] / tot;
+  // FFParticle::Blend for one kind
+  const double nm = d->n_mie;
+  const double cn = nm / (nm - 6.0) * std::pow(nm / 6.0, (6.0 / (nm - 6.0)));
+  p.nexp = nm;
+  p.sigmaSq = d->sigma * d->sigma;
+  p.eps_cn = cn * std::sqrt(d->epsilon * d->epsilon);
+  p.rcut = cfg->rcut;
+  p.rcutSq = cfg->rcut * cfg->rcut;
+  p.rcutLowSq = cfg->rcut_low * cfg->rcut_low;
+  p.beta = 1 / cfg->temperature;
+  p.sigmaSq_f = (float)p.sigmaSq;
+  p.eps_cn_f = (float)p.eps_cn;
+  // the FP32 distance pre-filter of the plain form passes every pair within
+  // Rcut: FP32 copies of positions lie within L 2^-24 of the FP64 ones
+  double lmax = std::max(std::max(c.ax[0][0], c.ax[0][1]),
+                         std::max(c.ax[1][0], c.ax[1][2]));
+  double rpad = cfg->rcut + 1e-5 * lmax + 1e-4;
+  p.rcutSq_f = g.precision == GB_MIXED ? (float)p.rcutSq
+                                       : (float)(rpad * rpad);
+  if ((rc = gemc_alloc(g, &p.x, n)) || (rc = gemc_alloc(g, &p.y, n)) ||
+      (rc = gemc_alloc(g, &p.z, n)) || (rc = gemc_alloc(g, &p.cx, n)) ||
+      (rc = gemc_alloc(g, &p.cy, n)) || (rc = gemc_alloc(g, &p.cz, n)) ||
+      (rc = gemc_alloc(g, &p.lookup, n)) || (rc = gemc_alloc(g, &p.ctl, 1)))
+    return fail(rc);
+  auto up = [&](void *dst, const void *src, size_t bytes) {
+    return g.CudaCheck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice,
+                                       g.stream),
+                       "upload");
+  };
+  if ((rc = up(p.x, x.data(), n * 8)) || (rc = up(p.y, y.data(), n * 8)) ||
+      (rc = up(p.z, z.data(), n * 8)) || (rc = up(p.cx, cx.data(), n * 8)) ||
+      (rc = up(p.cy, cy.data(), n * 8)) || (rc = up(p.cz, cz.data(), n * 8)) ||
+      (rc = up(p.lookup, lookup.data(), n * 4)) ||
+      (rc = up(p.ctl, &c, sizeof c)))
+    return fail(rc);
+  // initial energies (System::Init -> SystemTotal), FP64
+  double e2[2];
+  if ((rc = gemc_recompute(g, e2)))
+    return fail(rc);
+  c.e[0] = e2[0];
+  c.e[1] = e2[1];
+  if ((rc = up(p.ctl, &c, sizeof c)) ||
+      (rc = g.CudaCheck(cudaStreamSynchronize(g.stream), "sync")))
+    return fail(rc);
+  *out = h;
+  return OK;
+}
+
+void gb_gemc_destroy(gb_gemc *h) {
+  if (!h)
+    return;
+  gemc_free(h->g);
+  delete h;
+}
+
+const char *gb_gemc_error(const gb_gemc *h) {
+  if (!h)
+    return g_gemc_create_error.c_str();
+  return h->g.last_error.c_str();
+}
+
+int gb_gemc_run(gb_gemc *h, int64_t first_step, int64_t nsteps,
+                int32_t *trace_i5, double *trace_d8) {
+  using namespace gb;
+  if (!h)
+    return ERR_ARG;
+  Gemc &g = h->g;
+  if (nsteps < 0 || nsteps > (int64_t)1 << 30)
+    return g.Fail(ERR_ARG, "step count out of range");
+  if (first_step != g.next_step)
+    return g.Fail(ERR_STATE, "steps must continue from the last one run");
+  if (g.h_ctl.err)
+    return g.Fail(ERR_STATE, "an earlier run stopped on an invalid volume");
+  if (nsteps == 0)
+    return OK;
+  int rc;
+  cudaSetDevice(g.device);
+  const bool trace = trace_i5 || trace_d8;
+  if (trace && (size_t)nsteps > g.trace_cap) {
+    if ((rc = gemc_alloc(g, &g.d_tr_i, 5 * (size_t)nsteps)) ||
+        (rc = gemc_alloc(g, &g.d_tr_d, 8 * (size_t)nsteps)))
+      return rc;
+    g.trace_cap = (size_t)nsteps;
+  }
+  g.p.tr_i = trace ? g.d_tr_i : nullptr;
+  g.p.tr_d = trace ? g.d_tr_d : nullptr;
+  g.p.first = first_step;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  rc = gemc_launch(g, (int)nsteps, e0, e1);
+  if (!rc)
+    rc = g.CudaCheck(cudaMemcpyAsync(&g.h_ctl, g.p.ctl, sizeof(GemcCtl),
+                                     cudaMemcpyDeviceToHost, g.stream),
+                     "download");
+  if (!rc && trace_i5)
+    rc = g.CudaCheck(cudaMemcpyAsync(trace_i5, g.d_tr_i,
+                                     5 * sizeof(int32_t) * (size_t)nsteps,
+                                     cudaMemcpyDeviceToHost, g.stream),
+                     "download");
+  if (!rc && trace_d8)
+    rc = g.CudaCheck(cudaMemcpyAsync(trace_d8, g.d_tr_d,
+                                     8 * sizeof(double) * (size_t)nsteps,
+                                     cudaMemcpyDeviceToHost, g.stream),
+                     "download");
+  if (!rc)
+    rc = g.CudaCheck(cudaStreamSynchronize(g.stream), "GEMC run");
+  if (!rc)
+    cudaEventElapsedTime(&g.last_ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc)
+    return rc;
+  if (g.h_ctl.err)
+    return g.Fail(ERR_STATE,
+                  "a volume exchange would shrink a box below 2 Rcut (the "
+                  "reference stops its run there)");
+  g.next_step += nsteps;
+  return OK;
+}
+
+int gb_gemc_state(gb_gemc *h, double *energy2, double *edges6,
+                  int32_t *n_box0, double *scales4, int64_t *counts12,
+                  double *last_ms) {
+  if (!h)
+    return gb::ERR_ARG;
+  const gb::GemcCtl &c = h->g.h_ctl;
+  for (int b = 0; b < 2; ++b) {
+    if (energy2)
+      energy2[b] = c.e[b];
+    if (edges6)
+      for (int d = 0; d < 3; ++d)
+        edges6[3 * b + d] = c.ax[b][d];
+    if (scales4) {
+      scales4[2 * b] = c.scale[b][0];
+      scales4[2 * b + 1] = c.scale[b][2];
+    }
+    if (counts12)
+      for (int k = 0; k < 3; ++k) {
+        counts12[6 * b + 2 * k] = c.tries[b][k];
+        counts12[6 * b + 2 * k + 1] = c.acc[b][k];
+      }
+  }
+  if (n_box0)
+    *n_box0 = c.start1;
+  if (last_ms)
+    *last_ms = h->g.last_ms;
+  return gb::OK;
+}
+
+int gb_gemc_coords(gb_gemc *h, double *xyz, double *com, int32_t *lookup) {
+  if (!h)
+    return gb::ERR_ARG;
+  gb::Gemc &g = h->g;
+  const int n = g.p.n;
+  std::vector<double> t(6 * (size_t)n);
+  double *src[6] = {g.p.x, g.p.y, g.p.z, g.p.cx, g.p.cy, g.p.cz};
+  int rc;
+  for (int k = 0; k < 6; ++k)
+    if ((rc = g.CudaCheck(cudaMemcpyAsync(t.data() + (size_t)k * n, src[k],
+                                          (size_t)n * 8,
+                                          cudaMemcpyDeviceToHost, g.stream),
+                          "download")))
+      return rc;
+  if (lookup && (rc = g.CudaCheck(cudaMemcpyAsync(lookup, g.p.lookup,
+                                                  (size_t)n * 4,
+                                                  cudaMemcpyDeviceToHost,
+                                                  g.stream),
+                                  "download")))
+    return rc;
+  if ((rc = g.CudaCheck(cudaStreamSynchronize(g.stream), "sync")))
+    return rc;
+  for (int i = 0; i < n; ++i)
+    for (int d = 0; d < 3; ++d) {
+      if (xyz)
+        xyz[3 * i + d] = t[(size_t)d * n + i];
+      if (com)
+        com[3 * i + d] = t[(size_t)(3 + d) * n + i];
+    }
+  return gb::OK;
+}
+
+int gb_gemc_system_total(gb_gemc *h, double *energy2) {
+  if (!h || !energy2)
+    return gb::ERR_ARG;
+  cudaSetDevice(h->g.device);
+  return gb::gemc_recompute(h->g, energy2);
+}
+
+}  // extern "C"

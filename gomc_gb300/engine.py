@@ -481,6 +481,99 @@ class Box:
         return sc, cnt
 
 
+class Gemc:
+    """Gibbs-ensemble NVT run of single-site LJ particles in two boxes
+    (gb_gemc_*): displacement, CBMC molecule transfer and volume exchange,
+    the whole move loop in one persistent launch on the device."""
+
+    def __init__(self, pos0, pos1, box0, box1, epsilon: float, sigma: float,
+                 n_mie: float, temperature: float, rcut: float, seed: int,
+                 frac3: Sequence[float], adj_steps: int, cbmc_first: int = 10,
+                 rcut_low: float = 0.0, precision: int = GB_FP64,
+                 device: int = 0, cluster_size: int = 0):
+        L = lib()
+        self.h = None
+        self._p0 = np.ascontiguousarray(pos0, dtype=np.float64).reshape(-1, 3)
+        self._p1 = np.ascontiguousarray(pos1, dtype=np.float64).reshape(-1, 3)
+        self.n = len(self._p0) + len(self._p1)
+        d = _lib.GemcDesc()
+        d.n0, d.n1 = len(self._p0), len(self._p1)
+        d.pos0, d.pos1 = _dp(self._p0), _dp(self._p1)
+        for k in range(3):
+            d.box0[k] = float(box0[k])
+            d.box1[k] = float(box1[k])
+        d.epsilon, d.sigma, d.n_mie = float(epsilon), float(sigma), float(n_mie)
+        c = _lib.GemcConfig()
+        c.temperature, c.rcut, c.rcut_low = (float(temperature), float(rcut),
+                                             float(rcut_low))
+        for k in range(3):
+            c.frac[k] = float(frac3[k])
+        c.adj_steps, c.cbmc_first = int(adj_steps), int(cbmc_first)
+        c.precision, c.device = int(precision), int(device)
+        c.cluster_size, c.seed = int(cluster_size), int(seed)
+        h = C.c_void_p()
+        rc = L.gb_gemc_create(C.byref(d), C.byref(c), C.byref(h))
+        if rc:
+            raise _lib.GbError(rc, (L.gb_gemc_error(None) or b"").decode())
+        self.h = h.value
+        self.next_step = 0
+
+    def close(self) -> None:
+        if self.h:
+            lib().gb_gemc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc: int) -> None:
+        if rc:
+            raise _lib.GbError(rc, (lib().gb_gemc_error(self.h) or b"")
+                               .decode())
+
+    def run(self, nsteps: int, trace: bool = False):
+        """Run the next nsteps steps; with trace, per-step arrays."""
+        ti = td = None
+        if trace:
+            ti = np.empty((nsteps, 5), np.int32)
+            td = np.empty((nsteps, 8))
+        self._chk(lib().gb_gemc_run(self.h, self.next_step, int(nsteps),
+                                    None if ti is None else _ip(ti),
+                                    None if td is None else _dp(td)))
+        self.next_step += int(nsteps)
+        if not trace:
+            return None
+        return dict(kind=ti[:, 0], box=ti[:, 1], mol=ti[:, 2],
+                    accepted=ti[:, 3], n0=ti[:, 4], d=td[:, :4],
+                    energy=td[:, 4:6], volume=td[:, 6:8])
+
+    def state(self) -> dict:
+        e, ax, sc = np.empty(2), np.empty((2, 3)), np.empty((2, 2))
+        cnt = np.empty((2, 3, 2), np.int64)
+        n0 = C.c_int32()
+        ms = C.c_double()
+        self._chk(lib().gb_gemc_state(self.h, _dp(e), _dp(ax), C.byref(n0),
+                                      _dp(sc), cnt.ctypes.data_as(
+                                          C.POINTER(C.c_int64)),
+                                      C.byref(ms)))
+        return dict(energy=e, axes=ax, n0=n0.value, scales=sc, counts=cnt,
+                    last_ms=ms.value)
+
+    def coords(self):
+        xyz, com = np.empty((self.n, 3)), np.empty((self.n, 3))
+        lk = np.empty(self.n, np.int32)
+        self._chk(lib().gb_gemc_coords(self.h, _dp(xyz), _dp(com), _ip(lk)))
+        return xyz, com, lk
+
+    def system_total(self) -> np.ndarray:
+        e = np.empty(2)
+        self._chk(lib().gb_gemc_system_total(self.h, _dp(e)))
+        return e
+
+
 def mc_run_batch(boxes: Sequence[Box], first_step: int, nsteps: int) -> None:
     arr = (C.c_void_p * len(boxes))(*[b.h for b in boxes])
     rc = lib().gb_mc_run_batch(arr, len(boxes), int(first_step), int(nsteps))

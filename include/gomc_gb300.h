@@ -398,6 +398,68 @@ int gb_server_stats(gb_server *srv, double *out12);
 int gb_server_occupancy(gb_server *srv, double *out10);
 const char *gb_server_error(const gb_server *srv);
 
+/* ---- Gibbs ensemble (GEMC NVT) of single-site LJ particles ----
+ * Two boxes exchanging volume and molecules, run on one GPU as one
+ * persistent launch of one thread-block cluster: the reference's GEMC move
+ * loop (System::ChooseAndRunMove / RunMove, src/System.cpp:262-302) over
+ * Translate (src/moves/Translate.h:52-138), MoleculeTransfer with CBMC
+ * first-atom trials (src/moves/MoleculeTransfer.h:71-245,
+ * src/cbmc/DCSingle.cpp:23-90) and VolumeTransfer GEMC-NVT
+ * (src/moves/VolumeTransfer.h:71-318), with the MoveSettings adjustment
+ * (src/MoveSettings.cpp:94-238) and the reference's MT19937 stream seeded
+ * with Random_Seed (drawn on the device, since how many numbers a move takes
+ * depends on the molecule counts of the boxes).  One molecule kind of one
+ * LJ (Mie) site, no charges, no tail correction; both boxes must fit one
+ * CTA's shared memory (about 2,900 molecules in all in the mixed form, 3,300
+ * in the FP64 form: GB_ERR_UNSUPPORTED beyond). */
+typedef struct gb_gemc gb_gemc;
+typedef struct gb_gemc_desc {
+  int32_t n0, n1;               /* molecules in box 0 and box 1 */
+  const double *pos0, *pos1;    /* [n0 * 3], [n1 * 3] as read from the PDBs */
+  double box0[3], box1[3];      /* orthogonal edges, A */
+  double epsilon, sigma, n_mie; /* the LJ site: K, A, repulsion exponent */
+} gb_gemc_desc;
+typedef struct gb_gemc_config {
+  double temperature, rcut, rcut_low; /* Temperature, Rcut, RcutLow */
+  double frac[3];         /* DisFreq, VolFreq, SwapFreq */
+  int32_t adj_steps;      /* AdjSteps */
+  int32_t cbmc_first;     /* CBMC_First (1..16) */
+  int32_t precision;      /* GB_FP64, or GB_MIXED: FP32 pair energies on
+                             exact fixed-point separations, FP64 sums */
+  int32_t device;
+  int32_t cluster_size;   /* CTAs of the cluster: 1, 2, 4, 8, 16 (0 = 16) */
+  uint32_t seed;          /* Random_Seed */
+} gb_gemc_config;
+/* System::Init of the two boxes: wrapped coordinates, centres, the molecule
+ * lookup (box 0's molecules then box 1's), initial SystemTotal. */
+int gb_gemc_create(const gb_gemc_desc *desc, const gb_gemc_config *cfg,
+                   gb_gemc **out);
+void gb_gemc_destroy(gb_gemc *g);
+const char *gb_gemc_error(const gb_gemc *g); /* NULL: last create error */
+/* Steps [first_step, first_step + nsteps), continuing the last run.  Trace
+ * arrays may be NULL; per step trace_i5 = move kind (0 displacement, 10
+ * molecule transfer, 13 volume exchange: src/MoveConst.h), box (source box
+ * of a transfer, first box of a volume pair), molecule (-1 if none), accepted,
+ * molecules in box 0 after the step; trace_d8 = four move values
+ * (displacement: dE, overlap; transfer: new and old Rosenbluth weights, new
+ * and old trial energies; volume: the trial energies of both boxes), then
+ * the running energies and volumes of both boxes.  GB_ERR_STATE if a volume
+ * exchange would shrink a box below 2 Rcut (the reference exits there). */
+int gb_gemc_run(gb_gemc *g, int64_t first_step, int64_t nsteps,
+                int32_t *trace_i5, double *trace_d8);
+/* running inter energies, edges of both boxes, molecules in box 0, move
+ * scales (displacement, volume; per box), tries / accepted of displacement,
+ * transfer and volume per box, device time of the last run (ms) */
+int gb_gemc_state(gb_gemc *g, double *energy2, double *edges6,
+                  int32_t *n_box0, double *scales4, int64_t *counts12,
+                  double *last_ms);
+/* coordinates and centres of every molecule [n * 3] and the molecule
+ * lookup [n] (box 0's section first) */
+int gb_gemc_coords(gb_gemc *g, double *xyz, double *com, int32_t *lookup);
+/* full FP64 recompute of both boxes' inter energies (CalculateEnergy::
+ * SystemTotal, src/CalculateEnergy.cpp:83-153) */
+int gb_gemc_system_total(gb_gemc *g, double *energy2);
+
 /* ---- Reciprocal energy without device allocation ----
  * No counterpart in the reference.  It is the reduction behind BoxReciprocal
  * (src/Ewald.cpp:375-406), E = sum_k prefact[k] (sumR[k]^2 + sumI[k]^2),
