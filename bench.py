@@ -19,6 +19,10 @@ mixed   : the mixed-precision form (FP32 pair / per-k arithmetic, FP64
           accumulators), several independent chains batched on one GPU.
 serving : a stream of water jobs of mixed size through the job server
           (continuous batching), throughput and p50/p99 per-sweep latency.
+gemc    : the Gibbs-ensemble configuration (2,400 + 300 LJ spheres,
+          displacement / volume exchange / CBMC swap), both boxes in one
+          persistent launch, FP64 and mixed forms, with the host
+          restatement's rate beside it.
 roofline: the dominant kernel (the persistent chain kernel) against the
           measured FP64 pipe peak of this GPU (float64 GEMM timed here).
 
@@ -486,6 +490,93 @@ def run_drift(args, dev, engine):
             "bar": "total-energy drift <= 1e-8 relative between recomputes"}
 
 
+GEMC_CFG = dict(temperature=150.0, rcut=12.0, eps=148.0, sigma=3.73,
+                frac=(0.8, 0.01, 0.19), adj=100, cbmc_first=10, seed=3333)
+
+
+def gemc_boxes():
+    """The Gibbs-ensemble configuration: 2,400 LJ spheres in a 40 A box and
+    300 in a 90 A box at seeded non-overlapping random positions."""
+    from gomc_gb300.systems import lj_sphere_box
+    s0 = lj_sphere_box(2400, 40.0, seed=31, epsilon=GEMC_CFG["eps"],
+                       sigma=GEMC_CFG["sigma"], min_sep=2.4, name="LJ")
+    s1 = lj_sphere_box(300, 90.0, seed=32, epsilon=GEMC_CFG["eps"],
+                       sigma=GEMC_CFG["sigma"], min_sep=3.5, name="LJ")
+    return s0, s1
+
+
+def run_gemc(args, dev, engine, torch):
+    """Gibbs-ensemble NVT of LJ spheres (both boxes in one persistent
+    launch): moves/s of the FP64 and mixed forms, device time per launch of
+    --gemc-moves moves, L2 flushed between launches; the oracle's host
+    restatement of the same run as the CPU baseline."""
+    from gomc_gb300._lib import GB_FP64, GB_MIXED
+    s0, s1 = gemc_boxes()
+    g = GEMC_CFG
+    M = args.gemc_moves
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32,
+                        device=dev)
+    out = {"workload": "GEMC NVT, LJ spheres eps/kB 148 K, sigma 3.73 A, "
+                       "Rcut 12 A, T 150 K: 2,400 in 40 A + 300 in 90 A, "
+                       "displacement / volume / swap 0.8 / 0.01 / 0.19, "
+                       "10 CBMC trials, %d moves per launch" % M}
+    runs = {}
+    for name, prec in (("fp64", GB_FP64), ("mixed", GB_MIXED)):
+        gm = engine.Gemc(s0.pos, s1.pos, s0.box, s1.box, g["eps"], g["sigma"],
+                         12.0, g["temperature"], g["rcut"], g["seed"],
+                         g["frac"], g["adj"], g["cbmc_first"], precision=prec,
+                         device=dev)
+        for _ in range(args.warmup):
+            gm.run(M)
+        ms = []
+        kinds = np.zeros(3, np.int64)
+        acc = np.zeros(3, np.int64)
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize(dev)
+            r = gm.run(M, trace=True)
+            ms.append(gm.state()["last_ms"])
+            for i, k in enumerate((0, 13, 10)):
+                sel = r["kind"] == k
+                kinds[i] += int(sel.sum())
+                acc[i] += int(r["accepted"][sel].sum())
+        st = gm.state()
+        tot = gm.system_total()
+        runs[name] = {
+            "value": args.steps * M / (sum(ms) / 1e3), "unit": "moves/s",
+            "us_per_move": sum(ms) * 1e3 / (args.steps * M),
+            "launch_ms": [round(v, 3) for v in ms],
+            "moves_by_kind": {"displacement": int(kinds[0]),
+                              "volume": int(kinds[1]),
+                              "transfer": int(kinds[2])},
+            "accepted_by_kind": {"displacement": int(acc[0]),
+                                 "volume": int(acc[1]),
+                                 "transfer": int(acc[2])},
+            "molecules_box0": st["n0"],
+            "running_vs_recompute_rel": [
+                float(abs(st["energy"][b] - tot[b]) / max(abs(tot[b]), 1.0))
+                for b in range(2)]}
+        gm.close()
+    out.update(runs)
+    out["mixed_speedup_vs_fp64"] = runs["mixed"]["value"] / runs["fp64"]["value"]
+    if not args.no_cpu:
+        from oracle import oracle as O
+        ob = O.OracleGemc(s0.pos, s1.pos, s0.box, s1.box, g["eps"],
+                          g["sigma"], 12.0, g["temperature"], g["rcut"],
+                          g["seed"], g["frac"], g["adj"], g["cbmc_first"])
+        t0 = time.time()
+        done = 0
+        while time.time() - t0 < args.gemc_cpu_seconds:
+            ob.run(done, 500)
+            done += 500
+        dt = time.time() - t0
+        out["cpu_baseline"] = {"value": done / dt, "unit": "moves/s",
+                               "cores": 1, "kind": "port",
+                               "sample": "first %d moves of the same run "
+                                         "(%.1f s)" % (done, dt)}
+    return out
+
+
 def run_serving(args, dev):
     """Serving stream on one GPU, scaled down from 256 jobs x 100 sweeps
     (the longest job alone then needs 2 x 20,000 sequential moves, the tail):
@@ -626,6 +717,9 @@ def run_gb300(args, rank, world):
     serving_stats = None
     if not args.no_serving and rank == 0:
         serving_stats = run_serving(args, dev)
+    gemc_stats = None
+    if not args.no_gemc and rank == 0:
+        gemc_stats = run_gemc(args, dev, engine, torch)
     drift_run = None
     if args.drift_moves > 0 and rank == 0:
         drift_run = run_drift(args, dev, engine)
@@ -678,6 +772,7 @@ def run_gb300(args, rank, world):
         "chain_kernel_ms_per_launch": kern_ms,
         "mixed": mixed,
         "serving": serving_stats,
+        "gemc": gemc_stats,
     }
     if drift_run:
         line["mixed_drift_run"] = drift_run
@@ -712,6 +807,10 @@ def main():
     ap.add_argument("--drift-moves", type=int, default=0,
                     help="also run one mixed chain this many moves and "
                          "report the drift of every 10,000-move window")
+    ap.add_argument("--no-gemc", action="store_true")
+    ap.add_argument("--gemc-moves", type=int, default=20000,
+                    help="moves per launch of the Gibbs-ensemble line")
+    ap.add_argument("--gemc-cpu-seconds", type=float, default=5.0)
     ap.add_argument("--small", action="store_true",
                     help="256-water box instead of the 8000-water workload")
     args = ap.parse_args()
