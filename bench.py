@@ -490,6 +490,86 @@ def run_drift(args, dev, engine):
             "bar": "total-energy drift <= 1e-8 relative between recomputes"}
 
 
+MP_FRAC = (0.495, 0.495, 0.01)
+
+
+def run_multiparticle(args, dev, engine, torch, batch_chains):
+    """Config 1 with the MultiParticle move in the mix (translate / rotate /
+    MultiParticle 0.495 / 0.495 / 0.01): moves/s of the FP64 chain, of one
+    mixed chain and of the batched mixed replicas, with the device time per
+    move of each move type (chain segments, MultiParticle kernel
+    sequences: BoxForce, the full structure factor, BoxForceReciprocal)."""
+    from gomc_gb300._lib import GB_FP64, GB_MIXED
+    M = args.moves_per_step
+    steps = max(3, args.steps // 2)
+    out = {"workload": WORKLOAD.replace("translate/rotate 50/50",
+                                        "translate/rotate/MultiParticle "
+                                        "0.495/0.495/0.01"),
+           "moves_per_step": M, "steps": steps}
+
+    def timed_run(boxes, stream, batched):
+        for b in boxes:
+            b.mc_timing(reset=True)
+        step = 0
+        for _ in range(args.warmup):
+            if batched:
+                engine.mc_run_batch(boxes, step, M)
+            else:
+                boxes[0].mc_run(step, M)
+            step += M
+        for b in boxes:
+            b.mc_timing(reset=True)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            if batched:
+                engine.mc_run_batch(boxes, step, M)
+            else:
+                boxes[0].mc_run(step, M)
+            step += M
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+        tm = [b.mc_timing() for b in boxes]
+        chain_ms = sum(t["chain_ms"] for t in tm)
+        mp_ms = sum(t["mp_ms"] for t in tm)
+        chain_moves = sum(t["chain_moves"] for t in tm)
+        mp_moves = sum(t["mp_moves"] for t in tm)
+        total = steps * M * len(boxes)
+        return {"value": total / wall, "unit": "moves/s",
+                "wall_s": wall, "replicas": len(boxes),
+                "single_molecule_us_per_move":
+                    chain_ms * 1e3 / max(chain_moves, 1),
+                "multiparticle_ms_per_move": mp_ms / max(mp_moves, 1),
+                "multiparticle_moves": mp_moves,
+                "device_ms": {"chains": chain_ms, "multiparticle": mp_ms}}
+
+    sysm, cfg = make_system(0)
+    box = engine.Box(sysm, cfg, device=dev, precision=GB_FP64)
+    box.mc_init(SEED + 5, MP_FRAC, ADJ, scales=SCALES)
+    out["fp64"] = timed_run([box], None, False)
+    box.close()
+    box = engine.Box(sysm, cfg, device=dev, precision=GB_MIXED)
+    box.mc_init(SEED + 5, MP_FRAC, ADJ, scales=SCALES, recompute_freq=10000,
+                cluster_size=args.cluster or 16)
+    out["mixed_single"] = timed_run([box], None, False)
+    box.close()
+    boxes = []
+    for i in range(batch_chains):
+        s_i, c_i = make_system(2000 + i)
+        b = engine.Box(s_i, c_i, device=dev, precision=GB_MIXED)
+        b.mc_init(SEED + 2000 + i, MP_FRAC, ADJ, scales=SCALES,
+                  recompute_freq=10000, cluster_size=args.cluster or 8)
+        boxes.append(b)
+    out["mixed_batched"] = timed_run(boxes, None, True)
+    for b in boxes:
+        b.close()
+    out["note"] = ("wall-clock moves/s (host move drawing and the "
+                   "MultiParticle kernel sequences' synchronisations "
+                   "included); per-type device times from CUDA events on "
+                   "the boxes' streams")
+    return out
+
+
 GEMC_CFG = dict(temperature=150.0, rcut=12.0, eps=148.0, sigma=3.73,
                 frac=(0.8, 0.01, 0.19), adj=100, cbmc_first=10, seed=3333)
 
@@ -528,6 +608,11 @@ def run_gemc(args, dev, engine, torch):
                          device=dev)
         for _ in range(args.warmup):
             gm.run(M)
+        # where one launch's time goes (an untimed launch with the phase
+        # clocks of the cluster's first CTA)
+        gm.profile(True)
+        gm.run(M)
+        phases = gm.profile(False)
         ms = []
         kinds = np.zeros(3, np.int64)
         acc = np.zeros(3, np.int64)
@@ -553,6 +638,7 @@ def run_gemc(args, dev, engine, torch):
                                  "volume": int(acc[1]),
                                  "transfer": int(acc[2])},
             "molecules_box0": st["n0"],
+            "phase_us_per_move": phases,
             "running_vs_recompute_rel": [
                 float(abs(st["energy"][b] - tot[b]) / max(abs(tot[b]), 1.0))
                 for b in range(2)]}
@@ -720,6 +806,10 @@ def run_gb300(args, rank, world):
     gemc_stats = None
     if not args.no_gemc and rank == 0:
         gemc_stats = run_gemc(args, dev, engine, torch)
+    mp_stats = None
+    if not args.no_mp and rank == 0:
+        mp_stats = run_multiparticle(args, dev, engine, torch,
+                                     args.mp_chains)
     drift_run = None
     if args.drift_moves > 0 and rank == 0:
         drift_run = run_drift(args, dev, engine)
@@ -773,6 +863,7 @@ def run_gb300(args, rank, world):
         "mixed": mixed,
         "serving": serving_stats,
         "gemc": gemc_stats,
+        "multiparticle": mp_stats,
     }
     if drift_run:
         line["mixed_drift_run"] = drift_run
@@ -808,6 +899,10 @@ def main():
                     help="also run one mixed chain this many moves and "
                          "report the drift of every 10,000-move window")
     ap.add_argument("--no-gemc", action="store_true")
+    ap.add_argument("--no-mp", action="store_true",
+                    help="skip the line with MultiParticle moves in the mix")
+    ap.add_argument("--mp-chains", type=int, default=16,
+                    help="replicas of the batched mixed MultiParticle run")
     ap.add_argument("--gemc-moves", type=int, default=20000,
                     help="moves per launch of the Gibbs-ensemble line")
     ap.add_argument("--gemc-cpu-seconds", type=float, default=5.0)

@@ -156,6 +156,7 @@ SIGNATURES = {
     "gb_gemc_state": (C.c_int, [_P, _D, _D, _I, _D, _L, _D]),
     "gb_gemc_coords": (C.c_int, [_P, _D, _D, _I]),
     "gb_gemc_system_total": (C.c_int, [_P, _D]),
+    "gb_gemc_profile": (C.c_int, [_P, C.c_int32, _D, _L]),
     "gb_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P)]),
     "gb_server_destroy": (None, [_P]),
     "gb_server_submit": (C.c_int, [_P, C.POINTER(SystemDesc),

@@ -107,7 +107,10 @@ int checkpoint_save(Box &b, void *buf, int64_t bytes) {
   if (b.mc) {
     McState &s = *b.mc;
     McBlock m;
-    s.stream->mt().Save(m.mt, &m.mt_left, &m.mt_next);
+    int32_t left = 0, next = 0;
+    stream_state_at_next(s, m.mt, &left, &next);
+    m.mt_left = left;
+    m.mt_next = next;
     if ((rc = b.CudaCheck(cudaMemcpy(&m.set, s.d_set, sizeof(Settings),
                                      cudaMemcpyDeviceToHost),
                           "checkpoint read")))
@@ -208,6 +211,8 @@ int checkpoint_load(Box &b, const void *buf, int64_t bytes) {
   if (h.has_mc) {
     McState &s = *b.mc;
     s.stream->mt().Load(m.mt, m.mt_left, m.mt_next);
+    s.ahead.clear();  // records drawn ahead belong to the old position
+    s.ahead_pos = 0;
     s.next_step = h.next_step;
     if ((rc = b.CudaCheck(cudaMemcpy(s.d_set, &m.set, sizeof(Settings),
                                      cudaMemcpyHostToDevice),

@@ -63,6 +63,8 @@ struct Move {
   double nax[2][3], nhalf[2][3], nvol[2], nvolInv[2], sc[2][3];  // volume
   double d[4];             // values reported in the trace
   double tot[PMAX];        // cluster sums of the partials
+  unsigned words[6 * GEMC_NTMAX];  // raw words of the transfer's trials
+  double wts[2 * GEMC_NTMAX];      // trial weights
 };
 
 struct GemcShared {
@@ -374,6 +376,16 @@ __global__ void __launch_bounds__(GEMC_THREADS)
   __syncthreads();
   cluster.sync();
 
+  const bool prof = p.prof && rank == 0 && tid == 0;
+  long long pacc[3][5] = {}, pcnt[3] = {0, 0, 0};
+  long long tclk = prof ? clock64() : 0;
+  auto mark = [&](int slot, int ph) {
+    if (prof && slot >= 0) {
+      long long now = clock64();
+      pacc[slot][ph] += now - tclk;
+      tclk = now;
+    }
+  };
   for (int t = 0; t < p.nsteps; ++t) {
     const long long step = p.first + t;
     const int par = t & 1;
@@ -443,27 +455,27 @@ __global__ void __launch_bounds__(GEMC_THREADS)
         // destination box, PickWeighted), DCSingle::BuildOld (trials in the
         // source box, trial 0 at the molecule)
         (void)R.randInt(1);
-        for (int k = 0; k < nt; ++k) {
-          double vx = R.randExc01() * c.ax[b1][0];
-          double vy = R.randExc01() * c.ax[b1][1];
-          double vz = R.randExc01() * c.ax[b1][2];
-          if (lane == 0) {
-            M.tr[k][0] = vx;
-            M.tr[k][1] = vy;
-            M.tr[k][2] = vz;
-          }
+        // the trials' raw words in order (new trials, PickWeighted's word,
+        // old trials), then each lane scales its own coordinates
+        unsigned *wbuf = M.words;
+        for (int k = 0; k < 3 * nt; ++k) {
+          unsigned w = R.u32();
+          if (lane == 0)
+            wbuf[k] = w;
         }
         pick_word = R.u32();
-        for (int k = 0; k < nt; ++k) {
-          double vx = R.randExc01() * c.ax[b][0];
-          double vy = R.randExc01() * c.ax[b][1];
-          double vz = R.randExc01() * c.ax[b][2];
-          if (lane == 0) {
-            M.tr[nt + k][0] = vx;
-            M.tr[nt + k][1] = vy;
-            M.tr[nt + k][2] = vz;
-          }
+        for (int k = 0; k < 3 * nt; ++k) {
+          unsigned w = R.u32();
+          if (lane == 0)
+            wbuf[3 * nt + k] = w;
         }
+        __syncwarp();
+        for (int q = lane; q < 6 * nt; q += 32) {
+          const int k = q / 3, d = q - 3 * k;
+          const double ax = k < nt ? c.ax[b1][d] : c.ax[b][d];
+          M.tr[k][d] = (double)wbuf[q] * (1.0 / 4294967296.0) * ax;
+        }
+        __syncwarp();
         if (lane == 0) {
           M.tr[nt][0] = wrapd(A.px[m], c.ax[b][0]);
           M.tr[nt][1] = wrapd(A.py[m], c.ax[b][1]);
@@ -528,6 +540,9 @@ __global__ void __launch_bounds__(GEMC_THREADS)
     if (c.err)
       break;  // every CTA drew the same volume change
     const int kind = M.kind, b = M.b, b1 = M.b1, m = M.m;
+    const int pslot = kind == GEMC_DISPLACE ? 0 : kind == GEMC_TRANSFER ? 1
+                      : kind == GEMC_VOLUME ? 2 : -1;
+    mark(pslot, 0);
     int nval = 0;
     // ---------------- energy phase (all CTAs) ----------------
     float lt[2][3];
@@ -573,9 +588,12 @@ __global__ void __launch_bounds__(GEMC_THREADS)
       // its box's cell list): new trials in the destination box, old trials
       // in the source box
       nval = 3 * nt;
-      for (int k = 0; k < 2 * nt; ++k) {
+      // one warp per trial, over this CTA's slice of the trial's box
+      for (int k = warp; k < 2 * nt; k += NW) {
         const int bb = k < nt ? b1 : b;
         const int a0 = first_of(c, bb), nb = count_of(c, n, bb);
+        const int lo = (int)((long long)nb * rank / C);
+        const int hi = (int)((long long)nb * (rank + 1) / C);
         double sx = M.tr[k][0], sy = M.tr[k][1], sz = M.tr[k][2];
         unsigned ux = 0, uy = 0, uz = 0;
         if (MIXED) {
@@ -585,7 +603,7 @@ __global__ void __launch_bounds__(GEMC_THREADS)
         }
         double acc = 0.0;
         int ovl = 0;
-        for (int i = gt; i < nb; i += G) {
+        for (int i = lo + lane; i < hi; i += 32) {
           int j = A.lookup[a0 + i];
           if (j == m)
             continue;
@@ -593,9 +611,15 @@ __global__ void __launch_bounds__(GEMC_THREADS)
                             (float)sz, ux, uy, uz, MIXED ? lt[bb] : nullptr,
                             acc, ovl);
         }
-        warp_put(S, k, acc);
-        if (k < nt)
-          warp_put(S, 2 * nt + k, (double)ovl);
+        for (int o = 16; o > 0; o >>= 1) {
+          acc += __shfl_down_sync(0xffffffffu, acc, o);
+          ovl += __shfl_down_sync(0xffffffffu, ovl, o);
+        }
+        if (lane == 0) {
+          S.part[par][k] = acc;
+          if (k < nt)
+            S.part[par][2 * nt + k] = (double)ovl;
+        }
       }
     } else if (kind == GEMC_VOLUME) {
       // Coordinates::TranslateOneBox for both boxes into the trial arrays,
@@ -707,8 +731,10 @@ __global__ void __launch_bounds__(GEMC_THREADS)
       warp_put(S, 1, eb[1]);
     }
     __syncthreads();
-    // this CTA's partials, warps in order
-    if (tid < nval) {
+    mark(pslot, 1);
+    // this CTA's partials, warps in order (a transfer's trials went straight
+    // to their slots)
+    if (tid < nval && kind != GEMC_TRANSFER) {
       double v = 0.0;
       for (int w = 0; w < NW; ++w)
         v += S.wred[w][tid];
@@ -718,12 +744,20 @@ __global__ void __launch_bounds__(GEMC_THREADS)
     asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
     asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
     if (tid < nval) {
+      // the ranks' partials loaded together, added in rank order
+      double pr[16];
+#pragma unroll
+      for (int r = 0; r < 16; ++r)
+        pr[r] = r < C ? cluster.map_shared_rank(&S.part[par][0],
+                                                (unsigned)r)[tid]
+                      : 0.0;
       double v = 0.0;
       for (int r = 0; r < C; ++r)
-        v += cluster.map_shared_rank(&S.part[par][0], (unsigned)r)[tid];
+        v += pr[r];
       M.tot[tid] = v;
     }
     __syncthreads();
+    mark(pslot, 2);
     // ---------------- decision (identical in every CTA) ----------------
     if (warp == 0) {
       MtCursor R{c.mt, c.mt_left, c.mt_next};
@@ -749,9 +783,15 @@ __global__ void __launch_bounds__(GEMC_THREADS)
         }
       } else if (kind == GEMC_TRANSFER) {
         if (M.ok) {
+          // the Boltzmann weights of all trials, one lane each, then added
+          // in trial order
+          double *wv = M.wts;
+          for (int k = lane; k < 2 * nt; k += 32)
+            wv[k] = exp(-1 * p.beta * ((0.0 + M.tot[k]) + 0.0));
+          __syncwarp();
           double stepWeight = 0.0, w[GEMC_NTMAX];
           for (int k = 0; k < nt; ++k) {
-            w[k] = exp(-1 * p.beta * ((0.0 + M.tot[k]) + 0.0));
+            w[k] = wv[k];
             stepWeight += w[k];
           }
           // PRNG::PickWeighted (src/PRNG.h:167-200)
@@ -776,7 +816,7 @@ __global__ void __launch_bounds__(GEMC_THREADS)
           double Wn = 1.0 * (stepWeight / nt);
           double sumOld = 0.0;
           for (int k = 0; k < nt; ++k)
-            sumOld += exp(-1 * p.beta * ((0.0 + M.tot[nt + k]) + 0.0));
+            sumOld += wv[nt + k];
           double Wo = 1.0 * (sumOld / nt);
           double eNew = 0.0 + M.tot[winner], eOld = 0.0 + M.tot[nt];
           int nsrc = count_of(c, n, b), ndest = count_of(c, n, b1);
@@ -830,6 +870,7 @@ __global__ void __launch_bounds__(GEMC_THREADS)
       }
     }
     __syncthreads();
+    mark(pslot, 3);
     // ---------------- commit ----------------
     const int acc = S.accept;
     if (acc && kind == GEMC_DISPLACE) {
@@ -939,6 +980,16 @@ __global__ void __launch_bounds__(GEMC_THREADS)
       td[7] = c.vol[1];
     }
     __syncthreads();
+    mark(pslot, 4);
+    if (prof && pslot >= 0)
+      pcnt[pslot]++;
+  }
+  if (prof) {
+    for (int k = 0; k < 3; ++k) {
+      for (int ph = 0; ph < 5; ++ph)
+        p.prof[5 * k + ph] += pacc[k][ph];
+      p.prof[15 + k] += pcnt[k];
+    }
   }
   // ---- write the state back (CTA 0) ----
   __syncthreads();
@@ -1332,6 +1383,7 @@ int gb_gemc_run(gb_gemc *h, int64_t first_step, int64_t nsteps,
   }
   g.p.tr_i = trace ? g.d_tr_i : nullptr;
   g.p.tr_d = trace ? g.d_tr_d : nullptr;
+  g.p.prof = g.profile ? g.d_prof : nullptr;
   g.p.first = first_step;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaEventCreate(&e0);
@@ -1426,6 +1478,41 @@ int gb_gemc_coords(gb_gemc *h, double *xyz, double *com, int32_t *lookup) {
         com[3 * i + d] = t[(size_t)(3 + d) * n + i];
     }
   return gb::OK;
+}
+
+int gb_gemc_profile(gb_gemc *h, int32_t enable, double *us15,
+                    int64_t *moves3) {
+  using namespace gb;
+  if (!h)
+    return ERR_ARG;
+  Gemc &g = h->g;
+  int rc;
+  cudaSetDevice(g.device);
+  if (!g.d_prof) {
+    if ((rc = gemc_alloc(g, &g.d_prof, 18)) ||
+        (rc = g.CudaCheck(cudaMemsetAsync(g.d_prof, 0, 18 * sizeof(long long),
+                                          g.stream),
+                          "memset")))
+      return rc;
+  }
+  long long hp[18];
+  if ((rc = g.CudaCheck(cudaMemcpyAsync(hp, g.d_prof, sizeof hp,
+                                        cudaMemcpyDeviceToHost, g.stream),
+                        "download")) ||
+      (rc = g.CudaCheck(cudaMemsetAsync(g.d_prof, 0, sizeof hp, g.stream),
+                        "memset")) ||
+      (rc = g.CudaCheck(cudaStreamSynchronize(g.stream), "sync")))
+    return rc;
+  int khz = 0;
+  cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, g.device);
+  for (int k = 0; k < 15; ++k)
+    if (us15)
+      us15[k] = khz > 0 ? (double)hp[k] / (khz * 1e-3) : 0.0;
+  for (int k = 0; k < 3; ++k)
+    if (moves3)
+      moves3[k] = hp[15 + k];
+  g.profile = enable != 0;
+  return OK;
 }
 
 int gb_gemc_system_total(gb_gemc *h, double *energy2) {

@@ -46,6 +46,10 @@ struct GemcParams {
   int nsteps;
   int *tr_i;     // per step: kind, box, molecule, accepted, molecules in box 0
   double *tr_d;  // per step: four move values, energies, volumes
+  // phase clocks of CTA 0 (NULL: not collected): [kind slot 0 displacement,
+  // 1 transfer, 2 volume][phase: draw, energies, exchange, decision,
+  // commit], then the moves of each kind slot
+  long long *prof;
 };
 
 struct Gemc {
@@ -62,6 +66,8 @@ struct Gemc {
   size_t trace_cap = 0;
   double *d_tot = nullptr;  // recompute output
   float last_ms = 0.0f;     // device time of the last run
+  long long *d_prof = nullptr;  // phase clocks (gb_gemc_profile)
+  bool profile = false;
   int Fail(int code, const std::string &msg) {
     last_error = msg;
     return code;

@@ -1609,6 +1609,7 @@ void mc_destroy(Box &b) {
   if (s.h_desc)
     cudaFreeHost(s.h_desc);
   delete s.stream;
+  delete s.ahead_from;
   delete b.mc;
   b.mc = nullptr;
 }
@@ -1773,10 +1774,64 @@ int mc_init(Box &b, const gb_mc_params &p) {
 }
 
 // Draw moves up to `step` without running them (restart at a later step).
+void draw_next(McState &s, MoveRec *r) {
+  if (s.ahead_pos < s.ahead.size()) {
+    *r = s.ahead[s.ahead_pos++];
+    if (s.ahead_pos == s.ahead.size()) {
+      s.ahead.clear();
+      s.ahead_pos = 0;
+    }
+    return;
+  }
+  s.stream->Next(r);
+}
+
+// Single-molecule moves before box s's next MultiParticle move, at most
+// cap; the records it draws to see that wait in s.ahead.
+static int64_t singles_ahead(McState &s, int64_t cap) {
+  if (s.params.frac[2] <= 0)
+    return cap;
+  int64_t k = 0;
+  for (; k < cap; ++k) {
+    size_t idx = s.ahead_pos + (size_t)k;
+    if (idx >= s.ahead.size()) {
+      if (s.ahead.size() == s.ahead_pos) {
+        // the first record drawn ahead: keep the stream's position
+        if (!s.ahead_from)
+          s.ahead_from = new MoveStream(*s.stream);
+        else
+          *s.ahead_from = *s.stream;
+        s.ahead.clear();
+        s.ahead_pos = 0;
+        idx = 0;
+      }
+      MoveRec r;
+      s.stream->Next(&r);
+      s.ahead.push_back(r);
+    }
+    if (s.ahead[idx].kind == 2)
+      break;
+  }
+  return k;
+}
+
+void stream_state_at_next(McState &s, uint32_t st[624], int32_t *left,
+                          int32_t *next) {
+  if (s.ahead_pos >= s.ahead.size()) {
+    s.stream->mt().Save(st, left, next);
+    return;
+  }
+  MoveStream tmp(*s.ahead_from);
+  MoveRec r;
+  for (size_t i = 0; i < s.ahead_pos; ++i)
+    tmp.Next(&r);
+  tmp.mt().Save(st, left, next);
+}
+
 static void skip_to(McState &s, int64_t step) {
   MoveRec r;
   while (s.next_step < step) {
-    s.stream->Next(&r);
+    draw_next(s, &r);
     s.next_step++;
   }
 }
@@ -2084,7 +2139,7 @@ int mc_run(Box &b, int64_t first, int64_t nsteps, int32_t *kind, int32_t *mol,
     if ((rc = b.Sync()))  // the previous chunk may still read h_moves
       return rc;
     for (int64_t i = 0; i < chunk; ++i)
-      s.stream->Next(&s.h_moves[i]);
+      draw_next(s, &s.h_moves[i]);
     s.next_step += chunk;
     if ((rc = b.CudaCheck(cudaMemcpyAsync(s.d_moves, s.h_moves,
                                           chunk * sizeof(MoveRec),
@@ -2227,7 +2282,7 @@ int mixed_launch(const std::vector<Box *> &boxes,
       if ((rc = b.Sync()))  // h_moves is free
         return rc;
       for (int64_t t = 0; t < m; ++t)
-        s.stream->Next(&s.h_moves[t]);
+        draw_next(s, &s.h_moves[t]);
       if ((rc = b.CudaCheck(cudaMemcpyAsync(s.d_moves, s.h_moves,
                                             m * sizeof(MoveRec),
                                             cudaMemcpyHostToDevice, L.stream),
@@ -2337,18 +2392,56 @@ int64_t mixed_segment_limit(Box &b, int64_t cap) {
   int64_t R = s.params.recompute_freq;
   if (R > 0)
     m = std::min(m, R - s.next_step % R);
-  return m;
+  // a chain segment ends before the box's next MultiParticle move
+  return singles_ahead(s, m);
+}
+
+// Run fn(i) for every listed box on up to four helper threads (each box's
+// work waits on its own stream only); the first error is returned.
+template <class F>
+static int for_boxes_concurrently(const std::vector<Box *> &boxes,
+                                  const std::vector<size_t> &idx, F fn) {
+  if (idx.empty())
+    return OK;
+  if (idx.size() == 1)
+    return fn(idx[0]);
+  const int dev = boxes[idx[0]]->cfg.device;
+  const int nt = (int)std::min<size_t>(idx.size(), 4);
+  std::vector<int> rcs(idx.size(), OK);
+  std::atomic<size_t> next{0};
+  auto worker = [&] {
+    cudaError_t e = cudaSetDevice(dev);
+    for (size_t k; (k = next++) < idx.size();)
+      rcs[k] = e != cudaSuccess ? boxes[idx[k]]->CudaCheck(e, "cudaSetDevice")
+                                : fn(idx[k]);
+  };
+  std::vector<std::thread> th;
+  for (int k = 0; k < nt; ++k) {
+    try {
+      th.emplace_back(worker);
+    } catch (const std::system_error &) {
+      break;
+    }
+  }
+  if (th.empty())
+    worker();
+  for (auto &x : th)
+    x.join();
+  for (int r : rcs)
+    if (r)
+      return r;
+  return OK;
 }
 
 int mc_run_batch(const std::vector<Box *> &boxes, int64_t first,
                  int64_t nsteps) {
-  // FP64 boxes, boxes with MultiParticle moves or a single box run one after
+  // FP64 boxes, boxes on several devices or a single box run one after
   // another through mc_run.
   bool all_mixed = boxes.size() > 1;
   for (Box *b : boxes) {
     if (!b->mc)
       return b->Fail(ERR_STATE, "gb_mc_init has not been called");
-    if (b->cfg.precision != GB_MIXED || b->mc->params.frac[2] > 0)
+    if (b->cfg.precision != GB_MIXED)
       all_mixed = false;
     if (b->cfg.device != boxes[0]->cfg.device)
       all_mixed = false;
@@ -2370,18 +2463,44 @@ int mc_run_batch(const std::vector<Box *> &boxes, int64_t first,
   std::vector<int64_t> left(boxes.size(), nsteps), n(boxes.size());
   std::vector<Box *> leaders;
   for (;;) {
-    bool any = false;
+    bool any = false, more = false;
     for (size_t i = 0; i < boxes.size(); ++i) {
       n[i] = left[i] > 0 ? mixed_segment_limit(*boxes[i], left[i]) : 0;
       any = any || n[i] > 0;
+      more = more || left[i] > 0;
     }
-    if (!any)
+    if (!more)
       break;
-    if ((rc = mixed_launch(boxes, n, &leaders)) ||
-        (rc = mixed_complete(boxes, n, leaders)))
-      return rc;
+    if (any) {
+      if ((rc = mixed_launch(boxes, n, &leaders)) ||
+          (rc = mixed_complete(boxes, n, leaders)))
+        return rc;
+      for (size_t i = 0; i < boxes.size(); ++i)
+        left[i] -= n[i];
+    }
+    // boxes whose next move is a MultiParticle move run it now, several at
+    // once (each a kernel sequence on its own stream), with the periodic
+    // FP64 recompute that falls due after it
+    std::vector<size_t> mp;
     for (size_t i = 0; i < boxes.size(); ++i)
-      left[i] -= n[i];
+      if (left[i] > 0 && singles_ahead(*boxes[i]->mc, 1) == 0)
+        mp.push_back(i);
+    rc = for_boxes_concurrently(boxes, mp, [&](size_t i) {
+      Box &b = *boxes[i];
+      McState &s = *b.mc;
+      MoveRec r;
+      draw_next(s, &r);
+      const int64_t step = s.next_step++;
+      int e = run_mp(b, s, step, r.mol, nullptr, nullptr);
+      const int64_t R = s.params.recompute_freq;
+      if (!e && R > 0 && (step + 1) % R == 0)
+        e = recompute_fp64(b, s);
+      return e;
+    });
+    if (rc)
+      return rc;
+    for (size_t i : mp)
+      left[i] -= 1;
   }
   return OK;
 }

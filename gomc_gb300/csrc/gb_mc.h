@@ -86,6 +86,13 @@ struct McState {
   int64_t recomputes = 0;
   MoveStream *stream = nullptr;
   int64_t next_step = 0;     // step the stream is positioned at
+  // moves drawn ahead of next_step (batched runs look ahead for the next
+  // MultiParticle move, where a box's chain segment has to end), and a copy
+  // of the stream from before the first of them (checkpoints save the
+  // generator's position at next_step)
+  std::vector<MoveRec> ahead;
+  size_t ahead_pos = 0;
+  MoveStream *ahead_from = nullptr;
   Settings *d_set = nullptr; // device copy of Settings
   MoveRec *d_moves = nullptr;
   MoveRec *h_moves = nullptr;  // pinned
@@ -166,6 +173,11 @@ int mixed_complete(const std::vector<Box *> &boxes,
                    std::vector<char> *due = nullptr);
 int mc_recompute(Box &b);
 int64_t mixed_segment_limit(Box &b, int64_t cap);
+// The next move record of box b's stream (drawn-ahead records first).
+void draw_next(McState &s, MoveRec *r);
+// The MT19937 state of the stream positioned at next_step.
+void stream_state_at_next(McState &s, uint32_t st[624], int32_t *left,
+                          int32_t *next);
 void mc_destroy(Box &b);
 
 // Timed choice of the mixed chain's cluster size (gb_tune.cu)

@@ -573,6 +573,21 @@ class Gemc:
         self._chk(lib().gb_gemc_system_total(self.h, _dp(e)))
         return e
 
+    def profile(self, enable: bool = True) -> dict:
+        """Phase clocks since the last call (us per kind and phase) and the
+        moves of each kind; switches collection on or off."""
+        us = np.empty((3, 5))
+        mv = np.empty(3, np.int64)
+        self._chk(lib().gb_gemc_profile(self.h, int(enable), _dp(us),
+                                        mv.ctypes.data_as(
+                                            C.POINTER(C.c_int64))))
+        kinds = ("displacement", "transfer", "volume")
+        phases = ("draw", "energies", "exchange", "decision", "commit")
+        return {k: dict(moves=int(mv[i]),
+                        us_per_move={ph: float(us[i, j] / max(mv[i], 1))
+                                     for j, ph in enumerate(phases)})
+                for i, k in enumerate(kinds)}
+
 
 def mc_run_batch(boxes: Sequence[Box], first_step: int, nsteps: int) -> None:
     arr = (C.c_void_p * len(boxes))(*[b.h for b in boxes])

@@ -459,6 +459,14 @@ int gb_gemc_coords(gb_gemc *g, double *xyz, double *com, int32_t *lookup);
 /* full FP64 recompute of both boxes' inter energies (CalculateEnergy::
  * SystemTotal, src/CalculateEnergy.cpp:83-153) */
 int gb_gemc_system_total(gb_gemc *g, double *energy2);
+/* Where the device time of the move loop goes (no reference counterpart):
+ * the clocks of the cluster's first CTA since the last call, per move kind
+ * (displacement, transfer, volume) and phase (drawing the random numbers,
+ * pair energies, exchange of the partials, decision, commit), as us15 in
+ * microseconds at the rated SM clock, and the moves of each kind; `enable`
+ * switches the collection on or off for the following runs. */
+int gb_gemc_profile(gb_gemc *g, int32_t enable, double *us15,
+                    int64_t *moves3);
 
 /* ---- Reciprocal energy without device allocation ----
  * No counterpart in the reference.  It is the reduction behind BoxReciprocal

@@ -92,7 +92,12 @@ def test_mixed_drift_between_recomputes(gb):
     b.close()
 
 
-def test_batch_matches_alone(gb):
+@pytest.mark.parametrize("frac", [[0.5, 0.5, 0.0], [0.47, 0.47, 0.06]])
+def test_batch_matches_alone(gb, frac):
+    """Boxes of uneven size batched in one launch per segment end where each
+    runs alone; with MultiParticle moves in the mix, a box's segment ends
+    before its next MultiParticle move, which runs beside the other boxes'
+    (each on its own stream)."""
     sizes = [(256, 19.7, 9.0), (2000, 39.1, 10.0), (1000, 31.0, 10.0)]
 
     def boxes(seed0):
@@ -101,7 +106,7 @@ def test_batch_matches_alone(gb):
             b = make(gb, n, L, rc, gb.GB_MIXED, seed=seed0 + i)
             # an FP64 recompute every 200 moves: the batched run makes
             # several boxes' recomputes at once
-            b.mc_init(500 + i, [0.5, 0.5, 0.0], 300, scales=SCALES,
+            b.mc_init(500 + i, frac, 300, scales=SCALES,
                       cluster_size=8, recompute_freq=200)
             out.append(b)
         return out
@@ -120,8 +125,19 @@ def test_batch_matches_alone(gb):
         sm, cm = m.mc_state()
         np.testing.assert_array_equal(sm, sa)
         np.testing.assert_array_equal(cm, ca)
+        if frac[2] > 0:
+            assert cm[4] > 0  # MultiParticle moves ran
         dm, da = m.mc_drift(), a.mc_drift()
         assert dm == da and dm["recomputes"] == 3
+    # a checkpoint taken between batched runs (records drawn ahead pending)
+    # resumes the box's own stream where it stands
+    blob = mixed[0].checkpoint()
+    gb.mc_run_batch(mixed, 700, 150)
+    want = (mixed[0].coords(), mixed[0].energy())
+    mixed[0].restore(blob)
+    mixed[0].mc_run(700, 150)
+    np.testing.assert_array_equal(mixed[0].coords(), want[0])
+    np.testing.assert_array_equal(mixed[0].energy(), want[1])
     for b in alone + mixed:
         b.close()
 
