@@ -53,14 +53,23 @@ constexpr double TARGET = 0.5;            // MoveSettings::TARGET_ACCEPT_FRACT
 constexpr double TINY = 1.0e-7;           // MoveSettings::TINY_AMOUNT
 constexpr double TURN = 4294967296.0;
 
-// One move as warp 0 drew it.
+constexpr int WQ = 96;  // per-warp queue of FP64 pair candidates
+
+// One move as warp 0 drew it, with what every warp needs of it in the
+// number formats its pair loop uses.
 struct Move {
   int kind, b, b1, m, ok;
   double u_acc;            // acceptance uniform (displacement, volume)
   unsigned pick_word;      // raw word of PickWeighted (transfer)
-  double nx, ny, nz, ncx, ncy, ncz;  // displacement: new position, centre
+  double np[3], nc[3];     // displacement: new position; centre (CTA 0)
+  float nf[3];             // its FP32 copy
+  unsigned nt[3];          // its fixed-point turns (mixed form)
   double tr[2 * GEMC_NTMAX][3];     // transfer: new trials, then old trials
+  float trf[2 * GEMC_NTMAX][3];
+  unsigned trt[2 * GEMC_NTMAX][3];
   double nax[2][3], nhalf[2][3], nvol[2], nvolInv[2], sc[2][3];  // volume
+  float vcut[2];           // volume: FP32 pre-filter of the old distances
+  float nlt[2][3];         // volume: FP32 turn lengths at the new edges
   double d[4];             // values reported in the trace
   double tot[PMAX];        // cluster sums of the partials
   unsigned words[6 * GEMC_NTMAX];  // raw words of the transfer's trials
@@ -70,8 +79,12 @@ struct Move {
 struct GemcShared {
   GemcCtl c;
   Move mv;
+  float axf[2][3], halff[2][3], ltf[2][3];  // FP32 edges, half edges, turns
+  float pcut[2];  // FP32 distance pre-filter (FP64 form): Rcut with room
+                  // for the FP32 copies' rounding, L 2^-24 per coordinate
   double part[2][PMAX];       // this CTA's partials, by move parity
-  double wred[NW][PMAX];
+  double wred[NW][2];         // per-warp sums (displacement, volume)
+  int2 wq[NW][WQ];            // per-warp FP64 candidate queues
   int accept;
 };
 
@@ -283,54 +296,115 @@ struct Arrays {
   }
 };
 
-// Pair energy of particle j (box b) with a point given by FP64 position
-// (sx, sy, sz) / FP32 copy / turns; adds to acc, counts RcutLow overlaps.
-template <bool MIXED>
-__device__ __forceinline__ void pair_point(const GemcParams &p,
-                                           const GemcCtl &c, const Arrays<MIXED> &A,
-                                           int b, int j, double sx, double sy,
-                                           double sz, float fxp, float fyp,
-                                           float fzp, unsigned txp,
-                                           unsigned typ, unsigned tzp,
-                                           const float *lt, double &acc,
-                                           int &ovl) {
-  if (!MIXED) {
-    float dx = mimgf(fxp - A.fx[j], (float)c.ax[b][0], (float)c.half[b][0]);
-    float dy = mimgf(fyp - A.fy[j], (float)c.ax[b][1], (float)c.half[b][1]);
-    float dz = mimgf(fzp - A.fz[j], (float)c.ax[b][2], (float)c.half[b][2]);
-    float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    if (r2 < p.rcutSq_f) {
-      double ex = mimg(sx - A.px[j], c.ax[b][0], c.half[b][0]);
-      double ey = mimg(sy - A.py[j], c.ax[b][1], c.half[b][1]);
-      double ez = mimg(sz - A.pz[j], c.ax[b][2], c.half[b][2]);
-      double d2 = ex * ex + ey * ey + ez * ez;
-      if (d2 < p.rcutSq) {
-        if (d2 < p.rcutLowSq)
-          ++ovl;
-        acc += lj64(p, d2);
-      }
+// FP32 copies of the box edges for the pair loops (after every change).
+__device__ void box_consts(GemcShared &S, double rcut) {
+  for (int b = 0; b < 2; ++b) {
+    for (int d = 0; d < 3; ++d) {
+      S.axf[b][d] = (float)S.c.ax[b][d];
+      S.halff[b][d] = (float)S.c.half[b][d];
+      S.ltf[b][d] = (float)(S.c.ax[b][d] / TURN);
     }
-  } else {
-    float dx = (float)(int)(txp - A.tx[j]) * lt[0];
-    float dy = (float)(int)(typ - A.ty[j]) * lt[1];
-    float dz = (float)(int)(tzp - A.tz[j]) * lt[2];
-    float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    if (r2 < p.rcutSq_f) {
-      if (r2 < (float)p.rcutLowSq)
-        ++ovl;
-      acc += (double)lj32(p, r2);
-    }
+    const double lmax =
+        fmax(S.c.ax[b][0], fmax(S.c.ax[b][1], S.c.ax[b][2]));
+    const double r = rcut + 1e-5 * lmax + 1e-4;
+    S.pcut[b] = (float)(r * r);
   }
 }
 
-// Warp sum, then the CTA's warps in order into wred[.][slot] (lane 0).
-__device__ __forceinline__ void warp_put(GemcShared &S, int slot, double v) {
+// Error-free FP32 accumulation: (hi, lo) += v.
+__device__ __forceinline__ void two_sum_add(float &hi, float &lo, float v) {
+  float s = hi + v;
+  float bp = s - hi;
+  float err = (hi - (s - bp)) + (v - bp);
+  hi = s;
+  lo += err;
+}
+// Warp sum of a float-float pair, to lane 0.
+__device__ __forceinline__ void warp_two_sum(float &hi, float &lo) {
+  for (int o = 16; o > 0; o >>= 1) {
+    float h2 = __shfl_down_sync(0xffffffffu, hi, o);
+    float l2 = __shfl_down_sync(0xffffffffu, lo, o);
+    two_sum_add(hi, lo, h2);
+    lo += l2;
+  }
+}
+__device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1)
     v += __shfl_down_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0)
-    S.wred[threadIdx.x >> 5][slot] = v;
+  return v;
+}
+__device__ __forceinline__ int warp_sum_i(int v) {
+  for (int o = 16; o > 0; o >>= 1)
+    v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float r2_turns(unsigned ax, unsigned ay,
+                                          unsigned az, unsigned bx,
+                                          unsigned by, unsigned bz,
+                                          const float *lt) {
+  float dx = (float)(int)(ax - bx) * lt[0];
+  float dy = (float)(int)(ay - by) * lt[1];
+  float dz = (float)(int)(az - bz) * lt[2];
+  return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+__device__ __forceinline__ float r2_f32(float ax, float ay, float az,
+                                        float bx, float by, float bz,
+                                        const float *L, const float *H) {
+  float dx = mimgf(ax - bx, L[0], H[0]);
+  float dy = mimgf(ay - by, L[1], H[1]);
+  float dz = mimgf(az - bz, L[2], H[2]);
+  return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+__device__ __forceinline__ double r2_f64(double ax, double ay, double az,
+                                         double bx, double by, double bz,
+                                         const double *L, const double *H) {
+  double ex = mimg(ax - bx, L[0], H[0]);
+  double ey = mimg(ay - by, L[1], H[1]);
+  double ez = mimg(az - bz, L[2], H[2]);
+  return ex * ex + ey * ey + ez * ez;
 }
 
+// Evaluates a warp's queued candidates 32 at a time, in queue order (all:
+// also the last partial group), and moves the rest to the queue's front.
+// Between flushes a warp adds at most 64 entries to fewer than 32, so the
+// queue never holds more than 95.
+template <class F>
+__device__ __forceinline__ void qflush(int2 *q, int &qn, bool all, int lane,
+                                       F &eval) {
+  while (qn >= 32 || (all && qn > 0)) {
+    __syncwarp();
+    if (lane < qn)
+      eval(q[lane]);
+    const int rest = qn > 32 ? qn - 32 : 0;
+    int2 a = make_int2(0, 0), a2 = make_int2(0, 0);
+    if (lane < rest)
+      a = q[32 + lane];
+    if (lane + 32 < rest)
+      a2 = q[64 + lane];
+    __syncwarp();
+    if (lane < rest)
+      q[lane] = a;
+    if (lane + 32 < rest)
+      q[lane + 32] = a2;
+    __syncwarp();
+    qn = rest;
+  }
+}
+
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// The Gibbs-ensemble loop (src/moves/*.h of the GEMC build; the move
+// sequence of System::RunningCheck / ChooseAndRunMove): warp 0 of every CTA
+// draws the move from its copy of the MT19937 state, every CTA evaluates
+// its slice of the pair terms, the partials meet over distributed shared
+// memory, and every CTA takes the same decision.
+//   FP64 form: an FP32 distance pre-filter queues the candidate pairs of
+//   each warp in order; the queue is evaluated in FP64 on full warps.
+//   Mixed form: FP32 pair energies on exact fixed-point separations, summed
+//   error-free in float-float, one FP64 value per warp.
 template <bool MIXED>
 __global__ void __launch_bounds__(GEMC_THREADS)
     k_gemc(const GemcParams p) {
@@ -340,7 +414,7 @@ __global__ void __launch_bounds__(GEMC_THREADS)
   const int C = (int)cluster.num_blocks();
   const int rank = (int)cluster.block_rank();
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int gt = rank * GEMC_THREADS + tid, G = C * GEMC_THREADS;
+  const unsigned lt_mask = (1u << lane) - 1u;
   const int n = p.n, nt = p.nt;
   Arrays<MIXED> A(dyn + (sizeof(GemcShared) + 15) / 16 * 16, n);
   GemcCtl &c = S.c;
@@ -353,9 +427,10 @@ __global__ void __launch_bounds__(GEMC_THREADS)
       dst[i] = src[i];
   }
   __syncthreads();
-  for (int i = tid; i < n; i += GEMC_THREADS) {
+  if (tid == 0)
+    box_consts(S, p.rcut);
+  for (int i = tid; i < n; i += GEMC_THREADS)
     A.lookup[i] = p.lookup[i];
-  }
   __syncthreads();
   for (int i = tid; i < n; i += GEMC_THREADS) {
     int j = A.lookup[i];
@@ -386,38 +461,37 @@ __global__ void __launch_bounds__(GEMC_THREADS)
       tclk = now;
     }
   };
+  Move &M = S.mv;
+
   for (int t = 0; t < p.nsteps; ++t) {
     const long long step = p.first + t;
     const int par = t & 1;
-    Move &M = S.mv;
     // ---------------- draw the move (warp 0) ----------------
     if (warp == 0) {
       if (lane == 0)
         settings_adjust(c, step, p.adj);
       __syncwarp();
       MtCursor R{c.mt, c.mt_left, c.mt_next};
-      // System::PickMove: PRNG::PickArbDist, Wt = 1
-      double sum = 0.0, prevSum = 0.0, draw = R.rand01() * 1.0;
-      int pick;
-      for (pick = 0; pick < GEMC_KINDS && sum < draw; ++pick) {
-        prevSum = sum;
-        sum += p.perc[pick];
-      }
-      if (pick != 0)
-        --pick;
-      double subDraw = draw - prevSum;
-      double movPerc = p.perc[pick];
-      int kind = pick, b = -1, b1 = -1, m = -1, ok = 0;
-      double u_acc = 0.0;
+      // System::PickMove: PRNG::PickArbDist (Wt = 1) walks the running sums
+      // of the weights and takes the first kind whose sum reaches the draw
+      const double draw = R.rand01() * 1.0;
+      const bool ge = lane < GEMC_KINDS && p.cum[lane] >= draw;
+      const unsigned bal = __ballot_sync(0xffffffffu, ge);
+      const int kind = bal ? __ffs(bal) - 1 : GEMC_KINDS - 1;
+      const double prevSum = kind > 0 ? p.cum[kind - 1] : 0.0;
+      const double subDraw = draw - prevSum;
+      int b = -1, b1 = -1, m = -1, ok = 0;
       unsigned pick_word = 0;
+      if (kind == GEMC_DISPLACE || kind == GEMC_TRANSFER ||
+          kind == GEMC_VOLUME) {
+        // PRNG::PickBox: (uint)(subDraw / boxDiv) of two boxes, boxDiv =
+        // movPerc / 2; the rounded quotient reaches 1 exactly when subDraw
+        // reaches boxDiv
+        b = subDraw >= p.boxdiv[kind] ? 1 : 0;
+        b1 = 1 - b;
+      }
       if (kind == GEMC_DISPLACE || kind == GEMC_TRANSFER) {
-        // PRNG::PickMolAndBox / PickMolAndBoxPair2: box from the sub-draw,
-        // then a molecule of the (single) kind in it
-        double boxDiv = movPerc / 2;
-        b = (int)(unsigned)(subDraw / boxDiv);
-        if (b >= 2)
-          b--;
-        b1 = b == 0 ? 1 : 0;
+        // PRNG::PickMol / PickMol2: a molecule of the (single) kind
         int nb = count_of(c, n, b);
         if (nb > 0) {
           unsigned off = R.randInt((unsigned)nb - 1u);
@@ -425,38 +499,37 @@ __global__ void __launch_bounds__(GEMC_THREADS)
           ok = 1;
         }
       } else if (kind == GEMC_VOLUME) {
-        double boxDiv = movPerc / 2;
-        b = (int)(unsigned)(subDraw / boxDiv);
-        if (b >= 2)
-          b--;
-        b1 = b == 0 ? 1 : 0;
         ok = 1;
       }
       if (kind == GEMC_DISPLACE && ok) {
-        // Coordinates::TranslateRand with PRNG::SymXYZ
-        double bound = c.scale[b][0], bound2 = 2.0 * bound;
-        double sx = R.rand01() * bound2 - bound;
-        double sy = R.rand01() * bound2 - bound;
-        double sz = R.rand01() * bound2 - bound;
-        u_acc = R.rand01();
-        if (lane == 0) {
-          M.nx = wrapd(A.px[m] + sx, c.ax[b][0]);
-          M.ny = wrapd(A.py[m] + sy, c.ax[b][1]);
-          M.nz = wrapd(A.pz[m] + sz, c.ax[b][2]);
-          // the centres are kept by CTA 0 alone (global memory)
-          if (rank == 0) {
-            M.ncx = wrapd(p.cx[m] + sx, c.ax[b][0]);
-            M.ncy = wrapd(p.cy[m] + sy, c.ax[b][1]);
-            M.ncz = wrapd(p.cz[m] + sz, c.ax[b][2]);
+        // Coordinates::TranslateRand with PRNG::SymXYZ (three words), then
+        // the acceptance word; lane d takes axis d
+        const unsigned w0 = R.u32(), w1 = R.u32(), w2 = R.u32(),
+                       w3 = R.u32();
+        if (lane < 3) {
+          const unsigned w = lane == 0 ? w0 : lane == 1 ? w1 : w2;
+          const double bound = c.scale[b][0], bound2 = 2.0 * bound;
+          const double sh = (double)w * (1.0 / 4294967295.0) * bound2 - bound;
+          const double pv = lane == 0 ? A.px[m] : lane == 1 ? A.py[m] : A.pz[m];
+          const double nv = wrapd(pv + sh, c.ax[b][lane]);
+          M.np[lane] = nv;
+          M.nf[lane] = (float)nv;
+          if (MIXED)
+            M.nt[lane] = turns(nv, 1.0 / c.ax[b][lane]);
+          if (rank == 0) {  // the centres are CTA 0's (global memory)
+            const double cv =
+                lane == 0 ? p.cx[m] : lane == 1 ? p.cy[m] : p.cz[m];
+            M.nc[lane] = wrapd(cv + sh, c.ax[b][lane]);
           }
+        } else if (lane == 3) {
+          M.u_acc = (double)w3 * (1.0 / 4294967295.0);
         }
       } else if (kind == GEMC_TRANSFER && ok) {
         // DCLinear::Build: direction, DCSingle::BuildNew (trials in the
         // destination box, PickWeighted), DCSingle::BuildOld (trials in the
-        // source box, trial 0 at the molecule)
+        // source box, trial 0 at the molecule): the raw words in order, then
+        // each lane scales its own coordinates
         (void)R.randInt(1);
-        // the trials' raw words in order (new trials, PickWeighted's word,
-        // old trials), then each lane scales its own coordinates
         unsigned *wbuf = M.words;
         for (int k = 0; k < 3 * nt; ++k) {
           unsigned w = R.u32();
@@ -472,14 +545,15 @@ __global__ void __launch_bounds__(GEMC_THREADS)
         __syncwarp();
         for (int q = lane; q < 6 * nt; q += 32) {
           const int k = q / 3, d = q - 3 * k;
-          const double ax = k < nt ? c.ax[b1][d] : c.ax[b][d];
-          M.tr[k][d] = (double)wbuf[q] * (1.0 / 4294967296.0) * ax;
-        }
-        __syncwarp();
-        if (lane == 0) {
-          M.tr[nt][0] = wrapd(A.px[m], c.ax[b][0]);
-          M.tr[nt][1] = wrapd(A.py[m], c.ax[b][1]);
-          M.tr[nt][2] = wrapd(A.pz[m], c.ax[b][2]);
+          const int bb = k < nt ? b1 : b;
+          double v = (double)wbuf[q] * (1.0 / 4294967296.0) * c.ax[bb][d];
+          if (k == nt)
+            v = wrapd(d == 0 ? A.px[m] : d == 1 ? A.py[m] : A.pz[m],
+                      c.ax[b][d]);
+          M.tr[k][d] = v;
+          M.trf[k][d] = (float)v;
+          if (MIXED)
+            M.trt[k][d] = turns(v, 1.0 / c.ax[bb][d]);
         }
       } else if (kind == GEMC_VOLUME) {
         // Coordinates::VolumeTransferTranslate: PRNG::Sym, then
@@ -499,10 +573,9 @@ __global__ void __launch_bounds__(GEMC_THREADS)
           }
           const int bp[2] = {b, b1};
           double vTot = (c.vol[bp[0]] + c.vol[bp[1]]);
-          double target[2] = {c.vol[bp[0]] + transfer, 0.0};
           for (int i = 0; i < 2; ++i) {
             int bb = bp[i];
-            double v = i == 0 ? target[0] : vTot - M.nvol[bp[0]];
+            double v = i == 0 ? c.vol[bp[0]] + transfer : vTot - M.nvol[bp[0]];
             double ratio = cbrt(v / M.nvol[bb]);
             for (int d = 0; d < 3; ++d) {
               M.nax[bb][d] *= ratio;
@@ -513,16 +586,28 @@ __global__ void __launch_bounds__(GEMC_THREADS)
           }
           for (int i = 0; i < 2; ++i) {
             int bb = bp[i];
-            for (int d = 0; d < 3; ++d)
+            double smin = 1e300;
+            for (int d = 0; d < 3; ++d) {
               M.sc[bb][d] = M.nax[bb][d] / c.ax[bb][d];
+              smin = fmin(smin, M.sc[bb][d]);
+              M.nlt[bb][d] = (float)(M.nax[bb][d] / TURN);
+            }
+            // a new separation is the old one scaled by sc per axis: the
+            // FP32 pre-filter on the old distances, with room for rounding
+            double lmax = fmax(c.ax[bb][0], fmax(c.ax[bb][1], c.ax[bb][2]));
+            double rr = (p.rcut + 1e-5 * lmax + 1e-4) / smin;
+            M.vcut[bb] = (float)(rr * rr);
             if (M.nhalf[bb][0] < p.rcut || M.nhalf[bb][1] < p.rcut ||
                 M.nhalf[bb][2] < p.rcut || M.nvol[bb] < c.minVol[bb])
               c.err = 1;
           }
         }
         __syncwarp();
-        if (!c.err)
-          u_acc = R.rand01();
+        if (!c.err) {
+          double u = R.rand01();
+          if (lane == 0)
+            M.u_acc = u;
+        }
       }
       if (lane == 0) {
         M.kind = kind;
@@ -530,7 +615,6 @@ __global__ void __launch_bounds__(GEMC_THREADS)
         M.b1 = b1;
         M.m = m;
         M.ok = ok;
-        M.u_acc = u_acc;
         M.pick_word = pick_word;
         c.mt_left = R.left;
         c.mt_next = R.next;
@@ -544,152 +628,281 @@ __global__ void __launch_bounds__(GEMC_THREADS)
                       : kind == GEMC_VOLUME ? 2 : -1;
     mark(pslot, 0);
     int nval = 0;
+    int2 *q = S.wq[warp];
     // ---------------- energy phase (all CTAs) ----------------
-    float lt[2][3];
-    if (MIXED)
-      for (int bb = 0; bb < 2; ++bb)
-        for (int d = 0; d < 3; ++d)
-          lt[bb][d] = (float)(c.ax[bb][d] / TURN);
     if (kind == GEMC_DISPLACE && M.ok) {
-      // Translate::CalcEn -> MoleculeInter (molecule out of the cell list)
+      // Translate::CalcEn -> MoleculeInter (the molecule out of the cell
+      // list): this CTA's slice of the box's molecules
       nval = 2;
-      double acc = 0.0;
-      int ovl = 0, ovl_old = 0;
       const int a0 = first_of(c, b), nb = count_of(c, n, b);
-      unsigned ntx = 0, nty = 0, ntz = 0;
-      if (MIXED) {
-        ntx = turns(M.nx, 1.0 / c.ax[b][0]);
-        nty = turns(M.ny, 1.0 / c.ax[b][1]);
-        ntz = turns(M.nz, 1.0 / c.ax[b][2]);
-      }
-      for (int i = gt; i < nb; i += G) {
-        int j = A.lookup[a0 + i];
-        if (j == m)
-          continue;
-        double eo = 0.0, en = 0.0;
-        if (!MIXED) {
-          pair_point<MIXED>(p, c, A, b, j, A.px[m], A.py[m], A.pz[m], A.fx[m],
-                            A.fy[m], A.fz[m], 0, 0, 0, nullptr, eo, ovl_old);
-          pair_point<MIXED>(p, c, A, b, j, M.nx, M.ny, M.nz, (float)M.nx,
-                            (float)M.ny, (float)M.nz, 0, 0, 0, nullptr, en,
-                            ovl);
-        } else {
-          pair_point<MIXED>(p, c, A, b, j, 0, 0, 0, 0, 0, 0, A.tx[m], A.ty[m],
-                            A.tz[m], lt[b], eo, ovl_old);
-          pair_point<MIXED>(p, c, A, b, j, 0, 0, 0, 0, 0, 0, ntx, nty, ntz,
-                            lt[b], en, ovl);
+      const int lo = (int)((long long)nb * rank / C);
+      const int hi = (int)((long long)nb * (rank + 1) / C);
+      if (!MIXED) {
+        const float *L = S.axf[b], *H = S.halff[b];
+        const float ofx = A.fx[m], ofy = A.fy[m], ofz = A.fz[m];
+        const float nfx = M.nf[0], nfy = M.nf[1], nfz = M.nf[2];
+        const double opx = A.px[m], opy = A.py[m], opz = A.pz[m];
+        const double npx = M.np[0], npy = M.np[1], npz = M.np[2];
+        double acc = 0.0;
+        int ovl = 0, qn = 0;
+        const float pc = S.pcut[b];
+        auto eval = [&](int2 e) {  // e = (molecule, 1: new position)
+          const bool nw = e.y != 0;
+          double d2 = r2_f64(nw ? npx : opx, nw ? npy : opy, nw ? npz : opz,
+                             A.px[e.x], A.py[e.x], A.pz[e.x], c.ax[b],
+                             c.half[b]);
+          if (d2 < p.rcutSq) {
+            double en = lj64(p, d2);
+            acc += nw ? en : -en;
+            if (nw && d2 < p.rcutLowSq)
+              ++ovl;
+          }
+        };
+        for (int i0 = lo + warp * 32; i0 < hi; i0 += GEMC_THREADS) {
+          const int i = i0 + lane;
+          int j = i < hi ? A.lookup[a0 + i] : -1;
+          bool co = false, cn = false;
+          if (j >= 0 && j != m) {
+            const float jx = A.fx[j], jy = A.fy[j], jz = A.fz[j];
+            co = r2_f32(ofx, ofy, ofz, jx, jy, jz, L, H) < pc;
+            cn = r2_f32(nfx, nfy, nfz, jx, jy, jz, L, H) < pc;
+          }
+          const unsigned bo = __ballot_sync(0xffffffffu, co);
+          if (co)
+            q[qn + __popc(bo & lt_mask)] = make_int2(j, 0);
+          qn += __popc(bo);
+          const unsigned bn = __ballot_sync(0xffffffffu, cn);
+          if (cn)
+            q[qn + __popc(bn & lt_mask)] = make_int2(j, 1);
+          qn += __popc(bn);
+          qflush(q, qn, false, lane, eval);
         }
-        acc += en - eo;
+        qflush(q, qn, true, lane, eval);
+        acc = warp_sum(acc);
+        ovl = warp_sum_i(ovl);
+        if (lane == 0) {
+          S.wred[warp][0] = acc;
+          S.wred[warp][1] = (double)ovl;
+        }
+      } else {
+        const float *lt = S.ltf[b];
+        const unsigned otx = A.tx[m], oty = A.ty[m], otz = A.tz[m];
+        const unsigned ntx = M.nt[0], nty = M.nt[1], ntz = M.nt[2];
+        float sh = 0.0f, sl = 0.0f;
+        int ovl = 0;
+        for (int i = lo + tid; i < hi; i += GEMC_THREADS) {
+          const int j = A.lookup[a0 + i];
+          if (j == m)
+            continue;
+          const unsigned jx = A.tx[j], jy = A.ty[j], jz = A.tz[j];
+          const float ro = r2_turns(otx, oty, otz, jx, jy, jz, lt);
+          const float rn = r2_turns(ntx, nty, ntz, jx, jy, jz, lt);
+          const float eo = ro < p.rcutSq_f ? lj32(p, ro) : 0.0f;
+          float en = 0.0f;
+          if (rn < p.rcutSq_f) {
+            en = lj32(p, rn);
+            if (rn < p.rcutLowSq_f)
+              ++ovl;
+          }
+          two_sum_add(sh, sl, en);
+          two_sum_add(sh, sl, -eo);
+        }
+        warp_two_sum(sh, sl);
+        ovl = warp_sum_i(ovl);
+        if (lane == 0) {
+          S.wred[warp][0] = (double)sh + (double)sl;
+          S.wred[warp][1] = (double)ovl;
+        }
       }
-      warp_put(S, 0, acc);
-      warp_put(S, 1, (double)ovl);
     } else if (kind == GEMC_TRANSFER && M.ok) {
       // CalculateEnergy::ParticleInter of each trial (the molecule is out of
       // its box's cell list): new trials in the destination box, old trials
-      // in the source box
+      // in the source box; warp w takes trials w, w + 8, ... over this
+      // CTA's slice of the trial's box
       nval = 3 * nt;
-      // one warp per trial, over this CTA's slice of the trial's box
-      for (int k = warp; k < 2 * nt; k += NW) {
-        const int bb = k < nt ? b1 : b;
-        const int a0 = first_of(c, bb), nb = count_of(c, n, bb);
-        const int lo = (int)((long long)nb * rank / C);
-        const int hi = (int)((long long)nb * (rank + 1) / C);
-        double sx = M.tr[k][0], sy = M.tr[k][1], sz = M.tr[k][2];
-        unsigned ux = 0, uy = 0, uz = 0;
-        if (MIXED) {
-          ux = turns(sx, 1.0 / c.ax[bb][0]);
-          uy = turns(sy, 1.0 / c.ax[bb][1]);
-          uz = turns(sz, 1.0 / c.ax[bb][2]);
+      if (!MIXED) {
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        int ov[4] = {0, 0, 0, 0};
+        int qn = 0;
+        auto eval = [&](int2 e) {  // e = (molecule, trial of this warp)
+          const int k = warp + NW * e.y;
+          const int bb = k < nt ? b1 : b;
+          double d2 = r2_f64(M.tr[k][0], M.tr[k][1], M.tr[k][2], A.px[e.x],
+                             A.py[e.x], A.pz[e.x], c.ax[bb], c.half[bb]);
+          if (d2 < p.rcutSq) {
+            double en = lj64(p, d2);
+            bool lowr = d2 < p.rcutLowSq;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+              if (u == e.y) {
+                acc[u] += en;
+                ov[u] += lowr ? 1 : 0;
+              }
+          }
+        };
+        for (int kl = 0; warp + NW * kl < 2 * nt; ++kl) {
+          const int k = warp + NW * kl;
+          const int bb = k < nt ? b1 : b;
+          const int a0 = first_of(c, bb), nb = count_of(c, n, bb);
+          const int lo = (int)((long long)nb * rank / C);
+          const int hi = (int)((long long)nb * (rank + 1) / C);
+          const float sx = M.trf[k][0], sy = M.trf[k][1], sz = M.trf[k][2];
+          const float *L = S.axf[bb], *H = S.halff[bb];
+          const float pc = S.pcut[bb];
+          for (int i0 = lo; i0 < hi; i0 += 32) {
+            const int i = i0 + lane;
+            int j = i < hi ? A.lookup[a0 + i] : -1;
+            bool cd = j >= 0 && j != m &&
+                      r2_f32(sx, sy, sz, A.fx[j], A.fy[j], A.fz[j], L, H) < pc;
+            const unsigned bc = __ballot_sync(0xffffffffu, cd);
+            if (cd)
+              q[qn + __popc(bc & lt_mask)] = make_int2(j, kl);
+            qn += __popc(bc);
+            qflush(q, qn, false, lane, eval);
+          }
         }
-        double acc = 0.0;
-        int ovl = 0;
-        for (int i = lo + lane; i < hi; i += 32) {
-          int j = A.lookup[a0 + i];
-          if (j == m)
-            continue;
-          pair_point<MIXED>(p, c, A, bb, j, sx, sy, sz, (float)sx, (float)sy,
-                            (float)sz, ux, uy, uz, MIXED ? lt[bb] : nullptr,
-                            acc, ovl);
+        qflush(q, qn, true, lane, eval);
+        for (int kl = 0; warp + NW * kl < 2 * nt; ++kl) {
+          const int k = warp + NW * kl;
+          double a = 0.0;
+          int o = 0;
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (u == kl) {
+              a = acc[u];
+              o = ov[u];
+            }
+          a = warp_sum(a);
+          o = warp_sum_i(o);
+          if (lane == 0) {
+            S.part[par][k] = a;
+            if (k < nt)
+              S.part[par][2 * nt + k] = (double)o;
+          }
         }
-        for (int o = 16; o > 0; o >>= 1) {
-          acc += __shfl_down_sync(0xffffffffu, acc, o);
-          ovl += __shfl_down_sync(0xffffffffu, ovl, o);
-        }
-        if (lane == 0) {
-          S.part[par][k] = acc;
-          if (k < nt)
-            S.part[par][2 * nt + k] = (double)ovl;
+      } else {
+        for (int k = warp; k < 2 * nt; k += NW) {
+          const int bb = k < nt ? b1 : b;
+          const int a0 = first_of(c, bb), nb = count_of(c, n, bb);
+          const int lo = (int)((long long)nb * rank / C);
+          const int hi = (int)((long long)nb * (rank + 1) / C);
+          const unsigned ux = M.trt[k][0], uy = M.trt[k][1], uz = M.trt[k][2];
+          const float *lt = S.ltf[bb];
+          float sh = 0.0f, sl = 0.0f;
+          int ovl = 0;
+          for (int i = lo + lane; i < hi; i += 32) {
+            const int j = A.lookup[a0 + i];
+            if (j == m)
+              continue;
+            const float r2 =
+                r2_turns(ux, uy, uz, A.tx[j], A.ty[j], A.tz[j], lt);
+            if (r2 < p.rcutSq_f) {
+              two_sum_add(sh, sl, lj32(p, r2));
+              if (r2 < p.rcutLowSq_f)
+                ++ovl;
+            }
+          }
+          warp_two_sum(sh, sl);
+          ovl = warp_sum_i(ovl);
+          if (lane == 0) {
+            S.part[par][k] = (double)sh + (double)sl;
+            if (k < nt)
+              S.part[par][2 * nt + k] = (double)ovl;
+          }
         }
       }
     } else if (kind == GEMC_VOLUME) {
-      // Coordinates::TranslateOneBox for both boxes into the trial arrays,
+      // Coordinates::TranslateOneBox of both boxes into the trial arrays,
       // then BoxInter of both boxes at the new axes.  The centres are CTA
       // 0's (global memory): a cluster barrier first makes its latest
-      // writes visible to every CTA.
+      // writes visible; every CTA moves its slice of the molecules, and a
+      // second barrier lets each copy the other slices.
       nval = 2;
-      asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
-      asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
-      for (int i = tid; i < n; i += GEMC_THREADS) {
-        int j = A.lookup[i];
-        int bb = i < c.start1 ? 0 : 1;
-        double ocx = p.cx[j], ocy = p.cy[j], ocz = p.cz[j];
-        double ncx = ocx * M.sc[bb][0], ncy = ocy * M.sc[bb][1],
-               ncz = ocz * M.sc[bb][2];
-        double ux = unwrapd(A.px[j], ocx, c.ax[bb][0], c.half[bb][0]);
-        double uy = unwrapd(A.py[j], ocy, c.ax[bb][1], c.half[bb][1]);
-        double uz = unwrapd(A.pz[j], ocz, c.ax[bb][2], c.half[bb][2]);
-        double nx = wrapd(ux + (ncx - ocx), M.nax[bb][0]);
-        double ny = wrapd(uy + (ncy - ocy), M.nax[bb][1]);
-        double nz = wrapd(uz + (ncz - ocz), M.nax[bb][2]);
-        A.qx[j] = nx;
-        A.qy[j] = ny;
-        A.qz[j] = nz;
-        if (MIXED) {
-          A.ux[j] = turns(nx, 1.0 / M.nax[bb][0]);
-          A.uy[j] = turns(ny, 1.0 / M.nax[bb][1]);
-          A.uz[j] = turns(nz, 1.0 / M.nax[bb][2]);
+      cluster_barrier();
+      {
+        const int lo = (int)((long long)n * rank / C);
+        const int hi = (int)((long long)n * (rank + 1) / C);
+        for (int i = lo + tid; i < hi; i += GEMC_THREADS) {
+          int j = A.lookup[i];
+          int bb = i < c.start1 ? 0 : 1;
+          double ocx = p.cx[j], ocy = p.cy[j], ocz = p.cz[j];
+          double ncx = ocx * M.sc[bb][0], ncy = ocy * M.sc[bb][1],
+                 ncz = ocz * M.sc[bb][2];
+          double ux = unwrapd(A.px[j], ocx, c.ax[bb][0], c.half[bb][0]);
+          double uy = unwrapd(A.py[j], ocy, c.ax[bb][1], c.half[bb][1]);
+          double uz = unwrapd(A.pz[j], ocz, c.ax[bb][2], c.half[bb][2]);
+          double nx = wrapd(ux + (ncx - ocx), M.nax[bb][0]);
+          double ny = wrapd(uy + (ncy - ocy), M.nax[bb][1]);
+          double nz = wrapd(uz + (ncz - ocz), M.nax[bb][2]);
+          A.qx[j] = nx;
+          A.qy[j] = ny;
+          A.qz[j] = nz;
+          if (MIXED) {
+            A.ux[j] = turns(nx, 1.0 / M.nax[bb][0]);
+            A.uy[j] = turns(ny, 1.0 / M.nax[bb][1]);
+            A.uz[j] = turns(nz, 1.0 / M.nax[bb][2]);
+          }
+        }
+      }
+      cluster_barrier();
+      for (int r = 0; r < C; ++r) {
+        if (r == rank)
+          continue;
+        const int lo = (int)((long long)n * r / C);
+        const int hi = (int)((long long)n * (r + 1) / C);
+        const double *rqx = cluster.map_shared_rank(A.qx, (unsigned)r);
+        const double *rqy = cluster.map_shared_rank(A.qy, (unsigned)r);
+        const double *rqz = cluster.map_shared_rank(A.qz, (unsigned)r);
+        for (int i = lo + tid; i < hi; i += GEMC_THREADS) {
+          int j = A.lookup[i];
+          A.qx[j] = rqx[j];
+          A.qy[j] = rqy[j];
+          A.qz[j] = rqz[j];
+          if (MIXED) {
+            A.ux[j] = cluster.map_shared_rank(A.ux, (unsigned)r)[j];
+            A.uy[j] = cluster.map_shared_rank(A.uy, (unsigned)r)[j];
+            A.uz[j] = cluster.map_shared_rank(A.uz, (unsigned)r)[j];
+          }
         }
       }
       __syncthreads();
-      double eb[2] = {0.0, 0.0};
-      float nlt[2][3];
-      for (int bb = 0; bb < 2; ++bb)
-        for (int d = 0; d < 3; ++d)
-          nlt[bb][d] = (float)(M.nax[bb][d] / TURN);
       // pair tiles of 32 x 32 (block row <= block column) dealt to the
-      // cluster's warps; lane l takes row i of its tile
+      // cluster's warps; lane l takes row l of its tile
       const int gw = rank * NW + warp, GW = C * NW;
+      double ebox[2] = {0.0, 0.0};
       for (int bb = 0; bb < 2; ++bb) {
         const int a0 = first_of(c, bb), nb = count_of(c, n, bb);
         const int nbt = (nb + 31) / 32;
         const int ntile = nbt * (nbt + 1) / 2;
-        const float ax0 = (float)M.nax[bb][0], ax1 = (float)M.nax[bb][1],
-                    ax2 = (float)M.nax[bb][2];
-        const float hf0 = (float)M.nhalf[bb][0], hf1 = (float)M.nhalf[bb][1],
-                    hf2 = (float)M.nhalf[bb][2];
         double acc = 0.0;
+        float sh = 0.0f, sl = 0.0f;
+        int qn = 0;
+        const float *L = S.axf[bb], *H = S.halff[bb];
+        const float vcut = M.vcut[bb];
+        const float *nlt = M.nlt[bb];
+        auto eval = [&](int2 e) {  // e = (molecule, molecule)
+          double d2 = r2_f64(A.qx[e.x], A.qy[e.x], A.qz[e.x], A.qx[e.y],
+                             A.qy[e.y], A.qz[e.y], M.nax[bb], M.nhalf[bb]);
+          if (d2 < p.rcutSq)
+            acc += lj64(p, d2);
+        };
         for (int tl = gw; tl < ntile; tl += GW) {
-          // tile index -> (ib, jb), jb >= ib
           int ib = 0, rem = tl;
           while (rem >= nbt - ib) {
             rem -= nbt - ib;
             ++ib;
           }
-          int jb = ib + rem;
-          int i = ib * 32 + lane;
-          bool act = i < nb;
-          int pi = act ? A.lookup[a0 + i] : 0;
-          double xi = 0, yi = 0, zi = 0;
+          const int jb = ib + rem;
+          const int i = ib * 32 + lane;
+          const bool act = i < nb;
+          const int pi = act ? A.lookup[a0 + i] : 0;
           float fxi = 0, fyi = 0, fzi = 0;
           unsigned txi = 0, tyi = 0, tzi = 0;
           if (act) {
             if (!MIXED) {
-              xi = A.qx[pi];
-              yi = A.qy[pi];
-              zi = A.qz[pi];
-              fxi = (float)xi;
-              fyi = (float)yi;
-              fzi = (float)zi;
+              fxi = A.fx[pi];
+              fyi = A.fy[pi];
+              fzi = A.fz[pi];
             } else {
               txi = A.ux[pi];
               tyi = A.uy[pi];
@@ -698,37 +911,36 @@ __global__ void __launch_bounds__(GEMC_THREADS)
           }
           const int j0 = jb * 32, j1 = min(nb, j0 + 32);
           for (int jj = j0; jj < j1; ++jj) {
-            if (!act || jj <= i)
-              continue;
-            int pj = A.lookup[a0 + jj];
+            const int pj = A.lookup[a0 + jj];
+            const bool valid = act && jj > i;
             if (!MIXED) {
-              double xj = A.qx[pj], yj = A.qy[pj], zj = A.qz[pj];
-              float dx = mimgf(fxi - (float)xj, ax0, hf0);
-              float dy = mimgf(fyi - (float)yj, ax1, hf1);
-              float dz = mimgf(fzi - (float)zj, ax2, hf2);
-              float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-              if (r2 < p.rcutSq_f) {
-                double ex = mimg(xi - xj, M.nax[bb][0], M.nhalf[bb][0]);
-                double ey = mimg(yi - yj, M.nax[bb][1], M.nhalf[bb][1]);
-                double ez = mimg(zi - zj, M.nax[bb][2], M.nhalf[bb][2]);
-                double d2 = ex * ex + ey * ey + ez * ez;
-                if (d2 < p.rcutSq)
-                  acc += lj64(p, d2);
-              }
-            } else {
-              float dx = (float)(int)(txi - A.ux[pj]) * nlt[bb][0];
-              float dy = (float)(int)(tyi - A.uy[pj]) * nlt[bb][1];
-              float dz = (float)(int)(tzi - A.uz[pj]) * nlt[bb][2];
-              float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+              bool cd = valid && r2_f32(fxi, fyi, fzi, A.fx[pj], A.fy[pj],
+                                        A.fz[pj], L, H) < vcut;
+              const unsigned bc = __ballot_sync(0xffffffffu, cd);
+              if (cd)
+                q[qn + __popc(bc & lt_mask)] = make_int2(pi, pj);
+              qn += __popc(bc);
+              qflush(q, qn, false, lane, eval);
+            } else if (valid) {
+              const float r2 = r2_turns(txi, tyi, tzi, A.ux[pj], A.uy[pj],
+                                        A.uz[pj], nlt);
               if (r2 < p.rcutSq_f)
-                acc += (double)lj32(p, r2);
+                two_sum_add(sh, sl, lj32(p, r2));
             }
           }
         }
-        eb[bb] = acc;
+        if (!MIXED) {
+          qflush(q, qn, true, lane, eval);
+          ebox[bb] = warp_sum(acc);
+        } else {
+          warp_two_sum(sh, sl);
+          ebox[bb] = (double)sh + (double)sl;
+        }
       }
-      warp_put(S, 0, eb[0]);
-      warp_put(S, 1, eb[1]);
+      if (lane == 0) {
+        S.wred[warp][0] = ebox[0];
+        S.wred[warp][1] = ebox[1];
+      }
     }
     __syncthreads();
     mark(pslot, 1);
@@ -741,8 +953,7 @@ __global__ void __launch_bounds__(GEMC_THREADS)
       S.part[par][tid] = v;
     }
     // ---------------- exchange: one cluster barrier ----------------
-    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
-    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+    cluster_barrier();
     if (tid < nval) {
       // the ranks' partials loaded together, added in rank order
       double pr[16];
@@ -774,9 +985,8 @@ __global__ void __launch_bounds__(GEMC_THREADS)
             M.d[0] = dLJ;
             M.d[1] = ovl ? 1.0 : 0.0;
             M.d[2] = M.d[3] = 0.0;
-          }
-          if (lane == 0)
             settings_update(c, 0, acc, b);
+          }
         } else if (lane == 0) {
           settings_update(c, 0, 0, b);
           M.d[0] = M.d[1] = M.d[2] = M.d[3] = 0.0;
@@ -789,18 +999,16 @@ __global__ void __launch_bounds__(GEMC_THREADS)
           for (int k = lane; k < 2 * nt; k += 32)
             wv[k] = exp(-1 * p.beta * ((0.0 + M.tot[k]) + 0.0));
           __syncwarp();
-          double stepWeight = 0.0, w[GEMC_NTMAX];
-          for (int k = 0; k < nt; ++k) {
-            w[k] = wv[k];
-            stepWeight += w[k];
-          }
+          double stepWeight = 0.0;
+          for (int k = 0; k < nt; ++k)
+            stepWeight += wv[k];
           // PRNG::PickWeighted (src/PRNG.h:167-200)
           double draw = ((double)M.pick_word * (1.0 / 4294967295.0)) *
                         stepWeight;
           double s = 0.0;
           int winner = -1;
           for (int k = 0; k < nt; ++k) {
-            s += w[k];
+            s += wv[k];
             if (s >= draw) {
               winner = k;
               break;
@@ -808,7 +1016,7 @@ __global__ void __launch_bounds__(GEMC_THREADS)
           }
           if (winner < 0) {
             int lastZero = nt;
-            for (int k = nt - 1; k > 0 && w[k] == 0.0; --k)
+            for (int k = nt - 1; k > 0 && wv[k] == 0.0; --k)
               lastZero = k;
             winner = lastZero - 1;  // |draw - total| < 0.001 in practice
           }
@@ -833,9 +1041,11 @@ __global__ void __launch_bounds__(GEMC_THREADS)
             if (acc) {
               c.e[b] -= eOld;
               c.e[b1] += eNew;
-              M.nx = M.tr[winner][0];
-              M.ny = M.tr[winner][1];
-              M.nz = M.tr[winner][2];
+              for (int d = 0; d < 3; ++d) {
+                M.np[d] = M.tr[winner][d];
+                M.nf[d] = M.trf[winner][d];
+                M.nt[d] = M.trt[winner][d];
+              }
             }
             settings_update(c, 1, acc, b1);
           }
@@ -873,59 +1083,47 @@ __global__ void __launch_bounds__(GEMC_THREADS)
     mark(pslot, 3);
     // ---------------- commit ----------------
     const int acc = S.accept;
-    if (acc && kind == GEMC_DISPLACE) {
+    if (acc && (kind == GEMC_DISPLACE || kind == GEMC_TRANSFER)) {
       if (tid == 0) {
-        A.px[m] = M.nx;
-        A.py[m] = M.ny;
-        A.pz[m] = M.nz;
+        A.px[m] = M.np[0];
+        A.py[m] = M.np[1];
+        A.pz[m] = M.np[2];
         if (!MIXED) {
-          A.fx[m] = (float)M.nx;
-          A.fy[m] = (float)M.ny;
-          A.fz[m] = (float)M.nz;
+          A.fx[m] = M.nf[0];
+          A.fy[m] = M.nf[1];
+          A.fz[m] = M.nf[2];
         } else {
-          A.tx[m] = turns(M.nx, 1.0 / c.ax[b][0]);
-          A.ty[m] = turns(M.ny, 1.0 / c.ax[b][1]);
-          A.tz[m] = turns(M.nz, 1.0 / c.ax[b][2]);
+          A.tx[m] = M.nt[0];
+          A.ty[m] = M.nt[1];
+          A.tz[m] = M.nt[2];
         }
-        if (rank == 0) {
-          p.cx[m] = M.ncx;
-          p.cy[m] = M.ncy;
-          p.cz[m] = M.ncz;
-        }
-      }
-    } else if (acc && kind == GEMC_TRANSFER) {
-      if (tid == 0) {
-        // new coordinates; COM::SetNew of one atom; MoleculeLookup::Shift
-        A.px[m] = M.nx;
-        A.py[m] = M.ny;
-        A.pz[m] = M.nz;
-        if (!MIXED) {
-          A.fx[m] = (float)M.nx;
-          A.fy[m] = (float)M.ny;
-          A.fz[m] = (float)M.nz;
-        } else {
-          A.tx[m] = turns(M.nx, 1.0 / c.ax[b1][0]);
-          A.ty[m] = turns(M.ny, 1.0 / c.ax[b1][1]);
-          A.tz[m] = turns(M.nz, 1.0 / c.ax[b1][2]);
-        }
-        if (rank == 0) {
-          p.cx[m] = wrapd(M.nx * (1.0 / 1.0), c.ax[b1][0]);
-          p.cy[m] = wrapd(M.ny * (1.0 / 1.0), c.ax[b1][1]);
-          p.cz[m] = wrapd(M.nz * (1.0 / 1.0), c.ax[b1][2]);
-        }
-        int a0 = first_of(c, b), nb = count_of(c, n, b), idx = a0;
-        for (int i = 0; i < nb; ++i)
-          if (A.lookup[a0 + i] == m) {
-            idx = a0 + i;
-            break;
+        if (kind == GEMC_DISPLACE) {
+          if (rank == 0) {
+            p.cx[m] = M.nc[0];
+            p.cy[m] = M.nc[1];
+            p.cz[m] = M.nc[2];
           }
-        int ni = b == 0 ? --c.start1 : c.start1++;
-        int tmp = A.lookup[idx];
-        A.lookup[idx] = A.lookup[ni];
-        A.lookup[ni] = tmp;
-        int left = count_of(c, n, b);
-        if (left == 0 || left == 1)
-          c.e[b] = 0.0;
+        } else {
+          // COM::SetNew of one atom; MoleculeLookup::Shift
+          if (rank == 0) {
+            p.cx[m] = wrapd(M.np[0] * (1.0 / 1.0), c.ax[b1][0]);
+            p.cy[m] = wrapd(M.np[1] * (1.0 / 1.0), c.ax[b1][1]);
+            p.cz[m] = wrapd(M.np[2] * (1.0 / 1.0), c.ax[b1][2]);
+          }
+          int a0 = first_of(c, b), nb = count_of(c, n, b), idx = a0;
+          for (int i = 0; i < nb; ++i)
+            if (A.lookup[a0 + i] == m) {
+              idx = a0 + i;
+              break;
+            }
+          int ni = b == 0 ? --c.start1 : c.start1++;
+          int tmp = A.lookup[idx];
+          A.lookup[idx] = A.lookup[ni];
+          A.lookup[ni] = tmp;
+          int left = count_of(c, n, b);
+          if (left == 0 || left == 1)
+            c.e[b] = 0.0;
+        }
       }
     } else if (acc && kind == GEMC_VOLUME) {
       // new positions, centres and axes
@@ -962,6 +1160,7 @@ __global__ void __launch_bounds__(GEMC_THREADS)
           c.vol[bb] = M.nvol[bb];
           c.volInv[bb] = M.nvolInv[bb];
         }
+        box_consts(S, p.rcut);
       }
     }
     if (rank == 0 && tid == 0 && p.tr_i) {
@@ -1006,7 +1205,7 @@ __global__ void __launch_bounds__(GEMC_THREADS)
     for (int i = tid; i < (int)(sizeof(GemcCtl) / 4); i += GEMC_THREADS)
       dst[i] = src[i];
   }
-  cluster.sync();  // no CTA leaves while another may read its partials
+  cluster.sync();  // no CTA leaves while another may read its shared memory
 }
 
 // BoxInter of both boxes from the FP64 masters (the periodic check of the
@@ -1297,6 +1496,16 @@ int gb_gemc_create(const gb_gemc_desc *d, const gb_gemc_config *cfg,
     tot += raw[k];
   for (int k = 0; k < GEMC_KINDS; ++k)
     p.perc[k] = raw[k] / tot;
+  // the running sums PRNG::PickArbDist forms (src/PRNG.h:153-163), in its
+  // order of additions
+  {
+    double sum = 0.0;
+    for (int k = 0; k < GEMC_KINDS; ++k) {
+      sum += p.perc[k];
+      p.cum[k] = sum;
+      p.boxdiv[k] = p.perc[k] / 2;
+    }
+  }
   // FFParticle::Blend for one kind
   const double nm = d->n_mie;
   const double cn = nm / (nm - 6.0) * std::pow(nm / 6.0, (6.0 / (nm - 6.0)));
@@ -1308,6 +1517,7 @@ int gb_gemc_create(const gb_gemc_desc *d, const gb_gemc_config *cfg,
   p.rcutLowSq = cfg->rcut_low * cfg->rcut_low;
   p.beta = 1 / cfg->temperature;
   p.sigmaSq_f = (float)p.sigmaSq;
+  p.rcutLowSq_f = (float)p.rcutLowSq;
   p.eps_cn_f = (float)p.eps_cn;
   // the FP32 distance pre-filter of the plain form passes every pair within
   // Rcut: FP32 copies of positions lie within L 2^-24 of the FP64 ones

@@ -37,8 +37,10 @@ struct GemcCtl {
 struct GemcParams {
   int n, nt, adj, cluster;
   double perc[GEMC_KINDS];
+  double cum[GEMC_KINDS];     // cumulative weights of PickArbDist's walk
+  double boxdiv[GEMC_KINDS];  // movPerc / 2 (PRNG::PickBox)
   double sigmaSq, eps_cn, nexp, rcut, rcutSq, rcutLowSq, beta;
-  float sigmaSq_f, eps_cn_f, rcutSq_f;
+  float sigmaSq_f, eps_cn_f, rcutSq_f, rcutLowSq_f;
   double *x, *y, *z, *cx, *cy, *cz;  // positions and centres (FP64 masters)
   int *lookup;                        // molecule lookup, box 0 then box 1
   GemcCtl *ctl;
