@@ -785,6 +785,15 @@ def run_gb300(args, rank, world):
             step += M
     barrier()
     timing = box.mc_timing(reset=True)
+    # where a move's time goes: the chain's phase clocks over 2,000 further
+    # moves (outside the timed steps)
+    box.mc_profile(enable=True)
+    box.mc_run(step, 2000)
+    step += 2000
+    pr = box.mc_profile(enable=False)
+    phase_us = {who: {k: v / max(pr["moves"][i], 1)
+                      for k, v in pr[who].items()}
+                for i, who in enumerate(("cta0", "leader"))}
     t_total = float(sum(times))
     t_total = max_over_ranks(t_total, dist, torch, dev)
     value = world * args.steps * M / t_total
@@ -842,7 +851,9 @@ def run_gb300(args, rank, world):
         if dist:
             dist.destroy_process_group()
         return
-    launches = timing["chain_launches"] + 10 * timing["mp_moves"]
+    # per chain launch: k_fill_u64 (partial slots), k_chain_fp64, and the
+    # grid rebuild k_cell_scatter + k_cell_sort_fill
+    launches = 4 * timing["chain_launches"] + 10 * timing["mp_moves"]
     kern_ms = timing["chain_ms"] / max(timing["chain_launches"], 1)
     moves_per_launch = timing["chain_moves"] / max(timing["chain_launches"], 1)
     fl = flop_per_move(K)
@@ -884,6 +895,7 @@ def run_gb300(args, rank, world):
         "step_ms": [round(t * 1e3, 3) for t in times],
         "e2e_step_ms": [round(t * 1e3, 3) for t in e2e_times],
         "chain_kernel_ms_per_launch": kern_ms,
+        "chain_phase_us_per_move": phase_us,
         "mixed": mixed,
         "serving": serving_stats,
         "gemc": gemc_stats,

@@ -6,17 +6,21 @@
 // rotation axis and the Metropolis uniform -- into MoveRec records.
 //
 // Device: a persistent cooperative "chain" kernel runs a segment of
-// displacement / rotation moves.  Every CTA owns a fixed chunk of k-vectors
-// whose Ref and New structure factors live in its shared memory for the whole
-// segment, plus a share of the (atom, old/new, neighbour cell) real-space
-// units.  Per move:
-//   phase A  all CTAs: real-space and reciprocal partials -> global slots
-//   barrier
-//   phase B  all CTAs: add the partials in one fixed order (identical in every
-//            CTA), take the same Metropolis decision, commit their own k-chunk;
-//            CTA 0 commits coordinates and the cell grid; designated CTAs
-//            build the next move's phase tables
-//   barrier
+// displacement / rotation moves on one CTA per SM.  Every CTA owns a fixed
+// chunk of k-vectors, whose Ref and New structure factors live in its shared
+// memory for the whole segment, and a strided share of the atoms, whose
+// positions, charges and fixed-point turns live there too.  Per move:
+//   phase A  all CTAs: the moved atoms (old and new positions) against the
+//            own atoms (every G-th atom) (FP32 pre-test, FP64 pair terms of the pairs inside
+//            the cutoff) and the k-chunk's structure-factor change ->
+//            partial slots in global memory
+//   phase B  the last CTA adds the partials in one fixed order, takes the
+//            Metropolis decision, commits the coordinates and publishes the
+//            decision in one word; every CTA then commits its own k-chunk
+//            and own atoms.  Meanwhile designated CTAs build the next
+//            move's context (header and phase tables) in global memory.
+// The cell grid is rebuilt from the coordinates after each segment
+// (CellList::GridAll).
 // Move-size adjustment (MoveSettings::AdjustMoves) is replayed identically in
 // every CTA.  Barriers spin a bounded number of times and then raise an error
 // flag that the host turns into GB_ERR_TIMEOUT.
@@ -412,6 +416,10 @@ struct ChainArgs {
   int nrows_max;  // phase rows of the largest molecule (6 x its atoms)
   int *tr_i;      // [n][3] or null
   double *tr_d;   // [n][3] or null
+  // phase clocks (NULL: not collected): [0 CTA 0, 1 the leader][phase:
+  // context load, real-space listing, pair terms and k-vectors to the
+  // partials, decision wait, commit and next context], then moves
+  long long *prof;
 };
 
 struct ChainShared {
@@ -723,6 +731,15 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
   // all three per k-vector.
   double2 *exy = tab + (size_t)(2 * MAX_MOL_ATOMS * 3) * (b.kmax + 1);
   unsigned short *pidx = (unsigned short *)(exy + NPAIR_CAP * 2 * MAX_MOL_ATOMS);
+  // this CTA's own atoms, resident for the whole launch: atoms cta,
+  // cta + G, cta + 2G, ... (strided, so that the atoms near any molecule,
+  // and with them the pair terms of its moves, spread over all CTAs);
+  // x, y | z, q | fixed-point turns and the meta word
+  const int own_per = (b.n_atoms + G - 1) / G;
+  const int on = cta < b.n_atoms ? (b.n_atoms - cta + G - 1) / G : 0;
+  double2 *oxy = (double2 *)(((uintptr_t)(pidx + kc_max) + 15) & ~(uintptr_t)15);
+  double2 *ozq = oxy + own_per;
+  uint4 *ot = (uint4 *)(ozq + own_per);
   __shared__ char2 pair_n[NPAIR_CAP];
   __shared__ int npair;
   for (int i = threadIdx.x; i < kc; i += CT) {
@@ -731,6 +748,15 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     sI[i] = b.sumIref[k];
     pf[i] = b.prefact[k];
     kn[i] = b.kn[k];
+  }
+  for (int i = threadIdx.x; i < on; i += CT) {
+    const int a = cta + G * i;
+    const double x = b.x[a], y = b.y[a], z = b.z[a];
+    oxy[i] = make_double2(x, y);
+    ozq[i] = make_double2(z, b.q[a]);
+    ot[i] = make_uint4(to_turns(x, b.invL[0]), to_turns(y, b.invL[1]),
+                       to_turns(z, b.invL[2]),
+                       (unsigned)pack_meta(b.mol[a], b.kind[a]));
   }
   if (threadIdx.x == 0) {
     S.set = *A.set;
@@ -788,6 +814,17 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
   if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
     return;
 
+  const int pslot = cta == 0 ? 0 : cta == G - 1 ? 1 : -1;
+  const bool prof = A.prof && threadIdx.x == 0 && pslot >= 0;
+  long long pacc[5] = {0, 0, 0, 0, 0};
+  long long tclk = prof ? clock64() : 0;
+  auto mark = [&](int ph) {
+    if (prof) {
+      long long now = clock64();
+      pacc[ph] += now - tclk;
+      tclk = now;
+    }
+  };
   for (int t = 0; t < A.n; ++t) {
     // ---------------- phase A ----------------
     // the header and the rows of the largest molecule in one round trip
@@ -797,6 +834,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     for (int i = threadIdx.x; i < A.nrows_max * stride; i += CT)
       tab[i] = __ldcg((const double2 *)(ctx_t + HDR) + i);
     __syncthreads();
+    mark(0);
     int m = (int)S.hdr[0];
     int na = (int)S.hdr[2];
     // The next move's context does not depend on this move's outcome unless
@@ -814,20 +852,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     if (wload)
       ctx_pre1(A, t + 1, pre);
     double lj = 0.0, re = 0.0, ovl = 0.0, er = 0.0;
-    // Real space: the candidates of all (atom, old/new, neighbour cell)
-    // units, numbered through a prefix sum of the units' slot counts and
-    // dealt out over the whole grid, so the in-cutoff pair terms (the
-    // FP64-heavy part) land evenly on the SMs.
-    int units = na * 2 * NB27;
-    __shared__ int u_cell[MAX_MOL_ATOMS * 2 * NB27];
-    __shared__ int u_off[MAX_MOL_ATOMS * 2 * NB27 + 1];
-    for (int u = threadIdx.x; u < units; u += CT) {
-      int a = u / (2 * NB27), side = (u / NB27) % 2, nn = u % NB27;
-      int cell = (int)S.hdr[(side ? 16 : 8) + a];
-      int c2 = nbr_cell(b.edge, cell, nn);
-      u_cell[u] = c2;
-      u_off[u + 1] = __ldcg(b.cell_count + c2);
-    }
+    // first atom of the moved molecule, for the commit to the own atoms
+    const int a0m = __ldg(b.mstart + m);
     // x-y column products times the atom's charge, one per (column,
     // old/new atom)
     for (int e = threadIdx.x; e < npair * 2 * na; e += CT) {
@@ -837,81 +863,50 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
       double2 v = cmul2(rx[pair_n[p].x], tab_at(rx + stride, pair_n[p].y));
       exy[e] = make_double2(q * v.x, q * v.y);
     }
-    __syncthreads();
     if (wload)
       ctx_pre2(A, t + 1, pre);
-    if (threadIdx.x < 32) {
-      // inclusive scan of the counts: each lane a contiguous run of units
-      int per = (units + 31) / 32;
-      int lo = threadIdx.x * per, hi = min(units, lo + per);
-      int run = 0;
-      for (int u = lo; u < hi; ++u)
-        run += u_off[u + 1];
-      int incl = run;
-      for (int o = 1; o < 32; o <<= 1) {
-        int v = __shfl_up_sync(0xffffffffu, incl, o);
-        if ((int)threadIdx.x >= o)
-          incl += v;
-      }
-      int acc0 = incl - run;
-      for (int u = lo; u < hi; ++u) {
-        acc0 += u_off[u + 1];
-        u_off[u + 1] = acc0;
-      }
-      if (threadIdx.x == 0)
-        u_off[0] = 0;
-    }
-    __syncthreads();
-    const int total = u_off[units];
-    // (1) Every warp tests candidates against the cutoff -- consecutive
-    //     candidates to different CTAs -- and the pairs inside it are
-    //     compacted, in candidate order, into a shared list (ballot and a
-    //     scan over the warps, so the order and every sum stay fixed).
+    // (1) Real space: this CTA's own atoms against the old and new
+    //     positions of the moved atoms.  An FP32 pre-test on the
+    //     fixed-point turns (the wrapped integer difference is the minimum
+    //     image; the exact FP64 test is made where the listed pairs are
+    //     evaluated), and the pairs inside it compacted, in (own atom,
+    //     position) order, into a shared list (a warp scan and a scan over
+    //     the warps, so the order and every sum stay fixed).  Every pair
+    //     within the cutoff is found, as the 27 neighbour cells of the
+    //     cell list find it, and the moved molecule's own atoms are left out
+    //     as CellList::RemoveMol leaves them out.
     __shared__ double2 icl_pos[ICL_MAX][2];  // neighbour x, y | z, q
     __shared__ int icl_meta[ICL_MAX];
     __shared__ short icl_unit[ICL_MAX];
     __shared__ int icl_warp[CT / 32 + 1];
+    const int npos = 2 * na;
+    const uint32_t *pturn = (const uint32_t *)(S.hdr + 84);
     int icl_n = 0;
-    for (int base = cta; base < total; base += total_threads) {
-      int idx = base + threadIdx.x * G;
-      bool in = false;
-      int u = 0, s = 0, mj = 0;
-      if (idx < total) {
-        int lo = 0, hi = units - 1;  // last unit whose offset <= idx
-        while (lo < hi) {
-          int mid = (lo + hi + 1) >> 1;
-          if (u_off[mid] <= idx)
-            lo = mid;
-          else
-            hi = mid - 1;
-        }
-        u = lo;
-        int a = u / (2 * NB27), side = (u / NB27) % 2;
-        s = u_cell[u] * b.cap + (idx - u_off[u]);
-        mj = __ldcg(b.cell_meta + s);
-        uint4 f = __ldcg(b.cell_fix + s);
-        if (meta_mol(mj) != m) {
-          // FP32 pre-test on the fixed-point turns (the wrapped integer
-          // difference is the minimum image); the exact FP64 test is made
-          // where the listed pairs are evaluated
-          const uint32_t *pt =
-              (const uint32_t *)(S.hdr + 84) + (side * na + a) * 3;
-          float dx = (float)(int)(pt[0] - f.x) * turn_f[0];
-          float dy = (float)(int)(pt[1] - f.y) * turn_f[1];
-          float dz = (float)(int)(pt[2] - f.z) * turn_f[2];
-          in = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < cut_f;
+    for (int base = 0; base < on; base += CT) {
+      const int i = base + threadIdx.x;
+      unsigned hit = 0;  // bit p: position p = side * na + atom passed
+      uint4 f = make_uint4(0, 0, 0, 0);
+      if (i < on) {
+        f = ot[i];
+        if (meta_mol((int)f.w) != m) {
+          for (int pp = 0; pp < npos; ++pp) {
+            float dx = (float)(int)(pturn[3 * pp] - f.x) * turn_f[0];
+            float dy = (float)(int)(pturn[3 * pp + 1] - f.y) * turn_f[1];
+            float dz = (float)(int)(pturn[3 * pp + 2] - f.z) * turn_f[2];
+            if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < cut_f)
+              hit |= 1u << pp;
+          }
         }
       }
-      // the listed pairs' neighbour data, loaded while the list is formed
-      double2 pxy = make_double2(0.0, 0.0), pzq = pxy;
-      if (in) {
-        const double2 *pq = (const double2 *)(b.cell_pos + s);
-        pxy = __ldcg(pq);
-        pzq = __ldcg(pq + 1);
+      const int cnt = __popc(hit);
+      int incl = cnt;
+      for (int o = 1; o < 32; o <<= 1) {
+        int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o)
+          incl += v;
       }
-      unsigned mask = __ballot_sync(0xffffffffu, in);
-      if (lane == 0)
-        icl_warp[warp] = __popc(mask);
+      if (lane == 31)
+        icl_warp[warp] = incl;
       __syncthreads();
       if (threadIdx.x == 0) {
         int run = icl_n;
@@ -923,21 +918,30 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
         icl_warp[CT / 32] = run;
       }
       __syncthreads();
-      if (in) {
-        int pos = icl_warp[warp] + __popc(mask & ((1u << lane) - 1u));
-        if (pos < ICL_MAX) {
-          icl_pos[pos][0] = pxy;
-          icl_pos[pos][1] = pzq;
-          icl_meta[pos] = mj;
-          icl_unit[pos] = (short)u;
-        } else {
-          // past the list (not met at liquid densities): evaluated here
-          pair_term(A, S, u, pxy, pzq, mj, lj, re, ovl);
+      if (hit) {
+        const double2 pxy = oxy[i], pzq = ozq[i];
+        int pos = icl_warp[warp] + incl - cnt;
+        for (unsigned h = hit; h; h &= h - 1) {
+          const int pp = __ffs(h) - 1;
+          const int side = pp >= na ? 1 : 0, a = pp - side * na;
+          const int u = (a * 2 + side) * NB27;
+          if (pos < ICL_MAX) {
+            icl_pos[pos][0] = pxy;
+            icl_pos[pos][1] = pzq;
+            icl_meta[pos] = (int)f.w;
+            icl_unit[pos] = (short)u;
+          } else {
+            // past the list (not met at liquid densities): evaluated here
+            pair_term(A, S, u, pxy, pzq, (int)f.w, lj, re, ovl);
+          }
+          ++pos;
         }
       }
       icl_n = icl_warp[CT / 32];
       __syncthreads();
     }
+    __syncthreads();  // the x-y products (a CTA may own no atoms)
+    mark(1);
     // (2) Warp 3 evaluates the listed pairs (the FP64-heavy LJ and
     //     erfc-screened Coulomb terms) while warps 0, 1, 2, 4, 5, 6 take the
     //     k-vectors: with warps issued to the SM's four sub-partitions by
@@ -1018,6 +1022,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
           __stcg(part_t + (size_t)cta * 4 + 3, any ? 1.0 : 0.0);
       }
     }
+    mark(2);
     // ---------------- phase B ----------------
     // The last CTA (the leader) waits for every CTA's partials, reduces them
     // in a fixed order, decides, commits an accepted move (coordinates,
@@ -1180,39 +1185,18 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
         }
         acc = __shfl_sync(0xffffffffu, acc, 0);
         if (acc) {
-          // Atoms that stay in their cell are rewritten in place by one
-          // lane each; then the atoms that change cell are relinked one
-          // after another, in atom order -- the slot layout that relinking
-          // every atom in order would give.
-          int a0 = b.mstart[m], a = lane;
-          bool stay = false;
-          if (a < na) {
-            const double *np = S.hdr + 48 + 3 * a;
-            b.x[a0 + a] = np[0];
-            b.y[a0 + a] = np[1];
-            b.z[a0 + a] = np[2];
-            int c1 = (int)S.hdr[16 + a];
-            stay = __ldcg(b.atom_cell + a0 + a) == c1;
-            if (stay)
-              cell_write_slot(b, c1, __ldcg(b.atom_slot + a0 + a), a0 + a,
-                              np[0], np[1], np[2],
-                              (const uint32_t *)(S.hdr + 84) + (na + a) * 3);
+          // the new coordinates and centre (the cell grid is rebuilt from
+          // the coordinates after the launch)
+          if (lane < na) {
+            const double *np = S.hdr + 48 + 3 * lane;
+            b.x[a0m + lane] = np[0];
+            b.y[a0m + lane] = np[1];
+            b.z[a0m + lane] = np[2];
           }
-          unsigned moving = __ballot_sync(0xffffffffu, a < na && !stay);
-          __syncwarp();
-          if (a == 0) {
-            for (int i = 0; i < na; ++i)
-              if (moving & (1u << i)) {
-                const double *np = S.hdr + 48 + 3 * i;
-                cell_move_atom(b, a0 + i, np[0], np[1], np[2],
-                               (int)S.hdr[16 + i],
-                               (const uint32_t *)(S.hdr + 84) + (na + i) * 3);
-              }
-            if ((int)S.hdr[1] == 0) {
-              b.cx[m] = S.hdr[4];
-              b.cy[m] = S.hdr[5];
-              b.cz[m] = S.hdr[6];
-            }
+          if (lane == 0 && (int)S.hdr[1] == 0) {
+            b.cx[m] = S.hdr[4];
+            b.cy[m] = S.hdr[5];
+            b.cz[m] = S.hdr[6];
           }
           __syncwarp();
         }
@@ -1255,6 +1239,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     __syncthreads();
     if (!S.ok)
       return;
+    mark(3);
     const int acc = S.accept;
     if (threadIdx.x == 0)
       settings_update(S.set, (int)S.hdr[1], acc);
@@ -1263,6 +1248,18 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
         sR[i] = nR[i];
         sI[i] = nI[i];
       }
+      // the moved atoms this CTA owns take their new positions
+      for (int a = threadIdx.x; a < na; a += CT) {
+        const int ga = a0m + a, i = ga / G;
+        if (ga - i * G == cta) {
+          const double *np = S.hdr + 48 + 3 * a;
+          const uint32_t *pt = (const uint32_t *)(S.hdr + 84) + (na + a) * 3;
+          oxy[i] = make_double2(np[0], np[1]);
+          ozq[i].x = np[2];
+          ot[i] = make_uint4(pt[0], pt[1], pt[2], ot[i].w);
+        }
+      }
+      __syncthreads();  // before the next context overwrites the header
     }
     if (t + 1 < A.n) {
       long long step = A.first + t + 1;
@@ -1281,6 +1278,12 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
           return;
       }
     }
+    mark(4);
+  }
+  if (prof) {
+    for (int ph = 0; ph < 5; ++ph)
+      A.prof[5 * pslot + ph] += pacc[ph];
+    A.prof[10 + pslot] += A.n;
   }
   // write back this CTA's structure factors; the leader the settings and
   // the running energies
@@ -1616,10 +1619,12 @@ void mc_destroy(Box &b) {
 
 static size_t chain_smem(const Box &b, int grid) {
   int kc_max = (b.dev.K + grid - 1) / grid;
+  size_t own_per = ((size_t)b.dev.n_atoms + grid - 1) / grid;
   return sizeof(double) * ((5 * (size_t)kc_max + (kc_max + 1) / 2 + 1) & ~(size_t)1) +
          sizeof(double2) * (size_t)(2 * MAX_MOL_ATOMS * 3) * (b.dev.kmax + 1) +
          sizeof(double2) * (size_t)NPAIR_CAP * 2 * MAX_MOL_ATOMS +
-         sizeof(unsigned short) * (size_t)kc_max + 64;
+         sizeof(unsigned short) * (size_t)kc_max + 64 +
+         own_per * (2 * sizeof(double2) + sizeof(uint4));
 }
 
 int mc_init(Box &b, const gb_mc_params &p) {
@@ -1868,6 +1873,38 @@ static void harvest(McState &s) {
   s.mp_ev.clear();
 }
 
+int mc_profile(Box &b, int enable, double *us10, int64_t *moves2) {
+  if (!b.mc)
+    return b.Fail(ERR_STATE, "gb_mc_init has not been called");
+  McState &s = *b.mc;
+  int rc;
+  if (!s.d_prof) {
+    if ((rc = mc_alloc(b, s, &s.d_prof, 12)) ||
+        (rc = b.CudaCheck(cudaMemsetAsync(s.d_prof, 0, 12 * sizeof(long long),
+                                          b.stream),
+                          "memset")))
+      return rc;
+  }
+  long long hp[12];
+  if ((rc = b.CudaCheck(cudaMemcpyAsync(hp, s.d_prof, sizeof hp,
+                                        cudaMemcpyDeviceToHost, b.stream),
+                        "download")) ||
+      (rc = b.CudaCheck(cudaMemsetAsync(s.d_prof, 0, sizeof hp, b.stream),
+                        "memset")) ||
+      (rc = b.Sync()))
+    return rc;
+  int khz = 0;
+  cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, b.cfg.device);
+  for (int k = 0; k < 10; ++k)
+    if (us10)
+      us10[k] = khz > 0 ? (double)hp[k] / (khz * 1e-3) : 0.0;
+  for (int k = 0; k < 2; ++k)
+    if (moves2)
+      moves2[k] = hp[10 + k];
+  s.profile = enable != 0;
+  return OK;
+}
+
 int mc_timing(Box &b, int reset, double *chain_ms, int64_t *chain_launches,
               int64_t *chain_moves, double *mp_ms, int64_t *mp_moves) {
   if (!b.mc)
@@ -1912,6 +1949,7 @@ static int run_chain(Box &b, McState &s, const MoveRec *moves, int64_t first,
   A.nrows_max = b.dev.K > 0 ? 6 * s.na_max : 0;
   A.tr_i = tr_i;
   A.tr_d = tr_d;
+  A.prof = s.profile ? s.d_prof : nullptr;
   void *args[] = {&A};
   size_t sm = chain_smem(b, s.grid);
   // the per-launch counters of the decision protocol start from zero
@@ -1930,6 +1968,10 @@ static int run_chain(Box &b, McState &s, const MoveRec *moves, int64_t first,
                                                    dim3(s.grid), dim3(CT), args,
                                                    sm, b.stream),
                        "chain kernel");
+  // the chain keeps positions, not cell slots: CellList::GridAll of the new
+  // coordinates brings the grid up to date
+  if (!rc)
+    rc = launch_grid_all(b, b.dev);
   cudaEventRecord(ev.second, b.stream);
   s.chain_ev.push_back(ev);
   s.chain_ev_moves.push_back(n);

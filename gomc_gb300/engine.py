@@ -447,6 +447,19 @@ class Box:
         return dict(chain_ms=cm.value, chain_launches=cl.value,
                     chain_moves=cn.value, mp_ms=mm.value, mp_moves=mn.value)
 
+    def mc_profile(self, enable: bool = True) -> dict:
+        """FP64 chain phase clocks since the last call (gb_mc_profile): per
+        move phase, microseconds of CTA 0 and of the deciding CTA."""
+        us = np.zeros(10)
+        mv = np.zeros(2, np.int64)
+        self._chk(lib().gb_mc_profile(self.h, int(enable), _dp(us),
+                                      mv.ctypes.data_as(C.POINTER(C.c_int64))))
+        names = ["context", "listing", "partials", "decision_wait",
+                 "commit_next"]
+        return dict(cta0=dict(zip(names, us[:5].tolist())),
+                    leader=dict(zip(names, us[5:].tolist())),
+                    moves=mv.tolist())
+
     def mc_layout(self) -> dict:
         c, n = C.c_int32(), C.c_int32()
         sm = C.c_int64()
