@@ -794,6 +794,8 @@ def run_gb300(args, rank, world):
     phase_us = {who: {k: v / max(pr["moves"][i], 1)
                       for k, v in pr[who].items()}
                 for i, who in enumerate(("cta0", "leader"))}
+    phase_us["cta0"]["context_written_after_phase_a"] = (
+        pr["cta0_context_written_after_phase_a"] / max(pr["moves"][0], 1))
     t_total = float(sum(times))
     t_total = max_over_ranks(t_total, dist, torch, dev)
     value = world * args.steps * M / t_total

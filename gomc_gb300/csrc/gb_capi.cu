@@ -448,12 +448,12 @@ int gb_mc_timing(gb_box *box, int32_t reset, double *chain_ms,
   return gb::mc_timing(*box->b, reset, chain_ms, chain_launches, chain_moves,
                        mp_ms, mp_moves);
 }
-int gb_mc_profile(gb_box *box, int32_t enable, double *us10,
+int gb_mc_profile(gb_box *box, int32_t enable, double *us13,
                   int64_t *moves2) {
   int rc = guard(box);
   if (rc)
     return rc;
-  return gb::mc_profile(*box->b, enable, us10, moves2);
+  return gb::mc_profile(*box->b, enable, us13, moves2);
 }
 int gb_mc_drift(gb_box *box, double *max4, double *last4, int64_t *n) {
   int rc = guard(box);

@@ -227,7 +227,8 @@ __device__ bool wait_geq(const unsigned *p, unsigned target, int *err,
     if ((it & 255u) == 0 && *(volatile int *)err)
       return false;
   }
-  __threadfence();
+  // the acquire load that saw the target orders this thread's later
+  // reads (and, through the CTA barrier after it, the other threads')
   return *(volatile int *)err == 0;
 }
 
@@ -248,7 +249,7 @@ __device__ bool warp_wait_all(const unsigned *flags, int n, unsigned target,
     bool mine = true;
 #pragma unroll 4
     for (int c = lane; c < n; c += 32)
-      mine &= (int)(*(const volatile unsigned *)(flags + c) - target) >= 0;
+      mine &= (int)(ld_acquire(flags + c) - target) >= 0;
     if (__all_sync(0xffffffffu, mine))
       break;
     int bad = 0;
@@ -263,7 +264,6 @@ __device__ bool warp_wait_all(const unsigned *flags, int n, unsigned target,
     if (__shfl_sync(0xffffffffu, bad, 0))
       return false;
   }
-  __threadfence();
   return true;
 }
 
@@ -387,6 +387,12 @@ constexpr int PART_MAX_GRID = 256;  // partial slots the leader holds per lane: 
 constexpr int NPAIR_CAP = 64; // (n_x, n_y) columns a CTA's k-chunk may span
                               // for the shared x-y phase products
 
+// CTAs of the chain grid without a k-chunk: the context writers 0 ..
+// nrows_max - 1 when they are at most half the grid, else none.
+__host__ __device__ inline int chain_kless(int nrows_max, int grid) {
+  return nrows_max > 0 && 2 * nrows_max <= grid ? nrows_max : 0;
+}
+
 // doubles of one move context: the header and 2 MAX_MOL_ATOMS x 3 phase
 // rows of kmax + 1 double2 entries
 __host__ __device__ constexpr size_t chain_ctx_len(int stride) {
@@ -418,7 +424,9 @@ struct ChainArgs {
   double *tr_d;   // [n][3] or null
   // phase clocks (NULL: not collected): [0 CTA 0, 1 the leader][phase:
   // context load, real-space listing, pair terms and k-vectors to the
-  // partials, decision wait, commit and next context], then moves
+  // partials, decision wait, commit and next context], then moves; then,
+  // from the end of phase A, the leader's last partial, its last context
+  // flag, and CTA 0's part of the next context written
   long long *prof;
 };
 
@@ -430,8 +438,13 @@ struct ChainShared {
   double red3[3][CT / 32];
   int ovl_any;
   double tot[4];
-  int accept, flag, ok;
+  int accept, flag, ok, bok;
   unsigned gen;
+  // the last decided move: its molecule, outcome and new positions and
+  // centre (the leader writes them to global memory after it publishes)
+  int last_m, last_acc;
+  double last_newp[MAX_MOL_ATOMS][3], last_newcom[3];
+  long long pclk[3];  // phase-clock marks of other warps (gb_mc_profile)
   // inputs and new positions of the context being built
   double b_oldp[MAX_MOL_ATOMS][3], b_newp[MAX_MOL_ATOMS][3];
   double b_com[3], b_newcom[3], b_prop[12], b_q[MAX_MOL_ATOMS];
@@ -459,10 +472,11 @@ __device__ __forceinline__ bool ctx_writer(const ChainArgs &A, int na) {
 // (threads tid = 0..count-1 of the CTA, count >= 128; the tasks sit on
 // different warps so that they overlap): the proposal applied
 // (Coordinates::TranslateRand / RotateRand arithmetic, see apply_proposal),
-// the header (CTA 0), this CTA's phase row, and -- with `report` -- this
-// CTA's flag for the leader.
+// the header (CTA 0) and this CTA's phase row.  Used where a context is
+// built behind a grid barrier (the first move, and a move that follows one
+// of the same molecule or a settings adjustment).
 __device__ void build_ctx_rest(const ChainArgs &A, ChainShared &S, int t,
-                               int tid, int count, bool report) {
+                               int tid, int count) {
   const DevBox &b = A.b;
   const int m = S.b_m, na = S.b_na, kind = S.b_kind;
   const int G = gridDim.x;
@@ -543,14 +557,92 @@ __device__ void build_ctx_rest(const ChainArgs &A, ChainShared &S, int t,
         tab[(size_t)rr * stride + n] = cis_turns64((uint64_t)n * u);
     }
   }
-  if (report) {
-    // this CTA's part of the context is written: flag it for the leader
-    group_sync(count);
-    if (tid == 0) {
-      __threadfence();
-      st_release(A.seq + SEQ_CTX + blockIdx.x, (unsigned)t);
+}
+
+// Move t's context from the inputs in S.b_* by one warp, then this CTA's
+// flag for the leader: the same tasks as build_ctx_rest, in sequence.
+__device__ void build_ctx_warp(const ChainArgs &A, ChainShared &S, int t) {
+  const DevBox &b = A.b;
+  const int lane = threadIdx.x & 31;
+  const int m = S.b_m, na = S.b_na, kind = S.b_kind;
+  const int G = gridDim.x;
+  const int stride = b.kmax + 1;
+  const int nrows = b.K > 0 ? 2 * na * 3 : 0;
+  const double *prop = S.b_prop;
+  if (lane < na) {
+    const int a = lane;
+    double v[3], w[3];
+    if (kind == 0) {
+      for (int d = 0; d < 3; ++d)
+        w[d] = wrap1(__dadd_rn(S.b_oldp[a][d], prop[d]), b.L[d]);
+    } else {
+      for (int d = 0; d < 3; ++d) {
+        v[d] = unwrap1(S.b_oldp[a][d], S.b_com[d], b.L[d], b.half[d]);
+        v[d] = __dadd_rn(v[d], -S.b_com[d]);
+      }
+      for (int i = 0; i < 3; ++i) {
+        double u = __dadd_rn(__dadd_rn(__dmul_rn(prop[3 * i], v[0]),
+                                       __dmul_rn(prop[3 * i + 1], v[1])),
+                             __dmul_rn(prop[3 * i + 2], v[2]));
+        w[i] = wrap1(__dadd_rn(u, S.b_com[i]), b.L[i]);
+      }
+    }
+    for (int d = 0; d < 3; ++d)
+      S.b_newp[a][d] = w[d];
+  } else if (lane >= 8 && lane < 11) {
+    const int d = lane - 8;
+    S.b_newcom[d] = kind == 0 ? wrap1(__dadd_rn(S.b_com[d], prop[d]), b.L[d])
+                              : S.b_com[d];
+  }
+  __syncwarp();
+  double *const ctx = A.ctx + (size_t)(t & 1) * A.ctx_len;
+  if (blockIdx.x == 0) {
+    double *h = ctx;
+    if (lane == 0) {
+      h[0] = m;
+      h[1] = kind;
+      h[2] = na;
+      h[3] = S.b_pacc;
+      h[80] = S.b_lpacc;
+      h[81] = S.b_lpacc + 1e-9;  // the decision's margins, precomputed
+      h[82] = S.b_lpacc - 1e-9;
+      for (int d = 0; d < 3; ++d)
+        h[4 + d] = S.b_newcom[d];
+    }
+    if (lane >= 16 && lane < 16 + 2 * na) {
+      const int i = lane - 16, a = i % na, side = i / na;
+      const double *p = side ? S.b_newp[a] : S.b_oldp[a];
+      h[(side ? 16 : 8) + a] = position_to_cell_fast(b, p[0], p[1], p[2]);
+      for (int d = 0; d < 3; ++d)
+        h[(side ? 48 : 24) + 3 * a + d] = p[d];
+      if (side == 0) {
+        double q = S.b_q[a];
+        h[72 + a] = fabs(q) < 0.000000001 ? 0.0 : q;
+        h[108 + a] = q;  // the charge and kind of the real-space terms
+        ((int *)(h + 116))[a] = S.b_ka[a];
+      }
+    }
+    for (int i = lane; i < 6 * na; i += 32) {
+      const int pa = i / 3, d = i % 3;  // pa = side * na + atom
+      const double *p = pa < na ? S.b_oldp[pa] : S.b_newp[pa - na];
+      ((uint32_t *)(h + 84))[i] = to_turns(p[d], b.invL[d]);
     }
   }
+  // phase rows exp(i n 2 pi r_d / L_d), n = 0..kmax (as build_ctx_rest)
+  double2 *tab = (double2 *)(ctx + HDR);
+  for (int rr = blockIdx.x; rr < nrows; rr += G) {
+    const int p = rr / 3, d = rr % 3;
+    const double coord = p < na ? S.b_oldp[p][d] : S.b_newp[p - na][d];
+    double tt = coord * b.invL[d];
+    if (tt >= 1.0)
+      tt -= 1.0;
+    const uint64_t u = __double2ull_rn(tt * 18446744073709551616.0);  // 2^64
+    for (int n = lane; n < stride; n += 32)
+      tab[(size_t)rr * stride + n] = cis_turns64((uint64_t)n * u);
+  }
+  __syncwarp();
+  if (lane == 0)  // a release store: it orders the warp's writes before it
+    st_release(A.seq + SEQ_CTX + blockIdx.x, (unsigned)t);
 }
 
 // Build move t's context with threads [first, first + count) of the CTA,
@@ -593,7 +685,7 @@ __device__ void build_ctx(const ChainArgs &A, ChainShared &S, int t,
     S.b_ka[a] = b.kind[a0 + a];
   }
   group_sync(count);
-  build_ctx_rest(A, S, t, tid, count, false);
+  build_ctx_rest(A, S, t, tid, count);
 }
 
 // Inputs of move t's context gathered by one warp in registers, in two
@@ -616,7 +708,9 @@ __device__ __forceinline__ void ctx_pre1(const ChainArgs &A, int t, CtxPre &c) {
   c.a0 = A.b.mstart[c.m];
   c.na = A.b.mstart[c.m + 1] - c.a0;
 }
-__device__ __forceinline__ void ctx_pre2(const ChainArgs &A, int t, CtxPre &c) {
+__device__ __forceinline__ void ctx_pre2(const ChainArgs &A,
+                                         const ChainShared &S, int t,
+                                         CtxPre &c) {
   const DevBox &b = A.b;
   const int lane = threadIdx.x & 31;
   c.writer = ctx_writer(A, c.na);
@@ -624,13 +718,18 @@ __device__ __forceinline__ void ctx_pre2(const ChainArgs &A, int t, CtxPre &c) {
   c.ka = 0;
   if (!c.writer)
     return;
+  // the molecule of the move decided last has its new positions here (the
+  // leader writes them to global memory only after it publishes)
+  const bool last = c.m == S.last_m && S.last_acc;
   if (lane < 12)
     c.v0 = A.prop[(size_t)t * 12 + lane];
   else if (lane < 15)
-    c.v0 = __ldcg((lane == 12 ? b.cx : lane == 13 ? b.cy : b.cz) + c.m);
+    c.v0 = last ? S.last_newcom[lane - 12]
+                : __ldcg((lane == 12 ? b.cx : lane == 13 ? b.cy : b.cz) + c.m);
   if (lane < 3 * c.na) {
     int a = lane / 3, d = lane % 3;
-    c.v1 = __ldcg((d == 0 ? b.x : d == 1 ? b.y : b.z) + c.a0 + a);
+    c.v1 = last ? S.last_newp[a][d]
+                : __ldcg((d == 0 ? b.x : d == 1 ? b.y : b.z) + c.a0 + a);
   }
   if (lane < c.na) {
     c.q = b.q[c.a0 + lane];
@@ -660,14 +759,6 @@ __device__ __forceinline__ void ctx_pre_store(ChainShared &S, const CtxPre &c) {
   }
 }
 
-// CTAs that write part of move t's context: CTA 0 (header) and one CTA
-// per phase row.
-__device__ __forceinline__ unsigned ctx_builders(const ChainArgs &A, int t) {
-  int m = A.moves[t].mol;
-  int na = A.b.mstart[m + 1] - A.b.mstart[m];
-  int nrows = A.b.K > 0 ? 2 * na * 3 : 0;
-  return (unsigned)max(1, min((int)gridDim.x, nrows));
-}
 
 // FP64 term of one candidate pair of the chain: unit u (atom, old/new side,
 // neighbour cell) against cell slot s: the exact minimum-image distance and
@@ -716,9 +807,17 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
   const DevBox &b = A.b;
   const FF &ff = *A.ff;
   int G = gridDim.x, cta = blockIdx.x;
-  int kc_max = (b.K + G - 1) / G;
-  int kbeg = min(b.K, cta * kc_max);
-  int kc = min(kc_max, b.K - kbeg);
+  // The context writers (CTAs below nrows_max) build the next move's
+  // context during phase A; they take no k-vectors, so that its FP64 chain
+  // does not queue behind the k-vector warps' (the others' chunks grow by a
+  // few lanes of the same warp passes).
+  const int nkb = chain_kless(A.nrows_max, G);
+  const int kG = G - nkb;
+  int kc_max = (b.K + kG - 1) / kG;
+  int kbeg = cta < nkb ? b.K : min(b.K, (cta - nkb) * kc_max);
+  int kc = cta < nkb ? 0 : min(kc_max, b.K - kbeg);
+  const bool kless = cta < nkb;
+  const int pw = kless ? 0 : 3;  // the warp that evaluates the pair terms
   double *sR = dyn, *sI = sR + kc_max, *nR = sI + kc_max, *nI = nR + kc_max,
          *pf = nI + kc_max;
   char4 *kn = (char4 *)(pf + kc_max);
@@ -759,6 +858,9 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
                        (unsigned)pack_meta(b.mol[a], b.kind[a]));
   }
   if (threadIdx.x == 0) {
+    S.pclk[0] = S.pclk[1] = S.pclk[2] = 0;
+    S.last_m = -1;
+    S.last_acc = 0;
     S.set = *A.set;
     for (int i = 0; i < 5; ++i)
       S.e_run[i] = b.energy[i];
@@ -816,7 +918,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
 
   const int pslot = cta == 0 ? 0 : cta == G - 1 ? 1 : -1;
   const bool prof = A.prof && threadIdx.x == 0 && pslot >= 0;
-  long long pacc[5] = {0, 0, 0, 0, 0};
+  long long pacc[5] = {0, 0, 0, 0, 0}, poff[3] = {0, 0, 0}, tb = 0;
   long long tclk = prof ? clock64() : 0;
   auto mark = [&](int ph) {
     if (prof) {
@@ -825,7 +927,20 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
       tclk = now;
     }
   };
+  // the molecule of the move after the current one, loaded a move ahead;
+  // warp 7 also loads that move's record and atom range a move ahead
+  int nmol = A.n > 1 ? A.moves[1].mol : -1;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  CtxPre pre_nx;
+  pre_nx.writer = false;
+  if (warp == 7 && A.n > 1)
+    ctx_pre1(A, 1, pre_nx);
   for (int t = 0; t < A.n; ++t) {
+    const int mol_next = nmol;
+    nmol = t + 2 < A.n ? A.moves[t + 2].mol : -1;
+    CtxPre pre = pre_nx;
+    if (warp == 7 && t + 2 < A.n)
+      ctx_pre1(A, t + 2, pre_nx);
     // ---------------- phase A ----------------
     // the header and the rows of the largest molecule in one round trip
     const double *ctx_t = A.ctx + (size_t)(t & 1) * A.ctx_len;
@@ -843,14 +958,18 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     // barrier.  Otherwise warp 7 of each context writer gathers its inputs
     // during this phase (the loads overlap it) and the writer builds it
     // right after its partials are out.
-    const bool spec = t + 1 < A.n && A.moves[t + 1].mol != m &&
+    const bool spec = t + 1 < A.n && mol_next != m &&
                       (A.first + t + 2) % S.set.adj != 0;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    CtxPre pre;
     pre.writer = false;
     const bool wload = spec && warp == 7;
-    if (wload)
-      ctx_pre1(A, t + 1, pre);
+    // the leader's warp 4 counts the next context's writers now (the loads
+    // arrive during this phase)
+    int nbuild = 1;
+    if (spec && warp == 4 && cta == G - 1) {
+      const int a0n = __ldg(b.mstart + mol_next);
+      const int nan = __ldg(b.mstart + mol_next + 1) - a0n;
+      nbuild = max(1, min(G, b.K > 0 ? 2 * nan * 3 : 0));
+    }
     double lj = 0.0, re = 0.0, ovl = 0.0, er = 0.0;
     // first atom of the moved molecule, for the commit to the own atoms
     const int a0m = __ldg(b.mstart + m);
@@ -864,7 +983,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
       exy[e] = make_double2(q * v.x, q * v.y);
     }
     if (wload)
-      ctx_pre2(A, t + 1, pre);
+      ctx_pre2(A, S, t + 1, pre);
     // (1) Real space: this CTA's own atoms against the old and new
     //     positions of the moved atoms.  An FP32 pre-test on the
     //     fixed-point turns (the wrapped integer difference is the minimum
@@ -946,14 +1065,49 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     //     erfc-screened Coulomb terms) while warps 0, 1, 2, 4, 5, 6 take the
     //     k-vectors: with warps issued to the SM's four sub-partitions by
     //     warp index modulo 4, the pair terms run beside the k-vectors
-    //     instead of after them.
+    //     instead of after them.  In a context writer without k-vectors
+    //     warp 0 takes the pairs and warps 1..7 build the next context.
     const int n_eval = min(icl_n, ICL_MAX);
-    if (warp == 3) {
+    if (warp == pw) {
       for (int i = lane; i < n_eval; i += 32)
         pair_term(A, S, icl_unit[i], icl_pos[i][0], icl_pos[i][1],
                   icl_meta[i], lj, re, ovl);
     }
-    if (warp != 3 && warp != 7) {
+    if (kless) {
+      // A context writer without k-vectors: warps 1..7 build its part of
+      // the next move's context now, from the inputs warp 7 gathered at the
+      // start of this phase, so that the context is complete by the time
+      // the other CTAs' partials are in.
+      if (spec && warp >= 1) {
+        if (warp == 7) {
+          if (pre.writer)
+            ctx_pre_store(S, pre);
+          if (lane == 0)
+            S.b_writer = pre.writer;
+        }
+        group_sync(CT - 32);
+        if (S.b_writer) {
+          build_ctx_rest(A, S, t + 1, (int)threadIdx.x - 32, CT - 32);
+          group_sync(CT - 32);
+          if (threadIdx.x == 32) {
+            // a release store: it orders the writes of the warps that met
+            // at the barrier before it
+            st_release(A.seq + SEQ_CTX + blockIdx.x, (unsigned)(t + 1));
+            if (A.prof)
+              S.pclk[2] = clock64();
+          }
+        }
+      }
+    } else if (wload && pre.writer) {
+      // warp 7 of a context writer with k-vectors (a grid too small for
+      // k-less writers) builds its part beside the k-vector warps
+      ctx_pre_store(S, pre);
+      __syncwarp();
+      build_ctx_warp(A, S, t + 1);
+      if (A.prof && lane == 0)
+        S.pclk[2] = clock64();
+    }
+    if (!kless && warp != 3 && warp != 7) {
       const int kw = warp < 3 ? warp : warp - 1;  // 0..5
       for (int i = kw * 32 + lane; i < kc; i += 6 * 32) {
         char4 n = kn[i];
@@ -995,15 +1149,23 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
         er += (srn * srn + sin_ * sin_) * pf[i];
       }
     }
-    // CTA partials: the three sums in one pass (warp shuffles, then lanes
-    // 0..2 of warp 0 each add one quantity over the warps, fixed order);
-    // the overlap flag by vote
+    // CTA partials in a fixed order: the pair terms are warp 3's (all
+    // warps' when the list overflowed and other threads evaluated pairs),
+    // the reciprocal energy is the k-vector warps'; only those warps reduce
+    // (warp shuffles, then lanes 0..2 of warp 0 add over the warps); the
+    // overlap flag by vote
     {
+      const bool all_pairs = icl_n > ICL_MAX;
       double v0 = lj, v1 = re, v2 = er;
-      for (int o = 16; o > 0; o >>= 1) {
-        v0 += __shfl_down_sync(0xffffffffu, v0, o);
-        v1 += __shfl_down_sync(0xffffffffu, v1, o);
-        v2 += __shfl_down_sync(0xffffffffu, v2, o);
+      if (warp == pw || all_pairs) {
+        for (int o = 16; o > 0; o >>= 1) {
+          v0 += __shfl_down_sync(0xffffffffu, v0, o);
+          v1 += __shfl_down_sync(0xffffffffu, v1, o);
+        }
+      }
+      if (!kless && warp != 3 && warp != 7) {
+        for (int o = 16; o > 0; o >>= 1)
+          v2 += __shfl_down_sync(0xffffffffu, v2, o);
       }
       int any = __syncthreads_or(ovl > 0.0);
       if (lane == 0) {
@@ -1015,14 +1177,20 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
       double *part_t = A.part + (size_t)(t & 1) * G * 4;
       if (threadIdx.x < 3) {
         double r = 0.0;
-        for (int w = 0; w < CT / 32; ++w)
-          r += S.red3[threadIdx.x][w];
+        if (threadIdx.x < 2 && !all_pairs) {
+          r = S.red3[threadIdx.x][pw];
+        } else if (threadIdx.x < 2 || !kless) {
+          for (int w = 0; w < CT / 32; ++w)
+            if (threadIdx.x < 2 || (w != 3 && w != 7))
+              r += S.red3[threadIdx.x][w];
+        }
         __stcg(part_t + (size_t)cta * 4 + threadIdx.x, r);
         if (threadIdx.x == 0)
           __stcg(part_t + (size_t)cta * 4 + 3, any ? 1.0 : 0.0);
       }
     }
     mark(2);
+    tb = tclk;  // phase B starts
     // ---------------- phase B ----------------
     // The last CTA (the leader) waits for every CTA's partials, reduces them
     // in a fixed order, decides, commits an accepted move (coordinates,
@@ -1036,22 +1204,20 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     // word orders the decision, the commit and the next context before
     // every CTA's next phase A.
     const bool leader = cta == G - 1;
-    // threads of this CTA that build its part of the next context (when it
-    // is a writer): warps 1..7, or warps 4..7 in the leader, from the inputs
-    // warp 7 gathered during phase A, with the FP64 pipes free
-    const int bfirst = leader ? 128 : 32;
-    if ((int)threadIdx.x >= bfirst) {
-      if (spec) {
-        if (warp == 7) {
-          if (pre.writer)
-            ctx_pre_store(S, pre);
-          if (lane == 0)
-            S.b_writer = pre.writer;
+    if ((int)threadIdx.x >= 128) {
+      if (leader && warp == 4) {
+        // the writers' flags of the next context, polled from the start of
+        // phase B beside the partials; warp 0 reads the outcome at barrier
+        // 3 before it publishes
+        int bok = spec ? warp_wait_all(A.seq + SEQ_CTX, nbuild,
+                                       (unsigned)(t + 1), b.err)
+                       : 1;
+        if (lane == 0) {
+          S.bok = bok;
+          if (A.prof)
+            S.pclk[1] = clock64();
         }
-        group_sync(CT - bfirst);
-        if (S.b_writer)
-          build_ctx_rest(A, S, t + 1, (int)threadIdx.x - bfirst, CT - bfirst,
-                         true);
+        asm volatile("bar.sync 3, 64;" ::: "memory");
       }
     } else if (leader) {
       // Warps 0..3 of the leader each gather one quantity over all CTAs
@@ -1114,19 +1280,24 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
           break;
         }
       }
+      if (A.prof && lane == 0 && q == 0)
+        S.pclk[0] = clock64();
       double pv[PF];
 #pragma unroll
       for (int i = 0; i < PF; ++i)
         pv[i] = got == 0 ? pp[0][i] : got == 1 ? pp[1][i] : pp[2][i];
-      if (ok) {
-        // read: mark this quantity's slots empty for move t + 2 (ordered
-        // before the decision word that every later writer waits for)
+      // read: this quantity's slots are marked empty for move t + 2 after
+      // the decision word is out (before the next word, which every writer
+      // of move t + 2 waits for)
+      auto reset_slots = [&]() {
 #pragma unroll
         for (int i = 0; i < PF; ++i) {
           int c = lane + 32 * i;
           if (c < G)
             __stcg(part_t + (size_t)c * 4 + q, __longlong_as_double(PART_EMPTY));
         }
+      };
+      if (ok) {
         if (q < 3) {
           double v = 0.0;
 #pragma unroll
@@ -1151,18 +1322,9 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
       asm volatile("bar.sync 2, 128;" ::: "memory");
       ok = S.red3[0][0] != 0.0 && S.red3[0][1] != 0.0 && S.red3[0][2] != 0.0 &&
            S.red3[0][3] != 0.0;
+      if (warp != 0 && ok)
+        reset_slots();  // not ordered before warp 0's release below
       int acc = 0;
-      if (warp == 1 && ok) {
-        // the writers' flags of the next context, checked while warp 0
-        // decides and commits
-        int bok = spec ? warp_wait_all(A.seq + SEQ_CTX,
-                                       (int)ctx_builders(A, t + 1),
-                                       (unsigned)(t + 1), b.err)
-                       : 1;
-        if (lane == 0)
-          S.red3[1][0] = bok;
-        asm volatile("bar.sync 3, 64;" ::: "memory");
-      }
       if (warp == 0 && ok) {
         double dLJ = 0.0, dRe = 0.0, dRc = 0.0;
         if (lane == 0) {
@@ -1184,8 +1346,20 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
           acc = res && !over;
         }
         acc = __shfl_sync(0xffffffffu, acc, 0);
+        // the next context must be complete before the word goes out
+        asm volatile("bar.sync 3, 64;" ::: "memory");
+        ok = S.bok != 0;
+        // release: it orders the next context (through warp 4's acquire
+        // and barrier 3); no store of this move precedes it, so it does
+        // not wait for one
+        if (lane == 0 && ok)
+          st_release(A.seq, 2u * (unsigned)(t + 1) + (unsigned)acc);
+        if (ok)
+          reset_slots();
         if (acc) {
-          // the new coordinates and centre (the cell grid is rebuilt from
+          // the new coordinates and centre, after the word: the next
+          // context reads them from the last move's copy in shared memory,
+          // later ones after the next word (the cell grid is rebuilt from
           // the coordinates after the launch)
           if (lane < na) {
             const double *np = S.hdr + 48 + 3 * lane;
@@ -1199,13 +1373,6 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
             b.cz[m] = S.hdr[6];
           }
           __syncwarp();
-        }
-        // the next context must be complete before the word goes out
-        asm volatile("bar.sync 3, 64;" ::: "memory");
-        ok = S.red3[1][0] != 0.0;
-        if (lane == 0 && ok) {
-          __threadfence();
-          st_release(A.seq, 2u * (unsigned)(t + 1) + (unsigned)acc);
         }
         if (lane == 0) {
           // off the critical path: running energies and the trace
@@ -1225,9 +1392,12 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
           S.accept = acc;
           S.ok = ok;
         }
-      } else if (warp == 0 && lane == 0) {
-        S.accept = 0;
-        S.ok = 0;
+      } else if (warp == 0) {
+        asm volatile("bar.sync 3, 64;" ::: "memory");  // warp 4 is there
+        if (lane == 0) {
+          S.accept = 0;
+          S.ok = 0;
+        }
       }
     } else {
       if (threadIdx.x == 0) {
@@ -1240,13 +1410,31 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     if (!S.ok)
       return;
     mark(3);
+    if (prof) {
+      // when, after this CTA's phase A, the leader had every partial and
+      // every context flag, and this CTA (a context writer) had written
+      // its part of the next context
+      for (int k = 0; k < 3; ++k)
+        if (S.pclk[k])
+          poff[k] += S.pclk[k] - tb;
+      S.pclk[0] = S.pclk[1] = S.pclk[2] = 0;
+    }
     const int acc = S.accept;
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0) {
       settings_update(S.set, (int)S.hdr[1], acc);
+      S.last_m = m;
+      S.last_acc = acc;
+    }
     if (acc) {
       for (int i = threadIdx.x; i < kc; i += CT) {
         sR[i] = nR[i];
         sI[i] = nI[i];
+      }
+      for (int i = threadIdx.x; i < 3 * na + 3; i += CT) {
+        if (i < 3 * na)
+          S.last_newp[i / 3][i % 3] = S.hdr[48 + i];
+        else
+          S.last_newcom[i - 3 * na] = S.hdr[4 + i - 3 * na];
       }
       // the moved atoms this CTA owns take their new positions
       for (int a = threadIdx.x; a < na; a += CT) {
@@ -1284,6 +1472,12 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     for (int ph = 0; ph < 5; ++ph)
       A.prof[5 * pslot + ph] += pacc[ph];
     A.prof[10 + pslot] += A.n;
+    if (pslot == 1) {
+      A.prof[12] += poff[0];
+      A.prof[13] += poff[1];
+    } else {
+      A.prof[14] += poff[2];
+    }
   }
   // write back this CTA's structure factors; the leader the settings and
   // the running energies
@@ -1617,8 +1811,9 @@ void mc_destroy(Box &b) {
   b.mc = nullptr;
 }
 
-static size_t chain_smem(const Box &b, int grid) {
-  int kc_max = (b.dev.K + grid - 1) / grid;
+static size_t chain_smem(const Box &b, int grid, int nrows_max) {
+  const int kG = grid - chain_kless(nrows_max, grid);
+  int kc_max = (b.dev.K + kG - 1) / kG;
   size_t own_per = ((size_t)b.dev.n_atoms + grid - 1) / grid;
   return sizeof(double) * ((5 * (size_t)kc_max + (kc_max + 1) / 2 + 1) & ~(size_t)1) +
          sizeof(double2) * (size_t)(2 * MAX_MOL_ATOMS * 3) * (b.dev.kmax + 1) +
@@ -1674,7 +1869,7 @@ int mc_init(Box &b, const gb_mc_params &p) {
     return rc;
   // chain-kernel geometry: one CTA per SM (cooperative residency checked)
   int per_sm = 0;
-  size_t sm = chain_smem(b, b.sm_count);
+  size_t sm = chain_smem(b, b.sm_count, b.dev.K > 0 ? 6 * na_max : 0);
   raise_smem_limit((const void *)k_chain_fp64, sm);
   if ((rc = b.CudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                             &per_sm, k_chain_fp64, CT, sm),
@@ -1873,19 +2068,19 @@ static void harvest(McState &s) {
   s.mp_ev.clear();
 }
 
-int mc_profile(Box &b, int enable, double *us10, int64_t *moves2) {
+int mc_profile(Box &b, int enable, double *us13, int64_t *moves2) {
   if (!b.mc)
     return b.Fail(ERR_STATE, "gb_mc_init has not been called");
   McState &s = *b.mc;
   int rc;
   if (!s.d_prof) {
-    if ((rc = mc_alloc(b, s, &s.d_prof, 12)) ||
-        (rc = b.CudaCheck(cudaMemsetAsync(s.d_prof, 0, 12 * sizeof(long long),
+    if ((rc = mc_alloc(b, s, &s.d_prof, 15)) ||
+        (rc = b.CudaCheck(cudaMemsetAsync(s.d_prof, 0, 15 * sizeof(long long),
                                           b.stream),
                           "memset")))
       return rc;
   }
-  long long hp[12];
+  long long hp[15];
   if ((rc = b.CudaCheck(cudaMemcpyAsync(hp, s.d_prof, sizeof hp,
                                         cudaMemcpyDeviceToHost, b.stream),
                         "download")) ||
@@ -1895,9 +2090,9 @@ int mc_profile(Box &b, int enable, double *us10, int64_t *moves2) {
     return rc;
   int khz = 0;
   cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, b.cfg.device);
-  for (int k = 0; k < 10; ++k)
-    if (us10)
-      us10[k] = khz > 0 ? (double)hp[k] / (khz * 1e-3) : 0.0;
+  for (int k = 0; k < 13; ++k)
+    if (us13)
+      us13[k] = khz > 0 ? (double)hp[k < 10 ? k : k + 2] / (khz * 1e-3) : 0.0;
   for (int k = 0; k < 2; ++k)
     if (moves2)
       moves2[k] = hp[10 + k];
@@ -1951,7 +2146,7 @@ static int run_chain(Box &b, McState &s, const MoveRec *moves, int64_t first,
   A.tr_d = tr_d;
   A.prof = s.profile ? s.d_prof : nullptr;
   void *args[] = {&A};
-  size_t sm = chain_smem(b, s.grid);
+  size_t sm = chain_smem(b, s.grid, A.nrows_max);
   // the per-launch counters of the decision protocol start from zero
   int rc = b.CudaCheck(cudaMemsetAsync(s.d_seq, 0,
                                        (SEQ_CTX + PART_MAX_GRID) *

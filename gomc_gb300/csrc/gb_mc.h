@@ -128,7 +128,7 @@ struct McState {
 
 int mc_timing(Box &b, int reset, double *chain_ms, int64_t *chain_launches,
               int64_t *chain_moves, double *mp_ms, int64_t *mp_moves);
-int mc_profile(Box &b, int enable, double *us10, int64_t *moves2);
+int mc_profile(Box &b, int enable, double *us13, int64_t *moves2);
 
 // One chain of the mixed-precision chain kernel (gb_mixed.cu).
 struct MixedChain {

@@ -450,14 +450,17 @@ class Box:
     def mc_profile(self, enable: bool = True) -> dict:
         """FP64 chain phase clocks since the last call (gb_mc_profile): per
         move phase, microseconds of CTA 0 and of the deciding CTA."""
-        us = np.zeros(10)
+        us = np.zeros(13)
         mv = np.zeros(2, np.int64)
         self._chk(lib().gb_mc_profile(self.h, int(enable), _dp(us),
                                       mv.ctypes.data_as(C.POINTER(C.c_int64))))
         names = ["context", "listing", "partials", "decision_wait",
                  "commit_next"]
         return dict(cta0=dict(zip(names, us[:5].tolist())),
-                    leader=dict(zip(names, us[5:].tolist())),
+                    leader=dict(zip(names, us[5:10].tolist()),
+                                last_partial_after_phase_a=us[10],
+                                last_context_flag_after_phase_a=us[11]),
+                    cta0_context_written_after_phase_a=us[12],
                     moves=mv.tolist())
 
     def mc_layout(self) -> dict:

@@ -272,11 +272,14 @@ int gb_mc_timing(gb_box *box, int32_t reset, double *chain_ms,
  * the clocks of CTA 0 and of the deciding CTA (the last) since the last
  * call, per phase of a move (loading the move's context, listing the
  * real-space pairs, pair terms and k-vectors to the partials, waiting for
- * the decision, commit and the next context), as us10 (CTA 0's five, then
- * the last CTA's five) in microseconds at the rated SM clock, and the moves
- * each CTA timed; `enable` switches the collection on or off for the
- * following runs.  The mixed form is not timed here. */
-int gb_mc_profile(gb_box *box, int32_t enable, double *us10, int64_t *moves2);
+ * the decision, commit and the next context), as us13[0..9] (CTA 0's five,
+ * then the last CTA's five) in microseconds at the rated SM clock; us13[10]
+ * and [11]: when, counted from the end of its own phase A, the last CTA had
+ * every partial and every flag of the next context, and us13[12] when CTA 0
+ * had written its part of the next context; and the moves each CTA timed.
+ * `enable` switches the collection on or off for the following runs.  The
+ * mixed form is not timed here. */
+int gb_mc_profile(gb_box *box, int32_t enable, double *us13, int64_t *moves2);
 /* Mixed form: relative difference between the running energies and the
  * periodic full FP64 recompute (inter, real, recip, total), largest and
  * latest, and the number of recomputes so far.  No reference counterpart
