@@ -171,7 +171,10 @@ def measured_peaks(torch, dev):
     return out
 
 
-CHAIN_FP64_DRAM_BYTES_1000 = 3.32e6
+# DRAM bytes (read + write) of one 1,000-move k_chain_fp64 launch of the
+# 8,000-water workload after the L2 flush: mean of 13 launches of this
+# command's FP64 line under ncu (dram__bytes_read.sum 2.42 MB, write 0)
+CHAIN_FP64_DRAM_BYTES_1000 = 2.42e6
 SMALL = False  # --small: the 256-water, 19.7 A box (for profiler captures)
 
 
@@ -860,9 +863,8 @@ def run_gb300(args, rank, world):
     moves_per_launch = timing["chain_moves"] / max(timing["chain_launches"], 1)
     fl = flop_per_move(K)
     achieved = fl * moves_per_launch / (kern_ms / 1e3) / 1e12
-    # DRAM bytes (read + write) of one 1,000-move k_chain_fp64 launch of
-    # this workload after the L2 flush, from an ncu capture of this command
-    # (profiles/k_chain_fp64_8000water_full.md); other move counts: null
+    # DRAM bytes of one 1,000-move launch from an ncu capture of this
+    # command; other move counts: null
     traffic = (CHAIN_FP64_DRAM_BYTES_1000
                if not SMALL and round(moves_per_launch) == 1000 else None)
     roof = {"bound": "fp64", "achieved": achieved,

@@ -144,6 +144,7 @@ SIGNATURES = {
                                   C.c_int64]),
     "gb_mc_timing": (C.c_int, [_P, C.c_int32, _D, _L, _L, _D, _L]),
     "gb_mc_profile": (C.c_int, [_P, C.c_int32, _D, _L]),
+    "gb_mc_set_wait_limit": (C.c_int, [_P, C.c_int64]),
     "gb_box_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "gb_mc_layout": (C.c_int, [_P, _I, _I, _L]),
     "gb_mc_autotune": (C.c_int, [_P, C.c_int32, C.c_int32, _I, _D]),

@@ -448,6 +448,12 @@ int gb_mc_timing(gb_box *box, int32_t reset, double *chain_ms,
   return gb::mc_timing(*box->b, reset, chain_ms, chain_launches, chain_moves,
                        mp_ms, mp_moves);
 }
+int gb_mc_set_wait_limit(gb_box *box, int64_t polls) {
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  return gb::mc_set_wait_limit(*box->b, polls);
+}
 int gb_mc_profile(gb_box *box, int32_t enable, double *us13,
                   int64_t *moves2) {
   int rc = guard(box);

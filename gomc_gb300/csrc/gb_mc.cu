@@ -172,13 +172,13 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
   return v;
 }
 
-constexpr unsigned SPIN_LIMIT = 1u << 22;
+constexpr unsigned SPIN_LIMIT = 1u << 22;  // default polls of a device wait
 
 // Grid-wide barrier with a bounded wait.  bar[0] counts arrivals, bar[1] is
 // the generation.  Returns false (and sets DERR_BARRIER_TIMEOUT) when the
 // wait gives up or another CTA reported an error.
 __device__ bool grid_sync(unsigned *bar, unsigned nblocks, unsigned &gen,
-                          int *err, int *s_flag) {
+                          int *err, int *s_flag, unsigned limit) {
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
@@ -192,7 +192,7 @@ __device__ bool grid_sync(unsigned *bar, unsigned nblocks, unsigned &gen,
     } else {
       unsigned it = 0;
       while (ld_acquire(&bar[1]) == g) {
-        if (++it > SPIN_LIMIT) {
+        if (++it > limit) {
           atomicOr(err, DERR_BARRIER_TIMEOUT);
           ok = 0;
           break;
@@ -215,12 +215,12 @@ __device__ bool grid_sync(unsigned *bar, unsigned nblocks, unsigned &gen,
 // false when the wait gives up (DERR_BARRIER_TIMEOUT) or another CTA has
 // reported an error.
 __device__ bool wait_geq(const unsigned *p, unsigned target, int *err,
-                         bool backoff = false) {
+                         unsigned limit, bool backoff = false) {
   unsigned it = 0;
   while ((int)(ld_acquire(p) - target) < 0) {
     if (backoff)
       __nanosleep(64);
-    if (++it > SPIN_LIMIT) {
+    if (++it > limit) {
       atomicOr(err, DERR_BARRIER_TIMEOUT);
       return false;
     }
@@ -242,7 +242,7 @@ __global__ void k_fill_u64(unsigned long long *p, int n, unsigned long long v) {
 // loads its flags together, then the warp votes, so a round of checks costs
 // one memory round trip.  Bounded like grid_sync.
 __device__ bool warp_wait_all(const unsigned *flags, int n, unsigned target,
-                              int *err) {
+                              int *err, unsigned limit) {
   const int lane = threadIdx.x & 31;
   unsigned it = 0;
   for (;;) {
@@ -254,7 +254,7 @@ __device__ bool warp_wait_all(const unsigned *flags, int n, unsigned target,
       break;
     int bad = 0;
     if (lane == 0) {
-      if (++it > SPIN_LIMIT) {
+      if (++it > limit) {
         atomicOr(err, DERR_BARRIER_TIMEOUT);
         bad = 1;
       } else if ((it & 255u) == 0 && *(volatile int *)err) {
@@ -428,6 +428,7 @@ struct ChainArgs {
   // from the end of phase A, the leader's last partial, its last context
   // flag, and CTA 0's part of the next context written
   long long *prof;
+  unsigned spin;  // polls after which a device wait gives up
 };
 
 struct ChainShared {
@@ -910,10 +911,10 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     settings_adjust(S.set, A.first);
   __syncthreads();
   make_props(0);
-  if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
+  if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag, A.spin))
     return;
   build_ctx(A, S, 0, nullptr, 0, 0, CT);
-  if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
+  if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag, A.spin))
     return;
 
   const int pslot = cta == 0 ? 0 : cta == G - 1 ? 1 : -1;
@@ -1210,7 +1211,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
         // phase B beside the partials; warp 0 reads the outcome at barrier
         // 3 before it publishes
         int bok = spec ? warp_wait_all(A.seq + SEQ_CTX, nbuild,
-                                       (unsigned)(t + 1), b.err)
+                                       (unsigned)(t + 1), b.err, A.spin)
                        : 1;
         if (lane == 0) {
           S.bok = bok;
@@ -1268,7 +1269,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
           break;
         int bad = 0;
         if (lane == 0) {
-          if (++it > SPIN_LIMIT) {
+          if (++it > A.spin) {
             atomicOr(b.err, DERR_BARRIER_TIMEOUT);
             bad = 1;
           } else if ((it & 255u) == 0 && *(volatile int *)b.err) {
@@ -1401,7 +1402,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
       }
     } else {
       if (threadIdx.x == 0) {
-        int ok = wait_geq(A.seq, 2u * (unsigned)(t + 1), b.err, false);
+        int ok = wait_geq(A.seq, 2u * (unsigned)(t + 1), b.err, A.spin);
         S.accept = ok ? (int)(ld_acquire(A.seq) & 1u) : 0;
         S.ok = ok;
       }
@@ -1457,12 +1458,12 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
           settings_adjust(S.set, step);
         __syncthreads();
         make_props(t + 1);
-        if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
+        if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag, A.spin))
           return;
       }
       if (!spec) {
         build_ctx(A, S, t + 1, S.hdr, acc, 0, CT);
-        if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag))
+        if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag, A.spin))
           return;
       }
     }
@@ -1897,6 +1898,10 @@ int mc_init(Box &b, const gb_mc_params &p) {
     return rc;
   if ((rc = b.CudaCheck(cudaMemsetAsync(s.d_bar, 0, 32, b.stream), "memset")))
     return rc;
+  // a new loop starts without the error of an earlier one (a wait that gave
+  // up left the box's state as it was before that call)
+  if ((rc = b.CudaCheck(cudaMemsetAsync(b.dev.err, 0, 16, b.stream), "memset")))
+    return rc;
   if (b.cfg.precision == GB_MIXED) {
     // FP32 pair terms assume the 12-6 form
     for (int i = 0; i < b.ff.n_kinds * b.ff.n_kinds; ++i)
@@ -2068,6 +2073,15 @@ static void harvest(McState &s) {
   s.mp_ev.clear();
 }
 
+int mc_set_wait_limit(Box &b, int64_t polls) {
+  if (!b.mc)
+    return b.Fail(ERR_STATE, "gb_mc_init has not been called");
+  if (polls < 0 || polls > 0xffffffffLL)
+    return b.Fail(ERR_ARG, "the wait limit must be 0 (default) to 2^32 - 1");
+  b.mc->spin_limit = polls == 0 ? SPIN_LIMIT : (unsigned)polls;
+  return OK;
+}
+
 int mc_profile(Box &b, int enable, double *us13, int64_t *moves2) {
   if (!b.mc)
     return b.Fail(ERR_STATE, "gb_mc_init has not been called");
@@ -2145,14 +2159,20 @@ static int run_chain(Box &b, McState &s, const MoveRec *moves, int64_t first,
   A.tr_i = tr_i;
   A.tr_d = tr_d;
   A.prof = s.profile ? s.d_prof : nullptr;
+  A.spin = s.spin_limit;
   void *args[] = {&A};
   size_t sm = chain_smem(b, s.grid, A.nrows_max);
-  // the per-launch counters of the decision protocol start from zero
+  // the per-launch counters of the decision protocol and the grid barrier
+  // start from zero
   int rc = b.CudaCheck(cudaMemsetAsync(s.d_seq, 0,
                                        (SEQ_CTX + PART_MAX_GRID) *
                                            sizeof(unsigned),
                                        b.stream),
                        "memset");
+  if (!rc)
+    rc = b.CudaCheck(cudaMemsetAsync(s.d_bar, 0, 8 * sizeof(unsigned),
+                                     b.stream),
+                     "memset");
   if (rc)
     return rc;
   k_fill_u64<<<(2 * s.grid * 4 + 255) / 256, 256, 0, b.stream>>>(

@@ -123,12 +123,14 @@ struct McState {
   double chain_ms = 0.0, mp_ms = 0.0;
   int64_t chain_launches = 0, chain_moves = 0, mp_moves = 0;
   long long *d_prof = nullptr;  // FP64 chain phase clocks (gb_mc_profile)
+  unsigned spin_limit = 1u << 22;  // polls of a device wait (gb_mc_set_wait_limit)
   bool profile = false;
 };
 
 int mc_timing(Box &b, int reset, double *chain_ms, int64_t *chain_launches,
               int64_t *chain_moves, double *mp_ms, int64_t *mp_moves);
 int mc_profile(Box &b, int enable, double *us13, int64_t *moves2);
+int mc_set_wait_limit(Box &b, int64_t polls);
 
 // One chain of the mixed-precision chain kernel (gb_mixed.cu).
 struct MixedChain {

@@ -62,26 +62,101 @@ __global__ void k_reduce_partials(const double *__restrict__ part, int n, int w,
 // with the pairs inside the cutoff, not with the pairs scanned.
 constexpr int QW = 64;  // queue slots per warp
 
+// Bulk asynchronous copies (the TMA engine's untiled form) from global to
+// this CTA's shared memory, completed on an mbarrier: the copy engine moves
+// a cell's slots while no thread issues a load.  Addresses and sizes are
+// multiples of 16 bytes (cell slot arrays are padded to multiples of 32).
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src,
+                                         unsigned bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait on phase 0 of the barrier; false (and the box's error word
+// set) when it gives up, after a second bounded wait for the copies.
+__device__ bool mbar_wait_bounded(uint64_t *bar, int *err) {
+  constexpr unsigned LIMIT = 1u << 22;
+  for (unsigned it = 0; it < LIMIT; ++it)
+    if (mbar_try_wait(bar, 0))
+      return true;
+  atomicOr(err, DERR_BARRIER_TIMEOUT);
+  for (unsigned it = 0; it < LIMIT; ++it)
+    if (mbar_try_wait(bar, 0))
+      break;
+  return false;
+}
+
+// One CTA per (cell c, neighbour cell c2) tile.  Thread 0 starts bulk copies
+// of both cells' slots (positions and charges, meta words, atom ids) into
+// shared memory; then every warp scans 32 atoms of c against c2.
 __global__ void __launch_bounds__(RT) k_box_inter(DevBox b, const FF *__restrict__ pff,
                                                   double *part) {
-  extern __shared__ __align__(32) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   __shared__ int2 queue[RT / 32][QW];
+  __shared__ __align__(8) uint64_t bar;
   const FF &ff = *pff;
   int tile = blockIdx.x;
   int c = tile / NB27, n = tile % NB27;
   int c2 = b.nbr[c * NB27 + n];
   int n1 = b.cell_count[c], n2 = b.cell_count[c2];
-  double4_32a *sp = (double4_32a *)smem;
-  float4 *sf = (float4 *)(sp + b.cap);
-  int *sm = (int *)(sf + b.cap);
-  int *sa = sm + b.cap;
+  if (n1 == 0 || n2 == 0) {  // no pair in this tile
+    if (threadIdx.x == 0) {
+      part[2 * tile] = 0.0;
+      part[2 * tile + 1] = 0.0;
+    }
+    return;
+  }
+  const int cap = b.cap;
+  double4_32a *sp = (double4_32a *)smem;  // neighbour cell c2
+  float4 *sf = (float4 *)(sp + cap);
+  int *sm = (int *)(sf + cap);
+  int *sa = sm + cap;
+  double4_32a *cp = (double4_32a *)(sa + cap);  // cell c
+  int *cm = (int *)(cp + cap);
+  int *ca = cm + cap;
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar))
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    const unsigned p1 = (unsigned)n1 * 32, p2 = (unsigned)n2 * 32;
+    const unsigned w1 = (unsigned)((n1 + 3) & ~3) * 4;
+    const unsigned w2 = (unsigned)((n2 + 3) & ~3) * 4;
+    asm volatile(
+        "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+            smem_u32(&bar)),
+        "r"(p1 + p2 + 2 * (w1 + w2))
+        : "memory");
+    const size_t o1 = (size_t)c * cap, o2 = (size_t)c2 * cap;
+    bulk_g2s(sp, b.cell_pos + o2, p2, &bar);
+    bulk_g2s(sm, b.cell_meta + o2, w2, &bar);
+    bulk_g2s(sa, b.cell_atom + o2, w2, &bar);
+    bulk_g2s(cp, b.cell_pos + o1, p1, &bar);
+    bulk_g2s(cm, b.cell_meta + o1, w1, &bar);
+    bulk_g2s(ca, b.cell_atom + o1, w1, &bar);
+  }
+  __syncthreads();  // the barrier is initialised before anyone waits on it
+  const bool ok = mbar_wait_bounded(&bar, b.err);
+  if (!ok)
+    return;  // the error word reports it; no partial is read
   for (int j = threadIdx.x; j < n2; j += RT) {
-    size_t s = (size_t)c2 * b.cap + j;
-    double4_32a p = b.cell_pos[s];
-    sp[j] = p;
+    const double4_32a p = sp[j];
     sf[j] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.0f);
-    sm[j] = b.cell_meta[s];
-    sa[j] = b.cell_atom[s];
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -97,14 +172,14 @@ __global__ void __launch_bounds__(RT) k_box_inter(DevBox b, const FF *__restrict
   double lj = 0.0, re = 0.0;
   // FP64 energy of queued pair e (slot of cell c, slot of the neighbour cell)
   auto eval = [&](int2 e) {
-    double4_32a pi = b.cell_pos[(size_t)c * b.cap + e.x];
+    double4_32a pi = cp[e.x];
     double4_32a pj = sp[e.y];
     double dx = min_image(pi.x - pj.x, b.L[0], b.half[0]);
     double dy = min_image(pi.y - pj.y, b.L[1], b.half[1]);
     double dz = min_image(pi.z - pj.z, b.L[2], b.half[2]);
     double distSq = dsq3(dx, dy, dz);
     if (ff.rcutSq > distSq) {
-      int ki = meta_kind(b.cell_meta[(size_t)c * b.cap + e.x]);
+      int ki = meta_kind(cm[e.x]);
       int kj = meta_kind(sm[e.y]);
       if (ff.electrostatic) {
         double qq = pi.w * pj.w * QQ_FACT;
@@ -121,13 +196,12 @@ __global__ void __launch_bounds__(RT) k_box_inter(DevBox b, const FF *__restrict
     int ai = -1, moli = -1;
     float px = 0.0f, py = 0.0f, pz = 0.0f;
     if (act) {
-      size_t si = (size_t)c * b.cap + i;
-      double4_32a p = b.cell_pos[si];
+      double4_32a p = cp[i];
       px = (float)p.x;
       py = (float)p.y;
       pz = (float)p.z;
-      ai = b.cell_atom[si];
-      moli = meta_mol(b.cell_meta[si]);
+      ai = ca[i];
+      moli = meta_mol(cm[i]);
     }
     for (int j = 0; j < n2; ++j) {
       bool in = false;
@@ -259,8 +333,10 @@ int launch_box_inter_view(Box &bx, const DevBox &b, double *d_out2) {
   int rc = bx.EnsureScratch((size_t)tiles * 2);
   if (rc)
     return rc;
-  size_t sh = (size_t)b.cap * (sizeof(double4_32a) + sizeof(float4) +
-                                2 * sizeof(int));
+  // neighbour cell: positions, FP32 copies, meta, atom ids; cell c:
+  // positions, meta, atom ids
+  size_t sh = (size_t)b.cap * (2 * sizeof(double4_32a) + sizeof(float4) +
+                                4 * sizeof(int));
   raise_smem_limit((const void *)k_box_inter, sh);
   k_box_inter<<<tiles, RT, sh, bx.stream>>>(b, bx.d_ff, bx.d_scratch);
   k_reduce_partials<<<1, RT, 0, bx.stream>>>(bx.d_scratch, tiles, 2, d_out2, 0);

@@ -447,6 +447,11 @@ class Box:
         return dict(chain_ms=cm.value, chain_launches=cl.value,
                     chain_moves=cn.value, mp_ms=mm.value, mp_moves=mn.value)
 
+    def mc_set_wait_limit(self, polls: int = 0) -> None:
+        """Polls after which the FP64 chain's device waits give up
+        (gb_mc_set_wait_limit; 0: the default)."""
+        self._chk(lib().gb_mc_set_wait_limit(self.h, int(polls)))
+
     def mc_profile(self, enable: bool = True) -> dict:
         """FP64 chain phase clocks since the last call (gb_mc_profile): per
         move phase, microseconds of CTA 0 and of the deciding CTA."""

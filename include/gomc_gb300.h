@@ -268,6 +268,15 @@ int gb_mc_state(gb_box *box, double *scales4, int64_t *counts6);
 int gb_mc_timing(gb_box *box, int32_t reset, double *chain_ms,
                  int64_t *chain_launches, int64_t *chain_moves, double *mp_ms,
                  int64_t *mp_moves);
+/* Polls after which a wait inside the FP64 chain kernel (the grid barrier,
+ * the partials, the next move's context, the decision word) gives up, 0 for
+ * the default 2^22 (seconds of waiting).  A wait that gives up sets the
+ * box's device error word: the CTAs leave the kernel without committing the
+ * move, gb_mc_run returns GB_ERR_TIMEOUT, and the coordinates, energies and
+ * structure factors stay as they were before the call; gb_mc_init clears
+ * the error before the loop runs again.  No reference counterpart (the
+ * reference has no device-side waits). */
+int gb_mc_set_wait_limit(gb_box *box, int64_t polls);
 /* Where the device time of the FP64 chain goes (no reference counterpart):
  * the clocks of CTA 0 and of the deciding CTA (the last) since the last
  * call, per phase of a move (loading the move's context, listing the
