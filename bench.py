@@ -711,16 +711,40 @@ def run_serving(args, dev):
     srv = serving.Server(device=dev, quantum=args.serve_quantum)
     srv.start()
     t0 = time.perf_counter()
+    jids = []
     for i, (s, n) in enumerate(zip(systems, sizes)):
         target = t0 + float(np.sum(gaps[:i + 1]))
         delay = target - time.perf_counter()
         if delay > 0:
             time.sleep(delay)
-        srv.submit(s, cfg, seed=SEED + i, nsteps=int(n) * sweeps,
-                   scales=SCALES, adj_steps=ADJ, recompute_freq=10000)
-    srv.drain(timeout_s=600)
+        jids.append(srv.submit(s, cfg, seed=SEED + i, nsteps=int(n) * sweeps,
+                               scales=SCALES, adj_steps=ADJ,
+                               recompute_freq=10000))
+    srv.drain(timeout_s=args.serve_timeout)
     st = srv.stats()
+    # per size class (quartiles of N): queueing (submission to admission)
+    # and the time per sweep once admitted, which grows with N (a sweep is
+    # N sequential moves of one chain)
+    jobs = [srv.job(j) for j in jids]
     srv.close()
+    edges = np.quantile(sizes, [0.0, 0.25, 0.5, 0.75, 1.0])
+    by_size = []
+    for q in range(4):
+        sel = [k for k in range(J) if (sizes[k] >= edges[q]) and
+               (sizes[k] < edges[q + 1] or q == 3)]
+        if not sel:
+            continue
+        wait = np.array([jobs[k]["t_admit"] - jobs[k]["t_submit"]
+                         for k in sel])
+        run = np.array([(jobs[k]["t_done"] - jobs[k]["t_admit"]) / sweeps
+                        for k in sel])
+        by_size.append({"waters": [int(sizes[sel].min()), int(sizes[sel].max())],
+                        "jobs": len(sel),
+                        "queue_s": {"p50": float(np.percentile(wait, 50)),
+                                    "p99": float(np.percentile(wait, 99))},
+                        "s_per_sweep_admitted": {
+                            "p50": float(np.percentile(run, 50)),
+                            "p99": float(np.percentile(run, 99))}})
     return {
         "workload": "%d water jobs, N log-uniform in [500, 20000] (sum %d "
                     "molecules), %d sweeps each, Poisson arrivals at %.1f "
@@ -739,7 +763,7 @@ def run_serving(args, dev):
                                          "stops_smem", "stops_ctas",
                                          "launch_balance", "round_gap_s")},
         "helper_busy_s": st["helper_busy_s"], "round_busy_s": st["round_busy_s"],
-        "jobs_done": st["jobs_done"]}
+        "jobs_done": st["jobs_done"], "by_size_quartile": by_size}
 
 
 def run_gb300(args, rank, world):
@@ -935,6 +959,8 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=64.0,
                     help="job arrivals per second (Poisson)")
     ap.add_argument("--serve-quantum", type=int, default=1000)
+    ap.add_argument("--serve-timeout", type=float, default=600.0,
+                    help="seconds the serving stream may take to drain")
     ap.add_argument("--mixed-equil-moves", type=int, default=20000,
                     help="untimed moves of every batched replica before "
                          "the measured steps")

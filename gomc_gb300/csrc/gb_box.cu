@@ -116,7 +116,9 @@ void build_ff(const HostSystem &s, const BoxConfig &c, FF *ff) {
 }
 
 // ---------------------------------------------------------------------------
-// Table of erfc(alpha r) / r over r^2 in [0.5, 2^e1) A^2, 2^e1 > s_max: per
+// Table of erfc(alpha r) / r (with `force`: the force factor
+// (erfc(alpha r) / r + 2 alpha / sqrt(pi) exp(-alpha^2 r^2)) / r^2) over r^2
+// in [0.5, 2^e1) A^2, 2^e1 > s_max: per
 // segment (64 per binade) the degree-8 Chebyshev interpolant at 9 first-kind
 // Chebyshev nodes, computed in long double and stored as monomial
 // coefficients in u = 2 (s - a) / h - 1.  Interpolation error below 1.1e-16
@@ -124,7 +126,7 @@ void build_ff(const HostSystem &s, const BoxConfig &c, FF *ff) {
 // the widest segments, where exp(-alpha^2 r^2) bends most per segment).
 // ---------------------------------------------------------------------------
 static void erfc_table(double alpha, double s_max, std::vector<double> &tab,
-                       int *key0, int *nseg) {
+                       int *key0, int *nseg, bool force = false) {
   constexpr int D = ETAB_DEG, NC = ETAB_DEG + 1;
   const int E0 = -1;
   int e1 = E0;
@@ -157,6 +159,8 @@ static void erfc_table(double alpha, double s_max, std::vector<double> &tab,
       long double sv = a + h * (node[i] + 1.0L) * 0.5L;
       long double r = sqrtl(sv);
       f[i] = erfcl(al * r) / r;
+      if (force)  // the force factor (src/FFParticle.cpp:401-446)
+        f[i] = (f[i] + al * 2.0L / sqrtl(pi) * expl(-al * al * sv)) / sv;
     }
     for (int k = 0; k < NC; ++k) {
       long double acc = 0.0L;
@@ -663,15 +667,21 @@ int Box::Init(const HostSystem &s0, const BoxConfig &c) {
       (rc = up(d.mstart, s.mstart.data(), (M + 1) * 4)))
     return rc;
   ff.erfc_tab = nullptr;
+  ff.vir_tab = nullptr;
   ff.etab_key0 = ff.etab_nseg = 0;
   if (c.ewald) {
-    std::vector<double> et;
-    double *d_et = nullptr;
+    std::vector<double> et, vt;
+    double *d_et = nullptr, *d_vt = nullptr;
     erfc_table(ff.alpha, ff.rcutCoulSq, et, &ff.etab_key0, &ff.etab_nseg);
+    erfc_table(ff.alpha, ff.rcutCoulSq, vt, &ff.etab_key0, &ff.etab_nseg,
+               true);
     if ((rc = Alloc(&d_et, et.size())) ||
-        (rc = up(d_et, et.data(), et.size() * sizeof(double))))
+        (rc = up(d_et, et.data(), et.size() * sizeof(double))) ||
+        (rc = Alloc(&d_vt, vt.size())) ||
+        (rc = up(d_vt, vt.data(), vt.size() * sizeof(double))))
       return rc;
     ff.erfc_tab = d_et;
+    ff.vir_tab = d_vt;
   }
   if ((rc = up(d_ff, &ff, sizeof(FF))))
     return rc;
@@ -1538,10 +1548,11 @@ int Box::SetBox(const double L[3], const double *xyz, const double *com) {
     return rc;
   // force-field constants that depend on the edges (the mixed form's FP32
   // turn length); the erfc table does not
-  const double *etab = ff.erfc_tab;
+  const double *etab = ff.erfc_tab, *vtab = ff.vir_tab;
   int key0 = ff.etab_key0, nseg = ff.etab_nseg;
   build_ff(s, cfg, &ff);
   ff.erfc_tab = etab;
+  ff.vir_tab = vtab;
   ff.etab_key0 = key0;
   ff.etab_nseg = nseg;
   if ((rc = CudaCheck(cudaMemcpyAsync(d_ff, &ff, sizeof(FF),

@@ -26,9 +26,11 @@
 // the positions go back to global memory at the end of the launch.
 //
 // Pair sums cover each box's particles in lookup order (all pairs inside the
-// cutoff; the reference's cell lists enumerate the same pairs), FP64 pairs
-// behind an FP32 distance pre-filter in the plain form, FP32 pair energies on
-// exact fixed-point separations with FP64 accumulation in the mixed form.
+// cutoff; the reference's cell lists enumerate the same pairs).  Plain form:
+// an FP32 distance pre-filter queues each warp's candidate pairs in order and
+// full warps evaluate the queue in FP64.  Mixed form: FP32 pair energies on
+// exact fixed-point separations, float-float sums per thread and warp, FP64
+// across warps and CTAs.
 #include "gb_gemc.h"
 #include "gb_pair.cuh"
 
@@ -86,6 +88,7 @@ struct GemcShared {
   double wred[NW][2];         // per-warp sums (displacement, volume)
   int2 wq[NW][WQ];            // per-warp FP64 candidate queues
   int accept;
+  int slot;                   // a transferred molecule's slot in the lookup
 };
 
 __device__ __forceinline__ double wrapd(double v, double ax) {
@@ -1083,6 +1086,16 @@ __global__ void __launch_bounds__(GEMC_THREADS)
     mark(pslot, 3);
     // ---------------- commit ----------------
     const int acc = S.accept;
+    if (acc && kind == GEMC_TRANSFER) {
+      // MoleculeLookup::Shift needs the molecule's slot in its box's
+      // section of the lookup: the threads scan it together (the molecule
+      // appears once)
+      const int a0 = first_of(c, b), nb = count_of(c, n, b);
+      for (int i = tid; i < nb; i += GEMC_THREADS)
+        if (A.lookup[a0 + i] == m)
+          S.slot = a0 + i;
+      __syncthreads();
+    }
     if (acc && (kind == GEMC_DISPLACE || kind == GEMC_TRANSFER)) {
       if (tid == 0) {
         A.px[m] = M.np[0];
@@ -1110,12 +1123,7 @@ __global__ void __launch_bounds__(GEMC_THREADS)
             p.cy[m] = wrapd(M.np[1] * (1.0 / 1.0), c.ax[b1][1]);
             p.cz[m] = wrapd(M.np[2] * (1.0 / 1.0), c.ax[b1][2]);
           }
-          int a0 = first_of(c, b), nb = count_of(c, n, b), idx = a0;
-          for (int i = 0; i < nb; ++i)
-            if (A.lookup[a0 + i] == m) {
-              idx = a0 + i;
-              break;
-            }
+          const int idx = S.slot;
           int ni = b == 0 ? --c.start1 : c.start1++;
           int tmp = A.lookup[idx];
           A.lookup[idx] = A.lookup[ni];

@@ -62,6 +62,9 @@ struct FF {
   // only): 64 segments per binade of r^2 from 0.5 A^2, 9 coefficients each;
   // segment of r^2 = (its IEEE exponent and top 6 mantissa bits) - key0
   const double *erfc_tab;
+  // (erfc(alpha r) / r + 2 alpha / sqrt(pi) exp(-alpha^2 r^2)) / r^2, the
+  // Coulomb force factor of FFParticle::CalcCoulombVir, on the same segments
+  const double *vir_tab;
   int etab_key0, etab_nseg;
   // soft-core settings at lambda < 1 (Forcefield::sc_*,
   // src/Forcefield.cpp:59-75)

@@ -39,20 +39,28 @@ __device__ __forceinline__ double lj_virial(const FF &ff, double distSq,
 // Outside it (r^2 < 0.5 A^2 or no table): the direct formula.  About a dozen
 // FP64 operations against ~100 for sqrt, erfc and the division, which
 // matters on GB300's two FP64 lanes per SM and clock.
-__device__ __forceinline__ double erfc_over_r(const FF &ff, double s) {
+// The segment polynomial of table `tab` at r^2 = s; false outside the range.
+__device__ __forceinline__ bool seg_poly(const FF &ff, const double *tab,
+                                         double s, double *out) {
   long long bits = __double_as_longlong(s);
   int seg = (int)(bits >> 46) - ff.etab_key0;
-  if (ff.erfc_tab != nullptr && (unsigned)seg < (unsigned)ff.etab_nseg) {
-    double a = __longlong_as_double(bits & ~((1LL << 46) - 1));
-    double scale = __longlong_as_double((2053LL - (bits >> 52)) << 52);
-    double u = fma(s - a, scale, -1.0);
-    const double *c = ff.erfc_tab + (size_t)seg * (ETAB_DEG + 1);
-    double p = __ldg(c + ETAB_DEG);
+  if (tab == nullptr || (unsigned)seg >= (unsigned)ff.etab_nseg)
+    return false;
+  double a = __longlong_as_double(bits & ~((1LL << 46) - 1));
+  double scale = __longlong_as_double((2053LL - (bits >> 52)) << 52);
+  double u = fma(s - a, scale, -1.0);
+  const double *c = tab + (size_t)seg * (ETAB_DEG + 1);
+  double p = __ldg(c + ETAB_DEG);
 #pragma unroll
-    for (int m = ETAB_DEG - 1; m >= 0; --m)
-      p = fma(p, u, __ldg(c + m));
+  for (int m = ETAB_DEG - 1; m >= 0; --m)
+    p = fma(p, u, __ldg(c + m));
+  *out = p;
+  return true;
+}
+__device__ __forceinline__ double erfc_over_r(const FF &ff, double s) {
+  double p;
+  if (seg_poly(ff, ff.erfc_tab, s, &p))
     return p;
-  }
   double r = sqrt(s);
   return erfc(ff.alpha * r) / r;
 }
@@ -72,6 +80,13 @@ __device__ __forceinline__ double coulomb_virial(const FF &ff, double distSq,
                                                  double qq) {
   if (ff.rcutCoulSq < distSq)
     return 0.0;
+  if (ff.ewald) {
+    // the force factor from its table (same segments and accuracy as
+    // erfc_over_r), else the direct formula
+    double p;
+    if (seg_poly(ff, ff.vir_tab, distSq, &p))
+      return qq * p;
+  }
   double dist = sqrt(distSq);
   if (ff.ewald) {
     double constValue = ff.alpha * M_2_SQRTPI;

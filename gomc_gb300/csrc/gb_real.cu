@@ -609,6 +609,15 @@ int launch_correction(Box &bx, double *d_out) {
 // Energies count each pair once (i < j); forces gather every pair.
 // ---------------------------------------------------------------------------
 constexpr int FG = 3;  // neighbour-shell groups
+// Each thread owns one atom of cell c per pass and gathers the force on it
+// from the CTA's third of the neighbour shell.  Per neighbour cell (staged in
+// shared memory with FP32 copies of the positions) a thread first marks the
+// neighbours that pass an FP32 distance pre-filter in a bit mask, then the
+// warp walks the masks together: in each round every thread evaluates its
+// next marked pair in FP64 (exact cutoff test, forces, and the energy of
+// pairs with i < j).  The FP64 work then follows the pairs inside the
+// cutoff, and each atom's sum runs over its pairs in neighbour order.
+constexpr int FMW = 8;  // 64-bit mask words per neighbour-cell chunk (512)
 __global__ void __launch_bounds__(RT) k_box_force(DevBox b, const FF *__restrict__ pff,
                                                   double *fpart, double *epart) {
   extern __shared__ __align__(32) unsigned char smem[];
@@ -616,10 +625,17 @@ __global__ void __launch_bounds__(RT) k_box_force(DevBox b, const FF *__restrict
   int c = blockIdx.x, g = blockIdx.y;
   int n1 = b.cell_count[c];
   double4_32a *sp = (double4_32a *)smem;
-  int *sm = (int *)(sp + b.cap);
+  float4 *sf = (float4 *)(sp + b.cap);
+  int *sm = (int *)(sf + b.cap);
   int *sa = sm + b.cap;
+  const float Lf[3] = {(float)b.L[0], (float)b.L[1], (float)b.L[2]};
+  const float Hf[3] = {(float)b.half[0], (float)b.half[1], (float)b.half[2]};
+  // FP32 positions are within L 2^-24 of the FP64 ones; the pre-filter
+  // radius covers twice that per axis plus 1e-4 of Rcut^2
+  const double lmax = fmax(b.L[0], fmax(b.L[1], b.L[2]));
+  const double rpad = ff.rcut + 1e-6 * lmax;
+  const float cut_f = (float)(rpad * rpad * 1.0001);
   double lj = 0.0, re = 0.0;
-  // each thread owns up to ceil(n1 / RT) atoms; loop per owned atom
   for (int base = 0; base < n1; base += RT) {
     int i = base + threadIdx.x;
     bool own = i < n1;
@@ -631,49 +647,84 @@ __global__ void __launch_bounds__(RT) k_box_force(DevBox b, const FF *__restrict
       mi = b.cell_meta[si];
       ai = b.cell_atom[si];
     }
+    const float pxf = (float)pi.x, pyf = (float)pi.y, pzf = (float)pi.z;
+    const int moli = meta_mol(mi), ki = meta_kind(mi);
     double fx = 0, fy = 0, fz = 0;
     for (int nn = g * (NB27 / FG); nn < (g + 1) * (NB27 / FG); ++nn) {
       int c2 = b.nbr[c * NB27 + nn];
       int n2 = b.cell_count[c2];
       __syncthreads();
       for (int j = threadIdx.x; j < n2; j += RT) {
-        size_t s = (size_t)c2 * b.cap + j;
-        sp[j] = b.cell_pos[s];
-        sm[j] = b.cell_meta[s];
-        sa[j] = b.cell_atom[s];
+        size_t s2 = (size_t)c2 * b.cap + j;
+        const double4_32a p = b.cell_pos[s2];
+        sp[j] = p;
+        sf[j] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.0f);
+        sm[j] = b.cell_meta[s2];
+        sa[j] = b.cell_atom[s2];
       }
       __syncthreads();
-      if (!own)
-        continue;
-      int moli = meta_mol(mi), ki = meta_kind(mi);
-      for (int j = 0; j < n2; ++j) {
-        int mj = sm[j];
-        if (moli == meta_mol(mj))
-          continue;
-        double4_32a pj = sp[j];
-        double dx = min_image(pi.x - pj.x, b.L[0], b.half[0]);
-        double dy = min_image(pi.y - pj.y, b.L[1], b.half[1]);
-        double dz = min_image(pi.z - pj.z, b.L[2], b.half[2]);
-        double distSq = dsq3(dx, dy, dz);
-        if (ff.rcutSq > distSq) {
-          int idx = ki + meta_kind(mj) * ff.n_kinds;
-          double fR = 0.0;
-          bool hasR = false;
-          if (ff.electrostatic) {
-            double qq = pi.w * pj.w * QQ_FACT;
-            if (qq != 0.0) {
-              if (ai < sa[j])
-                re += coulomb_energy(ff, distSq, qq);
-              fR = coulomb_virial(ff, distSq, qq);
-              hasR = true;
+      for (int jb = 0; jb < n2; jb += 64 * FMW) {
+        // candidates of this thread's atom among neighbours jb .. jb + 511
+        unsigned long long mk[FMW];
+#pragma unroll
+        for (int w = 0; w < FMW; ++w) {
+          unsigned long long m = 0;
+          const int j0 = jb + 64 * w;
+          if (own)
+            for (int k = 0; k < 64 && j0 + k < n2; ++k) {
+              const int j = j0 + k;
+              const float4 q = sf[j];
+              float dx = pxf - q.x, dy = pyf - q.y, dz = pzf - q.z;
+              dx = dx > Hf[0] ? dx - Lf[0] : dx < -Hf[0] ? dx + Lf[0] : dx;
+              dy = dy > Hf[1] ? dy - Lf[1] : dy < -Hf[1] ? dy + Lf[1] : dy;
+              dz = dz > Hf[2] ? dz - Lf[2] : dz < -Hf[2] ? dz + Lf[2] : dz;
+              if (fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < cut_f &&
+                  moli != meta_mol(sm[j]))
+                m |= 1ull << k;
             }
+          mk[w] = m;
+        }
+        // rounds: every thread takes its next marked neighbour
+        for (;;) {
+          int j = -1;
+#pragma unroll
+          for (int w = 0; w < FMW; ++w)
+            if (j < 0 && mk[w]) {
+              const int k = __ffsll((long long)mk[w]) - 1;
+              mk[w] &= mk[w] - 1;
+              j = jb + 64 * w + k;
+            }
+          if (!__any_sync(0xffffffffu, j >= 0))
+            break;
+          if (j < 0)
+            continue;
+          const int mj = sm[j];
+          const double4_32a pj = sp[j];
+          double dx = min_image(pi.x - pj.x, b.L[0], b.half[0]);
+          double dy = min_image(pi.y - pj.y, b.L[1], b.half[1]);
+          double dz = min_image(pi.z - pj.z, b.L[2], b.half[2]);
+          double distSq = dsq3(dx, dy, dz);
+          if (ff.rcutSq > distSq) {
+            int idx = ki + meta_kind(mj) * ff.n_kinds;
+            double fR = 0.0;
+            bool hasR = false;
+            const bool first = ai < sa[j];
+            if (ff.electrostatic) {
+              double qq = pi.w * pj.w * QQ_FACT;
+              if (qq != 0.0) {
+                if (first)
+                  re += coulomb_energy(ff, distSq, qq);
+                fR = coulomb_virial(ff, distSq, qq);
+                hasR = true;
+              }
+            }
+            if (first)
+              lj += lj_energy(ff, distSq, idx);
+            double fL = lj_virial(ff, distSq, idx);
+            fx += dx * fL + (hasR ? dx * fR : 0.0);
+            fy += dy * fL + (hasR ? dy * fR : 0.0);
+            fz += dz * fL + (hasR ? dz * fR : 0.0);
           }
-          if (ai < sa[j])
-            lj += lj_energy(ff, distSq, idx);
-          double fL = lj_virial(ff, distSq, idx);
-          fx += dx * fL + (hasR ? dx * fR : 0.0);
-          fy += dy * fL + (hasR ? dy * fR : 0.0);
-          fz += dz * fL + (hasR ? dz * fR : 0.0);
         }
       }
     }
@@ -724,7 +775,8 @@ int launch_box_force(Box &bx, const DevBox &b, double *aF, double *mF,
     return rc;
   double *fpart = bx.d_scratch;
   double *epart = fpart + (size_t)FG * b.n_atoms * 3;
-  size_t sh = (size_t)b.cap * (sizeof(double4_32a) + 2 * sizeof(int));
+  size_t sh = (size_t)b.cap * (sizeof(double4_32a) + sizeof(float4) +
+                                2 * sizeof(int));
   raise_smem_limit((const void *)k_box_force, sh);
   k_box_force<<<dim3(b.ncell, FG), RT, sh, bx.stream>>>(b, bx.d_ff, fpart, epart);
   k_force_gather<<<(b.n_mol + 127) / 128, 128, 0, bx.stream>>>(b, fpart, aF,

@@ -445,9 +445,10 @@ __global__ void __launch_bounds__(FA) k_force_recip(DevBox b, const FF *__restri
   int pad = 3 * stride + 1;  // per-atom table stride (odd) against conflicts
   double2 *ktab = tab + (size_t)FA * pad;
   double *kxs = (double *)ktab;
-  double *kys = kxs + FK, *kzs = kys + FK, *pfs = kzs + FK, *srs = pfs + FK,
-         *sis = srs + FK;
-  char4 *kns = (char4 *)(sis + FK);
+  // per k-vector: the components of k and the prefactor times the
+  // structure factor, prefact * (sumR, sumI)
+  double *kys = kxs + FK, *kzs = kys + FK, *pas = kzs + FK, *pbs = pas + FK;
+  char4 *kns = (char4 *)(pbs + FK);
   int a = blockIdx.x * FA + threadIdx.x;
   bool own = a < b.n_atoms;
   double cv[3];
@@ -496,29 +497,40 @@ __global__ void __launch_bounds__(FA) k_force_recip(DevBox b, const FF *__restri
       kxs[i] = b.kx[k];
       kys[i] = b.ky[k];
       kzs[i] = b.kz[k];
-      pfs[i] = b.prefact[k];
-      srs[i] = sR[k];
-      sis[i] = sI[k];
+      const double pf = b.prefact[k];
+      pas[i] = pf * sR[k];
+      pbs[i] = pf * sI[k];
       kns[i] = b.kn[k];
     }
     __syncthreads();
     if (!charged)
       continue;
+    // Ewald::BoxForceReciprocal: factor_k = 2 q prefact_k (sin(k.r) sumR -
+    // cos(k.r) sumI), F += factor_k k.  The common 2 q is applied once per
+    // atom; the k-vectors run x outer, y, z inner, so the x-y phase product
+    // is formed once per (n_x, n_y) column.
+    int px = -1000, py = -1000;
+    double2 exy = make_double2(0.0, 0.0);
     for (int i = 0; i < nk; ++i) {
-      char4 n = kns[i];
-      double2 e = cmul(cmul(my[n.x], pick(my + stride, n.y)),
-                       pick(my + 2 * stride, n.z));
-      double factor = 2.0 * q * pfs[i] * 1.0 * (e.y * srs[i] - e.x * sis[i]);
-      fx += factor * kxs[i];
-      fy += factor * kys[i];
-      fz += factor * kzs[i];
+      const char4 n = kns[i];
+      if (n.x != px || n.y != py) {
+        exy = cmul(my[n.x], pick(my + stride, n.y));
+        px = n.x;
+        py = n.y;
+      }
+      const double2 e = cmul(exy, pick(my + 2 * stride, n.z));
+      const double t = e.y * pas[i] - e.x * pbs[i];
+      fx += t * kxs[i];
+      fy += t * kys[i];
+      fz += t * kzs[i];
     }
   }
   if (own) {
+    const double q2 = 2.0 * q;
     double *f = fpart + ((size_t)blockIdx.y * b.n_atoms + a) * 3;
-    f[0] = fx + (blockIdx.y == 0 ? FX : 0.0);
-    f[1] = fy + (blockIdx.y == 0 ? FY : 0.0);
-    f[2] = fz + (blockIdx.y == 0 ? FZ : 0.0);
+    f[0] = q2 * fx + (blockIdx.y == 0 ? FX : 0.0);
+    f[1] = q2 * fy + (blockIdx.y == 0 ? FY : 0.0);
+    f[2] = q2 * fz + (blockIdx.y == 0 ? FZ : 0.0);
   }
 }
 

@@ -198,7 +198,8 @@ size_t job_bytes(const Job &j, int K, int kmax, int csize, size_t moves) {
   size_t slot = 4 + 32 + 4 + 16 + 4;  // atom, pos, meta, fix, qlo
   size_t box = N * (3 * 8 + 8 + 4 * 4 + 6 * 8) + M * (3 * 8 + 4 + 9 * 8) +
                ncell * (4 + NB27 * 4) + NC * slot + (size_t)K * (9 * 8 + 8) +
-               4096 * 8 + sizeof(FF) + 256;
+               2 * 12 * 64 * (ETAB_DEG + 1) * 8 +  // erfc and force tables
+               sizeof(FF) + 256;
   size_t mc = moves * (sizeof(MoveRec) + 12 * 8) +
               N * (3 * 8 + 6 * 8 + 8) + M * (3 * 8 + 12 * 8 + 4) +
               NC * slot + ncell * 4 + 256 * sizeof(MixedChain) +
