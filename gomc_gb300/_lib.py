@@ -83,6 +83,33 @@ class GemcConfig(C.Structure):
                 ("cluster_size", C.c_int32), ("seed", C.c_uint32)]
 
 
+B2, M16, MP2 = 2, 16, 2
+
+
+class GomcChk(C.Structure):
+    """gb_gomc_chk (include/gomc_gb300.h): the Monte Carlo loop state of a
+    GOMC checkpoint file (src/Checkpoint.h)."""
+    _fields_ = [("step", C.c_uint64), ("true_step", C.c_uint64),
+                ("mt_state", C.c_uint32 * 624), ("mt_left", C.c_uint32),
+                ("seed_location", C.c_uint32), ("seed_left", C.c_uint32),
+                ("seed_value", C.c_uint32),
+                ("n_box", C.c_int32), ("n_move", C.c_int32),
+                ("n_kind", C.c_int32),
+                ("scale", (C.c_double * M16) * B2),
+                ("accept_percent", (C.c_double * M16) * B2),
+                ("accepted", (C.c_uint32 * M16) * B2),
+                ("tries", (C.c_uint32 * M16) * B2),
+                ("temp_accepted", (C.c_uint32 * M16) * B2),
+                ("temp_tries", (C.c_uint32 * M16) * B2),
+                ("mp_tries", (C.c_uint32 * MP2) * B2),
+                ("mp_accepted", (C.c_uint32 * MP2) * B2),
+                ("mp_interval_accepted", (C.c_uint32 * MP2) * B2),
+                ("mp_interval_tries", (C.c_uint32 * MP2) * B2),
+                ("mp_t_max", C.c_double * B2), ("mp_r_max", C.c_double * B2),
+                ("single_move_accepted", C.c_int32 * B2),
+                ("records_offset", C.c_int64)]
+
+
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int32)
@@ -145,6 +172,13 @@ SIGNATURES = {
     "gb_mc_timing": (C.c_int, [_P, C.c_int32, _D, _L, _L, _D, _L]),
     "gb_mc_profile": (C.c_int, [_P, C.c_int32, _D, _L]),
     "gb_mc_set_wait_limit": (C.c_int, [_P, C.c_int64]),
+    "gb_gomc_checkpoint_read": (C.c_int, [C.c_void_p, C.c_int64,
+                                          C.POINTER(GomcChk)]),
+    "gb_gomc_checkpoint_write": (C.c_int, [C.c_void_p, C.c_int64,
+                                           C.POINTER(GomcChk), C.c_void_p,
+                                           C.c_int64, _L]),
+    "gb_mc_get_gomc_state": (C.c_int, [_P, C.POINTER(GomcChk)]),
+    "gb_mc_set_gomc_state": (C.c_int, [_P, C.POINTER(GomcChk)]),
     "gb_box_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "gb_mc_layout": (C.c_int, [_P, _I, _I, _L]),
     "gb_mc_autotune": (C.c_int, [_P, C.c_int32, C.c_int32, _I, _D]),

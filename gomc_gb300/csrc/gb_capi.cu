@@ -448,6 +448,27 @@ int gb_mc_timing(gb_box *box, int32_t reset, double *chain_ms,
   return gb::mc_timing(*box->b, reset, chain_ms, chain_launches, chain_moves,
                        mp_ms, mp_moves);
 }
+int gb_gomc_checkpoint_read(const void *buf, int64_t bytes,
+                            gb_gomc_chk *out) {
+  return gb::gomc_chk_read(buf, bytes, out);
+}
+int gb_gomc_checkpoint_write(const void *tmpl, int64_t tmpl_bytes,
+                             const gb_gomc_chk *in, void *out,
+                             int64_t out_cap, int64_t *out_bytes) {
+  return gb::gomc_chk_write(tmpl, tmpl_bytes, in, out, out_cap, out_bytes);
+}
+int gb_mc_get_gomc_state(gb_box *box, gb_gomc_chk *out) {
+  int rc = guard(box);
+  if (rc || !out)
+    return rc ? rc : gb::ERR_ARG;
+  return gb::mc_get_gomc_state(*box->b, out);
+}
+int gb_mc_set_gomc_state(gb_box *box, const gb_gomc_chk *in) {
+  int rc = guard(box);
+  if (rc || !in)
+    return rc ? rc : gb::ERR_ARG;
+  return gb::mc_set_gomc_state(*box->b, in);
+}
 int gb_mc_set_wait_limit(gb_box *box, int64_t polls) {
   int rc = guard(box);
   if (rc)

@@ -189,6 +189,13 @@ void mc_destroy(Box &b);
 int mc_autotune(Box &b, int objective, int trial_moves, int *chosen,
                 double *us_per_move4);
 
+// The reference's checkpoint file (gb_gomc_chk.cu)
+int gomc_chk_read(const void *buf, int64_t bytes, gb_gomc_chk *out);
+int gomc_chk_write(const void *tmpl, int64_t tbytes, const gb_gomc_chk *in,
+                   void *out, int64_t cap, int64_t *out_bytes);
+int mc_get_gomc_state(Box &b, gb_gomc_chk *c);
+int mc_set_gomc_state(Box &b, const gb_gomc_chk *c);
+
 // Checkpoints of a box's dynamic state (gb_ckpt.cu)
 int checkpoint_size(Box &b, int64_t *bytes);
 int checkpoint_save(Box &b, void *buf, int64_t bytes);

@@ -447,6 +447,18 @@ class Box:
         return dict(chain_ms=cm.value, chain_launches=cl.value,
                     chain_moves=cn.value, mp_ms=mm.value, mp_moves=mn.value)
 
+    def mc_get_gomc_state(self) -> "_lib.GomcChk":
+        """The loop state as a GOMC checkpoint holds it
+        (gb_mc_get_gomc_state)."""
+        c = _lib.GomcChk()
+        self._chk(lib().gb_mc_get_gomc_state(self.h, C.byref(c)))
+        return c
+
+    def mc_set_gomc_state(self, chk: "_lib.GomcChk") -> None:
+        """Continue from a GOMC checkpoint's loop state
+        (gb_mc_set_gomc_state); the next mc_run starts at chk.step."""
+        self._chk(lib().gb_mc_set_gomc_state(self.h, C.byref(chk)))
+
     def mc_set_wait_limit(self, polls: int = 0) -> None:
         """Polls after which the FP64 chain's device waits give up
         (gb_mc_set_wait_limit; 0: the default)."""
@@ -728,3 +740,25 @@ class CellList:
 
     def CellMembership(self):
         return self.box.cell_membership()
+
+
+def gomc_checkpoint_read(data: bytes) -> "_lib.GomcChk":
+    """The loop state of a GOMC checkpoint file's bytes
+    (gb_gomc_checkpoint_read; CheckpointSetup's reading of it)."""
+    c = _lib.GomcChk()
+    buf = C.create_string_buffer(bytes(data), len(data))
+    check(lib().gb_gomc_checkpoint_read(buf, len(data), C.byref(c)))
+    return c
+
+
+def gomc_checkpoint_write(template: bytes, chk: "_lib.GomcChk") -> bytes:
+    """A GOMC checkpoint file: `template` (a GOMC checkpoint of the same
+    system) with the loop state of `chk` (gb_gomc_checkpoint_write)."""
+    t = C.create_string_buffer(bytes(template), len(template))
+    n = C.c_int64()
+    check(lib().gb_gomc_checkpoint_write(t, len(template), C.byref(chk),
+                                         None, 0, C.byref(n)))
+    out = C.create_string_buffer(n.value)
+    check(lib().gb_gomc_checkpoint_write(t, len(template), C.byref(chk),
+                                         out, n.value, C.byref(n)))
+    return out.raw[:n.value]

@@ -338,6 +338,58 @@ int gb_checkpoint_size(gb_box *box, int64_t *bytes);
 int gb_checkpoint_save(gb_box *box, void *buf, int64_t bytes);
 int gb_checkpoint_load(gb_box *box, const void *buf, int64_t bytes);
 
+/* ---- The reference's checkpoint file (src/Checkpoint.h:27-169) ----
+ * GOMC checkpoints (CheckpointOutput::saveCheckpointFile,
+ * src/CheckpointOutput.cpp:55-90, a cereal binary archive) carry the Monte
+ * Carlo loop state -- step, the MT19937 state (src/MersenneTwister.h
+ * save / load), the move settings (src/MoveSettings.h) -- followed by the
+ * molecule lookup, the molecule setup and the PDB atom records.  These
+ * calls exchange the loop state with a stock GOMC run: read it from a GOMC
+ * checkpoint into gb_gomc_chk, move it into or out of a box's loop, and
+ * write a GOMC checkpoint as a copy of a template checkpoint of the same
+ * system (the reference's own, which holds the records a box does not) with
+ * the loop state replaced.  Coordinates travel separately (gb_set_coords /
+ * gb_get_coords; the reference restarts them from its restart coordinate
+ * files).  Per-move arrays hold molecule kind 0 (the loop moves one kind). */
+#define GB_CHK_BOXES 2
+#define GB_CHK_MOVES 16
+#define GB_CHK_MP 2
+typedef struct gb_gomc_chk {
+  uint64_t step, true_step;   /* stepNumber, trueStepNumber */
+  uint32_t mt_state[624];     /* saveArray[0..623] */
+  uint32_t mt_left;           /* saveArray[624] */
+  uint32_t seed_location, seed_left, seed_value;
+  int32_t n_box, n_move, n_kind;  /* the file's vector shapes */
+  double scale[GB_CHK_BOXES][GB_CHK_MOVES];
+  double accept_percent[GB_CHK_BOXES][GB_CHK_MOVES];
+  uint32_t accepted[GB_CHK_BOXES][GB_CHK_MOVES];
+  uint32_t tries[GB_CHK_BOXES][GB_CHK_MOVES];
+  uint32_t temp_accepted[GB_CHK_BOXES][GB_CHK_MOVES];
+  uint32_t temp_tries[GB_CHK_BOXES][GB_CHK_MOVES];
+  uint32_t mp_tries[GB_CHK_BOXES][GB_CHK_MP];     /* MPDISPLACE, MPROTATE */
+  uint32_t mp_accepted[GB_CHK_BOXES][GB_CHK_MP];
+  uint32_t mp_interval_accepted[GB_CHK_BOXES][GB_CHK_MP];
+  uint32_t mp_interval_tries[GB_CHK_BOXES][GB_CHK_MP];
+  double mp_t_max[GB_CHK_BOXES], mp_r_max[GB_CHK_BOXES];
+  int32_t single_move_accepted[GB_CHK_BOXES];
+  int64_t records_offset;     /* bytes before the lookup / setup records */
+} gb_gomc_chk;
+/* CheckpointSetup::loadCheckpointFile's reading of the loop state
+ * (src/CheckpointSetup.cpp:45-82, SetMoveSettings / SetPRNGVariables
+ * :118-148).  GB_ERR_ARG for a truncated or malformed archive. */
+int gb_gomc_checkpoint_read(const void *buf, int64_t bytes, gb_gomc_chk *out);
+/* A GOMC checkpoint: `tmpl` (a GOMC checkpoint of the same system) with the
+ * loop state of `in`; *out_bytes receives the size (out == NULL: size
+ * only; GB_ERR_ARG when it exceeds out_cap). */
+int gb_gomc_checkpoint_write(const void *tmpl, int64_t tmpl_bytes,
+                             const gb_gomc_chk *in, void *out,
+                             int64_t out_cap, int64_t *out_bytes);
+/* The box's loop state as a GOMC checkpoint holds it (box 0, kind 0), and
+ * back: after gb_mc_set_gomc_state the next gb_mc_run starts at chk->step
+ * with the reference's random stream and move settings at that step. */
+int gb_mc_get_gomc_state(gb_box *box, gb_gomc_chk *out);
+int gb_mc_set_gomc_state(gb_box *box, const gb_gomc_chk *in);
+
 /* ---- Continuous-batching job server ----
  * No counterpart in the reference (it runs one simulation per process,
  * src/Simulation.cpp:116-168).  A server runs many independent

@@ -19,7 +19,13 @@
 //     BoxReciprocalSetup, BoxInter at new axes) and the state after one
 //     accepted volume change,
 //   - a per-step trace of the reference Monte Carlo loop
-//     (src/Simulation.cpp:94-96 without output, src/System.cpp:262-302).
+//     (src/Simulation.cpp:94-96 without output, src/System.cpp:262-302),
+//   - with GOMC_PROBE_CHK_STEP=N, the reference's own checkpoint file
+//     (CheckpointOutput::saveCheckpointFile, src/CheckpointOutput.cpp:55-90)
+//     after N steps of that loop, with the coordinates and the loop state it
+//     holds; `ref_probe --read-chk file outdir` reads a checkpoint back with
+//     the reference's deserializer (src/CheckpointSetup.cpp:45-82) and dumps
+//     the same state.
 // It is test infrastructure: it runs only in the build container.
 #include <cstdio>
 #include <cstdlib>
@@ -60,6 +66,8 @@
 #if ENSEMBLE == GEMC
 #include "MoleculeTransfer.h"
 #include "VolumeTransfer.h"
+#include "Checkpoint.h"
+#include "CheckpointOutput.h"
 #endif
 #undef private
 #undef protected
@@ -97,6 +105,61 @@ static void dump_coords(const std::string &dir, const char *name,
 // Known-answer vectors of the reference's random streams: MTRand(seed)
 // (src/MersenneTwister.h) and Random123Wrapper's Philox4x64-10
 // (src/Random123Wrapper.cpp:16-84).
+// The Monte Carlo state a checkpoint holds (step, MT19937, move settings of
+// box 0 for molecule kind 0), one value per line.
+static void dump_chk_state(const std::string &dir, const Checkpoint &c) {
+  FILE *f = open_out(dir, "chk_state.txt");
+  fprintf(f, "%llu %llu\n", (unsigned long long)c.stepNumber,
+          (unsigned long long)c.trueStepNumber);
+  for (int i = 0; i < N_array_size + 1; ++i)
+    fprintf(f, "%u\n", c.saveArray[i]);
+  fprintf(f, "%u %u %u\n", c.seedLocation, c.seedLeft, c.seedValue);
+  const uint nm = c.scaleVec[0].size();
+  fprintf(f, "%u\n", nm);
+  for (uint m = 0; m < nm; ++m)
+    fprintf(f, "%.17g %.17g %u %u %u %u\n", c.scaleVec[0][m][0],
+            c.acceptPercentVec[0][m][0], c.acceptedVec[0][m][0],
+            c.triesVec[0][m][0], c.tempAcceptedVec[0][m][0],
+            c.tempTriesVec[0][m][0]);
+  for (uint t = 0; t < c.mp_triesVec[0].size(); ++t)
+    fprintf(f, "%u %u %u %u\n", c.mp_triesVec[0][t], c.mp_acceptedVec[0][t],
+            c.mp_interval_triesVec[0][t], c.mp_interval_acceptedVec[0][t]);
+  fprintf(f, "%.17g %.17g %d\n", c.mp_t_maxVec[0], c.mp_r_maxVec[0],
+          (int)c.isSingleMoveAcceptedVec[0]);
+  fclose(f);
+}
+
+// A checkpoint file read back as CheckpointSetup::loadCheckpointFile reads
+// it: the Checkpoint object, then the molecule lookup's arrays.
+static int read_chk(const char *file, const std::string &dir) {
+  std::ifstream ifs(file, std::ios::binary);
+  if (!ifs.is_open())
+    return 1;
+  Checkpoint c;
+  cereal::BinaryInputArchive ia(ifs);
+  ia >> c;
+  MoleculeLookup &ml = c.originalMoleculeLookup;
+  std::vector<uint32_t> a(ml.molLookupCount), b(ml.boxAndKindStartLength),
+      sw(ml.boxAndKindSwappableLength);
+  std::vector<int32_t> mi(ml.atomCount), ai(ml.atomCount), mk(ml.atomCount),
+      ak(ml.atomCount);
+  std::vector<double> q(ml.atomCount);
+  ia(cereal::binary_data(a.data(), 4 * a.size()));
+  ia(cereal::binary_data(b.data(), 4 * b.size()));
+  ia(cereal::binary_data(sw.data(), 4 * sw.size()));
+  ia(cereal::binary_data(mi.data(), 4 * mi.size()));
+  ia(cereal::binary_data(ai.data(), 4 * ai.size()));
+  ia(cereal::binary_data(mk.data(), 4 * mk.size()));
+  ia(cereal::binary_data(ak.data(), 4 * ak.size()));
+  ia(cereal::binary_data(q.data(), 8 * q.size()));
+  dump_chk_state(dir, c);
+  FILE *f = open_out(dir, "chk_lookup.txt");
+  for (uint32_t v : a)
+    fprintf(f, "%u\n", v);
+  fclose(f);
+  return 0;
+}
+
 static int dump_kat(const std::string &dir) {
   FILE *f = open_out(dir, "kat_mt.txt");
   const unsigned seeds[3] = {1234u, 4321u, 4294967295u};
@@ -130,6 +193,8 @@ static int dump_kat(const std::string &dir) {
 int main(int argc, char **argv) {
   if (argc == 3 && std::string(argv[1]) == "--kat")
     return dump_kat(argv[2]);
+  if (argc == 4 && std::string(argv[1]) == "--read-chk")
+    return read_chk(argv[2], argv[3]);
   if (argc < 4) {
     fprintf(stderr,
             "usage: ref_probe in.conf outdir nsteps [proposals.txt|-] "
@@ -515,7 +580,24 @@ int main(int argc, char **argv) {
   if (nsteps > 0) {
     FILE *f = open_out(outdir, "trace.txt");
     MoveSettings &ms = sys.moveSettings;
+    const char *chk_env = getenv("GOMC_PROBE_CHK_STEP");
+    const long chk_step = chk_env ? atol(chk_env) : -1;
     for (long step = 0; step < nsteps; ++step) {
+      if (step == chk_step) {
+        // the checkpoint the reference writes after step chk_step - 1
+        // (DoOutputRestart: the next run starts at chk_step)
+        CheckpointOutput co(sys, stat, sim.set);
+        co.filename = outdir + "/restart.chk";
+        co.restartFromCheckpoint = false;  // a first run: true step = step
+        co.startStep = 0;
+        co.saveCheckpointFile(chk_step, ms, sys.prng, stat.mol,
+                              sys.molLookupRef);
+        Checkpoint c(chk_step, chk_step, ms, sys.prng, stat.mol,
+                     sys.molLookupRef, sim.set.mol, sim.set.pdb.atoms);
+        dump_chk_state(outdir, c);
+        dump_coords(outdir, "coords_chk.txt", sys.coordinates);
+        dump_coords(outdir, "com_chk.txt", sys.com);
+      }
       ms.AdjustMoves(step);
       sys.r123wrapper.SetStep(step);
       double draw = 0;

@@ -442,6 +442,60 @@ def make_gemc(ref: str, name: str = "c3_gemc") -> None:
         print("wrote", name)
 
 
+# checkpoint fixture: the reference's own checkpoint file after CHK_STEP of
+# CHK_TOTAL steps of c0_water's Monte Carlo loop, with the state it holds
+CHK_STEP, CHK_TOTAL = 600, 1000
+
+
+def _chk_state(path):
+    """chk_state.txt of the probe: steps, MT19937 save array and seeds,
+    per-move settings of box 0 / kind 0, MultiParticle counters."""
+    with open(path) as f:
+        lines = [ln.split() for ln in f]
+    steps = np.array([int(v) for v in lines[0]], dtype=np.uint64)
+    mt = np.array([int(lines[1 + i][0]) for i in range(625)], dtype=np.uint64)
+    seeds = np.array([int(v) for v in lines[626]], dtype=np.uint64)
+    nm = int(lines[627][0])
+    moves = np.array([[float(v) for v in lines[628 + m]] for m in range(nm)])
+    mp = np.array([[int(v) for v in ln] for ln in lines[628 + nm:630 + nm]],
+                  dtype=np.uint64)
+    mpmax = np.array([float(v) for v in lines[630 + nm]])
+    return dict(chk_steps=steps, chk_mt=mt, chk_seeds=seeds, chk_moves=moves,
+                chk_mp=mp, chk_mpmax=mpmax)
+
+
+def make_checkpoint(probe: str, name: str = "c0_water") -> None:
+    """The reference's checkpoint file (CheckpointOutput) after CHK_STEP
+    steps, the coordinates and loop state it belongs to, and the trace of
+    the whole CHK_TOTAL-step run, so that a box handed that state continues
+    the reference's run."""
+    builder, cfg, _, _ = FIXTURES[name]
+    sysm = builder()
+    with tempfile.TemporaryDirectory() as d:
+        write_reference_inputs(d, sysm, cfg)
+        out = os.path.join(d, "out")
+        os.makedirs(out)
+        env = dict(os.environ, GOMC_PROBE_CHK_STEP=str(CHK_STEP))
+        subprocess.check_call([probe, "in.conf", out, str(CHK_TOTAL)], cwd=d,
+                              env=env, stdout=subprocess.DEVNULL)
+        with open(os.path.join(out, "restart.chk"), "rb") as f:
+            chk = np.frombuffer(f.read(), dtype=np.uint8)
+        arrays = dict(chk=chk,
+                      coords_chk=np.loadtxt(os.path.join(out, "coords_chk.txt")),
+                      com_chk=np.loadtxt(os.path.join(out, "com_chk.txt")),
+                      trace=np.loadtxt(os.path.join(out, "trace.txt")),
+                      coords_final=np.loadtxt(os.path.join(out,
+                                                           "coords_final.txt")),
+                      **_chk_state(os.path.join(out, "chk_state.txt")))
+        meta = dict(name=name, chk_step=CHK_STEP, total=CHK_TOTAL,
+                    final=_energies(os.path.join(out, "energies_final.txt")))
+        arrays["meta_json"] = np.frombuffer(json.dumps(meta).encode(),
+                                            dtype=np.uint8)
+        np.savez_compressed(os.path.join(HERE, "chk_" + name + ".npz"),
+                            **arrays)
+        print("wrote chk_" + name)
+
+
 def make_kat(probe: str) -> None:
     """Known-answer vectors of the reference's MT19937 and Philox4x64-10."""
     with tempfile.TemporaryDirectory() as d:
@@ -459,7 +513,8 @@ def make_kat(probe: str) -> None:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default=os.environ.get("GOMC_REFERENCE"))
-    ap.add_argument("--only", choices=("particles", "volumes", "gemc"),
+    ap.add_argument("--only", choices=("particles", "volumes", "gemc",
+                                       "checkpoint"),
                     default=None,
                     help="only the ParticleInter, volume-move or GEMC vectors")
     ap.add_argument("names", nargs="*")
@@ -473,6 +528,9 @@ def main():
         return
     if a.only == "gemc":
         make_gemc(a.ref)
+        return
+    if a.only == "checkpoint":
+        make_checkpoint(probe)
         return
     if a.only == "volumes":
         for n in (a.names or list(VOLUME_FRACS)):
@@ -495,6 +553,8 @@ def main():
             make_volumes(probe, n)
     if not a.names or "c3_gemc" in a.names:
         make_gemc(a.ref)
+    if not a.names:
+        make_checkpoint(probe)
 
 
 if __name__ == "__main__":

@@ -129,3 +129,46 @@ def test_rejected_load_leaves_box_unchanged(gb):
     for a, b in zip(_state(box), want):
         np.testing.assert_array_equal(a, b)
     box.close()
+
+
+def test_continues_reference_run_from_its_checkpoint(gb):
+    """Hand-off from a stock GOMC run: the reference's own checkpoint after
+    600 steps of c0_water (tests/golden/chk_c0_water.npz) and the
+    coordinates it belongs to go into a fresh box (gb_set_coords,
+    gb_mc_set_gomc_state); the box's next 400 moves are the reference's
+    steps 600-999 -- same molecules, kinds and decisions, energy changes to
+    1e-10 -- and its loop state at step 1,000, written back as a GOMC
+    checkpoint over the reference's file, reads back with the reference's
+    move counts and scales at that step."""
+    import json
+    import os
+    from tests.golden_util import GOLDEN
+    z, meta = load("c0_water")
+    zc = np.load(os.path.join(GOLDEN, "chk_c0_water.npz"))
+    mc = json.loads(bytes(zc["meta_json"]).decode())
+    first, total = mc["chk_step"], mc["total"]
+    box = gb.Box(system_of(z, meta), config_of(meta))
+    box.mc_init(meta["config"]["random_seed"], move_fractions(meta),
+                meta["config"]["adj_steps"])
+    box.set_coords(zc["coords_chk"], zc["com_chk"].reshape(-1, 3))
+    chk = gb.gomc_checkpoint_read(bytes(zc["chk"]))
+    box.mc_set_gomc_state(chk)
+    r = box.mc_run(first, total - first, trace=True)
+    tr = zc["trace"][first:total]
+    np.testing.assert_array_equal(r["kind"], tr[:, 1].astype(int))
+    np.testing.assert_array_equal(r["mol"], tr[:, 2].astype(int))
+    np.testing.assert_array_equal(r["accepted"], tr[:, 3].astype(int))
+    scale = np.maximum(np.abs(tr[-1, 8:11]), 1.0)
+    for j in range(3):
+        bound = 1e-10 * np.maximum(scale[j], np.abs(tr[:, 5 + j]))
+        assert (np.abs(r["de"][:, j] - tr[:, 5 + j]) <= bound).all(), j
+    np.testing.assert_allclose(box.coords(), zc["coords_final"], rtol=0,
+                               atol=1e-9)
+    out = gb.gomc_checkpoint_write(bytes(zc["chk"]), box.mc_get_gomc_state())
+    back = gb.gomc_checkpoint_read(out)
+    assert back.step == total
+    for k in (0, 1):
+        tries, acc, scl = mc["final"]["move%d" % k]
+        assert back.tries[0][k] == tries and back.accepted[0][k] == acc
+        assert abs(back.scale[0][k] - scl) <= 1e-12 * scl
+    box.close()
