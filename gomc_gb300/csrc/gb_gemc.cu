@@ -63,7 +63,7 @@ struct Move {
   int kind, b, b1, m, ok;
   double u_acc;            // acceptance uniform (displacement, volume)
   unsigned pick_word;      // raw word of PickWeighted (transfer)
-  double np[3], nc[3];     // displacement: new position; centre (CTA 0)
+  double np[3], sh[3];     // displacement: new position; shift
   float nf[3];             // its FP32 copy
   unsigned nt[3];          // its fixed-point turns (mixed form)
   double tr[2 * GEMC_NTMAX][3];     // transfer: new trials, then old trials
@@ -74,7 +74,7 @@ struct Move {
   float nlt[2][3];         // volume: FP32 turn lengths at the new edges
   double d[4];             // values reported in the trace
   double tot[PMAX];        // cluster sums of the partials
-  unsigned words[6 * GEMC_NTMAX];  // raw words of the transfer's trials
+  unsigned words[6 * GEMC_NTMAX + 2];  // raw words of a transfer's build
   double wts[2 * GEMC_NTMAX];      // trial weights
 };
 
@@ -170,21 +170,42 @@ __device__ void mt_phase(unsigned *st, int lo, int hi) {
 struct MtCursor {
   unsigned *st;
   int left, next;
-  __device__ unsigned u32() {
-    if (left == 0) {
-      mt_phase(st, 0, 227);
-      mt_phase(st, 227, 454);
-      mt_phase(st, 454, 623);
-      mt_phase(st, 623, 624);
-      left = 624;
-      next = 0;
-    }
-    --left;
-    unsigned y = st[next++];
+  __device__ void reload() {
+    mt_phase(st, 0, 227);
+    mt_phase(st, 227, 454);
+    mt_phase(st, 454, 623);
+    mt_phase(st, 623, 624);
+    left = 624;
+    next = 0;
+  }
+  __device__ static unsigned temper(unsigned y) {
     y ^= (y >> 11);
     y ^= (y << 7) & 0x9d2c5680u;
     y ^= (y << 15) & 0xefc60000u;
     return y ^ (y >> 18);
+  }
+  __device__ unsigned u32() {
+    if (left == 0)
+      reload();
+    --left;
+    return temper(st[next++]);
+  }
+  // The next `count` words of the stream into dst (shared memory), the lanes
+  // of the warp tempering one word each -- the same words, in the same
+  // order, as `count` calls of u32(); every lane calls it.
+  __device__ void bulk(unsigned *dst, int count, int lane) {
+    int done = 0;
+    while (done < count) {
+      if (left == 0)
+        reload();
+      const int take = min(left, count - done);
+      for (int i = lane; i < take; i += 32)
+        dst[done + i] = temper(st[next + i]);
+      next += take;
+      left -= take;
+      done += take;
+    }
+    __syncwarp();
   }
   __device__ double rand01() { return (double)u32() * (1.0 / 4294967295.0); }
   __device__ double randExc01() {
@@ -466,6 +487,7 @@ __global__ void __launch_bounds__(GEMC_THREADS)
   };
   Move &M = S.mv;
 
+  double cpend = 0.0;  // CTA 0, warp 0, lanes 0-2: a displaced centre
   for (int t = 0; t < p.nsteps; ++t) {
     const long long step = p.first + t;
     const int par = t & 1;
@@ -516,14 +538,13 @@ __global__ void __launch_bounds__(GEMC_THREADS)
           const double pv = lane == 0 ? A.px[m] : lane == 1 ? A.py[m] : A.pz[m];
           const double nv = wrapd(pv + sh, c.ax[b][lane]);
           M.np[lane] = nv;
+          M.sh[lane] = sh;
           M.nf[lane] = (float)nv;
           if (MIXED)
             M.nt[lane] = turns(nv, 1.0 / c.ax[b][lane]);
-          if (rank == 0) {  // the centres are CTA 0's (global memory)
-            const double cv =
-                lane == 0 ? p.cx[m] : lane == 1 ? p.cy[m] : p.cz[m];
-            M.nc[lane] = wrapd(cv + sh, c.ax[b][lane]);
-          }
+          if (rank == 0)  // the centres are CTA 0's (global memory): the
+                          // load is consumed at the commit
+            cpend = lane == 0 ? p.cx[m] : lane == 1 ? p.cy[m] : p.cz[m];
         } else if (lane == 3) {
           M.u_acc = (double)w3 * (1.0 / 4294967295.0);
         }
@@ -532,24 +553,17 @@ __global__ void __launch_bounds__(GEMC_THREADS)
         // destination box, PickWeighted), DCSingle::BuildOld (trials in the
         // source box, trial 0 at the molecule): the raw words in order, then
         // each lane scales its own coordinates
-        (void)R.randInt(1);
+        // randInt(1) draws one word (a 1-bit mask never rejects), then
+        // 3 nt words, the PickWeighted word, 3 nt words: 6 nt + 2 words
         unsigned *wbuf = M.words;
-        for (int k = 0; k < 3 * nt; ++k) {
-          unsigned w = R.u32();
-          if (lane == 0)
-            wbuf[k] = w;
-        }
-        pick_word = R.u32();
-        for (int k = 0; k < 3 * nt; ++k) {
-          unsigned w = R.u32();
-          if (lane == 0)
-            wbuf[3 * nt + k] = w;
-        }
-        __syncwarp();
+        R.bulk(wbuf, 6 * nt + 2, lane);
+        pick_word = wbuf[1 + 3 * nt];
+        wbuf += 1;  // the trial words: [0, 3 nt) new, [3 nt + 1, ...) old
         for (int q = lane; q < 6 * nt; q += 32) {
           const int k = q / 3, d = q - 3 * k;
           const int bb = k < nt ? b1 : b;
-          double v = (double)wbuf[q] * (1.0 / 4294967296.0) * c.ax[bb][d];
+          const unsigned w = wbuf[q < 3 * nt ? q : q + 1];
+          double v = (double)w * (1.0 / 4294967296.0) * c.ax[bb][d];
           if (k == nt)
             v = wrapd(d == 0 ? A.px[m] : d == 1 ? A.py[m] : A.pz[m],
                       c.ax[b][d]);
@@ -1111,11 +1125,7 @@ __global__ void __launch_bounds__(GEMC_THREADS)
           A.tz[m] = M.nt[2];
         }
         if (kind == GEMC_DISPLACE) {
-          if (rank == 0) {
-            p.cx[m] = M.nc[0];
-            p.cy[m] = M.nc[1];
-            p.cz[m] = M.nc[2];
-          }
+          // the centre: below, by the lanes that loaded it
         } else {
           // COM::SetNew of one atom; MoleculeLookup::Shift
           if (rank == 0) {
@@ -1133,7 +1143,12 @@ __global__ void __launch_bounds__(GEMC_THREADS)
             c.e[b] = 0.0;
         }
       }
-    } else if (acc && kind == GEMC_VOLUME) {
+    }
+    if (acc && kind == GEMC_DISPLACE && rank == 0 && warp == 0 && lane < 3) {
+      double *cc = lane == 0 ? p.cx : lane == 1 ? p.cy : p.cz;
+      cc[m] = wrapd(cpend + M.sh[lane], c.ax[b][lane]);
+    }
+    if (acc && kind == GEMC_VOLUME) {
       // new positions, centres and axes
       for (int i = tid; i < n; i += GEMC_THREADS) {
         int j = A.lookup[i];

@@ -700,14 +700,27 @@ struct CtxPre {
   double v0, v1, q;
   bool writer;
 };
-__device__ __forceinline__ void ctx_pre1(const ChainArgs &A, int t, CtxPre &c) {
-  const MoveRec &r = A.moves[t];
-  c.m = r.mol;
-  c.kind = r.kind;
-  c.pacc = r.pacc;
-  c.lpacc = r.lpacc;
-  c.a0 = A.b.mstart[c.m];
-  c.na = A.b.mstart[c.m + 1] - c.a0;
+// The static inputs of a move's context, gathered two moves ahead in two
+// steps so that no load is waited for: the move record first, a move later
+// the molecule's atom range (whose address needs the record's molecule).
+__device__ __forceinline__ void ctx_pre_record(const ChainArgs &A, int t,
+                                               CtxPre &c) {
+  c.m = -1;
+  if (t < A.n) {
+    const MoveRec &r = A.moves[t];
+    c.m = r.mol;
+    c.kind = r.kind;
+    c.pacc = r.pacc;
+    c.lpacc = r.lpacc;
+  }
+}
+__device__ __forceinline__ void ctx_pre_range(const ChainArgs &A, CtxPre &c,
+                                              int &a1) {
+  c.a0 = a1 = 0;
+  if (c.m >= 0) {
+    c.a0 = A.b.mstart[c.m];
+    a1 = A.b.mstart[c.m + 1];
+  }
 }
 __device__ __forceinline__ void ctx_pre2(const ChainArgs &A,
                                          const ChainShared &S, int t,
@@ -929,19 +942,32 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     }
   };
   // the molecule of the move after the current one, loaded a move ahead;
-  // warp 7 also loads that move's record and atom range a move ahead
+  // warps 7 (context inputs) and 4 (the leader's count of context writers)
+  // carry the next moves' records and atom ranges through a two-stage
+  // pipeline: at move t the record of move t + 3 is requested, the atom
+  // range of move t + 2, and move t + 1's are complete
   int nmol = A.n > 1 ? A.moves[1].mol : -1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  CtxPre pre_nx;
-  pre_nx.writer = false;
-  if (warp == 7 && A.n > 1)
-    ctx_pre1(A, 1, pre_nx);
+  const bool piper = warp == 7 || warp == 4;
+  CtxPre pipe_a, pipe_b;  // record of t + 2 (a), record and range of t + 1 (b)
+  int pipe_b1 = 0;
+  pipe_a.writer = pipe_b.writer = false;
+  pipe_a.m = pipe_b.m = -1;
+  if (piper) {
+    ctx_pre_record(A, 1, pipe_b);
+    ctx_pre_range(A, pipe_b, pipe_b1);
+    ctx_pre_record(A, 2, pipe_a);
+  }
   for (int t = 0; t < A.n; ++t) {
     const int mol_next = nmol;
     nmol = t + 2 < A.n ? A.moves[t + 2].mol : -1;
-    CtxPre pre = pre_nx;
-    if (warp == 7 && t + 2 < A.n)
-      ctx_pre1(A, t + 2, pre_nx);
+    CtxPre pre = pipe_b;
+    pre.na = pipe_b1 - pipe_b.a0;
+    if (piper) {
+      pipe_b = pipe_a;
+      ctx_pre_range(A, pipe_b, pipe_b1);
+      ctx_pre_record(A, t + 3, pipe_a);
+    }
     // ---------------- phase A ----------------
     // the header and the rows of the largest molecule in one round trip
     const double *ctx_t = A.ctx + (size_t)(t & 1) * A.ctx_len;
@@ -963,14 +989,9 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
                       (A.first + t + 2) % S.set.adj != 0;
     pre.writer = false;
     const bool wload = spec && warp == 7;
-    // the leader's warp 4 counts the next context's writers now (the loads
-    // arrive during this phase)
-    int nbuild = 1;
-    if (spec && warp == 4 && cta == G - 1) {
-      const int a0n = __ldg(b.mstart + mol_next);
-      const int nan = __ldg(b.mstart + mol_next + 1) - a0n;
-      nbuild = max(1, min(G, b.K > 0 ? 2 * nan * 3 : 0));
-    }
+    // the next context's writers, counted by the leader's warp 4 from the
+    // next move's atom count its pipeline holds
+    const int nbuild = max(1, min(G, b.K > 0 ? 2 * pre.na * 3 : 0));
     double lj = 0.0, re = 0.0, ovl = 0.0, er = 0.0;
     // first atom of the moved molecule, for the commit to the own atoms
     const int a0m = __ldg(b.mstart + m);
