@@ -326,6 +326,13 @@ __global__ void __launch_bounds__(MT_THREADS)
     // then it is built during the cluster barrier before the decision.
     const bool spec = t + 1 < C.n && C.moves[t + 1].mol != m &&
                       (C.first + t + 2) % S.set.adj != 0;
+    // the moved atoms' current cells and slots, for the commit of rank 0
+    // (loaded now, used after the decision)
+    int cur_cell = -1, cur_slot = -1;
+    if (rank == 0 && threadIdx.x < na) {
+      cur_cell = __ldcg(b.atom_cell + h.a0 + threadIdx.x);
+      cur_slot = __ldcg(b.atom_slot + h.a0 + threadIdx.x);
+    }
     // ---------------- real space ----------------
     // Each neighbour j is taken once: from the new position's cells when it
     // is inside the cutoff there (then as the difference u(r') - u(r) if it
@@ -642,19 +649,38 @@ __global__ void __launch_bounds__(MT_THREADS)
         s32I[i] = im.hi;
         loI[i] = im.lo;
       }
-      if (rank == 0 && threadIdx.x == 0) {
-        for (int a = 0; a < na; ++a) {
+      if (rank == 0 && threadIdx.x < 32) {
+        // Atoms that stay in their cell are rewritten in place by one lane
+        // each; then the atoms that change cell are relinked one after
+        // another, in atom order -- the slot layout that relinking every
+        // atom in order would give.
+        const int a = threadIdx.x;
+        bool stay = false;
+        if (a < na) {
           const double *np = h.newp[a];
-          int at = h.a0 + a;
+          const int at = h.a0 + a;
           b.x[at] = np[0];
           b.y[at] = np[1];
           b.z[at] = np[2];
-          cell_move_atom(b, at, np[0], np[1], np[2], h.cell_new[a]);
+          stay = cur_cell == h.cell_new[a];
+          if (stay)
+            cell_write_slot(b, cur_cell, cur_slot, at, np[0], np[1], np[2],
+                            h.un[a]);
         }
-        if (h.kind == 0) {
-          b.cx[m] = h.newcom[0];
-          b.cy[m] = h.newcom[1];
-          b.cz[m] = h.newcom[2];
+        const unsigned moving = __ballot_sync(0xffffffffu, a < na && !stay);
+        __syncwarp();
+        if (a == 0) {
+          for (int i = 0; i < na; ++i)
+            if (moving & (1u << i)) {
+              const double *np = h.newp[i];
+              cell_move_atom(b, h.a0 + i, np[0], np[1], np[2], h.cell_new[i],
+                             h.un[i]);
+            }
+          if (h.kind == 0) {
+            b.cx[m] = h.newcom[0];
+            b.cy[m] = h.newcom[1];
+            b.cz[m] = h.newcom[2];
+          }
         }
       }
     }
