@@ -50,8 +50,18 @@ struct MHdr {
   int ka[MAXA];
 };
 
+// Inputs of the next move's header that warp 7 loaded during the current
+// move (its record, atom range, proposal, centre, positions, charges).
+struct MPre {
+  int m, kind, a0, na;
+  double lpacc;
+  double prop[12], com[3], oldp[MAXA][3], q[MAXA];
+  int ka[MAXA];
+};
+
 struct MShared {
   MHdr hh[2];  // this move's header and the next one's, by move parity
+  MPre pre;
   Settings set;
   double e_run[5];
   double part[4];        // this CTA's partial: LJ, real, recip, overlap
@@ -147,33 +157,44 @@ __device__ __forceinline__ float2 tabf(const float2 *row, int n) {
 // Header of move t into h (all threads of the CTA call it); prev is the
 // previous move's header, whose new positions are the current ones when
 // that move was accepted and touched the same molecule.
+// With `pre`, the inputs come from warp 7's loads (S.pre) instead of
+// global memory.
 __device__ void mixed_header(const MixedChain &C, MShared &S, int t,
                              bool prev_acc, int prev_m, int prev_kind,
-                             const MHdr &prev, MHdr &h) {
+                             const MHdr &prev, MHdr &h, bool pre = false) {
   const DevBox &b = C.b;
   const MoveRec &r = C.moves[t];
-  int m = r.mol;
-  int a0 = b.mstart[m], na = b.mstart[m + 1] - a0;
+  const MPre &P = S.pre;
+  int m = pre ? P.m : r.mol;
+  int a0 = pre ? P.a0 : b.mstart[m];
+  int na = pre ? P.na : b.mstart[m + 1] - a0;
+  const int rkind = pre ? P.kind : r.kind;
+  const double rlpacc = pre ? P.lpacc : r.lpacc;
   bool same = prev_acc && prev_m == m;
   // the previous header still holds that move's new positions
   __shared__ double oldp[MAXA][3], com[3];
   if (threadIdx.x < 12)
-    S.prop[threadIdx.x] = C.prop[(size_t)t * 12 + threadIdx.x];
+    S.prop[threadIdx.x] = pre ? P.prop[threadIdx.x]
+                              : C.prop[(size_t)t * 12 + threadIdx.x];
   if (threadIdx.x < 3) {
     int d = threadIdx.x;
     const double *cs[3] = {b.cx, b.cy, b.cz};
-    com[d] = (same && prev_kind == 0) ? prev.newcom[d] : __ldcg(cs[d] + m);
+    com[d] = (same && prev_kind == 0) ? prev.newcom[d]
+             : pre                    ? P.com[d]
+                                      : __ldcg(cs[d] + m);
   }
   if (threadIdx.x >= 32 && threadIdx.x < 32 + 3 * na) {
     int i = threadIdx.x - 32, a = i / 3, d = i % 3;
     const double *xs[3] = {b.x, b.y, b.z};
-    oldp[a][d] = same ? prev.newp[a][d] : __ldcg(xs[d] + a0 + a);
+    oldp[a][d] = same ? prev.newp[a][d]
+                 : pre ? P.oldp[a][d]
+                       : __ldcg(xs[d] + a0 + a);
   }
   __syncthreads();
   if (threadIdx.x < na) {
     int a = threadIdx.x;
     double w[3];
-    if (r.kind == 0) {
+    if (rkind == 0) {
       for (int d = 0; d < 3; ++d)
         w[d] = wrap1(__dadd_rn(oldp[a][d], S.prop[d]), b.L[d]);
     } else {
@@ -203,24 +224,24 @@ __device__ void mixed_header(const MixedChain &C, MShared &S, int t,
     }
     h.cell_old[a] = position_to_cell_fast(b, oldp[a][0], oldp[a][1], oldp[a][2]);
     h.cell_new[a] = position_to_cell_fast(b, w[0], w[1], w[2]);
-    double q = b.q[a0 + a];
+    double q = pre ? P.q[a] : b.q[a0 + a];
     bool q0 = fabs(q) < 0.000000001;
     h.qf[a] = q0 ? 0.0f : (float)q;
     h.qflo[a] = q0 ? 0.0f : (float)(q - (double)(float)q);
     double qs = q * SQRT_QQ_FACT;
     h.qs[a] = q0 ? 0.0f : (float)qs;
     h.qslo[a] = q0 ? 0.0f : (float)(qs - (double)(float)qs);
-    h.ka[a] = b.kind[a0 + a];
+    h.ka[a] = pre ? P.ka[a] : b.kind[a0 + a];
   }
   if (threadIdx.x == 64) {
     h.m = m;
-    h.kind = r.kind;
+    h.kind = rkind;
     h.na = na;
     h.a0 = a0;
-    h.lpacc = r.lpacc;
+    h.lpacc = rlpacc;
     for (int d = 0; d < 3; ++d)
-      h.newcom[d] = r.kind == 0 ? wrap1(__dadd_rn(com[d], S.prop[d]), b.L[d])
-                                : com[d];
+      h.newcom[d] = rkind == 0 ? wrap1(__dadd_rn(com[d], S.prop[d]), b.L[d])
+                               : com[d];
   }
   __syncthreads();
 }
@@ -317,8 +338,65 @@ __global__ void __launch_bounds__(MT_THREADS)
                       b.cellSize[1] * b.cellSize[1] < ff.rcutSq ||
                       b.cellSize[2] * b.cellSize[2] < ff.rcutSq;
 
+  // Warp 7 gathers the next move's header inputs one move ahead: the move
+  // record two moves ahead, its atom range a move later, and at the start
+  // of a move the proposal, centre, positions and charges of the next one,
+  // so that the next header is built from registers inside the cluster
+  // barrier.
+  const int wid = threadIdx.x >> 5, lid = threadIdx.x & 31;
+  int pa_m = -1, pa_kind = 0, pb_m = -1, pb_kind = 0, pb_a0 = 0, pb_a1 = 0;
+  double pa_lp = 0.0, pb_lp = 0.0;
+  auto pipe_record = [&](int t) {
+    pa_m = -1;
+    if (t < C.n) {
+      pa_m = C.moves[t].mol;
+      pa_kind = C.moves[t].kind;
+      pa_lp = C.moves[t].lpacc;
+    }
+  };
+  auto pipe_range = [&]() {
+    pb_m = pa_m;
+    pb_kind = pa_kind;
+    pb_lp = pa_lp;
+    if (pb_m >= 0) {
+      pb_a0 = b.mstart[pb_m];
+      pb_a1 = b.mstart[pb_m + 1];
+    }
+  };
+  if (wid == 7) {
+    pipe_record(1);
+    pipe_range();
+    pipe_record(2);
+  }
   for (int t = 0; t < C.n; ++t) {
     const MHdr &h = S.hh[t & 1];
+    // warp 7: the next move's inputs (their record and range loaded before)
+    int n_m = -1, n_kind = 0, n_a0 = 0, n_na = 0;
+    double n_lp = 0.0, v_prop = 0.0, v_com = 0.0, v_pos = 0.0, v_q = 0.0;
+    int v_k = 0;
+    if (wid == 7) {
+      n_m = pb_m;
+      n_kind = pb_kind;
+      n_lp = pb_lp;
+      n_a0 = pb_a0;
+      n_na = pb_a1 - pb_a0;
+      if (n_m >= 0) {
+        if (lid < 12)
+          v_prop = C.prop[(size_t)(t + 1) * 12 + lid];
+        if (lid < 3)
+          v_com = __ldcg((lid == 0 ? b.cx : lid == 1 ? b.cy : b.cz) + n_m);
+        if (lid < 3 * n_na) {
+          const int a = lid / 3, d = lid % 3;
+          v_pos = __ldcg((d == 0 ? b.x : d == 1 ? b.y : b.z) + n_a0 + a);
+        }
+        if (lid < n_na) {
+          v_q = b.q[n_a0 + lid];
+          v_k = b.kind[n_a0 + lid];
+        }
+      }
+      pipe_range();
+      pipe_record(t + 3);
+    }
     const float2 *const tab = tabs + (t & 1) * tab_len;
     const int m = h.m, na = h.na;
     // The next header does not depend on this move's outcome unless the
@@ -594,7 +672,28 @@ __global__ void __launch_bounds__(MT_THREADS)
     // header meanwhile, wait before reading the other CTAs' partials
     asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
     if (spec) {
-      mixed_header(C, S, t + 1, false, -1, 0, h, S.hh[(t + 1) & 1]);
+      if (wid == 7) {
+        MPre &P = S.pre;
+        if (lid == 0) {
+          P.m = n_m;
+          P.kind = n_kind;
+          P.a0 = n_a0;
+          P.na = n_na;
+          P.lpacc = n_lp;
+        }
+        if (lid < 12)
+          P.prop[lid] = v_prop;
+        if (lid < 3)
+          P.com[lid] = v_com;
+        if (lid < 3 * n_na)
+          P.oldp[lid / 3][lid % 3] = v_pos;
+        if (lid < n_na) {
+          P.q[lid] = v_q;
+          P.ka[lid] = v_k;
+        }
+      }
+      __syncthreads();
+      mixed_header(C, S, t + 1, false, -1, 0, h, S.hh[(t + 1) & 1], true);
       mixed_tables(C, S.hh[(t + 1) & 1], tabs + ((t + 1) & 1) * tab_len);
     }
     asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
