@@ -1138,9 +1138,9 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
         double dR = 0, dI = 0;
         const double2 *col = npair > 0 ? exy + (size_t)pidx[i] * 2 * na : nullptr;
         for (int a = 0; a < na; ++a) {
-          double q = S.hdr[72 + a];
-          if (q == 0.0)
-            continue;
+          // a zero charge contributes exact zeros (the x-y products carry
+          // the charge), so no FP64 test of it is made here
+          const double q = S.hdr[72 + a];
           const double2 *ro = tab + (size_t)(a * 3) * stride;
           const double2 *rn = tab + (size_t)((na + a) * 3) * stride;
           double2 xo, xn;
