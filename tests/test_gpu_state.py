@@ -74,3 +74,33 @@ def test_set_coords_computes_centres(gb):
     for i, term in enumerate(("inter", "real", "recip")):
         assert abs(e[i] - st[term]) <= REL * abs(st[term]), term
     box.close()
+
+
+def test_chain_profile_accounts_for_the_chain(gb):
+    """gb_mc_profile: the FP64 chain's phase clocks of CTA 0 and of the
+    deciding CTA cover the moves run with collection on, add up to about
+    the chain's device time, and collection off adds nothing."""
+    z, meta = load("c0_water")
+    box = gb.Box(system_of(z, meta), config_of(meta))
+    box.mc_init(meta["config"]["random_seed"], move_fractions(meta),
+                meta["config"]["adj_steps"])
+    box.mc_run(0, 100)
+    box.mc_profile(enable=True)
+    box.mc_timing(reset=True)
+    box.mc_run(100, 400)
+    t = box.mc_timing(reset=True)
+    pr = box.mc_profile(enable=False)
+    assert pr["moves"] == [400, 400]
+    for who in ("cta0", "leader"):
+        phases = pr[who]
+        keys = ("context", "listing", "partials", "decision_wait",
+                "commit_next")
+        assert all(phases[k] >= 0.0 for k in keys)
+        total_us = sum(phases[k] for k in keys)
+        # the clocks run inside the kernel; the events also hold the launch,
+        # the prologue and the grid rebuild
+        assert 0.5 * t["chain_ms"] * 1e3 <= total_us <= 1.05 * t["chain_ms"] * 1e3
+    box.mc_run(500, 100)
+    again = box.mc_profile(enable=False)
+    assert again["moves"] == [0, 0]
+    box.close()
