@@ -364,9 +364,12 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
                      "ms_per_step": sum(t_single) / args.steps * 1e3,
                      "us_per_move": sum(t_single) / (args.steps * M) * 1e6,
                      "ctas_per_chain": layout["ctas_per_chain"],
+                     "unit_lanes": tune_single and
+                     tune_single["chosen"]["unit_lanes"],
                      "autotune_us_per_move": tune_single and {
-                         str(k): v for k, v in
-                         tune_single["us_per_move"].items()}}
+                         "%d x %d" % (t["ctas"], t["unit_lanes"]):
+                         round(t["us_per_move"], 2)
+                         for t in tune_single["tried"]}}
 
     # batched replicas, one launch per step for every chain; the cluster
     # size from the autotuner's throughput objective on the first replica
@@ -380,13 +383,14 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
         tune_batch = b0.mc_autotune("throughput")
     lay0 = b0.mc_layout()
     csize = lay0["ctas_per_chain"]
+    lanes = tune_batch["chosen"]["unit_lanes"] if tune_batch else 0
     boxes.append(b0)
     B = args.mixed_chains or lay0["max_concurrent"]
     for i in range(1, B):
         s_i, c_i = make_system(rank * 1000 + i)
         b = engine.Box(s_i, c_i, device=dev, precision=GB_MIXED)
         b.mc_init(SEED + rank * 1000 + i, FRAC, ADJ, scales=SCALES,
-                  recompute_freq=10000, cluster_size=csize)
+                  recompute_freq=10000, cluster_size=csize, unit_lanes=lanes)
         boxes.append(b)
     st_batch = torch.cuda.ExternalStream(boxes[0].stream_ptr(), device=dev)
     bstep = [0]
@@ -463,8 +467,10 @@ def run_mixed(args, dev, rank, world, torch, engine, barrier, dist,
         "kernel_launches": timing["chain_launches"],
         "speedup_vs_fp64": batched / fp64_value,
         "ctas_per_chain": csize,
-        "autotune_us_per_move": tune_batch and {str(k): v for k, v in
-                                                tune_batch["us_per_move"].items()},
+        "unit_lanes": lanes,
+        "autotune_us_per_move": tune_batch and {
+            "%d x %d" % (t["ctas"], t["unit_lanes"]): round(t["us_per_move"], 2)
+            for t in tune_batch["tried"]},
         "clocks": clk.summary()}
     out["e2e"] = {"value": world * args.steps * M * B / t_e2e,
                   "unit": "moves/s",

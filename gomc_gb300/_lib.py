@@ -55,7 +55,14 @@ class McParams(C.Structure):
                 ("adj_steps", C.c_int32), ("use_scales", C.c_int32),
                 ("scales", C.c_double * 4), ("recompute_freq", C.c_int32),
                 ("cluster_size", C.c_int32), ("flush_every", C.c_int32),
-                ("move_buffer", C.c_int32)]
+                ("move_buffer", C.c_int32), ("unit_lanes", C.c_int32),
+                ("grid_ctas", C.c_int32), ("writer_kchunk", C.c_int32)]
+
+
+class McShape(C.Structure):
+    _fields_ = [("ctas", C.c_int32), ("unit_lanes", C.c_int32),
+                ("writer_kchunk", C.c_int32), ("max_concurrent", C.c_int32),
+                ("us_per_move", C.c_double)]
 
 
 class ServerConfig(C.Structure):
@@ -181,7 +188,9 @@ SIGNATURES = {
     "gb_mc_set_gomc_state": (C.c_int, [_P, C.POINTER(GomcChk)]),
     "gb_box_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "gb_mc_layout": (C.c_int, [_P, _I, _I, _L]),
-    "gb_mc_autotune": (C.c_int, [_P, C.c_int32, C.c_int32, _I, _D]),
+    "gb_mc_autotune": (C.c_int, [_P, C.c_int32, C.c_int32,
+                                 C.POINTER(McShape), C.POINTER(McShape),
+                                 C.c_int32, _I]),
     "gb_mc_drift": (C.c_int, [_P, _D, _D, _L]),
     "gb_recip_energy_noalloc": (C.c_int, [_P, _P, _P, C.c_int32, _P, _P]),
     "gb_gemc_create": (C.c_int, [C.POINTER(GemcDesc), C.POINTER(GemcConfig),

@@ -164,17 +164,17 @@ int gb_molecule_inter(gb_box *box, int32_t mol, const double *new_pos,
   return rc;
 }
 int gb_mc_autotune(gb_box *box, int32_t objective, int32_t trial_moves,
-                   int32_t *cluster_size, double *us_per_move4) {
+                   gb_mc_shape *chosen, gb_mc_shape *tried, int32_t cap,
+                   int32_t *n_tried) {
   int rc = guard(box);
   if (rc)
     return rc;
+  if (cap < 0 || (cap > 0 && !tried))
+    return box->b->Fail(gb::ERR_ARG, "tried must hold cap shapes");
   if ((rc = all_in_grid(*box->b)))
     return rc;
-  int c = 0;
-  rc = gb::mc_autotune(*box->b, objective, trial_moves, &c, us_per_move4);
-  if (!rc && cluster_size)
-    *cluster_size = c;
-  return rc;
+  return gb::mc_autotune(*box->b, objective, trial_moves, chosen, tried, cap,
+                         n_tried);
 }
 
 int gb_checkpoint_size(gb_box *box, int64_t *bytes) {

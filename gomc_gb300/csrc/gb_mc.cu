@@ -388,9 +388,10 @@ constexpr int NPAIR_CAP = 64; // (n_x, n_y) columns a CTA's k-chunk may span
                               // for the shared x-y phase products
 
 // CTAs of the chain grid without a k-chunk: the context writers 0 ..
-// nrows_max - 1 when they are at most half the grid, else none.
-__host__ __device__ inline int chain_kless(int nrows_max, int grid) {
-  return nrows_max > 0 && 2 * nrows_max <= grid ? nrows_max : 0;
+// nrows_max - 1 when they are at most half the grid, else none; none when
+// the writers are asked to hold k-vectors too (writer_k).
+inline int chain_kless(int nrows_max, int grid, bool writer_k) {
+  return !writer_k && nrows_max > 0 && 2 * nrows_max <= grid ? nrows_max : 0;
 }
 
 // doubles of one move context: the header and 2 MAX_MOL_ATOMS x 3 phase
@@ -420,6 +421,7 @@ struct ChainArgs {
   double *ctx;    // [2][ctx_len], by move parity: HDR + tables
   size_t ctx_len;
   int nrows_max;  // phase rows of the largest molecule (6 x its atoms)
+  int nkless;     // CTAs 0 .. nkless - 1 hold no k-vectors (context writers)
   int *tr_i;      // [n][3] or null
   double *tr_d;   // [n][3] or null
   // phase clocks (NULL: not collected): [0 CTA 0, 1 the leader][phase:
@@ -825,7 +827,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
   // context during phase A; they take no k-vectors, so that its FP64 chain
   // does not queue behind the k-vector warps' (the others' chunks grow by a
   // few lanes of the same warp passes).
-  const int nkb = chain_kless(A.nrows_max, G);
+  const int nkb = A.nkless;
   const int kG = G - nkb;
   int kc_max = (b.K + kG - 1) / kG;
   int kbeg = cta < nkb ? b.K : min(b.K, (cta - nkb) * kc_max);
@@ -1833,8 +1835,9 @@ void mc_destroy(Box &b) {
   b.mc = nullptr;
 }
 
-static size_t chain_smem(const Box &b, int grid, int nrows_max) {
-  const int kG = grid - chain_kless(nrows_max, grid);
+static size_t chain_smem(const Box &b, int grid, int nrows_max,
+                         bool writer_k) {
+  const int kG = grid - chain_kless(nrows_max, grid, writer_k);
   int kc_max = (b.dev.K + kG - 1) / kG;
   size_t own_per = ((size_t)b.dev.n_atoms + grid - 1) / grid;
   return sizeof(double) * ((5 * (size_t)kc_max + (kc_max + 1) / 2 + 1) & ~(size_t)1) +
@@ -1889,9 +1892,21 @@ int mc_init(Box &b, const gb_mc_params &p) {
                                         cudaMemcpyHostToDevice, b.stream),
                         "upload")))
     return rc;
-  // chain-kernel geometry: one CTA per SM (cooperative residency checked)
+  // chain-kernel geometry: at most one CTA per SM (cooperative residency
+  // checked), one CTA per SM unless asked for fewer; one CTA at least per
+  // phase row of the largest molecule (each writes one row of a context)
+  if (p.writer_kchunk != 0 && p.writer_kchunk != 1)
+    return b.Fail(ERR_ARG, "writer_kchunk must be 0 or 1");
+  if (p.grid_ctas < 0 || p.grid_ctas > b.sm_count)
+    return b.Fail(ERR_ARG, "grid_ctas must be 0 or 2 .. the SM count");
+  s.grid = p.grid_ctas ? p.grid_ctas : b.sm_count;
+  const int nrows_max = b.dev.K > 0 ? 6 * na_max : 0;
+  if (s.grid < 2 || s.grid < nrows_max)
+    return b.Fail(ERR_ARG,
+                  "the chain grid needs 2 CTAs and one per phase row of the "
+                  "largest molecule (6 x its atoms)");
   int per_sm = 0;
-  size_t sm = chain_smem(b, b.sm_count, b.dev.K > 0 ? 6 * na_max : 0);
+  size_t sm = chain_smem(b, s.grid, nrows_max, p.writer_kchunk != 0);
   raise_smem_limit((const void *)k_chain_fp64, sm);
   if ((rc = b.CudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                             &per_sm, k_chain_fp64, CT, sm),
@@ -1899,8 +1914,7 @@ int mc_init(Box &b, const gb_mc_params &p) {
     return rc;
   if (per_sm < 1)
     return b.Fail(ERR_UNSUPPORTED, "chain kernel does not fit on an SM");
-  s.grid = b.sm_count;
-  if (s.grid > PART_MAX_GRID || s.grid < 2)
+  if (s.grid > PART_MAX_GRID)
     return b.Fail(ERR_UNSUPPORTED, "the chain needs 2 to 256 SMs");
   if (p.move_buffer < 0)
     return b.Fail(ERR_ARG, "move_buffer must be >= 0");
@@ -1956,7 +1970,19 @@ int mc_init(Box &b, const gb_mc_params &p) {
     if (cold_global &&
         (rc = mc_alloc(b, s, &s.d_cold, mixed_cold_buffer(b.dev.K, s.cluster))))
       return rc;
-    s.flush_every = p.flush_every > 0 ? p.flush_every : 64;
+    // threads per real-space unit: as asked, else the smallest of 32, 64,
+    // 128 that covers a cell's mean occupancy in one pass, 128 above that
+    // (timed on SPC/E water at Rcut 9-10 A: 64 lanes at 56 atoms per cell,
+    // 128 at 94 and 111; 256 was slower at each)
+    int lanes = p.unit_lanes;
+    if (lanes == 0) {
+      const double cells = (double)b.dev.edge[0] * b.dev.edge[1] * b.dev.edge[2];
+      const double occ = cells > 0 ? b.dev.n_atoms / cells : 0.0;
+      lanes = occ <= 32 ? 32 : occ <= 64 ? 64 : 128;
+    }
+    if (lanes != 32 && lanes != 64 && lanes != 128 && lanes != 256)
+      return b.Fail(ERR_ARG, "unit_lanes must be 0, 32, 64, 128 or 256");
+    s.ulog = lanes == 32 ? 5 : lanes == 64 ? 6 : lanes == 128 ? 7 : 8;
     s.desc_cap = 256;
     if ((rc = mc_alloc(b, s, &s.d_desc, s.desc_cap)))
       return rc;
@@ -2177,12 +2203,13 @@ static int run_chain(Box &b, McState &s, const MoveRec *moves, int64_t first,
   A.ctx = s.d_ctx;
   A.ctx_len = chain_ctx_len(b.dev.kmax + 1);
   A.nrows_max = b.dev.K > 0 ? 6 * s.na_max : 0;
+  A.nkless = chain_kless(A.nrows_max, s.grid, s.params.writer_kchunk != 0);
   A.tr_i = tr_i;
   A.tr_d = tr_d;
   A.prof = s.profile ? s.d_prof : nullptr;
   A.spin = s.spin_limit;
   void *args[] = {&A};
-  size_t sm = chain_smem(b, s.grid, A.nrows_max);
+  size_t sm = chain_smem(b, s.grid, A.nrows_max, s.params.writer_kchunk != 0);
   // the per-launch counters of the decision protocol and the grid barrier
   // start from zero
   int rc = b.CudaCheck(cudaMemsetAsync(s.d_seq, 0,
@@ -2224,7 +2251,7 @@ static MixedChain fill_mixed(Box &b, McState &s, const MoveRec *moves,
   c.prop = s.d_prop;
   c.first = first;
   c.n = n;
-  c.flush_every = s.flush_every;
+  c.ulog = s.ulog;
   c.tr_i = tr_i;
   c.tr_d = tr_d;
   c.cold = s.d_cold;

@@ -80,7 +80,7 @@ struct McState {
   MixedChain *d_desc = nullptr;   // [desc_cap]
   MixedChain *h_desc = nullptr;   // pinned
   int desc_cap = 0, desc_next = 0;
-  int flush_every = 64;
+  int ulog = 7;  // log2 of the threads per real-space unit
   double drift_max[4] = {0, 0, 0, 0};  // inter, real, recip, total (relative)
   double drift_last[4] = {0, 0, 0, 0};
   int64_t recomputes = 0;
@@ -141,7 +141,7 @@ struct MixedChain {
   double *prop;
   int64_t first;
   int n;
-  int flush_every;
+  int ulog;  // log2 of the threads per real-space unit (5, 6 or 7)
   int *tr_i;
   double *tr_d;
   unsigned char *cold;  // cold per-k arrays in global memory (NULL: in smem)
@@ -185,9 +185,9 @@ void stream_state_at_next(McState &s, uint32_t st[624], int32_t *left,
                           int32_t *next);
 void mc_destroy(Box &b);
 
-// Timed choice of the mixed chain's cluster size (gb_tune.cu)
-int mc_autotune(Box &b, int objective, int trial_moves, int *chosen,
-                double *us_per_move4);
+// Timed choice of the chain's launch shape (gb_tune.cu)
+int mc_autotune(Box &b, int objective, int trial_moves, gb_mc_shape *chosen,
+                gb_mc_shape *tried, int cap, int *n_tried);
 
 // The reference's checkpoint file (gb_gomc_chk.cu)
 int gomc_chk_read(const void *buf, int64_t bytes, gb_gomc_chk *out);

@@ -418,7 +418,10 @@ __global__ void __launch_bounds__(MT_THREADS)
     // inside only before.  Differences use r'^2 - r^2 = delta . (d + d').
     float lj_h = 0.f, lj_l = 0.f, re_h = 0.f, re_l = 0.f, ovl = 0.f;
     const int units = na * 2 * NB27;
-    const int lane128 = threadIdx.x & 127, half = threadIdx.x >> 7;
+    // a unit's neighbour-cell slots are tiled over ul threads: slot lu,
+    // lu + ul, ... of unit usub of this CTA's upc units per pass
+    const int ul = 1 << C.ulog, upc = MT_THREADS >> C.ulog;
+    const int lu = threadIdx.x & (ul - 1), usub = threadIdx.x >> C.ulog;
     // the units' neighbour cells and slot counts, all at once
     __shared__ int mu_c2[2 * MAXA * NB27], mu_n2[2 * MAXA * NB27];
     for (int u = threadIdx.x; u < units; u += MT_THREADS) {
@@ -585,25 +588,25 @@ __global__ void __launch_bounds__(MT_THREADS)
         }
       }
     };
-    // This CTA takes units rank*2 + half, stepping 2 csize; a thread takes
-    // slot lane128 of its unit (and lane128 + 128, ... in fuller cells).
-    // The next unit's slot data are loaded while this one is evaluated.
-    const int ustep = 2 * csize;
+    // This CTA takes units rank upc + usub, stepping upc csize; a thread
+    // takes slot lu of its unit (and lu + ul, ... in fuller cells).  The
+    // next unit's slot data are loaded while this one is evaluated.
+    const int ustep = upc * csize;
     int pu = -1, pmj = 0;
     size_t ps = 0;
     uint4 pfix = make_uint4(0, 0, 0, 0);
     auto fetch = [&](int ub) {
-      int u = ub + half;
+      int u = ub + usub;
       pu = -1;
-      if (u < units && lane128 < mu_n2[u]) {
-        ps = (size_t)mu_c2[u] * b.cap + lane128;
+      if (u < units && lu < mu_n2[u]) {
+        ps = (size_t)mu_c2[u] * b.cap + lu;
         pmj = __ldcg(b.cell_meta + ps);
         pfix = __ldcg(b.cell_fix + ps);
         pu = u;
       }
     };
-    fetch(rank * 2);
-    for (int ub = rank * 2; ub < units; ub += ustep) {
+    fetch(rank * upc);
+    for (int ub = rank * upc; ub < units; ub += ustep) {
       const int u = pu, mj = pmj;
       const size_t s = ps;
       const uint4 f = pfix;
@@ -611,9 +614,9 @@ __global__ void __launch_bounds__(MT_THREADS)
         fetch(ub + ustep);
       if (u >= 0)
         pair(u, s, mj, f);
-      const int uu = ub + half;
+      const int uu = ub + usub;
       if (uu < units)
-        for (int j = lane128 + 128; j < mu_n2[uu]; j += 128) {
+        for (int j = lu + ul; j < mu_n2[uu]; j += ul) {
           size_t s2 = (size_t)mu_c2[uu] * b.cap + j;
           pair(uu, s2, __ldcg(b.cell_meta + s2), __ldcg(b.cell_fix + s2));
         }

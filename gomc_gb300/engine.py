@@ -71,9 +71,13 @@ def config_struct(cfg, precision: int, device: int):
 def mc_params(seed: int, move_frac: Sequence[float], adj_steps: int,
               scales: Optional[Sequence[float]] = None,
               recompute_freq: int = 0, cluster_size: int = 0,
-              flush_every: int = 0, move_buffer: int = 0):
+              flush_every: int = 0, move_buffer: int = 0,
+              unit_lanes: int = 0, grid_ctas: int = 0,
+              writer_kchunk: int = 0):
     """gb_mc_params (Random_Seed, DisFreq / RotFreq / MultiParticleFreq,
-    AdjSteps and the mixed form's settings)."""
+    AdjSteps and the launch shape: the mixed form's cluster size and
+    threads per real-space unit, the FP64 form's grid CTAs and whether its
+    context writers hold k-vectors)."""
     p = _lib.McParams()
     p.seed = int(seed) & 0xFFFFFFFF
     for i in range(3):
@@ -87,6 +91,9 @@ def mc_params(seed: int, move_frac: Sequence[float], adj_steps: int,
     p.cluster_size = int(cluster_size)
     p.flush_every = int(flush_every)
     p.move_buffer = int(move_buffer)
+    p.unit_lanes = int(unit_lanes)
+    p.grid_ctas = int(grid_ctas)
+    p.writer_kchunk = int(writer_kchunk)
     return p
 
 
@@ -396,9 +403,12 @@ class Box:
     def mc_init(self, seed: int, move_frac: Sequence[float], adj_steps: int,
                 scales: Optional[Sequence[float]] = None,
                 recompute_freq: int = 0, cluster_size: int = 0,
-                flush_every: int = 0, move_buffer: int = 0) -> None:
+                flush_every: int = 0, move_buffer: int = 0,
+                unit_lanes: int = 0, grid_ctas: int = 0,
+                writer_kchunk: int = 0) -> None:
         p = mc_params(seed, move_frac, adj_steps, scales, recompute_freq,
-                      cluster_size, flush_every, move_buffer)
+                      cluster_size, flush_every, move_buffer, unit_lanes,
+                      grid_ctas, writer_kchunk)
         self._chk(lib().gb_mc_init(self.h, C.byref(p)))
 
     def checkpoint(self) -> bytes:
@@ -490,16 +500,27 @@ class Box:
 
     def mc_autotune(self, objective: str = "latency",
                     trial_moves: int = 0) -> dict:
-        """Time each fitting cluster size on this machine's own state and keep
+        """Time each launch shape that fits on this machine's own state and keep
         the best ('latency': one chain; 'throughput': as many chains as the
-        GPU holds); the Monte Carlo state is unchanged."""
-        c = C.c_int32()
-        us = np.zeros(4)
+        GPU holds).  Mixed form: cluster size x threads per real-space unit;
+        FP64 form: grid CTAs x whether the context writers hold k-vectors.
+        The Monte Carlo state is unchanged.  Returns the chosen shape and
+        every shape tried with its trial microseconds per move (0: it does
+        not fit)."""
+        best = _lib.McShape()
+        tried = (_lib.McShape * 32)()
+        n = C.c_int32()
         self._chk(lib().gb_mc_autotune(
             self.h, 0 if objective == "latency" else 1, int(trial_moves),
-            C.byref(c), _dp(us)))
-        return dict(cluster_size=c.value,
-                    us_per_move={2: us[0], 4: us[1], 8: us[2], 16: us[3]})
+            C.byref(best), tried, 32, C.byref(n)))
+
+        def shape(s):
+            return dict(ctas=s.ctas, unit_lanes=s.unit_lanes,
+                        writer_kchunk=s.writer_kchunk,
+                        max_concurrent=s.max_concurrent,
+                        us_per_move=s.us_per_move)
+        return dict(chosen=shape(best),
+                    tried=[shape(tried[i]) for i in range(n.value)])
 
     def stream_ptr(self) -> int:
         p = C.c_void_p()

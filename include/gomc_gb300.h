@@ -245,11 +245,23 @@ typedef struct gb_mc_params {
   int32_t use_scales;     /* 1: start from scales[] instead of the defaults */
   double scales[4];       /* displacement, rotation, MP t_max, MP r_max */
   int32_t recompute_freq; /* GB300RecomputeFreq (mixed form), 0 = never */
-  int32_t cluster_size;   /* mixed form: CTAs per chain (0 = autotuned) */
+  int32_t cluster_size;   /* mixed form: CTAs per chain, 2, 4, 8 or 16
+                             (0 = the largest that fits) */
   int32_t flush_every;    /* not used (kept for layout): the mixed form's
                              structure factors are float-float and need no
                              periodic FP64 fold */
   int32_t move_buffer;    /* moves drawn and uploaded per chunk (0 = 65536) */
+  int32_t unit_lanes;     /* mixed form: threads per real-space unit (one
+                             atom's old or new position against one
+                             neighbour cell's slots): 32, 64, 128 or 256
+                             (0 = the smallest of 32, 64, 128 at least the
+                             mean atoms per cell, else 128) */
+  int32_t grid_ctas;      /* FP64 form: CTAs of the cooperative grid, 2 to
+                             the SM count (0 = one per SM) */
+  int32_t writer_kchunk;  /* FP64 form: 1 = the CTAs that write the next
+                             move's context also hold k-vectors (the
+                             k-chunk spreads over the whole grid); 0 = they
+                             hold none when they are at most half the grid */
 } gb_mc_params;
 
 int gb_mc_init(gb_box *box, const gb_mc_params *params);
@@ -302,18 +314,32 @@ int gb_mc_drift(gb_box *box, double *max4, double *last4, int64_t *recomputes);
  * counterpart. */
 int gb_mc_layout(gb_box *box, int32_t *ctas_per_chain, int32_t *max_concurrent,
                  int64_t *smem_bytes);
-/* Autotuner of the mixed form's chain geometry (no reference counterpart):
- * times a trial segment of `trial_moves` moves (0 = 200) for each cluster
- * size 2, 4, 8, 16 that fits the box -- it fixes the k-vectors per CTA and
- * the threads per molecule move -- on the box's own state, which is
- * checkpointed and restored around every trial, and keeps the best for the
- * objective: 0 = shortest move latency of one chain, 1 = most moves/s with
- * as many chains as the GPU holds at once.  The Monte Carlo state after the
- * call is the state before it; gb_mc_layout shows the choice.
- * us_per_move4 (may be NULL) receives each candidate's latency (0 where a
- * shape does not fit). */
+/* One launch shape of a chain and its trial time (gb_mc_autotune). */
+typedef struct gb_mc_shape {
+  int32_t ctas;           /* mixed form: cluster size; FP64 form: grid CTAs */
+  int32_t unit_lanes;     /* mixed form: threads per real-space unit */
+  int32_t writer_kchunk;  /* FP64 form: context writers hold k-vectors */
+  int32_t max_concurrent; /* chains of this shape the GPU holds at once */
+  double us_per_move;     /* trial latency (0: the shape does not fit) */
+} gb_mc_shape;
+/* Autotuner of the chain geometry (no reference counterpart).  Mixed form:
+ * the cluster size (2, 4, 8, 16: the k-chunk each CTA holds and the CTAs on
+ * one move) times the threads per real-space unit (32, 64, 128: how a
+ * neighbour cell's slots are tiled over threads).  FP64 form: the grid's
+ * CTAs (the SM count and 3/4, 1/2, 1/4 of it: the threads on one move and
+ * the k-chunk per CTA) times whether the context writers hold k-vectors
+ * (the k-chunk at a fixed grid).  Each shape that fits the box runs a trial
+ * segment of `trial_moves` moves (0 = 200) on the box's own state, which is
+ * checkpointed and restored around every trial; the best shape for the
+ * objective is kept: 0 = shortest move latency of one chain, 1 = most
+ * moves/s with as many chains as the GPU holds at once (mixed form; the
+ * FP64 form holds one chain).  The Monte Carlo state after the call is the
+ * state before it.  `chosen` (may be NULL) receives the kept shape; `tried`
+ * (may be NULL) up to `cap` shapes in the order tried, their number in
+ * *n_tried (may be NULL). */
 int gb_mc_autotune(gb_box *box, int32_t objective, int32_t trial_moves,
-                   int32_t *cluster_size, double *us_per_move4);
+                   gb_mc_shape *chosen, gb_mc_shape *tried, int32_t cap,
+                   int32_t *n_tried);
 /* The CUDA stream (cudaStream_t) every call on this machine is ordered on. */
 int gb_box_stream(gb_box *box, void **stream);
 

@@ -144,15 +144,18 @@ def test_batch_matches_alone(gb, frac):
 
 def test_autotune_keeps_state_and_matches_fixed_shape(gb):
     """The autotuner restores the state it found, and a box it tuned runs
-    exactly as a box initialised with the chosen cluster size."""
+    exactly as a box initialised with the chosen cluster size and threads
+    per real-space unit."""
     params = dict(scales=SCALES, recompute_freq=0)
     tuned = make(gb, 2000, 39.1, 10.0, gb.GB_MIXED, seed=31)
     tuned.mc_init(41, [0.5, 0.5, 0.0], 300, **params)
     tuned.mc_run(0, 300)
     before = (tuned.coords(), tuned.energy(), tuned.mc_state())
     res = tuned.mc_autotune("throughput", 120)
-    c = res["cluster_size"]
-    assert c in (2, 4, 8, 16) and res["us_per_move"][c] > 0
+    c, lanes = res["chosen"]["ctas"], res["chosen"]["unit_lanes"]
+    assert c in (2, 4, 8, 16) and lanes in (32, 64, 128, 256)
+    assert len(res["tried"]) == 16
+    assert res["chosen"]["us_per_move"] > 0
     assert tuned.mc_layout()["ctas_per_chain"] == c
     after = (tuned.coords(), tuned.energy(), tuned.mc_state())
     np.testing.assert_array_equal(before[0], after[0])
@@ -164,7 +167,8 @@ def test_autotune_keeps_state_and_matches_fixed_shape(gb):
     fixed.mc_init(41, [0.5, 0.5, 0.0], 300, **params)
     fixed.mc_run(0, 300)
     blob = fixed.checkpoint()
-    fixed.mc_init(41, [0.5, 0.5, 0.0], 300, cluster_size=c, **params)
+    fixed.mc_init(41, [0.5, 0.5, 0.0], 300, cluster_size=c, unit_lanes=lanes,
+                  **params)
     fixed.restore(blob)
     tuned.mc_run(300, 400)
     fixed.mc_run(300, 400)

@@ -1,0 +1,138 @@
+"""Every launch shape the autotuner can choose runs the same Markov chain.
+
+FP64 form: the cooperative grid at fewer CTAs than SMs, and with or without
+k-vectors on the CTAs that write the next move's context -- the same
+decisions as the reference's own trace of the seeded run, every move's
+energy change within 1e-10.  Mixed form: every cluster size x threads per
+real-space unit takes the reference's decisions, with running energies
+within 1e-6 of a full FP64 recompute.  The autotuner leaves the state as it
+found it, and the shape it keeps continues the chain exactly as a box
+initialised with that shape.
+"""
+import numpy as np
+import pytest
+
+from tests.golden_util import config_of, load, move_fractions, system_of
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-10
+
+
+@pytest.fixture(scope="module")
+def gb():
+    from gomc_gb300 import engine
+    engine.lib(build_if_missing=True)
+    return engine
+
+
+def sm_count(gb, z, meta):
+    box = gb.Box(system_of(z, meta), config_of(meta))
+    box.mc_init(1, move_fractions(meta), meta["config"]["adj_steps"])
+    n = box.mc_layout()["ctas_per_chain"]
+    box.close()
+    return n
+
+
+def check_trace(r, z, rel):
+    tr = z["trace"]
+    np.testing.assert_array_equal(r["kind"], tr[:, 1].astype(int))
+    np.testing.assert_array_equal(r["mol"], tr[:, 2].astype(int))
+    np.testing.assert_array_equal(r["accepted"], tr[:, 3].astype(int))
+    scale = np.maximum(np.abs(tr[-1, 8:11]), 1.0)
+    for j in range(3):
+        bound = rel * np.maximum(scale[j], np.abs(tr[:, 5 + j]))
+        err = np.abs(r["de"][:, j] - tr[:, 5 + j])
+        assert (err <= bound).all(), (j, err.max())
+
+
+@pytest.mark.parametrize("name", ["c0_water", "w1728", "c1_water"])
+@pytest.mark.parametrize("quarters,writer_k", [(4, 1), (3, 0), (2, 0), (2, 1),
+                                               (1, 0)])
+def test_fp64_grid_shapes_match_reference(gb, name, quarters, writer_k):
+    z, meta = load(name)
+    grid = sm_count(gb, z, meta) * quarters // 4
+    box = gb.Box(system_of(z, meta), config_of(meta))
+    box.mc_init(meta["config"]["random_seed"], move_fractions(meta),
+                meta["config"]["adj_steps"], grid_ctas=grid,
+                writer_kchunk=writer_k)
+    assert box.mc_layout()["ctas_per_chain"] == grid
+    r = box.mc_run(0, z["trace"].shape[0], trace=True)
+    check_trace(r, z, REL)
+    np.testing.assert_allclose(box.coords(), z["coords_final"], rtol=0,
+                               atol=1e-9)
+    box.close()
+
+
+def test_fp64_grid_rejects_too_few_ctas(gb):
+    from gomc_gb300._lib import GbError
+    z, meta = load("c0_water")
+    box = gb.Box(system_of(z, meta), config_of(meta))
+    # one CTA per phase row of a water (6 x 3 atoms) at least
+    with pytest.raises(GbError):
+        box.mc_init(1, move_fractions(meta), meta["config"]["adj_steps"],
+                    grid_ctas=12)
+    with pytest.raises(GbError):
+        box.mc_init(1, move_fractions(meta), meta["config"]["adj_steps"],
+                    writer_kchunk=2)
+    box.close()
+
+
+@pytest.mark.parametrize("lanes", [32, 64, 128, 256])
+@pytest.mark.parametrize("cluster", [2, 4, 8, 16])
+def test_mixed_unit_lanes_take_reference_decisions(gb, cluster, lanes):
+    z, meta = load("w1728")
+    box = gb.Box(system_of(z, meta), config_of(meta), precision=gb.GB_MIXED)
+    box.mc_init(meta["config"]["random_seed"], move_fractions(meta),
+                meta["config"]["adj_steps"], cluster_size=cluster,
+                unit_lanes=lanes)
+    assert box.mc_layout()["ctas_per_chain"] == cluster
+    tr = z["trace"]
+    r = box.mc_run(0, tr.shape[0], trace=True)
+    np.testing.assert_array_equal(r["accepted"], tr[:, 3].astype(int))
+    run = box.energy()
+    st = box.system_total()
+    for i, term in enumerate(("inter", "real", "recip")):
+        assert abs(run[i] - st[term]) <= 1e-6 * abs(st[term]), term
+    box.close()
+
+
+def test_fp64_autotune_keeps_state_and_matches_fixed_shape(gb):
+    z, meta = load("w1728")
+    seed, frac = meta["config"]["random_seed"], move_fractions(meta)
+    adj = meta["config"]["adj_steps"]
+    tuned = gb.Box(system_of(z, meta), config_of(meta))
+    tuned.mc_init(seed, frac, adj)
+    tuned.mc_run(0, 300)
+    before = (tuned.coords(), tuned.energy(), tuned.mc_state())
+    res = tuned.mc_autotune("latency", 100)
+    tried = res["tried"]
+    assert len(tried) == 8
+    assert all(t["us_per_move"] > 0 for t in tried)
+    best = res["chosen"]
+    assert best["us_per_move"] == min(t["us_per_move"] for t in tried)
+    assert tuned.mc_layout()["ctas_per_chain"] == best["ctas"]
+    after = (tuned.coords(), tuned.energy(), tuned.mc_state())
+    np.testing.assert_array_equal(before[0], after[0])
+    np.testing.assert_array_equal(before[1], after[1])
+    for x, y in zip(before[2], after[2]):
+        np.testing.assert_array_equal(x, y)
+    fixed = gb.Box(system_of(z, meta), config_of(meta))
+    fixed.mc_init(seed, frac, adj)
+    fixed.mc_run(0, 300)
+    blob = fixed.checkpoint()
+    fixed.mc_init(seed, frac, adj, grid_ctas=best["ctas"],
+                  writer_kchunk=best["writer_kchunk"])
+    fixed.restore(blob)
+    n = z["trace"].shape[0] - 300
+    a = tuned.mc_run(300, n, trace=True)
+    b = fixed.mc_run(300, n, trace=True)
+    np.testing.assert_array_equal(a["accepted"], b["accepted"])
+    np.testing.assert_array_equal(a["de"], b["de"])
+    np.testing.assert_array_equal(tuned.coords(), fixed.coords())
+    np.testing.assert_array_equal(tuned.energy(), fixed.energy())
+    # and the reference's decisions over the whole run
+    np.testing.assert_array_equal(a["accepted"],
+                                  z["trace"][300:, 3].astype(int))
+    tuned.close()
+    fixed.close()
