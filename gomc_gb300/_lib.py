@@ -56,12 +56,14 @@ class McParams(C.Structure):
                 ("scales", C.c_double * 4), ("recompute_freq", C.c_int32),
                 ("cluster_size", C.c_int32), ("flush_every", C.c_int32),
                 ("move_buffer", C.c_int32), ("unit_lanes", C.c_int32),
-                ("grid_ctas", C.c_int32), ("writer_kchunk", C.c_int32)]
+                ("grid_ctas", C.c_int32), ("writer_kchunk", C.c_int32),
+                ("moves_in_flight", C.c_int32)]
 
 
 class McShape(C.Structure):
     _fields_ = [("ctas", C.c_int32), ("unit_lanes", C.c_int32),
-                ("writer_kchunk", C.c_int32), ("max_concurrent", C.c_int32),
+                ("writer_kchunk", C.c_int32), ("moves_in_flight", C.c_int32),
+                ("max_concurrent", C.c_int32),
                 ("us_per_move", C.c_double)]
 
 

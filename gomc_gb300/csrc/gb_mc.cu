@@ -364,8 +364,11 @@ __device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
 }
 __device__ __forceinline__ double2 tab_at(const double2 *row, int n) {
   double2 v = row[n < 0 ? -n : n];
-  if (n < 0)
-    v.y = -v.y;
+  // exp(-i x) = conj(exp(i x)): the sign bit of the imaginary part flipped
+  // by an integer operation (the same value as a negation)
+  v.y = __longlong_as_double(
+      (long long)((unsigned long long)__double_as_longlong(v.y) ^
+                  ((unsigned long long)(n < 0) << 63)));
   return v;
 }
 
@@ -418,10 +421,14 @@ struct ChainArgs {
   unsigned *seq;  // [0] decision published (2 (t + 1) + accept); from
                   // SEQ_CTX: per CTA, its part of the context of move t
                   // written (t)
-  double *ctx;    // [2][ctx_len], by move parity: HDR + tables
+  double *ctx;    // [nctx][ctx_len], by move modulo nctx: HDR + tables
   size_t ctx_len;
+  int nctx;       // context buffers: 2 (one move in flight) or 3 (two)
   int nrows_max;  // phase rows of the largest molecule (6 x its atoms)
   int nkless;     // CTAs 0 .. nkless - 1 hold no k-vectors (context writers)
+  // permutation of the atom index for the pipelined chain's atom ownership
+  // (p = a * perm_m mod n_atoms, a = p * perm_minv mod n_atoms)
+  unsigned long long perm_m, perm_minv;
   int *tr_i;      // [n][3] or null
   double *tr_d;   // [n][3] or null
   // phase clocks (NULL: not collected): [0 CTA 0, 1 the leader][phase:
@@ -442,7 +449,7 @@ struct ChainShared {
   int ovl_any;
   double tot[4];
   int accept, flag, ok, bok;
-  unsigned gen;
+  unsigned gen, word;
   // the last decided move: its molecule, outcome and new positions and
   // centre (the leader writes them to global memory after it publishes)
   int last_m, last_acc;
@@ -512,7 +519,7 @@ __device__ void build_ctx_rest(const ChainArgs &A, ChainShared &S, int t,
                               : S.b_com[d];
   }
   group_sync(count);
-  double *const ctx = A.ctx + (size_t)(t & 1) * A.ctx_len;
+  double *const ctx = A.ctx + (size_t)(t % A.nctx) * A.ctx_len;
   if (blockIdx.x == 0) {
     double *h = ctx;
     if (tid == 64) {
@@ -598,7 +605,7 @@ __device__ void build_ctx_warp(const ChainArgs &A, ChainShared &S, int t) {
                               : S.b_com[d];
   }
   __syncwarp();
-  double *const ctx = A.ctx + (size_t)(t & 1) * A.ctx_len;
+  double *const ctx = A.ctx + (size_t)(t % A.nctx) * A.ctx_len;
   if (blockIdx.x == 0) {
     double *h = ctx;
     if (lane == 0) {
@@ -972,7 +979,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     }
     // ---------------- phase A ----------------
     // the header and the rows of the largest molecule in one round trip
-    const double *ctx_t = A.ctx + (size_t)(t & 1) * A.ctx_len;
+    const double *ctx_t = A.ctx + (size_t)(t % A.nctx) * A.ctx_len;
     for (int i = threadIdx.x; i < HDR; i += CT)
       S.hdr[i] = __ldcg(ctx_t + i);
     for (int i = threadIdx.x; i < A.nrows_max * stride; i += CT)
@@ -1516,6 +1523,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
   }
 }
 
+#include "gb_chain_pipe.cuh"
+
 // ===========================================================================
 // MultiParticle kernels (src/moves/MultiParticle.h)
 // ===========================================================================
@@ -1835,13 +1844,57 @@ void mc_destroy(Box &b) {
   b.mc = nullptr;
 }
 
+// A multiplier near 0.618 n coprime with n and its inverse modulo n: the
+// permutation a -> a m mod n spreads runs of nearby indices over the range
+// (multiplicative hashing with the golden ratio).
+static void chain_perm(int n, unsigned long long *m, unsigned long long *minv) {
+  if (n <= 2) {
+    *m = *minv = 1;
+    return;
+  }
+  long long c = (long long)(0.6180339887498949 * n);
+  auto gcd = [](long long x, long long y) {
+    while (y) {
+      long long r = x % y;
+      x = y;
+      y = r;
+    }
+    return x;
+  };
+  while (gcd(c, n) != 1)
+    ++c;
+  // extended Euclid: c * u = 1 mod n
+  long long r0 = n, r1 = c % n, u0 = 0, u1 = 1;
+  while (r1) {
+    long long q = r0 / r1, t = r0 - q * r1;
+    r0 = r1;
+    r1 = t;
+    t = u0 - q * u1;
+    u0 = u1;
+    u1 = t;
+  }
+  if (u0 < 0)
+    u0 += n;
+  *m = (unsigned long long)(c % n);
+  *minv = (unsigned long long)u0;
+}
+
 static size_t chain_smem(const Box &b, int grid, int nrows_max,
-                         bool writer_k) {
-  const int kG = grid - chain_kless(nrows_max, grid, writer_k);
+                         bool writer_k, bool pipe) {
+  // the pipelined chain spreads atoms and k-vectors over all CTAs but the
+  // deciding one, and holds four k-chunk buffers instead of two
+  const int work = pipe ? grid - 1 : grid;
+  const int kG = work - chain_kless(nrows_max, work, writer_k);
   int kc_max = (b.dev.K + kG - 1) / kG;
-  size_t own_per = ((size_t)b.dev.n_atoms + grid - 1) / grid;
-  return sizeof(double) * ((5 * (size_t)kc_max + (kc_max + 1) / 2 + 1) & ~(size_t)1) +
-         sizeof(double2) * (size_t)(2 * MAX_MOL_ATOMS * 3) * (b.dev.kmax + 1) +
+  // (the pipelined chain's atoms are owned by the CTAs with a k-chunk)
+  const int owners = pipe ? kG : grid;
+  size_t own_per = ((size_t)b.dev.n_atoms + owners - 1) / owners;
+  const size_t kvec =
+      pipe ? chain_pipe_kvec_doubles(kc_max)
+           : ((5 * (size_t)kc_max + (kc_max + 1) / 2 + 1) & ~(size_t)1);
+  return sizeof(double) * kvec +
+         (pipe ? 2 : 1) * sizeof(double2) * (size_t)(2 * MAX_MOL_ATOMS * 3) *
+             (b.dev.kmax + 1) +
          sizeof(double2) * (size_t)NPAIR_CAP * 2 * MAX_MOL_ATOMS +
          sizeof(unsigned short) * (size_t)kc_max + 64 +
          own_per * (2 * sizeof(double2) + sizeof(uint4));
@@ -1897,19 +1950,31 @@ int mc_init(Box &b, const gb_mc_params &p) {
   // phase row of the largest molecule (each writes one row of a context)
   if (p.writer_kchunk != 0 && p.writer_kchunk != 1)
     return b.Fail(ERR_ARG, "writer_kchunk must be 0 or 1");
+  if (p.moves_in_flight < 0 || p.moves_in_flight > 2)
+    return b.Fail(ERR_ARG, "moves_in_flight must be 0, 1 or 2");
+  // two moves in flight unless asked for one or the grid leaves no CTA to
+  // decide (the writers' rows and the deciding CTA need nrows + 1 CTAs)
+  s.pipe = p.moves_in_flight == 2 ||
+           (p.moves_in_flight == 0 &&
+            (p.grid_ctas ? p.grid_ctas : b.sm_count) >=
+                std::max(3, (b.dev.K > 0 ? 6 * na_max : 0) + 1));
   if (p.grid_ctas < 0 || p.grid_ctas > b.sm_count)
     return b.Fail(ERR_ARG, "grid_ctas must be 0 or 2 .. the SM count");
   s.grid = p.grid_ctas ? p.grid_ctas : b.sm_count;
   const int nrows_max = b.dev.K > 0 ? 6 * na_max : 0;
-  if (s.grid < 2 || s.grid < nrows_max)
+  // (and, with two moves in flight, one more CTA that only decides)
+  if (s.grid < 3 || s.grid < nrows_max + (s.pipe ? 1 : 0))
     return b.Fail(ERR_ARG,
-                  "the chain grid needs 2 CTAs and one per phase row of the "
-                  "largest molecule (6 x its atoms)");
+                  "the chain grid needs 3 CTAs and one per phase row of the "
+                  "largest molecule (6 x its atoms), plus the deciding CTA "
+                  "with two moves in flight");
   int per_sm = 0;
-  size_t sm = chain_smem(b, s.grid, nrows_max, p.writer_kchunk != 0);
-  raise_smem_limit((const void *)k_chain_fp64, sm);
+  const void *kfn = s.pipe ? (const void *)k_chain_fp64_pipe
+                           : (const void *)k_chain_fp64;
+  size_t sm = chain_smem(b, s.grid, nrows_max, p.writer_kchunk != 0, s.pipe);
+  raise_smem_limit(kfn, sm);
   if ((rc = b.CudaCheck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                            &per_sm, k_chain_fp64, CT, sm),
+                            &per_sm, kfn, CT, sm),
                         "occupancy")))
     return rc;
   if (per_sm < 1)
@@ -1922,10 +1987,10 @@ int mc_init(Box &b, const gb_mc_params &p) {
   int stride = b.dev.kmax + 1;
   if ((rc = mc_alloc(b, s, &s.d_moves, s.move_cap)) ||
       (rc = mc_alloc(b, s, &s.d_prop, s.move_cap * 12)) ||
-      (rc = mc_alloc(b, s, &s.d_part, 2 * (size_t)s.grid * 4)) ||
+      (rc = mc_alloc(b, s, &s.d_part, 3 * (size_t)s.grid * 8)) ||
       (rc = mc_alloc(b, s, &s.d_bar, 8)) ||
       (rc = mc_alloc(b, s, &s.d_seq, SEQ_CTX + PART_MAX_GRID)) ||
-      (rc = mc_alloc(b, s, &s.d_ctx, 2 * chain_ctx_len(stride))) ||
+      (rc = mc_alloc(b, s, &s.d_ctx, 3 * chain_ctx_len(stride))) ||
       (rc = mc_alloc(b, s, &s.d_mp, 16)))
     return rc;
   if ((rc = b.CudaCheck(cudaMallocHost(&s.h_moves, s.move_cap * sizeof(MoveRec)),
@@ -2203,13 +2268,17 @@ static int run_chain(Box &b, McState &s, const MoveRec *moves, int64_t first,
   A.ctx = s.d_ctx;
   A.ctx_len = chain_ctx_len(b.dev.kmax + 1);
   A.nrows_max = b.dev.K > 0 ? 6 * s.na_max : 0;
-  A.nkless = chain_kless(A.nrows_max, s.grid, s.params.writer_kchunk != 0);
+  A.nkless = chain_kless(A.nrows_max, s.pipe ? s.grid - 1 : s.grid,
+                         s.params.writer_kchunk != 0);
+  A.nctx = s.pipe ? 3 : 2;
+  chain_perm(b.dev.n_atoms, &A.perm_m, &A.perm_minv);
   A.tr_i = tr_i;
   A.tr_d = tr_d;
   A.prof = s.profile ? s.d_prof : nullptr;
   A.spin = s.spin_limit;
   void *args[] = {&A};
-  size_t sm = chain_smem(b, s.grid, A.nrows_max, s.params.writer_kchunk != 0);
+  size_t sm = chain_smem(b, s.grid, A.nrows_max, s.params.writer_kchunk != 0,
+                         s.pipe);
   // the per-launch counters of the decision protocol and the grid barrier
   // start from zero
   int rc = b.CudaCheck(cudaMemsetAsync(s.d_seq, 0,
@@ -2223,14 +2292,14 @@ static int run_chain(Box &b, McState &s, const MoveRec *moves, int64_t first,
                      "memset");
   if (rc)
     return rc;
-  k_fill_u64<<<(2 * s.grid * 4 + 255) / 256, 256, 0, b.stream>>>(
-      (unsigned long long *)s.d_part, 2 * s.grid * 4, PART_EMPTY);
+  k_fill_u64<<<(3 * s.grid * 8 + 255) / 256, 256, 0, b.stream>>>(
+      (unsigned long long *)s.d_part, 3 * s.grid * 8, PART_EMPTY);
   auto ev = ev_pair();
   cudaEventRecord(ev.first, b.stream);
-  rc = b.CudaCheck(cudaLaunchCooperativeKernel((void *)k_chain_fp64,
-                                                   dim3(s.grid), dim3(CT), args,
-                                                   sm, b.stream),
-                       "chain kernel");
+  rc = b.CudaCheck(cudaLaunchCooperativeKernel(
+                       s.pipe ? (void *)k_chain_fp64_pipe : (void *)k_chain_fp64,
+                       dim3(s.grid), dim3(CT), args, sm, b.stream),
+                   "chain kernel");
   // the chain keeps positions, not cell slots: CellList::GridAll of the new
   // coordinates brings the grid up to date
   if (!rc)

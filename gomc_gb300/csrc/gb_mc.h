@@ -107,6 +107,7 @@ struct McState {
   unsigned *d_bar = nullptr; // grid barrier words
   double *d_ctx = nullptr;   // per-move context (positions, tables)
   int grid = 0, kchunk = 0;
+  bool pipe = false;  // FP64 chain: two moves in flight (k_chain_fp64_pipe)
   // MultiParticle buffers (new state)
   double *d_xn = nullptr, *d_yn = nullptr, *d_zn = nullptr;
   double *d_cxn = nullptr, *d_cyn = nullptr, *d_czn = nullptr;

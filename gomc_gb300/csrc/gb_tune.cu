@@ -4,7 +4,8 @@
 // real-space unit (an atom position against a neighbour cell's slots).
 // FP64 form: the CTAs of the cooperative grid (the threads on one move and
 // the k-chunk per CTA) times whether the CTAs that write the next move's
-// context also hold k-vectors (the k-chunk at a fixed grid).  Each candidate
+// context also hold k-vectors (the k-chunk at a fixed grid) times one or
+// two moves in flight.  Each candidate
 // is timed on the box's own system: the box's state is checkpointed, the
 // candidate runs a short trial segment, the state is restored; the best
 // candidate is kept.  No counterpart in the reference (its GPU kernels use
@@ -40,7 +41,7 @@ int mc_autotune(Box &b, int objective, int trial_moves, gb_mc_shape *chosen,
   if (mixed) {
     for (int c : {2, 4, 8, 16})
       for (int lanes : {32, 64, 128, 256})
-        cands.push_back({c, lanes, 0, 0, 0.0});
+        cands.push_back({c, lanes, 0, 0, 0, 0.0});
   } else {
     const int sms = b.sm_count;
     int prev = 0;
@@ -50,7 +51,8 @@ int mc_autotune(Box &b, int objective, int trial_moves, gb_mc_shape *chosen,
         continue;
       prev = g;
       for (int wk : {0, 1})
-        cands.push_back({g, 0, wk, 1, 0.0});
+        for (int fl : {1, 2})
+          cands.push_back({g, 0, wk, fl, 1, 0.0});
     }
   }
   double best = -1.0;
@@ -65,6 +67,7 @@ int mc_autotune(Box &b, int objective, int trial_moves, gb_mc_shape *chosen,
     } else {
       q.grid_ctas = cs.ctas;
       q.writer_kchunk = cs.writer_kchunk;
+      q.moves_in_flight = cs.moves_in_flight;
     }
     if (mc_init(b, q) == OK) {
       if ((rc = checkpoint_load(b, saved.data(), bytes)))
@@ -108,6 +111,7 @@ int mc_autotune(Box &b, int objective, int trial_moves, gb_mc_shape *chosen,
   } else {
     q.grid_ctas = best_s.ctas;
     q.writer_kchunk = best_s.writer_kchunk;
+    q.moves_in_flight = best_s.moves_in_flight;
   }
   if ((rc = mc_init(b, q)) || (rc = checkpoint_load(b, saved.data(), bytes)))
     return rc;

@@ -73,11 +73,11 @@ def mc_params(seed: int, move_frac: Sequence[float], adj_steps: int,
               recompute_freq: int = 0, cluster_size: int = 0,
               flush_every: int = 0, move_buffer: int = 0,
               unit_lanes: int = 0, grid_ctas: int = 0,
-              writer_kchunk: int = 0):
+              writer_kchunk: int = 0, moves_in_flight: int = 0):
     """gb_mc_params (Random_Seed, DisFreq / RotFreq / MultiParticleFreq,
     AdjSteps and the launch shape: the mixed form's cluster size and
     threads per real-space unit, the FP64 form's grid CTAs and whether its
-    context writers hold k-vectors)."""
+    context writers hold k-vectors and its moves in flight)."""
     p = _lib.McParams()
     p.seed = int(seed) & 0xFFFFFFFF
     for i in range(3):
@@ -94,6 +94,7 @@ def mc_params(seed: int, move_frac: Sequence[float], adj_steps: int,
     p.unit_lanes = int(unit_lanes)
     p.grid_ctas = int(grid_ctas)
     p.writer_kchunk = int(writer_kchunk)
+    p.moves_in_flight = int(moves_in_flight)
     return p
 
 
@@ -405,10 +406,10 @@ class Box:
                 recompute_freq: int = 0, cluster_size: int = 0,
                 flush_every: int = 0, move_buffer: int = 0,
                 unit_lanes: int = 0, grid_ctas: int = 0,
-                writer_kchunk: int = 0) -> None:
+                writer_kchunk: int = 0, moves_in_flight: int = 0) -> None:
         p = mc_params(seed, move_frac, adj_steps, scales, recompute_freq,
                       cluster_size, flush_every, move_buffer, unit_lanes,
-                      grid_ctas, writer_kchunk)
+                      grid_ctas, writer_kchunk, moves_in_flight)
         self._chk(lib().gb_mc_init(self.h, C.byref(p)))
 
     def checkpoint(self) -> bytes:
@@ -503,7 +504,8 @@ class Box:
         """Time each launch shape that fits on this machine's own state and keep
         the best ('latency': one chain; 'throughput': as many chains as the
         GPU holds).  Mixed form: cluster size x threads per real-space unit;
-        FP64 form: grid CTAs x whether the context writers hold k-vectors.
+        FP64 form: grid CTAs x whether the context writers hold k-vectors x
+        one or two moves in flight.
         The Monte Carlo state is unchanged.  Returns the chosen shape and
         every shape tried with its trial microseconds per move (0: it does
         not fit)."""
@@ -517,6 +519,7 @@ class Box:
         def shape(s):
             return dict(ctas=s.ctas, unit_lanes=s.unit_lanes,
                         writer_kchunk=s.writer_kchunk,
+                        moves_in_flight=s.moves_in_flight,
                         max_concurrent=s.max_concurrent,
                         us_per_move=s.us_per_move)
         return dict(chosen=shape(best),

@@ -262,6 +262,11 @@ typedef struct gb_mc_params {
                              move's context also hold k-vectors (the
                              k-chunk spreads over the whole grid); 0 = they
                              hold none when they are at most half the grid */
+  int32_t moves_in_flight; /* FP64 form: 2 = the next move runs while this
+                              one is decided, on both of its outcomes, and
+                              one CTA of the grid only decides; 1 = one move
+                              at a time (0 = 2 where the grid has a CTA to
+                              spare for deciding, else 1) */
 } gb_mc_params;
 
 int gb_mc_init(gb_box *box, const gb_mc_params *params);
@@ -290,14 +295,18 @@ int gb_mc_timing(gb_box *box, int32_t reset, double *chain_ms,
  * reference has no device-side waits). */
 int gb_mc_set_wait_limit(gb_box *box, int64_t polls);
 /* Where the device time of the FP64 chain goes (no reference counterpart):
- * the clocks of CTA 0 and of the deciding CTA (the last) since the last
- * call, per phase of a move (loading the move's context, listing the
+ * the clocks of a work CTA and of the deciding CTA (the last) since the
+ * last call, per phase of a move (loading the move's context, listing the
  * real-space pairs, pair terms and k-vectors to the partials, waiting for
- * the decision, commit and the next context), as us13[0..9] (CTA 0's five,
- * then the last CTA's five) in microseconds at the rated SM clock; us13[10]
- * and [11]: when, counted from the end of its own phase A, the last CTA had
- * every partial and every flag of the next context, and us13[12] when CTA 0
- * had written its part of the next context; and the moves each CTA timed.
+ * the decision, commit and the next context), as us13[0..9] (the work
+ * CTA's five, then the last CTA's five) in microseconds at the rated SM
+ * clock.  The work CTA is CTA 0 with one move in flight and the first CTA
+ * with a k-chunk with two (the deciding CTA then only waits for the
+ * partials, decides and commits: its listing phase is zero).  With one
+ * move in flight us13[10] and [11]: when, counted from the end of its own
+ * phase A, the last CTA had every partial and every flag of the next
+ * context, and us13[12] when CTA 0 had written its part of the next
+ * context (zero with two moves in flight); and the moves each CTA timed.
  * `enable` switches the collection on or off for the following runs.  The
  * mixed form is not timed here. */
 int gb_mc_profile(gb_box *box, int32_t enable, double *us13, int64_t *moves2);
@@ -319,6 +328,7 @@ typedef struct gb_mc_shape {
   int32_t ctas;           /* mixed form: cluster size; FP64 form: grid CTAs */
   int32_t unit_lanes;     /* mixed form: threads per real-space unit */
   int32_t writer_kchunk;  /* FP64 form: context writers hold k-vectors */
+  int32_t moves_in_flight;/* FP64 form: 1 or 2 */
   int32_t max_concurrent; /* chains of this shape the GPU holds at once */
   double us_per_move;     /* trial latency (0: the shape does not fit) */
 } gb_mc_shape;
@@ -328,7 +338,7 @@ typedef struct gb_mc_shape {
  * neighbour cell's slots are tiled over threads).  FP64 form: the grid's
  * CTAs (the SM count and 3/4, 1/2, 1/4 of it: the threads on one move and
  * the k-chunk per CTA) times whether the context writers hold k-vectors
- * (the k-chunk at a fixed grid).  Each shape that fits the box runs a trial
+ * (the k-chunk at a fixed grid) times one or two moves in flight.  Each shape that fits the box runs a trial
  * segment of `trial_moves` moves (0 = 200) on the box's own state, which is
  * checkpointed and restored around every trial; the best shape for the
  * objective is kept: 0 = shortest move latency of one chain, 1 = most

@@ -12,7 +12,8 @@ initialised with that shape.
 import numpy as np
 import pytest
 
-from tests.golden_util import config_of, load, move_fractions, system_of
+from tests.golden_util import (NAMES, config_of, load, move_fractions,
+                               system_of)
 
 pytestmark = pytest.mark.gpu
 
@@ -55,12 +56,61 @@ def test_fp64_grid_shapes_match_reference(gb, name, quarters, writer_k):
     box = gb.Box(system_of(z, meta), config_of(meta))
     box.mc_init(meta["config"]["random_seed"], move_fractions(meta),
                 meta["config"]["adj_steps"], grid_ctas=grid,
-                writer_kchunk=writer_k)
+                writer_kchunk=writer_k, moves_in_flight=1)
     assert box.mc_layout()["ctas_per_chain"] == grid
     r = box.mc_run(0, z["trace"].shape[0], trace=True)
     check_trace(r, z, REL)
     np.testing.assert_allclose(box.coords(), z["coords_final"], rtol=0,
                                atol=1e-9)
+    box.close()
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("flight", [1, 2])
+def test_fp64_moves_in_flight_match_reference(gb, name, flight):
+    """The chain that decides each move before the next one starts, and the
+    chain that runs each move while the previous one is decided, both take
+    the reference's decisions, every energy change within 1e-10."""
+    z, meta = load(name)
+    box = gb.Box(system_of(z, meta), config_of(meta))
+    box.mc_init(meta["config"]["random_seed"], move_fractions(meta),
+                meta["config"]["adj_steps"], moves_in_flight=flight)
+    r = box.mc_run(0, z["trace"].shape[0], trace=True)
+    tr = z["trace"]
+    np.testing.assert_array_equal(r["kind"], tr[:, 1].astype(int))
+    np.testing.assert_array_equal(r["mol"], tr[:, 2].astype(int))
+    np.testing.assert_array_equal(r["accepted"], tr[:, 3].astype(int))
+    scale = np.maximum(np.abs(tr[-1, 8:11]), 1.0)
+    single = tr[:, 1] < 2
+    for j in range(3):
+        ref = tr[single, 5 + j]
+        bound = REL * np.maximum(scale[j], np.abs(ref))
+        err = np.abs(r["de"][single, j] - ref)
+        assert (err <= bound).all(), (j, err.max())
+    e = box.energy()
+    for j in range(3):
+        assert abs(e[j] - tr[-1, 8 + j]) <= REL * max(scale[j], 1.0)
+    np.testing.assert_allclose(box.coords(), z["coords_final"], rtol=0,
+                               atol=1e-9)
+    # and a fresh recompute agrees with the running totals
+    st = box.system_total()
+    for j, term in enumerate(("inter", "real", "recip")):
+        assert abs(e[j] - st[term]) <= REL * scale[j], term
+    box.close()
+
+
+@pytest.mark.parametrize("quarters,writer_k", [(2, 0), (1, 1)])
+def test_fp64_two_moves_in_flight_other_grids(gb, quarters, writer_k):
+    """Two moves in flight at fewer grid CTAs, with and without k-vectors on
+    the context writers."""
+    z, meta = load("c1_water")
+    grid = sm_count(gb, z, meta) * quarters // 4
+    box = gb.Box(system_of(z, meta), config_of(meta))
+    box.mc_init(meta["config"]["random_seed"], move_fractions(meta),
+                meta["config"]["adj_steps"], grid_ctas=grid,
+                writer_kchunk=writer_k, moves_in_flight=2)
+    r = box.mc_run(0, z["trace"].shape[0], trace=True)
+    check_trace(r, z, REL)
     box.close()
 
 
@@ -107,7 +157,7 @@ def test_fp64_autotune_keeps_state_and_matches_fixed_shape(gb):
     before = (tuned.coords(), tuned.energy(), tuned.mc_state())
     res = tuned.mc_autotune("latency", 100)
     tried = res["tried"]
-    assert len(tried) == 8
+    assert len(tried) == 16  # 4 grids x writers' k-vectors x moves in flight
     assert all(t["us_per_move"] > 0 for t in tried)
     best = res["chosen"]
     assert best["us_per_move"] == min(t["us_per_move"] for t in tried)
@@ -122,7 +172,8 @@ def test_fp64_autotune_keeps_state_and_matches_fixed_shape(gb):
     fixed.mc_run(0, 300)
     blob = fixed.checkpoint()
     fixed.mc_init(seed, frac, adj, grid_ctas=best["ctas"],
-                  writer_kchunk=best["writer_kchunk"])
+                  writer_kchunk=best["writer_kchunk"],
+                  moves_in_flight=best["moves_in_flight"])
     fixed.restore(blob)
     n = z["trace"].shape[0] - 300
     a = tuned.mc_run(300, n, trace=True)
