@@ -64,6 +64,81 @@ __host__ __device__ inline size_t chain_pipe_kvec_doubles(int kc_max) {
   return ((9 * (size_t)kc_max + (kc_max + 1) / 2 + 1) & ~(size_t)1);
 }
 
+// Minimum-image wrap of one axis decided on fixed-point turns when a pair
+// is listed: 1 for -L, 2 for +L (2 bits per axis).  Only a pair near half a
+// box edge apart -- far outside the cutoff -- could be decided otherwise
+// than by the FP64 test of BoxDimensions::MinImage.
+__device__ __forceinline__ unsigned turn_wrap(const uint32_t *tp, uint4 f) {
+  const uint32_t tf[3] = {f.x, f.y, f.z};
+  unsigned w = 0;
+  for (int d = 0; d < 3; ++d) {
+    const long long dt = (long long)tp[d] - (long long)tf[d];
+    if (dt > 2147483648LL)
+      w |= 1u << (2 * d);
+    else if (dt < -2147483648LL)
+      w |= 2u << (2 * d);
+  }
+  return w;
+}
+
+// pair_term of the chain with two moves in flight, with fewer FP64
+// instructions (a warp's FP64 instruction holds its SM sub-partition's FP64
+// unit for about 64 cycles on GB300, so their count sets the time of a
+// pass over the pair list): the minimum image from the listed wrap bits
+// (the same FP64 differences: x - L is x + (-L)), the neighbour's charge
+// stored times QQ_FACT, and -- where every kind pair has the 12-6 form --
+// 1 / r^2 by two Newton-Raphson steps from the FP32 reciprocal (relative
+// error below 2^-90 before the final rounding) with sigma^2 / r^2 as a
+// product; the Coulomb cutoff is tested only where it is shorter than the
+// pair cutoff.
+__device__ __forceinline__ void pair_term_pipe(const ChainArgs &A,
+                                               const ChainShared &S, int u,
+                                               double2 pxy, double2 pzq,
+                                               int mj, unsigned wrap,
+                                               bool lj12, bool coul_cut,
+                                               double &lj, double &re,
+                                               double &ovl) {
+  const DevBox &b = A.b;
+  const FF &ff = *A.ff;
+  const int a = u / (2 * NB27), side = (u / NB27) % 2;
+  const double *pp = S.hdr + (side ? 48 : 24) + 3 * a;
+  double dx = pp[0] - pxy.x, dy = pp[1] - pxy.y, dz = pp[2] - pzq.x;
+  dx += (wrap & 1u) ? -b.L[0] : (wrap & 2u) ? b.L[0] : 0.0;
+  dy += (wrap & 4u) ? -b.L[1] : (wrap & 8u) ? b.L[1] : 0.0;
+  dz += (wrap & 16u) ? -b.L[2] : (wrap & 32u) ? b.L[2] : 0.0;
+  const double d2 = dsq3(dx, dy, dz);
+  if (!(ff.rcutSq > d2))
+    return;
+  if (side && d2 < ff.rcutLowSq)
+    ovl = 1.0;
+  double e = 0.0;
+  if (ff.electrostatic && !(coul_cut && ff.rcutCoulSq < d2)) {
+    const double qq = S.hdr[108 + a] * pzq.y;
+    e = ff.ewald ? qq * erfc_over_r(ff, d2) : qq / sqrt(d2);
+  }
+  const int idx = ((const int *)(S.hdr + 116))[a] + meta_kind(mj) * ff.n_kinds;
+  double l;
+  if (lj12) {
+    double y = (double)__frcp_rn((float)d2);
+    double r = fma(-d2, y, 1.0);
+    y = fma(y, r, y);
+    r = fma(-d2, y, 1.0);
+    y = fma(y, r, y);
+    const double rRat2 = ff.sigmaSq[idx] * y;
+    const double attract = rRat2 * rRat2 * rRat2;
+    l = ff.eps_cn[idx] * (attract * attract - attract);
+  } else {
+    l = lj_energy(ff, d2, idx);
+  }
+  if (side) {
+    re += e;
+    lj += l;
+  } else {
+    re -= e;
+    lj -= l;
+  }
+}
+
 __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
   extern __shared__ double dyn[];
   __shared__ ChainShared S;
@@ -106,9 +181,14 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
   // first), so without the permutation the atoms near a molecule can crowd
   // onto a few CTAs and lengthen their pair lists.
   const int OWN = W - nkb;
-  auto perm = [&](int a) {
-    return (int)(((unsigned long long)a * A.perm_m) % (unsigned long long)b.n_atoms);
+  // x mod n_atoms by Barrett reduction (perm_r = floor((2^64 - 1) / n)):
+  // integer multiplies only, no 64-bit division
+  auto mod_n = [&](unsigned long long x) {
+    const unsigned long long n = (unsigned long long)b.n_atoms;
+    unsigned long long r = x - __umul64hi(x, A.perm_r) * n;
+    return (int)(r >= n ? r - n : r);
   };
+  auto perm = [&](int a) { return mod_n((unsigned long long)a * A.perm_m); };
   const int orank = cta - nkb;  // this CTA's rank among the owners
   const int own_per = (b.n_atoms + OWN - 1) / OWN;
   const int on = (!leader && orank >= 0 && orank < b.n_atoms)
@@ -129,16 +209,20 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
     kn[i] = b.kn[k];
   }
   for (int i = threadIdx.x; i < on; i += CT) {
-    const int a = (int)(((unsigned long long)(orank + OWN * i) * A.perm_minv) %
-                        (unsigned long long)b.n_atoms);
+    const int a = mod_n((unsigned long long)(orank + OWN * i) * A.perm_minv);
     const double x = b.x[a], y = b.y[a], z = b.z[a];
     oxy[i] = make_double2(x, y);
-    ozq[i] = make_double2(z, b.q[a]);
+    ozq[i] = make_double2(z, b.q[a] * QQ_FACT);  // the charge times QQ_FACT
     ot[i] = make_uint4(to_turns(x, b.invL[0]), to_turns(y, b.invL[1]),
                        to_turns(z, b.invL[2]),
                        (unsigned)pack_meta(b.mol[a], b.kind[a]));
   }
+  __shared__ int lj12_sh;
   if (threadIdx.x == 0) {
+    int all12 = 1;
+    for (int i = 0; i < ff.n_kinds * ff.n_kinds; ++i)
+      all12 &= ff.eps_cn[i] == 0.0 || ff.nexp[i] == 12.0;
+    lj12_sh = all12;
     S.last_m = -1;
     S.last_acc = 0;
     S.set = *A.set;
@@ -166,6 +250,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
 
   const int total_threads = G * CT;
   const int gtid = cta * CT + threadIdx.x;
+  const bool lj12 = lj12_sh != 0;
+  const bool coul_cut = ff.rcutCoulSq < ff.rcutSq;
   const float turn_f[3] = {(float)(b.L[0] * 2.3283064365386963e-10),
                            (float)(b.L[1] * 2.3283064365386963e-10),
                            (float)(b.L[2] * 2.3283064365386963e-10)};
@@ -209,9 +295,9 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // the settings adjustment before a move (the next move's proposals are
   // made after it), behind a grid barrier; false when a wait gave up
-  auto adjust_before = [&](int t1) -> bool {
+  auto adjust_before = [&](int t1, bool bnd) -> bool {
     long long step = A.first + t1;
-    if ((step + 1) % S.set.adj != 0)
+    if (!bnd)
       return true;
     __syncthreads();
     if (threadIdx.x == 0)
@@ -221,6 +307,10 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
     return grid_sync(A.bar, G, S.gen, b.err, &S.flag, A.spin);
   };
   int nmol = A.n > 1 ? A.moves[1].mol : -1;
+  // (first + t + 2) mod AdjSteps, carried from move to move (no 64-bit
+  // division per move): zero where a settings adjustment precedes move
+  // t + 1
+  int adj_r = (int)((A.first + 2) % S.set.adj);
 
   if (leader) {
     // ---------------- the deciding CTA ----------------
@@ -230,6 +320,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
     for (int t = 0; t < A.n; ++t) {
       const int mol_next = nmol;
       nmol = t + 2 < A.n ? A.moves[t + 2].mol : -1;
+      const bool bnd = adj_r == 0;
+      adj_r = adj_r + 1 == S.set.adj ? 0 : adj_r + 1;
       // this move's header: complete once CTA 0 has flagged the context
       // when it was built during the previous move's phase A, and behind
       // the last grid barrier otherwise
@@ -247,8 +339,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
       const int m = (int)S.hdr[0];
       const int na = (int)S.hdr[2];
       const int a0m = __ldg(b.mstart + m);
-      const bool nspec = t + 1 < A.n && mol_next != m &&
-                         (A.first + t + 2) % S.set.adj != 0 &&
+      const bool nspec = t + 1 < A.n && mol_next != m && !bnd &&
                          !(pend && mol_next == m_prev);
       const int var = pend ? acc_prev : 0;  // the partials' outcome set
       double *part_t = A.part + (size_t)(t % 3) * G * 8;
@@ -422,7 +513,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
       if (threadIdx.x == 0)
         settings_update(S.set, (int)S.hdr[1], acc);
       if (!nspec && t + 1 < A.n) {
-        if (!adjust_before(t + 1))
+        if (!adjust_before(t + 1, bnd))
           return;
         // the next context is built by the work CTAs behind this barrier
         if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag, A.spin))
@@ -453,6 +544,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
     for (int t = 0; t < A.n; ++t) {
       const int mol_next = nmol;
       nmol = t + 2 < A.n ? A.moves[t + 2].mol : -1;
+      const bool bnd = adj_r == 0;
+      adj_r = adj_r + 1 == S.set.adj ? 0 : adj_r + 1;
       CtxPre pre = pipe_b;
       pre.na = pipe_b1 - pipe_b.a0;
       if (piper) {
@@ -469,8 +562,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
       const int a0m = t == 0 ? __ldg(b.mstart + m) : nx_a0;
       const int na = t == 0 ? __ldg(b.mstart + m + 1) - a0m : nx_na;
       // may move t + 1 run before this move's decision
-      const bool nspec = t + 1 < A.n && mol_next != m &&
-                         (A.first + t + 2) % S.set.adj != 0 &&
+      const bool nspec = t + 1 < A.n && mol_next != m && !bnd &&
                          !(pend && mol_next == m_prev);
       pre.writer = false;
       const bool wload = nspec && warp == 7;
@@ -498,6 +590,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
       // share, 1 / 2 an atom of the previous move's molecule at its old
       // position (that move rejected) / its new one (accepted)
       __shared__ unsigned char icl_cls[ICL_MAX];
+      __shared__ unsigned char icl_wrap[ICL_MAX];  // turn_wrap of the pair
       __shared__ int icl_warp[CT / 32 + 1];
       const int npos = 2 * na;
       const uint32_t *pturn = (const uint32_t *)(S.hdr + 84);
@@ -532,14 +625,17 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
           const int pp = __ffs(h) - 1;
           const int side = pp >= na ? 1 : 0, a = pp - side * na;
           const int u = (a * 2 + side) * NB27;
+          const unsigned wr = turn_wrap(pturn + 3 * pp, f);
           if (pos < ICL_MAX) {
             icl_pos[pos][0] = pxy;
             icl_pos[pos][1] = pzq;
             icl_meta[pos] = (int)f.w;
             icl_unit[pos] = (short)u;
             icl_cls[pos] = 0;
+            icl_wrap[pos] = (unsigned char)wr;
           } else {
-            pair_term(A, S, u, pxy, pzq, (int)f.w, lj, re, ovl);
+            pair_term_pipe(A, S, u, pxy, pzq, (int)f.w, wr, lj12, coul_cut, lj,
+                           re, ovl);
           }
           ++pos;
         }
@@ -589,16 +685,20 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
               pxy = make_double2(np[0], np[1]);
               pzq.x = np[2];
             }
+            const unsigned wr = turn_wrap(pturn + 3 * pp, f);
             if (pos < ICL_MAX) {
               icl_pos[pos][0] = pxy;
               icl_pos[pos][1] = pzq;
               icl_meta[pos] = (int)f.w;
               icl_unit[pos] = (short)u;
               icl_cls[pos] = (unsigned char)(1 + vr);
+              icl_wrap[pos] = (unsigned char)wr;
             } else if (vr) {
-              pair_term(A, S, u, pxy, pzq, (int)f.w, ljA, reA, ovA);
+              pair_term_pipe(A, S, u, pxy, pzq, (int)f.w, wr, lj12, coul_cut,
+                             ljA, reA, ovA);
             } else {
-              pair_term(A, S, u, pxy, pzq, (int)f.w, ljR, reR, ovR);
+              pair_term_pipe(A, S, u, pxy, pzq, (int)f.w, wr, lj12, coul_cut,
+                             ljR, reR, ovR);
             }
           }
           n += __popc(mask);
@@ -612,8 +712,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
       auto eval_pairs = [&](int n_eval, int first, int step) {
         for (int i = first * 32 + lane; i < n_eval; i += step * 32) {
           double l = 0.0, r = 0.0, o = 0.0;
-          pair_term(A, S, icl_unit[i], icl_pos[i][0], icl_pos[i][1],
-                    icl_meta[i], l, r, o);
+          pair_term_pipe(A, S, icl_unit[i], icl_pos[i][0], icl_pos[i][1],
+                         icl_meta[i], icl_wrap[i], lj12, coul_cut, l, r, o);
           const int c = icl_cls[i];
           if (c == 0) {
             lj += l;
@@ -1066,7 +1166,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
         have_next = false;
         __syncthreads();
         if (t + 1 < A.n) {
-          if (!adjust_before(t + 1))
+          if (!adjust_before(t + 1, bnd))
             return;
           build_ctx(A, S, t + 1, S.hdr, acc, 0, CT);
           if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag, A.spin))

@@ -429,6 +429,7 @@ struct ChainArgs {
   // permutation of the atom index for the pipelined chain's atom ownership
   // (p = a * perm_m mod n_atoms, a = p * perm_minv mod n_atoms)
   unsigned long long perm_m, perm_minv;
+  unsigned long long perm_r;  // floor((2^64 - 1) / n_atoms), for x mod n_atoms
   int *tr_i;      // [n][3] or null
   double *tr_d;   // [n][3] or null
   // phase clocks (NULL: not collected): [0 CTA 0, 1 the leader][phase:
@@ -2272,6 +2273,7 @@ static int run_chain(Box &b, McState &s, const MoveRec *moves, int64_t first,
                          s.params.writer_kchunk != 0);
   A.nctx = s.pipe ? 3 : 2;
   chain_perm(b.dev.n_atoms, &A.perm_m, &A.perm_minv);
+  A.perm_r = ~0ULL / (unsigned long long)std::max(b.dev.n_atoms, 1);
   A.tr_i = tr_i;
   A.tr_d = tr_d;
   A.prof = s.profile ? s.d_prof : nullptr;
