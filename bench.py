@@ -171,10 +171,13 @@ def measured_peaks(torch, dev):
     return out
 
 
-# DRAM bytes (read + write) of one 1,000-move k_chain_fp64 launch of the
-# 8,000-water workload after the L2 flush: mean of 13 launches of this
-# command's FP64 line under ncu (dram__bytes_read.sum 2.42 MB, write 0)
-CHAIN_FP64_DRAM_BYTES_1000 = 2.42e6
+# DRAM bytes (read + write) of one 1,000-move launch of each FP64 chain
+# kernel on the 8,000-water workload after the L2 flush, from ncu captures
+# of this command's FP64 line (dram__bytes_read.sum + dram__bytes_write.sum):
+# two moves in flight 2.54 MB read, 0 written (mean of 10 launches); one
+# move in flight 2.42 MB, 0 (mean of 13)
+CHAIN_FP64_DRAM_BYTES_1000 = {"k_chain_fp64_pipe": 2.54e6,
+                              "k_chain_fp64": 2.42e6}
 SMALL = False  # --small: the 256-water, 19.7 A box (for profiler captures)
 
 
@@ -793,6 +796,9 @@ def run_gb300(args, rank, world):
     box = engine.Box(sysm, cfg, device=dev)
     K, kmax = box.num_kvectors()
     box.mc_init(SEED + rank, FRAC, ADJ, scales=SCALES)
+    shape = box.mc_shape()
+    chain_kernel = ("k_chain_fp64_pipe" if shape["moves_in_flight"] == 2
+                    else "k_chain_fp64")
     stream = torch.cuda.ExternalStream(box.stream_ptr(), device=dev)
     M = args.moves_per_step
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32,
@@ -886,8 +892,8 @@ def run_gb300(args, rank, world):
         if dist:
             dist.destroy_process_group()
         return
-    # per chain launch: k_fill_u64 (partial slots), k_chain_fp64, and the
-    # grid rebuild k_cell_scatter + k_cell_sort_fill
+    # per chain launch: k_fill_u64 (partial slots), the chain kernel, and
+    # the grid rebuild k_cell_scatter + k_cell_sort_fill
     launches = 4 * timing["chain_launches"] + 10 * timing["mp_moves"]
     kern_ms = timing["chain_ms"] / max(timing["chain_launches"], 1)
     moves_per_launch = timing["chain_moves"] / max(timing["chain_launches"], 1)
@@ -895,14 +901,14 @@ def run_gb300(args, rank, world):
     achieved = fl * moves_per_launch / (kern_ms / 1e3) / 1e12
     # DRAM bytes of one 1,000-move launch from an ncu capture of this
     # command; other move counts: null
-    traffic = (CHAIN_FP64_DRAM_BYTES_1000
+    traffic = (CHAIN_FP64_DRAM_BYTES_1000.get(chain_kernel)
                if not SMALL and round(moves_per_launch) == 1000 else None)
     roof = {"bound": "fp64", "achieved": achieved,
             "peak": peaks["fp64_tflops"], "unit": "TFLOP/s",
             "frac": achieved / peaks["fp64_tflops"], "traffic": traffic,
             "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + "
                             "dram__bytes_write.sum)",
-            "kernel": "k_chain_fp64",
+            "kernel": chain_kernel,
             "per_unit": "%.3g FP64 flop per move (%d k-vectors), plus %d "
                         "sin/cos evaluations" % (fl, K, sincos_per_move(K)),
             "peak_source": peaks["pipe_peak_source"],
@@ -918,7 +924,10 @@ def run_gb300(args, rank, world):
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "moves_per_step": M,
                    "l2": "flushed between steps (512 MB write)",
-                   "precision": "FP64 plain form", "k_vectors": K},
+                   "precision": "FP64 plain form", "k_vectors": K,
+                   "chain": {"kernel": chain_kernel,
+                             "grid_ctas": shape["ctas"],
+                             "moves_in_flight": shape["moves_in_flight"]}},
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "moves/s",

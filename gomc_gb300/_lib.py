@@ -190,6 +190,7 @@ SIGNATURES = {
     "gb_mc_set_gomc_state": (C.c_int, [_P, C.POINTER(GomcChk)]),
     "gb_box_stream": (C.c_int, [_P, C.POINTER(_P)]),
     "gb_mc_layout": (C.c_int, [_P, _I, _I, _L]),
+    "gb_mc_shape_get": (C.c_int, [_P, C.POINTER(McShape)]),
     "gb_mc_autotune": (C.c_int, [_P, C.c_int32, C.c_int32,
                                  C.POINTER(McShape), C.POINTER(McShape),
                                  C.c_int32, _I]),

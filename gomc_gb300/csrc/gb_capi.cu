@@ -525,6 +525,29 @@ int gb_mc_layout(gb_box *box, int32_t *ctas_per_chain,
     *smem_bytes = (int64_t)sm;
   return gb::OK;
 }
+int gb_mc_shape_get(gb_box *box, gb_mc_shape *shape) {
+  int rc = guard(box);
+  if (rc)
+    return rc;
+  gb::Box &b = *box->b;
+  if (!shape)
+    return b.Fail(gb::ERR_ARG, "shape is NULL");
+  if (!b.mc)
+    return b.Fail(gb::ERR_STATE, "gb_mc_init has not been called");
+  gb::McState &s = *b.mc;
+  *shape = gb_mc_shape{};
+  if (b.cfg.precision == GB_MIXED) {
+    shape->ctas = s.cluster;
+    shape->unit_lanes = 1 << s.ulog;
+    shape->max_concurrent = gb::max_active_clusters(s.cluster, s.mixed_smem);
+  } else {
+    shape->ctas = s.grid;
+    shape->writer_kchunk = s.params.writer_kchunk;
+    shape->moves_in_flight = s.pipe ? 2 : 1;
+    shape->max_concurrent = 1;
+  }
+  return gb::OK;
+}
 int gb_box_stream(gb_box *box, void **stream) {
   int rc = guard(box);
   if (rc)

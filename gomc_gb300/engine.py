@@ -499,6 +499,15 @@ class Box:
         return dict(ctas_per_chain=c.value, max_concurrent=n.value,
                     smem_bytes=sm.value)
 
+    def mc_shape(self) -> dict:
+        """The chain's launch shape (gb_mc_shape_get)."""
+        sh = _lib.McShape()
+        self._chk(lib().gb_mc_shape_get(self.h, C.byref(sh)))
+        return dict(ctas=sh.ctas, unit_lanes=sh.unit_lanes,
+                    writer_kchunk=sh.writer_kchunk,
+                    moves_in_flight=sh.moves_in_flight,
+                    max_concurrent=sh.max_concurrent)
+
     def mc_autotune(self, objective: str = "latency",
                     trial_moves: int = 0) -> dict:
         """Time each launch shape that fits on this machine's own state and keep

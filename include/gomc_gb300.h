@@ -350,6 +350,9 @@ typedef struct gb_mc_shape {
 int gb_mc_autotune(gb_box *box, int32_t objective, int32_t trial_moves,
                    gb_mc_shape *chosen, gb_mc_shape *tried, int32_t cap,
                    int32_t *n_tried);
+/* The launch shape gb_mc_init (or the autotuner) chose for this box's
+ * chain, its trial time zero.  No reference counterpart. */
+int gb_mc_shape_get(gb_box *box, gb_mc_shape *shape);
 /* The CUDA stream (cudaStream_t) every call on this machine is ordered on. */
 int gb_box_stream(gb_box *box, void **stream);
 
