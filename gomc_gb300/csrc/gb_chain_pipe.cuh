@@ -64,6 +64,14 @@ __host__ __device__ inline size_t chain_pipe_kvec_doubles(int kc_max) {
   return ((9 * (size_t)kc_max + (kc_max + 1) / 2 + 1) & ~(size_t)1);
 }
 
+// The pair list of a k-chunk CTA: one segment of PSEG entries per warp
+// (its own atoms' pairs, found by a warp-level scan) and one for the
+// previous move's atoms, so that the list needs one CTA barrier and no
+// CTA-wide prefix sum.
+constexpr int PSEG = 64;
+constexpr int PNSEG = CT / 32 + 1;
+constexpr int ICL_CAP = PSEG * PNSEG;
+
 // Minimum-image wrap of one axis decided on fixed-point turns when a pair
 // is listed: 1 for -L, 2 for +L (2 bits per axis).  Only a pair near half a
 // box edge apart -- far outside the cutoff -- could be decided otherwise
@@ -583,15 +591,15 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
       // move is undecided, its atoms are left out of the pre-test and listed
       // after the others on both of its outcomes, so that one warp pass
       // takes them all.
-      __shared__ double2 icl_pos[ICL_MAX][2];
-      __shared__ int icl_meta[ICL_MAX];
-      __shared__ short icl_unit[ICL_MAX];
+      __shared__ double2 icl_pos[ICL_CAP][2];
+      __shared__ int icl_meta[ICL_CAP];
+      __shared__ short icl_unit[ICL_CAP];
       // entry class: 0 an own atom that both outcomes of the previous move
       // share, 1 / 2 an atom of the previous move's molecule at its old
       // position (that move rejected) / its new one (accepted)
-      __shared__ unsigned char icl_cls[ICL_MAX];
-      __shared__ unsigned char icl_wrap[ICL_MAX];  // turn_wrap of the pair
-      __shared__ int icl_warp[CT / 32 + 1];
+      __shared__ unsigned char icl_cls[ICL_CAP];
+      __shared__ unsigned char icl_wrap[ICL_CAP];  // turn_wrap of the pair
+      __shared__ int seg_cnt[PNSEG];  // entries found per segment
       const int npos = 2 * na;
       const uint32_t *pturn = (const uint32_t *)(S.hdr + 84);
       int n_prev = 0;  // own atoms of the previous molecule (usually 0 or 1)
@@ -617,16 +625,16 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
         }
         return hit;
       };
-      // list own atom i's passing positions from slot pos on (past the
-      // list: evaluated here, not met at liquid densities)
-      auto list_hits = [&](int i, unsigned hit, uint4 f, int pos) {
+      // list own atom i's passing positions from slot pos on, below slot
+      // lim (past it: evaluated here, not met at liquid densities)
+      auto list_hits = [&](int i, unsigned hit, uint4 f, int pos, int lim) {
         const double2 pxy = oxy[i], pzq = ozq[i];
         for (unsigned h = hit; h; h &= h - 1) {
           const int pp = __ffs(h) - 1;
           const int side = pp >= na ? 1 : 0, a = pp - side * na;
           const int u = (a * 2 + side) * NB27;
           const unsigned wr = turn_wrap(pturn + 3 * pp, f);
-          if (pos < ICL_MAX) {
+          if (pos < lim) {
             icl_pos[pos][0] = pxy;
             icl_pos[pos][1] = pzq;
             icl_meta[pos] = (int)f.w;
@@ -642,9 +650,9 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
       };
       // The previous move's atoms this CTA owns on both outcomes (entries
       // c = (atom, outcome, position)), pre-tested like the others and
-      // appended in order from slot n0 by one warp; those past the list
-      // are evaluated here.  Returns the entries listed in all.
-      auto list_prev = [&](int n0) -> int {
+      // appended in order from slot n0 by one warp, below slot lim; those
+      // past it are evaluated here.  Returns the end of the entries.
+      auto list_prev = [&](int n0, int lim) -> int {
         int n = n0;
         const int nc = na_prev * 2 * npos;
         for (int base = 0; base < nc; base += 32) {
@@ -686,7 +694,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
               pzq.x = np[2];
             }
             const unsigned wr = turn_wrap(pturn + 3 * pp, f);
-            if (pos < ICL_MAX) {
+            if (pos < lim) {
               icl_pos[pos][0] = pxy;
               icl_pos[pos][1] = pzq;
               icl_meta[pos] = (int)f.w;
@@ -709,8 +717,22 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
       // class's sums; the previous move's pairs past a full list directly
       // (entries first * 32 + lane, stepping step * 32: the passes of 32
       // entries split between two warps when the list is longer than one)
-      auto eval_pairs = [&](int n_eval, int first, int step) {
-        for (int i = first * 32 + lane; i < n_eval; i += step * 32) {
+      // (entry v of the list: slot v, or with segments the v-th listed
+      // entry counting through the segments in order)
+      auto eval_pairs = [&](int n_eval, int first, int step, bool segs) {
+        for (int v = first * 32 + lane; v < n_eval; v += step * 32) {
+          int i = v;
+          if (segs) {
+            int r = v;
+            for (int sg = 0; sg < PNSEG; ++sg) {
+              const int c = min(seg_cnt[sg], PSEG);
+              if (r < c) {
+                i = sg * PSEG + r;
+                break;
+              }
+              r -= c;
+            }
+          }
           double l = 0.0, r = 0.0, o = 0.0;
           pair_term_pipe(A, S, icl_unit[i], icl_pos[i][0], icl_pos[i][1],
                          icl_meta[i], icl_wrap[i], lj12, coul_cut, l, r, o);
@@ -851,15 +873,15 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
                 incl += v;
             }
             if (hit)
-              list_hits(i, hit, f, icl_n + incl - cnt);
+              list_hits(i, hit, f, icl_n + incl - cnt, ICL_CAP);
             icl_n += __shfl_sync(0xffffffffu, incl, 31);
           }
           __syncwarp();
           if (ncomb > 0)
-            icl_n = list_prev(icl_n);
+            icl_n = list_prev(icl_n, ICL_CAP);
           __syncwarp();
           mark(1);
-          eval_pairs(min(icl_n, ICL_MAX), 0, 1);
+          eval_pairs(min(icl_n, ICL_CAP), 0, 1, false);
           store_pairs_warp(false);
           if (lane == 0) {
             __stcg(part_c + 2, 0.0);
@@ -905,7 +927,9 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
         mark(0);
         if (wload)
           ctx_pre2(A, S, t + 1, pre);
-        int icl_n = 0;
+        // each warp lists its atoms' pairs into its own segment; warp 0
+        // the previous move's atoms into the last
+        int n_w = 0;
         for (int base = 0; base < on; base += CT) {
           const int i = base + threadIdx.x;
           uint4 f = make_uint4(0, 0, 0, 0);
@@ -917,42 +941,35 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
             if (lane >= o)
               incl += v;
           }
-          if (lane == 31)
-            icl_warp[warp] = incl;
-          __syncthreads();
-          if (threadIdx.x == 0) {
-            int run = icl_n;
-            for (int w = 0; w < CT / 32; ++w) {
-              int c = icl_warp[w];
-              icl_warp[w] = run;
-              run += c;
-            }
-            icl_warp[CT / 32] = run;
-          }
-          __syncthreads();
           if (hit)
-            list_hits(i, hit, f, icl_warp[warp] + incl - cnt);
-          icl_n = icl_warp[CT / 32];
-          __syncthreads();
+            list_hits(i, hit, f, warp * PSEG + n_w + incl - cnt,
+                      (warp + 1) * PSEG);
+          n_w += __shfl_sync(0xffffffffu, incl, 31);
         }
-        __shared__ int icl_total;
+        if (lane == 0)
+          seg_cnt[warp] = n_w;
         if (warp == 0) {
-          const int n = ncomb > 0 ? list_prev(icl_n) : icl_n;
+          const int b0 = (PNSEG - 1) * PSEG;
+          const int n = ncomb > 0 ? list_prev(b0, ICL_CAP) - b0 : 0;
           if (lane == 0)
-            icl_total = n;
+            seg_cnt[PNSEG - 1] = n;
         }
         __syncthreads();  // the listed pairs
         mark(1);
-        // pairs past the list were evaluated where they were found (not met
-        // at liquid densities): then the pair sums are the CTA's
-        const bool all_pairs = icl_total > ICL_MAX;
-        const int n_eval = min(icl_total, ICL_MAX);
+        // pairs past a full segment were evaluated where they were found
+        // (not met at liquid densities): then the pair sums are the CTA's
+        int n_eval = 0;
+        bool all_pairs = false;
+        for (int sg = 0; sg < PNSEG; ++sg) {
+          n_eval += min(seg_cnt[sg], PSEG);
+          all_pairs |= seg_cnt[sg] > PSEG;
+        }
         // A list longer than one warp pass: warp 4 (another sub-partition)
         // takes every second pass after its k-vectors, instead of warp 3
         // taking them all in sequence.
         const bool split = n_eval > 32 && !all_pairs;
         if (warp == pw) {
-          eval_pairs(n_eval, 0, split ? 2 : 1);
+          eval_pairs(n_eval, 0, split ? 2 : 1, true);
           if (!all_pairs)
             store_pairs_warp(split);
         } else if (warp == 7) {
@@ -1043,7 +1060,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
           if (split && warp == 4) {
             // the second pair warp: its passes, summed, to warp 3
             lj = re = ovl = ljR = reR = ovR = ljA = reA = ovA = 0.0;
-            eval_pairs(n_eval, 1, 2);
+            eval_pairs(n_eval, 1, 2, true);
             double v[4] = {lj + ljR, re + reR, lj + ljA, re + reA};
             for (int o = 16; o > 0; o >>= 1)
               for (int j = 0; j < 4; ++j)
