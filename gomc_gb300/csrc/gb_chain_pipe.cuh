@@ -99,11 +99,39 @@ __device__ __forceinline__ unsigned turn_wrap(const uint32_t *tp, uint4 f) {
 // error below 2^-90 before the final rounding) with sigma^2 / r^2 as a
 // product; the Coulomb cutoff is tested only where it is shorter than the
 // pair cutoff.
+// The force field's pair tables held in shared memory by the chain with two
+// moves in flight: the erfc(alpha r)/r segments (NULL: read from global
+// memory) and the LJ sigma^2 and epsilon C_n of every kind pair.
+struct PairTabs {
+  const double *etab;
+  const double *sig2, *eps;
+};
+
+// erfc(alpha r) / r as erfc_over_r: the same segment polynomial, its
+// coefficients read from shared memory
+__device__ __forceinline__ double erfc_over_r_tab(const FF &ff,
+                                                  const double *tab, double s) {
+  const long long bits = __double_as_longlong(s);
+  const int seg = (int)(bits >> 46) - ff.etab_key0;
+  if (tab == nullptr || (unsigned)seg >= (unsigned)ff.etab_nseg)
+    return erfc_over_r(ff, s);
+  const double a = __longlong_as_double(bits & ~((1LL << 46) - 1));
+  const double scale = __longlong_as_double((2053LL - (bits >> 52)) << 52);
+  const double u = fma(s - a, scale, -1.0);
+  const double *c = tab + (size_t)seg * (ETAB_DEG + 1);
+  double p = c[ETAB_DEG];
+#pragma unroll
+  for (int m = ETAB_DEG - 1; m >= 0; --m)
+    p = fma(p, u, c[m]);
+  return p;
+}
+
 __device__ __forceinline__ void pair_term_pipe(const ChainArgs &A,
                                                const ChainShared &S, int u,
                                                double2 pxy, double2 pzq,
                                                int mj, unsigned wrap,
                                                bool lj12, bool coul_cut,
+                                               const PairTabs &pt,
                                                double &lj, double &re,
                                                double &ovl) {
   const DevBox &b = A.b;
@@ -122,7 +150,7 @@ __device__ __forceinline__ void pair_term_pipe(const ChainArgs &A,
   double e = 0.0;
   if (ff.electrostatic && !(coul_cut && ff.rcutCoulSq < d2)) {
     const double qq = S.hdr[108 + a] * pzq.y;
-    e = ff.ewald ? qq * erfc_over_r(ff, d2) : qq / sqrt(d2);
+    e = ff.ewald ? qq * erfc_over_r_tab(ff, pt.etab, d2) : qq / sqrt(d2);
   }
   const int idx = ((const int *)(S.hdr + 116))[a] + meta_kind(mj) * ff.n_kinds;
   double l;
@@ -132,9 +160,9 @@ __device__ __forceinline__ void pair_term_pipe(const ChainArgs &A,
     y = fma(y, r, y);
     r = fma(-d2, y, 1.0);
     y = fma(y, r, y);
-    const double rRat2 = ff.sigmaSq[idx] * y;
+    const double rRat2 = pt.sig2[idx] * y;
     const double attract = rRat2 * rRat2 * rRat2;
-    l = ff.eps_cn[idx] * (attract * attract - attract);
+    l = pt.eps[idx] * (attract * attract - attract);
   } else {
     l = lj_energy(ff, d2, idx);
   }
@@ -206,6 +234,10 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
       (double2 *)(((uintptr_t)(pidx + kc_max) + 15) & ~(uintptr_t)15);
   double2 *const ozq = oxy + own_per;
   uint4 *const ot = (uint4 *)(ozq + own_per);
+  // the erfc(alpha r)/r segments after them (k-chunk CTAs, Ewald on)
+  double *const etab_s = (double *)(ot + own_per);
+  __shared__ double lj_sig2_s[MAX_KINDS * MAX_KINDS];
+  __shared__ double lj_eps_s[MAX_KINDS * MAX_KINDS];
   __shared__ char2 pair_n[NPAIR_CAP];
   __shared__ int npair;
   int bS = 0, bP = -1;  // committed and pending k-chunk buffers
@@ -225,6 +257,15 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
                        to_turns(z, b.invL[2]),
                        (unsigned)pack_meta(b.mol[a], b.kind[a]));
   }
+  const bool own_tab = !leader && !kless && ff.erfc_tab != nullptr;
+  if (own_tab)
+    for (int i = threadIdx.x; i < ff.etab_nseg * (ETAB_DEG + 1); i += CT)
+      etab_s[i] = ff.erfc_tab[i];
+  for (int i = threadIdx.x; i < ff.n_kinds * ff.n_kinds; i += CT) {
+    lj_sig2_s[i] = ff.sigmaSq[i];
+    lj_eps_s[i] = ff.eps_cn[i];
+  }
+  const PairTabs ptab{own_tab ? etab_s : nullptr, lj_sig2_s, lj_eps_s};
   __shared__ int lj12_sh;
   if (threadIdx.x == 0) {
     int all12 = 1;
@@ -642,8 +683,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
             icl_cls[pos] = 0;
             icl_wrap[pos] = (unsigned char)wr;
           } else {
-            pair_term_pipe(A, S, u, pxy, pzq, (int)f.w, wr, lj12, coul_cut, lj,
-                           re, ovl);
+            pair_term_pipe(A, S, u, pxy, pzq, (int)f.w, wr, lj12, coul_cut, ptab,
+                           lj, re, ovl);
           }
           ++pos;
         }
@@ -703,10 +744,10 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
               icl_wrap[pos] = (unsigned char)wr;
             } else if (vr) {
               pair_term_pipe(A, S, u, pxy, pzq, (int)f.w, wr, lj12, coul_cut,
-                             ljA, reA, ovA);
+                             ptab, ljA, reA, ovA);
             } else {
               pair_term_pipe(A, S, u, pxy, pzq, (int)f.w, wr, lj12, coul_cut,
-                             ljR, reR, ovR);
+                             ptab, ljR, reR, ovR);
             }
           }
           n += __popc(mask);
@@ -735,7 +776,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
           }
           double l = 0.0, r = 0.0, o = 0.0;
           pair_term_pipe(A, S, icl_unit[i], icl_pos[i][0], icl_pos[i][1],
-                         icl_meta[i], icl_wrap[i], lj12, coul_cut, l, r, o);
+                         icl_meta[i], icl_wrap[i], lj12, coul_cut, ptab, l, r,
+                         o);
           const int c = icl_cls[i];
           if (c == 0) {
             lj += l;

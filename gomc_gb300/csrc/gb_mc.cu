@@ -1898,7 +1898,11 @@ static size_t chain_smem(const Box &b, int grid, int nrows_max,
              (b.dev.kmax + 1) +
          sizeof(double2) * (size_t)NPAIR_CAP * 2 * MAX_MOL_ATOMS +
          sizeof(unsigned short) * (size_t)kc_max + 64 +
-         own_per * (2 * sizeof(double2) + sizeof(uint4));
+         own_per * (2 * sizeof(double2) + sizeof(uint4)) +
+         // (the pipelined chain's copy of the erfc(alpha r)/r segments)
+         (pipe && b.ff.erfc_tab ? sizeof(double) * (size_t)b.ff.etab_nseg *
+                                      (ETAB_DEG + 1)
+                                : 0);
 }
 
 int mc_init(Box &b, const gb_mc_params &p) {
