@@ -280,21 +280,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
     S.gen = ld_acquire(&A.bar[1]);
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int np = 0;
-    for (int i = 0; i < kc && np >= 0; ++i) {
-      char4 n = kn[i];
-      if (np == 0 || pair_n[np - 1].x != n.x || pair_n[np - 1].y != n.y) {
-        if (np == NPAIR_CAP) {
-          np = -1;  // too many columns: form all three products per k
-          break;
-        }
-        pair_n[np++] = make_char2(n.x, n.y);
-      }
-      pidx[i] = (unsigned short)(np - 1);
-    }
-    npair = np;
-  }
+  if (threadIdx.x == 0)
+    npair = chunk_columns(kn, kc, pair_n, pidx);
   __syncthreads();
 
   const int total_threads = G * CT;
@@ -1025,48 +1012,18 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
         } else {
           const int kw = warp < 3 ? warp : warp - 1;  // 0..5
           // the x-y column products first (named barrier 4: the six warps)
-          for (int e = kw * 32 + lane; e < npair * 2 * na; e += 6 * 32) {
-            int p = e / (2 * na), r = e - p * 2 * na;
-            const double2 *rx = tab + (size_t)(r * 3) * stride;
-            double q = S.hdr[72 + (r < na ? r : r - na)];
-            double2 v = cmul2(rx[pair_n[p].x], tab_at(rx + stride, pair_n[p].y));
-            exy[e] = make_double2(q * v.x, q * v.y);
-          }
+          xy_products(kw * 32 + lane, 6 * 32, npair, pair_n, tab, stride, na,
+                      S.hdr + 72, exy);
           asm volatile("bar.sync 4, 192;" ::: "memory");
           const double *sR = KR(bS), *sI = KI(bS);
           const double *pR = pend ? KR(bP) : nullptr;
           const double *pI = pend ? KI(bP) : nullptr;
           double *rR = KR(bR), *rI = KI(bR), *aR = KR(bA), *aI = KI(bA);
           for (int i = kw * 32 + lane; i < kc; i += 6 * 32) {
-            char4 n = kn[i];
-            double dR = 0, dI = 0;
-            const double2 *col =
-                npair > 0 ? exy + (size_t)pidx[i] * 2 * na : nullptr;
-            for (int a = 0; a < na; ++a) {
-              const double q = S.hdr[72 + a];
-              const double2 *ro = tab + (size_t)(a * 3) * stride;
-              const double2 *rn = tab + (size_t)((na + a) * 3) * stride;
-              double2 xo, xn;
-              if (col) {
-                xo = col[a];
-                xn = col[na + a];
-              } else {
-                double2 vo = cmul2(ro[n.x], tab_at(ro + stride, n.y));
-                double2 vn = cmul2(rn[n.x], tab_at(rn + stride, n.y));
-                xo = make_double2(q * vo.x, q * vo.y);
-                xn = make_double2(q * vn.x, q * vn.y);
-              }
-              double2 zo = tab_at(ro + 2 * stride, n.z);
-              double2 zn = tab_at(rn + 2 * stride, n.z);
-              dR = fma(xn.x, zn.x, dR);
-              dR = fma(-xn.y, zn.y, dR);
-              dR = fma(-xo.x, zo.x, dR);
-              dR = fma(xo.y, zo.y, dR);
-              dI = fma(xn.x, zn.y, dI);
-              dI = fma(xn.y, zn.x, dI);
-              dI = fma(-xo.x, zo.y, dI);
-              dI = fma(-xo.y, zo.x, dI);
-            }
+            double dR, dI;
+            kvec_delta(kn[i],
+                       npair > 0 ? exy + (size_t)pidx[i] * 2 * na : nullptr,
+                       tab, stride, na, S.hdr + 72, dR, dI);
             double srn = sR[i] + dR, sin_ = sI[i] + dI;
             rR[i] = srn;
             rI[i] = sin_;

@@ -825,6 +825,81 @@ __device__ __forceinline__ void pair_term(const ChainArgs &A,
   }
 }
 
+// The (n_x, n_y) columns a k-chunk spans (its k-vectors run x outer, y, z
+// inner): pair_n[c] the columns in order and pidx[i] the column of
+// k-vector i; returns their number, or -1 when there are more than
+// NPAIR_CAP (the products are then formed per k-vector).  One thread.
+__device__ inline int chunk_columns(const char4 *kn, int kc, char2 *pair_n,
+                                    unsigned short *pidx) {
+  int np = 0;
+  for (int i = 0; i < kc; ++i) {
+    char4 n = kn[i];
+    if (np == 0 || pair_n[np - 1].x != n.x || pair_n[np - 1].y != n.y) {
+      if (np == NPAIR_CAP)
+        return -1;
+      pair_n[np++] = make_char2(n.x, n.y);
+    }
+    pidx[i] = (unsigned short)(np - 1);
+  }
+  return np;
+}
+
+// The charge-weighted x-y products of a move for each column of the chunk
+// and each old / new atom position, entries e = e0, e0 + step, ... of
+// npair x 2 na (exy[column * 2 na + side * na + atom]).
+__device__ __forceinline__ void xy_products(int e0, int step, int npair,
+                                            const char2 *pair_n,
+                                            const double2 *tab, int stride,
+                                            int na, const double *q,
+                                            double2 *exy) {
+  for (int e = e0; e < npair * 2 * na; e += step) {
+    int p = e / (2 * na), r = e - p * 2 * na;
+    const double2 *rx = tab + (size_t)(r * 3) * stride;
+    double qa = q[r < na ? r : r - na];
+    double2 v = cmul2(rx[pair_n[p].x], tab_at(rx + stride, pair_n[p].y));
+    exy[e] = make_double2(qa * v.x, qa * v.y);
+  }
+}
+
+// The change of the structure factor at k-vector n from a move context:
+// the sum over the moved atoms of q (e^{i k.r_new} - e^{i k.r_old}), four
+// FMAs per atom and side.  col: the move's charge-weighted x-y products of
+// this k-vector's (n_x, n_y) column (old atoms, then new), or NULL to form
+// them from the phase rows `tab` (stride entries per row, rows atom-major
+// old then new, x, y, z); q: the charges (hdr + 72).  A zero charge gives
+// exact zeros (the products carry the charge), so it is not tested.
+__device__ __forceinline__ void kvec_delta(char4 n, const double2 *col,
+                                           const double2 *tab, int stride,
+                                           int na, const double *q,
+                                           double &dR, double &dI) {
+  dR = 0.0;
+  dI = 0.0;
+  for (int a = 0; a < na; ++a) {
+    const double2 *ro = tab + (size_t)(a * 3) * stride;
+    const double2 *rn = tab + (size_t)((na + a) * 3) * stride;
+    double2 xo, xn;
+    if (col) {
+      xo = col[a];
+      xn = col[na + a];
+    } else {
+      double2 vo = cmul2(ro[n.x], tab_at(ro + stride, n.y));
+      double2 vn = cmul2(rn[n.x], tab_at(rn + stride, n.y));
+      xo = make_double2(q[a] * vo.x, q[a] * vo.y);
+      xn = make_double2(q[a] * vn.x, q[a] * vn.y);
+    }
+    double2 zo = tab_at(ro + 2 * stride, n.z);
+    double2 zn = tab_at(rn + 2 * stride, n.z);
+    dR = fma(xn.x, zn.x, dR);
+    dR = fma(-xn.y, zn.y, dR);
+    dR = fma(-xo.x, zo.x, dR);
+    dR = fma(xo.y, zo.y, dR);
+    dI = fma(xn.x, zn.y, dI);
+    dI = fma(xn.y, zn.x, dI);
+    dI = fma(-xo.x, zo.y, dI);
+    dI = fma(-xo.y, zo.x, dI);
+  }
+}
+
 __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
   extern __shared__ double dyn[];
   __shared__ ChainShared S;
@@ -891,21 +966,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     S.gen = ld_acquire(&A.bar[1]);
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int np = 0;
-    for (int i = 0; i < kc && np >= 0; ++i) {
-      char4 n = kn[i];
-      if (np == 0 || pair_n[np - 1].x != n.x || pair_n[np - 1].y != n.y) {
-        if (np == NPAIR_CAP) {
-          np = -1;  // too many columns: form all three products per k
-          break;
-        }
-        pair_n[np++] = make_char2(n.x, n.y);
-      }
-      pidx[i] = (unsigned short)(np - 1);
-    }
-    npair = np;
-  }
+  if (threadIdx.x == 0)
+    npair = chunk_columns(kn, kc, pair_n, pidx);
   __syncthreads();
 
   const int total_threads = G * CT;
@@ -1007,13 +1069,8 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     const int a0m = __ldg(b.mstart + m);
     // x-y column products times the atom's charge, one per (column,
     // old/new atom)
-    for (int e = threadIdx.x; e < npair * 2 * na; e += CT) {
-      int p = e / (2 * na), r = e - p * 2 * na;
-      const double2 *rx = tab + (size_t)(r * 3) * stride;
-      double q = S.hdr[72 + (r < na ? r : r - na)];
-      double2 v = cmul2(rx[pair_n[p].x], tab_at(rx + stride, pair_n[p].y));
-      exy[e] = make_double2(q * v.x, q * v.y);
-    }
+    xy_products(threadIdx.x, CT, npair, pair_n, tab, stride, na, S.hdr + 72,
+                exy);
     if (wload)
       ctx_pre2(A, S, t + 1, pre);
     // (1) Real space: this CTA's own atoms against the old and new
@@ -1142,38 +1199,9 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64(ChainArgs A) {
     if (!kless && warp != 3 && warp != 7) {
       const int kw = warp < 3 ? warp : warp - 1;  // 0..5
       for (int i = kw * 32 + lane; i < kc; i += 6 * 32) {
-        char4 n = kn[i];
-        // sum over the atoms of q (e^{i k.r_new} - e^{i k.r_old}), the
-        // charge already in the x-y product: four FMAs per (atom, side)
-        double dR = 0, dI = 0;
-        const double2 *col = npair > 0 ? exy + (size_t)pidx[i] * 2 * na : nullptr;
-        for (int a = 0; a < na; ++a) {
-          // a zero charge contributes exact zeros (the x-y products carry
-          // the charge), so no FP64 test of it is made here
-          const double q = S.hdr[72 + a];
-          const double2 *ro = tab + (size_t)(a * 3) * stride;
-          const double2 *rn = tab + (size_t)((na + a) * 3) * stride;
-          double2 xo, xn;
-          if (col) {
-            xo = col[a];
-            xn = col[na + a];
-          } else {
-            double2 vo = cmul2(ro[n.x], tab_at(ro + stride, n.y));
-            double2 vn = cmul2(rn[n.x], tab_at(rn + stride, n.y));
-            xo = make_double2(q * vo.x, q * vo.y);
-            xn = make_double2(q * vn.x, q * vn.y);
-          }
-          double2 zo = tab_at(ro + 2 * stride, n.z);
-          double2 zn = tab_at(rn + 2 * stride, n.z);
-          dR = fma(xn.x, zn.x, dR);
-          dR = fma(-xn.y, zn.y, dR);
-          dR = fma(-xo.x, zo.x, dR);
-          dR = fma(xo.y, zo.y, dR);
-          dI = fma(xn.x, zn.y, dI);
-          dI = fma(xn.y, zn.x, dI);
-          dI = fma(-xo.x, zo.y, dI);
-          dI = fma(-xo.y, zo.x, dI);
-        }
+        double dR, dI;
+        kvec_delta(kn[i], npair > 0 ? exy + (size_t)pidx[i] * 2 * na : nullptr,
+                   tab, stride, na, S.hdr + 72, dR, dI);
         double srn = sR[i] + dR;
         double sin_ = sI[i] + dI;
         nR[i] = srn;
