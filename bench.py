@@ -791,7 +791,6 @@ def run_gb300(args, rank, world):
         if dist:
             dist.barrier()
 
-    peaks = measured_peaks(torch, dev) if rank == 0 else {}
     sysm, cfg = make_system(rank)
     box = engine.Box(sysm, cfg, device=dev)
     K, kmax = box.num_kvectors()
@@ -892,6 +891,11 @@ def run_gb300(args, rank, world):
         if dist:
             dist.destroy_process_group()
         return
+    # the pipe peaks for the roofline, timed after every timed line: the
+    # chain kernel of a box set up after these GEMMs ran about 5 % slower
+    # (8.51 against 8.12 ms per 1,000-move launch on one GB300; the cause
+    # was not isolated)
+    peaks = measured_peaks(torch, dev)
     # per chain launch: k_fill_u64 (partial slots), the chain kernel, and
     # the grid rebuild k_cell_scatter + k_cell_sort_fill
     launches = 4 * timing["chain_launches"] + 10 * timing["mp_moves"]
