@@ -126,14 +126,16 @@ __device__ __forceinline__ double erfc_over_r_tab(const FF &ff,
   return p;
 }
 
-__device__ __forceinline__ void pair_term_pipe(const ChainArgs &A,
-                                               const ChainShared &S, int u,
-                                               double2 pxy, double2 pzq,
-                                               int mj, unsigned wrap,
-                                               bool lj12, bool coul_cut,
-                                               const PairTabs &pt,
-                                               double &lj, double &re,
-                                               double &ovl) {
+// One pair's terms, signed for the side (new position +, old -): false
+// outside the cutoff.  pzq: the neighbour's z and the pair's charge
+// product q_i q_j QQ_FACT (formed when the pair was listed).
+__device__ __forceinline__ bool pair_energy_pipe(const ChainArgs &A,
+                                                 const ChainShared &S, int u,
+                                                 double2 pxy, double2 pzq,
+                                                 int mj, unsigned wrap,
+                                                 bool lj12, bool coul_cut,
+                                                 const PairTabs &pt, double &e,
+                                                 double &l, bool &ov) {
   const DevBox &b = A.b;
   const FF &ff = *A.ff;
   const int a = u / (2 * NB27), side = (u / NB27) % 2;
@@ -144,16 +146,12 @@ __device__ __forceinline__ void pair_term_pipe(const ChainArgs &A,
   dz += (wrap & 16u) ? -b.L[2] : (wrap & 32u) ? b.L[2] : 0.0;
   const double d2 = dsq3(dx, dy, dz);
   if (!(ff.rcutSq > d2))
-    return;
-  if (side && d2 < ff.rcutLowSq)
-    ovl = 1.0;
-  double e = 0.0;
-  if (ff.electrostatic && !(coul_cut && ff.rcutCoulSq < d2)) {
-    const double qq = S.hdr[108 + a] * pzq.y;
-    e = ff.ewald ? qq * erfc_over_r_tab(ff, pt.etab, d2) : qq / sqrt(d2);
-  }
+    return false;
+  ov = side && d2 < ff.rcutLowSq;
+  e = 0.0;
+  if (ff.electrostatic && !(coul_cut && ff.rcutCoulSq < d2))
+    e = ff.ewald ? pzq.y * erfc_over_r_tab(ff, pt.etab, d2) : pzq.y / sqrt(d2);
   const int idx = ((const int *)(S.hdr + 116))[a] + meta_kind(mj) * ff.n_kinds;
-  double l;
   if (lj12) {
     double y = (double)__frcp_rn((float)d2);
     double r = fma(-d2, y, 1.0);
@@ -166,12 +164,30 @@ __device__ __forceinline__ void pair_term_pipe(const ChainArgs &A,
   } else {
     l = lj_energy(ff, d2, idx);
   }
-  if (side) {
+  // the old position's terms subtracted: the sign bit flipped (exact)
+  const unsigned long long neg = side ? 0ull : 0x8000000000000000ull;
+  e = __longlong_as_double((long long)((unsigned long long)__double_as_longlong(e) ^ neg));
+  l = __longlong_as_double((long long)((unsigned long long)__double_as_longlong(l) ^ neg));
+  return true;
+}
+
+// pair_energy_pipe added to one set of sums
+__device__ __forceinline__ void pair_term_pipe(const ChainArgs &A,
+                                               const ChainShared &S, int u,
+                                               double2 pxy, double2 pzq,
+                                               int mj, unsigned wrap,
+                                               bool lj12, bool coul_cut,
+                                               const PairTabs &pt,
+                                               double &lj, double &re,
+                                               double &ovl) {
+  double e, l;
+  bool ov;
+  if (pair_energy_pipe(A, S, u, pxy, pzq, mj, wrap, lj12, coul_cut, pt, e, l,
+                       ov)) {
     re += e;
     lj += l;
-  } else {
-    re -= e;
-    lj -= l;
+    if (ov)
+      ovl = 1.0;
   }
 }
 
@@ -656,11 +672,12 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
       // list own atom i's passing positions from slot pos on, below slot
       // lim (past it: evaluated here, not met at liquid densities)
       auto list_hits = [&](int i, unsigned hit, uint4 f, int pos, int lim) {
-        const double2 pxy = oxy[i], pzq = ozq[i];
+        const double2 pxy = oxy[i], oq = ozq[i];
         for (unsigned h = hit; h; h &= h - 1) {
           const int pp = __ffs(h) - 1;
           const int side = pp >= na ? 1 : 0, a = pp - side * na;
           const int u = (a * 2 + side) * NB27;
+          const double2 pzq = make_double2(oq.x, S.hdr[108 + a] * oq.y);
           const unsigned wr = turn_wrap(pturn + 3 * pp, f);
           if (pos < lim) {
             icl_pos[pos][0] = pxy;
@@ -721,6 +738,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
               pxy = make_double2(np[0], np[1]);
               pzq.x = np[2];
             }
+            pzq.y *= S.hdr[108 + a];  // q_i q_j QQ_FACT
             const unsigned wr = turn_wrap(pturn + 3 * pp, f);
             if (pos < lim) {
               icl_pos[pos][0] = pxy;
@@ -761,23 +779,28 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
               r -= c;
             }
           }
-          double l = 0.0, r = 0.0, o = 0.0;
-          pair_term_pipe(A, S, icl_unit[i], icl_pos[i][0], icl_pos[i][1],
-                         icl_meta[i], icl_wrap[i], lj12, coul_cut, ptab, l, r,
-                         o);
+          double e, l;
+          bool o;
+          if (!pair_energy_pipe(A, S, icl_unit[i], icl_pos[i][0],
+                                icl_pos[i][1], icl_meta[i], icl_wrap[i], lj12,
+                                coul_cut, ptab, e, l, o))
+            continue;
           const int c = icl_cls[i];
           if (c == 0) {
             lj += l;
-            re += r;
-            ovl = fmax(ovl, o);
+            re += e;
+            if (o)
+              ovl = 1.0;
           } else if (c == 1) {
             ljR += l;
-            reR += r;
-            ovR = fmax(ovR, o);
+            reR += e;
+            if (o)
+              ovR = 1.0;
           } else {
             ljA += l;
-            reA += r;
-            ovA = fmax(ovA, o);
+            reA += e;
+            if (o)
+              ovA = 1.0;
           }
         }
       };
