@@ -130,7 +130,7 @@ __device__ __forceinline__ double erfc_over_r_tab(const FF &ff,
 // outside the cutoff.  pzq: the neighbour's z and the pair's charge
 // product q_i q_j QQ_FACT (formed when the pair was listed).
 __device__ __forceinline__ bool pair_energy_pipe(const ChainArgs &A,
-                                                 const ChainShared &S, int u,
+                                                 const double *hdr, int u,
                                                  double2 pxy, double2 pzq,
                                                  int mj, unsigned wrap,
                                                  bool lj12, bool coul_cut,
@@ -139,7 +139,7 @@ __device__ __forceinline__ bool pair_energy_pipe(const ChainArgs &A,
   const DevBox &b = A.b;
   const FF &ff = *A.ff;
   const int a = u / (2 * NB27), side = (u / NB27) % 2;
-  const double *pp = S.hdr + (side ? 48 : 24) + 3 * a;
+  const double *pp = hdr + (side ? 48 : 24) + 3 * a;
   double dx = pp[0] - pxy.x, dy = pp[1] - pxy.y, dz = pp[2] - pzq.x;
   dx += (wrap & 1u) ? -b.L[0] : (wrap & 2u) ? b.L[0] : 0.0;
   dy += (wrap & 4u) ? -b.L[1] : (wrap & 8u) ? b.L[1] : 0.0;
@@ -151,7 +151,7 @@ __device__ __forceinline__ bool pair_energy_pipe(const ChainArgs &A,
   e = 0.0;
   if (ff.electrostatic && !(coul_cut && ff.rcutCoulSq < d2))
     e = ff.ewald ? pzq.y * erfc_over_r_tab(ff, pt.etab, d2) : pzq.y / sqrt(d2);
-  const int idx = ((const int *)(S.hdr + 116))[a] + meta_kind(mj) * ff.n_kinds;
+  const int idx = ((const int *)(hdr + 116))[a] + meta_kind(mj) * ff.n_kinds;
   if (lj12) {
     double y = (double)__frcp_rn((float)d2);
     double r = fma(-d2, y, 1.0);
@@ -173,7 +173,7 @@ __device__ __forceinline__ bool pair_energy_pipe(const ChainArgs &A,
 
 // pair_energy_pipe added to one set of sums
 __device__ __forceinline__ void pair_term_pipe(const ChainArgs &A,
-                                               const ChainShared &S, int u,
+                                               const double *hdr, int u,
                                                double2 pxy, double2 pzq,
                                                int mj, unsigned wrap,
                                                bool lj12, bool coul_cut,
@@ -182,7 +182,7 @@ __device__ __forceinline__ void pair_term_pipe(const ChainArgs &A,
                                                double &ovl) {
   double e, l;
   bool ov;
-  if (pair_energy_pipe(A, S, u, pxy, pzq, mj, wrap, lj12, coul_cut, pt, e, l,
+  if (pair_energy_pipe(A, hdr, u, pxy, pzq, mj, wrap, lj12, coul_cut, pt, e, l,
                        ov)) {
     re += e;
     lj += l;
@@ -194,7 +194,6 @@ __device__ __forceinline__ void pair_term_pipe(const ChainArgs &A,
 __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
   extern __shared__ double dyn[];
   __shared__ ChainShared S;
-  __shared__ double hdrp[HDR];            // the previous move's header
   __shared__ double red6[6][CT / 32];     // warp sums, both outcomes
   const DevBox &b = A.b;
   const FF &ff = *A.ff;
@@ -222,7 +221,6 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
   double2 *const tab1 = tab0 + (size_t)(2 * MAX_MOL_ATOMS * 3) * stride;
   double2 *tab = tab0;
   double2 *const exy = tab1 + (size_t)(2 * MAX_MOL_ATOMS * 3) * stride;
-  __shared__ double hdr_next[HDR];  // the next move's header, prefetched
   unsigned short *const pidx =
       (unsigned short *)(exy + NPAIR_CAP * 2 * MAX_MOL_ATOMS);
   // The atoms are owned by the work CTAs with a k-chunk (the context
@@ -593,6 +591,10 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
     int m_prev = -1, na_prev = 0, a0_prev = 0;
     int mol_cur = A.n > 0 ? A.moves[0].mol : -1;
     bool have_next = false;  // this move's context prefetched into smem
+    // three header buffers in turn: this move's (hc), the previous move's
+    // while it is undecided (hq), the next move's, prefetched (hn)
+    __shared__ double hbuf[3][HDR];
+    int hc = 0, hq = 1, hn = 2;
     for (int t = 0; t < A.n; ++t) {
       const int mol_next = nmol;
       nmol = t + 2 < A.n ? A.moves[t + 2].mol : -1;
@@ -645,7 +647,9 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
       __shared__ unsigned char icl_wrap[ICL_CAP];  // turn_wrap of the pair
       __shared__ int seg_cnt[PNSEG];  // entries found per segment
       const int npos = 2 * na;
-      const uint32_t *pturn = (const uint32_t *)(S.hdr + 84);
+      double *const hd = hbuf[hc];        // this move's header
+      const double *const hdrp = hbuf[hq];  // the previous move's
+      const uint32_t *pturn = (const uint32_t *)(hd + 84);
       int n_prev = 0;  // own atoms of the previous molecule (usually 0 or 1)
       if (pend)
         for (int ap = 0; ap < na_prev; ++ap)
@@ -677,7 +681,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
           const int pp = __ffs(h) - 1;
           const int side = pp >= na ? 1 : 0, a = pp - side * na;
           const int u = (a * 2 + side) * NB27;
-          const double2 pzq = make_double2(oq.x, S.hdr[108 + a] * oq.y);
+          const double2 pzq = make_double2(oq.x, hd[108 + a] * oq.y);
           const unsigned wr = turn_wrap(pturn + 3 * pp, f);
           if (pos < lim) {
             icl_pos[pos][0] = pxy;
@@ -687,7 +691,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
             icl_cls[pos] = 0;
             icl_wrap[pos] = (unsigned char)wr;
           } else {
-            pair_term_pipe(A, S, u, pxy, pzq, (int)f.w, wr, lj12, coul_cut, ptab,
+            pair_term_pipe(A, hd, u, pxy, pzq, (int)f.w, wr, lj12, coul_cut, ptab,
                            lj, re, ovl);
           }
           ++pos;
@@ -738,7 +742,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
               pxy = make_double2(np[0], np[1]);
               pzq.x = np[2];
             }
-            pzq.y *= S.hdr[108 + a];  // q_i q_j QQ_FACT
+            pzq.y *= hd[108 + a];  // q_i q_j QQ_FACT
             const unsigned wr = turn_wrap(pturn + 3 * pp, f);
             if (pos < lim) {
               icl_pos[pos][0] = pxy;
@@ -748,10 +752,10 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
               icl_cls[pos] = (unsigned char)(1 + vr);
               icl_wrap[pos] = (unsigned char)wr;
             } else if (vr) {
-              pair_term_pipe(A, S, u, pxy, pzq, (int)f.w, wr, lj12, coul_cut,
+              pair_term_pipe(A, hd, u, pxy, pzq, (int)f.w, wr, lj12, coul_cut,
                              ptab, ljA, reA, ovA);
             } else {
-              pair_term_pipe(A, S, u, pxy, pzq, (int)f.w, wr, lj12, coul_cut,
+              pair_term_pipe(A, hd, u, pxy, pzq, (int)f.w, wr, lj12, coul_cut,
                              ptab, ljR, reR, ovR);
             }
           }
@@ -781,7 +785,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
           }
           double e, l;
           bool o;
-          if (!pair_energy_pipe(A, S, icl_unit[i], icl_pos[i][0],
+          if (!pair_energy_pipe(A, hd, icl_unit[i], icl_pos[i][0],
                                 icl_pos[i][1], icl_meta[i], icl_wrap[i], lj12,
                                 coul_cut, ptab, e, l, o))
             continue;
@@ -895,7 +899,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
           const double *ctx_n = A.ctx + (size_t)((t + 1) % A.nctx) * A.ctx_len;
           double2 *tabn = tab == tab0 ? tab1 : tab0;
           for (int i = lane; i < HDR; i += 32)
-            hdr_next[i] = __ldcg(ctx_n + i);
+            hbuf[hn][i] = __ldcg(ctx_n + i);
           for (int i = lane; i < A.nrows_max * stride; i += 32)
             tabn[i] = __ldcg((const double2 *)(ctx_n + HDR) + i);
         }
@@ -909,7 +913,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
         // does not depend on this move's header).
         if (warp == 0) {
           for (int i = lane; i < HDR; i += 32)
-            S.hdr[i] = __ldcg(ctx_t + i);
+            hd[i] = __ldcg(ctx_t + i);
           __syncwarp();
           mark(0);
           int icl_n = 0;
@@ -965,17 +969,16 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
         // soon as they are summed.  Warp 7 of a context writer with
         // k-vectors builds its part of the next context.
         if (have_next) {
-          // prefetched by the polling warp during the previous phase A
-          for (int i = threadIdx.x; i < HDR; i += CT)
-            S.hdr[i] = hdr_next[i];
+          // header and rows prefetched by the polling warp during the
+          // previous phase A (behind that phase's closing barriers)
           tab = tab == tab0 ? tab1 : tab0;
         } else {
           for (int i = threadIdx.x; i < HDR; i += CT)
-            S.hdr[i] = __ldcg(ctx_t + i);
+            hd[i] = __ldcg(ctx_t + i);
           for (int i = threadIdx.x; i < A.nrows_max * stride; i += CT)
             tab[i] = __ldcg((const double2 *)(ctx_t + HDR) + i);
+          __syncthreads();
         }
-        __syncthreads();
         mark(0);
         if (wload)
           ctx_pre2(A, S, t + 1, pre);
@@ -1036,7 +1039,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
           const int kw = warp < 3 ? warp : warp - 1;  // 0..5
           // the x-y column products first (named barrier 4: the six warps)
           xy_products(kw * 32 + lane, 6 * 32, npair, pair_n, tab, stride, na,
-                      S.hdr + 72, exy);
+                      hd + 72, exy);
           asm volatile("bar.sync 4, 192;" ::: "memory");
           const double *sR = KR(bS), *sI = KI(bS);
           const double *pR = pend ? KR(bP) : nullptr;
@@ -1046,7 +1049,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
             double dR, dI;
             kvec_delta(kn[i],
                        npair > 0 ? exy + (size_t)pidx[i] * 2 * na : nullptr,
-                       tab, stride, na, S.hdr + 72, dR, dI);
+                       tab, stride, na, hd + 72, dR, dI);
             double srn = sR[i] + dR, sin_ = sI[i] + dI;
             rR[i] = srn;
             rI[i] = sin_;
@@ -1179,8 +1182,6 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
       }
       mark(3);
       if (nspec) {
-        for (int i = threadIdx.x; i < HDR; i += CT)
-          hdrp[i] = S.hdr[i];
         m_prev = m;
         na_prev = na;
         a0_prev = a0m;
@@ -1193,12 +1194,12 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
         const int acc = dec_outcome(word, t);
         __syncthreads();
         if (threadIdx.x == 0) {
-          settings_update(S.set, (int)S.hdr[1], acc);
+          settings_update(S.set, (int)hd[1], acc);
           S.last_m = m;
           S.last_acc = acc;
         }
         if (acc) {
-          commit_atoms(S.hdr, na, a0m);
+          commit_atoms(hd, na, a0m);
           bS = bP;
         }
         bP = -1;
@@ -1207,7 +1208,7 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
         if (t + 1 < A.n) {
           if (!adjust_before(t + 1, bnd))
             return;
-          build_ctx(A, S, t + 1, S.hdr, acc, 0, CT);
+          build_ctx(A, S, t + 1, hd, acc, 0, CT);
           if (!grid_sync(A.bar, G, S.gen, b.err, &S.flag, A.spin))
             return;
         }
@@ -1215,6 +1216,12 @@ __global__ void __launch_bounds__(CT, 1) k_chain_fp64_pipe(ChainArgs A) {
       }
       mark(4);
       mol_cur = mol_next;
+      // the headers' roles: this move's becomes the previous one's, the
+      // prefetched one (or a free buffer) this move's
+      const int hfree = hq;
+      hq = hc;
+      hc = hn;
+      hn = hfree;
     }
   }
   if (prof) {
