@@ -11,7 +11,9 @@ prefix, which the reference skips with an "Unknown input" warning:
 
 * ``GB300Precision``  ``fp64`` (plain form, default) or ``mixed``
 * ``GB300RecomputeFreq``  full FP64 recompute interval of the mixed form
-* ``GB300Autotune``  ``true`` to let the autotuner pick launch shapes
+* ``GB300Autotune``  ``true``: ``Box.mc_init`` times the chain's launch
+  shapes on the box's own state (``gb_mc_autotune``, latency objective)
+  and keeps the fastest, unless the call names a shape
 """
 from __future__ import annotations
 

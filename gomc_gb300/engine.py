@@ -411,6 +411,12 @@ class Box:
                       cluster_size, flush_every, move_buffer, unit_lanes,
                       grid_ctas, writer_kchunk, moves_in_flight)
         self._chk(lib().gb_mc_init(self.h, C.byref(p)))
+        # in.conf GB300Autotune: the chain's launch shape timed on this machine
+        # (latency objective), unless the call named one
+        shape_given = (cluster_size or unit_lanes or grid_ctas or writer_kchunk
+                       or moves_in_flight)
+        if getattr(self.cfg, "autotune", False) and not shape_given:
+            self.mc_autotune("latency")
 
     def checkpoint(self) -> bytes:
         """The box's dynamic state (and its Monte Carlo state after

@@ -187,3 +187,19 @@ def test_fp64_autotune_keeps_state_and_matches_fixed_shape(gb):
                                   z["trace"][300:, 3].astype(int))
     tuned.close()
     fixed.close()
+
+
+def test_inconf_autotune_keeps_reference_decisions(gb):
+    """GB300Autotune true: mc_init times the launch shapes on the box and
+    keeps one; the chain still takes the reference's decisions."""
+    z, meta = load("w1728")
+    cfg = config_of(meta)
+    cfg.autotune = True
+    box = gb.Box(system_of(z, meta), cfg)
+    box.mc_init(meta["config"]["random_seed"], move_fractions(meta),
+                meta["config"]["adj_steps"])
+    shape = box.mc_shape()
+    assert shape["moves_in_flight"] in (1, 2) and shape["ctas"] >= 2
+    r = box.mc_run(0, z["trace"].shape[0], trace=True)
+    check_trace(r, z, REL)
+    box.close()
