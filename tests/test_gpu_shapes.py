@@ -203,3 +203,66 @@ def test_inconf_autotune_keeps_reference_decisions(gb):
     r = box.mc_run(0, z["trace"].shape[0], trace=True)
     check_trace(r, z, REL)
     box.close()
+
+
+def _eight_site_box(n_mol, box_len, seed):
+    """Rigid 8-site molecules (a 1 A cube of alternating +-0.25 e sites, LJ
+    on every site) on a lattice with random orientations: the largest
+    molecule the move loop takes (48 phase rows of a move context)."""
+    import math
+    from gomc_gb300.systems import AtomKind, MolSystem, MoleculeType
+    rng = np.random.default_rng(seed)
+    n = int(math.ceil(n_mol ** (1.0 / 3.0) - 1e-9))
+    sp = box_len / n
+    idx = np.arange(n_mol)
+    c = np.stack([(idx // (n * n) + 0.5) * sp, ((idx // n) % n + 0.5) * sp,
+                  (idx % n + 0.5) * sp], axis=1)
+    local = 0.5 * np.array([[x, y, z] for x in (-1, 1) for y in (-1, 1)
+                            for z in (-1, 1)], dtype=np.float64)
+    q = rng.normal(size=(n_mol, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    w, x, y, z = q.T
+    rot = np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w),
+                    2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w),
+                    2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)],
+                   axis=1).reshape(n_mol, 3, 3)
+    pos = (c[:, None, :] + np.einsum("mij,aj->mai", rot, local)).reshape(-1, 3)
+    pos = np.round(np.mod(pos, box_len), 3)
+    pos[pos >= box_len] -= box_len
+    charges = [0.25, -0.25, -0.25, 0.25, -0.25, 0.25, 0.25, -0.25]
+    mt = MoleculeType(name="CUB", atom_names=["C%d" % i for i in range(8)],
+                      atom_kinds=[0] * 8, charges=charges)
+    return MolSystem(box=np.array([box_len] * 3), kinds=[AtomKind("CS", 40.0, 2.5)],
+                     mol_types=[mt], pos=pos,
+                     atom_kind=np.zeros(8 * n_mol, np.int32),
+                     atom_charge=np.tile(np.array(charges), n_mol),
+                     atom_mol=np.repeat(np.arange(n_mol, dtype=np.int32), 8),
+                     mol_start=np.arange(0, 8 * n_mol + 1, 8, dtype=np.int32),
+                     mol_type=np.zeros(n_mol, np.int32))
+
+
+@pytest.mark.parametrize("flight", [1, 2])
+def test_eight_site_molecules_match_oracle(gb, flight):
+    """Both FP64 chains on molecules of eight sites (context writers for
+    48 phase rows) take the oracle's decisions, every move's energy change
+    within 1e-10 of the oracle's."""
+    from gomc_gb300.config import SimConfig
+    from oracle import oracle as O
+    sysm = _eight_site_box(343, 36.0, seed=11)
+    cfg = SimConfig(temperature=300.0, rcut=9.0, tolerance=1e-5)
+    seed, frac, adj, n = 77, [0.5, 0.5, 0.0], 100, 300
+    box = gb.Box(sysm, cfg)
+    box.mc_init(seed, frac, adj, moves_in_flight=flight)
+    assert box.mc_shape()["moves_in_flight"] == flight
+    r = box.mc_run(0, n, trace=True)
+    O.set_threads(4)
+    ob = O.OracleBox(sysm, cfg)
+    ob.mc_init(seed, frac, adj)
+    r2 = ob.mc_run(0, n)
+    np.testing.assert_array_equal(r["mol"], r2["mol"])
+    np.testing.assert_array_equal(r["accepted"], r2["accepted"])
+    e = np.abs(np.asarray(box.energy())[:3])
+    for j in range(3):
+        bound = REL * np.maximum(max(e[j], 1.0), np.abs(r2["de"][:, j]))
+        assert (np.abs(r["de"][:, j] - r2["de"][:, j]) <= bound).all(), j
+    box.close()
