@@ -266,3 +266,31 @@ def test_eight_site_molecules_match_oracle(gb, flight):
         bound = REL * np.maximum(max(e[j], 1.0), np.abs(r2["de"][:, j]))
         assert (np.abs(r["de"][:, j] - r2["de"][:, j]) <= bound).all(), j
     box.close()
+
+
+@pytest.mark.parametrize("flight", [1, 2])
+def test_eight_site_long_lists_match_oracle(gb, flight):
+    """A grid of 50 CTAs (no context writer without k-vectors) and a 12 A
+    cutoff: about 140 listed pairs per CTA, more than a warp's segment
+    holds in the chain with two moves in flight (the pairs past it are
+    evaluated where they are found); still the oracle's decisions."""
+    from gomc_gb300.config import SimConfig
+    from oracle import oracle as O
+    sysm = _eight_site_box(343, 36.0, seed=12)
+    cfg = SimConfig(temperature=300.0, rcut=12.0, tolerance=1e-5)
+    seed, frac, adj, n = 78, [0.5, 0.5, 0.0], 100, 200
+    box = gb.Box(sysm, cfg)
+    box.mc_init(seed, frac, adj, grid_ctas=50, moves_in_flight=flight)
+    assert box.mc_shape()["ctas"] == 50
+    r = box.mc_run(0, n, trace=True)
+    O.set_threads(4)
+    ob = O.OracleBox(sysm, cfg)
+    ob.mc_init(seed, frac, adj)
+    r2 = ob.mc_run(0, n)
+    np.testing.assert_array_equal(r["mol"], r2["mol"])
+    np.testing.assert_array_equal(r["accepted"], r2["accepted"])
+    e = np.abs(np.asarray(box.energy())[:3])
+    for j in range(3):
+        bound = REL * np.maximum(max(e[j], 1.0), np.abs(r2["de"][:, j]))
+        assert (np.abs(r["de"][:, j] - r2["de"][:, j]) <= bound).all(), j
+    box.close()
